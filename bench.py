@@ -1,0 +1,375 @@
+#!/usr/bin/env python3
+"""Benchmark: particle-seconds tracked per second on the field-storage workload.
+
+Workload (the configuration the headline metric is quoted on): 1e6 UCN per
+GPU in a closed cylinder R = 0.2 m, H = 0.1 m (256 segments, 1,024 triangles),
+64^3 tricubic table of the quadrupole |B| = 1.5 T r/0.2 m + 10 uT along z,
++-mu grad|B| force with 50/50 spin states, 250 neV walls with 5 % Lambert and
+1e-4 loss per bounce, tau = 880 s, 0-250 neV isotropic, FP64 state.  A step
+advances every live particle through one lab-time window (default 0.02 s);
+particles pause at RK step boundaries, so windows compose bit-identically to
+one uninterrupted run.  Synthetic, seeded inputs (no dataset).
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-s tracked/s at stated energy drift: batched vs plain GPU form, 1 GB300"
+UNIT = "particle-s/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=1_000_000, help="particles per GPU")
+    p.add_argument("--window", type=float, default=0.02, help="lab-time window per step [s]")
+    p.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    p.add_argument("--mode", default="plain", choices=["plain", "batched"])
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--e2e-steps", type=int, default=2)
+    return p.parse_args()
+
+
+# ----------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if self.proc is None:
+            return out
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return out
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for k, nme in enumerate(names):
+                if r[5 + k].lower() == "active":
+                    reasons.add(nme)
+        out["sm_mhz"] = statistics.median(sm) if sm else None
+        out["sm_max_mhz"] = max(mx) if mx else None
+        out["reasons"] = sorted(reasons)
+        out["samples"] = len(rows)
+        return out
+
+
+# ----------------------------------------------------------------------------
+def algorithmic_work(st, precision):
+    """FP64/FP32 flops of one call from the device event counters, per unit of
+    work: RK try 650 + 6 RHS; RHS = 60 (equation of motion) + 1,248 (tricubic
+    B and grad B, 3 x (64 + 3 x 48) FMA); B-only table value 384; dense-output
+    state 150; BVH node test 24; segment-triangle test 60."""
+    tries = st["rk_accepted"] + st["rk_rejected"]
+    rhs = st["rhs_evals"]
+    bonly = max(0, st["field_evals"] - rhs)
+    field_flops = rhs * 1248 + bonly * 384
+    other64 = tries * 650 + rhs * 60 + st["dense_evals"] * 150 + st["bvh_nodes"] * 24 + st["tri_tests"] * 60
+    if precision == "fp32":
+        return other64, field_flops
+    return other64 + field_flops, 0
+
+
+def setup_ours(args, rank):
+    from pentrack_gb300 import Engine, _abi as A, workloads
+    device = int(os.environ.get("LOCAL_RANK", 0))
+    scene = workloads.field_storage_scene()
+    engine = Engine(scene, device=device)
+    _, params, parts = workloads.field_storage(n=args.n, engine=engine, first_id=rank * args.n)
+    params.field_precision = A.PREC_FP32 if args.precision == "fp32" else A.PREC_FP64
+    params.mode = A.MODE_BATCHED if args.mode == "batched" else A.MODE_PLAIN
+    return engine, params, parts, device
+
+
+def cpu_baseline(args, n_hint=2048):
+    """The oracle (FP64 CPU restatement of the reference path) on all host cores,
+    on the first ids of the same workload over the same lab-time span."""
+    from oracle import pyoracle
+    from pentrack_gb300 import Engine, workloads
+    T = (args.warmup + args.steps) * args.window
+    cores = os.cpu_count()
+    scene = workloads.field_storage_scene()
+    orc = pyoracle.Oracle(scene)
+    eng = None
+    try:
+        eng = Engine(scene)
+    except Exception:
+        pass
+    m = n_hint
+    total_ps, total_s = 0.0, 0.0
+    while True:
+        _, params, parts = workloads.field_storage(n=m, simtime=T, engine=eng)
+        t0 = time.perf_counter()
+        out, st = orc.integrate(params, parts, nthreads=cores)
+        dt = time.perf_counter() - t0
+        total_ps, total_s = st["particle_seconds"], dt
+        if dt >= 0.5 * args.cpu_seconds or m >= 1 << 20:
+            break
+        m = int(min(1 << 20, m * max(2.0, args.cpu_seconds / max(dt, 1e-3))))
+    return {"value": total_ps / total_s, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"oracle on {cores} threads: first {m} UCN of the workload tracked over 0-{T:g} s "
+                      f"({total_ps:.4g} particle-s in {total_s:.2f} s)"}
+
+
+def energy_drift(engine, parts, out):
+    """(H_end - H_start)/(t_end - t_start) per particle [eV/s] for particles
+    still stored: H = Ekin + m g z - pol mu |B| (+ Fermi potential, 0 inside)."""
+    from pentrack_gb300 import scenes
+    live = out.stop_id == 0
+    if live.sum() == 0:
+        return None
+    idx = np.nonzero(live)[0][:20000]
+    m = scenes.M_N
+    c2 = scenes.C0 ** 2
+
+    def H(t, y):
+        v2 = (y[3:6] ** 2).sum(0)
+        q = np.column_stack([y[0], y[1], y[2], t])
+        B = engine.field(q)[0]
+        return 0.5 * m * v2 * (1 + 0.75 * v2 / c2) + m * scenes.GRAV * y[2] - y[7] * (scenes.MU_N / scenes.ELE_E) * np.sqrt((B ** 2).sum(1))
+
+    h0 = H(parts.t[idx], parts.y[:, idx])
+    h1 = H(out.t[idx], out.y[:, idx])
+    rate = np.abs(h1 - h0) / np.maximum(out.t[idx] - parts.t[idx], 1e-30)
+    return {"median_eV_per_s": float(np.median(rate)), "p99_eV_per_s": float(np.percentile(rate, 99)),
+            "particles": int(len(idx))}
+
+
+def e2e_run(args, engine, params, rank):
+    """The reference-facing call: pt_integrate with host (pinned) buffers, a
+    fresh chunk of the workload per step tracked through one window."""
+    from pentrack_gb300 import workloads
+    import torch
+    n = args.n
+    T = args.window
+
+    def pinned_set(seed_first):
+        _, p, parts = workloads.field_storage(n=n, simtime=T, engine=engine, first_id=seed_first)
+        for k in ("id", "t", "y", "spin"):
+            a = getattr(parts, k)
+            tt = torch.empty(a.shape, dtype=torch.from_numpy(a).dtype, pin_memory=True)
+            tt.numpy()[...] = a
+            setattr(parts, k, tt.numpy())
+        return p, parts
+
+    h2d = d2h = 0
+    total_ps, total_s = 0.0, 0.0
+    for k in range(1 + args.e2e_steps):
+        p, parts = pinned_set(10_000_000 * (k + 1) + rank * n)
+        p.field_precision, p.mode = params.field_precision, params.mode
+        t0 = time.perf_counter()
+        out, st = engine.integrate(p, parts)
+        dt = time.perf_counter() - t0
+        if k == 0:
+            continue
+        total_ps += st["particle_seconds"]
+        total_s += dt
+        h2d = n * (8 + 8 + 72 + 40)
+        d2h = n * (8 + 8 + 72 + 40 + 4 * 4 + 8 * 6)
+    return {"value": total_ps / total_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "steps": args.e2e_steps, "call": "pt_integrate (host buffers, full H2D/D2H per step)"}
+
+
+def load_traffic():
+    path = os.path.join(ROOT, "profiles", "k_plain_field_storage_traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f)
+    return None
+
+
+def run_ours(args, rank, world):
+    import torch
+    engine, params, parts, device = setup_ours(args, rank)
+    from pentrack_gb300 import lib
+    import ctypes
+    peak = ctypes.c_double(0)
+    lib().pt_probe_fp64(engine.h, ctypes.byref(peak))
+    batch = engine.batch(params, parts)
+    t_now = 0.0
+    for _ in range(args.warmup):
+        t_now += args.window
+        batch.advance(t_now)
+    dist = world > 1
+    if dist:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(device)
+    clocks = Clocks(device)
+    clocks.start()
+    agg = None
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        t_now += args.window
+        st = batch.advance(t_now)
+        if agg is None:
+            agg = dict(st)
+        else:
+            for k, v in st.items():
+                if isinstance(v, (int, float)) and k != "active":
+                    agg[k] += v
+            agg["active"] = st["active"]
+    torch.cuda.synchronize(device)
+    elapsed = time.perf_counter() - t0
+    clk = clocks.stop()
+    psec = agg["particle_seconds"]
+    device_ms = agg["span_ms"]
+    if dist:
+        t = torch.tensor([device_ms / 1e3, psec], dtype=torch.float64, device=f"cuda:{device}")
+        tmax = t[0:1].clone()
+        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+        tot = t[1:2].clone()
+        torch.distributed.all_reduce(tot, op=torch.distributed.ReduceOp.SUM)
+        device_s, psec_all = float(tmax[0]), float(tot[0])
+        torch.distributed.barrier()
+    else:
+        device_s, psec_all = device_ms / 1e3, psec
+    out_state = batch.read()
+    if rank != 0:
+        return None
+    f64, f32 = algorithmic_work(agg, args.precision)
+    launches = max(1, agg["dominant_launches"])
+    avg_launch_s = agg["dominant_kernel_ms"] / 1e3 / launches
+    achieved = f64 / launches / avg_launch_s / 1e12
+    traffic = load_traffic()
+    line = {
+        "metric": METRIC,
+        "value": psec_all / device_s,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": device_s * 1e3 / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f64 state, f32 field",
+        "data": "synthetic (seeded Philox sources; analytic quadrupole table)",
+        "config": {"workload": f"field storage: {args.n} UCN/GPU, cylinder R=0.2 m H=0.1 m (1024 triangles), "
+                               f"64^3 tricubic quadrupole, 250 neV walls 5% Lambert 1e-4 loss, tau 880 s",
+                   "window_s": args.window, "form": args.mode, "field_precision": args.precision,
+                   "l2": "per-step particle state > L2 (350 B x 1e6); field table L2-resident by design",
+                   "parallelism": f"replicas x{world}"},
+        "gpu_launches": int(agg["launches"]),
+        "wall_s": elapsed,
+        "clocks": clk,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+                     "frac": achieved / peak.value if peak.value else None,
+                     "peak_source": "measured: pt_probe_fp64 DFMA kernel on this GPU",
+                     "traffic": traffic.get("bytes_per_launch") if traffic else None,
+                     "kernel": agg["dominant_kernel"], "launches": int(launches),
+                     "avg_launch_ms": avg_launch_s * 1e3,
+                     "fp64_flops_per_launch": f64 / launches, "fp32_flops_per_launch": f32 / launches},
+        "events": {k: agg[k] for k in ("rk_accepted", "rk_rejected", "rhs_evals", "field_evals", "hits",
+                                        "bisection_levels", "bvh_nodes", "tri_tests", "subsegments", "dense_evals")},
+        "live_particles": int(agg["active"]),
+    }
+    line["energy_drift"] = energy_drift(engine, parts, out_state)
+    if not args.no_e2e:
+        try:
+            line["e2e"] = e2e_run(args, engine, params, rank)
+        except Exception as ex:  # report, never hide
+            line["e2e"] = {"error": str(ex)}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args)
+    return line
+
+
+def run_reference(args, rank, world):
+    """The reference path's CPU implementation (the oracle port: the reference
+    itself cannot be built without Boost/CGAL) on all host cores."""
+    if rank != 0:
+        return None
+    from oracle import pyoracle
+    from pentrack_gb300 import workloads
+    cores = os.cpu_count()
+    scene = workloads.field_storage_scene()
+    orc = pyoracle.Oracle(scene)
+    m = 4096
+    T = (args.warmup + args.steps) * args.window
+    total_ps = total_s = 0.0
+    for k in range(args.warmup + args.steps):
+        _, params, parts = workloads.field_storage(n=m, simtime=T, first_id=k * m)
+        t0 = time.perf_counter()
+        out, st = orc.integrate(params, parts, nthreads=cores)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            total_ps += st["particle_seconds"]
+            total_s += dt
+    value = total_ps / total_s
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded Philox sources; analytic quadrupole table)", "impl": "reference",
+            "config": {"workload": "field storage (same scene); per step 4096 UCN tracked over "
+                                   f"0-{T:g} s", "parallelism": f"{cores} host threads"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} x 4096 UCN over 0-{T:g} s on {cores} threads"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if world > 1:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        torch.distributed.init_process_group("nccl")
+    from pentrack_gb300 import build
+    if args.impl == "ours":
+        build.build_engine()
+    build.build_oracle()
+    line = run_reference(args, rank, world) if args.impl == "reference" else run_ours(args, rank, world)
+    if rank == 0 and line is not None:
+        print(json.dumps(line))
+    if world > 1:
+        import torch
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

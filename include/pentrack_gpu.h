@@ -1,0 +1,259 @@
+/*
+ * pentrack_gpu.h -- C ABI of the GB300 particle-tracking engine.
+ *
+ * Drop-in for PENTrack's per-particle hot path
+ *   TTracker::IntegrateParticle            (include/tracking.h:46-47, src/tracking.cpp:17-173)
+ * together with the collaborators it calls on every step
+ *   TFieldManager::BField / EField          (include/fields.h:46,61; src/fields.cpp:139-182)
+ *   TGeometry::CheckSegment / GetCollisions (include/geometry.h:104-155; src/geometry.cpp:139-175)
+ *   TNeutron::OnHit / OnStep, TProton/TElectron::OnStep (src/neutron.cpp:187-282,
+ *                                            src/proton.cpp:25-33, src/electron.cpp:25-32)
+ *
+ * The reference keeps its scene in private members (TGeometry::solids,
+ * TTriangleMesh::meshes, TFieldManager::fields), so the engine is built from
+ * the same raw inputs those classes read from config.in: triangles of the STL
+ * files, the [MATERIALS]/[GEOMETRY] tables and the [FIELDS] lines.  The C++
+ * host layer (pentrack_gb300/csrc/pt_host.hpp) fills these structs from a
+ * config.in exactly like TGeometry(TConfig&) and TFieldManager(TConfig&).
+ *
+ * Conventions: only C types cross the boundary; the caller owns every array
+ * it passes and no pointer to caller memory is kept after a call returns;
+ * a context owns all device memory; calls on one context come from one host
+ * thread.  Errors never throw across the ABI: every entry returns pt_status.
+ * Per-particle outcomes use the reference's stopID integers.
+ */
+#ifndef PENTRACK_GPU_H
+#define PENTRACK_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference throws std::runtime_error instead) ---- */
+typedef int32_t pt_status;
+enum {
+    PT_OK = 0,
+    PT_ERR_INVALID = -1,      /* invalid scene / parameters (reference: runtime_error at setup) */
+    PT_ERR_UNSUPPORTED = -2,  /* field type or option the device path does not implement */
+    PT_ERR_OOM = -3,
+    PT_ERR_CUDA = -4,
+    PT_ERR_TIMEOUT = -5,
+    PT_ERR_CANCELLED = -6,    /* pt_cancel() was called: partial results are valid */
+    PT_ERR_IO = -7,
+    PT_ERR_NO_DEVICE = -8
+};
+
+/* ---- per-particle stop IDs: identical integers to include/globals.h:13-23 ---- */
+enum {
+    PT_ID_UNKNOWN = 0,
+    PT_ID_NOT_FINISH = -1,
+    PT_ID_HIT_BOUNDARIES = -2,
+    PT_ID_ODEINT_ERROR = -3,
+    PT_ID_DECAYED = -4,
+    PT_ID_INITIAL_NOT_FOUND = -5,
+    PT_ID_CGAL_ERROR = -6,
+    PT_ID_GEOMETRY_ERROR = -7,
+    PT_ID_ABSORBED_IN_MATERIAL = 1,
+    PT_ID_ABSORBED_ON_SURFACE = 2
+};
+
+/* particle species (src/neutron.cpp:15, src/proton.cpp, src/electron.cpp) */
+enum { PT_NEUTRON = 0, PT_PROTON = 1, PT_ELECTRON = 2 };
+
+/* field kinds the device path implements (src/fields.cpp:31-130) */
+enum {
+    PT_FIELD_TAB3D = 1,     /* OPERA3D / 3Dtable / COMSOL: TabField3, tricubic  (src/field_3d.cpp:417-529) */
+    PT_FIELD_HARMONIC = 2,  /* HarmonicExpansionBField, l <= 5        (src/harmonicfields.cpp:50-829) */
+    PT_FIELD_UNIFORM_E = 3  /* EDMStaticEField                        (src/edmfields.cpp:181-187) */
+};
+
+/* scheduling form of the tracking kernels */
+enum {
+    PT_MODE_PLAIN = 0,   /* fixed step-batch launches: one lane per particle, K accepted steps per launch */
+    PT_MODE_BATCHED = 1  /* phase-split: converged RK-try launches + hit-resolution launches over work queues */
+};
+
+/* arithmetic of the field evaluation (the state update, step control and
+ * narrow-phase intersection are always FP64) */
+enum { PT_PREC_FP64 = 0, PT_PREC_FP32 = 1 };
+
+/* material: the nine columns of materials.in, in order (src/geometry.cpp:10-52).
+ * Units as in the file: neV, neV, probability, probability, m, m, T, probability, probability. */
+typedef struct pt_material {
+    double fermi_real;
+    double fermi_imag;
+    double diff_prob;
+    double spinflip_prob;
+    double rms_roughness;     /* MicroRoughness: must be 0 on the device path */
+    double correl_length;     /* MicroRoughness: must be 0 on the device path */
+    double internal_bfield;
+    double modified_lambert_prob;
+    double loss_per_bounce;
+} pt_material;
+
+/* solid: one [GEOMETRY] line (include/geometry.h:40-68).  solids[0] must be the
+ * default solid (ID 1), which owns no triangles. */
+typedef struct pt_solid {
+    uint32_t id;               /* priority: higher ID wins */
+    int32_t material;          /* index into pt_scene_desc.materials */
+    int32_t n_ignore;          /* number of [start,end) ignore intervals */
+    int32_t reserved;
+    const double *ignore_times; /* 2*n_ignore values: start0, end0, start1, end1, ... */
+} pt_solid;
+
+/* one [FIELDS] entry wrapped in its TFieldContainer (include/field.h:268-281):
+ * constant B/E scale factors, box [min,max) and smooth boundary width. */
+typedef struct pt_field {
+    int32_t type;
+    int32_t reserved0;
+    double b_scale;             /* TFieldScaler restricted to a constant; 0 switches B off */
+    double e_scale;             /* likewise for E/V */
+    double xmax, xmin, ymax, ymin, zmax, zmin; /* box; xmax<=xmin etc. means "no box" */
+    double boundary_width;
+    /* PT_FIELD_TAB3D: rectilinear grid of raw samples in SI units (m, T, V) */
+    int32_t nx, ny, nz, reserved1;
+    const double *x, *y, *z;   /* sorted, unique axis coordinates */
+    const double *bx, *by, *bz, *v; /* [ix][iy][iz] row-major (iz fastest); NULL = component absent */
+    /* PT_FIELD_HARMONIC */
+    double offset[3];
+    int32_t n_coeff, reserved2;
+    const int32_t *l, *m;
+    const double *g;
+    /* PT_FIELD_UNIFORM_E: E [V/m]; potential V = e[2]*z as in src/edmfields.cpp:186 */
+    double e[3];
+} pt_field;
+
+typedef struct pt_scene_desc {
+    int64_t n_triangles;
+    const double *triangles;      /* 9 doubles per triangle: v0, v1, v2 [m] in STL winding (normal = (v1-v0)x(v2-v0)) */
+    const int32_t *triangle_solid;/* index into solids[] for every triangle */
+    int32_t n_solids;
+    int32_t n_materials;
+    const pt_solid *solids;
+    const pt_material *materials;
+    int32_t n_fields;
+    int32_t reserved;
+    const pt_field *fields;
+} pt_scene_desc;
+
+/* run parameters: the [GLOBAL] simtime plus the particle's [PARTICLES]/species
+ * options read by TTracker::IntegrateParticle (src/tracking.cpp:19-60). */
+typedef struct pt_run_params {
+    int32_t species;
+    int32_t mode;              /* PT_MODE_* */
+    int32_t field_precision;   /* PT_PREC_* */
+    int32_t flipspin;          /* particle option flipspin */
+    double simtime;            /* lab-time limit: reaching it gives ID_NOT_FINISH */
+    double tau;                /* mean lifetime [s]; >0: proper-time limit ~ Exp(1/tau) */
+    double tmax;               /* proper-time limit used when tau == 0 (reaching it gives ID_DECAYED) */
+    double lmax;               /* trajectory-length limit */
+    double bmax;               /* spin option Bmax [T] */
+    int32_t n_spintimes;       /* number of doubles in spintimes (pairs of [start,end)) */
+    int32_t steps_per_launch;  /* plain form: accepted RK steps per lane per launch (0 = default) */
+    const double *spintimes;
+    uint64_t seed;             /* Philox4x32-10 key; stream counter keyed by particle id */
+    int32_t block_size;        /* 0 = autotuned */
+    int32_t max_launches;      /* 0 = unlimited */
+    double timeout_s;          /* host wait limit per call (0 = none) */
+} pt_run_params;
+
+/* structure-of-arrays particle batch (host memory).  y and spin are
+ * component-major: y[c*n + i] is component c of particle i.
+ * y = (x, y, z, vx, vy, vz, proper time, polarisation, path length)  include/particle.h:21
+ * spin = (Sx, Sy, Sz, integrated time, integrated phase)               include/particle.h:22 */
+typedef struct pt_particles {
+    int64_t n;
+    int64_t *id;       /* particle number: keys the random stream */
+    double *t;
+    double *y;         /* 9*n */
+    double *spin;      /* 5*n */
+    /* written by the engine (may be NULL on input): */
+    int32_t *stop_id;
+    int32_t *solid;    /* ID of the highest-priority solid the particle is in */
+    int32_t *n_hit;
+    int32_t *n_step;   /* sub-segments, as TParticle::Nstep (src/particle.cpp:205) */
+    int32_t *n_spinflip;
+    int32_t *reserved;
+    double *h_max;     /* max total energy [eV] (src/particle.cpp:202) */
+    double *noflip_prob;
+    double *tau;       /* sampled proper-time limit */
+    double *h_start;   /* initial total energy [eV] */
+    int64_t *n_accepted; /* accepted RK steps */
+    int64_t *n_rejected; /* rejected RK tries */
+} pt_particles;
+
+/* event counters and timings of one call */
+typedef struct pt_stats {
+    double kernel_ms;          /* device time of this call's tracking launches (CUDA events on the launch stream) */
+    double span_ms;            /* device time from the call's first to its last event on the launch stream */
+    double wall_ms;            /* host wall time of the call */
+    double particle_seconds;   /* sum over particles of the lab time tracked in this call */
+    int64_t launches;
+    int64_t active;            /* particles not yet stopped after the call */
+    int64_t rk_accepted, rk_rejected, rhs_evals, field_evals, hits, bisection_levels;
+    int64_t bvh_nodes, tri_tests, subsegments, dense_evals;
+    double dominant_kernel_ms; /* summed device time of the dominant kernel */
+    int64_t dominant_launches;
+    char dominant_kernel[48];
+} pt_stats;
+
+typedef struct pt_ctx pt_ctx;
+typedef struct pt_batch pt_batch;
+
+/* Build the device scene (BVH, Hermite field tables, materials) on CUDA device
+ * `device`.  Replaces TGeometry(TConfig&) (src/geometry.cpp:93-137) and
+ * TFieldManager(TConfig&) (src/fields.cpp:19-136) as far as the hot path needs. */
+pt_status pt_create(const pt_scene_desc *scene, int32_t device, pt_ctx **out);
+void pt_destroy(pt_ctx *ctx);
+/* Text of the last error on this context (or of the last failed pt_create when ctx is NULL). */
+const char *pt_last_error(const pt_ctx *ctx);
+/* Ask running kernels to stop at the next step boundary (the reference's quit
+ * flag, include/globals.h:33, polled at src/tracking.cpp:97). */
+pt_status pt_cancel(pt_ctx *ctx);
+
+/* One-shot drop-in for a loop of TTracker::IntegrateParticle calls
+ * (src/main.cpp:152-172): host arrays in, host arrays out, all particles
+ * tracked to their stop ID. */
+pt_status pt_integrate(pt_ctx *ctx, const pt_run_params *params, const pt_particles *in,
+                       pt_particles *out, pt_stats *stats);
+
+/* Device-resident batch: upload once, advance in windows, read back. */
+pt_status pt_batch_create(pt_ctx *ctx, const pt_run_params *params, const pt_particles *in, pt_batch **out);
+/* Advance every live particle until it stops or, at a step boundary, its lab
+ * time reaches t_pause (resuming later is bit-identical to never pausing). */
+pt_status pt_batch_advance(pt_ctx *ctx, pt_batch *batch, double t_pause, pt_stats *stats);
+pt_status pt_batch_read(pt_ctx *ctx, pt_batch *batch, pt_particles *out);
+void pt_batch_destroy(pt_batch *batch);
+
+/* Field of the whole scene at n points (x,y,z,t interleaved, 4n doubles):
+ * TFieldManager::BField with gradient and EField.  Any output may be NULL. */
+pt_status pt_field_eval(pt_ctx *ctx, int64_t n, const double *xyzt, int32_t precision,
+                        double *B, double *dBidxj, double *V, double *E);
+
+/* All segment-mesh collisions of n segments (p1, p2: 6 doubles each), sorted by
+ * (s ascending, solid ID descending) as TTriangleMesh::Collision
+ * (src/trianglemesh.cpp:134-164).  For segment i, count[i] hits are written to
+ * s/normal(3)/solid_id/distnormal at offsets i*max_hits.. ; count[i] = -1 on a
+ * coplanar (CGAL error) case. */
+pt_status pt_segment_collisions(pt_ctx *ctx, int64_t n, const double *seg, int32_t max_hits,
+                                int32_t *count, double *s, double *normal, int32_t *solid_id,
+                                double *distnormal);
+
+/* IDs of solids containing each point by +z ray parity (TTriangleMesh::GetSolids,
+ * include/trianglemesh.h:181-188) as a bit mask over scene solid indices. */
+pt_status pt_point_solids(pt_ctx *ctx, int64_t n, const double *p, uint64_t *mask);
+
+/* Calibration: FP64 fused-multiply-add throughput of this device measured by
+ * a dependent-chain DFMA kernel over all SMs (TFLOP/s, 2 flops per FMA). */
+pt_status pt_probe_fp64(pt_ctx *ctx, double *tflops);
+
+/* Library version string. */
+const char *pt_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PENTRACK_GPU_H */

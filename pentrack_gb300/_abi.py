@@ -1,0 +1,124 @@
+"""ctypes mirror of include/pentrack_gpu.h (the engine's C ABI)."""
+import ctypes as C
+
+c_double_p = C.POINTER(C.c_double)
+c_int32_p = C.POINTER(C.c_int32)
+c_int64_p = C.POINTER(C.c_int64)
+c_uint64_p = C.POINTER(C.c_uint64)
+
+PT_OK = 0
+STATUS = {
+    0: "PT_OK", -1: "PT_ERR_INVALID", -2: "PT_ERR_UNSUPPORTED", -3: "PT_ERR_OOM", -4: "PT_ERR_CUDA",
+    -5: "PT_ERR_TIMEOUT", -6: "PT_ERR_CANCELLED", -7: "PT_ERR_IO", -8: "PT_ERR_NO_DEVICE",
+}
+PT_ERR_CANCELLED = -6
+
+# stop IDs: include/globals.h:13-23 of the reference
+ID_UNKNOWN, ID_NOT_FINISH, ID_HIT_BOUNDARIES, ID_ODEINT_ERROR, ID_DECAYED = 0, -1, -2, -3, -4
+ID_INITIAL_NOT_FOUND, ID_CGAL_ERROR, ID_GEOMETRY_ERROR = -5, -6, -7
+ID_ABSORBED_IN_MATERIAL, ID_ABSORBED_ON_SURFACE = 1, 2
+
+NEUTRON, PROTON, ELECTRON = 0, 1, 2
+FIELD_TAB3D, FIELD_HARMONIC, FIELD_UNIFORM_E = 1, 2, 3
+MODE_PLAIN, MODE_BATCHED = 0, 1
+PREC_FP64, PREC_FP32 = 0, 1
+
+
+class Material(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "fermi_real", "fermi_imag", "diff_prob", "spinflip_prob", "rms_roughness", "correl_length",
+        "internal_bfield", "modified_lambert_prob", "loss_per_bounce")]
+
+
+class Solid(C.Structure):
+    _fields_ = [("id", C.c_uint32), ("material", C.c_int32), ("n_ignore", C.c_int32), ("reserved", C.c_int32),
+                ("ignore_times", c_double_p)]
+
+
+class Field(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32), ("reserved0", C.c_int32),
+        ("b_scale", C.c_double), ("e_scale", C.c_double),
+        ("xmax", C.c_double), ("xmin", C.c_double), ("ymax", C.c_double), ("ymin", C.c_double),
+        ("zmax", C.c_double), ("zmin", C.c_double), ("boundary_width", C.c_double),
+        ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("reserved1", C.c_int32),
+        ("x", c_double_p), ("y", c_double_p), ("z", c_double_p),
+        ("bx", c_double_p), ("by", c_double_p), ("bz", c_double_p), ("v", c_double_p),
+        ("offset", C.c_double * 3), ("n_coeff", C.c_int32), ("reserved2", C.c_int32),
+        ("l", c_int32_p), ("m", c_int32_p), ("g", c_double_p),
+        ("e", C.c_double * 3),
+    ]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [
+        ("n_triangles", C.c_int64), ("triangles", c_double_p), ("triangle_solid", c_int32_p),
+        ("n_solids", C.c_int32), ("n_materials", C.c_int32),
+        ("solids", C.POINTER(Solid)), ("materials", C.POINTER(Material)),
+        ("n_fields", C.c_int32), ("reserved", C.c_int32), ("fields", C.POINTER(Field)),
+    ]
+
+
+class RunParams(C.Structure):
+    _fields_ = [
+        ("species", C.c_int32), ("mode", C.c_int32), ("field_precision", C.c_int32), ("flipspin", C.c_int32),
+        ("simtime", C.c_double), ("tau", C.c_double), ("tmax", C.c_double), ("lmax", C.c_double), ("bmax", C.c_double),
+        ("n_spintimes", C.c_int32), ("steps_per_launch", C.c_int32), ("spintimes", c_double_p),
+        ("seed", C.c_uint64), ("block_size", C.c_int32), ("max_launches", C.c_int32), ("timeout_s", C.c_double),
+    ]
+
+
+class Particles(C.Structure):
+    _fields_ = [
+        ("n", C.c_int64), ("id", c_int64_p), ("t", c_double_p), ("y", c_double_p), ("spin", c_double_p),
+        ("stop_id", c_int32_p), ("solid", c_int32_p), ("n_hit", c_int32_p), ("n_step", c_int32_p),
+        ("n_spinflip", c_int32_p), ("reserved", c_int32_p),
+        ("h_max", c_double_p), ("noflip_prob", c_double_p), ("tau", c_double_p), ("h_start", c_double_p),
+        ("n_accepted", c_int64_p), ("n_rejected", c_int64_p),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("kernel_ms", C.c_double), ("span_ms", C.c_double), ("wall_ms", C.c_double), ("particle_seconds", C.c_double),
+        ("launches", C.c_int64), ("active", C.c_int64),
+        ("rk_accepted", C.c_int64), ("rk_rejected", C.c_int64), ("rhs_evals", C.c_int64), ("field_evals", C.c_int64),
+        ("hits", C.c_int64), ("bisection_levels", C.c_int64),
+        ("bvh_nodes", C.c_int64), ("tri_tests", C.c_int64), ("subsegments", C.c_int64), ("dense_evals", C.c_int64),
+        ("dominant_kernel_ms", C.c_double), ("dominant_launches", C.c_int64), ("dominant_kernel", C.c_char * 48),
+    ]
+
+    def as_dict(self):
+        d = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            d[name] = v.decode() if isinstance(v, bytes) else v
+        return d
+
+
+def declare(lib):
+    """Attach argument/return types of every exported entry point."""
+    P = C.POINTER
+    vp = C.c_void_p
+    sig = {
+        "pt_create": (C.c_int32, [P(SceneDesc), C.c_int32, P(vp)]),
+        "pt_destroy": (None, [vp]),
+        "pt_last_error": (C.c_char_p, [vp]),
+        "pt_cancel": (C.c_int32, [vp]),
+        "pt_integrate": (C.c_int32, [vp, P(RunParams), P(Particles), P(Particles), P(Stats)]),
+        "pt_batch_create": (C.c_int32, [vp, P(RunParams), P(Particles), P(vp)]),
+        "pt_batch_advance": (C.c_int32, [vp, vp, C.c_double, P(Stats)]),
+        "pt_batch_read": (C.c_int32, [vp, vp, P(Particles)]),
+        "pt_batch_destroy": (None, [vp]),
+        "pt_field_eval": (C.c_int32, [vp, C.c_int64, c_double_p, C.c_int32, c_double_p, c_double_p, c_double_p, c_double_p]),
+        "pt_segment_collisions": (C.c_int32, [vp, C.c_int64, c_double_p, C.c_int32, c_int32_p, c_double_p, c_double_p,
+                                              c_int32_p, c_double_p]),
+        "pt_point_solids": (C.c_int32, [vp, C.c_int64, c_double_p, c_uint64_p]),
+        "pt_probe_fp64": (C.c_int32, [vp, c_double_p]),
+        "pt_version": (C.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return sig

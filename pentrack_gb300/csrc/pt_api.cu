@@ -1,0 +1,695 @@
+/*
+ * pt_api.cu -- kernels and the C ABI of the GB300 tracking engine
+ * (declared in include/pentrack_gpu.h).
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "pt_lane.cuh"
+#include "pt_scene.hpp"
+
+using namespace ptd;
+
+/* ================================================================== */
+/* kernels                                                            */
+/* ================================================================== */
+namespace {
+
+__device__ __forceinline__ void flush_counters(DCounters *C, const LaneCounters &lc, double psec, bool active) {
+    /* warp-aggregated atomics */
+    unsigned long long v[11] = {lc.rk_acc, lc.rk_rej, lc.rhs, lc.fields, lc.hits, lc.bisect, lc.nodes, lc.tris, lc.subseg, lc.dense,
+                                active ? 1ull : 0ull};
+    const unsigned mask = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    for (int k = 0; k < 11; ++k) {
+        unsigned long long s = v[k];
+        for (int o = 16; o > 0; o >>= 1) {
+            unsigned long long w = __shfl_down_sync(mask, s, o);
+            if (lane + o < 32 && ((mask >> (lane + o)) & 1)) s += w;
+        }
+        v[k] = s;
+    }
+    double ps = psec;
+    for (int o = 16; o > 0; o >>= 1) {
+        double w = __shfl_down_sync(mask, ps, o);
+        if (lane + o < 32 && ((mask >> (lane + o)) & 1)) ps += w;
+    }
+    if (lane == leader) {
+        unsigned long long *dst[11] = {&C->rk_accepted, &C->rk_rejected, &C->rhs_evals, &C->field_evals, &C->hits,
+                                       &C->bisection_levels, &C->bvh_nodes, &C->tri_tests, &C->subsegments,
+                                       &C->dense_evals, &C->active};
+        for (int k = 0; k < 11; ++k) if (v[k]) atomicAdd(dst[k], v[k]);
+        if (ps != 0) atomicAdd(&C->particle_seconds, ps);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_init(DScene S, DRun R, DBatch b, DCounters *C) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.n) return;
+    Lane L(S, R);
+    const int64_t n = b.n;
+    L.id = b.id[i];
+    L.t = b.t[i];
+    for (int c = 0; c < 9; ++c) { L.y[c] = b.y[c * n + i]; L.dydt[c] = 0; }
+    for (int c = 0; c < 5; ++c) L.spin[c] = b.spin[c * n + i];
+    L.stop = PT_ID_UNKNOWN;
+    QueryStats qs{0, 0};
+    L.init(qs);
+    L.store(b, i);
+    b.hstart[i] = L.hmax;
+    b.t_last[i] = L.t;
+}
+
+/* Plain form: every lane advances its particle by up to `steps` LOOP-A
+ * iterations, then the launch ends and the host relaunches. */
+__global__ void __launch_bounds__(128) k_plain(DScene S, DRun R, DBatch b, DCounters *C, int steps) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.n) return;
+    if (b.stop_id[i] != PT_ID_UNKNOWN || b.t[i] >= R.t_pause) return;
+    Lane L(S, R);
+    L.load(b, i);
+    const double t0 = L.t;
+    for (int s = 0; s < steps; ++s) {
+        L.step();
+        if (L.stop != PT_ID_UNKNOWN || L.t >= R.t_pause) break;
+        if (*R.cancel) break;
+    }
+    L.store(b, i);
+    bool active = (L.stop == PT_ID_UNKNOWN && L.t < R.t_pause);
+    flush_counters(C, L.lc, L.t - t0, active);
+}
+
+/* FP64 throughput probe: 8 independent dependent-FMA chains per thread */
+__global__ void k_fp64_probe(double *out, int iters, double a, double b) {
+    double x0 = threadIdx.x * 1e-9, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == 1.2345) out[0] = s;
+}
+
+__global__ void k_field(DScene S, int prec, int64_t n, const double *xyzt, double *B, double *dB, double *V, double *E) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double *q = xyzt + 4 * i;
+    double b[3], db[3][3], v, e[3];
+    bfield<true>(S, prec, q[0], q[1], q[2], b, db);
+    efield(S, prec, q[0], q[1], q[2], v, e);
+    if (B) for (int k = 0; k < 3; ++k) B[3 * i + k] = b[k];
+    if (dB) for (int k = 0; k < 9; ++k) dB[9 * i + k] = db[k / 3][k % 3];
+    if (V) V[i] = v;
+    if (E) for (int k = 0; k < 3; ++k) E[3 * i + k] = e[k];
+}
+
+__global__ void k_collisions(DScene S, int64_t n, const double *seg, int maxh, int *count, double *s, double *nrm, int *sid,
+                             double *dn) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Coll c[PT_MAX_COLLS];
+    QueryStats qs{0, 0};
+    bool cp;
+    int h = mesh_query<1>(S, seg + 6 * i, seg + 6 * i + 3, 0.0, 1.0, c, PT_MAX_COLLS, nullptr, qs, cp);
+    if (cp) { count[i] = -1; return; }
+    count[i] = h;
+    int k = h < maxh ? h : maxh;
+    if (k > PT_MAX_COLLS) k = PT_MAX_COLLS;
+    for (int j = 0; j < k; ++j) {
+        int64_t o = i * maxh + j;
+        s[o] = c[j].s;
+        for (int a = 0; a < 3; ++a) nrm[3 * o + a] = c[j].n[a];
+        sid[o] = (int)c[j].id;
+        dn[o] = c[j].dn;
+    }
+}
+
+__global__ void k_point_solids(DScene S, int64_t n, const double *p, unsigned long long *mask) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    QueryStats qs{0, 0};
+    mask[i] = point_solids(S, p + 3 * i, qs);
+}
+
+} // namespace
+
+/* ================================================================== */
+/* host side                                                          */
+/* ================================================================== */
+namespace {
+thread_local std::string g_create_err;
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+} // namespace
+
+struct pt_ctx {
+    int device = 0;
+    std::string err;
+    DScene scene;
+    std::vector<void *> allocs;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs0 = nullptr, evs1 = nullptr;
+    int *cancel_host = nullptr;
+    int *cancel_dev = nullptr;
+    DCounters *counters = nullptr;
+    DCounters *counters_host = nullptr;
+    int sm_count = 0;
+};
+
+struct pt_batch {
+    pt_ctx *ctx = nullptr;
+    DBatch b{};
+    DRun run{};
+    std::vector<double> spintimes;
+    std::vector<void *> allocs;
+    int max_launches = 0;
+    double timeout_s = 0;
+};
+
+namespace {
+
+bool ck(pt_ctx *c, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return true;
+    if (c) c->err = std::string(what) + ": " + cudaGetErrorString(e);
+    else g_create_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return false;
+}
+
+template <class T> T *dalloc(std::vector<void *> &list, size_t count, cudaError_t &e) {
+    void *p = nullptr;
+    e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+    if (e == cudaSuccess) list.push_back(p);
+    return (T *)p;
+}
+
+template <class T> T *dupload(std::vector<void *> &list, const T *src, size_t count, cudaError_t &e) {
+    T *d = dalloc<T>(list, count, e);
+    if (e != cudaSuccess) return nullptr;
+    if (count) e = cudaMemcpy(d, src, count * sizeof(T), cudaMemcpyHostToDevice);
+    return d;
+}
+
+DSpecies make_species(int s) {
+    DSpecies d{};
+    d.kind = s;
+    if (s == PT_PROTON) {
+        d.q = PT_PROTON_Q; d.m = PT_PROTON_M; d.mu = PT_PROTON_MU; d.gamma = PT_PROTON_GAMMA; d.inv_mkg = PT_PROTON_INV_MKG;
+        d.fgrav = PT_PROTON_FGRAV; d.mu_over_e = PT_PROTON_MU_OVER_E; d.q_over_e = PT_PROTON_Q_OVER_E; d.mc2 = PT_PROTON_MC2; d.mg = PT_PROTON_MG;
+    } else if (s == PT_ELECTRON) {
+        d.q = PT_ELECTRON_Q; d.m = PT_ELECTRON_M; d.mu = PT_ELECTRON_MU; d.gamma = PT_ELECTRON_GAMMA; d.inv_mkg = PT_ELECTRON_INV_MKG;
+        d.fgrav = PT_ELECTRON_FGRAV; d.mu_over_e = PT_ELECTRON_MU_OVER_E; d.q_over_e = PT_ELECTRON_Q_OVER_E; d.mc2 = PT_ELECTRON_MC2; d.mg = PT_ELECTRON_MG;
+    } else {
+        d.kind = PT_NEUTRON;
+        d.q = PT_NEUTRON_Q; d.m = PT_NEUTRON_M; d.mu = PT_NEUTRON_MU; d.gamma = PT_NEUTRON_GAMMA; d.inv_mkg = PT_NEUTRON_INV_MKG;
+        d.fgrav = PT_NEUTRON_FGRAV; d.mu_over_e = PT_NEUTRON_MU_OVER_E; d.q_over_e = PT_NEUTRON_Q_OVER_E; d.mc2 = PT_NEUTRON_MC2; d.mg = PT_NEUTRON_MG;
+    }
+    return d;
+}
+
+pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
+    cudaError_t e = cudaSuccess;
+    std::string &err = c->err;
+    if (!d || d->n_solids < 1 || !d->solids || d->solids[0].id != 1) { err = "solids[0] must be the default solid with ID 1"; return PT_ERR_INVALID; }
+    if (d->n_solids > PT_MAX_SOLIDS) { err = "at most 64 solids are supported"; return PT_ERR_UNSUPPORTED; }
+    if (d->n_fields > PT_MAX_FIELDS) { err = "at most 8 fields are supported"; return PT_ERR_UNSUPPORTED; }
+    if (d->n_triangles > 0 && (!d->triangles || !d->triangle_solid)) { err = "triangles missing"; return PT_ERR_INVALID; }
+    /* materials */
+    std::vector<DMat> mats(d->n_materials);
+    for (int i = 0; i < d->n_materials; ++i) {
+        const pt_material &m = d->materials[i];
+        if (m.rms_roughness != 0 || m.correl_length != 0) { err = "MicroRoughness materials are not implemented on the device path"; return PT_ERR_UNSUPPORTED; }
+        if (m.diff_prob < 0 || m.diff_prob > 1 || m.spinflip_prob < 0 || m.spinflip_prob > 1 || m.loss_per_bounce < 0 || m.loss_per_bounce > 1) {
+            err = "material probability outside 0..1"; return PT_ERR_INVALID;
+        }
+        mats[i] = DMat{m.fermi_real, m.fermi_imag, m.diff_prob, m.spinflip_prob, m.internal_bfield, m.modified_lambert_prob, m.loss_per_bounce};
+    }
+    /* solids */
+    std::vector<DSolid> solids(d->n_solids);
+    for (int i = 0; i < d->n_solids; ++i) {
+        const pt_solid &s = d->solids[i];
+        DSolid &o = solids[i];
+        std::memset(&o, 0, sizeof(o));
+        o.id = s.id;
+        o.mat = s.material;
+        if (s.material < 0 || s.material >= d->n_materials) { err = "solid references an undefined material"; return PT_ERR_INVALID; }
+        if (s.n_ignore > PT_MAX_IGNORE) { err = "at most 4 ignore intervals per solid"; return PT_ERR_UNSUPPORTED; }
+        o.n_ign = s.n_ignore;
+        for (int k = 0; k < 2 * s.n_ignore; ++k) o.ign[k] = s.ignore_times[k];
+        for (int k = 0; k < 3; ++k) { o.lo[k] = 1e300; o.hi[k] = -1e300; }
+        for (int j = 0; j < i; ++j)
+            if (solids[j].id == o.id) { err = "solid IDs must be unique"; return PT_ERR_INVALID; }
+    }
+    /* triangles */
+    std::vector<pth::HostTri> tris((size_t)d->n_triangles);
+    double zmax = -1e300;
+    for (int64_t t = 0; t < d->n_triangles; ++t) {
+        pth::HostTri &h = tris[t];
+        const double *v = d->triangles + 9 * t;
+        for (int k = 0; k < 3; ++k) { h.a[k] = v[k]; h.b[k] = v[3 + k]; h.c[k] = v[6 + k]; }
+        double e1[3] = {h.b[0] - h.a[0], h.b[1] - h.a[1], h.b[2] - h.a[2]};
+        double e2[3] = {h.c[0] - h.a[0], h.c[1] - h.a[1], h.c[2] - h.a[2]};
+        double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        double nl = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        for (int k = 0; k < 3; ++k) h.n[k] = n[k] / nl;
+        h.solid = d->triangle_solid[t];
+        h.pad = 0;
+        if (h.solid <= 0 || h.solid >= d->n_solids) { err = "triangle solid index out of range"; return PT_ERR_INVALID; }
+        DSolid &so = solids[h.solid];
+        for (int k = 0; k < 3; ++k) {
+            so.lo[k] = std::min(so.lo[k], std::min(h.a[k], std::min(h.b[k], h.c[k])));
+            so.hi[k] = std::max(so.hi[k], std::max(h.a[k], std::max(h.b[k], h.c[k])));
+        }
+        zmax = std::max(zmax, std::max(h.a[2], std::max(h.b[2], h.c[2])));
+    }
+    std::vector<pth::HostNode> nodes;
+    pth::build_bvh(tris, nodes);
+    static_assert(sizeof(pth::HostTri) == sizeof(DTri), "triangle layout");
+    static_assert(sizeof(pth::HostNode) == sizeof(DNode), "node layout");
+    DScene &S = c->scene;
+    std::memset(&S, 0, sizeof(S));
+    S.n_tris = (int)tris.size();
+    S.n_nodes = (int)nodes.size();
+    S.n_solids = d->n_solids;
+    S.n_mats = d->n_materials;
+    S.n_fields = d->n_fields;
+    S.mesh_zmax = tris.empty() ? 0.0 : zmax;
+    S.tris = (const DTri *)dupload(c->allocs, (const DTri *)tris.data(), tris.size(), e);
+    if (e) return ck(c, e, "upload triangles"), PT_ERR_CUDA;
+    S.nodes = (const DNode *)dupload(c->allocs, (const DNode *)nodes.data(), nodes.size(), e);
+    if (e) return ck(c, e, "upload bvh"), PT_ERR_CUDA;
+    S.solids = dupload(c->allocs, solids.data(), solids.size(), e);
+    if (e) return ck(c, e, "upload solids"), PT_ERR_CUDA;
+    S.mats = dupload(c->allocs, mats.data(), mats.size(), e);
+    if (e) return ck(c, e, "upload materials"), PT_ERR_CUDA;
+    /* fields */
+    for (int fi = 0; fi < d->n_fields; ++fi) {
+        const pt_field &f = d->fields[fi];
+        DField &o = S.fields[fi];
+        std::memset(&o, 0, sizeof(o));
+        o.type = f.type;
+        o.bscale = f.b_scale; o.escale = f.e_scale;
+        o.xmax = f.xmax; o.xmin = f.xmin; o.ymax = f.ymax; o.ymin = f.ymin; o.zmax = f.zmax; o.zmin = f.zmin;
+        o.bw = f.boundary_width;
+        if (o.bw < 0 || (o.xmin < o.xmax && o.ymin < o.ymax && o.zmin < o.zmax &&
+                         (o.bw > (o.xmax - o.xmin) / 2 || o.bw > (o.ymax - o.ymin) / 2 || o.bw > (o.zmax - o.zmin) / 2))) {
+            err = "You defined a field with an invalid boundary. Check field parameters.";
+            return PT_ERR_INVALID;
+        }
+        if (f.type == PT_FIELD_TAB3D) {
+            if (f.nx < 2 || f.ny < 2 || f.nz < 2 || !f.x || !f.y || !f.z) { err = "3D table needs at least 2 points per axis"; return PT_ERR_INVALID; }
+            std::vector<double> ax[3] = {std::vector<double>(f.x, f.x + f.nx), std::vector<double>(f.y, f.y + f.ny),
+                                         std::vector<double>(f.z, f.z + f.nz)};
+            for (int a = 0; a < 3; ++a)
+                for (size_t k = 1; k < ax[a].size(); ++k)
+                    if (!(ax[a][k] > ax[a][k - 1])) { err = "3D table axes must be strictly increasing"; return PT_ERR_INVALID; }
+            o.has_b = (f.bx || f.by || f.bz) ? 1 : 0;
+            o.has_v = f.v ? 1 : 0;
+            o.ncomp = o.has_v ? 4 : 3;
+            size_t tot = (size_t)f.nx * f.ny * f.nz;
+            std::vector<double> nd(tot * o.ncomp * 8, 0.0);
+            std::vector<double> zero(tot, 0.0);
+            const double *comp[4] = {f.bx, f.by, f.bz, f.v};
+            for (int k = 0; k < o.ncomp; ++k) pth::hermite_nodes(ax, comp[k] ? comp[k] : zero.data(), k, o.ncomp * 8, nd);
+            std::vector<float> nd32(nd.size());
+            for (size_t k = 0; k < nd.size(); ++k) nd32[k] = (float)nd[k];
+            o.node64 = dupload(c->allocs, nd.data(), nd.size(), e);
+            if (e) return ck(c, e, "upload table"), PT_ERR_CUDA;
+            o.node32 = dupload(c->allocs, nd32.data(), nd32.size(), e);
+            if (e) return ck(c, e, "upload table"), PT_ERR_CUDA;
+            int n3[3] = {f.nx, f.ny, f.nz};
+            for (int a = 0; a < 3; ++a) {
+                o.n[a] = n3[a];
+                o.ax[a] = dupload(c->allocs, ax[a].data(), ax[a].size(), e);
+                if (e) return ck(c, e, "upload axis"), PT_ERR_CUDA;
+                o.a0[a] = ax[a][0];
+                o.inv_h[a] = (double)(ax[a].size() - 1) / (ax[a].back() - ax[a][0]);
+            }
+        } else if (f.type == PT_FIELD_HARMONIC) {
+            std::vector<double> coef;
+            std::vector<int> expo;
+            if (!pth::harmonic_polynomial(f.n_coeff, f.l, f.m, f.g, coef, expo, err)) return PT_ERR_INVALID;
+            o.has_b = 1;
+            o.n_mono = (int)coef.size();
+            o.mono_c = dupload(c->allocs, coef.data(), coef.size(), e);
+            if (e) return ck(c, e, "upload harmonic"), PT_ERR_CUDA;
+            o.mono_e = dupload(c->allocs, expo.data(), expo.size(), e);
+            if (e) return ck(c, e, "upload harmonic"), PT_ERR_CUDA;
+            for (int k = 0; k < 3; ++k) o.offset[k] = f.offset[k];
+        } else if (f.type == PT_FIELD_UNIFORM_E) {
+            o.has_v = 1;
+            for (int k = 0; k < 3; ++k) o.e[k] = f.e[k];
+        } else {
+            err = "unsupported field type";
+            return PT_ERR_UNSUPPORTED;
+        }
+    }
+    return PT_OK;
+}
+
+void free_list(std::vector<void *> &l) {
+    for (void *p : l) cudaFree(p);
+    l.clear();
+}
+
+int grid_for(int64_t n, int block) { return (int)((n + block - 1) / block); }
+
+} // namespace
+
+extern "C" {
+
+const char *pt_version(void) { return "pentrack_gb300 0.1 (sm_103a)"; }
+
+const char *pt_last_error(const pt_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_err.c_str(); }
+
+pt_status pt_create(const pt_scene_desc *scene, int32_t device, pt_ctx **out) {
+    if (!out) return PT_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        g_create_err = "no CUDA device";
+        return PT_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= ndev) { g_create_err = "bad device index"; return PT_ERR_INVALID; }
+    std::unique_ptr<pt_ctx> c(new pt_ctx());
+    c->device = device;
+    if (!ck(nullptr, cudaSetDevice(device), "cudaSetDevice")) return PT_ERR_CUDA;
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    pt_status st = build_scene(c.get(), scene);
+    if (st != PT_OK) {
+        g_create_err = c->err;
+        free_list(c->allocs);
+        return st;
+    }
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess ||
+        (e = cudaEventCreate(&c->evs0)) != cudaSuccess || (e = cudaEventCreate(&c->evs1)) != cudaSuccess ||
+        (e = cudaHostAlloc((void **)&c->cancel_host, sizeof(int), cudaHostAllocMapped)) != cudaSuccess ||
+        (e = cudaHostGetDevicePointer((void **)&c->cancel_dev, c->cancel_host, 0)) != cudaSuccess ||
+        (e = cudaMalloc((void **)&c->counters, sizeof(DCounters))) != cudaSuccess ||
+        (e = cudaHostAlloc((void **)&c->counters_host, sizeof(DCounters), 0)) != cudaSuccess) {
+        g_create_err = std::string("context setup: ") + cudaGetErrorString(e);
+        free_list(c->allocs);
+        return PT_ERR_CUDA;
+    }
+    *c->cancel_host = 0;
+    *out = c.release();
+    return PT_OK;
+}
+
+void pt_destroy(pt_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_list(c->allocs);
+    if (c->counters) cudaFree(c->counters);
+    if (c->counters_host) cudaFreeHost(c->counters_host);
+    if (c->cancel_host) cudaFreeHost(c->cancel_host);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->evs0) cudaEventDestroy(c->evs0);
+    if (c->evs1) cudaEventDestroy(c->evs1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+pt_status pt_cancel(pt_ctx *c) {
+    if (!c) return PT_ERR_INVALID;
+    *(volatile int *)c->cancel_host = 1;
+    return PT_OK;
+}
+
+pt_status pt_batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles *in, pt_batch **out) {
+    if (!c || !p || !in || !out || in->n < 0 || !in->id || !in->t || !in->y) return PT_ERR_INVALID;
+    cudaSetDevice(c->device);
+    *out = nullptr;
+    if (p->n_spintimes > PT_MAX_SPINTIMES) { c->err = "at most 8 spintimes intervals"; return PT_ERR_UNSUPPORTED; }
+    if (p->species < PT_NEUTRON || p->species > PT_ELECTRON) { c->err = "unknown species"; return PT_ERR_INVALID; }
+    std::unique_ptr<pt_batch> B(new pt_batch());
+    B->ctx = c;
+    B->max_launches = p->max_launches;
+    B->timeout_s = p->timeout_s;
+    DRun &R = B->run;
+    std::memset(&R, 0, sizeof(R));
+    R.sp = make_species(p->species);
+    R.simtime = p->simtime; R.tau = p->tau; R.tmax = p->tmax; R.lmax = p->lmax; R.bmax = p->bmax;
+    R.n_spintimes = p->n_spintimes;
+    for (int k = 0; k < p->n_spintimes; ++k) R.spintimes[k] = p->spintimes[k];
+    R.flipspin = p->flipspin;
+    R.prec = p->field_precision;
+    R.steps_per_launch = p->steps_per_launch > 0 ? p->steps_per_launch : 64;
+    R.seed = p->seed;
+    R.t_pause = INFINITY;
+    R.cancel = c->cancel_dev;
+    const int64_t n = in->n;
+    DBatch &b = B->b;
+    b.n = n;
+    cudaError_t e = cudaSuccess;
+#define ALLOC(field, T, cnt) b.field = dalloc<T>(B->allocs, (size_t)(cnt), e); if (e) { free_list(B->allocs); return ck(c, e, "batch alloc"), PT_ERR_OOM; }
+    ALLOC(id, int64_t, n) ALLOC(t, double, n) ALLOC(y, double, 9 * n) ALLOC(dydt, double, 9 * n) ALLOC(dt, double, n)
+    ALLOC(spin, double, 5 * n) ALLOC(tau, double, n) ALLOC(hmax, double, n) ALLOC(noflip, double, n) ALLOC(hstart, double, n)
+    ALLOC(t_last, double, n) ALLOC(stop_id, int32_t, n) ALLOC(nhit, int32_t, n) ALLOC(nstep, int32_t, n)
+    ALLOC(nspinflip, int32_t, n) ALLOC(nsol, int32_t, n) ALLOC(flags, uint32_t, n) ALLOC(stack, uint64_t, n)
+    ALLOC(rng_n, uint64_t, n) ALLOC(nacc, int64_t, n) ALLOC(nrej, int64_t, n)
+#undef ALLOC
+    if (n > 0) {
+        if ((e = cudaMemcpyAsync(b.id, in->id, n * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream)) ||
+            (e = cudaMemcpyAsync(b.t, in->t, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) ||
+            (e = cudaMemcpyAsync(b.y, in->y, 9 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream))) {
+            free_list(B->allocs);
+            return ck(c, e, "batch upload"), PT_ERR_CUDA;
+        }
+        if (in->spin) e = cudaMemcpyAsync(b.spin, in->spin, 5 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+        else e = cudaMemsetAsync(b.spin, 0, 5 * n * sizeof(double), c->stream);
+        if (e) { free_list(B->allocs); return ck(c, e, "batch upload"), PT_ERR_CUDA; }
+        k_init<<<grid_for(n, 128), 128, 0, c->stream>>>(c->scene, R, b, c->counters);
+        if ((e = cudaGetLastError()) || (e = cudaStreamSynchronize(c->stream))) {
+            free_list(B->allocs);
+            return ck(c, e, "init kernel"), PT_ERR_CUDA;
+        }
+    }
+    *out = B.release();
+    return PT_OK;
+}
+
+void pt_batch_destroy(pt_batch *B) {
+    if (!B) return;
+    if (B->ctx) cudaSetDevice(B->ctx->device);
+    free_list(B->allocs);
+    delete B;
+}
+
+pt_status pt_batch_advance(pt_ctx *c, pt_batch *B, double t_pause, pt_stats *stats) {
+    if (!c || !B) return PT_ERR_INVALID;
+    cudaSetDevice(c->device);
+    auto w0 = std::chrono::steady_clock::now();
+    DRun R = B->run;
+    R.t_pause = t_pause;
+    pt_stats acc;
+    std::memset(&acc, 0, sizeof(acc));
+    std::snprintf(acc.dominant_kernel, sizeof(acc.dominant_kernel), "k_plain");
+    cudaError_t e;
+    int steps = R.steps_per_launch;
+    const int block = 128;
+    const int64_t n = B->b.n;
+    bool cancelled = false, timed_out = false;
+    cudaEventRecord(c->evs0, c->stream);
+    for (int launch = 0; n > 0; ++launch) {
+        if ((e = cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream))) return ck(c, e, "memset"), PT_ERR_CUDA;
+        cudaEventRecord(c->ev0, c->stream);
+        k_plain<<<grid_for(n, block), block, 0, c->stream>>>(c->scene, R, B->b, c->counters, steps);
+        cudaEventRecord(c->ev1, c->stream);
+        if ((e = cudaGetLastError())) return ck(c, e, "k_plain launch"), PT_ERR_CUDA;
+        if ((e = cudaMemcpyAsync(c->counters_host, c->counters, sizeof(DCounters), cudaMemcpyDeviceToHost, c->stream)))
+            return ck(c, e, "counters"), PT_ERR_CUDA;
+        if ((e = cudaStreamSynchronize(c->stream))) return ck(c, e, "k_plain"), PT_ERR_CUDA;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        const DCounters &k = *c->counters_host;
+        acc.kernel_ms += ms;
+        acc.dominant_kernel_ms += ms;
+        acc.dominant_launches += 1;
+        acc.launches += 1;
+        acc.rk_accepted += k.rk_accepted; acc.rk_rejected += k.rk_rejected; acc.rhs_evals += k.rhs_evals;
+        acc.field_evals += k.field_evals; acc.hits += k.hits; acc.bisection_levels += k.bisection_levels;
+        acc.bvh_nodes += k.bvh_nodes; acc.tri_tests += k.tri_tests; acc.subsegments += k.subsegments;
+        acc.dense_evals += k.dense_evals; acc.particle_seconds += k.particle_seconds;
+        acc.active = (int64_t)k.active;
+        if (*(volatile int *)c->cancel_host) { cancelled = true; break; }
+        if (k.active == 0) break;
+        if (B->max_launches > 0 && launch + 1 >= B->max_launches) { timed_out = true; break; }
+        if (B->timeout_s > 0 && std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count() > B->timeout_s) {
+            timed_out = true;
+            break;
+        }
+    }
+    cudaEventRecord(c->evs1, c->stream);
+    cudaEventSynchronize(c->evs1);
+    {
+        float sp = 0;
+        cudaEventElapsedTime(&sp, c->evs0, c->evs1);
+        acc.span_ms = sp;
+    }
+    acc.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+    if (stats) *stats = acc;
+    if (cancelled) { *(volatile int *)c->cancel_host = 0; return PT_ERR_CANCELLED; }
+    if (timed_out) { c->err = "particles still active at the launch or time limit"; return PT_ERR_TIMEOUT; }
+    return PT_OK;
+}
+
+pt_status pt_batch_read(pt_ctx *c, pt_batch *B, pt_particles *o) {
+    if (!c || !B || !o) return PT_ERR_INVALID;
+    cudaSetDevice(c->device);
+    const DBatch &b = B->b;
+    const int64_t n = b.n;
+    if (o->n != n) { c->err = "output batch size differs"; return PT_ERR_INVALID; }
+    cudaError_t e = cudaSuccess;
+#define GET(dst, src, T, cnt) if (o->dst && !e) e = cudaMemcpyAsync(o->dst, b.src, (size_t)(cnt) * sizeof(T), cudaMemcpyDeviceToHost, c->stream);
+    GET(id, id, int64_t, n) GET(t, t, double, n) GET(y, y, double, 9 * n) GET(spin, spin, double, 5 * n)
+    GET(stop_id, stop_id, int32_t, n) GET(n_hit, nhit, int32_t, n) GET(n_step, nstep, int32_t, n)
+    GET(n_spinflip, nspinflip, int32_t, n) GET(h_max, hmax, double, n) GET(noflip_prob, noflip, double, n)
+    GET(tau, tau, double, n) GET(h_start, hstart, double, n) GET(n_accepted, nacc, int64_t, n) GET(n_rejected, nrej, int64_t, n)
+#undef GET
+    if (!e) e = cudaStreamSynchronize(c->stream);
+    if (e) return ck(c, e, "batch read"), PT_ERR_CUDA;
+    if (o->solid) {
+        /* ID of the highest-priority non-ignored solid on each particle's stack */
+        std::vector<uint64_t> st(n);
+        std::vector<int32_t> ns(n);
+        std::vector<DSolid> solids(c->scene.n_solids);
+        if ((e = cudaMemcpy(st.data(), b.stack, n * sizeof(uint64_t), cudaMemcpyDeviceToHost)) ||
+            (e = cudaMemcpy(ns.data(), b.nsol, n * sizeof(int32_t), cudaMemcpyDeviceToHost)) ||
+            (e = cudaMemcpy(solids.data(), c->scene.solids, solids.size() * sizeof(DSolid), cudaMemcpyDeviceToHost)))
+            return ck(c, e, "batch read"), PT_ERR_CUDA;
+        for (int64_t i = 0; i < n; ++i) {
+            int best = 0;
+            for (int k = 1; k < ns[i] && k < PT_MAX_STACK; ++k) {
+                uint8_t vb = (uint8_t)(st[i] >> (8 * best)), vk = (uint8_t)(st[i] >> (8 * k));
+                bool ib = vb >> 7, ik = vk >> 7;
+                if (ib || (!ik && solids[vb & 63].id < solids[vk & 63].id)) best = k;
+            }
+            o->solid[i] = (int32_t)solids[(uint8_t)(st[i] >> (8 * best)) & 63].id;
+        }
+    }
+    return PT_OK;
+}
+
+pt_status pt_integrate(pt_ctx *c, const pt_run_params *p, const pt_particles *in, pt_particles *out, pt_stats *stats) {
+    if (!c || !p || !in || !out) return PT_ERR_INVALID;
+    auto w0 = std::chrono::steady_clock::now();
+    pt_batch *B = nullptr;
+    pt_status st = pt_batch_create(c, p, in, &B);
+    if (st != PT_OK) return st;
+    pt_stats s;
+    std::memset(&s, 0, sizeof(s));
+    st = pt_batch_advance(c, B, INFINITY, &s);
+    if (st == PT_OK || st == PT_ERR_CANCELLED) {
+        pt_status st2 = pt_batch_read(c, B, out);
+        if (st == PT_OK) st = st2;
+    }
+    pt_batch_destroy(B);
+    s.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+    if (stats) *stats = s;
+    return st;
+}
+
+pt_status pt_field_eval(pt_ctx *c, int64_t n, const double *xyzt, int32_t prec, double *B, double *dB, double *V, double *E) {
+    if (!c || n < 0 || (!xyzt && n)) return PT_ERR_INVALID;
+    if (n == 0) return PT_OK;
+    cudaSetDevice(c->device);
+    std::vector<void *> tmp;
+    cudaError_t e = cudaSuccess;
+    double *dq = dupload(tmp, xyzt, 4 * n, e);
+    double *dB_ = dalloc<double>(tmp, 3 * n, e), *ddB = dalloc<double>(tmp, 9 * n, e), *dV = dalloc<double>(tmp, n, e),
+           *dE = dalloc<double>(tmp, 3 * n, e);
+    if (e) { free_list(tmp); return ck(c, e, "field eval alloc"), PT_ERR_OOM; }
+    k_field<<<grid_for(n, 128), 128, 0, c->stream>>>(c->scene, prec, n, dq, dB_, ddB, dV, dE);
+    e = cudaGetLastError();
+    if (!e && B) e = cudaMemcpyAsync(B, dB_, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (!e && dB) e = cudaMemcpyAsync(dB, ddB, 9 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (!e && V) e = cudaMemcpyAsync(V, dV, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (!e && E) e = cudaMemcpyAsync(E, dE, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaStreamSynchronize(c->stream);
+    free_list(tmp);
+    if (e) return ck(c, e, "field eval"), PT_ERR_CUDA;
+    return PT_OK;
+}
+
+pt_status pt_segment_collisions(pt_ctx *c, int64_t n, const double *seg, int32_t max_hits, int32_t *count, double *s,
+                                double *normal, int32_t *solid_id, double *distnormal) {
+    if (!c || n < 0 || max_hits < 1 || !count) return PT_ERR_INVALID;
+    if (n == 0) return PT_OK;
+    cudaSetDevice(c->device);
+    std::vector<void *> tmp;
+    cudaError_t e = cudaSuccess;
+    double *dseg = dupload(tmp, seg, 6 * n, e);
+    int *dc = dalloc<int>(tmp, n, e);
+    double *ds = dalloc<double>(tmp, n * max_hits, e), *dn = dalloc<double>(tmp, 3 * n * max_hits, e),
+           *ddn = dalloc<double>(tmp, n * max_hits, e);
+    int *dsid = dalloc<int>(tmp, n * max_hits, e);
+    if (e) { free_list(tmp); return ck(c, e, "collision alloc"), PT_ERR_OOM; }
+    k_collisions<<<grid_for(n, 128), 128, 0, c->stream>>>(c->scene, n, dseg, max_hits, dc, ds, dn, dsid, ddn);
+    e = cudaGetLastError();
+    if (!e) e = cudaMemcpyAsync(count, dc, n * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    if (!e && s) e = cudaMemcpyAsync(s, ds, n * max_hits * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (!e && normal) e = cudaMemcpyAsync(normal, dn, 3 * n * max_hits * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (!e && solid_id) e = cudaMemcpyAsync(solid_id, dsid, n * max_hits * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    if (!e && distnormal) e = cudaMemcpyAsync(distnormal, ddn, n * max_hits * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaStreamSynchronize(c->stream);
+    free_list(tmp);
+    if (e) return ck(c, e, "collisions"), PT_ERR_CUDA;
+    return PT_OK;
+}
+
+pt_status pt_probe_fp64(pt_ctx *c, double *tflops) {
+    if (!c || !tflops) return PT_ERR_INVALID;
+    cudaSetDevice(c->device);
+    double *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(double));
+    if (e) return ck(c, e, "probe"), PT_ERR_CUDA;
+    const int threads = 256, blocks = c->sm_count * 8, iters = 1 << 14;
+    k_fp64_probe<<<blocks, threads, 0, c->stream>>>(d, 64, 0.999999, 1e-7); /* warm-up */
+    cudaEventRecord(c->ev0, c->stream);
+    k_fp64_probe<<<blocks, threads, 0, c->stream>>>(d, iters, 0.999999, 1e-7);
+    cudaEventRecord(c->ev1, c->stream);
+    e = cudaStreamSynchronize(c->stream);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    cudaFree(d);
+    if (e) return ck(c, e, "probe"), PT_ERR_CUDA;
+    *tflops = 2.0 * 8.0 * (double)iters * threads * blocks / (ms * 1e-3) / 1e12;
+    return PT_OK;
+}
+
+pt_status pt_point_solids(pt_ctx *c, int64_t n, const double *p, uint64_t *mask) {
+    if (!c || n < 0 || !mask) return PT_ERR_INVALID;
+    if (n == 0) return PT_OK;
+    cudaSetDevice(c->device);
+    std::vector<void *> tmp;
+    cudaError_t e = cudaSuccess;
+    double *dp = dupload(tmp, p, 3 * n, e);
+    unsigned long long *dm = dalloc<unsigned long long>(tmp, n, e);
+    if (e) { free_list(tmp); return ck(c, e, "point solids alloc"), PT_ERR_OOM; }
+    k_point_solids<<<grid_for(n, 128), 128, 0, c->stream>>>(c->scene, n, dp, dm);
+    e = cudaGetLastError();
+    if (!e) e = cudaMemcpyAsync(mask, dm, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaStreamSynchronize(c->stream);
+    free_list(tmp);
+    if (e) return ck(c, e, "point solids"), PT_ERR_CUDA;
+    return PT_OK;
+}
+
+} // extern "C"

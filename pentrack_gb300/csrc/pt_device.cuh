@@ -1,0 +1,127 @@
+/*
+ * pt_device.cuh -- device-side data layout and per-particle physics of the
+ * GB300 tracking engine (sm_103a).
+ *
+ * One lane tracks one particle.  The per-lane step is the reference's LOOP A
+ * body (src/tracking.cpp:71-148): an error-controlled Dormand-Prince 5(4)
+ * step, decay/tmax clipping on the dense output, chord splitting to 1 mm,
+ * the segment-mesh test with bisection to 1e-8 m, the solid-stack update and
+ * the particle's wall/bulk physics.  All state arithmetic, step control and
+ * the narrow-phase triangle test are FP64; the broad phase of the mesh query
+ * runs on conservatively rounded FP32 boxes; the tricubic field can run in
+ * FP64 or FP32 (PT_PREC_*).
+ */
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+#include "../../include/pentrack_gpu.h"
+#include "../../include/pt_constants.h"
+
+#define PT_MAX_STACK 8        /* entries of the current-solids list (the reference's vector is unbounded) */
+#define PT_MAX_COLLS 8        /* collisions of one segment kept for DoHit */
+#define PT_MAX_FIELDS 8
+#define PT_MAX_SPINTIMES 16
+#define PT_MAX_IGNORE 4       /* ignore intervals per solid */
+#define PT_MAX_SOLIDS 64
+#define PT_MAX_TRIES 500      /* odeint failed_step_checker */
+#define PT_MAX_BISECT_WORK 4096 /* collision queries per bisection (the reference recurses without a bound) */
+#define PT_MAX_LAMBERT 10000
+#define PT_MAX_SUBSEGMENTS (1 << 20) /* chord pieces of one RK step */
+#define PT_MAX_HITS_PER_SEGMENT 64   /* surfaces crossed by one chord piece */
+
+/* lane flags */
+#define PT_F_DERIV 1u   /* FSAL derivative valid */
+#define PT_F_RESET 2u   /* re-initialise the stepper before the next step */
+#define PT_F_INIT 4u    /* initialised (tau sampled, solids found, Hmax set) */
+
+struct DTri {           /* one triangle, 112 B */
+    double a[3], b[3], c[3], n[3];
+    int solid;
+    int pad;
+};
+
+struct DNode {          /* flattened BVH node in depth-first order, 32 B */
+    float lo[3], hi[3];
+    int skip;           /* next node when this subtree is skipped */
+    int leaf;           /* -1 for inner nodes, else first_triangle*8 + count */
+};
+
+struct DSolid {
+    uint32_t id;
+    int mat;
+    int n_ign;
+    int pad;
+    double ign[2 * PT_MAX_IGNORE];
+    double lo[3], hi[3]; /* box of this solid's triangles (lo > hi: none) */
+};
+
+struct DMat {
+    double fermi_real, fermi_imag, diff, spinflip, ibf, modlambert, loss;
+};
+
+struct DField {
+    int type;
+    int ncomp;          /* Hermite components per node: 3 (B) or 4 (B and V) */
+    int has_b, has_v;
+    double bscale, escale;
+    double xmax, xmin, ymax, ymin, zmax, zmin, bw;
+    int n[3];
+    int pad0;
+    const double *ax[3];
+    double a0[3], inv_h[3];
+    const double *node64;  /* [node][comp][8]: f, fx, fy, fz, fxy, fxz, fyz, fxyz */
+    const float *node32;
+    double e[3];
+    /* harmonic polynomial: Phi = sum c * x^i y^j z^k, B = grad Phi */
+    int n_mono;
+    int pad1;
+    const double *mono_c;  /* coefficient of each monomial */
+    const int *mono_e;     /* packed exponents i | j<<4 | k<<8 */
+    double offset[3];
+};
+
+struct DScene {
+    int n_tris, n_nodes, n_solids, n_fields, n_mats;
+    int pad;
+    const DTri *tris;
+    const DNode *nodes;
+    const DSolid *solids;
+    const DMat *mats;
+    DField fields[PT_MAX_FIELDS];
+    double mesh_zmax;
+};
+
+struct DSpecies {
+    int kind;
+    int pad;
+    double q, m, mu, gamma, inv_mkg, fgrav, mu_over_e, q_over_e, mc2, mg;
+};
+
+struct DRun {
+    DSpecies sp;
+    double simtime, tau, tmax, lmax, bmax;
+    double spintimes[PT_MAX_SPINTIMES];
+    int n_spintimes, flipspin, prec, steps_per_launch;
+    uint64_t seed;
+    double t_pause;
+    volatile int *cancel;   /* host-mapped cancel word (the reference's quit flag) */
+};
+
+/* particle batch in device memory (structure of arrays, component-major) */
+struct DBatch {
+    int64_t n;
+    int64_t *id;
+    double *t, *y, *dydt, *dt, *spin, *tau, *hmax, *noflip, *hstart, *t_last;
+    int32_t *stop_id, *nhit, *nstep, *nspinflip, *nsol;
+    uint32_t *flags;
+    uint64_t *stack;    /* up to 8 entries: byte k = solid index (6 bits) | ignored << 7 */
+    uint64_t *rng_n;
+    int64_t *nacc, *nrej;
+};
+
+/* device event counters (one set per launch, summed with atomics per block) */
+struct DCounters {
+    unsigned long long rk_accepted, rk_rejected, rhs_evals, field_evals, hits, bisection_levels;
+    unsigned long long bvh_nodes, tri_tests, subsegments, dense_evals, active, paused;
+    double particle_seconds;
+};

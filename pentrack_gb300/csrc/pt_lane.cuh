@@ -1,0 +1,794 @@
+/*
+ * pt_lane.cuh -- one particle's integration loop on one lane.
+ *
+ * Lane holds the particle state of one TTracker::IntegrateParticle call
+ * (src/tracking.cpp:17-173) between kernel launches plus the dense-output
+ * data of its last accepted Dormand-Prince step.  step() performs exactly one
+ * iteration of the reference's LOOP A.
+ */
+#pragma once
+#include "pt_track.cuh"
+
+namespace ptd {
+
+struct LaneCounters {
+    unsigned rk_acc, rk_rej, rhs, fields, hits, bisect, subseg, dense;
+    unsigned nodes, tris;
+};
+
+struct Lane {
+    const DScene &S;
+    const DRun &R;
+    /* persistent state */
+    int64_t id;
+    double t, y[9], dydt[9], dt;
+    uint32_t flags;
+    double spin[5];
+    double tau, hmax, noflip;
+    int stop, nhit, nstep, nspinflip, nsol;
+    uint8_t sidx[PT_MAX_STACK];
+    bool sign[PT_MAX_STACK];
+    uint64_t rn;
+    int64_t nacc, nrej;
+    /* dense output of the last accepted step */
+    double to, tn, xo[9], dxo[9], k3[9], k4[9], k5[9], k6[9];
+    /* B-only evaluation cache (position + time) */
+    double bc_p[4], bc_B[3];
+    bool bc_ok;
+    LaneCounters lc;
+
+    __device__ Lane(const DScene &s, const DRun &r) : S(s), R(r) {
+        bc_ok = false;
+        lc = LaneCounters{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    }
+
+    __device__ double u01() { return uniform(R.seed, id, rn++); }
+
+    /* ---------------- persistence ---------------- */
+    __device__ void load(const DBatch &b, int64_t i) {
+        const int64_t n = b.n;
+        id = b.id[i];
+        t = b.t[i];
+        for (int c = 0; c < 9; ++c) { y[c] = b.y[c * n + i]; dydt[c] = b.dydt[c * n + i]; }
+        dt = b.dt[i];
+        flags = b.flags[i];
+        for (int c = 0; c < 5; ++c) spin[c] = b.spin[c * n + i];
+        tau = b.tau[i]; hmax = b.hmax[i]; noflip = b.noflip[i];
+        stop = b.stop_id[i]; nhit = b.nhit[i]; nstep = b.nstep[i]; nspinflip = b.nspinflip[i]; nsol = b.nsol[i];
+        uint64_t st = b.stack[i];
+        for (int k = 0; k < PT_MAX_STACK; ++k) {
+            uint8_t v = (uint8_t)(st >> (8 * k));
+            sidx[k] = v & 63;
+            sign[k] = (v >> 7) & 1;
+        }
+        rn = b.rng_n[i];
+        nacc = b.nacc[i]; nrej = b.nrej[i];
+    }
+    __device__ void store(const DBatch &b, int64_t i) const {
+        const int64_t n = b.n;
+        b.t[i] = t;
+        for (int c = 0; c < 9; ++c) { b.y[c * n + i] = y[c]; b.dydt[c * n + i] = dydt[c]; }
+        b.dt[i] = dt;
+        b.flags[i] = flags;
+        for (int c = 0; c < 5; ++c) b.spin[c * n + i] = spin[c];
+        b.tau[i] = tau; b.hmax[i] = hmax; b.noflip[i] = noflip;
+        b.stop_id[i] = stop; b.nhit[i] = nhit; b.nstep[i] = nstep; b.nspinflip[i] = nspinflip; b.nsol[i] = nsol;
+        uint64_t st = 0;
+        for (int k = 0; k < PT_MAX_STACK; ++k) st |= (uint64_t)(sidx[k] | (sign[k] ? 128 : 0)) << (8 * k);
+        b.stack[i] = st;
+        b.rng_n[i] = rn;
+        b.nacc[i] = nacc; b.nrej[i] = nrej;
+    }
+
+    /* ---------------- fields and equation of motion ---------------- */
+    __device__ void bonly(double x, double yy, double z, double tt, double B[3]) {
+        if (bc_ok && bc_p[0] == x && bc_p[1] == yy && bc_p[2] == z && bc_p[3] == tt) {
+            B[0] = bc_B[0]; B[1] = bc_B[1]; B[2] = bc_B[2];
+            return;
+        }
+        bfield<false>(S, R.prec, x, yy, z, B, nullptr);
+        ++lc.fields;
+        bc_p[0] = x; bc_p[1] = yy; bc_p[2] = z; bc_p[3] = tt;
+        bc_B[0] = B[0]; bc_B[1] = B[1]; bc_B[2] = B[2];
+        bc_ok = true;
+    }
+
+    /* TParticle::derivs + EquationOfMotion (src/particle.cpp:96-135) */
+    __device__ void derivs(const double *yy, double tt, double *d) {
+        const DSpecies &sp = R.sp;
+        double B[3] = {0, 0, 0}, dB[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, E[3] = {0, 0, 0}, V = 0;
+        if (sp.q != 0 || (sp.mu != 0 && yy[7] != 0)) {
+            bfield<true>(S, R.prec, yy[0], yy[1], yy[2], B, dB);
+            ++lc.fields;
+        }
+        if (sp.q != 0) efield(S, R.prec, yy[0], yy[1], yy[2], V, E);
+        ++lc.rhs;
+        d[0] = yy[3]; d[1] = yy[4]; d[2] = yy[5];
+        double F0 = 0, F1 = 0, F2 = sp.fgrav;
+        if (sp.q != 0) {
+            F0 += sp.q * (E[0] + yy[4] * B[2] - yy[5] * B[1]);
+            F1 += sp.q * (E[1] + yy[5] * B[0] - yy[3] * B[2]);
+            F2 += sp.q * (E[2] + yy[3] * B[1] - yy[4] * B[0]);
+        }
+        if (sp.mu != 0 && yy[7] != 0 && (B[0] != 0 || B[1] != 0 || B[2] != 0)) {
+            double Babs = sqrt(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
+            double g0 = (B[0] * dB[0][0] + B[1] * dB[1][0] + B[2] * dB[2][0]) / Babs;
+            double g1 = (B[0] * dB[0][1] + B[1] * dB[1][1] + B[2] * dB[2][1]) / Babs;
+            double g2 = (B[0] * dB[0][2] + B[1] * dB[1][2] + B[2] * dB[2][2]) / Babs;
+            F0 += yy[7] * sp.mu * g0;
+            F1 += yy[7] * sp.mu * g1;
+            F2 += yy[7] * sp.mu * g2;
+        }
+        double v2 = yy[3] * yy[3] + yy[4] * yy[4] + yy[5] * yy[5];
+        double ig = sqrt(1 - v2 / PT_C0_SQ);
+        double vF = yy[3] * F0 + yy[4] * F1 + yy[5] * F2;
+        double s = ig * sp.inv_mkg;
+        d[3] = s * (F0 - yy[3] * vF / PT_C0_SQ);
+        d[4] = s * (F1 - yy[4] * vF / PT_C0_SQ);
+        d[5] = s * (F2 - yy[5] * vF / PT_C0_SQ);
+        d[6] = ig;
+        d[7] = 0;
+        d[8] = sqrt(v2);
+    }
+
+    /* TParticle::GetKineticEnergy (src/particle.cpp:237-251) */
+    __device__ double ekin(const double *v) const {
+        double beta2 = (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) / PT_C0_SQ;
+        double gm1;
+        if (pow(beta2, 5) < 2.220446049250313e-16)
+            gm1 = (0.5 + (3.0 / 8.0 + (5.0 / 16.0 + 35.0 / 128.0 * beta2) * beta2) * beta2) * beta2;
+        else
+            gm1 = 1.0 / sqrt(1.0 - beta2) - 1.0;
+        return R.sp.mc2 * gm1;
+    }
+    __device__ double mat_pot(const DMat &m, double pol) const { return m.fermi_real * 1e-9 - m.ibf * R.sp.mu_over_e * pol; }
+    /* TParticle::GetPotentialEnergy (src/particle.cpp:254-269) + TNeutron material term */
+    __device__ double epot(double tt, const double *yy, int solid) {
+        const DSpecies &sp = R.sp;
+        double r = 0;
+        if (sp.q != 0 || sp.mu != 0) {
+            if (sp.mu != 0) {
+                double B[3];
+                bonly(yy[0], yy[1], yy[2], tt, B);
+                r += -yy[7] * sp.mu_over_e * sqrt(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
+            }
+            if (sp.q != 0) {
+                double V, E[3];
+                efield(S, R.prec, yy[0], yy[1], yy[2], V, E);
+                r += sp.q_over_e * V;
+            }
+        }
+        r += sp.mg * yy[2];
+        if (sp.kind == PT_NEUTRON) r += mat_pot(S.mats[S.solids[solid].mat], yy[7]);
+        return r;
+    }
+
+    /* ---------------- solids ---------------- */
+    /* TTracker::GetCurrentsolid (src/tracking.cpp:367-370) */
+    __device__ int current_solid(int n, const uint8_t *ix, const bool *ig) const {
+        int best = 0;
+        for (int i = 1; i < n; ++i) {
+            bool less = ig[best] || (!ig[i] && S.solids[ix[best]].id < S.solids[ix[i]].id);
+            if (less) best = i;
+        }
+        return ix[best];
+    }
+    __device__ int cur_solid() const { return current_solid(nsol, sidx, sign); }
+
+    /* ---------------- Dormand-Prince 5(4) with odeint's controller ---------------- */
+    __device__ bool rk_step() {
+        if (!(flags & PT_F_DERIV)) {
+            derivs(y, t, dydt);
+            flags |= PT_F_DERIV;
+        }
+        const double a2 = 1.0 / 5, a3 = 3.0 / 10, a4 = 4.0 / 5, a5 = 8.0 / 9;
+        const double b21 = 1.0 / 5;
+        const double b31 = 3.0 / 40, b32 = 9.0 / 40;
+        const double b41 = 44.0 / 45, b42 = -56.0 / 15, b43 = 32.0 / 9;
+        const double b51 = 19372.0 / 6561, b52 = -25360.0 / 2187, b53 = 64448.0 / 6561, b54 = -212.0 / 729;
+        const double b61 = 9017.0 / 3168, b62 = -355.0 / 33, b63 = 46732.0 / 5247, b64 = 49.0 / 176, b65 = -5103.0 / 18656;
+        const double c1 = 35.0 / 384, c3 = 500.0 / 1113, c4 = 125.0 / 192, c5 = -2187.0 / 6784, c6 = 11.0 / 84;
+        const double dc1 = c1 - 5179.0 / 57600, dc3 = c3 - 7571.0 / 16695, dc4 = c4 - 393.0 / 640,
+                     dc5 = c5 - (-92097.0) / 339200, dc6 = c6 - 187.0 / 2100, dc7 = -1.0 / 40;
+        double k2[9], xt[9], out[9], dout[9];
+        for (int tries = 0; tries < PT_MAX_TRIES; ++tries) {
+            for (int i = 0; i < 9; ++i) xt[i] = y[i] + (dt * b21) * dydt[i];
+            derivs(xt, t + dt * a2, k2);
+            for (int i = 0; i < 9; ++i) xt[i] = y[i] + (dt * b31) * dydt[i] + (dt * b32) * k2[i];
+            derivs(xt, t + dt * a3, k3);
+            for (int i = 0; i < 9; ++i) xt[i] = y[i] + (dt * b41) * dydt[i] + (dt * b42) * k2[i] + (dt * b43) * k3[i];
+            derivs(xt, t + dt * a4, k4);
+            for (int i = 0; i < 9; ++i)
+                xt[i] = y[i] + (dt * b51) * dydt[i] + (dt * b52) * k2[i] + (dt * b53) * k3[i] + (dt * b54) * k4[i];
+            derivs(xt, t + dt * a5, k5);
+            for (int i = 0; i < 9; ++i)
+                xt[i] = y[i] + (dt * b61) * dydt[i] + (dt * b62) * k2[i] + (dt * b63) * k3[i] + (dt * b64) * k4[i] + (dt * b65) * k5[i];
+            derivs(xt, t + dt, k6);
+            for (int i = 0; i < 9; ++i)
+                out[i] = y[i] + (dt * c1) * dydt[i] + (dt * c3) * k3[i] + (dt * c4) * k4[i] + (dt * c5) * k5[i] + (dt * c6) * k6[i];
+            derivs(out, t + dt, dout);
+            double adt = fabs(dt), m = 0;
+            for (int i = 0; i < 9; ++i) {
+                double e = (dt * dc1) * dydt[i] + (dt * dc3) * k3[i] + (dt * dc4) * k4[i] + (dt * dc5) * k5[i] + (dt * dc6) * k6[i] +
+                           (dt * dc7) * dout[i];
+                double r = fabs(e) / (1e-9 + 1e-9 * (fabs(y[i]) + adt * fabs(dydt[i])));
+                m = (m < r) ? r : m;
+            }
+            if (m > 1.0) {
+                dt *= fmax(0.9 * pow(m, -1.0 / 3.0), 0.2);
+                ++nrej;
+                ++lc.rk_rej;
+                continue;
+            }
+            to = t;
+            t += dt;
+            tn = t;
+            if (m < 0.5) {
+                m = fmax(0.00032, m); /* 5^-5 */
+                dt *= 0.9 * pow(m, -1.0 / 5.0);
+            }
+            for (int i = 0; i < 9; ++i) { xo[i] = y[i]; dxo[i] = dydt[i]; y[i] = out[i]; dydt[i] = dout[i]; }
+            ++nacc;
+            ++lc.rk_acc;
+            return true;
+        }
+        return false;
+    }
+
+    /* runge_kutta_dopri5::calc_state: continuous extension on [to, tn] */
+    __device__ void dense_coef(double tt, double &h, double bt[6]) const {
+        const double b1 = 35.0 / 384, b3 = 500.0 / 1113, b4 = 125.0 / 192, b5 = -2187.0 / 6784, b6 = 11.0 / 84;
+        h = tn - to;
+        const double th = (tt - to) / h;
+        const double X1 = 5.0 * (2558722523.0 - 31403016.0 * th) / 11282082432.0;
+        const double X3 = 100.0 * (882725551.0 - 15701508.0 * th) / 32700410799.0;
+        const double X4 = 25.0 * (443332067.0 - 31403016.0 * th) / 1880347072.0;
+        const double X5 = 32805.0 * (23143187.0 - 3489224.0 * th) / 199316789632.0;
+        const double X6 = 55.0 * (29972135.0 - 7076736.0 * th) / 822651844.0;
+        const double X7 = 10.0 * (7414447.0 - 829305.0 * th) / 29380423.0;
+        const double thm1 = th - 1.0, th2 = th * th;
+        const double A = th2 * (3.0 - 2.0 * th), B = th2 * thm1, C = th2 * thm1 * thm1, D = th * thm1 * thm1;
+        bt[0] = h * (A * b1 - C * X1 + D);
+        bt[1] = h * (A * b3 + C * X3);
+        bt[2] = h * (A * b4 - C * X4);
+        bt[3] = h * (A * b5 + C * X5);
+        bt[4] = h * (A * b6 - C * X6);
+        bt[5] = h * (B + C * X7);
+    }
+    __device__ void calc_state(double tt, double *o) {
+        double h, b[6];
+        dense_coef(tt, h, b);
+        for (int i = 0; i < 9; ++i)
+            o[i] = xo[i] + b[0] * dxo[i] + b[1] * k3[i] + b[2] * k4[i] + b[3] * k5[i] + b[4] * k6[i] + b[5] * dydt[i];
+        ++lc.dense;
+    }
+    __device__ void calc_pos(double tt, double *o) {
+        double h, b[6];
+        dense_coef(tt, h, b);
+        for (int i = 0; i < 3; ++i)
+            o[i] = xo[i] + b[0] * dxo[i] + b[1] * k3[i] + b[2] * k4[i] + b[3] * k5[i] + b[4] * k6[i] + b[5] * dydt[i];
+        ++lc.dense;
+    }
+
+    /* ---------------- geometry wrappers ---------------- */
+    /* any collision on segment p->q; returns -1 on a coplanar (CGAL error) case */
+    __device__ int any_hit(const double *p, const double *q) {
+        QueryStats qs{0, 0};
+        bool cp;
+        Coll dummy;
+        int h = mesh_query<0>(S, p, q, 0, 0, &dummy, 0, nullptr, qs, cp);
+        lc.nodes += qs.nodes;
+        lc.tris += qs.tris;
+        if (h) return 1;
+        return cp ? -1 : 0;
+    }
+    __device__ int all_hits(double x1, const double *p, double x2, const double *q, Coll *c) {
+        QueryStats qs{0, 0};
+        bool cp;
+        int h = mesh_query<1>(S, p, q, x1, x2, c, PT_MAX_COLLS, nullptr, qs, cp);
+        lc.nodes += qs.nodes;
+        lc.tris += qs.tris;
+        if (cp) return -1;
+        if (h > PT_MAX_COLLS) return -2;
+        return h;
+    }
+
+    /* ---------------- RotateVector (src/globals.cpp:40-64) ---------------- */
+    __device__ static void rotate_vector(double v[3], const double n[3], const double *x) {
+        double nn = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+        double xv[3];
+        bool use_base = (x == nullptr);
+        if (!use_base) {
+            double lam = (n[0] * x[0] + n[1] * x[1] + n[2] * x[2]) / nn;
+            for (int k = 0; k < 3; ++k) xv[k] = x[k] - lam * n[k];
+            if (xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2] < 1e-30) use_base = true;
+        }
+        if (use_base) { /* CGAL Plane_3::base1() */
+            double a = fabs(n[0]), bb = fabs(n[1]), c = fabs(n[2]);
+            if (n[0] == 0) { xv[0] = 1; xv[1] = 0; xv[2] = 0; }
+            else if (n[1] == 0) { xv[0] = 0; xv[1] = 1; xv[2] = 0; }
+            else if (n[2] == 0) { xv[0] = 0; xv[1] = 0; xv[2] = 1; }
+            else if (a <= bb && a <= c) { xv[0] = 0; xv[1] = -n[2]; xv[2] = n[1]; }
+            else if (bb <= a && bb <= c) { xv[0] = -n[2]; xv[1] = 0; xv[2] = n[0]; }
+            else { xv[0] = -n[1]; xv[1] = n[0]; xv[2] = 0; }
+        }
+        double xl = sqrt(xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2]);
+        double zl = sqrt(nn);
+        double xu[3] = {xv[0] / xl, xv[1] / xl, xv[2] / xl}, zu[3] = {n[0] / zl, n[1] / zl, n[2] / zl};
+        double yu[3] = {zu[1] * xu[2] - zu[2] * xu[1], zu[2] * xu[0] - zu[0] * xu[2], zu[0] * xu[1] - zu[1] * xu[0]};
+        double r[3];
+        for (int k = 0; k < 3; ++k) r[k] = xu[k] * v[0] + yu[k] * v[1] + zu[k] * v[2];
+        v[0] = r[0]; v[1] = r[1]; v[2] = r[2];
+    }
+
+    /* ---------------- neutron wall physics (src/neutron.cpp) ---------------- */
+    __device__ void reflect(double x1, const double *y1, double &x2, double *y2, const double *n) {
+        double vn = y1[3] * n[0] + y1[4] * n[1] + y1[5] * n[2];
+        x2 = x1;
+        y2[0] = y1[0]; y2[1] = y1[1]; y2[2] = y1[2];
+        y2[3] -= 2 * vn * n[0]; y2[4] -= 2 * vn * n[1]; y2[5] -= 2 * vn * n[2];
+        y2[6] = y1[6]; y2[8] = y1[8];
+    }
+    __device__ double sincos_draw() {
+        double u = u01();
+        double ca = cos(0.0), cb = cos(PT_PI / 2.);
+        return acos(sqrt(u * (cb * cb - ca * ca) + ca * ca));
+    }
+    __device__ void reflect_lambert(double x1, const double *y1, double &x2, double *y2, const double *normal, const DMat &mat) {
+        double vn = y1[3] * normal[0] + y1[4] * normal[1] + y1[5] * normal[2];
+        double n[3] = {normal[0], normal[1], normal[2]};
+        if (vn > 0) { vn *= -1; n[0] *= -1; n[1] *= -1; n[2] *= -1; }
+        x2 = x1;
+        y2[0] = y1[0]; y2[1] = y1[1]; y2[2] = y1[2];
+        double vabs = sqrt(y1[3] * y1[3] + y1[4] * y1[4] + y1[5] * y1[5]);
+        for (int it = 0;; ++it) {
+            double phi = 2. * PT_PI * u01();
+            double th = sincos_draw();
+            y2[3] = vabs * cos(phi) * sin(th);
+            y2[4] = vabs * sin(phi) * sin(th);
+            y2[5] = vabs * cos(th);
+            if (mat.diff > 0) rotate_vector(&y2[3], n, &y1[3]);
+            else {
+                double spec[3] = {y1[3] - 2 * vn * n[0], y1[4] - 2 * vn * n[1], y1[5] - 2 * vn * n[2]};
+                rotate_vector(&y2[3], spec, &y1[3]);
+            }
+            if (y2[3] * n[0] + y2[4] * n[1] + y2[5] * n[2] > 0) break;
+            if (it > PT_MAX_LAMBERT) { stop = PT_ID_GEOMETRY_ERROR; break; }
+        }
+        y2[6] = y1[6]; y2[8] = y1[8];
+    }
+    __device__ void transmit(const double *y1, double *y2, const double *n, double Estep) {
+        double vn = y1[3] * n[0] + y1[4] * n[1] + y1[5] * n[2];
+        double En = 0.5 * R.sp.m * vn * vn;
+        double k1 = sqrt(En), k2 = sqrt(En - Estep);
+        for (int i = 0; i < 3; i++) y2[i + 3] += (k2 / k1 - 1) * (n[i] * vn);
+    }
+    __device__ void transmit_lambert(const double *y1, double *y2, const double *normal, double Estep, const DMat &mat) {
+        double vn = y1[3] * normal[0] + y1[4] * normal[1] + y1[5] * normal[2];
+        double n[3] = {normal[0], normal[1], normal[2]};
+        if (vn < 0) { vn *= -1; n[0] *= -1; n[1] *= -1; n[2] *= -1; }
+        double En = 0.5 * R.sp.m * vn * vn;
+        double k1 = sqrt(En), k2 = sqrt(En - Estep);
+        double spec[3] = {y2[3], y2[4], y2[5]};
+        for (int i = 0; i < 3; ++i) spec[i] += (k2 / k1 - 1) * n[i] * vn;
+        double vabs = sqrt(spec[0] * spec[0] + spec[1] * spec[1] + spec[2] * spec[2]);
+        for (int it = 0;; ++it) {
+            double phi = 2. * PT_PI * u01();
+            double th = sincos_draw();
+            y2[3] = vabs * cos(phi) * sin(th);
+            y2[4] = vabs * sin(phi) * sin(th);
+            y2[5] = vabs * cos(th);
+            if (mat.diff > 0) rotate_vector(&y2[3], n, &y1[3]);
+            else rotate_vector(&y2[3], spec, &y1[3]);
+            if (y2[3] * n[0] + y2[4] * n[1] + y2[5] * n[2] > 0) break;
+            if (it > PT_MAX_LAMBERT) { stop = PT_ID_GEOMETRY_ERROR; break; }
+        }
+    }
+    /* TNeutron::OnHit (src/neutron.cpp:187-264); charged species: empty */
+    __device__ void on_hit(double x1, const double *y1, double &x2, double *y2, const double *normal, int leaving, int entering) {
+        if (R.sp.kind != PT_NEUTRON) return;
+        const DMat &ml = S.mats[S.solids[leaving].mat], &me = S.mats[S.solids[entering].mat];
+        double vn = y1[3] * normal[0] + y1[4] * normal[1] + y1[5] * normal[2];
+        double En = 0.5 * R.sp.m * vn * vn;
+        const DMat &mat = vn < 0 ? me : ml;
+        if (u01() < mat.spinflip) y2[7] *= -1;
+        double Estep = mat_pot(me, y2[7]) - mat_pot(ml, y2[7]);
+        double prob = u01();
+        double k1r, k1i, k2r, k2i;
+        csqrt(En, -ml.fermi_imag * 1e-9, k1r, k1i);
+        csqrt(En - Estep, -me.fermi_imag * 1e-9, k2r, k2i);
+        double nr = k1r - k2r, ni = k1i - k2i, dr = k1r + k2r, di = k1i + k2i;
+        double reflprob = (nr * nr + ni * ni) / (dr * dr + di * di);
+        if (En > Estep) {
+            if (prob < reflprob) {
+                if (u01() < mat.diff + mat.modlambert) reflect_lambert(x1, y1, x2, y2, normal, mat);
+                else reflect(x1, y1, x2, y2, normal);
+            } else {
+                if (u01() < mat.diff + mat.modlambert) transmit_lambert(y1, y2, normal, Estep, mat);
+                else transmit(y1, y2, normal, Estep);
+            }
+        } else {
+            double absprob = 1 - reflprob + mat.loss;
+            if (prob < absprob) stop = PT_ID_ABSORBED_ON_SURFACE;
+            else {
+                if (u01() < mat.diff + mat.modlambert) reflect_lambert(x1, y1, x2, y2, normal, mat);
+                else reflect(x1, y1, x2, y2, normal);
+            }
+        }
+    }
+    /* TNeutron::OnStep (src/neutron.cpp:267-282), TProton/TElectron::OnStep */
+    __device__ void on_step(double x1, const double *y1, double &x2, double *y2, int solid) {
+        if (R.sp.kind == PT_NEUTRON) {
+            const DMat &m = S.mats[S.solids[solid].mat];
+            if (m.fermi_imag > 0) {
+                double Er = 0.5 * R.sp.m * (y1[3] * y1[3] + y1[4] * y1[4] + y1[5] * y1[5]), Ei = m.fermi_imag * 1e-9;
+                double kr, ki;
+                csqrt(2 * R.sp.m * Er, 2 * R.sp.m * Ei, kr, ki);
+                ki = ki * PT_ELE_E / PT_HBAR;
+                double dx = y2[0] - y1[0], dy = y2[1] - y1[1], dz = y2[2] - y1[2];
+                double l = sqrt(dx * dx + dy * dy + dz * dz);
+                double abspath = -log(1 - u01()) / (2 * ki);
+                if (abspath < l) {
+                    x2 = x1 + abspath / l * (x2 - x1);
+                    calc_state(x2, y2);
+                    stop = PT_ID_ABSORBED_IN_MATERIAL;
+                }
+            }
+        } else {
+            if (S.solids[solid].id > 1) {
+                x2 = x1;
+                for (int i = 0; i < 9; ++i) y2[i] = y1[i];
+                stop = PT_ID_ABSORBED_IN_MATERIAL;
+            }
+        }
+    }
+
+    /* TTracker::DoStep + TParticle::DoStep (src/tracking.cpp:268-278, src/particle.cpp:196-206) */
+    __device__ bool do_step(double x1, const double *y1, double &x2, double *y2, int solid) {
+        double x2t = x2, y2t[9];
+        for (int i = 0; i < 9; ++i) y2t[i] = y2[i];
+        on_step(x1, y1, x2, y2, solid);
+        hmax = fmax(ekin(&y2[3]) + epot(x2, y2, solid), hmax);
+        if (y2t[7] != y2[7]) nspinflip++;
+        nstep++;
+        ++lc.subseg;
+        bool same = (x2t == x2);
+        for (int i = 0; i < 9; ++i) same = same && (y2[i] == y2t[i]);
+        return !same;
+    }
+
+    /* TTracker::iterate_collision (src/tracking.cpp:228-265) without recursion:
+     * the path from the root is kept as choice bits and intervals are
+     * re-derived from the root when the search backtracks.  Returns 1 with
+     * the final bracket [xa, xb] (aorig/borig: bracket end is an input end),
+     * 0 when no sub-chord collides, -1 on a CGAL-error case. */
+    __device__ int bisect(double x1, const double *p1, double x2, const double *p2, double &xa, bool &aorig, double &xb,
+                          bool &borig) {
+        uint64_t ch0 = 0, ch1 = 0; /* choice bit per level: 1 = second half */
+        uint64_t tr0 = 0, tr1 = 0; /* second half already tried at this level */
+        int level = 0;
+        double A = x1, B = x2, pA[3] = {p1[0], p1[1], p1[2]}, pB[3] = {p2[0], p2[1], p2[2]};
+        bool Ao = true, Bo = true;
+        int work = 0;
+        auto getbit = [](uint64_t a, uint64_t b, int l) -> bool { return l < 64 ? ((a >> l) & 1) : ((b >> (l - 64)) & 1); };
+        auto setbit = [](uint64_t &a, uint64_t &b, int l, bool v) {
+            if (l < 64) { if (v) a |= (1ull << l); else a &= ~(1ull << l); }
+            else { if (v) b |= (1ull << (l - 64)); else b &= ~(1ull << (l - 64)); }
+        };
+        while (true) {
+            /* termination tests at the entry of iterate_collision */
+            double dx = pB[0] - pA[0], dy = pB[1] - pA[1], dz = pB[2] - pA[2];
+            if (dx * dx + dy * dy + dz * dz < PT_REFLECT_TOLERANCE * PT_REFLECT_TOLERANCE || B - A < 4 * (A + B) * 2.220446049250313e-16 ||
+                level >= 100) {
+                xa = A; aorig = Ao; xb = B; borig = Bo;
+                return 1;
+            }
+            ++lc.bisect;
+            double xc = A + (B - A) * 0.5, pc[3];
+            calc_pos(xc, pc);
+            if (++work > PT_MAX_BISECT_WORK) return -1;
+            int h = any_hit(pA, pc);
+            if (h < 0) return -1;
+            if (h) {
+                setbit(ch0, ch1, level, false);
+                setbit(tr0, tr1, level, false);
+                B = xc; pB[0] = pc[0]; pB[1] = pc[1]; pB[2] = pc[2]; Bo = false;
+                ++level;
+                continue;
+            }
+            h = any_hit(pc, pB);
+            if (h < 0) return -1;
+            if (h) {
+                setbit(ch0, ch1, level, true);
+                setbit(tr0, tr1, level, true);
+                A = xc; pA[0] = pc[0]; pA[1] = pc[1]; pA[2] = pc[2]; Ao = false;
+                ++level;
+                continue;
+            }
+            /* neither half collides: backtrack to the nearest level whose second half is untried */
+            bool resumed = false;
+            while (level > 0 && !resumed) {
+                --level;
+                /* rebuild the interval of `level` from the root */
+                A = x1; B = x2; Ao = Bo = true;
+                pA[0] = p1[0]; pA[1] = p1[1]; pA[2] = p1[2];
+                pB[0] = p2[0]; pB[1] = p2[1]; pB[2] = p2[2];
+                for (int l = 0; l < level; ++l) {
+                    double m = A + (B - A) * 0.5, pm[3];
+                    calc_pos(m, pm);
+                    if (getbit(ch0, ch1, l)) { A = m; pA[0] = pm[0]; pA[1] = pm[1]; pA[2] = pm[2]; Ao = false; }
+                    else { B = m; pB[0] = pm[0]; pB[1] = pm[1]; pB[2] = pm[2]; Bo = false; }
+                }
+                if (getbit(tr0, tr1, level)) continue; /* both halves of this level done */
+                double m = A + (B - A) * 0.5, pm[3];
+                calc_pos(m, pm);
+                if (++work > PT_MAX_BISECT_WORK) return -1;
+                int hh = any_hit(pm, pB);
+                if (hh < 0) return -1;
+                setbit(tr0, tr1, level, true);
+                if (hh) {
+                    setbit(ch0, ch1, level, true);
+                    A = m; pA[0] = pm[0]; pA[1] = pm[1]; pA[2] = pm[2]; Ao = false;
+                    ++level;
+                    resumed = true;
+                }
+            }
+            if (!resumed) return 0;
+        }
+    }
+
+    /* TTracker::DoHit (src/tracking.cpp:280-365) */
+    __device__ bool do_hit(double x1, const double *y1, double &x2, double *y2) {
+        bool altered = false, traversed = true;
+        Coll colls[PT_MAX_COLLS];
+        int nc = all_hits(x1, y1, x2, y2, colls);
+        if (nc <= 0) { stop = PT_ID_CGAL_ERROR; return true; }
+        int nn = nsol;
+        uint8_t ni[PT_MAX_STACK];
+        bool ng[PT_MAX_STACK];
+        for (int i = 0; i < nn; ++i) { ni[i] = sidx[i]; ng[i] = sign[i]; }
+        for (int c = 0; c < nc; ++c) {
+            const Coll &cl = colls[c];
+            int found = -1;
+            for (int i = 0; i < nn; ++i) if (S.solids[ni[i]].id == cl.id) { found = i; break; }
+            if (cl.dn < 0) {
+                if (found >= 0) {
+                    if (cl.s > 0) {
+                        if (nn >= PT_MAX_STACK) { stop = PT_ID_GEOMETRY_ERROR; return true; }
+                        ni[nn] = (uint8_t)cl.solid; ng[nn] = ng[found]; ++nn;
+                    }
+                } else {
+                    if (nn >= PT_MAX_STACK) { stop = PT_ID_GEOMETRY_ERROR; return true; }
+                    ni[nn] = (uint8_t)cl.solid; ng[nn] = cl.ign; ++nn;
+                }
+            } else if (cl.dn > 0) {
+                if (found < 0) {
+                    if (cl.s > 0) { stop = PT_ID_GEOMETRY_ERROR; return true; }
+                } else {
+                    for (int i = found; i + 1 < nn; ++i) { ni[i] = ni[i + 1]; ng[i] = ng[i + 1]; }
+                    --nn;
+                }
+            } else {
+                stop = PT_ID_GEOMETRY_ERROR;
+                return true;
+            }
+        }
+        int leaving = cur_solid();
+        int entering = 0;
+        for (int i = 0; i < nn; ++i)
+            if (!ng[i] && S.solids[ni[i]].id > S.solids[entering].id) entering = ni[i];
+        if (S.solids[leaving].id != S.solids[entering].id) {
+            int ci = -1;
+            for (int c = 0; c < nc; ++c)
+                if (colls[c].id == S.solids[leaving].id || (colls[c].id == S.solids[entering].id && !colls[c].ign)) { ci = c; break; }
+            if (ci < 0) { stop = PT_ID_GEOMETRY_ERROR; return true; }
+            double x2t = x2, y2t[9];
+            for (int i = 0; i < 9; ++i) y2t[i] = y2[i];
+            on_hit(x1, y1, x2, y2, colls[ci].n, leaving, entering);
+            if (y2t[7] != y2[7]) nspinflip++;
+            nhit++;
+            ++lc.hits;
+            bool same = (x2t == x2);
+            for (int i = 0; i < 9; ++i) same = same && (y2[i] == y2t[i]);
+            if (same) { altered = false; traversed = true; }
+            else {
+                altered = true;
+                if (x2 == x2t && y2[0] == y2t[0] && y2[1] == y2t[1] && y2[2] == y2t[2]) traversed = true;
+                else if (x2 == x1 && y2[0] == y1[0] && y2[1] == y1[1] && y2[2] == y1[2]) traversed = false;
+                else { stop = PT_ID_GEOMETRY_ERROR; return true; }
+            }
+        }
+        if (traversed) {
+            nsol = nn;
+            for (int i = 0; i < nn; ++i) { sidx[i] = ni[i]; sign[i] = ng[i]; }
+        }
+        return altered || stop != PT_ID_UNKNOWN;
+    }
+
+    /* TTracker::CheckHit (src/tracking.cpp:176-226), tail recursion as a loop */
+    __device__ bool check_hit(double x1, const double *y1in, double &x2, double *y2) {
+        double ya[9];
+        for (int i = 0; i < 9; ++i) ya[i] = y1in[i];
+        for (int pass = 0;; ++pass) {
+            if (pass >= PT_MAX_HITS_PER_SEGMENT) { stop = PT_ID_CGAL_ERROR; return true; }
+            if (!check_segment(S, ya, y2)) { stop = PT_ID_HIT_BOUNDARIES; return true; }
+            if (x2 == x1) return false;
+            int cs = cur_solid();
+            int h = any_hit(ya, y2);
+            if (h < 0) { stop = PT_ID_CGAL_ERROR; return true; }
+            if (!h) return do_step(x1, ya, x2, y2, cs);
+            double xa, xb;
+            bool ao, bo;
+            int r = bisect(x1, ya, x2, y2, xa, ao, xb, bo);
+            if (r < 0) { stop = PT_ID_CGAL_ERROR; return true; }
+            if (r == 0) return false;
+            double yc1[9], yc2[9];
+            if (ao) for (int i = 0; i < 9; ++i) yc1[i] = ya[i];
+            else calc_state(xa, yc1);
+            if (bo) for (int i = 0; i < 9; ++i) yc2[i] = y2[i];
+            else calc_state(xb, yc2);
+            double xc1 = xa, xc2 = xb;
+            if (xc1 > x1 && do_step(x1, ya, xc1, yc1, cs)) {
+                x2 = xc1;
+                for (int i = 0; i < 9; ++i) y2[i] = yc1[i];
+                return true;
+            }
+            if (do_hit(xc1, yc1, xc2, yc2)) {
+                x2 = xc2;
+                for (int i = 0; i < 9; ++i) y2[i] = yc2[i];
+                return true;
+            }
+            if (!(xc2 > x1)) { stop = PT_ID_CGAL_ERROR; return true; } /* no progress along the segment */
+            x1 = xc2;
+            for (int i = 0; i < 9; ++i) ya[i] = yc2[i];
+        }
+    }
+
+    /* TTracker::IntegrateSpin decision logic (src/tracking.cpp:373-483) */
+    __device__ double integrate_spin(double x2, const double *y2) {
+        double B1[3], B2[3];
+        bonly(xo[0], xo[1], xo[2], to, B1);
+        bonly(y2[0], y2[1], y2[2], x2, B2);
+        double Babs1 = sqrt(B1[0] * B1[0] + B1[1] * B1[1] + B1[2] * B1[2]);
+        double Babs2 = sqrt(B2[0] * B2[0] + B2[1] * B2[1] + B2[2] * B2[2]);
+        if (R.sp.gamma == 0 || Babs2 == 0) {
+            for (int k = 0; k < 5; ++k) spin[k] = 0;
+            return xo[7];
+        } else if (Babs1 == 0 && Babs2 > 0) {
+            double s = (u01() < 0.5 ? 0 : 1) * 2 - 1;
+            for (int k = 0; k < 5; ++k) spin[k] = 0;
+            return s;
+        } else if (x2 > to && (Babs1 < R.bmax || Babs2 < R.bmax)) {
+            bool i1 = false, i2 = false;
+            for (int i = 0; i + 1 < R.n_spintimes; i += 2) {
+                i1 |= (to >= R.spintimes[i] && to < R.spintimes[i + 1]);
+                i2 |= (x2 >= R.spintimes[i] && x2 < R.spintimes[i + 1]);
+            }
+            if (i1 || i2) {
+                stop = PT_ID_ODEINT_ERROR; /* Bloch integration (LOOP D) is not on the device path */
+                return xo[7];
+            } else if (spin[0] != 0 || spin[1] != 0 || spin[2] != 0) {
+                double proj = (spin[0] * B1[0] + spin[1] * B1[1] + spin[2] * B1[2]) / Babs1 /
+                              sqrt(spin[0] * spin[0] + spin[1] * spin[1] + spin[2] * spin[2]);
+                if (proj * proj >= 1) { spin[0] = 0; spin[1] = 0; }
+                else {
+                    double az = 2. * PT_PI * u01();
+                    spin[0] = sqrt(1 - proj * proj) * sin(az);
+                    spin[1] = sqrt(1 - proj * proj) * cos(az);
+                }
+                spin[2] = proj;
+                rotate_vector(spin, B2, nullptr);
+            }
+        }
+        if (Babs2 > R.bmax && (spin[0] != 0 || spin[1] != 0 || spin[2] != 0)) {
+            double proj = (spin[0] * B2[0] + spin[1] * B2[1] + spin[2] * B2[2]) / Babs2 /
+                          sqrt(spin[0] * spin[0] + spin[1] * spin[1] + spin[2] * spin[2]);
+            for (int k = 0; k < 5; ++k) spin[k] = 0;
+            return proj;
+        }
+        return xo[7];
+    }
+
+    /* first-call setup: IntegrateParticle's prologue (src/tracking.cpp:19-69)
+     * and the TParticle constructor's Hmax (src/particle.cpp:88-89) */
+    __device__ void init(QueryStats &qs) {
+        rn = 0;
+        if (R.tau > 0) tau = -log(1 - u01()) * R.tau;
+        else tau = R.tmax;
+        nsol = 1;
+        sidx[0] = 0; sign[0] = false;
+        uint64_t m = point_solids(S, y, qs);
+        for (int s = 1; s < S.n_solids; ++s)
+            if (m & (1ull << s)) {
+                if (nsol < PT_MAX_STACK) { sidx[nsol] = (uint8_t)s; sign[nsol] = solid_ignored(S.solids[s], t); ++nsol; }
+                else stop = PT_ID_GEOMETRY_ERROR;
+            }
+        for (int k = nsol; k < PT_MAX_STACK; ++k) { sidx[k] = 0; sign[k] = false; }
+        double h0 = ekin(&y[3]) + epot(t, y, cur_solid());
+        hmax = h0;
+        noflip = 1;
+        nhit = nstep = nspinflip = 0;
+        nacc = nrej = 0;
+        dt = 10. * PT_MAX_TRACK_DEVIATION / sqrt(y[3] * y[3] + y[4] * y[4] + y[5] * y[5]);
+        flags = PT_F_INIT;
+        if (stop == PT_ID_UNKNOWN && t > R.simtime) stop = PT_ID_NOT_FINISH;
+    }
+
+    /* One iteration of LOOP A (src/tracking.cpp:71-148). */
+    __device__ void step() {
+        if (flags & PT_F_RESET) flags &= ~(PT_F_DERIV | PT_F_RESET); /* stepper.initialize(y, x, dt) */
+        double x1 = t, y1[9];
+        for (int i = 0; i < 9; ++i) y1[i] = y[i];
+        if (!rk_step()) { stop = PT_ID_ODEINT_ERROR; return; }
+        bool finite = isfinite(tn);
+        for (int i = 0; i < 9; ++i) finite = finite && isfinite(y[i]);
+        if (!finite) { /* a non-finite state would never stop: report it as an integrator failure */
+            t = x1;
+            for (int i = 0; i < 9; ++i) y[i] = y1[i];
+            stop = PT_ID_ODEINT_ERROR;
+            return;
+        }
+        double x = tn, yl[9];
+        for (int i = 0; i < 9; ++i) yl[i] = y[i];
+        if (tau > 0 && yl[6] > tau) {
+            x = x1 + (x - x1) * (tau - y1[6]) / (yl[6] - y1[6]);
+            calc_state(x, yl);
+        }
+        if (x > R.simtime) {
+            x = R.simtime;
+            calc_state(x, yl);
+        }
+        bool reset = (flags & PT_F_RESET) != 0;
+        int nsub = 0;
+        while (x1 < x) {
+            if (++nsub > PT_MAX_SUBSEGMENTS) { stop = PT_ID_ODEINT_ERROR; break; }
+            double l2 = (yl[8] - y1[8]) * (yl[8] - y1[8]);
+            double d2 = (yl[0] - y1[0]) * (yl[0] - y1[0]) + (yl[1] - y1[1]) * (yl[1] - y1[1]) + (yl[2] - y1[2]) * (yl[2] - y1[2]);
+            double dev2 = 0.25 * (l2 - d2);
+            double x2 = x, y2[9];
+            for (int i = 0; i < 9; ++i) y2[i] = yl[i];
+            if (dev2 > PT_MAX_TRACK_DEVIATION * PT_MAX_TRACK_DEVIATION) {
+                x2 = x1 + (x - x1) / ceil(sqrt(dev2) / PT_MAX_TRACK_DEVIATION);
+                if (!(x2 > x1)) { stop = PT_ID_ODEINT_ERROR; break; } /* split below time resolution */
+                calc_state(x2, y2);
+            }
+            reset = check_hit(x1, y1, x2, y2);
+            if (reset) {
+                x = x2;
+                for (int i = 0; i < 9; ++i) yl[i] = y2[i];
+            }
+            x1 = x2;
+            for (int i = 0; i < 9; ++i) y1[i] = y2[i];
+        }
+        /* IntegrateSpin + polarisation bookkeeping (src/tracking.cpp:128-138) */
+        double sproj = integrate_spin(x, yl);
+        bool flipped = xo[7] != yl[7];
+        if (sproj != xo[7]) {
+            double flipprob = 0.5 * (1 - yl[7] * sproj);
+            noflip *= 1. - flipprob;
+            if (R.flipspin) {
+                double prev = yl[7];
+                yl[7] = u01() < 0.5 * (sproj + 1) ? 1 : -1;
+                if (yl[7] != prev) ++nspinflip;
+            }
+            if (R.flipspin && flipped) yl[7] *= -1;
+        } else if (flipped) {
+            for (int k = 0; k < 5; ++k) spin[k] = 0;
+        }
+        if (stop == PT_ID_UNKNOWN && yl[6] >= tau) stop = PT_ID_DECAYED;
+        else if (stop == PT_ID_UNKNOWN && (x >= R.simtime || yl[8] >= R.lmax)) stop = PT_ID_NOT_FINISH;
+        /* After a reset the stepper restarts from the loop's (x, y); otherwise it
+         * continues from its own state (so a polarisation change made by
+         * DoPolarize without a reset does not reach the stepper, as in the
+         * reference); a stopped particle reports the loop's (x, y). */
+        if (reset || stop != PT_ID_UNKNOWN) {
+            t = x;
+            for (int i = 0; i < 9; ++i) y[i] = yl[i];
+            if (reset) flags |= PT_F_RESET;
+        } else {
+            t = tn;
+        }
+    }
+};
+
+} // namespace ptd

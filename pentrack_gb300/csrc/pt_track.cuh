@@ -1,0 +1,454 @@
+/*
+ * pt_track.cuh -- per-lane tracking physics (device functions).
+ *
+ * Restates, for one particle per lane, the reference's hot loop
+ *   TTracker::IntegrateParticle   src/tracking.cpp:17-173
+ *   TTracker::CheckHit            src/tracking.cpp:176-226   (tail recursion -> loop)
+ *   TTracker::iterate_collision   src/tracking.cpp:228-265   (recursion -> path-bit DFS)
+ *   TTracker::DoStep / DoHit      src/tracking.cpp:268-365
+ *   TTracker::IntegrateSpin       src/tracking.cpp:373-483   (decision logic; LOOP D not on device)
+ *   TParticle::derivs / EquationOfMotion / energies  src/particle.cpp:96-135, 196-269
+ *   TNeutron::OnHit / OnStep / Reflect* / Transmit*  src/neutron.cpp:25-282
+ *   TProton / TElectron ::OnStep  src/proton.cpp:25-33, src/electron.cpp:25-32
+ *   TFieldManager / TFieldContainer / TabField3     src/fields.cpp:139-182, src/field.cpp:48-169,
+ *                                                   src/field_3d.cpp:487-529
+ *   TGeometry::GetCollisions / GetSolids, TTriangleMesh::Collision
+ *                                 src/geometry.cpp:139-175, src/trianglemesh.cpp:134-171
+ * and Boost.odeint's dense-output Dormand-Prince 5(4) stepper with its
+ * default error checker and step adjuster (abs = rel = 1e-9, src/tracking.cpp:63).
+ */
+#pragma once
+#include "pt_device.cuh"
+
+namespace ptd {
+
+/* ---------------------------------------------------------------- */
+/* Philox4x32-10 stream keyed by (seed, particle id)                 */
+/* ---------------------------------------------------------------- */
+__device__ __forceinline__ double uniform(uint64_t seed, int64_t id, uint64_t draw) {
+    uint32_t x0 = (uint32_t)draw, x1 = (uint32_t)(draw >> 32), x2 = (uint32_t)(uint64_t)id, x3 = (uint32_t)((uint64_t)id >> 32);
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, x0), lo0 = 0xD2511F53u * x0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, x2), lo1 = 0xCD9E8D57u * x2;
+        uint32_t y0 = hi1 ^ x1 ^ k0, y2 = hi0 ^ x3 ^ k1;
+        x0 = y0; x1 = lo1; x2 = y2; x3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    uint64_t v = ((uint64_t)x0 << 32) | x1;
+    return (double)(v >> 11) * 0x1.0p-53;
+}
+
+/* ---------------------------------------------------------------- */
+/* exact-rounding geometric predicates (no FMA contraction, so the   */
+/* signs equal the oracle's FP64 evaluation bit for bit)             */
+/* ---------------------------------------------------------------- */
+__device__ __forceinline__ double orient3d(const double *a, const double *b, const double *c, const double *d) {
+    double adx = __dsub_rn(a[0], d[0]), bdx = __dsub_rn(b[0], d[0]), cdx = __dsub_rn(c[0], d[0]);
+    double ady = __dsub_rn(a[1], d[1]), bdy = __dsub_rn(b[1], d[1]), cdy = __dsub_rn(c[1], d[1]);
+    double adz = __dsub_rn(a[2], d[2]), bdz = __dsub_rn(b[2], d[2]), cdz = __dsub_rn(c[2], d[2]);
+    double t1 = __dmul_rn(adx, __dsub_rn(__dmul_rn(bdy, cdz), __dmul_rn(bdz, cdy)));
+    double t2 = __dmul_rn(bdx, __dsub_rn(__dmul_rn(cdy, adz), __dmul_rn(cdz, ady)));
+    double t3 = __dmul_rn(cdx, __dsub_rn(__dmul_rn(ady, bdz), __dmul_rn(adz, bdy)));
+    return __dadd_rn(__dadd_rn(t1, t2), t3);
+}
+__device__ __forceinline__ bool lex_less(const double *u, const double *v) {
+    if (u[0] != v[0]) return u[0] < v[0];
+    if (u[1] != v[1]) return u[1] < v[1];
+    return u[2] < v[2];
+}
+__device__ __forceinline__ double edge_orient(const double *p, const double *q, const double *u, const double *v) {
+    if (lex_less(v, u)) return -orient3d(p, q, v, u);
+    return orient3d(p, q, u, v);
+}
+/* closed segment x closed triangle: 1 hit (parameter s), 0 none, -1 coplanar */
+__device__ __forceinline__ int seg_tri(const double *p, const double *q, const DTri &t, double &s) {
+    double dp = orient3d(t.a, t.b, t.c, p), dq = orient3d(t.a, t.b, t.c, q);
+    if ((dp > 0 && dq > 0) || (dp < 0 && dq < 0)) return 0;
+    if (dp == 0 && dq == 0) return -1;
+    double e1 = edge_orient(p, q, t.a, t.b), e2 = edge_orient(p, q, t.b, t.c), e3 = edge_orient(p, q, t.c, t.a);
+    bool neg = (e1 < 0) || (e2 < 0) || (e3 < 0), pos = (e1 > 0) || (e2 > 0) || (e3 > 0);
+    if (neg && pos) return 0;
+    s = __ddiv_rn(dp, __dsub_rn(dp, dq));
+    return 1;
+}
+
+/* principal complex square root (same formula as the oracle) */
+__device__ __forceinline__ void csqrt(double a, double b, double &re, double &im) {
+    double m = sqrt(a * a + b * b);
+    if (a >= 0) {
+        double t = sqrt((a + m) * 0.5);
+        re = t;
+        im = (t == 0) ? b : b / (2 * t);
+    } else {
+        double t = sqrt((m - a) * 0.5);
+        re = fabs(b) / (2 * t);
+        im = copysign(t, b);
+    }
+}
+
+/* ---------------------------------------------------------------- */
+/* fields                                                            */
+/* ---------------------------------------------------------------- */
+__device__ __forceinline__ bool fbox_has(const DField &f) { return f.xmin < f.xmax && f.ymin < f.ymax && f.zmin < f.zmax; }
+__device__ __forceinline__ bool fbox_in(const DField &f, double x, double y, double z) {
+    if (!fbox_has(f)) return true;
+    return x >= f.xmin && x < f.xmax && y >= f.ymin && y < f.ymax && z >= f.zmin && z < f.zmax;
+}
+__device__ __forceinline__ double smthr(double x) { return ((6 * x - 15) * x + 10) * x * x * x; }
+__device__ __forceinline__ double smthr_der(double x) { return ((30 * x - 60) * x + 30) * x * x; }
+
+/* TFieldBoundaryBox::scaleScalarFieldAtBounds (src/field.cpp:71-112) */
+__device__ void scale_at_bounds(const DField &f, double x, double y, double z, double &F, double *dF) {
+    if (!fbox_has(f) || (F == 0 && dF == nullptr) || (F == 0 && dF[0] == 0 && dF[1] == 0 && dF[2] == 0)) return;
+    if (!fbox_in(f, x, y, z)) {
+        F = 0.;
+        if (dF) dF[0] = dF[1] = dF[2] = 0.;
+    } else if (f.bw > 0) {
+        double Fscale = 1.;
+        double dFadd[3] = {0., 0., 0.};
+        double lo[3] = {(x - f.xmin) / f.bw, (y - f.ymin) / f.bw, (z - f.zmin) / f.bw};
+        double hi[3] = {(f.xmax - x) / f.bw, (f.ymax - y) / f.bw, (f.zmax - z) / f.bw};
+        for (int i = 0; i < 3; ++i) {
+            if (0 <= lo[i] && lo[i] <= 1) {
+                Fscale *= smthr(lo[i]);
+                if (dF) dFadd[i] += F * smthr_der(lo[i]) / f.bw / smthr(lo[i]);
+            } else if (0 <= hi[i] && hi[i] <= 1) {
+                Fscale *= smthr(hi[i]);
+                if (dF) dFadd[i] += -F * smthr_der(hi[i]) / f.bw / smthr(hi[i]);
+            }
+        }
+        if (Fscale != 1.) {
+            F *= Fscale;
+            if (dF)
+                for (int i = 0; i < 3; i++) dF[i] = dF[i] * Fscale + dFadd[i] * Fscale;
+        }
+    }
+}
+
+/* upper_bound cell search of TabField3::Interpolate (src/field_3d.cpp:492-501):
+ * first grid coordinate > r; outside when none or the first one. */
+__device__ __forceinline__ bool locate(const DField &f, int a, double r, int &idx, double &u, double &h) {
+    const double *ax = f.ax[a];
+    int n = f.n[a];
+    double g = (r - f.a0[a]) * f.inv_h[a];
+    int k;
+    if (!(g > -1.0)) k = 0;
+    else if (!(g < (double)n)) k = n;
+    else k = (int)floor(g) + 1;
+    while (k < n && ax[k] <= r) ++k;
+    while (k > 0 && ax[k - 1] > r) --k;
+    if (k >= n || k == 0) return false;
+    idx = k - 1;
+    h = ax[k] - ax[k - 1];
+    u = (r - ax[k - 1]) / h;
+    return true;
+}
+
+template <class T> struct Herm {
+    T w[4], dw[4];
+    /* cubic Hermite weights of (f(0), f(1), h f'(0), h f'(1)) and their
+     * derivatives with respect to the physical coordinate */
+    __device__ __forceinline__ void set(T t, T h, T invh) {
+        T t2 = t * t, t3 = t2 * t;
+        w[0] = (T)2 * t3 - (T)3 * t2 + (T)1;
+        w[1] = (T)3 * t2 - (T)2 * t3;
+        w[2] = h * (t3 - (T)2 * t2 + t);
+        w[3] = h * (t3 - t2);
+        dw[0] = ((T)6 * t2 - (T)6 * t) * invh;
+        dw[1] = ((T)6 * t - (T)6 * t2) * invh;
+        dw[2] = (T)3 * t2 - (T)4 * t + (T)1;
+        dw[3] = (T)3 * t2 - (T)2 * t;
+    }
+};
+
+/* Tricubic value (+ gradient) of `nc` components starting at `c0` in one cell
+ * from the per-node Hermite data (f, fx, fy, fz, fxy, fxz, fyz, fxyz).  The
+ * tensor-product cubic Hermite interpolant equals the reference's
+ * Lekien-Marsden polynomial (src/field_3d.cpp:367-414 + tricubic_get_coeff):
+ * both are the unique tricubic matching those 64 corner data. */
+template <class T, bool GRAD>
+__device__ void hermite_cell(const T *__restrict__ nodes, int ncomp, int c0, int nc, const int *n, int ix, int iy, int iz,
+                             const Herm<T> &U, const Herm<T> &V, const Herm<T> &W, double *F, double (*dF)[3]) {
+    const int dtab[2][2][2] = {{{0, 3}, {2, 6}}, {{1, 5}, {4, 7}}};
+    const int64_t sz = n[2], sy = (int64_t)n[1] * n[2];
+    const int64_t base = ((int64_t)ix * n[1] + iy) * n[2] + iz;
+    const int stride = ncomp * 8;
+    for (int c = c0; c < c0 + nc; ++c) {
+        T f = 0, fx = 0, fy = 0, fz = 0;
+#pragma unroll
+        for (int cx = 0; cx < 2; ++cx)
+#pragma unroll
+            for (int ax = 0; ax < 2; ++ax) {
+                const int p = cx + 2 * ax;
+                T tp = 0, typ = 0, tzp = 0;
+#pragma unroll
+                for (int cy = 0; cy < 2; ++cy) {
+                    const T *n0 = nodes + (base + cx * sy + cy * sz) * stride + c * 8;
+                    const T *n1 = n0 + stride;
+#pragma unroll
+                    for (int ay = 0; ay < 2; ++ay) {
+                        const int q = cy + 2 * ay;
+                        const int d0 = dtab[ax][ay][0], d1 = dtab[ax][ay][1];
+                        T v0 = n0[d0], v1 = n1[d0], v2 = n0[d1], v3 = n1[d1];
+                        T s = v0 * W.w[0] + v1 * W.w[1] + v2 * W.w[2] + v3 * W.w[3];
+                        tp += s * V.w[q];
+                        if (GRAD) {
+                            T sp = v0 * W.dw[0] + v1 * W.dw[1] + v2 * W.dw[2] + v3 * W.dw[3];
+                            typ += s * V.dw[q];
+                            tzp += sp * V.w[q];
+                        }
+                    }
+                }
+                f += tp * U.w[p];
+                if (GRAD) {
+                    fx += tp * U.dw[p];
+                    fy += typ * U.w[p];
+                    fz += tzp * U.w[p];
+                }
+            }
+        F[c - c0] = (double)f;
+        if (GRAD) {
+            dF[c - c0][0] = (double)fx;
+            dF[c - c0][1] = (double)fy;
+            dF[c - c0][2] = (double)fz;
+        }
+    }
+}
+
+/* TabField3 B (and gradient) of one field; outputs untouched outside the grid */
+template <bool GRAD>
+__device__ void tab3_b(const DField &f, int prec, double x, double y, double z, double B[3], double (*dB)[3]) {
+    int ix, iy, iz;
+    double u, v, w, hx, hy, hz;
+    if (!locate(f, 0, x, ix, u, hx) || !locate(f, 1, y, iy, v, hy) || !locate(f, 2, z, iz, w, hz)) return;
+    if (prec == PT_PREC_FP32 && f.node32) {
+        Herm<float> U, V, W;
+        U.set((float)u, (float)hx, (float)(1.0 / hx));
+        V.set((float)v, (float)hy, (float)(1.0 / hy));
+        W.set((float)w, (float)hz, (float)(1.0 / hz));
+        hermite_cell<float, GRAD>(f.node32, f.ncomp, 0, 3, f.n, ix, iy, iz, U, V, W, B, dB);
+    } else {
+        Herm<double> U, V, W;
+        U.set(u, hx, 1.0 / hx);
+        V.set(v, hy, 1.0 / hy);
+        W.set(w, hz, 1.0 / hz);
+        hermite_cell<double, GRAD>(f.node64, f.ncomp, 0, 3, f.n, ix, iy, iz, U, V, W, B, dB);
+    }
+}
+
+/* TabField3 potential V and E = -grad V */
+__device__ void tab3_v(const DField &f, int prec, double x, double y, double z, double &Vv, double E[3]) {
+    int ix, iy, iz;
+    double u, v, w, hx, hy, hz;
+    if (!locate(f, 0, x, ix, u, hx) || !locate(f, 1, y, iy, v, hy) || !locate(f, 2, z, iz, w, hz)) return;
+    double F[1], dF[1][3];
+    if (prec == PT_PREC_FP32 && f.node32) {
+        Herm<float> U, V, W;
+        U.set((float)u, (float)hx, (float)(1.0 / hx));
+        V.set((float)v, (float)hy, (float)(1.0 / hy));
+        W.set((float)w, (float)hz, (float)(1.0 / hz));
+        hermite_cell<float, true>(f.node32, f.ncomp, 3, 1, f.n, ix, iy, iz, U, V, W, F, dF);
+    } else {
+        Herm<double> U, V, W;
+        U.set(u, hx, 1.0 / hx);
+        V.set(v, hy, 1.0 / hy);
+        W.set(w, hz, 1.0 / hz);
+        hermite_cell<double, true>(f.node64, f.ncomp, 3, 1, f.n, ix, iy, iz, U, V, W, F, dF);
+    }
+    Vv = F[0];
+    E[0] = -dF[0][0];
+    E[1] = -dF[0][1];
+    E[2] = -dF[0][2];
+}
+
+/* harmonic expansion: B = grad Phi of a polynomial Phi (offset applied) */
+template <bool GRAD>
+__device__ void harmonic_b(const DField &f, double x, double y, double z, double B[3], double (*dB)[3]) {
+    x += f.offset[0];
+    y += f.offset[1];
+    z += f.offset[2];
+    double px[8], py[8], pz[8];
+    px[0] = py[0] = pz[0] = 1.0;
+    for (int i = 1; i < 8; ++i) { px[i] = px[i - 1] * x; py[i] = py[i - 1] * y; pz[i] = pz[i - 1] * z; }
+    for (int m = 0; m < f.n_mono; ++m) {
+        double c = f.mono_c[m];
+        int e = f.mono_e[m], i = e & 15, j = (e >> 4) & 15, k = (e >> 8) & 15;
+        if (i > 0) B[0] += c * i * px[i - 1] * py[j] * pz[k];
+        if (j > 0) B[1] += c * j * px[i] * py[j - 1] * pz[k];
+        if (k > 0) B[2] += c * k * px[i] * py[j] * pz[k - 1];
+        if (GRAD) {
+            if (i > 1) dB[0][0] += c * i * (i - 1) * px[i - 2] * py[j] * pz[k];
+            if (j > 1) dB[1][1] += c * j * (j - 1) * px[i] * py[j - 2] * pz[k];
+            if (k > 1) dB[2][2] += c * k * (k - 1) * px[i] * py[j] * pz[k - 2];
+            if (i > 0 && j > 0) { double h = c * i * j * px[i - 1] * py[j - 1] * pz[k]; dB[0][1] += h; dB[1][0] += h; }
+            if (i > 0 && k > 0) { double h = c * i * k * px[i - 1] * py[j] * pz[k - 1]; dB[0][2] += h; dB[2][0] += h; }
+            if (j > 0 && k > 0) { double h = c * j * k * px[i] * py[j - 1] * pz[k - 1]; dB[1][2] += h; dB[2][1] += h; }
+        }
+    }
+}
+
+/* TFieldManager::BField (src/fields.cpp:139-164) over TFieldContainer::BField (src/field.cpp:139-155) */
+template <bool GRAD>
+__device__ void bfield(const DScene &S, int prec, double x, double y, double z, double B[3], double (*dB)[3]) {
+    B[0] = B[1] = B[2] = 0;
+    if (GRAD)
+        for (int i = 0; i < 3; ++i) dB[i][0] = dB[i][1] = dB[i][2] = 0;
+    for (int fi = 0; fi < S.n_fields; ++fi) {
+        const DField &f = S.fields[fi];
+        if (!f.has_b) continue;
+        if (!fbox_in(f, x, y, z) || f.bscale == 0.) continue;
+        double Bt[3] = {0, 0, 0}, dBt[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        if (f.type == PT_FIELD_TAB3D) tab3_b<GRAD>(f, prec, x, y, z, Bt, dBt);
+        else if (f.type == PT_FIELD_HARMONIC) harmonic_b<GRAD>(f, x, y, z, Bt, dBt);
+        for (int i = 0; i < 3; ++i) {
+            Bt[i] *= f.bscale;
+            if (GRAD) for (int j = 0; j < 3; ++j) dBt[i][j] *= f.bscale;
+        }
+        for (int i = 0; i < 3; ++i) scale_at_bounds(f, x, y, z, Bt[i], GRAD ? dBt[i] : nullptr);
+        for (int i = 0; i < 3; ++i) {
+            B[i] += Bt[i];
+            if (GRAD) for (int j = 0; j < 3; ++j) dB[i][j] += dBt[i][j];
+        }
+    }
+}
+
+/* TFieldManager::EField (src/fields.cpp:167-182) */
+__device__ void efield(const DScene &S, int prec, double x, double y, double z, double &V, double E[3]) {
+    V = 0;
+    E[0] = E[1] = E[2] = 0;
+    for (int fi = 0; fi < S.n_fields; ++fi) {
+        const DField &f = S.fields[fi];
+        if (!f.has_v) continue;
+        if (!fbox_in(f, x, y, z) || f.escale == 0.) continue;
+        double Vt = 0, Et[3] = {0, 0, 0};
+        if (f.type == PT_FIELD_UNIFORM_E) {
+            Et[0] = f.e[0]; Et[1] = f.e[1]; Et[2] = f.e[2];
+            Vt = Et[2] * z;
+        } else if (f.type == PT_FIELD_TAB3D) {
+            tab3_v(f, prec, x, y, z, Vt, Et);
+        }
+        Vt *= f.escale;
+        for (int i = 0; i < 3; ++i) Et[i] *= f.escale;
+        scale_at_bounds(f, x, y, z, Vt, Et);
+        V += Vt;
+        for (int i = 0; i < 3; ++i) E[i] += Et[i];
+    }
+}
+
+/* ---------------------------------------------------------------- */
+/* geometry queries                                                  */
+/* ---------------------------------------------------------------- */
+struct Coll {
+    double s, n[3], dn;
+    int solid;
+    uint32_t id;
+    bool ign;
+};
+
+__device__ __forceinline__ bool solid_ignored(const DSolid &s, double t) {
+    for (int i = 0; i < s.n_ign; ++i)
+        if (t >= s.ign[2 * i] && t < s.ign[2 * i + 1]) return true;
+    return false;
+}
+
+__device__ __forceinline__ bool seg_box(const double *p, const double *q, const double *lo, const double *hi) {
+    double t0 = 0, t1 = 1;
+    for (int k = 0; k < 3; ++k) {
+        double d = q[k] - p[k];
+        if (d == 0) {
+            if (p[k] < lo[k] || p[k] > hi[k]) return false;
+            continue;
+        }
+        double ta = __ddiv_rn(__dsub_rn(lo[k], p[k]), d), tb = __ddiv_rn(__dsub_rn(hi[k], p[k]), d);
+        if (ta > tb) { double tt = ta; ta = tb; tb = tt; }
+        t0 = fmax(t0, ta);
+        t1 = fmin(t1, tb);
+        if (t0 > t1) return false;
+    }
+    return true;
+}
+
+/* TGeometry::CheckSegment (include/geometry.h:104-106) */
+__device__ bool check_segment(const DScene &S, const double *p, const double *q) {
+    for (int s = 1; s < S.n_solids; ++s) {
+        const DSolid &so = S.solids[s];
+        if (so.lo[0] > so.hi[0]) continue;
+        if (seg_box(p, q, so.lo, so.hi)) return true;
+    }
+    return false;
+}
+
+struct QueryStats { unsigned nodes, tris; };
+
+/* Stackless traversal of the depth-first BVH with FP32 boxes rounded outward;
+ * the segment box is rounded outward too, so no triangle the FP64 test would
+ * hit is ever skipped.  mode 0: stop at the first hit; mode 1: collect all
+ * (sorted by s, then solid ID descending); mode 2: ray parity mask. */
+template <int MODE>
+__device__ int mesh_query(const DScene &S, const double *p, const double *q, double x1, double x2, Coll *out, int maxc,
+                          uint64_t *mask, QueryStats &qs, bool &coplanar) {
+    float lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) {
+        double a = fmin(p[k], q[k]), b = fmax(p[k], q[k]);
+        lo[k] = __double2float_rd(a);
+        hi[k] = __double2float_ru(b);
+    }
+    int nh = 0;
+    coplanar = false;
+    int i = 0;
+    const int nn = S.n_nodes;
+    while (i < nn) {
+        const DNode nd = S.nodes[i];
+        ++qs.nodes;
+        bool ov = !(nd.lo[0] > hi[0] || nd.hi[0] < lo[0] || nd.lo[1] > hi[1] || nd.hi[1] < lo[1] || nd.lo[2] > hi[2] ||
+                    nd.hi[2] < lo[2]);
+        if (!ov) { i = nd.skip; continue; }
+        if (nd.leaf < 0) { ++i; continue; }
+        int first = nd.leaf >> 3, cnt = nd.leaf & 7;
+        for (int j = first; j < first + cnt; ++j) {
+            const DTri &t = S.tris[j];
+            ++qs.tris;
+            double s;
+            int r = seg_tri(p, q, t, s);
+            if (r < 0) {
+                if (MODE != 2) coplanar = true;
+                continue;
+            }
+            if (r == 0) continue;
+            if (MODE == 0) return 1;
+            if (MODE == 2) { *mask ^= (1ull << t.solid); continue; }
+            Coll c;
+            c.s = s;
+            c.n[0] = t.n[0]; c.n[1] = t.n[1]; c.n[2] = t.n[2];
+            c.solid = t.solid;
+            c.id = S.solids[t.solid].id;
+            c.dn = (q[0] - p[0]) * t.n[0] + (q[1] - p[1]) * t.n[1] + (q[2] - p[2]) * t.n[2];
+            c.ign = solid_ignored(S.solids[t.solid], x1 + (x2 - x1) * s);
+            if (nh < maxc) {
+                /* insertion sort: ascending s, descending ID on ties (src/trianglemesh.cpp:151-161) */
+                int k = nh;
+                while (k > 0 && (out[k - 1].s > c.s || (out[k - 1].s == c.s && out[k - 1].id < c.id))) {
+                    out[k] = out[k - 1];
+                    --k;
+                }
+                out[k] = c;
+            }
+            ++nh;
+        }
+        i = nd.skip;
+    }
+    return nh;
+}
+
+/* TTriangleMesh::GetSolids (include/trianglemesh.h:181-188): +z ray parity */
+__device__ uint64_t point_solids(const DScene &S, const double *p, QueryStats &qs) {
+    double q[3] = {p[0], p[1], fmax(S.mesh_zmax, p[2]) + 1.0};
+    uint64_t mask = 0;
+    bool cp;
+    mesh_query<2>(S, p, q, 0, 0, nullptr, 0, &mask, qs, cp);
+    return mask;
+}
+
+} // namespace ptd

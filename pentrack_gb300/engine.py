@@ -1,0 +1,312 @@
+"""Python host binding of the engine's C ABI.
+
+Mirrors the reference's host-side objects for the tracking path:
+  Scene        -- what TGeometry(TConfig&) + TFieldManager(TConfig&) hold
+                  (src/geometry.cpp:93-137, src/fields.cpp:19-136)
+  Engine       -- a device context (pt_create) with IntegrateParticles, the
+                  batched form of TTracker::IntegrateParticle (include/tracking.h:46-47)
+  ParticleSet  -- the SoA start/end states the reference keeps per TParticle
+The library is loaded from this package directory; there is no CPU fallback:
+every call goes through libpentrack_gpu.so and fails loudly without it.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi as A
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+
+class EngineError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{A.STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def lib():
+    """Load the in-tree engine library (built by pentrack_gb300.build)."""
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "libpentrack_gpu.so")
+        if not os.path.exists(path):
+            raise RuntimeError(f"engine library {path} is missing: run pentrack_gb300.build.build_engine() first")
+        _LIB = C.CDLL(path)
+        A.declare(_LIB)
+    return _LIB
+
+
+def _dp(a):
+    return a.ctypes.data_as(A.c_double_p) if a is not None else None
+
+
+def _ip(a):
+    return a.ctypes.data_as(A.c_int32_p) if a is not None else None
+
+
+def _lp(a):
+    return a.ctypes.data_as(A.c_int64_p) if a is not None else None
+
+
+# ----------------------------------------------------------------------------
+class Scene:
+    """Raw scene inputs: triangles per solid, materials, solids and fields.
+
+    Solid 0 is the default solid (ID 1), as in the reference's [GEOMETRY]
+    section where ID 1 names the medium outside every STL (src/geometry.cpp:125-128).
+    """
+
+    def __init__(self):
+        self.materials = []       # list of 9-tuples (materials.in columns)
+        self.material_names = []
+        self.solids = []          # dicts: id, material, ignore (list of (t0, t1))
+        self.tri_blocks = []      # (triangles (n,9) float64, solid index)
+        self.fields = []          # dicts
+
+    # --- materials / solids -------------------------------------------------
+    def add_material(self, name, fermi_real, fermi_imag=0.0, diff_prob=0.0, spinflip_prob=0.0, rms_roughness=0.0,
+                     correl_length=0.0, internal_bfield=0.0, modified_lambert_prob=0.0, loss_per_bounce=0.0):
+        self.materials.append((fermi_real, fermi_imag, diff_prob, spinflip_prob, rms_roughness, correl_length,
+                               internal_bfield, modified_lambert_prob, loss_per_bounce))
+        self.material_names.append(name)
+        return len(self.materials) - 1
+
+    def material_index(self, name):
+        return self.material_names.index(name)
+
+    def add_solid(self, sid, material, triangles=None, ignore=()):
+        if isinstance(material, str):
+            material = self.material_index(material)
+        if not self.solids and sid != 1:
+            raise ValueError("the first solid must be the default solid with ID 1")
+        self.solids.append({"id": int(sid), "material": int(material), "ignore": list(ignore)})
+        idx = len(self.solids) - 1
+        if triangles is not None:
+            tri = np.ascontiguousarray(np.asarray(triangles, dtype=np.float64).reshape(-1, 9))
+            self.tri_blocks.append((tri, idx))
+        return idx
+
+    # --- fields -------------------------------------------------------------
+    def add_table3d(self, x, y, z, bx=None, by=None, bz=None, v=None, b_scale=1.0, e_scale=1.0, boundary_width=0.0,
+                    box=None):
+        """TabField3 on a rectilinear grid; arrays shaped (nx, ny, nz).  The
+        container box defaults to the table's extent (src/field_3d.cpp:306-309)."""
+        x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
+        f = {"type": A.FIELD_TAB3D, "x": x, "y": y, "z": z, "b_scale": b_scale, "e_scale": e_scale,
+             "boundary_width": boundary_width}
+        for k, arr in (("bx", bx), ("by", by), ("bz", bz), ("v", v)):
+            f[k] = None if arr is None else np.ascontiguousarray(arr, dtype=np.float64).reshape(-1)
+        f["box"] = box if box is not None else (x.max(), x.min(), y.max(), y.min(), z.max(), z.min())
+        self.fields.append(f)
+
+    def add_harmonic(self, coeffs, offset=(0.0, 0.0, 0.0), b_scale=1.0, boundary_width=0.0, box=(0, 0, 0, 0, 0, 0)):
+        """HarmonicExpansionBField: coeffs = [(l, m, G), ...]."""
+        l = np.array([c[0] for c in coeffs], dtype=np.int32)
+        m = np.array([c[1] for c in coeffs], dtype=np.int32)
+        g = np.array([c[2] for c in coeffs], dtype=np.float64)
+        self.fields.append({"type": A.FIELD_HARMONIC, "l": l, "m": m, "g": g, "offset": offset, "b_scale": b_scale,
+                            "e_scale": 0.0, "boundary_width": boundary_width, "box": box})
+
+    def add_uniform_e(self, ex, ey, ez, e_scale=1.0):
+        """EDMStaticEField (src/edmfields.cpp:181-187): no box, B scale 0."""
+        self.fields.append({"type": A.FIELD_UNIFORM_E, "e": (ex, ey, ez), "b_scale": 0.0, "e_scale": e_scale,
+                            "boundary_width": 0.0, "box": (0, 0, 0, 0, 0, 0)})
+
+    # --- ABI ------------------------------------------------------------------
+    def desc(self):
+        """Build a pt_scene_desc; the returned object keeps every array alive."""
+        keep = []
+        tris = [b[0] for b in self.tri_blocks]
+        sids = [np.full(len(b[0]), b[1], dtype=np.int32) for b in self.tri_blocks]
+        T = np.ascontiguousarray(np.concatenate(tris)) if tris else np.zeros((0, 9))
+        S = np.ascontiguousarray(np.concatenate(sids)) if sids else np.zeros(0, np.int32)
+        keep += [T, S]
+        mats = (A.Material * max(1, len(self.materials)))()
+        for i, m in enumerate(self.materials):
+            mats[i] = A.Material(*m)
+        sol = (A.Solid * len(self.solids))()
+        for i, s in enumerate(self.solids):
+            ig = np.ascontiguousarray(np.array(s["ignore"], dtype=np.float64).reshape(-1))
+            keep.append(ig)
+            sol[i] = A.Solid(s["id"], s["material"], len(s["ignore"]), 0, _dp(ig) if len(ig) else None)
+        flds = (A.Field * max(1, len(self.fields)))()
+        for i, f in enumerate(self.fields):
+            F = A.Field()
+            F.type = f["type"]
+            F.b_scale, F.e_scale = f["b_scale"], f["e_scale"]
+            F.xmax, F.xmin, F.ymax, F.ymin, F.zmax, F.zmin = f["box"]
+            F.boundary_width = f["boundary_width"]
+            if f["type"] == A.FIELD_TAB3D:
+                F.nx, F.ny, F.nz = len(f["x"]), len(f["y"]), len(f["z"])
+                F.x, F.y, F.z = _dp(f["x"]), _dp(f["y"]), _dp(f["z"])
+                F.bx, F.by, F.bz, F.v = (_dp(f[k]) for k in ("bx", "by", "bz", "v"))
+                keep += [f[k] for k in ("x", "y", "z", "bx", "by", "bz", "v")]
+            elif f["type"] == A.FIELD_HARMONIC:
+                F.n_coeff = len(f["l"])
+                F.l, F.m, F.g = _ip(f["l"]), _ip(f["m"]), _dp(f["g"])
+                F.offset[:] = f["offset"]
+                keep += [f["l"], f["m"], f["g"]]
+            elif f["type"] == A.FIELD_UNIFORM_E:
+                F.e[:] = f["e"]
+            flds[i] = F
+        d = A.SceneDesc(len(T), _dp(T), _ip(S), len(self.solids), len(self.materials), sol, mats, len(self.fields), 0,
+                        flds)
+        return d, (keep, mats, sol, flds)
+
+
+# ----------------------------------------------------------------------------
+class ParticleSet:
+    """SoA particle states: y is (9, n) = x, y, z, vx, vy, vz, proper time,
+    polarisation, path length (include/particle.h:21); spin is (5, n)."""
+
+    OUT_FIELDS = (("stop_id", np.int32), ("solid", np.int32), ("n_hit", np.int32), ("n_step", np.int32),
+                  ("n_spinflip", np.int32), ("h_max", np.float64), ("noflip_prob", np.float64), ("tau", np.float64),
+                  ("h_start", np.float64), ("n_accepted", np.int64), ("n_rejected", np.int64))
+
+    def __init__(self, n, id=None, t=None, y=None, spin=None):
+        self.n = int(n)
+        self.id = np.ascontiguousarray(np.arange(n, dtype=np.int64) if id is None else id, dtype=np.int64)
+        self.t = np.ascontiguousarray(np.zeros(n) if t is None else t, dtype=np.float64)
+        self.y = np.ascontiguousarray(np.zeros((9, n)) if y is None else y, dtype=np.float64)
+        self.spin = np.ascontiguousarray(np.zeros((5, n)) if spin is None else spin, dtype=np.float64)
+        for name, dt in self.OUT_FIELDS:
+            setattr(self, name, np.zeros(n, dtype=dt))
+
+    def copy(self):
+        p = ParticleSet(self.n, self.id.copy(), self.t.copy(), self.y.copy(), self.spin.copy())
+        for name, _ in self.OUT_FIELDS:
+            setattr(p, name, getattr(self, name).copy())
+        return p
+
+    def subset(self, idx):
+        p = ParticleSet(len(idx), self.id[idx], self.t[idx], self.y[:, idx], self.spin[:, idx])
+        return p
+
+    def abi(self, outputs=True):
+        P = A.Particles()
+        P.n = self.n
+        P.id, P.t, P.y, P.spin = _lp(self.id), _dp(self.t), _dp(self.y), _dp(self.spin)
+        if outputs:
+            P.stop_id, P.solid, P.n_hit, P.n_step, P.n_spinflip = (_ip(getattr(self, k)) for k in
+                                                                   ("stop_id", "solid", "n_hit", "n_step", "n_spinflip"))
+            P.h_max, P.noflip_prob, P.tau, P.h_start = (_dp(getattr(self, k)) for k in ("h_max", "noflip_prob", "tau", "h_start"))
+            P.n_accepted, P.n_rejected = _lp(self.n_accepted), _lp(self.n_rejected)
+        return P
+
+
+def run_params(species=A.NEUTRON, simtime=100.0, tau=0.0, tmax=9e99, lmax=9e99, bmax=0.0, spintimes=(), flipspin=0,
+               seed=1, mode=A.MODE_PLAIN, precision=A.PREC_FP64, steps_per_launch=0, block_size=0):
+    """pt_run_params from the reference's [GLOBAL] simtime and particle options
+    (tau, tmax, lmax, Bmax, spintimes, flipspin; src/tracking.cpp:19-60)."""
+    st = np.ascontiguousarray(np.array(spintimes, dtype=np.float64).reshape(-1))
+    p = A.RunParams()
+    p.species, p.mode, p.field_precision, p.flipspin = species, mode, precision, flipspin
+    p.simtime, p.tau, p.tmax, p.lmax, p.bmax = simtime, tau, tmax, lmax, bmax
+    p.n_spintimes = len(st)
+    p.spintimes = _dp(st) if len(st) else None
+    p.steps_per_launch = steps_per_launch
+    p.seed = seed
+    p.block_size = block_size
+    p._keep = st
+    return p
+
+
+class Engine:
+    """One device context: the scene on the GPU plus the tracking kernels."""
+
+    def __init__(self, scene, device=0):
+        L = lib()
+        self._desc, self._keep = scene.desc()
+        h = C.c_void_p()
+        st = L.pt_create(C.byref(self._desc), device, C.byref(h))
+        if st != A.PT_OK:
+            raise EngineError(st, L.pt_last_error(None).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().pt_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != A.PT_OK and st != A.PT_ERR_CANCELLED:
+            raise EngineError(st, lib().pt_last_error(self.h).decode())
+        return st
+
+    def integrate(self, params, particles):
+        """Track every particle to its stop ID (host arrays in and out)."""
+        out = particles.copy()
+        stats = A.Stats()
+        pin, pout = particles.abi(outputs=False), out.abi()
+        self._check(lib().pt_integrate(self.h, C.byref(params), C.byref(pin), C.byref(pout), C.byref(stats)))
+        return out, stats.as_dict()
+
+    def batch(self, params, particles):
+        return Batch(self, params, particles)
+
+    def field(self, xyzt, precision=A.PREC_FP64):
+        q = np.ascontiguousarray(xyzt, dtype=np.float64).reshape(-1, 4)
+        n = len(q)
+        B, dB, V, E = np.zeros((n, 3)), np.zeros((n, 3, 3)), np.zeros(n), np.zeros((n, 3))
+        self._check(lib().pt_field_eval(self.h, n, _dp(q), precision, _dp(B), _dp(dB), _dp(V), _dp(E)))
+        return B, dB, V, E
+
+    def collisions(self, segs, max_hits=8):
+        s = np.ascontiguousarray(segs, dtype=np.float64).reshape(-1, 6)
+        n = len(s)
+        cnt = np.zeros(n, np.int32)
+        ss, nn, sid, dn = np.zeros((n, max_hits)), np.zeros((n, max_hits, 3)), np.zeros((n, max_hits), np.int32), np.zeros((n, max_hits))
+        self._check(lib().pt_segment_collisions(self.h, n, _dp(s), max_hits, _ip(cnt), _dp(ss), _dp(nn), _ip(sid), _dp(dn)))
+        return cnt, ss, nn, sid, dn
+
+    def point_solids(self, pts):
+        p = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+        m = np.zeros(len(p), np.uint64)
+        self._check(lib().pt_point_solids(self.h, len(p), _dp(p), m.ctypes.data_as(A.c_uint64_p)))
+        return m
+
+    def cancel(self):
+        lib().pt_cancel(self.h)
+
+
+class Batch:
+    """Device-resident particle batch (pt_batch_*): advance in lab-time windows."""
+
+    def __init__(self, engine, params, particles):
+        self.engine = engine
+        self.n = particles.n
+        self._template = particles
+        h = C.c_void_p()
+        pin = particles.abi(outputs=False)
+        engine._check(lib().pt_batch_create(engine.h, C.byref(params), C.byref(pin), C.byref(h)))
+        self.h = h
+
+    def advance(self, t_pause=float("inf")):
+        st = A.Stats()
+        self.engine._check(lib().pt_batch_advance(self.engine.h, self.h, t_pause, C.byref(st)))
+        return st.as_dict()
+
+    def read(self):
+        out = self._template.copy()
+        p = out.abi()
+        self.engine._check(lib().pt_batch_read(self.engine.h, self.h, C.byref(p)))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().pt_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

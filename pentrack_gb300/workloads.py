@@ -1,0 +1,110 @@
+"""The benchmark workloads as synthetic scenes (seeded; no external data).
+
+cube_storage        closed 1 m cube (12 triangles) centred at the origin, gravity
+                    only, 335 neV walls, 10,000 UCN, 0-200 neV, 100 s
+field_storage       closed cylinder R = 0.2 m, z in [-0.05, 0.05] m, 256 segments
+                    (1,024 triangles), 64^3 OPERA3D-style table of the quadrupole
+                    B = (7.5 y, 7.5 x, 1e-5) T padded by one cell, 250 neV walls with
+                    5 % Lambert and 1e-4 loss per bounce, tau = 880 s, 0-250 neV,
+                    50/50 spin states, 200 s
+integration_test    the reference's test/IntegrationTest with the 3D table only:
+                    linear gradient dBz/dz = 0.5 T/m in a hollow unit cube
+"""
+import numpy as np
+
+from . import _abi as A
+from . import scenes as S
+from .engine import Scene, run_params
+
+
+def cube_storage(n=10000, seed=1001, simtime=100.0):
+    sc = Scene()
+    sc.add_material("default", 335.0)
+    sc.add_material("vacuum", 0.0)
+    sc.add_solid(1, "default")
+    sc.add_solid(2, "vacuum", S.box_mesh((-0.5, -0.5, -0.5), (0.5, 0.5, 0.5)))
+    ids = np.arange(n, dtype=np.int64)
+    pos, (E, ph, th, pol) = S.source_box(seed, ids, (-0.5, -0.5, -0.5), (0.5, 0.5, 0.5), 0.0, 200e-9, polarization=1.0)
+    parts = S.make_particles(seed, ids, pos, E, ph, th, pol)
+    params = run_params(A.NEUTRON, simtime=simtime, tau=0.0, tmax=9e99, lmax=9e99, bmax=0.1, spintimes=(0, 0), seed=seed)
+    return sc, params, parts
+
+
+def quadrupole_table(n=64, r=0.2, h=0.1, grad=7.5, b0=1e-5):
+    """Grid of n points per axis over the cylinder's box padded by one cell on
+    each side (the reference zeroes B outside a table), sampled from
+    B = (grad*y, grad*x, b0): |B_perp| = grad*r."""
+    cx = 2 * r / (n - 3)
+    cz = h / (n - 3)
+    x = -r - cx + cx * np.arange(n)
+    z = -h / 2 - cz + cz * np.arange(n)
+    X, Y, Z = np.meshgrid(x, x, z, indexing="ij")
+    return (x, x.copy(), z), (grad * Y, grad * X, np.full_like(X, b0))
+
+
+def field_storage_scene(table_n=64, nseg=256):
+    sc = Scene()
+    sc.add_material("wall", 250.0, 0.0, 0.05, 0.0, 0.0, 0.0, 0.0, 0.0, 1e-4)
+    sc.add_material("vacuum", 0.0)
+    sc.add_solid(1, "wall")
+    sc.add_solid(2, "vacuum", S.cylinder_mesh(0.2, -0.05, 0.05, nseg))
+    (x, y, z), (bx, by, bz) = quadrupole_table(table_n)
+    sc.add_table3d(x, y, z, bx, by, bz)
+    return sc
+
+
+def field_storage(n=1_000_000, seed=1002, simtime=200.0, table_n=64, engine=None, first_id=0):
+    """Scene, run parameters and initial particles.  `engine` (an Engine on the
+    same scene) supplies B at the start points for the initial spin."""
+    sc = field_storage_scene(table_n)
+    ids = np.arange(first_id, first_id + n, dtype=np.int64)
+    pos, (E, ph, th, pol) = S.source_cylinder(seed, ids, 0.0, 0.2, -0.05, 0.05, 0.0, 250e-9, polarization=0.0)
+    bf = None
+    if engine is not None:
+        def bf(p):
+            q = np.column_stack([p, np.zeros(len(p))])
+            return engine.field(q)[0]
+    parts = S.make_particles(seed, ids, pos, E, ph, th, pol, spinprojection=0.0, bfield=bf)
+    params = run_params(A.NEUTRON, simtime=simtime, tau=880.0, tmax=9e99, lmax=9e99, bmax=0.1, spintimes=(0, 0),
+                        seed=seed)
+    return sc, params, parts
+
+
+def hollow_cube_mesh():
+    """test/HollowUnitCube.STL: outer box [-0.001, 1.001]^3 and inner box [0, 1]^3
+    whose triangles face into the hollow (24 triangles)."""
+    outer = S.box_mesh((-0.001, -0.001, -0.001), (1.001, 1.001, 1.001))
+    inner = S.box_mesh((0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
+    inner = inner.reshape(-1, 3, 3)[:, [0, 2, 1], :].reshape(-1, 9)  # reversed winding
+    return np.vstack([outer, inner])
+
+
+def integration_test(n=1000, seed=7, mesh=None, table=None):
+    """test/IntegrationTest/config.in with only the OPERA3D gradient table
+    (dBz/dz = 0.5 T/m after the 5e-5 scale and cm->m conversion).  Particles
+    start at (0.1, 0.5, 0.01) with theta_v = 5 deg, E in [10, 150] neV, pol +1,
+    inside the hollow of a UCNdet-walled cube."""
+    sc = Scene()
+    sc.add_material("default", 0.0)
+    sc.add_material("UCNdet", 0.1, 1.0)
+    sc.add_solid(1, "default")
+    sc.add_solid(2, "UCNdet", hollow_cube_mesh() if mesh is None else mesh)
+    if table is None:
+        # VerticalLinearGradientField3D.tab: 6x6x6 grid 0..100 cm, BZ = 100*z[cm] Gauss units before the 5e-5 scale
+        ax = np.linspace(0.0, 1.0, 6)
+        X, Y, Z = np.meshgrid(ax, ax, ax, indexing="ij")
+        table = ((ax, ax.copy(), ax.copy()), (np.zeros_like(Z), np.zeros_like(Z), 10000.0 * Z))
+    (x, y, z), (bx, by, bz) = table
+    sc.add_table3d(x, y, z, bx, by, bz, b_scale=0.00005, e_scale=0.0)
+    ids = np.arange(n, dtype=np.int64)
+    pos, (E, ph, th, pol) = S.source_box(seed, ids, (0.1, 0.5, 0.01), (0.1, 0.5, 0.01), 10e-9, 150e-9,
+                                         theta=(5 * S.PI / 180, 5 * S.PI / 180), phi=(0.0, 0.0), polarization=1.0)
+    parts = S.make_particles(seed, ids, pos, E, ph, th, pol)
+    params = run_params(A.NEUTRON, simtime=10.0, tau=0.0, tmax=9e99, lmax=9e99, bmax=0.1, spintimes=(0, 0), seed=seed)
+    return sc, params, parts
+
+
+def integration_test_acceleration(grad=0.5):
+    """a = -g - |mu_n| dBz/dz / m_n, the analytic answer the reference's
+    showintegrationresult.cxx checks (-15.5754762729 m/s^2 for 1 T/m)."""
+    return -S.GRAV - abs(S.MU_N) * grad / (S.M_N * S.ELE_E)

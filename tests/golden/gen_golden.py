@@ -1,0 +1,75 @@
+"""Generate the golden vectors under tests/golden from the reference's own code.
+
+Run here, where the reference tree exists:  python tests/golden/gen_golden.py
+It builds oracle/_ref/libptref.so (`make -C oracle ref`), i.e. the vendored
+ALGLIB 3.15.0 and libtricubic sources of the reference compiled in place, and
+records:
+  alglib_spline.npz   spline1dgriddiffcubic(x, y) on uniform and random grids
+                      (the call TabField3::CalcDerivs makes, src/field_3d.cpp:356)
+  tricubic.npz        tricubic_get_coeff on random corner data
+                      (TabField3::PreInterpol, src/field_3d.cpp:410) and
+                      libtricubic's tricubic_eval value/derivatives at points
+  reference_fixtures.npz  the IntegrationTest geometry/table and the unit-cube
+                      STL read from the reference's test/ directory
+"""
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+
+def main():
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref"], check=True)
+    from oracle import pyoracle
+    from pentrack_gb300 import scenes
+
+    R = pyoracle.ref_lib()
+    assert R is not None
+    dp = lambda a: a.ctypes.data_as(pyoracle.A.c_double_p)  # noqa: E731
+    rng = np.random.default_rng(20191122)
+
+    xs, ys, ds, ns = [], [], [], []
+    for n in (2, 3, 4, 5, 7, 16, 64):
+        for k in range(6):
+            if k % 2 == 0:
+                x = np.linspace(-0.21, 0.21, n)
+            else:
+                x = np.sort(rng.uniform(-1.0, 1.0, n))
+                x[0] -= 0.5
+            y = rng.normal(size=n) * (10.0 ** rng.integers(-6, 2))
+            d = np.zeros(n)
+            assert R.ref_spline_derivs(n, dp(x), dp(y), dp(d)) == 0
+            xs.append(x); ys.append(y); ds.append(d); ns.append(n)
+    off = np.cumsum([0] + ns)
+    np.savez_compressed(os.path.join(HERE, "alglib_spline.npz"), n=np.array(ns), offset=off,
+                        x=np.concatenate(xs), y=np.concatenate(ys), d=np.concatenate(ds))
+
+    X = rng.normal(size=(64, 64))
+    Acoef = np.zeros((64, 64))
+    for i in range(64):
+        R.ref_tricubic_coeff(dp(np.ascontiguousarray(X[i])), dp(Acoef[i]))
+    pts = rng.uniform(0, 1, size=(64, 3))
+    ev = np.zeros((64, 4))
+    for i in range(64):
+        a = np.ascontiguousarray(Acoef[i])
+        for j, der in enumerate(((0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1))):
+            ev[i, j] = R.ref_tricubic_eval(dp(a), pts[i, 0], pts[i, 1], pts[i, 2], *der)
+    np.savez_compressed(os.path.join(HERE, "tricubic.npz"), x=X, a=Acoef, pts=pts, eval=ev)
+
+    ref = "/root/reference/test"
+    hollow = scenes.read_stl(os.path.join(ref, "HollowUnitCube.STL"))
+    cube = scenes.read_stl(os.path.join(ref, "UnitCubeCenteredOn(0,0,0).STL"))
+    axes, comps = scenes.read_opera3d(os.path.join(ref, "VerticalLinearGradientField3D.tab"), 0.01)
+    np.savez_compressed(os.path.join(HERE, "reference_fixtures.npz"), hollow=hollow, cube=cube,
+                        tab_x=axes[0], tab_y=axes[1], tab_z=axes[2], tab_bz=comps["BZ"], tab_bx=comps["BX"],
+                        tab_by=comps["BY"], tab_v=comps["V"])
+    print("golden vectors written to", HERE)
+
+
+if __name__ == "__main__":
+    main()
