@@ -197,6 +197,7 @@ typedef struct pt_stats {
     double dominant_kernel_ms; /* summed device time of the dominant kernel */
     int64_t dominant_launches;
     char dominant_kernel[48];
+    double try_ms, post_ms, slow_ms; /* batched form: device time per phase kernel */
 } pt_stats;
 
 typedef struct pt_ctx pt_ctx;

@@ -5,6 +5,7 @@
  */
 #include "pto.h"
 #include "../include/pt_constants.h"
+#include "../include/pt_detmath.h"
 
 #include <algorithm>
 #include <atomic>
@@ -530,6 +531,10 @@ Species species_of(int s) {
 
 struct OdeintError {};
 
+/* err^p of the step adjuster through the deterministic pow of pt_detmath.h
+ * (an infinite error gives 0, as the library pow does for negative p) */
+inline double det_pow(double m, double p) { return (m < 1e300) ? ptdm_pow(m, p) : 0.0; }
+
 /* Boost.odeint dense_output_runge_kutta<controlled_runge_kutta<runge_kutta_dopri5>>
  * made by make_dense_output(eps_abs, eps_rel, stepper) (src/tracking.cpp:63).
  * Restated from the published Dormand-Prince 5(4) tableau (FSAL), odeint's
@@ -563,37 +568,43 @@ template <int N> struct Dense5 {
         while (true) {
             ++tries;
             if (tries > 500) throw OdeintError();
-            for (int i = 0; i < N; ++i) xt[i] = 1.0 * x[i] + (dt * b21) * dxdt[i];
+            /* stage combinations as explicit fused multiply-add chains, term by
+             * term in tableau order (the kernels evaluate the same chains) */
+            for (int i = 0; i < N; ++i) xt[i] = std::fma(dt * b21, dxdt[i], x[i]);
             sys(xt, k2, t + dt * a2);
-            for (int i = 0; i < N; ++i) xt[i] = 1.0 * x[i] + (dt * b31) * dxdt[i] + (dt * b32) * k2[i];
+            for (int i = 0; i < N; ++i) xt[i] = std::fma(dt * b32, k2[i], std::fma(dt * b31, dxdt[i], x[i]));
             sys(xt, k3, t + dt * a3);
-            for (int i = 0; i < N; ++i) xt[i] = 1.0 * x[i] + (dt * b41) * dxdt[i] + (dt * b42) * k2[i] + (dt * b43) * k3[i];
+            for (int i = 0; i < N; ++i)
+                xt[i] = std::fma(dt * b43, k3[i], std::fma(dt * b42, k2[i], std::fma(dt * b41, dxdt[i], x[i])));
             sys(xt, k4, t + dt * a4);
             for (int i = 0; i < N; ++i)
-                xt[i] = 1.0 * x[i] + (dt * b51) * dxdt[i] + (dt * b52) * k2[i] + (dt * b53) * k3[i] + (dt * b54) * k4[i];
+                xt[i] = std::fma(dt * b54, k4[i], std::fma(dt * b53, k3[i], std::fma(dt * b52, k2[i], std::fma(dt * b51, dxdt[i], x[i]))));
             sys(xt, k5, t + dt * a5);
             for (int i = 0; i < N; ++i)
-                xt[i] = 1.0 * x[i] + (dt * b61) * dxdt[i] + (dt * b62) * k2[i] + (dt * b63) * k3[i] + (dt * b64) * k4[i] + (dt * b65) * k5[i];
+                xt[i] = std::fma(dt * b65, k5[i], std::fma(dt * b64, k4[i], std::fma(dt * b63, k3[i],
+                        std::fma(dt * b62, k2[i], std::fma(dt * b61, dxdt[i], x[i])))));
             sys(xt, k6, t + dt);
             for (int i = 0; i < N; ++i)
-                out[i] = 1.0 * x[i] + (dt * c1) * dxdt[i] + (dt * c3) * k3[i] + (dt * c4) * k4[i] + (dt * c5) * k5[i] + (dt * c6) * k6[i];
+                out[i] = std::fma(dt * c6, k6[i], std::fma(dt * c5, k5[i], std::fma(dt * c4, k4[i],
+                         std::fma(dt * c3, k3[i], std::fma(dt * c1, dxdt[i], x[i])))));
             sys(out, dout, t + dt);
             for (int i = 0; i < N; ++i)
-                err[i] = (dt * dc1) * dxdt[i] + (dt * dc3) * k3[i] + (dt * dc4) * k4[i] + (dt * dc5) * k5[i] + (dt * dc6) * k6[i] + (dt * dc7) * dout[i];
+                err[i] = std::fma(dt * dc7, dout[i], std::fma(dt * dc6, k6[i], std::fma(dt * dc5, k5[i],
+                         std::fma(dt * dc4, k4[i], std::fma(dt * dc3, k3[i], (dt * dc1) * dxdt[i])))));
             double adt = std::fabs(dt), m = 0;
             for (int i = 0; i < N; ++i) {
                 double e = std::fabs(err[i]) / (eps_abs + eps_rel * (1.0 * std::fabs(x[i]) + adt * std::fabs(dxdt[i])));
                 m = (m < e) ? e : m;
             }
             if (m > 1.0) {
-                dt *= std::max(0.9 * std::pow(m, -1.0 / 3.0), 0.2);
+                dt *= std::max(0.9 * det_pow(m, -1.0 / 3.0), 0.2);
                 ++n_rej;
                 continue;
             }
             t += dt;
             if (m < 0.5) {
-                m = std::max(std::pow(5.0, -5.0), m);
-                dt *= 0.9 * std::pow(m, -1.0 / 5.0);
+                m = std::max(0.00032, m); /* 5^-5 */
+                dt *= 0.9 * det_pow(m, -1.0 / 5.0);
             }
             for (int i = 0; i < N; ++i) { xo[i] = x[i]; dxdto[i] = dxdt[i]; x[i] = out[i]; dxdt[i] = dout[i]; }
             return;
@@ -616,7 +627,8 @@ template <int N> struct Dense5 {
         const double bt1 = A * b1 - C * X1 + D, bt3 = A * b3 + C * X3, bt4 = A * b4 - C * X4, bt5 = A * b5 + C * X5,
                      bt6 = A * b6 - C * X6, bt7 = B + C * X7;
         for (int i = 0; i < N; ++i)
-            y[i] = 1.0 * xo[i] + (h * bt1) * dxdto[i] + (h * bt3) * k3[i] + (h * bt4) * k4[i] + (h * bt5) * k5[i] + (h * bt6) * k6[i] + (h * bt7) * dxdt[i];
+            y[i] = std::fma(h * bt7, dxdt[i], std::fma(h * bt6, k6[i], std::fma(h * bt5, k5[i], std::fma(h * bt4, k4[i],
+                   std::fma(h * bt3, k3[i], std::fma(h * bt1, dxdto[i], xo[i]))))));
     }
 };
 
@@ -749,7 +761,8 @@ struct Tracker {
     double ekin(const double *v) const {
         double beta2 = (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) / PT_C0_SQ;
         double gm1;
-        if (std::pow(beta2, 5) < std::numeric_limits<double>::epsilon())
+        double b4 = beta2 * beta2;
+        if (b4 * b4 * beta2 < std::numeric_limits<double>::epsilon())
             gm1 = (0.5 + (3.0 / 8.0 + (5.0 / 16.0 + 35.0 / 128.0 * beta2) * beta2) * beta2) * beta2;
         else
             gm1 = 1.0 / std::sqrt(1.0 - beta2) - 1.0;

@@ -46,7 +46,10 @@ def build_engine(force=False, verbose=False):
     jobs = []
     for s, o in zip(srcs, objs):
         if force or _stale(o, [s] + headers):
-            jobs.append([NVCC] + ARCH + COMMON + ["-c", s, "-o", o])
+            # device code: no automatic contraction; the integrator's fused
+            # multiply-adds are explicit (identical chains in the oracle)
+            extra = ["-fmad=false"] if s.endswith(".cu") else []
+            jobs.append([NVCC] + ARCH + COMMON + extra + ["-c", s, "-o", o])
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for r in ex.map(_run, jobs):
             if verbose and r.stderr:

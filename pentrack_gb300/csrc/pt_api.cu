@@ -53,7 +53,7 @@ __device__ __forceinline__ void flush_counters(DCounters *C, const LaneCounters 
     }
 }
 
-__global__ void __launch_bounds__(128) k_init(DScene S, DRun R, DBatch b, DCounters *C) {
+__global__ void __launch_bounds__(128) k_init(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= b.n) return;
     Lane L(S, R);
@@ -65,14 +65,111 @@ __global__ void __launch_bounds__(128) k_init(DScene S, DRun R, DBatch b, DCount
     L.stop = PT_ID_UNKNOWN;
     QueryStats qs{0, 0};
     L.init(qs);
+    L.store_bc_commit(b, i);
     L.store(b, i);
     b.hstart[i] = L.hmax;
     b.t_last[i] = L.t;
 }
 
+/* append v to a work list (warp-aggregated atomic) */
+__device__ __forceinline__ void list_push(int32_t *list, int32_t *count, int32_t v) {
+    const unsigned m = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    const int rank = __popc(m & ((1u << lane) - 1));
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(m));
+    base = __shfl_sync(m, base, leader);
+    list[base + rank] = v;
+}
+
+/* active list of a batch: particles not stopped and before t_pause */
+__global__ void k_gather(const __grid_constant__ DBatch b, double t_pause, int32_t *list, int32_t *count) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.n) return;
+    if (b.stop_id[i] == PT_ID_UNKNOWN && b.t[i] < t_pause) list_push(list, count, (int32_t)i);
+}
+
+__global__ void k_zero_counts(int32_t *count, int a, int b, int c) {
+    if (threadIdx.x == 0) { count[a] = 0; count[b] = 0; count[c] = 0; }
+}
+
+/* Batched form, phase 1: exactly one Dormand-Prince try for every active
+ * particle (all lanes execute the same instruction stream). */
+__global__ void __launch_bounds__(128) k_try(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out) {
+    const int n = b.count[in];
+    const int32_t *lin = b.list[in];
+    Lane L(S, R);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = lin[k];
+        L.load_try_input(b, i);
+        int r = L.rk_try();
+        L.store_try_output(b, i, r == 1);
+        if (r == 1) {
+            uint32_t f = b.flags[i];
+            L.flags = f;
+            L.store_bc_try(b, i);
+            b.flags[i] = L.flags;
+            list_push(b.list[2], &b.count[2], i);
+        } else if (r == 0) {
+            list_push(b.list[out], &b.count[out], i);
+        } else {
+            b.stop_id[i] = PT_ID_ODEINT_ERROR;
+        }
+    }
+    flush_counters(C, L.lc, 0.0, false);
+}
+
+/* Batched form, phase 2: the common step completion (no clip, no split, no
+ * collision); other steps are queued for phase 3. */
+__global__ void __launch_bounds__(128) k_post(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out) {
+    const int n = b.count[2];
+    const int32_t *lp = b.list[2];
+    Lane L(S, R);
+    double ps = 0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = lp[k];
+        L.load(b, i);
+        L.load_dense(b, i);
+        L.load_bc(b, i);
+        const double t0 = L.t;
+        if (L.fast_post()) {
+            ps += L.t - t0;
+            L.store_bc_commit(b, i);
+            L.store(b, i);
+            if (L.stop == PT_ID_UNKNOWN && L.t < R.t_pause) list_push(b.list[out], &b.count[out], i);
+        } else {
+            list_push(b.list[3], &b.count[3], i);
+        }
+    }
+    flush_counters(C, L.lc, ps, false);
+}
+
+/* Batched form, phase 3: full post-step logic (chord split, bisection, hit
+ * physics, clipping) for the queued steps. */
+__global__ void __launch_bounds__(128) k_slow(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out) {
+    const int n = b.count[3];
+    const int32_t *ls = b.list[3];
+    Lane L(S, R);
+    double ps = 0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = ls[k];
+        L.load(b, i);
+        L.load_dense(b, i);
+        L.load_bc(b, i);
+        const double t0 = L.t;
+        L.post_step();
+        ps += L.t - t0;
+        L.store_bc_commit(b, i);
+        L.store(b, i);
+        if (L.stop == PT_ID_UNKNOWN && L.t < R.t_pause) list_push(b.list[out], &b.count[out], i);
+    }
+    flush_counters(C, L.lc, ps, false);
+}
+
 /* Plain form: every lane advances its particle by up to `steps` LOOP-A
  * iterations, then the launch ends and the host relaunches. */
-__global__ void __launch_bounds__(128) k_plain(DScene S, DRun R, DBatch b, DCounters *C, int steps) {
+__global__ void __launch_bounds__(128) k_plain(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int steps) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= b.n) return;
     if (b.stop_id[i] != PT_ID_UNKNOWN || b.t[i] >= R.t_pause) return;
@@ -100,7 +197,7 @@ __global__ void k_fp64_probe(double *out, int iters, double a, double b) {
     if (s == 1.2345) out[0] = s;
 }
 
-__global__ void k_field(DScene S, int prec, int64_t n, const double *xyzt, double *B, double *dB, double *V, double *E) {
+__global__ void k_field(const __grid_constant__ DScene S, int prec, int64_t n, const double *xyzt, double *B, double *dB, double *V, double *E) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double *q = xyzt + 4 * i;
@@ -113,7 +210,7 @@ __global__ void k_field(DScene S, int prec, int64_t n, const double *xyzt, doubl
     if (E) for (int k = 0; k < 3; ++k) E[3 * i + k] = e[k];
 }
 
-__global__ void k_collisions(DScene S, int64_t n, const double *seg, int maxh, int *count, double *s, double *nrm, int *sid,
+__global__ void k_collisions(const __grid_constant__ DScene S, int64_t n, const double *seg, int maxh, int *count, double *s, double *nrm, int *sid,
                              double *dn) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -134,7 +231,7 @@ __global__ void k_collisions(DScene S, int64_t n, const double *seg, int maxh, i
     }
 }
 
-__global__ void k_point_solids(DScene S, int64_t n, const double *p, unsigned long long *mask) {
+__global__ void k_point_solids(const __grid_constant__ DScene S, int64_t n, const double *p, unsigned long long *mask) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     QueryStats qs{0, 0};
@@ -366,6 +463,90 @@ void free_list(std::vector<void *> &l) {
 
 int grid_for(int64_t n, int block) { return (int)((n + block - 1) / block); }
 
+void add_counters(pt_stats &acc, const DCounters &k) {
+    acc.rk_accepted += k.rk_accepted; acc.rk_rejected += k.rk_rejected; acc.rhs_evals += k.rhs_evals;
+    acc.field_evals += k.field_evals; acc.hits += k.hits; acc.bisection_levels += k.bisection_levels;
+    acc.bvh_nodes += k.bvh_nodes; acc.tri_tests += k.tri_tests; acc.subsegments += k.subsegments;
+    acc.dense_evals += k.dense_evals; acc.particle_seconds += k.particle_seconds;
+}
+
+int persistent_grid(pt_ctx *c, const void *fn, int block) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, 0);
+    if (per_sm < 1) per_sm = 1;
+    return per_sm * c->sm_count;
+}
+
+/* Batched (phase-split) form: per iteration one RK try for every active
+ * particle (k_try), the common completion (k_post) and the full post-step
+ * logic for queued steps (k_slow), over work lists in device memory. */
+pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
+                          std::chrono::steady_clock::time_point w0, bool &cancelled, bool &timed_out) {
+    cudaError_t e;
+    DBatch &b = B->b;
+    const int64_t n = b.n;
+    const int block = 128;
+    const int g_try = persistent_grid(c, (const void *)k_try, block);
+    const int g_post = persistent_grid(c, (const void *)k_post, block);
+    const int g_slow = persistent_grid(c, (const void *)k_slow, block);
+    if ((e = cudaMemsetAsync(b.count, 0, 8 * sizeof(int32_t), c->stream))) return ck(c, e, "counts"), PT_ERR_CUDA;
+    k_gather<<<grid_for(n, 256), 256, 0, c->stream>>>(b, R.t_pause, b.list[0], &b.count[0]);
+    if ((e = cudaGetLastError())) return ck(c, e, "gather"), PT_ERR_CUDA;
+    cudaEvent_t ev[6];
+    for (int k = 0; k < 6; ++k) cudaEventCreate(&ev[k]);
+    double t_try = 0, t_post = 0, t_slow = 0;
+    int64_t l_try = 0;
+    int32_t *hcount = nullptr;
+    cudaHostAlloc((void **)&hcount, 8 * sizeof(int32_t), 0);
+    pt_status st = PT_OK;
+    for (int it = 0;; ++it) {
+        const int in = it & 1, out = in ^ 1;
+        if ((e = cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream))) { st = ck(c, e, "memset"), PT_ERR_CUDA; break; }
+        k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, out, 2, 3);
+        cudaEventRecord(ev[0], c->stream);
+        k_try<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, in, out);
+        cudaEventRecord(ev[1], c->stream);
+        k_post<<<g_post, block, 0, c->stream>>>(c->scene, R, b, c->counters, out);
+        cudaEventRecord(ev[2], c->stream);
+        k_slow<<<g_slow, block, 0, c->stream>>>(c->scene, R, b, c->counters, out);
+        cudaEventRecord(ev[3], c->stream);
+        if ((e = cudaGetLastError())) { st = ck(c, e, "batched launch"), PT_ERR_CUDA; break; }
+        cudaMemcpyAsync(hcount, b.count, 8 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+        cudaMemcpyAsync(c->counters_host, c->counters, sizeof(DCounters), cudaMemcpyDeviceToHost, c->stream);
+        if ((e = cudaStreamSynchronize(c->stream))) { st = ck(c, e, "batched iteration"), PT_ERR_CUDA; break; }
+        float a = 0, bb = 0, cc = 0;
+        cudaEventElapsedTime(&a, ev[0], ev[1]);
+        cudaEventElapsedTime(&bb, ev[1], ev[2]);
+        cudaEventElapsedTime(&cc, ev[2], ev[3]);
+        t_try += a; t_post += bb; t_slow += cc;
+        ++l_try;
+        acc.kernel_ms += a + bb + cc;
+        acc.launches += 3;
+        add_counters(acc, *c->counters_host);
+        acc.active = hcount[out];
+        if (*(volatile int *)c->cancel_host) { cancelled = true; break; }
+        if (hcount[out] == 0) break;
+        if (B->max_launches > 0 && 3 * (it + 1) >= B->max_launches) { timed_out = true; break; }
+        if (B->timeout_s > 0 && std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count() > B->timeout_s) {
+            timed_out = true;
+            break;
+        }
+    }
+    for (int k = 0; k < 6; ++k) cudaEventDestroy(ev[k]);
+    cudaFreeHost(hcount);
+    const char *name = "k_try";
+    double dom = t_try;
+    if (t_post > dom) { dom = t_post; name = "k_post"; }
+    if (t_slow > dom) { dom = t_slow; name = "k_slow"; }
+    acc.dominant_kernel_ms = dom;
+    acc.dominant_launches = l_try;
+    std::snprintf(acc.dominant_kernel, sizeof(acc.dominant_kernel), "%s", name);
+    acc.try_ms = t_try;
+    acc.post_ms = t_post;
+    acc.slow_ms = t_slow;
+    return st;
+}
+
 } // namespace
 
 extern "C" {
@@ -449,6 +630,7 @@ pt_status pt_batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles 
     R.n_spintimes = p->n_spintimes;
     for (int k = 0; k < p->n_spintimes; ++k) R.spintimes[k] = p->spintimes[k];
     R.flipspin = p->flipspin;
+    R.mode = p->mode;
     R.prec = p->field_precision;
     R.steps_per_launch = p->steps_per_launch > 0 ? p->steps_per_launch : 64;
     R.seed = p->seed;
@@ -463,7 +645,10 @@ pt_status pt_batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles 
     ALLOC(spin, double, 5 * n) ALLOC(tau, double, n) ALLOC(hmax, double, n) ALLOC(noflip, double, n) ALLOC(hstart, double, n)
     ALLOC(t_last, double, n) ALLOC(stop_id, int32_t, n) ALLOC(nhit, int32_t, n) ALLOC(nstep, int32_t, n)
     ALLOC(nspinflip, int32_t, n) ALLOC(nsol, int32_t, n) ALLOC(flags, uint32_t, n) ALLOC(stack, uint64_t, n)
-    ALLOC(rng_n, uint64_t, n) ALLOC(nacc, int64_t, n) ALLOC(nrej, int64_t, n)
+    ALLOC(rng_n, uint64_t, n) ALLOC(nacc, int64_t, n) ALLOC(nrej, int64_t, n) ALLOC(ntry, int32_t, n)
+    ALLOC(yn, double, 9 * n) ALLOC(dyn, double, 9 * n) ALLOC(kst, double, 36 * n) ALLOC(tn, double, n)
+    ALLOC(bc, double, 14 * n) ALLOC(count, int32_t, 8)
+    for (int k = 0; k < 4; ++k) { b.list[k] = dalloc<int32_t>(B->allocs, (size_t)n, e); if (e) { free_list(B->allocs); return ck(c, e, "batch alloc"), PT_ERR_OOM; } }
 #undef ALLOC
     if (n > 0) {
         if ((e = cudaMemcpyAsync(b.id, in->id, n * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream)) ||
@@ -506,8 +691,13 @@ pt_status pt_batch_advance(pt_ctx *c, pt_batch *B, double t_pause, pt_stats *sta
     const int block = 128;
     const int64_t n = B->b.n;
     bool cancelled = false, timed_out = false;
+    pt_status st = PT_OK;
     cudaEventRecord(c->evs0, c->stream);
-    for (int launch = 0; n > 0; ++launch) {
+    if (R.mode == PT_MODE_BATCHED && n > 0) {
+        st = advance_batched(c, B, R, acc, w0, cancelled, timed_out);
+        if (st != PT_OK) return st;
+    }
+    for (int launch = 0; n > 0 && R.mode != PT_MODE_BATCHED; ++launch) {
         if ((e = cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream))) return ck(c, e, "memset"), PT_ERR_CUDA;
         cudaEventRecord(c->ev0, c->stream);
         k_plain<<<grid_for(n, block), block, 0, c->stream>>>(c->scene, R, B->b, c->counters, steps);

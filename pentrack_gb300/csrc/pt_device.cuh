@@ -102,6 +102,7 @@ struct DRun {
     double simtime, tau, tmax, lmax, bmax;
     double spintimes[PT_MAX_SPINTIMES];
     int n_spintimes, flipspin, prec, steps_per_launch;
+    int mode, pad;
     uint64_t seed;
     double t_pause;
     volatile int *cancel;   /* host-mapped cancel word (the reference's quit flag) */
@@ -117,7 +118,17 @@ struct DBatch {
     uint64_t *stack;    /* up to 8 entries: byte k = solid index (6 bits) | ignored << 7 */
     uint64_t *rng_n;
     int64_t *nacc, *nrej;
+    int32_t *ntry;
+    /* phase-split form: result of the last accepted try and B-value caches */
+    double *yn, *dyn, *kst, *tn; /* yn, dyn: 9n; kst: k3..k6, 36n; tn: n */
+    double *bc;                  /* 2 slots x (x, y, z, t, Bx, By, Bz): 14n */
+    /* work lists of particle indices and their counts */
+    int32_t *list[4];            /* 0/1: active (ping-pong), 2: post, 3: slow */
+    int32_t *count;              /* 4 counts */
 };
+
+#define PT_F_BC0 8u   /* cache slot 0 valid */
+#define PT_F_BC1 16u  /* cache slot 1 valid */
 
 /* device event counters (one set per launch, summed with atomics per block) */
 struct DCounters {

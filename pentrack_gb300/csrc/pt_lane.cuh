@@ -8,6 +8,7 @@
  */
 #pragma once
 #include "pt_track.cuh"
+#include "../../include/pt_detmath.h"
 
 namespace ptd {
 
@@ -30,15 +31,20 @@ struct Lane {
     bool sign[PT_MAX_STACK];
     uint64_t rn;
     int64_t nacc, nrej;
-    /* dense output of the last accepted step */
-    double to, tn, xo[9], dxo[9], k3[9], k4[9], k5[9], k6[9];
-    /* B-only evaluation cache (position + time) */
-    double bc_p[4], bc_B[3];
-    bool bc_ok;
+    int ntry;           /* consecutive rejected tries of the current step */
+    /* dense output of the last accepted try: [to, tn], start state xo/dxo,
+     * stages k3..k6, end state yn with derivative dyn (FSAL) */
+    double to, tn, xo[9], dxo[9], k3[9], k4[9], k5[9], k6[9], yn[9], dyn[9];
+    /* two-slot cache of B-only field values keyed by (x, y, z, t) */
+    double bc_p[2][4], bc_B[2][3];
+    bool bc_ok[2];
+    int bc_next;
     LaneCounters lc;
 
     __device__ Lane(const DScene &s, const DRun &r) : S(s), R(r) {
-        bc_ok = false;
+        bc_ok[0] = bc_ok[1] = false;
+        bc_next = 0;
+        ntry = 0;
         lc = LaneCounters{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     }
 
@@ -63,6 +69,85 @@ struct Lane {
         }
         rn = b.rng_n[i];
         nacc = b.nacc[i]; nrej = b.nrej[i];
+        ntry = b.ntry[i];
+    }
+    /* the committed step state only (what one RK try needs) */
+    __device__ void load_try_input(const DBatch &b, int64_t i) {
+        const int64_t n = b.n;
+        t = b.t[i];
+        for (int c = 0; c < 9; ++c) { y[c] = b.y[c * n + i]; dydt[c] = b.dydt[c * n + i]; }
+        dt = b.dt[i];
+        ntry = b.ntry[i];
+        nacc = b.nacc[i]; nrej = b.nrej[i];
+    }
+    __device__ void store_try_output(const DBatch &b, int64_t i, bool accepted) const {
+        const int64_t n = b.n;
+        b.dt[i] = dt;
+        b.ntry[i] = ntry;
+        b.nacc[i] = nacc; b.nrej[i] = nrej;
+        if (accepted) {
+            for (int c = 0; c < 9; ++c) { b.yn[c * n + i] = yn[c]; b.dyn[c * n + i] = dyn[c]; }
+            for (int c = 0; c < 9; ++c) {
+                b.kst[(0 * 9 + c) * n + i] = k3[c];
+                b.kst[(1 * 9 + c) * n + i] = k4[c];
+                b.kst[(2 * 9 + c) * n + i] = k5[c];
+                b.kst[(3 * 9 + c) * n + i] = k6[c];
+            }
+            b.tn[i] = tn;
+        }
+    }
+    /* dense data of the accepted try (start = committed state) */
+    __device__ void load_dense(const DBatch &b, int64_t i) {
+        const int64_t n = b.n;
+        to = t;
+        for (int c = 0; c < 9; ++c) { xo[c] = y[c]; dxo[c] = dydt[c]; yn[c] = b.yn[c * n + i]; dyn[c] = b.dyn[c * n + i]; }
+        for (int c = 0; c < 9; ++c) {
+            k3[c] = b.kst[(0 * 9 + c) * n + i];
+            k4[c] = b.kst[(1 * 9 + c) * n + i];
+            k5[c] = b.kst[(2 * 9 + c) * n + i];
+            k6[c] = b.kst[(3 * 9 + c) * n + i];
+        }
+        tn = b.tn[i];
+    }
+    /* global B caches: slot 0 holds B at the committed point (t, y), slot 1 B
+     * at the end point of the last accepted try (tn, yn) */
+    __device__ void load_bc(const DBatch &b, int64_t i) {
+        const int64_t n = b.n;
+        bc_ok[0] = (flags & PT_F_BC0) != 0;
+        bc_ok[1] = (flags & PT_F_BC1) != 0;
+        for (int k = 0; k < 2; ++k) {
+            for (int c = 0; c < 4; ++c) bc_p[k][c] = b.bc[(k * 7 + c) * n + i];
+            for (int c = 0; c < 3; ++c) bc_B[k][c] = b.bc[(k * 7 + 4 + c) * n + i];
+        }
+        bc_next = 0;
+    }
+    __device__ int bc_find(double x, double yy, double z, double tt) const {
+        for (int k = 0; k < 2; ++k)
+            if (bc_ok[k] && bc_p[k][0] == x && bc_p[k][1] == yy && bc_p[k][2] == z && bc_p[k][3] == tt) return k;
+        return -1;
+    }
+    __device__ void bc_write(const DBatch &b, int64_t i, int slot, int k) const {
+        const int64_t n = b.n;
+        for (int c = 0; c < 4; ++c) b.bc[(slot * 7 + c) * n + i] = bc_p[k][c];
+        for (int c = 0; c < 3; ++c) b.bc[(slot * 7 + 4 + c) * n + i] = bc_B[k][c];
+    }
+    /* after a commit: keep B at the new committed point (flags stored by store()) */
+    __device__ void store_bc_commit(const DBatch &b, int64_t i) {
+        int k = bc_find(y[0], y[1], y[2], t);
+        flags &= ~(PT_F_BC0 | PT_F_BC1);
+        if (k >= 0) {
+            bc_write(b, i, 0, k);
+            flags |= PT_F_BC0;
+        }
+    }
+    /* after an accepted try: keep B at its end point (flags stored separately) */
+    __device__ void store_bc_try(const DBatch &b, int64_t i) {
+        int k = bc_find(yn[0], yn[1], yn[2], tn);
+        flags &= ~PT_F_BC1;
+        if (k >= 0) {
+            bc_write(b, i, 1, k);
+            flags |= PT_F_BC1;
+        }
     }
     __device__ void store(const DBatch &b, int64_t i) const {
         const int64_t n = b.n;
@@ -78,28 +163,38 @@ struct Lane {
         b.stack[i] = st;
         b.rng_n[i] = rn;
         b.nacc[i] = nacc; b.nrej[i] = nrej;
+        b.ntry[i] = ntry;
     }
 
     /* ---------------- fields and equation of motion ---------------- */
+    __device__ void bc_put(double x, double yy, double z, double tt, const double B[3]) {
+        int k = bc_next;
+        bc_next ^= 1;
+        bc_p[k][0] = x; bc_p[k][1] = yy; bc_p[k][2] = z; bc_p[k][3] = tt;
+        bc_B[k][0] = B[0]; bc_B[k][1] = B[1]; bc_B[k][2] = B[2];
+        bc_ok[k] = true;
+    }
     __device__ void bonly(double x, double yy, double z, double tt, double B[3]) {
-        if (bc_ok && bc_p[0] == x && bc_p[1] == yy && bc_p[2] == z && bc_p[3] == tt) {
-            B[0] = bc_B[0]; B[1] = bc_B[1]; B[2] = bc_B[2];
-            return;
-        }
+        for (int k = 0; k < 2; ++k)
+            if (bc_ok[k] && bc_p[k][0] == x && bc_p[k][1] == yy && bc_p[k][2] == z && bc_p[k][3] == tt) {
+                B[0] = bc_B[k][0]; B[1] = bc_B[k][1]; B[2] = bc_B[k][2];
+                return;
+            }
         bfield<false>(S, R.prec, x, yy, z, B, nullptr);
         ++lc.fields;
-        bc_p[0] = x; bc_p[1] = yy; bc_p[2] = z; bc_p[3] = tt;
-        bc_B[0] = B[0]; bc_B[1] = B[1]; bc_B[2] = B[2];
-        bc_ok = true;
+        bc_put(x, yy, z, tt, B);
     }
 
     /* TParticle::derivs + EquationOfMotion (src/particle.cpp:96-135) */
-    __device__ void derivs(const double *yy, double tt, double *d) {
+    __device__ void derivs(const double *yy, double tt, double *d, bool keepB = false) {
         const DSpecies &sp = R.sp;
         double B[3] = {0, 0, 0}, dB[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, E[3] = {0, 0, 0}, V = 0;
         if (sp.q != 0 || (sp.mu != 0 && yy[7] != 0)) {
             bfield<true>(S, R.prec, yy[0], yy[1], yy[2], B, dB);
             ++lc.fields;
+            /* the value part of the gradient evaluation is bit-identical to a
+             * B-only evaluation, so it can serve later B-only queries */
+            if (keepB) bc_put(yy[0], yy[1], yy[2], tt, B);
         }
         if (sp.q != 0) efield(S, R.prec, yy[0], yy[1], yy[2], V, E);
         ++lc.rhs;
@@ -135,7 +230,8 @@ struct Lane {
     __device__ double ekin(const double *v) const {
         double beta2 = (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) / PT_C0_SQ;
         double gm1;
-        if (pow(beta2, 5) < 2.220446049250313e-16)
+        double b4 = beta2 * beta2;
+        if (b4 * b4 * beta2 < 2.220446049250313e-16)
             gm1 = (0.5 + (3.0 / 8.0 + (5.0 / 16.0 + 35.0 / 128.0 * beta2) * beta2) * beta2) * beta2;
         else
             gm1 = 1.0 / sqrt(1.0 - beta2) - 1.0;
@@ -176,11 +272,12 @@ struct Lane {
     __device__ int cur_solid() const { return current_solid(nsol, sidx, sign); }
 
     /* ---------------- Dormand-Prince 5(4) with odeint's controller ---------------- */
-    __device__ bool rk_step() {
-        if (!(flags & PT_F_DERIV)) {
-            derivs(y, t, dydt);
-            flags |= PT_F_DERIV;
-        }
+    /* One try of controlled_runge_kutta::try_step on the committed state
+     * (t, y, dydt).  Returns 1 when accepted (dense data set, dt grown), 0
+     * when rejected (dt shrunk), -1 after 500 consecutive rejections (odeint's
+     * failed_step_checker).  The stage sums are explicit fused multiply-add
+     * chains in tableau order, the same chains the oracle evaluates. */
+    __device__ int rk_try() {
         const double a2 = 1.0 / 5, a3 = 3.0 / 10, a4 = 4.0 / 5, a5 = 8.0 / 9;
         const double b21 = 1.0 / 5;
         const double b31 = 3.0 / 40, b32 = 9.0 / 40;
@@ -190,49 +287,49 @@ struct Lane {
         const double c1 = 35.0 / 384, c3 = 500.0 / 1113, c4 = 125.0 / 192, c5 = -2187.0 / 6784, c6 = 11.0 / 84;
         const double dc1 = c1 - 5179.0 / 57600, dc3 = c3 - 7571.0 / 16695, dc4 = c4 - 393.0 / 640,
                      dc5 = c5 - (-92097.0) / 339200, dc6 = c6 - 187.0 / 2100, dc7 = -1.0 / 40;
-        double k2[9], xt[9], out[9], dout[9];
-        for (int tries = 0; tries < PT_MAX_TRIES; ++tries) {
-            for (int i = 0; i < 9; ++i) xt[i] = y[i] + (dt * b21) * dydt[i];
-            derivs(xt, t + dt * a2, k2);
-            for (int i = 0; i < 9; ++i) xt[i] = y[i] + (dt * b31) * dydt[i] + (dt * b32) * k2[i];
-            derivs(xt, t + dt * a3, k3);
-            for (int i = 0; i < 9; ++i) xt[i] = y[i] + (dt * b41) * dydt[i] + (dt * b42) * k2[i] + (dt * b43) * k3[i];
-            derivs(xt, t + dt * a4, k4);
-            for (int i = 0; i < 9; ++i)
-                xt[i] = y[i] + (dt * b51) * dydt[i] + (dt * b52) * k2[i] + (dt * b53) * k3[i] + (dt * b54) * k4[i];
-            derivs(xt, t + dt * a5, k5);
-            for (int i = 0; i < 9; ++i)
-                xt[i] = y[i] + (dt * b61) * dydt[i] + (dt * b62) * k2[i] + (dt * b63) * k3[i] + (dt * b64) * k4[i] + (dt * b65) * k5[i];
-            derivs(xt, t + dt, k6);
-            for (int i = 0; i < 9; ++i)
-                out[i] = y[i] + (dt * c1) * dydt[i] + (dt * c3) * k3[i] + (dt * c4) * k4[i] + (dt * c5) * k5[i] + (dt * c6) * k6[i];
-            derivs(out, t + dt, dout);
-            double adt = fabs(dt), m = 0;
-            for (int i = 0; i < 9; ++i) {
-                double e = (dt * dc1) * dydt[i] + (dt * dc3) * k3[i] + (dt * dc4) * k4[i] + (dt * dc5) * k5[i] + (dt * dc6) * k6[i] +
-                           (dt * dc7) * dout[i];
-                double r = fabs(e) / (1e-9 + 1e-9 * (fabs(y[i]) + adt * fabs(dydt[i])));
-                m = (m < r) ? r : m;
-            }
-            if (m > 1.0) {
-                dt *= fmax(0.9 * pow(m, -1.0 / 3.0), 0.2);
-                ++nrej;
-                ++lc.rk_rej;
-                continue;
-            }
-            to = t;
-            t += dt;
-            tn = t;
-            if (m < 0.5) {
-                m = fmax(0.00032, m); /* 5^-5 */
-                dt *= 0.9 * pow(m, -1.0 / 5.0);
-            }
-            for (int i = 0; i < 9; ++i) { xo[i] = y[i]; dxo[i] = dydt[i]; y[i] = out[i]; dydt[i] = dout[i]; }
-            ++nacc;
-            ++lc.rk_acc;
-            return true;
+        if (ntry >= PT_MAX_TRIES) return -1;
+        ++ntry;
+        double k2[9], xt[9];
+        const double h = dt;
+        for (int i = 0; i < 9; ++i) xt[i] = fma(h * b21, dydt[i], y[i]);
+        derivs(xt, t + h * a2, k2);
+        for (int i = 0; i < 9; ++i) xt[i] = fma(h * b32, k2[i], fma(h * b31, dydt[i], y[i]));
+        derivs(xt, t + h * a3, k3);
+        for (int i = 0; i < 9; ++i) xt[i] = fma(h * b43, k3[i], fma(h * b42, k2[i], fma(h * b41, dydt[i], y[i])));
+        derivs(xt, t + h * a4, k4);
+        for (int i = 0; i < 9; ++i)
+            xt[i] = fma(h * b54, k4[i], fma(h * b53, k3[i], fma(h * b52, k2[i], fma(h * b51, dydt[i], y[i]))));
+        derivs(xt, t + h * a5, k5);
+        for (int i = 0; i < 9; ++i)
+            xt[i] = fma(h * b65, k5[i], fma(h * b64, k4[i], fma(h * b63, k3[i], fma(h * b62, k2[i], fma(h * b61, dydt[i], y[i])))));
+        derivs(xt, t + h, k6);
+        for (int i = 0; i < 9; ++i)
+            yn[i] = fma(h * c6, k6[i], fma(h * c5, k5[i], fma(h * c4, k4[i], fma(h * c3, k3[i], fma(h * c1, dydt[i], y[i])))));
+        derivs(yn, t + h, dyn, true);
+        const double adt = fabs(h);
+        double m = 0;
+        for (int i = 0; i < 9; ++i) {
+            double e = fma(h * dc7, dyn[i], fma(h * dc6, k6[i], fma(h * dc5, k5[i], fma(h * dc4, k4[i], fma(h * dc3, k3[i], (h * dc1) * dydt[i])))));
+            double r = fabs(e) / (1e-9 + 1e-9 * (fabs(y[i]) + adt * fabs(dydt[i])));
+            m = (m < r) ? r : m;
         }
-        return false;
+        if (m > 1.0) {
+            dt *= fmax(0.9 * (m < 1e300 ? ptdm_pow(m, -1.0 / 3.0) : 0.0), 0.2);
+            ++nrej;
+            ++lc.rk_rej;
+            return 0;
+        }
+        to = t;
+        tn = t + h;
+        if (m < 0.5) {
+            m = fmax(0.00032, m); /* 5^-5 */
+            dt *= 0.9 * ptdm_pow(m, -1.0 / 5.0);
+        }
+        for (int i = 0; i < 9; ++i) { xo[i] = y[i]; dxo[i] = dydt[i]; }
+        ntry = 0;
+        ++nacc;
+        ++lc.rk_acc;
+        return 1;
     }
 
     /* runge_kutta_dopri5::calc_state: continuous extension on [to, tn] */
@@ -259,14 +356,14 @@ struct Lane {
         double h, b[6];
         dense_coef(tt, h, b);
         for (int i = 0; i < 9; ++i)
-            o[i] = xo[i] + b[0] * dxo[i] + b[1] * k3[i] + b[2] * k4[i] + b[3] * k5[i] + b[4] * k6[i] + b[5] * dydt[i];
+            o[i] = fma(b[5], dyn[i], fma(b[4], k6[i], fma(b[3], k5[i], fma(b[2], k4[i], fma(b[1], k3[i], fma(b[0], dxo[i], xo[i]))))));
         ++lc.dense;
     }
     __device__ void calc_pos(double tt, double *o) {
         double h, b[6];
         dense_coef(tt, h, b);
         for (int i = 0; i < 3; ++i)
-            o[i] = xo[i] + b[0] * dxo[i] + b[1] * k3[i] + b[2] * k4[i] + b[3] * k5[i] + b[4] * k6[i] + b[5] * dydt[i];
+            o[i] = fma(b[5], dyn[i], fma(b[4], k6[i], fma(b[3], k5[i], fma(b[2], k4[i], fma(b[1], k3[i], fma(b[0], dxo[i], xo[i]))))));
         ++lc.dense;
     }
 
@@ -710,26 +807,26 @@ struct Lane {
         nhit = nstep = nspinflip = 0;
         nacc = nrej = 0;
         dt = 10. * PT_MAX_TRACK_DEVIATION / sqrt(y[3] * y[3] + y[4] * y[4] + y[5] * y[5]);
-        flags = PT_F_INIT;
+        ntry = 0;
+        derivs(y, t, dydt); /* stepper.initialize + first derivative */
+        flags = PT_F_INIT | PT_F_DERIV;
         if (stop == PT_ID_UNKNOWN && t > R.simtime) stop = PT_ID_NOT_FINISH;
     }
 
-    /* One iteration of LOOP A (src/tracking.cpp:71-148). */
-    __device__ void step() {
-        if (flags & PT_F_RESET) flags &= ~(PT_F_DERIV | PT_F_RESET); /* stepper.initialize(y, x, dt) */
-        double x1 = t, y1[9];
-        for (int i = 0; i < 9; ++i) y1[i] = y[i];
-        if (!rk_step()) { stop = PT_ID_ODEINT_ERROR; return; }
+    /* The remainder of one LOOP-A iteration (src/tracking.cpp:87-147) after an
+     * accepted try: decay/tmax clipping, chord splitting, CheckHit, spin and
+     * stop checks, then commit. */
+    __device__ void post_step() {
+        double x1 = to, y1[9];
+        for (int i = 0; i < 9; ++i) y1[i] = xo[i];
+        double x = tn, yl[9];
+        for (int i = 0; i < 9; ++i) yl[i] = yn[i];
         bool finite = isfinite(tn);
-        for (int i = 0; i < 9; ++i) finite = finite && isfinite(y[i]);
+        for (int i = 0; i < 9; ++i) finite = finite && isfinite(yn[i]);
         if (!finite) { /* a non-finite state would never stop: report it as an integrator failure */
-            t = x1;
-            for (int i = 0; i < 9; ++i) y[i] = y1[i];
             stop = PT_ID_ODEINT_ERROR;
             return;
         }
-        double x = tn, yl[9];
-        for (int i = 0; i < 9; ++i) yl[i] = y[i];
         if (tau > 0 && yl[6] > tau) {
             x = x1 + (x - x1) * (tau - y1[6]) / (yl[6] - y1[6]);
             calc_state(x, yl);
@@ -738,7 +835,7 @@ struct Lane {
             x = R.simtime;
             calc_state(x, yl);
         }
-        bool reset = (flags & PT_F_RESET) != 0;
+        bool reset = false;
         int nsub = 0;
         while (x1 < x) {
             if (++nsub > PT_MAX_SUBSEGMENTS) { stop = PT_ID_ODEINT_ERROR; break; }
@@ -760,7 +857,12 @@ struct Lane {
             x1 = x2;
             for (int i = 0; i < 9; ++i) y1[i] = y2[i];
         }
-        /* IntegrateSpin + polarisation bookkeeping (src/tracking.cpp:128-138) */
+        finish_step(x, yl, reset);
+    }
+
+    /* IntegrateSpin + polarisation bookkeeping + stop checks
+     * (src/tracking.cpp:128-147), then commit the loop state. */
+    __device__ void finish_step(double x, double *yl, bool reset) {
         double sproj = integrate_spin(x, yl);
         bool flipped = xo[7] != yl[7];
         if (sproj != xo[7]) {
@@ -777,17 +879,55 @@ struct Lane {
         }
         if (stop == PT_ID_UNKNOWN && yl[6] >= tau) stop = PT_ID_DECAYED;
         else if (stop == PT_ID_UNKNOWN && (x >= R.simtime || yl[8] >= R.lmax)) stop = PT_ID_NOT_FINISH;
-        /* After a reset the stepper restarts from the loop's (x, y); otherwise it
-         * continues from its own state (so a polarisation change made by
-         * DoPolarize without a reset does not reach the stepper, as in the
-         * reference); a stopped particle reports the loop's (x, y). */
+        /* After a reset the stepper restarts from the loop's (x, y) with a fresh
+         * derivative (stepper.initialize); otherwise it continues from its own
+         * state (so a polarisation change by DoPolarize without a reset does
+         * not reach the stepper, as in the reference); a stopped particle
+         * reports the loop's (x, y). */
         if (reset || stop != PT_ID_UNKNOWN) {
             t = x;
             for (int i = 0; i < 9; ++i) y[i] = yl[i];
-            if (reset) flags |= PT_F_RESET;
+            if (stop == PT_ID_UNKNOWN) derivs(y, t, dydt);
         } else {
             t = tn;
+            for (int i = 0; i < 9; ++i) { y[i] = yn[i]; dydt[i] = dyn[i]; }
         }
+        flags |= PT_F_DERIV;
+    }
+
+    /* The common case of post_step decided up front: no decay/tmax clipping,
+     * no chord split, the chord inside the geometry box and no collision on
+     * it.  Then CheckHit reduces to DoStep and the sequence below is exactly
+     * what post_step would execute.  Returns false (nothing changed) when the
+     * step needs the full post_step. */
+    __device__ bool fast_post() {
+        bool finite = isfinite(tn);
+        for (int i = 0; i < 9; ++i) finite = finite && isfinite(yn[i]);
+        if (!finite) return false;
+        if (tau > 0 && yn[6] > tau) return false;
+        if (tn > R.simtime) return false;
+        double l2 = (yn[8] - xo[8]) * (yn[8] - xo[8]);
+        double d2 = (yn[0] - xo[0]) * (yn[0] - xo[0]) + (yn[1] - xo[1]) * (yn[1] - xo[1]) + (yn[2] - xo[2]) * (yn[2] - xo[2]);
+        if (0.25 * (l2 - d2) > PT_MAX_TRACK_DEVIATION * PT_MAX_TRACK_DEVIATION) return false;
+        if (!(to < tn)) return false;
+        if (!check_segment(S, xo, yn)) return false;
+        int cs = cur_solid();
+        const DMat &m = S.mats[S.solids[cs].mat];
+        if (R.sp.kind == PT_NEUTRON ? (m.fermi_imag > 0) : (S.solids[cs].id > 1)) return false; /* OnStep may act */
+        if (any_hit(xo, yn) != 0) return false;
+        double x2 = tn, y2[9];
+        for (int i = 0; i < 9; ++i) y2[i] = yn[i];
+        do_step(to, xo, x2, y2, cs); /* cannot alter the step here */
+        finish_step(tn, y2, false);
+        return true;
+    }
+
+    /* One iteration of LOOP A (src/tracking.cpp:71-148) for the plain form. */
+    __device__ void step() {
+        int r;
+        do { r = rk_try(); } while (r == 0);
+        if (r < 0) { stop = PT_ID_ODEINT_ERROR; return; }
+        post_step();
     }
 };
 

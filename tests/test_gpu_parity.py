@@ -60,7 +60,9 @@ def test_tab3_field_matches_oracle(eng, oracle_mod, kind):
         ax, comps = nonlinear_table()
         sc = table_scene(ax, comps, boundary_width=0.05, box=(0.25, -0.28, 0.3, -0.3, 0.2, -0.3))
     rng = np.random.default_rng(11)
-    q = np.column_stack([rng.uniform(-0.35, 0.35, (4000, 3)), np.zeros(4000)])
+    lo = np.array([a[0] for a in ax]) - 0.05
+    hi = np.array([a[-1] for a in ax]) + 0.05
+    q = np.column_stack([rng.uniform(lo, hi, (4000, 3)), np.zeros(4000)])
     q[:50, 0] = ax[0][rng.integers(0, len(ax[0]), 50)]  # exactly on grid planes
     e = eng(sc)
     B, dB, _, _ = e.field(q)
@@ -142,7 +144,7 @@ def test_collisions_match_oracle(eng, oracle_mod, mesh):
     c1, s1, n1, i1, d1 = e.collisions(segs)
     c2, s2, n2, i2, d2 = oracle_mod.Oracle(sc).collisions(segs)
     assert np.array_equal(c1, c2)
-    assert (c1 > 0).sum() > 300
+    assert (c1 > 0).sum() > 150
     for i in np.nonzero(c1 > 0)[0]:
         k = min(c1[i], 8)
         assert np.array_equal(s1[i, :k], s2[i, :k])
@@ -175,6 +177,10 @@ def test_cube_storage_parity(eng, oracle_mod):
     assert np.array_equal(gout.n_hit, oout.n_hit)
     assert np.all(gout.stop_id == A.ID_NOT_FINISH)
     assert gst["rk_accepted"] == ost["rk_accepted"]
+    # the FP64 arithmetic of the integrator is identical on both sides
+    # (explicit FMA chains, deterministic step-size power): bitwise end states
+    bitwise = np.all(gout.y == oout.y, axis=0) & (gout.t == oout.t)
+    assert bitwise.mean() >= 0.99, bitwise.mean()
 
 
 def test_integration_test_known_answer_gpu(eng):
@@ -230,3 +236,22 @@ def test_pause_and_resume_is_bit_identical(eng):
     assert st["active"] == 0
     for k in ("t", "y", "spin", "stop_id", "n_hit", "n_step", "h_max", "n_accepted"):
         assert np.array_equal(getattr(one, k), getattr(win, k)), k
+
+
+@pytest.mark.parametrize("precision", [A.PREC_FP64, A.PREC_FP32])
+def test_plain_and_batched_forms_are_bit_identical(eng, precision):
+    """The phase-split batched form schedules the same per-particle arithmetic
+    as the plain form, so every output is bit-identical."""
+    from pentrack_gb300 import workloads
+    sc, params, parts = workloads.field_storage(n=4096, simtime=0.4)
+    e = eng(sc)
+    params.field_precision = precision
+    params.mode = A.MODE_PLAIN
+    plain, sp = e.integrate(params, parts)
+    params.mode = A.MODE_BATCHED
+    batched, sb = e.integrate(params, parts)
+    for k in ("t", "y", "spin", "stop_id", "n_hit", "n_step", "n_spinflip", "h_max", "noflip_prob", "n_accepted",
+              "n_rejected", "solid"):
+        assert np.array_equal(getattr(plain, k), getattr(batched, k)), k
+    assert sp["rk_accepted"] == sb["rk_accepted"]
+    assert sb["try_ms"] > 0
