@@ -37,9 +37,12 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=1_000_000, help="particles per GPU")
-    p.add_argument("--window", type=float, default=0.02, help="lab-time window per step [s]")
-    p.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
-    p.add_argument("--mode", default="plain", choices=["plain", "batched"])
+    p.add_argument("--window", type=float, default=0.02, help="lab-time span of the CPU sample and e2e chunks [s]")
+    p.add_argument("--batch-steps", type=int, default=32, help="accepted RK steps per particle per bench step")
+    p.add_argument("--precision", default="fp32", choices=["fp64", "fp32"],
+                   help="field evaluation: fp64, or fp32 = mixed (corner values FP64, derivative terms FP32)")
+    p.add_argument("--mode", default="batched", choices=["plain", "batched"])
+    p.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison run")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -123,6 +126,26 @@ def setup_ours(args, rank):
     params.field_precision = A.PREC_FP32 if args.precision == "fp32" else A.PREC_FP64
     params.mode = A.MODE_BATCHED if args.mode == "batched" else A.MODE_PLAIN
     return engine, params, parts, device
+
+
+def plain_run(args, rank):
+    """The plain GPU form on the same workload and precision: one fixed
+    step-batch launch (one lane per particle) per bench step."""
+    from pentrack_gb300 import _abi as A
+    import torch
+    engine, params, parts, device = setup_ours(args, rank)
+    params.mode = A.MODE_PLAIN
+    batch = engine.batch(params, parts)
+    for _ in range(args.warmup):
+        batch.advance(max_steps=args.batch_steps)
+    torch.cuda.synchronize(device)
+    psec = ms = 0.0
+    for _ in range(args.steps):
+        st = batch.advance(max_steps=args.batch_steps)
+        psec += st["particle_seconds"]
+        ms += st["span_ms"]
+    return {"value": psec / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / args.steps,
+            "events": {"rk_accepted": st["rk_accepted"], "hits": st["hits"]}}
 
 
 def cpu_baseline(args, n_hint=2048):
@@ -230,10 +253,8 @@ def run_ours(args, rank, world):
     peak = ctypes.c_double(0)
     lib().pt_probe_fp64(engine.h, ctypes.byref(peak))
     batch = engine.batch(params, parts)
-    t_now = 0.0
     for _ in range(args.warmup):
-        t_now += args.window
-        batch.advance(t_now)
+        batch.advance(max_steps=args.batch_steps)
     dist = world > 1
     if dist:
         torch.distributed.barrier()
@@ -243,8 +264,7 @@ def run_ours(args, rank, world):
     agg = None
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        t_now += args.window
-        st = batch.advance(t_now)
+        st = batch.advance(max_steps=args.batch_steps)
         if agg is None:
             agg = dict(st)
         else:
@@ -271,9 +291,22 @@ def run_ours(args, rank, world):
     if rank != 0:
         return None
     f64, f32 = algorithmic_work(agg, args.precision)
-    launches = max(1, agg["dominant_launches"])
-    avg_launch_s = agg["dominant_kernel_ms"] / 1e3 / launches
-    achieved = f64 / launches / avg_launch_s / 1e12
+    if args.mode == "batched":
+        # dominant kernel of the batched form is k_try: one RK try per particle
+        tries = agg["rk_accepted"] + agg["rk_rejected"]
+        field_per_rhs = 1248
+        try_f64 = tries * (650 + 6 * 60) + (0 if args.precision == "fp32" else tries * 6 * field_per_rhs)
+        try_f64 += tries * 6 * 128 if args.precision == "fp32" else 0  # FP64 corner-value terms of the mixed field
+        launches = max(1, agg["dominant_launches"])
+        kern = {"k_try": agg["try_ms"], "k_post": agg["post_ms"], "k_slow": agg["slow_ms"]}
+        dom = max(kern, key=kern.get)
+        avg_launch_s = kern[dom] / 1e3 / launches
+        achieved = (try_f64 if dom == "k_try" else f64) / launches / avg_launch_s / 1e12
+        agg["dominant_kernel"] = dom
+    else:
+        launches = max(1, agg["dominant_launches"])
+        avg_launch_s = agg["dominant_kernel_ms"] / 1e3 / launches
+        achieved = f64 / launches / avg_launch_s / 1e12
     traffic = load_traffic()
     line = {
         "metric": METRIC,
@@ -290,7 +323,8 @@ def run_ours(args, rank, world):
         "data": "synthetic (seeded Philox sources; analytic quadrupole table)",
         "config": {"workload": f"field storage: {args.n} UCN/GPU, cylinder R=0.2 m H=0.1 m (1024 triangles), "
                                f"64^3 tricubic quadrupole, 250 neV walls 5% Lambert 1e-4 loss, tau 880 s",
-                   "window_s": args.window, "form": args.mode, "field_precision": args.precision,
+                   "step": f"one step-batch: every live particle advances {args.batch_steps} accepted RK steps",
+                   "form": args.mode, "field_precision": args.precision,
                    "l2": "per-step particle state > L2 (350 B x 1e6); field table L2-resident by design",
                    "parallelism": f"replicas x{world}"},
         "gpu_launches": int(agg["launches"]),
@@ -306,7 +340,10 @@ def run_ours(args, rank, world):
         "events": {k: agg[k] for k in ("rk_accepted", "rk_rejected", "rhs_evals", "field_evals", "hits",
                                         "bisection_levels", "bvh_nodes", "tri_tests", "subsegments", "dense_evals")},
         "live_particles": int(agg["active"]),
+        "phase_ms": {"k_try": agg["try_ms"], "k_post": agg["post_ms"], "k_slow": agg["slow_ms"]},
     }
+    if not args.no_plain and args.mode == "batched":
+        line["plain_form"] = plain_run(args, rank)
     line["energy_drift"] = energy_drift(engine, parts, out_state)
     if not args.no_e2e:
         try:

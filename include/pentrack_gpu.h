@@ -225,6 +225,9 @@ pt_status pt_batch_create(pt_ctx *ctx, const pt_run_params *params, const pt_par
 /* Advance every live particle until it stops or, at a step boundary, its lab
  * time reaches t_pause (resuming later is bit-identical to never pausing). */
 pt_status pt_batch_advance(pt_ctx *ctx, pt_batch *batch, double t_pause, pt_stats *stats);
+/* As pt_batch_advance, but each particle also pauses after max_steps accepted
+ * RK steps in this call (one fixed step-batch of the plain form; 0 = no limit). */
+pt_status pt_batch_advance_steps(pt_ctx *ctx, pt_batch *batch, double t_pause, int32_t max_steps, pt_stats *stats);
 pt_status pt_batch_read(pt_ctx *ctx, pt_batch *batch, pt_particles *out);
 void pt_batch_destroy(pt_batch *batch);
 

@@ -109,6 +109,7 @@ def declare(lib):
         "pt_integrate": (C.c_int32, [vp, P(RunParams), P(Particles), P(Particles), P(Stats)]),
         "pt_batch_create": (C.c_int32, [vp, P(RunParams), P(Particles), P(vp)]),
         "pt_batch_advance": (C.c_int32, [vp, vp, C.c_double, P(Stats)]),
+        "pt_batch_advance_steps": (C.c_int32, [vp, vp, C.c_double, C.c_int32, P(Stats)]),
         "pt_batch_read": (C.c_int32, [vp, vp, P(Particles)]),
         "pt_batch_destroy": (None, [vp]),
         "pt_field_eval": (C.c_int32, [vp, C.c_int64, c_double_p, C.c_int32, c_double_p, c_double_p, c_double_p, c_double_p]),

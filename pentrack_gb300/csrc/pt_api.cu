@@ -84,8 +84,15 @@ __global__ void k_gather(const __grid_constant__ DBatch b, double t_pause, int32
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= b.n) return;
     if (b.stop_id[i] != PT_ID_UNKNOWN) return;
+    b.nacc0[i] = b.nacc[i];
     if (b.flags[i] & PT_F_PENDING) list_push(b.list[3], &b.count[3], (int32_t)i); /* resume a deferred post-step */
     else if (b.t[i] < t_pause) list_push(list, count, (int32_t)i);
+}
+
+/* a committed particle keeps stepping in this advance call */
+__device__ __forceinline__ bool keeps_going(const DRun &R, const DBatch &b, const Lane &L, int i) {
+    if (L.stop != PT_ID_UNKNOWN || !(L.t < R.t_pause)) return false;
+    return R.max_steps <= 0 || L.nacc - b.nacc0[i] < R.max_steps;
 }
 
 __global__ void k_zero_counts(int32_t *count, int a, int b, int c) {
@@ -135,7 +142,7 @@ __global__ void __launch_bounds__(128) k_post(const __grid_constant__ DScene S, 
             ps += L.t - t0;
             L.store_bc_commit(b, i);
             L.store(b, i);
-            if (L.stop == PT_ID_UNKNOWN && L.t < R.t_pause) list_push(b.list[out], &b.count[out], i);
+            if (keeps_going(R, b, L, i)) list_push(b.list[out], &b.count[out], i);
         } else {
             b.flags[i] |= PT_F_PENDING;
             list_push(b.list[3], &b.count[3], i);
@@ -162,7 +169,7 @@ __global__ void __launch_bounds__(128) k_slow(const __grid_constant__ DScene S, 
         ps += L.t - t0;
         L.store_bc_commit(b, i);
         L.store(b, i);
-        if (L.stop == PT_ID_UNKNOWN && L.t < R.t_pause) list_push(b.list[out], &b.count[out], i);
+        if (keeps_going(R, b, L, i)) list_push(b.list[out], &b.count[out], i);
     }
     flush_counters(C, L.lc, ps, false);
 }
@@ -176,6 +183,7 @@ __global__ void __launch_bounds__(128) k_plain(const __grid_constant__ DScene S,
     Lane L(S, R);
     L.load(b, i);
     const double t0 = L.t;
+    if (R.max_steps > 0) steps = R.max_steps;
     for (int s = 0; s < steps; ++s) {
         L.step();
         if (L.stop != PT_ID_UNKNOWN || L.t >= R.t_pause) break;
@@ -669,7 +677,7 @@ pt_status pt_batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles 
     ALLOC(nspinflip, int32_t, n) ALLOC(nsol, int32_t, n) ALLOC(flags, uint32_t, n) ALLOC(stack, uint64_t, n)
     ALLOC(rng_n, uint64_t, n) ALLOC(nacc, int64_t, n) ALLOC(nrej, int64_t, n) ALLOC(ntry, int32_t, n)
     ALLOC(yn, double, 9 * n) ALLOC(dyn, double, 9 * n) ALLOC(kst, double, 36 * n) ALLOC(tn, double, n)
-    ALLOC(bc, double, 14 * n) ALLOC(count, int32_t, 8)
+    ALLOC(bc, double, 14 * n) ALLOC(count, int32_t, 8) ALLOC(nacc0, int64_t, n)
     for (int k = 0; k < 4; ++k) { b.list[k] = dalloc<int32_t>(B->allocs, (size_t)n, e); if (e) { free_list(B->allocs); return ck(c, e, "batch alloc"), PT_ERR_OOM; } }
 #undef ALLOC
     if (n > 0) {
@@ -700,11 +708,16 @@ void pt_batch_destroy(pt_batch *B) {
 }
 
 pt_status pt_batch_advance(pt_ctx *c, pt_batch *B, double t_pause, pt_stats *stats) {
-    if (!c || !B) return PT_ERR_INVALID;
+    return pt_batch_advance_steps(c, B, t_pause, 0, stats);
+}
+
+pt_status pt_batch_advance_steps(pt_ctx *c, pt_batch *B, double t_pause, int32_t max_steps, pt_stats *stats) {
+    if (!c || !B || max_steps < 0) return PT_ERR_INVALID;
     cudaSetDevice(c->device);
     auto w0 = std::chrono::steady_clock::now();
     DRun R = B->run;
     R.t_pause = t_pause;
+    R.max_steps = max_steps;
     pt_stats acc;
     std::memset(&acc, 0, sizeof(acc));
     std::snprintf(acc.dominant_kernel, sizeof(acc.dominant_kernel), "k_plain");
@@ -741,7 +754,7 @@ pt_status pt_batch_advance(pt_ctx *c, pt_batch *B, double t_pause, pt_stats *sta
         acc.dense_evals += k.dense_evals; acc.particle_seconds += k.particle_seconds;
         acc.active = (int64_t)k.active;
         if (*(volatile int *)c->cancel_host) { cancelled = true; break; }
-        if (k.active == 0) break;
+        if (k.active == 0 || max_steps > 0) break; /* a step budget is one fixed step-batch launch */
         if (B->max_launches > 0 && launch + 1 >= B->max_launches) { timed_out = true; break; }
         if (B->timeout_s > 0 && std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count() > B->timeout_s) {
             timed_out = true;

@@ -28,6 +28,7 @@
 #define PT_MAX_LAMBERT 10000
 #define PT_MAX_SUBSEGMENTS (1 << 20) /* chord pieces of one RK step */
 #define PT_MAX_HITS_PER_SEGMENT 64   /* surfaces crossed by one chord piece */
+#define PT_MAX_CAND 8                /* candidate triangles kept for a bisection */
 
 /* lane flags */
 #define PT_F_DERIV 1u   /* FSAL derivative valid */
@@ -102,7 +103,7 @@ struct DRun {
     double simtime, tau, tmax, lmax, bmax;
     double spintimes[PT_MAX_SPINTIMES];
     int n_spintimes, flipspin, prec, steps_per_launch;
-    int mode, pad;
+    int mode, max_steps;      /* max_steps: accepted RK steps per particle in one advance call (0 = no limit) */
     uint64_t seed;
     double t_pause;
     volatile int *cancel;   /* host-mapped cancel word (the reference's quit flag) */
@@ -119,6 +120,7 @@ struct DBatch {
     uint64_t *rng_n;
     int64_t *nacc, *nrej;
     int32_t *ntry;
+    int64_t *nacc0;              /* accepted steps at the start of the current advance call */
     /* phase-split form: result of the last accepted try and B-value caches */
     double *yn, *dyn, *kst, *tn; /* yn, dyn: 9n; kst: k3..k6, 36n; tn: n */
     double *bc;                  /* 2 slots x (x, y, z, t, Bx, By, Bz): 14n */

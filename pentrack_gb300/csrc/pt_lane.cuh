@@ -39,12 +39,17 @@ struct Lane {
     double bc_p[2][4], bc_B[2][3];
     bool bc_ok[2];
     int bc_next;
+    /* triangles that can touch the dense-output curve of the current chord piece
+     * (ncand < 0: not available, use the full BVH query) */
+    int cand[PT_MAX_CAND];
+    int ncand;
     LaneCounters lc;
 
     __device__ Lane(const DScene &s, const DRun &r) : S(s), R(r) {
         bc_ok[0] = bc_ok[1] = false;
         bc_next = 0;
         ntry = 0;
+        ncand = -1;
         lc = LaneCounters{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     }
 
@@ -370,6 +375,19 @@ struct Lane {
     /* ---------------- geometry wrappers ---------------- */
     /* any collision on segment p->q; returns -1 on a coplanar (CGAL error) case */
     __device__ int any_hit(const double *p, const double *q) {
+        if (ncand >= 0) {
+            bool cp = false;
+            for (int j = 0; j < ncand; ++j) {
+                const DTri &t = S.tris[cand[j]];
+                if (!tri_box_touch(t, p, q)) continue;
+                ++lc.tris;
+                double sv;
+                int r = seg_tri(p, q, t, sv);
+                if (r > 0) return 1;
+                if (r < 0) cp = true;
+            }
+            return cp ? -1 : 0;
+        }
         QueryStats qs{0, 0};
         bool cp;
         Coll dummy;
@@ -380,6 +398,31 @@ struct Lane {
         return cp ? -1 : 0;
     }
     __device__ int all_hits(double x1, const double *p, double x2, const double *q, Coll *c) {
+        if (ncand >= 0) {
+            int nh = 0;
+            for (int j = 0; j < ncand; ++j) {
+                const DTri &t = S.tris[cand[j]];
+                if (!tri_box_touch(t, p, q)) continue;
+                ++lc.tris;
+                double sv;
+                int r = seg_tri(p, q, t, sv);
+                if (r < 0) return -1;
+                if (r == 0) continue;
+                Coll cl;
+                cl.s = sv;
+                cl.n[0] = t.n[0]; cl.n[1] = t.n[1]; cl.n[2] = t.n[2];
+                cl.solid = t.solid;
+                cl.id = S.solids[t.solid].id;
+                cl.dn = (q[0] - p[0]) * t.n[0] + (q[1] - p[1]) * t.n[1] + (q[2] - p[2]) * t.n[2];
+                cl.ign = solid_ignored(S.solids[t.solid], x1 + (x2 - x1) * sv);
+                if (nh >= PT_MAX_COLLS) return -2;
+                int k = nh;
+                while (k > 0 && (c[k - 1].s > cl.s || (c[k - 1].s == cl.s && c[k - 1].id < cl.id))) { c[k] = c[k - 1]; --k; }
+                c[k] = cl;
+                ++nh;
+            }
+            return nh;
+        }
         QueryStats qs{0, 0};
         bool cp;
         int h = mesh_query<1>(S, p, q, x1, x2, c, PT_MAX_COLLS, nullptr, qs, cp);
@@ -388,6 +431,68 @@ struct Lane {
         if (cp) return -1;
         if (h > PT_MAX_COLLS) return -2;
         return h;
+    }
+
+    /* Conservative box of the dense-output positions for t in [ta, tb]: each
+     * coordinate is a degree-5 polynomial in theta = (t - to)/(tn - to); its
+     * Bernstein coefficients on [theta_a, theta_b] bound it (convex hull
+     * property), widened by 1e-9 m + 1e-12 relative to cover rounding.
+     * Every chord between two dense-output points of that interval lies in
+     * the box, so the triangles touching the box are all the bisection and
+     * DoHit can ever hit. */
+    __device__ void curve_box(double ta, double tb, double lo[3], double hi[3]) const {
+        /* theta^1..theta^5 coefficients of the continuous-extension weights of
+         * k1 (dxo), k3, k4, k5, k6, k7 (dyn), from runge_kutta_dopri5::calc_state */
+        const double Wc[6][5] = {
+            {1.0, -2.8605386690370884, 3.099577878709121, -1.1618105836403092, 0.013917207301610328},
+            {0.0, 4.047141499642786, -6.345354046938926, 2.795465086414005, -0.04801624082496286},
+            {0.0, -3.941160071112659, 10.904003027940295, -6.729317509209278, 0.4175162190483098},
+            {0.0, 2.8419447015870345, -7.547675862959386, 4.957636724931253, -0.5742817428041846},
+            {0.0, -1.6109886359167997, 4.218915839039518, -2.950103865566732, 0.47312904339639456},
+            {0.0, 1.523601174836727, -4.329466835790622, 3.0881301470710616, -0.2822644861171672}};
+        /* C(k,j)/C(5,j) for the monomial-to-Bernstein map */
+        const double Bm[6][6] = {{1, 0, 0, 0, 0, 0},
+                                 {1, 0.2, 0, 0, 0, 0},
+                                 {1, 0.4, 0.1, 0, 0, 0},
+                                 {1, 0.6, 0.3, 0.1, 0, 0},
+                                 {1, 0.8, 0.6, 0.4, 0.2, 0},
+                                 {1, 1, 1, 1, 1, 1}};
+        const double h = tn - to;
+        double t1 = (ta - to) / h, t2 = (tb - to) / h;
+        const double D = t2 - t1;
+        for (int k = 0; k < 3; ++k) {
+            double c[6];
+            c[0] = xo[k];
+            for (int j = 1; j <= 5; ++j)
+                c[j] = h * (Wc[0][j - 1] * dxo[k] + Wc[1][j - 1] * k3[k] + Wc[2][j - 1] * k4[k] + Wc[3][j - 1] * k5[k] +
+                            Wc[4][j - 1] * k6[k] + Wc[5][j - 1] * dyn[k]);
+            for (int i = 0; i < 5; ++i) /* Taylor shift to theta_a */
+                for (int j = 4; j >= i; --j) c[j] += t1 * c[j + 1];
+            double dj = 1;
+            for (int j = 1; j <= 5; ++j) { dj *= D; c[j] *= dj; }
+            double mn = 1e300, mx = -1e300, mag = 0;
+            for (int r = 0; r <= 5; ++r) {
+                double beta = 0;
+                for (int j = 0; j <= r; ++j) beta += Bm[r][j] * c[j];
+                mn = fmin(mn, beta);
+                mx = fmax(mx, beta);
+                mag = fmax(mag, fabs(beta));
+            }
+            double margin = 1e-9 + 1e-12 * mag;
+            lo[k] = mn - margin;
+            hi[k] = mx + margin;
+        }
+    }
+    /* set up the candidate triangles for chord pieces within [ta, tb] */
+    __device__ void prepare_candidates(double ta, double tb) {
+        double lo[3], hi[3];
+        curve_box(ta, tb, lo, hi);
+        bool ok = true;
+        for (int k = 0; k < 3; ++k) ok = ok && isfinite(lo[k]) && isfinite(hi[k]);
+        if (!ok) { ncand = -1; return; }
+        QueryStats qs{0, 0};
+        ncand = collect_candidates(S, lo, hi, cand, PT_MAX_CAND, qs);
+        lc.nodes += qs.nodes;
     }
 
     /* ---------------- RotateVector (src/globals.cpp:40-64) ---------------- */
@@ -704,6 +809,12 @@ struct Lane {
 
     /* TTracker::CheckHit (src/tracking.cpp:176-226), tail recursion as a loop */
     __device__ bool check_hit(double x1, const double *y1in, double &x2, double *y2) {
+        ncand = -1;
+        bool r = check_hit_loop(x1, y1in, x2, y2);
+        ncand = -1;
+        return r;
+    }
+    __device__ bool check_hit_loop(double x1, const double *y1in, double &x2, double *y2) {
         double ya[9];
         for (int i = 0; i < 9; ++i) ya[i] = y1in[i];
         for (int pass = 0;; ++pass) {
@@ -712,8 +823,9 @@ struct Lane {
             if (x2 == x1) return false;
             int cs = cur_solid();
             int h = any_hit(ya, y2);
-            if (h < 0) { stop = PT_ID_CGAL_ERROR; return true; }
-            if (!h) return do_step(x1, ya, x2, y2, cs);
+            if (h < 0) { stop = PT_ID_CGAL_ERROR; ncand = -1; return true; }
+            if (!h) { ncand = -1; return do_step(x1, ya, x2, y2, cs); }
+            if (ncand < 0 && x1 >= to && x2 <= tn) prepare_candidates(x1, x2);
             double xa, xb;
             bool ao, bo;
             int r = bisect(x1, ya, x2, y2, xa, ao, xb, bo);

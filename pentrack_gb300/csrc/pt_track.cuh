@@ -441,6 +441,84 @@ __device__ bool check_segment(const DScene &S, const double *p, const double *q)
 
 struct QueryStats { unsigned nodes, tris; };
 
+/* the triangle's own box touches the box of segment p-q (exact FP64 compares,
+ * the pre-test the oracle applies before every segment-triangle test) */
+__device__ __forceinline__ bool tri_box_touch(const DTri &t, const double *p, const double *q) {
+    for (int k = 0; k < 3; ++k) {
+        double tlo = fmin(t.a[k], fmin(t.b[k], t.c[k])), thi = fmax(t.a[k], fmax(t.b[k], t.c[k]));
+        double slo = fmin(p[k], q[k]), shi = fmax(p[k], q[k]);
+        if (tlo > shi || thi < slo) return false;
+    }
+    return true;
+}
+
+/* Separating-axis overlap test of a triangle and an axis-aligned box given by
+ * centre c and half sizes e (Akenine-Moeller, "Fast 3D triangle-box overlap
+ * testing", 2001): box axes, triangle normal, and the nine edge x axis
+ * cross products.  Used with a box enlarged by a safety margin, so FP64
+ * rounding can only add candidates, never drop one. */
+__device__ bool tri_box_overlap(const DTri &t, const double *c, const double *e) {
+    double v0[3], v1[3], v2[3];
+    for (int k = 0; k < 3; ++k) { v0[k] = t.a[k] - c[k]; v1[k] = t.b[k] - c[k]; v2[k] = t.c[k] - c[k]; }
+    for (int k = 0; k < 3; ++k) {
+        double mn = fmin(v0[k], fmin(v1[k], v2[k])), mx = fmax(v0[k], fmax(v1[k], v2[k]));
+        if (mn > e[k] || mx < -e[k]) return false;
+    }
+    double f[3][3];
+    for (int k = 0; k < 3; ++k) { f[0][k] = v1[k] - v0[k]; f[1][k] = v2[k] - v1[k]; f[2][k] = v0[k] - v2[k]; }
+    const double *vv[3] = {v0, v1, v2};
+    for (int i = 0; i < 3; ++i)       /* edge i */
+        for (int a = 0; a < 3; ++a) { /* box axis a: axis = e_a x f_i */
+            double ax[3] = {0, 0, 0};
+            const int a1 = (a + 1) % 3, a2 = (a + 2) % 3;
+            ax[a1] = -f[i][a2];
+            ax[a2] = f[i][a1];
+            double pmin = 1e300, pmax = -1e300;
+            for (int v = 0; v < 3; ++v) {
+                double pr = ax[0] * vv[v][0] + ax[1] * vv[v][1] + ax[2] * vv[v][2];
+                pmin = fmin(pmin, pr);
+                pmax = fmax(pmax, pr);
+            }
+            double r = e[0] * fabs(ax[0]) + e[1] * fabs(ax[1]) + e[2] * fabs(ax[2]);
+            if (pmin > r || pmax < -r) return false;
+        }
+    /* plane of the triangle */
+    double d = t.n[0] * v0[0] + t.n[1] * v0[1] + t.n[2] * v0[2];
+    double r = e[0] * fabs(t.n[0]) + e[1] * fabs(t.n[1]) + e[2] * fabs(t.n[2]);
+    if (d > r || d < -r) return false;
+    return true;
+}
+
+/* indices of the triangles that may touch the box [lo, hi]; -1 if more than maxc */
+__device__ int collect_candidates(const DScene &S, const double *lo, const double *hi, int *cand, int maxc, QueryStats &qs) {
+    float flo[3], fhi[3];
+    double c[3], e[3];
+    for (int k = 0; k < 3; ++k) {
+        flo[k] = __double2float_rd(lo[k]);
+        fhi[k] = __double2float_ru(hi[k]);
+        c[k] = 0.5 * (lo[k] + hi[k]);
+        e[k] = 0.5 * (hi[k] - lo[k]);
+    }
+    int nc = 0;
+    int i = 0;
+    while (i < S.n_nodes) {
+        const DNode nd = S.nodes[i];
+        ++qs.nodes;
+        bool ov = !(nd.lo[0] > fhi[0] || nd.hi[0] < flo[0] || nd.lo[1] > fhi[1] || nd.hi[1] < flo[1] || nd.lo[2] > fhi[2] ||
+                    nd.hi[2] < flo[2]);
+        if (!ov) { i = nd.skip; continue; }
+        if (nd.leaf < 0) { ++i; continue; }
+        int first = nd.leaf >> 3, cnt = nd.leaf & 7;
+        for (int j = first; j < first + cnt; ++j) {
+            if (!tri_box_overlap(S.tris[j], c, e)) continue;
+            if (nc >= maxc) return -1;
+            cand[nc++] = j;
+        }
+        i = nd.skip;
+    }
+    return nc;
+}
+
 /* Stackless traversal of the depth-first BVH with FP32 boxes rounded outward;
  * the segment box is rounded outward too, so no triangle the FP64 test would
  * hit is ever skipped.  mode 0: stop at the first hit; mode 1: collect all
@@ -468,6 +546,7 @@ __device__ int mesh_query(const DScene &S, const double *p, const double *q, dou
         int first = nd.leaf >> 3, cnt = nd.leaf & 7;
         for (int j = first; j < first + cnt; ++j) {
             const DTri &t = S.tris[j];
+            if (MODE != 2 && !tri_box_touch(t, p, q)) continue;
             ++qs.tris;
             double s;
             int r = seg_tri(p, q, t, s);

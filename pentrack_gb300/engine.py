@@ -289,9 +289,11 @@ class Batch:
         engine._check(lib().pt_batch_create(engine.h, C.byref(params), C.byref(pin), C.byref(h)))
         self.h = h
 
-    def advance(self, t_pause=float("inf")):
+    def advance(self, t_pause=float("inf"), max_steps=0):
+        """Advance live particles until they stop, reach lab time t_pause at a
+        step boundary, or (max_steps > 0) complete max_steps accepted steps."""
         st = A.Stats()
-        self.engine._check(lib().pt_batch_advance(self.engine.h, self.h, t_pause, C.byref(st)))
+        self.engine._check(lib().pt_batch_advance_steps(self.engine.h, self.h, t_pause, max_steps, C.byref(st)))
         return st.as_dict()
 
     def read(self):
