@@ -198,6 +198,7 @@ typedef struct pt_stats {
     int64_t dominant_launches;
     char dominant_kernel[48];
     double try_ms, post_ms, slow_ms; /* batched form: device time per phase kernel */
+    int64_t bisect_max;        /* largest number of collision queries of one bisection */
 } pt_stats;
 
 typedef struct pt_ctx pt_ctx;

@@ -53,6 +53,7 @@
 #define PT_ELECTRON_MG 0x1.ea718eae0a393p-35
 
 #define PT_C0_SQ 0x1.3f4d4eacdd756p+56
+#define PT_INV_C0_SQ 0x1.9a7ed39e826dap-57
 #define PT_MAX_TRACK_DEVIATION 0x1.0624dd2f1a9fcp-10 /* 0.001 m, include/particle.h:20 */
 #define PT_REFLECT_TOLERANCE 1e-8 /* include/trianglemesh.h:39 */
 

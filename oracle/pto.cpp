@@ -611,24 +611,32 @@ template <int N> struct Dense5 {
         }
     }
     /* runge_kutta_dopri5::calc_state: odeint's continuous extension between the
-     * last two accepted points */
+     * last two accepted points.  Its weights b_i(theta) (odeint's
+     * A b_i -/+ C X_i (+D) form with X_i linear in theta) are expanded here
+     * into monomials theta..theta^5 and evaluated by Horner's rule, with one
+     * division for theta; the engine evaluates the same expression. */
     void calc_state(double tt, double *y) const {
-        const double b1 = 35.0 / 384, b3 = 500.0 / 1113, b4 = 125.0 / 192, b5 = -2187.0 / 6784, b6 = 11.0 / 84;
+        static const double W[6][5] = {
+            {1.0, -2.8605386690370884, 3.099577878709121, -1.1618105836403092, 0.013917207301610328},
+            {0.0, 4.047141499642786, -6.345354046938926, 2.795465086414005, -0.04801624082496286},
+            {0.0, -3.941160071112659, 10.904003027940295, -6.729317509209278, 0.4175162190483098},
+            {0.0, 2.8419447015870345, -7.547675862959386, 4.957636724931253, -0.5742817428041846},
+            {0.0, -1.6109886359167997, 4.218915839039518, -2.950103865566732, 0.47312904339639456},
+            {0.0, 1.523601174836727, -4.329466835790622, 3.0881301470710616, -0.2822644861171672}};
         const double h = t - to;
         const double th = (tt - to) / h;
-        const double X1 = 5.0 * (2558722523.0 - 31403016.0 * th) / 11282082432.0;
-        const double X3 = 100.0 * (882725551.0 - 15701508.0 * th) / 32700410799.0;
-        const double X4 = 25.0 * (443332067.0 - 31403016.0 * th) / 1880347072.0;
-        const double X5 = 32805.0 * (23143187.0 - 3489224.0 * th) / 199316789632.0;
-        const double X6 = 55.0 * (29972135.0 - 7076736.0 * th) / 822651844.0;
-        const double X7 = 10.0 * (7414447.0 - 829305.0 * th) / 29380423.0;
-        const double thm1 = th - 1.0, th2 = th * th;
-        const double A = th2 * (3.0 - 2.0 * th), B = th2 * thm1, C = th2 * thm1 * thm1, D = th * thm1 * thm1;
-        const double bt1 = A * b1 - C * X1 + D, bt3 = A * b3 + C * X3, bt4 = A * b4 - C * X4, bt5 = A * b5 + C * X5,
-                     bt6 = A * b6 - C * X6, bt7 = B + C * X7;
+        double hb[6];
+        for (int k = 0; k < 6; ++k) {
+            double p = W[k][4];
+            p = std::fma(p, th, W[k][3]);
+            p = std::fma(p, th, W[k][2]);
+            p = std::fma(p, th, W[k][1]);
+            p = std::fma(p, th, W[k][0]);
+            hb[k] = h * (p * th);
+        }
         for (int i = 0; i < N; ++i)
-            y[i] = std::fma(h * bt7, dxdt[i], std::fma(h * bt6, k6[i], std::fma(h * bt5, k5[i], std::fma(h * bt4, k4[i],
-                   std::fma(h * bt3, k3[i], std::fma(h * bt1, dxdto[i], xo[i]))))));
+            y[i] = std::fma(hb[5], dxdt[i], std::fma(hb[4], k6[i], std::fma(hb[3], k5[i], std::fma(hb[2], k4[i],
+                   std::fma(hb[1], k3[i], std::fma(hb[0], dxdto[i], xo[i]))))));
     }
 };
 
@@ -737,21 +745,22 @@ struct Tracker {
             F[2] += sp.q * (E[2] + y[3] * B[1] - y[4] * B[0]);
         }
         if (sp.mu != 0 && y[7] != 0 && (B[0] != 0 || B[1] != 0 || B[2] != 0)) {
-            double Babs = std::sqrt(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
-            double dBdxi[3] = {(B[0] * dB[0][0] + B[1] * dB[1][0] + B[2] * dB[2][0]) / Babs,
-                               (B[0] * dB[0][1] + B[1] * dB[1][1] + B[2] * dB[2][1]) / Babs,
-                               (B[0] * dB[0][2] + B[1] * dB[1][2] + B[2] * dB[2][2]) / Babs};
+            /* grad|B| = (B . dB/dx_i)/|B| with one reciprocal */
+            double inv = 1.0 / std::sqrt(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
+            double dBdxi[3] = {(B[0] * dB[0][0] + B[1] * dB[1][0] + B[2] * dB[2][0]) * inv,
+                               (B[0] * dB[0][1] + B[1] * dB[1][1] + B[2] * dB[2][1]) * inv,
+                               (B[0] * dB[0][2] + B[1] * dB[1][2] + B[2] * dB[2][2]) * inv};
             F[0] += y[7] * sp.mu * dBdxi[0];
             F[1] += y[7] * sp.mu * dBdxi[1];
             F[2] += y[7] * sp.mu * dBdxi[2];
         }
         double v2 = y[3] * y[3] + y[4] * y[4] + y[5] * y[5];
-        double ig = std::sqrt(1 - v2 / PT_C0_SQ);
-        double vF = y[3] * F[0] + y[4] * F[1] + y[5] * F[2];
+        double ig = std::sqrt(1 - v2 * PT_INV_C0_SQ);
+        double vF = (y[3] * F[0] + y[4] * F[1] + y[5] * F[2]) * PT_INV_C0_SQ;
         double s = ig * sp.inv_mkg;
-        dydx[3] = s * (F[0] - y[3] * vF / PT_C0_SQ);
-        dydx[4] = s * (F[1] - y[4] * vF / PT_C0_SQ);
-        dydx[5] = s * (F[2] - y[5] * vF / PT_C0_SQ);
+        dydx[3] = s * (F[0] - y[3] * vF);
+        dydx[4] = s * (F[1] - y[4] * vF);
+        dydx[5] = s * (F[2] - y[5] * vF);
         dydx[6] = ig;
         dydx[7] = 0;
         dydx[8] = std::sqrt(v2);

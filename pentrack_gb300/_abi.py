@@ -87,6 +87,7 @@ class Stats(C.Structure):
         ("bvh_nodes", C.c_int64), ("tri_tests", C.c_int64), ("subsegments", C.c_int64), ("dense_evals", C.c_int64),
         ("dominant_kernel_ms", C.c_double), ("dominant_launches", C.c_int64), ("dominant_kernel", C.c_char * 48),
         ("try_ms", C.c_double), ("post_ms", C.c_double), ("slow_ms", C.c_double),
+        ("bisect_max", C.c_int64),
     ]
 
     def as_dict(self):

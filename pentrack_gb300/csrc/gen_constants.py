@@ -72,6 +72,7 @@ def main():
         lines.append(f"#define PT_{name}_MG {hx(m * c['PT_GRAVCONST'])}")
     lines.append("")
     lines.append("#define PT_C0_SQ " + hx(c["PT_C0"] * c["PT_C0"]))
+    lines.append("#define PT_INV_C0_SQ " + hx(L(1) / (c["PT_C0"] * c["PT_C0"])))
     lines.append("#define PT_MAX_TRACK_DEVIATION 0x1.0624dd2f1a9fcp-10 /* 0.001 m, include/particle.h:20 */")
     lines.append("#define PT_REFLECT_TOLERANCE 1e-8 /* include/trianglemesh.h:39 */")
     lines.append("")

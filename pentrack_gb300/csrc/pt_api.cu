@@ -40,6 +40,9 @@ __device__ __forceinline__ void flush_counters(DCounters *C, const LaneCounters 
     const int leader = __ffs(mask) - 1;
     for (int k = 0; k < 11; ++k) v[k] = warp_sum(mask, v[k]);
     double ps = warp_sum(mask, psec);
+    unsigned bm = lc.bisect_max;
+    for (unsigned m = mask; m; m &= m - 1) bm = max(bm, __shfl_sync(mask, lc.bisect_max, __ffs(m) - 1));
+    if (lane == leader && bm) atomicMax(&C->bisect_max, bm);
     if (lane == leader) {
         unsigned long long *dst[11] = {&C->rk_accepted, &C->rk_rejected, &C->rhs_evals, &C->field_evals, &C->hits,
                                        &C->bisection_levels, &C->bvh_nodes, &C->tri_tests, &C->subsegments,
@@ -393,6 +396,16 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
     S.mesh_zmax = tris.empty() ? 0.0 : zmax;
     S.tris = (const DTri *)dupload(c->allocs, (const DTri *)tris.data(), tris.size(), e);
     if (e) return ck(c, e, "upload triangles"), PT_ERR_CUDA;
+    {
+        /* FP32 planes for the side pre-test, in BVH triangle order */
+        std::vector<DTri32> t32(tris.size());
+        for (size_t k = 0; k < tris.size(); ++k) {
+            for (int a = 0; a < 3; ++a) { t32[k].a[a] = (float)tris[k].a[a]; t32[k].n[a] = (float)tris[k].n[a]; }
+            t32[k].pad[0] = t32[k].pad[1] = 0;
+        }
+        S.tri32 = dupload(c->allocs, t32.data(), t32.size(), e);
+        if (e) return ck(c, e, "upload triangle planes"), PT_ERR_CUDA;
+    }
     S.nodes = (const DNode *)dupload(c->allocs, (const DNode *)nodes.data(), nodes.size(), e);
     if (e) return ck(c, e, "upload bvh"), PT_ERR_CUDA;
     S.solids = dupload(c->allocs, solids.data(), solids.size(), e);
@@ -428,12 +441,18 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
             std::vector<double> zero(tot, 0.0);
             const double *comp[4] = {f.bx, f.by, f.bz, f.v};
             for (int k = 0; k < o.ncomp; ++k) pth::hermite_nodes(ax, comp[k] ? comp[k] : zero.data(), k, o.ncomp * 8, nd);
-            std::vector<float> nd32(nd.size());
-            for (size_t k = 0; k < nd.size(); ++k) nd32[k] = (float)nd[k];
             o.node64 = dupload(c->allocs, nd.data(), nd.size(), e);
             if (e) return ck(c, e, "upload table"), PT_ERR_CUDA;
-            o.node32 = dupload(c->allocs, nd32.data(), nd32.size(), e);
-            if (e) return ck(c, e, "upload table"), PT_ERR_CUDA;
+            {
+                std::vector<double> base;
+                std::vector<float> rem;
+                pth::mixed_cells(ax, nd, o.ncomp, base, rem);
+                o.cell64 = dupload(c->allocs, base.data(), base.size(), e);
+                if (e) return ck(c, e, "upload cell table"), PT_ERR_CUDA;
+                o.cell32 = dupload(c->allocs, rem.data(), rem.size(), e);
+                if (e) return ck(c, e, "upload cell table"), PT_ERR_CUDA;
+                o.node32 = nullptr;
+            }
             int n3[3] = {f.nx, f.ny, f.nz};
             for (int a = 0; a < 3; ++a) {
                 o.n[a] = n3[a];
@@ -441,6 +460,10 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
                 if (e) return ck(c, e, "upload axis"), PT_ERR_CUDA;
                 o.a0[a] = ax[a][0];
                 o.inv_h[a] = (double)(ax[a].size() - 1) / (ax[a].back() - ax[a][0]);
+                std::vector<double> iw(ax[a].size() - 1);
+                for (size_t k = 0; k + 1 < ax[a].size(); ++k) iw[k] = 1.0 / (ax[a][k + 1] - ax[a][k]);
+                o.inv_w[a] = dupload(c->allocs, iw.data(), iw.size(), e);
+                if (e) return ck(c, e, "upload axis"), PT_ERR_CUDA;
             }
         } else if (f.type == PT_FIELD_HARMONIC) {
             std::vector<double> coef;
@@ -476,6 +499,7 @@ void add_counters(pt_stats &acc, const DCounters &k) {
     acc.field_evals += k.field_evals; acc.hits += k.hits; acc.bisection_levels += k.bisection_levels;
     acc.bvh_nodes += k.bvh_nodes; acc.tri_tests += k.tri_tests; acc.subsegments += k.subsegments;
     acc.dense_evals += k.dense_evals; acc.particle_seconds += k.particle_seconds;
+    acc.bisect_max = std::max<int64_t>(acc.bisect_max, k.bisect_max);
 }
 
 int persistent_grid(pt_ctx *c, const void *fn, int block) {
@@ -748,10 +772,7 @@ pt_status pt_batch_advance_steps(pt_ctx *c, pt_batch *B, double t_pause, int32_t
         acc.dominant_kernel_ms += ms;
         acc.dominant_launches += 1;
         acc.launches += 1;
-        acc.rk_accepted += k.rk_accepted; acc.rk_rejected += k.rk_rejected; acc.rhs_evals += k.rhs_evals;
-        acc.field_evals += k.field_evals; acc.hits += k.hits; acc.bisection_levels += k.bisection_levels;
-        acc.bvh_nodes += k.bvh_nodes; acc.tri_tests += k.tri_tests; acc.subsegments += k.subsegments;
-        acc.dense_evals += k.dense_evals; acc.particle_seconds += k.particle_seconds;
+        add_counters(acc, k);
         acc.active = (int64_t)k.active;
         if (*(volatile int *)c->cancel_host) { cancelled = true; break; }
         if (k.active == 0 || max_steps > 0) break; /* a step budget is one fixed step-batch launch */

@@ -25,6 +25,7 @@
 #define PT_MAX_SOLIDS 64
 #define PT_MAX_TRIES 500      /* odeint failed_step_checker */
 #define PT_MAX_BISECT_WORK 4096 /* collision queries per bisection (the reference recurses without a bound) */
+#define PT_MAX_BISECT_LEVELS 100
 #define PT_MAX_LAMBERT 10000
 #define PT_MAX_SUBSEGMENTS (1 << 20) /* chord pieces of one RK step */
 #define PT_MAX_HITS_PER_SEGMENT 64   /* surfaces crossed by one chord piece */
@@ -39,6 +40,12 @@ struct DTri {           /* one triangle, 112 B */
     double a[3], b[3], c[3], n[3];
     int solid;
     int pad;
+};
+
+struct DTri32 {         /* FP32 plane of a triangle for the side pre-test, 32 B */
+    float a[3];         /* first vertex */
+    float n[3];         /* unit normal */
+    float pad[2];
 };
 
 struct DNode {          /* flattened BVH node in depth-first order, 32 B */
@@ -72,6 +79,12 @@ struct DField {
     double a0[3], inv_h[3];
     const double *node64;  /* [node][comp][8]: f, fx, fy, fz, fxy, fxz, fyz, fxyz */
     const float *node32;
+    /* mixed-precision cell table: per cell and component a linear base
+     * (f at the cell's first corner, gradient g) in FP64 and the Hermite data
+     * of the remainder f - base at the 8 corners in FP32 */
+    const double *cell64;  /* [cell][comp][4]: f0, gx, gy, gz */
+    const float *cell32;   /* [cell][comp][corner][8] */
+    const double *inv_w[3]; /* 1 / cell width per axis interval */
     double e[3];
     /* harmonic polynomial: Phi = sum c * x^i y^j z^k, B = grad Phi */
     int n_mono;
@@ -85,6 +98,7 @@ struct DScene {
     int n_tris, n_nodes, n_solids, n_fields, n_mats;
     int pad;
     const DTri *tris;
+    const DTri32 *tri32;
     const DNode *nodes;
     const DSolid *solids;
     const DMat *mats;
@@ -138,4 +152,5 @@ struct DCounters {
     unsigned long long rk_accepted, rk_rejected, rhs_evals, field_evals, hits, bisection_levels;
     unsigned long long bvh_nodes, tri_tests, subsegments, dense_evals, active, paused;
     double particle_seconds;
+    unsigned int bisect_max;
 };

@@ -14,7 +14,7 @@ namespace ptd {
 
 struct LaneCounters {
     unsigned rk_acc, rk_rej, rhs, fields, hits, bisect, subseg, dense;
-    unsigned nodes, tris;
+    unsigned nodes, tris, bisect_max;
 };
 
 struct Lane {
@@ -50,7 +50,7 @@ struct Lane {
         bc_next = 0;
         ntry = 0;
         ncand = -1;
-        lc = LaneCounters{0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        lc = LaneCounters{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     }
 
     __device__ double u01() { return uniform(R.seed, id, rn++); }
@@ -211,21 +211,21 @@ struct Lane {
             F2 += sp.q * (E[2] + yy[3] * B[1] - yy[4] * B[0]);
         }
         if (sp.mu != 0 && yy[7] != 0 && (B[0] != 0 || B[1] != 0 || B[2] != 0)) {
-            double Babs = sqrt(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
-            double g0 = (B[0] * dB[0][0] + B[1] * dB[1][0] + B[2] * dB[2][0]) / Babs;
-            double g1 = (B[0] * dB[0][1] + B[1] * dB[1][1] + B[2] * dB[2][1]) / Babs;
-            double g2 = (B[0] * dB[0][2] + B[1] * dB[1][2] + B[2] * dB[2][2]) / Babs;
+            double inv = 1.0 / sqrt(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
+            double g0 = (B[0] * dB[0][0] + B[1] * dB[1][0] + B[2] * dB[2][0]) * inv;
+            double g1 = (B[0] * dB[0][1] + B[1] * dB[1][1] + B[2] * dB[2][1]) * inv;
+            double g2 = (B[0] * dB[0][2] + B[1] * dB[1][2] + B[2] * dB[2][2]) * inv;
             F0 += yy[7] * sp.mu * g0;
             F1 += yy[7] * sp.mu * g1;
             F2 += yy[7] * sp.mu * g2;
         }
         double v2 = yy[3] * yy[3] + yy[4] * yy[4] + yy[5] * yy[5];
-        double ig = sqrt(1 - v2 / PT_C0_SQ);
-        double vF = yy[3] * F0 + yy[4] * F1 + yy[5] * F2;
+        double ig = sqrt(1 - v2 * PT_INV_C0_SQ);
+        double vF = (yy[3] * F0 + yy[4] * F1 + yy[5] * F2) * PT_INV_C0_SQ;
         double s = ig * sp.inv_mkg;
-        d[3] = s * (F0 - yy[3] * vF / PT_C0_SQ);
-        d[4] = s * (F1 - yy[4] * vF / PT_C0_SQ);
-        d[5] = s * (F2 - yy[5] * vF / PT_C0_SQ);
+        d[3] = s * (F0 - yy[3] * vF);
+        d[4] = s * (F1 - yy[4] * vF);
+        d[5] = s * (F2 - yy[5] * vF);
         d[6] = ig;
         d[7] = 0;
         d[8] = sqrt(v2);
@@ -337,36 +337,39 @@ struct Lane {
         return 1;
     }
 
-    /* runge_kutta_dopri5::calc_state: continuous extension on [to, tn] */
-    __device__ void dense_coef(double tt, double &h, double bt[6]) const {
-        const double b1 = 35.0 / 384, b3 = 500.0 / 1113, b4 = 125.0 / 192, b5 = -2187.0 / 6784, b6 = 11.0 / 84;
-        h = tn - to;
+    /* runge_kutta_dopri5::calc_state: continuous extension on [to, tn]; the
+     * weights b_i(theta) in monomial form by Horner's rule (the oracle
+     * evaluates the same expression) */
+    __device__ void dense_coef(double tt, double hb[6]) const {
+        const double W[6][5] = {
+            {1.0, -2.8605386690370884, 3.099577878709121, -1.1618105836403092, 0.013917207301610328},
+            {0.0, 4.047141499642786, -6.345354046938926, 2.795465086414005, -0.04801624082496286},
+            {0.0, -3.941160071112659, 10.904003027940295, -6.729317509209278, 0.4175162190483098},
+            {0.0, 2.8419447015870345, -7.547675862959386, 4.957636724931253, -0.5742817428041846},
+            {0.0, -1.6109886359167997, 4.218915839039518, -2.950103865566732, 0.47312904339639456},
+            {0.0, 1.523601174836727, -4.329466835790622, 3.0881301470710616, -0.2822644861171672}};
+        const double h = tn - to;
         const double th = (tt - to) / h;
-        const double X1 = 5.0 * (2558722523.0 - 31403016.0 * th) / 11282082432.0;
-        const double X3 = 100.0 * (882725551.0 - 15701508.0 * th) / 32700410799.0;
-        const double X4 = 25.0 * (443332067.0 - 31403016.0 * th) / 1880347072.0;
-        const double X5 = 32805.0 * (23143187.0 - 3489224.0 * th) / 199316789632.0;
-        const double X6 = 55.0 * (29972135.0 - 7076736.0 * th) / 822651844.0;
-        const double X7 = 10.0 * (7414447.0 - 829305.0 * th) / 29380423.0;
-        const double thm1 = th - 1.0, th2 = th * th;
-        const double A = th2 * (3.0 - 2.0 * th), B = th2 * thm1, C = th2 * thm1 * thm1, D = th * thm1 * thm1;
-        bt[0] = h * (A * b1 - C * X1 + D);
-        bt[1] = h * (A * b3 + C * X3);
-        bt[2] = h * (A * b4 - C * X4);
-        bt[3] = h * (A * b5 + C * X5);
-        bt[4] = h * (A * b6 - C * X6);
-        bt[5] = h * (B + C * X7);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            double p = W[k][4];
+            p = fma(p, th, W[k][3]);
+            p = fma(p, th, W[k][2]);
+            p = fma(p, th, W[k][1]);
+            p = fma(p, th, W[k][0]);
+            hb[k] = h * (p * th);
+        }
     }
     __device__ void calc_state(double tt, double *o) {
-        double h, b[6];
-        dense_coef(tt, h, b);
+        double b[6];
+        dense_coef(tt, b);
         for (int i = 0; i < 9; ++i)
             o[i] = fma(b[5], dyn[i], fma(b[4], k6[i], fma(b[3], k5[i], fma(b[2], k4[i], fma(b[1], k3[i], fma(b[0], dxo[i], xo[i]))))));
         ++lc.dense;
     }
     __device__ void calc_pos(double tt, double *o) {
-        double h, b[6];
-        dense_coef(tt, h, b);
+        double b[6];
+        dense_coef(tt, b);
         for (int i = 0; i < 3; ++i)
             o[i] = fma(b[5], dyn[i], fma(b[4], k6[i], fma(b[3], k5[i], fma(b[2], k4[i], fma(b[1], k3[i], fma(b[0], dxo[i], xo[i]))))));
         ++lc.dense;
@@ -377,7 +380,10 @@ struct Lane {
     __device__ int any_hit(const double *p, const double *q) {
         if (ncand >= 0) {
             bool cp = false;
+            float p32[3] = {(float)p[0], (float)p[1], (float)p[2]}, q32[3] = {(float)q[0], (float)q[1], (float)q[2]};
+            const float pm = (float)(fmax(fabs(p[0]), fabs(q[0])) + fmax(fabs(p[1]), fabs(q[1])) + fmax(fabs(p[2]), fabs(q[2])));
             for (int j = 0; j < ncand; ++j) {
+                if (same_side_f32(S.tri32[cand[j]], p32, q32, pm)) continue;
                 const DTri &t = S.tris[cand[j]];
                 if (!tri_box_touch(t, p, q)) continue;
                 ++lc.tris;
@@ -660,12 +666,15 @@ struct Lane {
     }
 
     /* TTracker::iterate_collision (src/tracking.cpp:228-265) without recursion:
-     * the path from the root is kept as choice bits and intervals are
-     * re-derived from the root when the search backtracks.  Returns 1 with
-     * the final bracket [xa, xb] (aorig/borig: bracket end is an input end),
-     * 0 when no sub-chord collides, -1 on a CGAL-error case. */
+     * a depth-first search over halves with an explicit stack of interval
+     * times (positions of stacked interval ends are recomputed from the dense
+     * output, which is deterministic).  Returns 1 with the final bracket
+     * [xa, xb] (aorig/borig: the bracket end is an input end), 0 when no
+     * sub-chord collides, -1 on a CGAL-error case or when the search exceeds
+     * its work bound. */
     __device__ int bisect(double x1, const double *p1, double x2, const double *p2, double &xa, bool &aorig, double &xb,
                           bool &borig) {
+        double stA[PT_MAX_BISECT_LEVELS + 1], stB[PT_MAX_BISECT_LEVELS + 1];
         uint64_t ch0 = 0, ch1 = 0; /* choice bit per level: 1 = second half */
         uint64_t tr0 = 0, tr1 = 0; /* second half already tried at this level */
         int level = 0;
@@ -683,9 +692,12 @@ struct Lane {
             if (dx * dx + dy * dy + dz * dz < PT_REFLECT_TOLERANCE * PT_REFLECT_TOLERANCE || B - A < 4 * (A + B) * 2.220446049250313e-16 ||
                 level >= 100) {
                 xa = A; aorig = Ao; xb = B; borig = Bo;
+                lc.bisect_max = max(lc.bisect_max, (unsigned)work);
                 return 1;
             }
             ++lc.bisect;
+            stA[level] = A;
+            stB[level] = B;
             double xc = A + (B - A) * 0.5, pc[3];
             calc_pos(xc, pc);
             if (++work > PT_MAX_BISECT_WORK) return -1;
@@ -707,21 +719,26 @@ struct Lane {
                 ++level;
                 continue;
             }
-            /* neither half collides: backtrack to the nearest level whose second half is untried */
+            /* neither half collides: back up to the nearest level whose second half is untried */
             bool resumed = false;
             while (level > 0 && !resumed) {
                 --level;
-                /* rebuild the interval of `level` from the root */
-                A = x1; B = x2; Ao = Bo = true;
-                pA[0] = p1[0]; pA[1] = p1[1]; pA[2] = p1[2];
-                pB[0] = p2[0]; pB[1] = p2[1]; pB[2] = p2[2];
-                for (int l = 0; l < level; ++l) {
-                    double m = A + (B - A) * 0.5, pm[3];
-                    calc_pos(m, pm);
-                    if (getbit(ch0, ch1, l)) { A = m; pA[0] = pm[0]; pA[1] = pm[1]; pA[2] = pm[2]; Ao = false; }
-                    else { B = m; pB[0] = pm[0]; pB[1] = pm[1]; pB[2] = pm[2]; Bo = false; }
-                }
                 if (getbit(tr0, tr1, level)) continue; /* both halves of this level done */
+                A = stA[level];
+                B = stB[level];
+                /* an interval end is an input end iff every choice above it went the same way */
+                bool allfirst = true, allsecond = true;
+                for (int l = 0; l < level; ++l) {
+                    bool c = getbit(ch0, ch1, l);
+                    allfirst = allfirst && !c;
+                    allsecond = allsecond && c;
+                }
+                Ao = allsecond;
+                Bo = allfirst;
+                if (Ao) { pA[0] = p1[0]; pA[1] = p1[1]; pA[2] = p1[2]; }
+                else calc_pos(A, pA);
+                if (Bo) { pB[0] = p2[0]; pB[1] = p2[1]; pB[2] = p2[2]; }
+                else calc_pos(B, pB);
                 double m = A + (B - A) * 0.5, pm[3];
                 calc_pos(m, pm);
                 if (++work > PT_MAX_BISECT_WORK) return -1;
@@ -735,7 +752,10 @@ struct Lane {
                     resumed = true;
                 }
             }
-            if (!resumed) return 0;
+            if (!resumed) {
+                lc.bisect_max = max(lc.bisect_max, (unsigned)work);
+                return 0;
+            }
         }
     }
 

@@ -31,6 +31,14 @@ void spline_derivs(int n, const double *x, const double *y, double *d);
  * (src/field_3d.cpp:374-381).  out[node*stride + comp*8 + k]. */
 void hermite_nodes(const std::vector<double> ax[3], const double *tab, int comp, int stride, std::vector<double> &out);
 
+/* Mixed-precision cell table from per-node Hermite data (stride ncomp*8):
+ * per cell and component a linear base (value at the cell's first corner and
+ * the mean of the 8 corner gradients) in FP64, and the Hermite data of the
+ * remainder (value minus base, first derivatives minus the base gradient,
+ * cross derivatives unchanged) at the 8 corners in FP32. */
+void mixed_cells(const std::vector<double> ax[3], const std::vector<double> &nodes, int ncomp, std::vector<double> &base,
+                 std::vector<float> &rem);
+
 /* Harmonic expansion (HarmonicExpandedBField, src/harmonicfields.cpp:50-829)
  * written as one scalar polynomial Phi with B = grad Phi.  Each G(l,m) adds
  * G * (l)! 2^|m| / (l+1+|m|)! * r^(l+1) P_(l+1)^|m|(cos theta) * {cos|m|phi (m>=0), sin|m|phi (m<0)}

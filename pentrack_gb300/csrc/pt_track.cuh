@@ -62,6 +62,23 @@ __device__ __forceinline__ double edge_orient(const double *p, const double *q, 
     if (lex_less(v, u)) return -orient3d(p, q, v, u);
     return orient3d(p, q, u, v);
 }
+/* Certified side pre-test in FP32: true when both segment ends lie strictly
+ * on the same side of the triangle's plane with a margin that covers the
+ * FP32 evaluation error (inputs rounded to FP32, dot product) and the FP64
+ * rounding of orient3d, so seg_tri would return 0 as well.  p32/q32 are the
+ * segment ends rounded to FP32; pm bounds max(|p|,|q|) componentwise sum. */
+__device__ __forceinline__ bool same_side_f32(const DTri32 &t, const float *p32, const float *q32, float pm) {
+    float dpx = p32[0] - t.a[0], dpy = p32[1] - t.a[1], dpz = p32[2] - t.a[2];
+    float dqx = q32[0] - t.a[0], dqy = q32[1] - t.a[1], dqz = q32[2] - t.a[2];
+    float sp = t.n[0] * dpx + t.n[1] * dpy + t.n[2] * dpz;
+    float sq = t.n[0] * dqx + t.n[1] * dqy + t.n[2] * dqz;
+    float am = fabsf(t.a[0]) + fabsf(t.a[1]) + fabsf(t.a[2]);
+    float lp = fabsf(dpx) + fabsf(dpy) + fabsf(dpz), lq = fabsf(dqx) + fabsf(dqy) + fabsf(dqz);
+    const float E = 1.2e-6f; /* ~10 FP32 ulps */
+    float bp = E * (pm + am + lp) + 1e-12f, bq = E * (pm + am + lq) + 1e-12f;
+    return (sp > bp && sq > bq) || (sp < -bp && sq < -bq);
+}
+
 /* closed segment x closed triangle: 1 hit (parameter s), 0 none, -1 coplanar */
 __device__ __forceinline__ int seg_tri(const double *p, const double *q, const DTri &t, double &s) {
     double dp = orient3d(t.a, t.b, t.c, p), dq = orient3d(t.a, t.b, t.c, q);
@@ -218,64 +235,89 @@ __device__ void hermite_cell(const T *__restrict__ nodes, int ncomp, int c0, int
     }
 }
 
-/* Mixed-precision cell evaluation (PT_PREC_FP32): the terms of the corner
- * values f, which carry the magnitude of B and whose differences make the
- * gradient, are summed in FP64; the terms of the corner derivatives
- * (fx .. fxyz, scaled by the cell size) are summed in FP32 and added.  The
- * FP32 rounding then acts on the small derivative terms only: ~1e-7 of the
- * field's gradient scale instead of ~1e-5 for an all-FP32 evaluation, below
- * the noise the 1e-9 step-size controller reacts to. */
+/* Mixed-precision cell evaluation (PT_PREC_FP32).  Within a cell the field is
+ * split exactly into a linear base L(x) = f0 + g.(x - x0) (f0: value at the
+ * cell's first corner, g: mean corner gradient), evaluated in FP64, and the
+ * remainder f - L, whose corner Hermite data were formed in FP64 on the host
+ * and stored in FP32; its tricubic is evaluated in FP32.  The remainder is
+ * O(h^2 f'') small (zero for a linear field), so the FP32 rounding stays
+ * ~1e-7 of a small quantity and the force is smooth to the 1e-9 step-size
+ * controller. */
 template <bool GRAD>
-__device__ void hermite_cell_mixed(const DField &f, int ix, int iy, int iz, double u, double v, double w, double hx, double hy,
-                                   double hz, double *F, double (*dF)[3]) {
-    Herm<float> Uf, Vf, Wf;
-    Uf.set((float)u, (float)hx, (float)(1.0 / hx));
-    Vf.set((float)v, (float)hy, (float)(1.0 / hy));
-    Wf.set((float)w, (float)hz, (float)(1.0 / hz));
-    double F32[3], dF32[3][3];
-    hermite_cell<float, GRAD, true>(f.node32, f.ncomp, 0, 3, f.n, ix, iy, iz, Uf, Vf, Wf, F32, dF32);
-    /* cubic Hermite value weights h00 = 2t^3 - 3t^2 + 1, h01 = 3t^2 - 2t^3 and slopes */
-    double uw[2], vw[2], ww[2], ud[2], vd[2], wd[2];
+__device__ void tab3_mixed(const DField &f, int c0, int nc, double x, double y, double z, double *F, double (*dF)[3]) {
+    int ix, iy, iz;
+    double u, v, w;
     {
-        double t2 = u * u, t3 = t2 * u;
-        uw[0] = 2 * t3 - 3 * t2 + 1; uw[1] = 3 * t2 - 2 * t3;
-        ud[0] = (6 * t2 - 6 * u) / hx; ud[1] = (6 * u - 6 * t2) / hx;
-        t2 = v * v; t3 = t2 * v;
-        vw[0] = 2 * t3 - 3 * t2 + 1; vw[1] = 3 * t2 - 2 * t3;
-        vd[0] = (6 * t2 - 6 * v) / hy; vd[1] = (6 * v - 6 * t2) / hy;
-        t2 = w * w; t3 = t2 * w;
-        ww[0] = 2 * t3 - 3 * t2 + 1; ww[1] = 3 * t2 - 2 * t3;
-        wd[0] = (6 * t2 - 6 * w) / hz; wd[1] = (6 * w - 6 * t2) / hz;
+        const double r[3] = {x, y, z};
+        int idx[3];
+        double loc[3];
+        for (int a = 0; a < 3; ++a) {
+            const double *ax = f.ax[a];
+            const int n = f.n[a];
+            double g = (r[a] - f.a0[a]) * f.inv_h[a];
+            int k;
+            if (!(g > -1.0)) k = 0;
+            else if (!(g < (double)n)) k = n;
+            else k = (int)floor(g) + 1;
+            while (k < n && ax[k] <= r[a]) ++k;
+            while (k > 0 && ax[k - 1] > r[a]) --k;
+            if (k >= n || k == 0) return;
+            idx[a] = k - 1;
+            loc[a] = (r[a] - ax[k - 1]) * f.inv_w[a][k - 1];
+        }
+        ix = idx[0]; iy = idx[1]; iz = idx[2];
+        u = loc[0]; v = loc[1]; w = loc[2];
     }
-    const int64_t sz = f.n[2], sy = (int64_t)f.n[1] * f.n[2];
-    const int64_t base = ((int64_t)ix * f.n[1] + iy) * f.n[2] + iz;
-    const int stride = f.ncomp * 8;
-    double a[3] = {0, 0, 0}, gx[3] = {0, 0, 0}, gy[3] = {0, 0, 0}, gz[3] = {0, 0, 0};
+    const double hx = f.ax[0][ix + 1] - f.ax[0][ix], hy = f.ax[1][iy + 1] - f.ax[1][iy], hz = f.ax[2][iz + 1] - f.ax[2][iz];
+    Herm<float> U, V, W;
+    U.set((float)u, (float)hx, (float)f.inv_w[0][ix]);
+    V.set((float)v, (float)hy, (float)f.inv_w[1][iy]);
+    W.set((float)w, (float)hz, (float)f.inv_w[2][iz]);
+    const int64_t cell = ((int64_t)ix * (f.n[1] - 1) + iy) * (f.n[2] - 1) + iz;
+    const float *cd = f.cell32 + cell * f.ncomp * 64;
+    const double *cb = f.cell64 + cell * f.ncomp * 4;
+    const double dx = x - f.ax[0][ix], dy = y - f.ax[1][iy], dz = z - f.ax[2][iz];
+    const int dtab[2][2][2] = {{{0, 3}, {2, 6}}, {{1, 5}, {4, 7}}};
+    for (int c = c0; c < c0 + nc; ++c) {
+        const float *cc = cd + c * 64;
+        float fr = 0, fx = 0, fy = 0, fz = 0;
 #pragma unroll
-    for (int cx = 0; cx < 2; ++cx)
+        for (int cx = 0; cx < 2; ++cx)
 #pragma unroll
-        for (int cy = 0; cy < 2; ++cy)
+            for (int ax_ = 0; ax_ < 2; ++ax_) {
+                const int p = cx + 2 * ax_;
+                float tp = 0, typ = 0, tzp = 0;
 #pragma unroll
-            for (int cz = 0; cz < 2; ++cz) {
-                const double *nd = f.node64 + (base + cx * sy + cy * sz + cz) * stride;
-                const double wv = uw[cx] * vw[cy] * ww[cz];
-                const double wx = ud[cx] * vw[cy] * ww[cz], wy = uw[cx] * vd[cy] * ww[cz], wz = uw[cx] * vw[cy] * wd[cz];
-                for (int c = 0; c < 3; ++c) {
-                    const double val = nd[c * 8];
-                    a[c] = fma(val, wv, a[c]);
-                    if (GRAD) {
-                        gx[c] = fma(val, wx, gx[c]);
-                        gy[c] = fma(val, wy, gy[c]);
-                        gz[c] = fma(val, wz, gz[c]);
+                for (int cy = 0; cy < 2; ++cy) {
+                    const float *n0 = cc + (cx + 2 * cy) * 8;  /* corner (cx, cy, 0) */
+                    const float *n1 = n0 + 4 * 8;             /* corner (cx, cy, 1) */
+#pragma unroll
+                    for (int ay = 0; ay < 2; ++ay) {
+                        const int q = cy + 2 * ay;
+                        const int d0 = dtab[ax_][ay][0], d1 = dtab[ax_][ay][1];
+                        const float v0 = n0[d0], v1 = n1[d0], v2 = n0[d1], v3 = n1[d1];
+                        const float sv = fmaf(v3, W.w[3], fmaf(v2, W.w[2], fmaf(v1, W.w[1], v0 * W.w[0])));
+                        tp = fmaf(sv, V.w[q], tp);
+                        if (GRAD) {
+                            const float sp = fmaf(v3, W.dw[3], fmaf(v2, W.dw[2], fmaf(v1, W.dw[1], v0 * W.dw[0])));
+                            typ = fmaf(sv, V.dw[q], typ);
+                            tzp = fmaf(sp, V.w[q], tzp);
+                        }
                     }
                 }
+                fr = fmaf(tp, U.w[p], fr);
+                if (GRAD) {
+                    fx = fmaf(tp, U.dw[p], fx);
+                    fy = fmaf(typ, U.w[p], fy);
+                    fz = fmaf(tzp, U.w[p], fz);
+                }
             }
-    for (int c = 0; c < 3; ++c) {
-        F[c] = a[c] + F32[c];
+        const double *b = cb + c * 4;
+        F[c - c0] = fma(b[3], dz, fma(b[2], dy, fma(b[1], dx, b[0]))) + (double)fr;
         if (GRAD) {
-            dF[c][0] = gx[c] + dF32[c][0];
-            dF[c][1] = gy[c] + dF32[c][1];
-            dF[c][2] = gz[c] + dF32[c][2];
+            dF[c - c0][0] = b[1] + (double)fx;
+            dF[c - c0][1] = b[2] + (double)fy;
+            dF[c - c0][2] = b[3] + (double)fz;
         }
     }
 }
@@ -283,12 +325,14 @@ __device__ void hermite_cell_mixed(const DField &f, int ix, int iy, int iz, doub
 /* TabField3 B (and gradient) of one field; outputs untouched outside the grid */
 template <bool GRAD>
 __device__ void tab3_b(const DField &f, int prec, double x, double y, double z, double B[3], double (*dB)[3]) {
+    if (prec == PT_PREC_FP32 && f.cell32) {
+        tab3_mixed<GRAD>(f, 0, 3, x, y, z, B, dB);
+        return;
+    }
     int ix, iy, iz;
     double u, v, w, hx, hy, hz;
     if (!locate(f, 0, x, ix, u, hx) || !locate(f, 1, y, iy, v, hy) || !locate(f, 2, z, iz, w, hz)) return;
-    if (prec == PT_PREC_FP32 && f.node32) {
-        hermite_cell_mixed<GRAD>(f, ix, iy, iz, u, v, w, hx, hy, hz, B, dB);
-    } else {
+    {
         Herm<double> U, V, W;
         U.set(u, hx, 1.0 / hx);
         V.set(v, hy, 1.0 / hy);
@@ -299,17 +343,13 @@ __device__ void tab3_b(const DField &f, int prec, double x, double y, double z, 
 
 /* TabField3 potential V and E = -grad V */
 __device__ void tab3_v(const DField &f, int prec, double x, double y, double z, double &Vv, double E[3]) {
-    int ix, iy, iz;
-    double u, v, w, hx, hy, hz;
-    if (!locate(f, 0, x, ix, u, hx) || !locate(f, 1, y, iy, v, hy) || !locate(f, 2, z, iz, w, hz)) return;
-    double F[1], dF[1][3];
-    if (prec == PT_PREC_FP32 && f.node32) {
-        Herm<float> U, V, W;
-        U.set((float)u, (float)hx, (float)(1.0 / hx));
-        V.set((float)v, (float)hy, (float)(1.0 / hy));
-        W.set((float)w, (float)hz, (float)(1.0 / hz));
-        hermite_cell<float, true>(f.node32, f.ncomp, 3, 1, f.n, ix, iy, iz, U, V, W, F, dF);
+    double F[1] = {Vv}, dF[1][3] = {{0, 0, 0}};
+    if (prec == PT_PREC_FP32 && f.cell32) {
+        tab3_mixed<true>(f, 3, 1, x, y, z, F, dF);
     } else {
+        int ix, iy, iz;
+        double u, v, w, hx, hy, hz;
+        if (!locate(f, 0, x, ix, u, hx) || !locate(f, 1, y, iy, v, hy) || !locate(f, 2, z, iz, w, hz)) return;
         Herm<double> U, V, W;
         U.set(u, hx, 1.0 / hx);
         V.set(v, hy, 1.0 / hy);
@@ -536,6 +576,8 @@ __device__ int mesh_query(const DScene &S, const double *p, const double *q, dou
     coplanar = false;
     int i = 0;
     const int nn = S.n_nodes;
+    float p32[3] = {(float)p[0], (float)p[1], (float)p[2]}, q32[3] = {(float)q[0], (float)q[1], (float)q[2]};
+    const float pm = (float)(fmax(fabs(p[0]), fabs(q[0])) + fmax(fabs(p[1]), fabs(q[1])) + fmax(fabs(p[2]), fabs(q[2])));
     while (i < nn) {
         const DNode nd = S.nodes[i];
         ++qs.nodes;
@@ -545,6 +587,7 @@ __device__ int mesh_query(const DScene &S, const double *p, const double *q, dou
         if (nd.leaf < 0) { ++i; continue; }
         int first = nd.leaf >> 3, cnt = nd.leaf & 7;
         for (int j = first; j < first + cnt; ++j) {
+            if (same_side_f32(S.tri32[j], p32, q32, pm)) continue;
             const DTri &t = S.tris[j];
             if (MODE != 2 && !tri_box_touch(t, p, q)) continue;
             ++qs.tris;
