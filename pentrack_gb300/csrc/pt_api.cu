@@ -400,8 +400,16 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
         /* FP32 planes for the side pre-test, in BVH triangle order */
         std::vector<DTri32> t32(tris.size());
         for (size_t k = 0; k < tris.size(); ++k) {
-            for (int a = 0; a < 3; ++a) { t32[k].a[a] = (float)tris[k].a[a]; t32[k].n[a] = (float)tris[k].n[a]; }
-            t32[k].pad[0] = t32[k].pad[1] = 0;
+            double m = 0;
+            for (int a = 0; a < 3; ++a) {
+                t32[k].a[a] = (float)tris[k].a[a];
+                t32[k].b[a] = (float)tris[k].b[a];
+                t32[k].c[a] = (float)tris[k].c[a];
+                t32[k].n[a] = (float)tris[k].n[a];
+                m = std::max(m, std::max(std::fabs(tris[k].a[a]), std::max(std::fabs(tris[k].b[a]), std::fabs(tris[k].c[a]))));
+            }
+            t32[k].m = std::nextafter((float)m, INFINITY);
+            t32[k].pad[0] = t32[k].pad[1] = t32[k].pad[2] = 0;
         }
         S.tri32 = dupload(c->allocs, t32.data(), t32.size(), e);
         if (e) return ck(c, e, "upload triangle planes"), PT_ERR_CUDA;

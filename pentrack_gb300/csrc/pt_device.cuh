@@ -42,10 +42,11 @@ struct DTri {           /* one triangle, 112 B */
     int pad;
 };
 
-struct DTri32 {         /* FP32 plane of a triangle for the side pre-test, 32 B */
-    float a[3];         /* first vertex */
-    float n[3];         /* unit normal */
-    float pad[2];
+struct DTri32 {         /* FP32 copy of a triangle for certified pre-tests, 64 B */
+    float a[3], b[3], c[3]; /* vertices rounded to nearest */
+    float n[3];             /* unit normal */
+    float m;                /* max |coordinate| of the FP64 vertices, rounded up */
+    float pad[3];
 };
 
 struct DNode {          /* flattened BVH node in depth-first order, 32 B */

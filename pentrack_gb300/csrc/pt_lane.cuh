@@ -380,10 +380,12 @@ struct Lane {
     __device__ int any_hit(const double *p, const double *q) {
         if (ncand >= 0) {
             bool cp = false;
-            float p32[3] = {(float)p[0], (float)p[1], (float)p[2]}, q32[3] = {(float)q[0], (float)q[1], (float)q[2]};
-            const float pm = (float)(fmax(fabs(p[0]), fabs(q[0])) + fmax(fabs(p[1]), fabs(q[1])) + fmax(fabs(p[2]), fabs(q[2])));
+            Seg32 s32;
+            seg32_make(p, q, s32);
             for (int j = 0; j < ncand; ++j) {
-                if (same_side_f32(S.tri32[cand[j]], p32, q32, pm)) continue;
+                const int r32 = seg_tri32(s32, S.tri32[cand[j]]);
+                if (r32 == 0) continue;
+                if (r32 == 1) return 1;
                 const DTri &t = S.tris[cand[j]];
                 if (!tri_box_touch(t, p, q)) continue;
                 ++lc.tris;

@@ -62,21 +62,71 @@ __device__ __forceinline__ double edge_orient(const double *p, const double *q, 
     if (lex_less(v, u)) return -orient3d(p, q, v, u);
     return orient3d(p, q, u, v);
 }
-/* Certified side pre-test in FP32: true when both segment ends lie strictly
- * on the same side of the triangle's plane with a margin that covers the
- * FP32 evaluation error (inputs rounded to FP32, dot product) and the FP64
- * rounding of orient3d, so seg_tri would return 0 as well.  p32/q32 are the
- * segment ends rounded to FP32; pm bounds max(|p|,|q|) componentwise sum. */
-__device__ __forceinline__ bool same_side_f32(const DTri32 &t, const float *p32, const float *q32, float pm) {
-    float dpx = p32[0] - t.a[0], dpy = p32[1] - t.a[1], dpz = p32[2] - t.a[2];
-    float dqx = q32[0] - t.a[0], dqy = q32[1] - t.a[1], dqz = q32[2] - t.a[2];
-    float sp = t.n[0] * dpx + t.n[1] * dpy + t.n[2] * dpz;
-    float sq = t.n[0] * dqx + t.n[1] * dqy + t.n[2] * dqz;
-    float am = fabsf(t.a[0]) + fabsf(t.a[1]) + fabsf(t.a[2]);
-    float lp = fabsf(dpx) + fabsf(dpy) + fabsf(dpz), lq = fabsf(dqx) + fabsf(dqy) + fabsf(dqz);
-    const float E = 1.2e-6f; /* ~10 FP32 ulps */
-    float bp = E * (pm + am + lp) + 1e-12f, bq = E * (pm + am + lq) + 1e-12f;
-    return (sp > bp && sq > bq) || (sp < -bp && sq < -bq);
+/* ---------------------------------------------------------------- */
+/* Certified FP32 segment-triangle decisions.  The FP64 test seg_tri  */
+/* decides from signs of orient3d determinants.  Each sign is first  */
+/* computed in FP32 from inputs rounded to FP32, with a bound on its  */
+/* error: moving each point by at most d = 2^-23 M per coordinate     */
+/* (M = max |coordinate|) changes 6x the tetrahedron volume by at     */
+/* most 2 d (sum of products of its edge lengths); the FP32           */
+/* arithmetic adds at most 16 eps32 x the permanent; the FP64         */
+/* rounding of seg_tri's own determinant is far below both.  A sign   */
+/* whose magnitude exceeds twice that bound equals the exact sign and */
+/* hence seg_tri's FP64 sign, so decided cases need no FP64 work.     */
+/* ---------------------------------------------------------------- */
+struct Seg32 {
+    float p[3], q[3];
+    float m; /* max |coordinate| of p, q (FP64 values), rounded up */
+};
+__device__ __forceinline__ void seg32_make(const double *p, const double *q, Seg32 &s) {
+    double m = 0;
+    for (int k = 0; k < 3; ++k) {
+        s.p[k] = (float)p[k];
+        s.q[k] = (float)q[k];
+        m = fmax(m, fmax(fabs(p[k]), fabs(q[k])));
+    }
+    s.m = __double2float_ru(m);
+}
+/* orient3d(a, b, c, d) in FP32 with its certification bound; returns the
+ * sign (+1/-1) when certain, 0 otherwise */
+__device__ __forceinline__ int orient_sign32(const float *a, const float *b, const float *c, const float *d, float M) {
+    const float adx = a[0] - d[0], bdx = b[0] - d[0], cdx = c[0] - d[0];
+    const float ady = a[1] - d[1], bdy = b[1] - d[1], cdy = c[1] - d[1];
+    const float adz = a[2] - d[2], bdz = b[2] - d[2], cdz = c[2] - d[2];
+    const float bc = bdy * cdz - bdz * cdy, ca = cdy * adz - cdz * ady, ab = ady * bdz - adz * bdy;
+    const float det = adx * bc + bdx * ca + cdx * ab;
+    const float perm = fabsf(adx) * (fabsf(bdy * cdz) + fabsf(bdz * cdy)) + fabsf(bdx) * (fabsf(cdy * adz) + fabsf(cdz * ady)) +
+                       fabsf(cdx) * (fabsf(ady * bdz) + fabsf(adz * bdy));
+    const float la = fabsf(adx) + fabsf(ady) + fabsf(adz), lb = fabsf(bdx) + fabsf(bdy) + fabsf(bdz),
+                lc = fabsf(cdx) + fabsf(cdy) + fabsf(cdz);
+    const float lab = fabsf(bdx - adx) + fabsf(bdy - ady) + fabsf(bdz - adz);
+    const float lac = fabsf(cdx - adx) + fabsf(cdy - ady) + fabsf(cdz - adz);
+    const float d_in = 2.4e-7f * M; /* 2 x 2^-23 M: rounding of the inputs, with slack */
+    const float s2 = lb * lc + la * lc + la * lb + lab * lac;
+    const float bound = 2.0f * (2.0f * d_in * s2 + 2.0e-6f * perm) + 1e-30f;
+    if (det > bound) return 1;
+    if (det < -bound) return -1;
+    return 0;
+}
+/* 1: certainly a point hit, 0: certainly no hit, -1: undecided (use seg_tri) */
+__device__ __forceinline__ int seg_tri32(const Seg32 &s, const DTri32 &t) {
+    const float M = fmaxf(s.m, t.m);
+    const int sp = orient_sign32(t.a, t.b, t.c, s.p, M), sq = orient_sign32(t.a, t.b, t.c, s.q, M);
+    if (sp != 0 && sp == sq) return 0;         /* both ends strictly on one side */
+    if (sp == 0 || sq == 0) return -1;
+    /* the segment crosses the plane: the edge signs decide (canonical edge order as in edge_orient) */
+    const float *v[3] = {t.a, t.b, t.c};
+    int e[3];
+    for (int k = 0; k < 3; ++k) {
+        const float *u = v[k], *w = v[(k + 1) % 3];
+        bool swap = (w[0] < u[0]) || (w[0] == u[0] && (w[1] < u[1] || (w[1] == u[1] && w[2] < u[2])));
+        int sg = swap ? -orient_sign32(s.p, s.q, w, u, M) : orient_sign32(s.p, s.q, u, w, M);
+        e[k] = sg;
+    }
+    bool neg = (e[0] < 0) || (e[1] < 0) || (e[2] < 0), pos = (e[0] > 0) || (e[1] > 0) || (e[2] > 0);
+    if (neg && pos) return 0;                  /* certainly outside */
+    if (e[0] != 0 && e[1] != 0 && e[2] != 0) return 1; /* certainly inside */
+    return -1;
 }
 
 /* closed segment x closed triangle: 1 hit (parameter s), 0 none, -1 coplanar */
@@ -576,8 +626,8 @@ __device__ int mesh_query(const DScene &S, const double *p, const double *q, dou
     coplanar = false;
     int i = 0;
     const int nn = S.n_nodes;
-    float p32[3] = {(float)p[0], (float)p[1], (float)p[2]}, q32[3] = {(float)q[0], (float)q[1], (float)q[2]};
-    const float pm = (float)(fmax(fabs(p[0]), fabs(q[0])) + fmax(fabs(p[1]), fabs(q[1])) + fmax(fabs(p[2]), fabs(q[2])));
+    Seg32 s32;
+    seg32_make(p, q, s32);
     while (i < nn) {
         const DNode nd = S.nodes[i];
         ++qs.nodes;
@@ -587,7 +637,9 @@ __device__ int mesh_query(const DScene &S, const double *p, const double *q, dou
         if (nd.leaf < 0) { ++i; continue; }
         int first = nd.leaf >> 3, cnt = nd.leaf & 7;
         for (int j = first; j < first + cnt; ++j) {
-            if (same_side_f32(S.tri32[j], p32, q32, pm)) continue;
+            const int r32 = seg_tri32(s32, S.tri32[j]);
+            if (r32 == 0) continue;
+            if (MODE == 0 && r32 == 1) return 1; /* a certain hit ends an any-hit query */
             const DTri &t = S.tris[j];
             if (MODE != 2 && !tri_box_touch(t, p, q)) continue;
             ++qs.tris;
