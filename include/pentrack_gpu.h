@@ -199,6 +199,8 @@ typedef struct pt_stats {
     char dominant_kernel[48];
     double try_ms, post_ms, slow_ms; /* batched form: device time per phase kernel */
     int64_t bisect_max;        /* largest number of collision queries of one bisection */
+    int64_t cand_calls, cand_overflow, cand_sum; /* candidate-triangle sets built for bisections */
+    int64_t tri32_tests;       /* FP32 certified segment-triangle tests */
 } pt_stats;
 
 typedef struct pt_ctx pt_ctx;

@@ -88,6 +88,7 @@ class Stats(C.Structure):
         ("dominant_kernel_ms", C.c_double), ("dominant_launches", C.c_int64), ("dominant_kernel", C.c_char * 48),
         ("try_ms", C.c_double), ("post_ms", C.c_double), ("slow_ms", C.c_double),
         ("bisect_max", C.c_int64),
+        ("cand_calls", C.c_int64), ("cand_overflow", C.c_int64), ("cand_sum", C.c_int64), ("tri32_tests", C.c_int64),
     ]
 
     def as_dict(self):

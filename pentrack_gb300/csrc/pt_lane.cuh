@@ -15,6 +15,7 @@ namespace ptd {
 struct LaneCounters {
     unsigned rk_acc, rk_rej, rhs, fields, hits, bisect, subseg, dense;
     unsigned nodes, tris, bisect_max;
+    unsigned cand_calls, cand_overflow, cand_sum, tri32;
 };
 
 struct Lane {
@@ -50,7 +51,7 @@ struct Lane {
         bc_next = 0;
         ntry = 0;
         ncand = -1;
-        lc = LaneCounters{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        lc = LaneCounters{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     }
 
     __device__ double u01() { return uniform(R.seed, id, rn++); }
@@ -383,6 +384,7 @@ struct Lane {
             Seg32 s32;
             seg32_make(p, q, s32);
             for (int j = 0; j < ncand; ++j) {
+                ++lc.tri32;
                 const int r32 = seg_tri32(s32, S.tri32[cand[j]]);
                 if (r32 == 0) continue;
                 if (r32 == 1) return 1;
@@ -501,6 +503,9 @@ struct Lane {
         QueryStats qs{0, 0};
         ncand = collect_candidates(S, lo, hi, cand, PT_MAX_CAND, qs);
         lc.nodes += qs.nodes;
+        ++lc.cand_calls;
+        if (ncand < 0) ++lc.cand_overflow;
+        else lc.cand_sum += ncand;
     }
 
     /* ---------------- RotateVector (src/globals.cpp:40-64) ---------------- */
