@@ -155,8 +155,9 @@ __global__ void __launch_bounds__(128) k_post(const __grid_constant__ DScene S, 
     flush_counters(C, L.lc, ps, false);
 }
 
-/* Batched form, phase 3: full post-step logic (chord split, bisection, hit
- * physics, clipping) for the queued steps. */
+/* Batched form, phase 3: the full post-step logic (chord split, CheckHit,
+ * hit physics, clipping) for the queued steps, run until the step completes
+ * or needs a bisection; those post-steps are suspended and queued for k_bisect. */
 __global__ void __launch_bounds__(128) k_slow(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out) {
     const int n = b.count[3];
     const int32_t *ls = b.list[3];
@@ -167,15 +168,40 @@ __global__ void __launch_bounds__(128) k_slow(const __grid_constant__ DScene S, 
         L.load(b, i);
         L.load_dense(b, i);
         L.load_bc(b, i);
+        if (L.flags & PT_F_SUSPENDED) L.load_post(b, i);
+        else L.ps.stage = PS_BEGIN;
+        L.flags &= ~(PT_F_PENDING | PT_F_SUSPENDED);
         const double t0 = L.t;
-        L.flags &= ~PT_F_PENDING;
-        L.post_step();
+        if (L.post_resume()) {
+            L.flags |= PT_F_PENDING | PT_F_SUSPENDED;
+            L.store_post(b, i);
+            L.store(b, i);
+            list_push(b.list[4], &b.count[4], i);
+            continue;
+        }
         ps += L.t - t0;
         L.store_bc_commit(b, i);
         L.store(b, i);
         if (keeps_going(R, b, L, i)) list_push(b.list[out], &b.count[out], i);
     }
     flush_counters(C, L.lc, ps, false);
+}
+
+/* Batched form, phase 4: the bisections (TTracker::iterate_collision) that
+ * suspended post-steps asked for; every lane runs the same search loop.  The
+ * post-steps go back to the slow list. */
+__global__ void __launch_bounds__(128) k_bisect(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C) {
+    const int n = b.count[4];
+    const int32_t *lq = b.list[4];
+    Lane L(S, R);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = lq[k];
+        L.load_bisect_request(b, i);
+        L.ps.bres = L.bisect(L.ps.cx1, L.ps.cya, L.ps.x2, L.ps.y2, L.ps.bxa, L.ps.bao, L.ps.bxb, L.ps.bbo);
+        L.store_bisect_result(b, i);
+        list_push(b.list[3], &b.count[3], i);
+    }
+    flush_counters(C, L.lc, 0.0, false);
 }
 
 /* Plain form: every lane advances its particle by up to `steps` LOOP-A
@@ -531,12 +557,13 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
     const int g_try = persistent_grid(c, (const void *)k_try, block);
     const int g_post = persistent_grid(c, (const void *)k_post, block);
     const int g_slow = persistent_grid(c, (const void *)k_slow, block);
+    const int g_bisect = persistent_grid(c, (const void *)k_bisect, block);
     if ((e = cudaMemsetAsync(b.count, 0, 8 * sizeof(int32_t), c->stream))) return ck(c, e, "counts"), PT_ERR_CUDA;
     k_gather<<<grid_for(n, 256), 256, 0, c->stream>>>(b, R.t_pause, b.list[0], &b.count[0]);
     if ((e = cudaGetLastError())) return ck(c, e, "gather"), PT_ERR_CUDA;
     cudaEvent_t ev[6];
     for (int k = 0; k < 6; ++k) cudaEventCreate(&ev[k]);
-    double t_try = 0, t_post = 0, t_slow = 0;
+    double t_try = 0, t_post = 0, t_slow = 0, t_bisect = 0;
     int64_t l_try = 0;
     int32_t *hcount = nullptr;
     cudaHostAlloc((void **)&hcount, 8 * sizeof(int32_t), 0);
@@ -567,24 +594,31 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
         acc.kernel_ms += a + bb;
         acc.launches += 2;
         int active = hcount[out], slow = hcount[3];
-        const int thresh = std::max(2048, active / 4);
-        if (slow > 0 && (slow >= thresh || active == 0)) {
+        /* rounds of k_slow (each queued post-step runs to its end or to its
+         * next bisection) and k_bisect, while the queue fills the GPU */
+        while (slow > 0 && (slow >= std::max(2048, active / 4) || active == 0)) {
             cudaEventRecord(ev[3], c->stream);
             k_slow<<<g_slow, block, 0, c->stream>>>(c->scene, R, b, c->counters, out);
             cudaEventRecord(ev[4], c->stream);
             k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 3, 3, 3);
+            k_bisect<<<g_bisect, block, 0, c->stream>>>(c->scene, R, b, c->counters);
+            cudaEventRecord(ev[5], c->stream);
+            k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 4, 4, 4);
             if ((e = cudaGetLastError())) { st = ck(c, e, "k_slow launch"), PT_ERR_CUDA; break; }
             cudaMemcpyAsync(hcount, b.count, 8 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
             if ((e = cudaStreamSynchronize(c->stream))) { st = ck(c, e, "k_slow"), PT_ERR_CUDA; break; }
-            float cc = 0;
+            float cc = 0, cb = 0;
             cudaEventElapsedTime(&cc, ev[3], ev[4]);
+            cudaEventElapsedTime(&cb, ev[4], ev[5]);
             t_slow += cc;
+            t_bisect += cb;
             ++l_slow;
-            acc.kernel_ms += cc;
-            acc.launches += 1;
+            acc.kernel_ms += cc + cb;
+            acc.launches += 2;
             active = hcount[out];
-            slow = 0;
+            slow = hcount[3];
         }
+        if (st != PT_OK) break;
         cudaMemcpy(c->counters_host, c->counters, sizeof(DCounters), cudaMemcpyDeviceToHost);
         add_counters(acc, *c->counters_host);
         acc.active = active + slow;
@@ -602,12 +636,14 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
     double dom = t_try;
     if (t_post > dom) { dom = t_post; name = "k_post"; }
     if (t_slow > dom) { dom = t_slow; name = "k_slow"; }
+    if (t_bisect > dom) { dom = t_bisect; name = "k_bisect"; }
     acc.dominant_kernel_ms = dom;
-    acc.dominant_launches = (dom == t_slow) ? l_slow : l_try;
+    acc.dominant_launches = (dom == t_slow || dom == t_bisect) ? l_slow : l_try;
     std::snprintf(acc.dominant_kernel, sizeof(acc.dominant_kernel), "%s", name);
     acc.try_ms = t_try;
     acc.post_ms = t_post;
     acc.slow_ms = t_slow;
+    acc.bisect_ms = t_bisect;
     return st;
 }
 
@@ -712,7 +748,8 @@ pt_status pt_batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles 
     ALLOC(rng_n, uint64_t, n) ALLOC(nacc, int64_t, n) ALLOC(nrej, int64_t, n) ALLOC(ntry, int32_t, n)
     ALLOC(yn, double, 9 * n) ALLOC(dyn, double, 9 * n) ALLOC(kst, double, 36 * n) ALLOC(tn, double, n)
     ALLOC(bc, double, 14 * n) ALLOC(count, int32_t, 8) ALLOC(nacc0, int64_t, n)
-    for (int k = 0; k < 4; ++k) { b.list[k] = dalloc<int32_t>(B->allocs, (size_t)n, e); if (e) { free_list(B->allocs); return ck(c, e, "batch alloc"), PT_ERR_OOM; } }
+    ALLOC(ps_d, double, 42 * n) ALLOC(ps_i, int32_t, (7 + PT_MAX_CAND) * n)
+    for (int k = 0; k < 5; ++k) { b.list[k] = dalloc<int32_t>(B->allocs, (size_t)n, e); if (e) { free_list(B->allocs); return ck(c, e, "batch alloc"), PT_ERR_OOM; } }
 #undef ALLOC
     if (n > 0) {
         if ((e = cudaMemcpyAsync(b.id, in->id, n * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream)) ||

@@ -29,7 +29,7 @@
 #define PT_MAX_LAMBERT 10000
 #define PT_MAX_SUBSEGMENTS (1 << 20) /* chord pieces of one RK step */
 #define PT_MAX_HITS_PER_SEGMENT 64   /* surfaces crossed by one chord piece */
-#define PT_MAX_CAND 8                /* candidate triangles kept for a bisection */
+#define PT_MAX_CAND 16               /* candidate triangles kept for a bisection */
 
 /* lane flags */
 #define PT_F_DERIV 1u   /* FSAL derivative valid */
@@ -139,14 +139,18 @@ struct DBatch {
     /* phase-split form: result of the last accepted try and B-value caches */
     double *yn, *dyn, *kst, *tn; /* yn, dyn: 9n; kst: k3..k6, 36n; tn: n */
     double *bc;                  /* 2 slots x (x, y, z, t, Bx, By, Bz): 14n */
+    /* suspended post-steps: 42 doubles and 7 + PT_MAX_CAND ints per particle */
+    double *ps_d;
+    int32_t *ps_i;
     /* work lists of particle indices and their counts */
-    int32_t *list[4];            /* 0/1: active (ping-pong), 2: post, 3: slow */
-    int32_t *count;              /* 4 counts */
+    int32_t *list[5];            /* 0/1: active (ping-pong), 2: post, 3: slow, 4: bisection */
+    int32_t *count;              /* counts of the lists */
 };
 
 #define PT_F_BC0 8u   /* cache slot 0 valid */
 #define PT_F_BC1 16u  /* cache slot 1 valid */
 #define PT_F_PENDING 32u /* an accepted try waits for the full post-step logic */
+#define PT_F_SUSPENDED 64u /* that post-step is suspended at a bisection (state in ps_d/ps_i) */
 
 /* device event counters (one set per launch, summed with atomics per block) */
 struct DCounters {

@@ -18,6 +18,19 @@ struct LaneCounters {
     unsigned cand_calls, cand_overflow, cand_sum, tri32;
 };
 
+/* Resumable state of one post-step (the remainder of LOOP A after an accepted
+ * try) while a bisection runs: the chord-piece loop (x1, x, x2 and states),
+ * the CheckHit loop position (cx1, cya, cs, pass) and the bisection request
+ * and result. */
+struct PostState {
+    double x1, x, x2, cx1;
+    double y1[9], yl[9], y2[9], cya[9];
+    double bxa, bxb;
+    int stage, cs, nsub, pass, bres;
+    bool reset, bao, bbo;
+};
+enum { PS_BEGIN = 0, PS_OUTER = 1, PS_CHECK = 2, PS_AFTER_BISECT = 3, PS_CHECK_DONE = 4 };
+
 struct Lane {
     const DScene &S;
     const DRun &R;
@@ -44,6 +57,7 @@ struct Lane {
      * (ncand < 0: not available, use the full BVH query) */
     int cand[PT_MAX_CAND];
     int ncand;
+    PostState ps;
     LaneCounters lc;
 
     __device__ Lane(const DScene &s, const DRun &r) : S(s), R(r) {
@@ -154,6 +168,70 @@ struct Lane {
             bc_write(b, i, 1, k);
             flags |= PT_F_BC1;
         }
+    }
+    /* suspended post-step (batched form) */
+    __device__ void load_post(const DBatch &b, int64_t i) {
+        const int64_t n = b.n;
+        const double *d = b.ps_d;
+        ps.x1 = d[0 * n + i]; ps.x = d[1 * n + i]; ps.x2 = d[2 * n + i]; ps.cx1 = d[3 * n + i];
+        ps.bxa = d[4 * n + i]; ps.bxb = d[5 * n + i];
+        for (int c = 0; c < 9; ++c) {
+            ps.y1[c] = d[(6 + c) * n + i];
+            ps.yl[c] = d[(15 + c) * n + i];
+            ps.y2[c] = d[(24 + c) * n + i];
+            ps.cya[c] = d[(33 + c) * n + i];
+        }
+        const int32_t *q = b.ps_i;
+        ps.stage = q[0 * n + i]; ps.cs = q[1 * n + i]; ps.nsub = q[2 * n + i]; ps.pass = q[3 * n + i]; ps.bres = q[4 * n + i];
+        const int fl = q[5 * n + i];
+        ps.reset = fl & 1; ps.bao = (fl >> 1) & 1; ps.bbo = (fl >> 2) & 1;
+        ncand = q[6 * n + i];
+        for (int k = 0; k < PT_MAX_CAND; ++k) cand[k] = q[(7 + k) * n + i];
+    }
+    __device__ void store_post(const DBatch &b, int64_t i) const {
+        const int64_t n = b.n;
+        double *d = b.ps_d;
+        d[0 * n + i] = ps.x1; d[1 * n + i] = ps.x; d[2 * n + i] = ps.x2; d[3 * n + i] = ps.cx1;
+        d[4 * n + i] = ps.bxa; d[5 * n + i] = ps.bxb;
+        for (int c = 0; c < 9; ++c) {
+            d[(6 + c) * n + i] = ps.y1[c];
+            d[(15 + c) * n + i] = ps.yl[c];
+            d[(24 + c) * n + i] = ps.y2[c];
+            d[(33 + c) * n + i] = ps.cya[c];
+        }
+        int32_t *q = b.ps_i;
+        q[0 * n + i] = ps.stage; q[1 * n + i] = ps.cs; q[2 * n + i] = ps.nsub; q[3 * n + i] = ps.pass; q[4 * n + i] = ps.bres;
+        q[5 * n + i] = (ps.reset ? 1 : 0) | (ps.bao ? 2 : 0) | (ps.bbo ? 4 : 0);
+        q[6 * n + i] = ncand;
+        for (int k = 0; k < PT_MAX_CAND; ++k) q[(7 + k) * n + i] = cand[k];
+    }
+    /* what a bisection of a suspended post-step reads: the dense data of the
+     * accepted try and the interval (cx1, cya) -> (x2, y2) (positions only)
+     * with its candidate triangles */
+    __device__ void load_bisect_request(const DBatch &b, int64_t i) {
+        const int64_t n = b.n;
+        t = b.t[i];
+        for (int c = 0; c < 9; ++c) { y[c] = b.y[c * n + i]; dydt[c] = b.dydt[c * n + i]; }
+        load_dense(b, i);
+        const double *d = b.ps_d;
+        ps.x2 = d[2 * n + i];
+        ps.cx1 = d[3 * n + i];
+        for (int c = 0; c < 3; ++c) {
+            ps.y2[c] = d[(24 + c) * n + i];
+            ps.cya[c] = d[(33 + c) * n + i];
+        }
+        const int32_t *q = b.ps_i;
+        ncand = q[6 * n + i];
+        for (int k = 0; k < PT_MAX_CAND; ++k) cand[k] = q[(7 + k) * n + i];
+    }
+    __device__ void store_bisect_result(const DBatch &b, int64_t i) const {
+        const int64_t n = b.n;
+        b.ps_d[4 * n + i] = ps.bxa;
+        b.ps_d[5 * n + i] = ps.bxb;
+        int32_t *q = b.ps_i;
+        q[4 * n + i] = ps.bres;
+        q[5 * n + i] = (q[5 * n + i] & 1) | (ps.bao ? 2 : 0) | (ps.bbo ? 4 : 0);
+        q[0 * n + i] = PS_AFTER_BISECT;
     }
     __device__ void store(const DBatch &b, int64_t i) const {
         const int64_t n = b.n;
@@ -834,52 +912,6 @@ struct Lane {
         return altered || stop != PT_ID_UNKNOWN;
     }
 
-    /* TTracker::CheckHit (src/tracking.cpp:176-226), tail recursion as a loop */
-    __device__ bool check_hit(double x1, const double *y1in, double &x2, double *y2) {
-        ncand = -1;
-        bool r = check_hit_loop(x1, y1in, x2, y2);
-        ncand = -1;
-        return r;
-    }
-    __device__ bool check_hit_loop(double x1, const double *y1in, double &x2, double *y2) {
-        double ya[9];
-        for (int i = 0; i < 9; ++i) ya[i] = y1in[i];
-        for (int pass = 0;; ++pass) {
-            if (pass >= PT_MAX_HITS_PER_SEGMENT) { stop = PT_ID_CGAL_ERROR; return true; }
-            if (!check_segment(S, ya, y2)) { stop = PT_ID_HIT_BOUNDARIES; return true; }
-            if (x2 == x1) return false;
-            int cs = cur_solid();
-            int h = any_hit(ya, y2);
-            if (h < 0) { stop = PT_ID_CGAL_ERROR; ncand = -1; return true; }
-            if (!h) { ncand = -1; return do_step(x1, ya, x2, y2, cs); }
-            if (ncand < 0 && x1 >= to && x2 <= tn) prepare_candidates(x1, x2);
-            double xa, xb;
-            bool ao, bo;
-            int r = bisect(x1, ya, x2, y2, xa, ao, xb, bo);
-            if (r < 0) { stop = PT_ID_CGAL_ERROR; return true; }
-            if (r == 0) return false;
-            double yc1[9], yc2[9];
-            if (ao) for (int i = 0; i < 9; ++i) yc1[i] = ya[i];
-            else calc_state(xa, yc1);
-            if (bo) for (int i = 0; i < 9; ++i) yc2[i] = y2[i];
-            else calc_state(xb, yc2);
-            double xc1 = xa, xc2 = xb;
-            if (xc1 > x1 && do_step(x1, ya, xc1, yc1, cs)) {
-                x2 = xc1;
-                for (int i = 0; i < 9; ++i) y2[i] = yc1[i];
-                return true;
-            }
-            if (do_hit(xc1, yc1, xc2, yc2)) {
-                x2 = xc2;
-                for (int i = 0; i < 9; ++i) y2[i] = yc2[i];
-                return true;
-            }
-            if (!(xc2 > x1)) { stop = PT_ID_CGAL_ERROR; return true; } /* no progress along the segment */
-            x1 = xc2;
-            for (int i = 0; i < 9; ++i) ya[i] = yc2[i];
-        }
-    }
-
     /* TTracker::IntegrateSpin decision logic (src/tracking.cpp:373-483) */
     __device__ double integrate_spin(double x2, const double *y2) {
         double B1[3], B2[3];
@@ -953,50 +985,123 @@ struct Lane {
     }
 
     /* The remainder of one LOOP-A iteration (src/tracking.cpp:87-147) after an
-     * accepted try: decay/tmax clipping, chord splitting, CheckHit, spin and
-     * stop checks, then commit. */
+     * accepted try -- decay/tmax clipping, chord splitting, CheckHit with its
+     * bisection, spin and stop checks, commit -- as a resumable state machine.
+     * Returns 1 when it needs the bisection of (ps.cx1, ps.cya) -> (ps.x2,
+     * ps.y2) (result expected in ps.bres/bxa/bxb/bao/bbo, then call again), 0
+     * when the step is finished.  Call with ps.stage = PS_BEGIN first. */
+    __device__ int post_resume() {
+        PostState &P = ps;
+        bool ch = false;
+        if (P.stage == PS_BEGIN) {
+            P.x1 = to;
+            for (int i = 0; i < 9; ++i) P.y1[i] = xo[i];
+            P.x = tn;
+            for (int i = 0; i < 9; ++i) P.yl[i] = yn[i];
+            bool finite = isfinite(tn);
+            for (int i = 0; i < 9; ++i) finite = finite && isfinite(yn[i]);
+            if (!finite) { /* a non-finite state would never stop: report it as an integrator failure */
+                stop = PT_ID_ODEINT_ERROR;
+                return 0;
+            }
+            if (tau > 0 && P.yl[6] > tau) {
+                P.x = P.x1 + (P.x - P.x1) * (tau - P.y1[6]) / (P.yl[6] - P.y1[6]);
+                calc_state(P.x, P.yl);
+            }
+            if (P.x > R.simtime) {
+                P.x = R.simtime;
+                calc_state(P.x, P.yl);
+            }
+            P.reset = false;
+            P.nsub = 0;
+            P.stage = PS_OUTER;
+        }
+        while (true) {
+            if (P.stage == PS_OUTER) {
+                if (!(P.x1 < P.x)) break;
+                if (++P.nsub > PT_MAX_SUBSEGMENTS) { stop = PT_ID_ODEINT_ERROR; break; }
+                double l2 = (P.yl[8] - P.y1[8]) * (P.yl[8] - P.y1[8]);
+                double d2 = (P.yl[0] - P.y1[0]) * (P.yl[0] - P.y1[0]) + (P.yl[1] - P.y1[1]) * (P.yl[1] - P.y1[1]) +
+                            (P.yl[2] - P.y1[2]) * (P.yl[2] - P.y1[2]);
+                double dev2 = 0.25 * (l2 - d2);
+                P.x2 = P.x;
+                for (int i = 0; i < 9; ++i) P.y2[i] = P.yl[i];
+                if (dev2 > PT_MAX_TRACK_DEVIATION * PT_MAX_TRACK_DEVIATION) {
+                    P.x2 = P.x1 + (P.x - P.x1) / ceil(sqrt(dev2) / PT_MAX_TRACK_DEVIATION);
+                    if (!(P.x2 > P.x1)) { stop = PT_ID_ODEINT_ERROR; break; } /* split below time resolution */
+                    calc_state(P.x2, P.y2);
+                }
+                /* TTracker::CheckHit (src/tracking.cpp:176-226) on (x1, y1) -> (x2, y2);
+                 * its tail recursion is the PS_CHECK loop */
+                ncand = -1;
+                P.cx1 = P.x1;
+                for (int i = 0; i < 9; ++i) P.cya[i] = P.y1[i];
+                P.pass = 0;
+                P.stage = PS_CHECK;
+            } else if (P.stage == PS_CHECK) {
+                if (P.pass++ >= PT_MAX_HITS_PER_SEGMENT) { stop = PT_ID_CGAL_ERROR; ch = true; P.stage = PS_CHECK_DONE; continue; }
+                if (!check_segment(S, P.cya, P.y2)) { stop = PT_ID_HIT_BOUNDARIES; ch = true; P.stage = PS_CHECK_DONE; continue; }
+                if (P.x2 == P.cx1) { ch = false; P.stage = PS_CHECK_DONE; continue; }
+                P.cs = cur_solid();
+                int h = any_hit(P.cya, P.y2);
+                if (h < 0) { stop = PT_ID_CGAL_ERROR; ch = true; P.stage = PS_CHECK_DONE; continue; }
+                if (!h) {
+                    ncand = -1;
+                    ch = do_step(P.cx1, P.cya, P.x2, P.y2, P.cs);
+                    P.stage = PS_CHECK_DONE;
+                    continue;
+                }
+                if (ncand < 0 && P.cx1 >= to && P.x2 <= tn) prepare_candidates(P.cx1, P.x2);
+                P.stage = PS_AFTER_BISECT;
+                return 1; /* TTracker::iterate_collision on (cx1, cya) -> (x2, y2) */
+            } else if (P.stage == PS_AFTER_BISECT) {
+                if (P.bres < 0) { stop = PT_ID_CGAL_ERROR; ch = true; P.stage = PS_CHECK_DONE; continue; }
+                if (P.bres == 0) { ch = false; P.stage = PS_CHECK_DONE; continue; }
+                double yc1[9], yc2[9];
+                if (P.bao) for (int i = 0; i < 9; ++i) yc1[i] = P.cya[i];
+                else calc_state(P.bxa, yc1);
+                if (P.bbo) for (int i = 0; i < 9; ++i) yc2[i] = P.y2[i];
+                else calc_state(P.bxb, yc2);
+                double xc1 = P.bxa, xc2 = P.bxb;
+                if (xc1 > P.cx1 && do_step(P.cx1, P.cya, xc1, yc1, P.cs)) {
+                    P.x2 = xc1;
+                    for (int i = 0; i < 9; ++i) P.y2[i] = yc1[i];
+                    ch = true;
+                    P.stage = PS_CHECK_DONE;
+                    continue;
+                }
+                if (do_hit(xc1, yc1, xc2, yc2)) {
+                    P.x2 = xc2;
+                    for (int i = 0; i < 9; ++i) P.y2[i] = yc2[i];
+                    ch = true;
+                    P.stage = PS_CHECK_DONE;
+                    continue;
+                }
+                if (!(xc2 > P.cx1)) { stop = PT_ID_CGAL_ERROR; ch = true; P.stage = PS_CHECK_DONE; continue; } /* no progress */
+                P.cx1 = xc2;
+                for (int i = 0; i < 9; ++i) P.cya[i] = yc2[i];
+                P.stage = PS_CHECK;
+            } else { /* PS_CHECK_DONE: back in the chord-piece loop */
+                ncand = -1;
+                P.reset = ch;
+                if (P.reset) {
+                    P.x = P.x2;
+                    for (int i = 0; i < 9; ++i) P.yl[i] = P.y2[i];
+                }
+                P.x1 = P.x2;
+                for (int i = 0; i < 9; ++i) P.y1[i] = P.y2[i];
+                P.stage = PS_OUTER;
+            }
+        }
+        finish_step(P.x, P.yl, P.reset);
+        return 0;
+    }
+
+    /* the whole post-step with the bisections run inline (plain form) */
     __device__ void post_step() {
-        double x1 = to, y1[9];
-        for (int i = 0; i < 9; ++i) y1[i] = xo[i];
-        double x = tn, yl[9];
-        for (int i = 0; i < 9; ++i) yl[i] = yn[i];
-        bool finite = isfinite(tn);
-        for (int i = 0; i < 9; ++i) finite = finite && isfinite(yn[i]);
-        if (!finite) { /* a non-finite state would never stop: report it as an integrator failure */
-            stop = PT_ID_ODEINT_ERROR;
-            return;
-        }
-        if (tau > 0 && yl[6] > tau) {
-            x = x1 + (x - x1) * (tau - y1[6]) / (yl[6] - y1[6]);
-            calc_state(x, yl);
-        }
-        if (x > R.simtime) {
-            x = R.simtime;
-            calc_state(x, yl);
-        }
-        bool reset = false;
-        int nsub = 0;
-        while (x1 < x) {
-            if (++nsub > PT_MAX_SUBSEGMENTS) { stop = PT_ID_ODEINT_ERROR; break; }
-            double l2 = (yl[8] - y1[8]) * (yl[8] - y1[8]);
-            double d2 = (yl[0] - y1[0]) * (yl[0] - y1[0]) + (yl[1] - y1[1]) * (yl[1] - y1[1]) + (yl[2] - y1[2]) * (yl[2] - y1[2]);
-            double dev2 = 0.25 * (l2 - d2);
-            double x2 = x, y2[9];
-            for (int i = 0; i < 9; ++i) y2[i] = yl[i];
-            if (dev2 > PT_MAX_TRACK_DEVIATION * PT_MAX_TRACK_DEVIATION) {
-                x2 = x1 + (x - x1) / ceil(sqrt(dev2) / PT_MAX_TRACK_DEVIATION);
-                if (!(x2 > x1)) { stop = PT_ID_ODEINT_ERROR; break; } /* split below time resolution */
-                calc_state(x2, y2);
-            }
-            reset = check_hit(x1, y1, x2, y2);
-            if (reset) {
-                x = x2;
-                for (int i = 0; i < 9; ++i) yl[i] = y2[i];
-            }
-            x1 = x2;
-            for (int i = 0; i < 9; ++i) y1[i] = y2[i];
-        }
-        finish_step(x, yl, reset);
+        ps.stage = PS_BEGIN;
+        while (post_resume() == 1)
+            ps.bres = bisect(ps.cx1, ps.cya, ps.x2, ps.y2, ps.bxa, ps.bao, ps.bxb, ps.bbo);
     }
 
     /* IntegrateSpin + polarisation bookkeeping + stop checks
