@@ -339,7 +339,7 @@ def run_ours(args, rank, world):
                      "fp64_flops_per_launch": f64 / launches, "fp32_flops_per_launch": f32 / launches},
         "events": {k: agg[k] for k in ("rk_accepted", "rk_rejected", "rhs_evals", "field_evals", "hits",
                                         "bisection_levels", "bvh_nodes", "tri_tests", "subsegments", "dense_evals",
-                                        "bisect_max", "cand_calls", "cand_overflow", "cand_sum", "tri32_tests")},
+                                        "bisect_max", "bisect_dead", "cand_calls", "cand_overflow", "cand_sum", "tri32_tests")},
         "live_particles": int(agg["active"]),
         "phase_ms": {"k_try": agg["try_ms"], "k_post": agg["post_ms"], "k_slow": agg["slow_ms"], "k_bisect": agg["bisect_ms"]},
     }

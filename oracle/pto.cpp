@@ -990,6 +990,7 @@ struct Tracker {
                 return true;
             }
         }
+        if (stats) stats->bisect_dead++;
         return false;
     }
 
@@ -1334,7 +1335,7 @@ int pto_track(pto_ctx *ctx, const pt_run_params *params, const pt_particles *in,
         std::memset(stats, 0, sizeof(*stats));
         for (auto &s : st) {
             stats->rk_accepted += s.rk_accepted; stats->rk_rejected += s.rk_rejected; stats->rhs_evals += s.rhs_evals;
-            stats->hits += s.hits; stats->bisection_levels += s.bisection_levels; stats->subsegments += s.subsegments;
+            stats->hits += s.hits; stats->bisection_levels += s.bisection_levels; stats->bisect_dead += s.bisect_dead; stats->subsegments += s.subsegments;
             stats->bvh_nodes += s.bvh_nodes; stats->particle_seconds += s.particle_seconds;
         }
         stats->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

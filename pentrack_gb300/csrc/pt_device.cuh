@@ -158,5 +158,5 @@ struct DCounters {
     unsigned long long bvh_nodes, tri_tests, subsegments, dense_evals, active, paused;
     double particle_seconds;
     unsigned int bisect_max;
-    unsigned long long cand_calls, cand_overflow, cand_sum, tri32;
+    unsigned long long cand_calls, cand_overflow, cand_sum, tri32, bisect_dead;
 };

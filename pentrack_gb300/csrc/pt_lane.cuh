@@ -15,7 +15,7 @@ namespace ptd {
 struct LaneCounters {
     unsigned rk_acc, rk_rej, rhs, fields, hits, bisect, subseg, dense;
     unsigned nodes, tris, bisect_max;
-    unsigned cand_calls, cand_overflow, cand_sum, tri32;
+    unsigned cand_calls, cand_overflow, cand_sum, tri32, dead;
 };
 
 /* Resumable state of one post-step (the remainder of LOOP A after an accepted
@@ -65,7 +65,7 @@ struct Lane {
         bc_next = 0;
         ntry = 0;
         ncand = -1;
-        lc = LaneCounters{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        lc = LaneCounters{};
     }
 
     __device__ double u01() { return uniform(R.seed, id, rn++); }
@@ -785,7 +785,7 @@ struct Lane {
             stB[level] = B;
             double xc = A + (B - A) * 0.5, pc[3];
             calc_pos(xc, pc);
-            if (++work > PT_MAX_BISECT_WORK) return -1;
+            if (++work > PT_MAX_BISECT_WORK) { lc.bisect_max = max(lc.bisect_max, (unsigned)work); return -1; }
             int h = any_hit(pA, pc);
             if (h < 0) return -1;
             if (h) {
@@ -804,29 +804,33 @@ struct Lane {
                 ++level;
                 continue;
             }
-            /* neither half collides: back up to the nearest level whose second half is untried */
+            /* neither half collides: this interval is a dead end; back up to
+             * the nearest level whose second half is untried */
+            ++lc.dead;
             bool resumed = false;
             while (level > 0 && !resumed) {
                 --level;
-                if (getbit(tr0, tr1, level)) continue; /* both halves of this level done */
+                if (getbit(tr0, tr1, level)) { ++lc.dead; continue; } /* both halves of this level done */
                 A = stA[level];
                 B = stB[level];
-                /* an interval end is an input end iff every choice above it went the same way */
+                /* the start is the input start iff every choice above this
+                 * level took the first half, the end is the input end iff
+                 * every choice took the second half */
                 bool allfirst = true, allsecond = true;
                 for (int l = 0; l < level; ++l) {
                     bool c = getbit(ch0, ch1, l);
                     allfirst = allfirst && !c;
                     allsecond = allsecond && c;
                 }
-                Ao = allsecond;
-                Bo = allfirst;
+                Ao = allfirst;
+                Bo = allsecond;
                 if (Ao) { pA[0] = p1[0]; pA[1] = p1[1]; pA[2] = p1[2]; }
                 else calc_pos(A, pA);
                 if (Bo) { pB[0] = p2[0]; pB[1] = p2[1]; pB[2] = p2[2]; }
                 else calc_pos(B, pB);
                 double m = A + (B - A) * 0.5, pm[3];
                 calc_pos(m, pm);
-                if (++work > PT_MAX_BISECT_WORK) return -1;
+                if (++work > PT_MAX_BISECT_WORK) { lc.bisect_max = max(lc.bisect_max, (unsigned)work); return -1; }
                 int hh = any_hit(pm, pB);
                 if (hh < 0) return -1;
                 setbit(tr0, tr1, level, true);
@@ -835,6 +839,8 @@ struct Lane {
                     A = m; pA[0] = pm[0]; pA[1] = pm[1]; pA[2] = pm[2]; Ao = false;
                     ++level;
                     resumed = true;
+                } else {
+                    ++lc.dead;
                 }
             }
             if (!resumed) {

@@ -30,6 +30,26 @@ def cube_storage(n=10000, seed=1001, simtime=100.0):
     return sc, params, parts
 
 
+def fenced_cube(n=2000, seed=1001, simtime=100.0):
+    """The closed unit cube of `cube_storage` with a free-standing block
+    (x in [-0.05, 0.05], y in [-0.3, 0.3], z in [-0.45, -0.2]) of the wall
+    material inside it.  Particles start on one side of the block; those
+    that fly over its edges make chords that cut a corner of the block while
+    neither half-chord does, which exercises the dead ends of the bisection
+    search (TTracker::iterate_collision returning false)."""
+    sc = Scene()
+    sc.add_material("default", 335.0)
+    sc.add_material("vacuum", 0.0)
+    sc.add_solid(1, "default")
+    sc.add_solid(2, "vacuum", S.box_mesh((-0.5, -0.5, -0.5), (0.5, 0.5, 0.5)))
+    sc.add_solid(3, "default", S.box_mesh((-0.05, -0.3, -0.45), (0.05, 0.3, -0.2)))
+    ids = np.arange(n, dtype=np.int64)
+    pos, (E, ph, th, pol) = S.source_box(seed, ids, (-0.5, -0.5, -0.1), (-0.1, 0.5, 0.5), 0.0, 200e-9, polarization=1.0)
+    parts = S.make_particles(seed, ids, pos, E, ph, th, pol)
+    params = run_params(A.NEUTRON, simtime=simtime, tau=0.0, tmax=9e99, lmax=9e99, bmax=0.1, spintimes=(0, 0), seed=seed)
+    return sc, params, parts
+
+
 def quadrupole_table(n=64, r=0.2, h=0.1, grad=7.5, b0=1e-5):
     """Grid of n points per axis over the cylinder's box padded by one cell on
     each side (the reference zeroes B outside a table), sampled from

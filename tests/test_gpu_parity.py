@@ -184,6 +184,29 @@ def test_cube_storage_parity(eng, oracle_mod):
     assert bitwise.mean() >= 0.99, bitwise.mean()
 
 
+@pytest.mark.parametrize("mode", [A.MODE_PLAIN, A.MODE_BATCHED])
+def test_fenced_cube_bisection_dead_ends(eng, oracle_mod, mode):
+    """Non-convex geometry: chords that cut a corner of the inner block while
+    neither half does make the bisection back up (iterate_collision returning
+    false at a level).  The GPU's stack-based search must visit the same
+    intervals as the recursive reference: identical dead-end counts, hit
+    counts and (almost always) bitwise end states."""
+    from pentrack_gb300 import workloads
+    sc, params, parts = workloads.fenced_cube(n=2000, simtime=100.0)
+    oout, ost = oracle_mod.Oracle(sc).integrate(params, parts)
+    params.mode = mode
+    gout, gst = eng(sc).integrate(params, parts)
+    assert ost["bisect_dead"] > 20
+    assert gst["bisect_dead"] == ost["bisect_dead"]
+    assert gst["bisection_levels"] == ost["bisection_levels"]
+    assert np.array_equal(gout.n_hit, oout.n_hit)
+    assert np.array_equal(gout.stop_id, oout.stop_id)
+    dpos, dvel = compare_states(gout, oout)
+    assert np.max(dpos) < 1e-6, np.max(dpos)
+    bitwise = np.all(gout.y == oout.y, axis=0) & (gout.t == oout.t)
+    assert bitwise.mean() >= 0.99, bitwise.mean()
+
+
 def test_integration_test_known_answer_gpu(eng):
     from pentrack_gb300 import workloads
     sc, params, parts = workloads.integration_test(n=500)
