@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(128) k_slow(const __grid_constant__ DScene S, 
 /* Batched form, phase 4: the bisections (TTracker::iterate_collision) that
  * suspended post-steps asked for; every lane runs the same search loop.  The
  * post-steps go back to the slow list. */
-__global__ void __launch_bounds__(128) k_bisect(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C) {
+__global__ void __launch_bounds__(128, 4) k_bisect(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C) {
     const int n = b.count[4];
     const int32_t *lq = b.list[4];
     Lane L(S, R);

@@ -210,9 +210,17 @@ struct Lane {
      * with its candidate triangles */
     __device__ void load_bisect_request(const DBatch &b, int64_t i) {
         const int64_t n = b.n;
-        t = b.t[i];
-        for (int c = 0; c < 9; ++c) { y[c] = b.y[c * n + i]; dydt[c] = b.dydt[c * n + i]; }
-        load_dense(b, i);
+        to = b.t[i];
+        tn = b.tn[i];
+        for (int c = 0; c < 3; ++c) { /* calc_pos reads the position components only */
+            xo[c] = b.y[c * n + i];
+            dxo[c] = b.dydt[c * n + i];
+            k3[c] = b.kst[(0 * 9 + c) * n + i];
+            k4[c] = b.kst[(1 * 9 + c) * n + i];
+            k5[c] = b.kst[(2 * 9 + c) * n + i];
+            k6[c] = b.kst[(3 * 9 + c) * n + i];
+            dyn[c] = b.dyn[c * n + i];
+        }
         const double *d = b.ps_d;
         ps.x2 = d[2 * n + i];
         ps.cx1 = d[3 * n + i];
@@ -753,100 +761,95 @@ struct Lane {
     /* TTracker::iterate_collision (src/tracking.cpp:228-265) without recursion:
      * a depth-first search over halves with an explicit stack of interval
      * times (positions of stacked interval ends are recomputed from the dense
-     * output, which is deterministic).  Returns 1 with the final bracket
-     * [xa, xb] (aorig/borig: the bracket end is an input end), 0 when no
-     * sub-chord collides, -1 on a CGAL-error case or when the search exceeds
-     * its work bound. */
+     * output, which is deterministic).  Every loop iteration makes exactly one
+     * chord query from one call site, so lanes of a warp that bisect at the
+     * same time stay converged whichever half they are in.  Returns 1 with the
+     * final bracket [xa, xb] (aorig/borig: the bracket end is an input end), 0
+     * when no sub-chord collides, -1 on a CGAL-error case or when the search
+     * exceeds its work bound. */
     __device__ int bisect(double x1, const double *p1, double x2, const double *p2, double &xa, bool &aorig, double &xb,
                           bool &borig) {
+        enum { ENTER, SECOND, RESUME };
         double stA[PT_MAX_BISECT_LEVELS + 1], stB[PT_MAX_BISECT_LEVELS + 1];
         uint64_t ch0 = 0, ch1 = 0; /* choice bit per level: 1 = second half */
         uint64_t tr0 = 0, tr1 = 0; /* second half already tried at this level */
         int level = 0;
         double A = x1, B = x2, pA[3] = {p1[0], p1[1], p1[2]}, pB[3] = {p2[0], p2[1], p2[2]};
+        double xc = 0, pc[3] = {0, 0, 0};
         bool Ao = true, Bo = true;
-        int work = 0;
+        int work = 0, phase = ENTER;
         auto getbit = [](uint64_t a, uint64_t b, int l) -> bool { return l < 64 ? ((a >> l) & 1) : ((b >> (l - 64)) & 1); };
         auto setbit = [](uint64_t &a, uint64_t &b, int l, bool v) {
             if (l < 64) { if (v) a |= (1ull << l); else a &= ~(1ull << l); }
             else { if (v) b |= (1ull << (l - 64)); else b &= ~(1ull << (l - 64)); }
         };
         while (true) {
-            /* termination tests at the entry of iterate_collision */
-            double dx = pB[0] - pA[0], dy = pB[1] - pA[1], dz = pB[2] - pA[2];
-            if (dx * dx + dy * dy + dz * dz < PT_REFLECT_TOLERANCE * PT_REFLECT_TOLERANCE || B - A < 4 * (A + B) * 2.220446049250313e-16 ||
-                level >= 100) {
-                xa = A; aorig = Ao; xb = B; borig = Bo;
-                lc.bisect_max = max(lc.bisect_max, (unsigned)work);
-                return 1;
-            }
-            ++lc.bisect;
-            stA[level] = A;
-            stB[level] = B;
-            double xc = A + (B - A) * 0.5, pc[3];
-            calc_pos(xc, pc);
-            if (++work > PT_MAX_BISECT_WORK) { lc.bisect_max = max(lc.bisect_max, (unsigned)work); return -1; }
-            int h = any_hit(pA, pc);
-            if (h < 0) return -1;
-            if (h) {
-                setbit(ch0, ch1, level, false);
-                setbit(tr0, tr1, level, false);
-                B = xc; pB[0] = pc[0]; pB[1] = pc[1]; pB[2] = pc[2]; Bo = false;
-                ++level;
-                continue;
-            }
-            h = any_hit(pc, pB);
-            if (h < 0) return -1;
-            if (h) {
-                setbit(ch0, ch1, level, true);
-                setbit(tr0, tr1, level, true);
-                A = xc; pA[0] = pc[0]; pA[1] = pc[1]; pA[2] = pc[2]; Ao = false;
-                ++level;
-                continue;
-            }
-            /* neither half collides: this interval is a dead end; back up to
-             * the nearest level whose second half is untried */
-            ++lc.dead;
-            bool resumed = false;
-            while (level > 0 && !resumed) {
-                --level;
-                if (getbit(tr0, tr1, level)) { ++lc.dead; continue; } /* both halves of this level done */
+            if (phase == ENTER) {
+                /* termination tests at the entry of iterate_collision */
+                double dx = pB[0] - pA[0], dy = pB[1] - pA[1], dz = pB[2] - pA[2];
+                if (dx * dx + dy * dy + dz * dz < PT_REFLECT_TOLERANCE * PT_REFLECT_TOLERANCE ||
+                    B - A < 4 * (A + B) * 2.220446049250313e-16 || level >= PT_MAX_BISECT_LEVELS) {
+                    xa = A; aorig = Ao; xb = B; borig = Bo;
+                    lc.bisect_max = max(lc.bisect_max, (unsigned)work);
+                    return 1;
+                }
+                ++lc.bisect;
+                stA[level] = A;
+                stB[level] = B;
+                xc = A + (B - A) * 0.5;
+                calc_pos(xc, pc);
+            } else if (phase == RESUME) {
+                /* second half of a stacked level: the start is the input start
+                 * iff every choice above took the first half, the end is the
+                 * input end iff every choice took the second half */
                 A = stA[level];
                 B = stB[level];
-                /* the start is the input start iff every choice above this
-                 * level took the first half, the end is the input end iff
-                 * every choice took the second half */
-                bool allfirst = true, allsecond = true;
-                for (int l = 0; l < level; ++l) {
-                    bool c = getbit(ch0, ch1, l);
-                    allfirst = allfirst && !c;
-                    allsecond = allsecond && c;
-                }
-                Ao = allfirst;
+                bool allsecond = true;
+                for (int l = 0; l < level; ++l) allsecond = allsecond && getbit(ch0, ch1, l);
                 Bo = allsecond;
-                if (Ao) { pA[0] = p1[0]; pA[1] = p1[1]; pA[2] = p1[2]; }
-                else calc_pos(A, pA);
                 if (Bo) { pB[0] = p2[0]; pB[1] = p2[1]; pB[2] = p2[2]; }
                 else calc_pos(B, pB);
-                double m = A + (B - A) * 0.5, pm[3];
-                calc_pos(m, pm);
-                if (++work > PT_MAX_BISECT_WORK) { lc.bisect_max = max(lc.bisect_max, (unsigned)work); return -1; }
-                int hh = any_hit(pm, pB);
-                if (hh < 0) return -1;
-                setbit(tr0, tr1, level, true);
-                if (hh) {
-                    setbit(ch0, ch1, level, true);
-                    A = m; pA[0] = pm[0]; pA[1] = pm[1]; pA[2] = pm[2]; Ao = false;
-                    ++level;
-                    resumed = true;
-                } else {
-                    ++lc.dead;
-                }
+                xc = A + (B - A) * 0.5;
+                calc_pos(xc, pc);
             }
-            if (!resumed) {
+            /* the one chord query of this iteration: first half (A, xc) on
+             * entering a level, else second half (xc, B) */
+            const bool first = (phase == ENTER);
+            double P[3], Q[3];
+            for (int k = 0; k < 3; ++k) {
+                P[k] = first ? pA[k] : pc[k];
+                Q[k] = first ? pc[k] : pB[k];
+            }
+            if (++work > PT_MAX_BISECT_WORK) { lc.bisect_max = max(lc.bisect_max, (unsigned)work); return -1; }
+            const int h = any_hit(P, Q);
+            if (h < 0) { lc.bisect_max = max(lc.bisect_max, (unsigned)work); return -1; }
+            if (phase == RESUME) setbit(tr0, tr1, level, true);
+            if (h) {
+                setbit(ch0, ch1, level, !first);
+                if (phase == ENTER) setbit(tr0, tr1, level, false);
+                if (phase == SECOND) setbit(tr0, tr1, level, true);
+                if (first) { B = xc; pB[0] = pc[0]; pB[1] = pc[1]; pB[2] = pc[2]; Bo = false; }
+                else { A = xc; pA[0] = pc[0]; pA[1] = pc[1]; pA[2] = pc[2]; Ao = false; }
+                ++level;
+                phase = ENTER;
+                continue;
+            }
+            if (phase == ENTER) { phase = SECOND; continue; }
+            /* neither half of this level leads to a collision: a dead end;
+             * back up to the nearest level whose second half is untried */
+            ++lc.dead;
+            bool found = false;
+            while (level > 0) {
+                --level;
+                if (getbit(tr0, tr1, level)) { ++lc.dead; continue; } /* both halves of this level done */
+                found = true;
+                break;
+            }
+            if (!found) {
                 lc.bisect_max = max(lc.bisect_max, (unsigned)work);
                 return 0;
             }
+            phase = RESUME;
         }
     }
 
