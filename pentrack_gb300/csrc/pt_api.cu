@@ -440,6 +440,48 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
         }
         S.tri32 = dupload(c->allocs, t32.data(), t32.size(), e);
         if (e) return ck(c, e, "upload triangle planes"), PT_ERR_CUDA;
+        /* FP64 normals with error bounds and canonical edges for seg_tri64c */
+        std::vector<DTriC> tc(tris.size());
+        const double eps = std::ldexp(1.0, -53);
+        for (size_t k = 0; k < tris.size(); ++k) {
+            const pth::HostTri &h = tris[k];
+            DTriC &q = tc[k];
+            std::memset(&q, 0, sizeof(q));
+            double e1[3], e2[3];
+            for (int a = 0; a < 3; ++a) { e1[a] = h.b[a] - h.a[a]; e2[a] = h.c[a] - h.a[a]; }
+            double dn = 0, n1 = 0, ea = 0;
+            for (int a = 0; a < 3; ++a) {
+                const int i1 = (a + 1) % 3, i2 = (a + 2) % 3;
+                const double p1 = e1[i1] * e2[i2], p2 = e1[i2] * e2[i1];
+                q.n[a] = p1 - p2;
+                dn = std::max(dn, 5 * eps * (std::fabs(p1) + std::fabs(p2)) * (1 + 1e-10));
+                n1 += std::fabs(q.n[a]);
+                ea = std::max(ea, std::max(std::fabs(e1[a]), std::fabs(e2[a])));
+            }
+            q.dn = std::nextafter((float)dn, INFINITY);
+            q.n1 = std::nextafter((float)(n1 * (1 + 1e-12)), INFINITY);
+            q.ea = std::nextafter((float)ea, INFINITY);
+            const double *V[3] = {h.a, h.b, h.c};
+            int edges = 0;
+            for (int j = 0; j < 3; ++j) {
+                const int iu = j, iv = (j + 1) % 3;
+                const double *u = V[iu], *v = V[iv];
+                const bool swap = (v[0] != u[0]) ? v[0] < u[0] : ((v[1] != u[1]) ? v[1] < u[1] : v[2] < u[2]);
+                const int cu = swap ? iv : iu, cv = swap ? iu : iv;
+                edges |= cv << (2 * j);
+                if (swap) edges |= 1 << (6 + j);
+                double en = 0;
+                for (int a = 0; a < 3; ++a) {
+                    const double d = V[cu][a] - V[cv][a];
+                    q.e[j][a] = (float)d;
+                    en = std::max(en, std::fabs(d));
+                }
+                q.en[j] = std::nextafter((float)en, INFINITY);
+            }
+            q.edges = edges;
+        }
+        S.tric = dupload(c->allocs, tc.data(), tc.size(), e);
+        if (e) return ck(c, e, "upload triangle certificates"), PT_ERR_CUDA;
     }
     S.nodes = (const DNode *)dupload(c->allocs, (const DNode *)nodes.data(), nodes.size(), e);
     if (e) return ck(c, e, "upload bvh"), PT_ERR_CUDA;

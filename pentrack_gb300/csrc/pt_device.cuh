@@ -49,6 +49,17 @@ struct DTri32 {         /* FP32 copy of a triangle for certified pre-tests, 64 B
     float pad[3];
 };
 
+struct DTriC {          /* data of the certified FP64 pre-test (seg_tri64c), 96 B */
+    double n[3];        /* (b - a) x (c - a) evaluated in FP64 */
+    float dn;           /* bound on |n - exact| per component */
+    float n1;           /* |n|_1, rounded up */
+    float ea;           /* max(|b - a|_inf, |c - a|_inf), rounded up */
+    int edges;          /* edge k (a-b, b-c, c-a): bits 2k..2k+1 = index of its lexicographically larger vertex v, bit 6+k = swapped */
+    float e[3][3];      /* edge k in canonical order: u - v (u lexicographically smaller), rounded to FP32 */
+    float en[3];        /* |u - v|_inf, rounded up */
+    float pad[2];
+};
+
 struct DNode {          /* flattened BVH node in depth-first order, 32 B */
     float lo[3], hi[3];
     int skip;           /* next node when this subtree is skipped */
@@ -100,6 +111,7 @@ struct DScene {
     int pad;
     const DTri *tris;
     const DTri32 *tri32;
+    const DTriC *tric;
     const DNode *nodes;
     const DSolid *solids;
     const DMat *mats;

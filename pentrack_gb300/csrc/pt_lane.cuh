@@ -475,6 +475,9 @@ struct Lane {
                 if (r32 == 0) continue;
                 if (r32 == 1) return 1;
                 const DTri &t = S.tris[cand[j]];
+                const int r64 = seg_tri64c(p, q, s32, t, S.tri32[cand[j]], S.tric[cand[j]]);
+                if (r64 == 0) continue;
+                if (r64 == 1) return 1;
                 if (!tri_box_touch(t, p, q)) continue;
                 ++lc.tris;
                 double sv;

@@ -129,6 +129,76 @@ __device__ __forceinline__ int seg_tri32(const Seg32 &s, const DTri32 &t) {
     return -1;
 }
 
+/* Certified decision from FP64 differences, the second tier after
+ * seg_tri32.  The plane sides are n . (x - a) with the FP64 normal n =
+ * (b - a) x (c - a) (orient3d(a, b, c, x) = -n_exact . (x - a)); the edge
+ * signs are orient3d(p, q, u, v) = (p - v) . ((q - p) x (u - v)) evaluated in
+ * FP32 from FP64 differences, whose relative rounding does not depend on the
+ * distance from the origin.  Each value is compared against its own error
+ * bound plus the error bound of seg_tri's FP64 orient3d, (7 + 56 eps) eps x
+ * permanent (Shewchuk, "Adaptive precision floating-point arithmetic and
+ * fast robust geometric predicates", 1997), with the permanent bounded by
+ * 6 x the product of the three difference norms; a value that clears both
+ * has the sign of the exact determinant and of seg_tri's FP64 one.
+ * 1: hit, 0: no hit, -1: undecided. */
+__device__ __forceinline__ int seg_tri64c(const double *p, const double *q, const Seg32 &s, const DTri &t, const DTri32 &t32,
+                                          const DTriC &c) {
+    const float u32 = 5.9604645e-8f;  /* 2^-24 */
+    const float e64 = 1.1102231e-16f; /* 2^-53, rounded up */
+    const float din = 2.4e-7f * fmaxf(s.m, t32.m); /* rounding of both FP32 copies of a coordinate difference */
+    float Rp = 0, Rq = 0;
+    for (int k = 0; k < 3; ++k) {
+        Rp = fmaxf(Rp, fabsf(s.p[k] - t32.a[k]));
+        Rq = fmaxf(Rq, fabsf(s.q[k] - t32.a[k]));
+    }
+    Rp = (Rp + din) * 1.0001f; /* >= |p - a|_inf */
+    Rq = (Rq + din) * 1.0001f;
+    double da[3], qa[3];
+    for (int k = 0; k < 3; ++k) { da[k] = p[k] - t.a[k]; qa[k] = q[k] - t.a[k]; }
+    const double sp = fma(c.n[0], da[0], fma(c.n[1], da[1], c.n[2] * da[2]));
+    const double sq = fma(c.n[0], qa[0], fma(c.n[1], qa[1], c.n[2] * qa[2]));
+    /* |sp - n_exact . (p - a)| <= 3 dn R + 4 eps |n|_1 R; seg_tri's orient3d(a, b, c, p) is within
+     * 7.01 eps x 6 R (ea + R)^2 of the exact determinant */
+    const float bp = 1.01f * ((3.0f * c.dn + 5.0f * e64 * c.n1) * Rp + 42.1f * e64 * Rp * (c.ea + Rp) * (c.ea + Rp));
+    const float bq = 1.01f * ((3.0f * c.dn + 5.0f * e64 * c.n1) * Rq + 42.1f * e64 * Rq * (c.ea + Rq) * (c.ea + Rq));
+    const float fp = __double2float_rz(sp), fq = __double2float_rz(sq);
+    const int gp = fp > bp ? 1 : (fp < -bp ? -1 : 0), gq = fq > bq ? 1 : (fq < -bq ? -1 : 0);
+    if (gp == 0 || gq == 0) return -1;
+    if (gp == gq) return 0; /* both ends strictly on one side */
+    /* the segment crosses the plane: edge signs (canonical order as in edge_orient) */
+    float D[3], Dn = 0;
+    for (int k = 0; k < 3; ++k) {
+        D[k] = (float)(q[k] - p[k]);
+        Dn = fmaxf(Dn, fabsf(D[k]));
+    }
+    Dn *= 1.0001f;
+    bool neg = false, pos = false, unsure = false;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int vi = (c.edges >> (2 * k)) & 3;
+        const double *v = vi == 0 ? t.a : (vi == 1 ? t.b : t.c);
+        float r[3], Rn = 0;
+        for (int i = 0; i < 3; ++i) {
+            r[i] = (float)(p[i] - v[i]);
+            Rn = fmaxf(Rn, fabsf(r[i]));
+        }
+        Rn *= 1.0001f;
+        const float *E = c.e[k];
+        const float c0 = D[1] * E[2] - D[2] * E[1], c1 = D[2] * E[0] - D[0] * E[2], c2 = D[0] * E[1] - D[1] * E[0];
+        const float val = r[0] * c0 + r[1] * c1 + r[2] * c2;
+        const float P = fabsf(r[0]) * (fabsf(D[1] * E[2]) + fabsf(D[2] * E[1])) + fabsf(r[1]) * (fabsf(D[2] * E[0]) + fabsf(D[0] * E[2])) +
+                        fabsf(r[2]) * (fabsf(D[0] * E[1]) + fabsf(D[1] * E[0]));
+        const float b = 1.01f * (16.0f * u32 * P + 42.1f * e64 * Rn * (Rn + Dn) * c.en[k]);
+        int g = val > b ? 1 : (val < -b ? -1 : 0);
+        if ((c.edges >> (6 + k)) & 1) g = -g;
+        neg = neg || g < 0;
+        pos = pos || g > 0;
+        unsure = unsure || g == 0;
+    }
+    if (neg && pos) return 0; /* certainly outside */
+    return unsure ? -1 : 1;
+}
+
 /* closed segment x closed triangle: 1 hit (parameter s), 0 none, -1 coplanar */
 __device__ __forceinline__ int seg_tri(const double *p, const double *q, const DTri &t, double &s) {
     double dp = orient3d(t.a, t.b, t.c, p), dq = orient3d(t.a, t.b, t.c, q);
@@ -641,6 +711,11 @@ __device__ int mesh_query(const DScene &S, const double *p, const double *q, dou
             if (r32 == 0) continue;
             if (MODE == 0 && r32 == 1) return 1; /* a certain hit ends an any-hit query */
             const DTri &t = S.tris[j];
+            if (r32 < 0) {
+                const int r64 = seg_tri64c(p, q, s32, t, S.tri32[j], S.tric[j]);
+                if (r64 == 0) continue;
+                if (MODE == 0 && r64 == 1) return 1;
+            }
             if (MODE != 2 && !tri_box_touch(t, p, q)) continue;
             ++qs.tris;
             double s;
