@@ -250,6 +250,21 @@ pt_status pt_segment_collisions(pt_ctx *ctx, int64_t n, const double *seg, int32
                                 int32_t *count, double *s, double *normal, int32_t *solid_id,
                                 double *distnormal);
 
+/* pt_segment_collisions without any device allocation: no counterpart in the
+ * reference (an addition for callers that must not allocate device memory
+ * per call).  Same arguments, results and
+ * errors as pt_segment_collisions; device scratch is a fixed 8 MiB array in
+ * the library's module, addressed with cudaGetSymbolAddress on the first call
+ * on each device (that device current), so make the first call before any
+ * stream capture.  Scratch needed: 48 n + 4 n + 44 n max_hits bytes plus
+ * 256-byte alignment per block; larger requests return PT_ERR_INVALID with the
+ * sizes in pt_last_error (n = 16384, max_hits = 8 fits).  Not reentrant: every
+ * context on a device shares the one scratch array, so calls on the same
+ * device must not overlap. */
+pt_status pt_segment_collisions_noalloc(pt_ctx *ctx, int64_t n, const double *seg, int32_t max_hits,
+                                        int32_t *count, double *s, double *normal, int32_t *solid_id,
+                                        double *distnormal);
+
 /* IDs of solids containing each point by +z ray parity (TTriangleMesh::GetSolids,
  * include/trianglemesh.h:181-188) as a bit mask over scene solid indices. */
 pt_status pt_point_solids(pt_ctx *ctx, int64_t n, const double *p, uint64_t *mask);

@@ -118,6 +118,8 @@ def declare(lib):
         "pt_field_eval": (C.c_int32, [vp, C.c_int64, c_double_p, C.c_int32, c_double_p, c_double_p, c_double_p, c_double_p]),
         "pt_segment_collisions": (C.c_int32, [vp, C.c_int64, c_double_p, C.c_int32, c_int32_p, c_double_p, c_double_p,
                                               c_int32_p, c_double_p]),
+        "pt_segment_collisions_noalloc": (C.c_int32, [vp, C.c_int64, c_double_p, C.c_int32, c_int32_p, c_double_p,
+                                                      c_double_p, c_int32_p, c_double_p]),
         "pt_point_solids": (C.c_int32, [vp, C.c_int64, c_double_p, c_uint64_p]),
         "pt_probe_fp64": (C.c_int32, [vp, c_double_p]),
         "pt_version": (C.c_char_p, []),

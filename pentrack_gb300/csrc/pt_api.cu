@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -303,6 +304,34 @@ struct pt_ctx {
     DCounters *counters_host = nullptr;
     int sm_count = 0;
 };
+
+/* Scratch of pt_segment_collisions_noalloc: a fixed device array in the
+ * module's own data (allocated when the module loads, never by a call).  All
+ * contexts on a device share it, so calls must not overlap.  Nothing in it
+ * needs to start at zero: k_collisions writes every segment's count and the
+ * result slots below min(count, max_hits); the slots after those keep values
+ * from earlier calls, as the allocating entry point leaves them undefined. */
+#define PT_NOALLOC_SCRATCH_BYTES (8ull << 20)
+static __device__ __align__(256) unsigned char g_noalloc_scratch[PT_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+/* device address of g_noalloc_scratch, resolved once per device with that
+ * device current */
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_addr[64] = {};
+cudaError_t noalloc_scratch(int device, unsigned char **out) {
+    if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e) return e;
+        g_noalloc_addr[device] = (unsigned char *)p;
+    }
+    *out = g_noalloc_addr[device];
+    return cudaSuccess;
+}
+} // namespace
 
 struct pt_batch {
     pt_ctx *ctx = nullptr;
@@ -986,6 +1015,46 @@ pt_status pt_segment_collisions(pt_ctx *c, int64_t n, const double *seg, int32_t
     if (!e) e = cudaStreamSynchronize(c->stream);
     free_list(tmp);
     if (e) return ck(c, e, "collisions"), PT_ERR_CUDA;
+    return PT_OK;
+}
+
+pt_status pt_segment_collisions_noalloc(pt_ctx *c, int64_t n, const double *seg, int32_t max_hits, int32_t *count, double *s,
+                                        double *normal, int32_t *solid_id, double *distnormal) {
+    if (!c || n < 0 || max_hits < 1 || !count || (n > 0 && !seg)) return PT_ERR_INVALID;
+    if (n == 0) return PT_OK;
+    /* scratch layout, every block 256-byte aligned: segments, counts, s, normals, distnormal, solid IDs */
+    const uint64_t un = (uint64_t)n, um = (uint64_t)max_hits;
+    if (un > PT_NOALLOC_SCRATCH_BYTES || um > PT_NOALLOC_SCRATCH_BYTES || un * um > PT_NOALLOC_SCRATCH_BYTES) {
+        c->err = "pt_segment_collisions_noalloc: n * max_hits exceeds the static scratch of " +
+                 std::to_string(PT_NOALLOC_SCRATCH_BYTES) + " bytes";
+        return PT_ERR_INVALID;
+    }
+    auto up = [](uint64_t b) { return (b + 255) & ~(uint64_t)255; };
+    const uint64_t o_cnt = up(48 * un), o_s = o_cnt + up(4 * un), o_nrm = o_s + up(8 * un * um), o_dn = o_nrm + up(24 * un * um),
+                   o_sid = o_dn + up(8 * un * um), end = o_sid + up(4 * un * um);
+    if (end > PT_NOALLOC_SCRATCH_BYTES) {
+        c->err = "pt_segment_collisions_noalloc: " + std::to_string(end) + " bytes of scratch needed for n = " + std::to_string(n) +
+                 ", max_hits = " + std::to_string(max_hits) + "; the static scratch holds " + std::to_string(PT_NOALLOC_SCRATCH_BYTES);
+        return PT_ERR_INVALID;
+    }
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e) return ck(c, e, "noalloc set device"), PT_ERR_CUDA;
+    unsigned char *base = nullptr;
+    if ((e = noalloc_scratch(c->device, &base))) return ck(c, e, "noalloc scratch address"), PT_ERR_CUDA;
+    double *dseg = (double *)base, *ds = (double *)(base + o_s), *dn = (double *)(base + o_nrm), *ddn = (double *)(base + o_dn);
+    int *dc = (int *)(base + o_cnt), *dsid = (int *)(base + o_sid);
+    e = cudaMemcpyAsync(dseg, seg, 48 * un, cudaMemcpyHostToDevice, c->stream);
+    if (!e) {
+        k_collisions<<<grid_for(n, 128), 128, 0, c->stream>>>(c->scene, n, dseg, max_hits, dc, ds, dn, dsid, ddn);
+        e = cudaGetLastError();
+    }
+    if (!e) e = cudaMemcpyAsync(count, dc, 4 * un, cudaMemcpyDeviceToHost, c->stream);
+    if (!e && s) e = cudaMemcpyAsync(s, ds, 8 * un * um, cudaMemcpyDeviceToHost, c->stream);
+    if (!e && normal) e = cudaMemcpyAsync(normal, dn, 24 * un * um, cudaMemcpyDeviceToHost, c->stream);
+    if (!e && solid_id) e = cudaMemcpyAsync(solid_id, dsid, 4 * un * um, cudaMemcpyDeviceToHost, c->stream);
+    if (!e && distnormal) e = cudaMemcpyAsync(distnormal, ddn, 8 * un * um, cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaStreamSynchronize(c->stream);
+    if (e) return ck(c, e, "noalloc collisions"), PT_ERR_CUDA;
     return PT_OK;
 }
 

@@ -267,6 +267,17 @@ class Engine:
         self._check(lib().pt_segment_collisions(self.h, n, _dp(s), max_hits, _ip(cnt), _dp(ss), _dp(nn), _ip(sid), _dp(dn)))
         return cnt, ss, nn, sid, dn
 
+    def collisions_noalloc(self, segs, max_hits=8):
+        """pt_segment_collisions_noalloc: the same query through the entry
+        point that uses the library's static device scratch (at most 8 MiB:
+        52 n + 44 n max_hits bytes) instead of allocating."""
+        s = np.ascontiguousarray(segs, dtype=np.float64).reshape(-1, 6)
+        n = len(s)
+        cnt = np.zeros(n, np.int32)
+        ss, nn, sid, dn = np.zeros((n, max_hits)), np.zeros((n, max_hits, 3)), np.zeros((n, max_hits), np.int32), np.zeros((n, max_hits))
+        self._check(lib().pt_segment_collisions_noalloc(self.h, n, _dp(s), max_hits, _ip(cnt), _dp(ss), _dp(nn), _ip(sid), _dp(dn)))
+        return cnt, ss, nn, sid, dn
+
     def point_solids(self, pts):
         p = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
         m = np.zeros(len(p), np.uint64)
