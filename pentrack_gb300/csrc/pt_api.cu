@@ -380,6 +380,7 @@ DSpecies make_species(int s) {
         d.q = PT_NEUTRON_Q; d.m = PT_NEUTRON_M; d.mu = PT_NEUTRON_MU; d.gamma = PT_NEUTRON_GAMMA; d.inv_mkg = PT_NEUTRON_INV_MKG;
         d.fgrav = PT_NEUTRON_FGRAV; d.mu_over_e = PT_NEUTRON_MU_OVER_E; d.q_over_e = PT_NEUTRON_Q_OVER_E; d.mc2 = PT_NEUTRON_MC2; d.mg = PT_NEUTRON_MG;
     }
+    d.muf = (float)d.mu;
     return d;
 }
 
@@ -553,7 +554,8 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
                 std::vector<double> base;
                 std::vector<float> rem;
                 pth::mixed_cells(ax, nd, o.ncomp, base, rem);
-                o.cell64 = dupload(c->allocs, base.data(), base.size(), e);
+                std::vector<float> basef(base.begin(), base.end());
+                o.cellb32 = dupload(c->allocs, basef.data(), basef.size(), e);
                 if (e) return ck(c, e, "upload cell table"), PT_ERR_CUDA;
                 o.cell32 = dupload(c->allocs, rem.data(), rem.size(), e);
                 if (e) return ck(c, e, "upload cell table"), PT_ERR_CUDA;
@@ -570,6 +572,13 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
                 for (size_t k = 0; k + 1 < ax[a].size(); ++k) iw[k] = 1.0 / (ax[a][k + 1] - ax[a][k]);
                 o.inv_w[a] = dupload(c->allocs, iw.data(), iw.size(), e);
                 if (e) return ck(c, e, "upload axis"), PT_ERR_CUDA;
+                std::vector<float> axf(ax[a].begin(), ax[a].end()), iwf(iw.begin(), iw.end());
+                o.ax32[a] = dupload(c->allocs, axf.data(), axf.size(), e);
+                if (e) return ck(c, e, "upload axis"), PT_ERR_CUDA;
+                o.inv_w32[a] = dupload(c->allocs, iwf.data(), iwf.size(), e);
+                if (e) return ck(c, e, "upload axis"), PT_ERR_CUDA;
+                o.a0f[a] = (float)o.a0[a];
+                o.inv_hf[a] = (float)o.inv_h[a];
             }
         } else if (f.type == PT_FIELD_HARMONIC) {
             std::vector<double> coef;

@@ -94,9 +94,12 @@ struct DField {
     /* mixed-precision cell table: per cell and component a linear base
      * (f at the cell's first corner, gradient g) in FP64 and the Hermite data
      * of the remainder f - base at the 8 corners in FP32 */
-    const double *cell64;  /* [cell][comp][4]: f0, gx, gy, gz */
+    const float *cellb32;  /* [cell][comp][4]: f0, gx, gy, gz */
     const float *cell32;   /* [cell][comp][corner][8] */
     const double *inv_w[3]; /* 1 / cell width per axis interval */
+    const float *ax32[3];   /* FP32 copies of the axes and widths for the FP32 field mode */
+    const float *inv_w32[3];
+    float a0f[3], inv_hf[3];
     double e[3];
     /* harmonic polynomial: Phi = sum c * x^i y^j z^k, B = grad Phi */
     int n_mono;
@@ -123,6 +126,8 @@ struct DSpecies {
     int kind;
     int pad;
     double q, m, mu, gamma, inv_mkg, fgrav, mu_over_e, q_over_e, mc2, mg;
+    float muf;          /* mu rounded to FP32 (FP32 field mode) */
+    float pad2;
 };
 
 struct DRun {

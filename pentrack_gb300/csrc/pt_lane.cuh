@@ -280,6 +280,10 @@ struct Lane {
     /* TParticle::derivs + EquationOfMotion (src/particle.cpp:96-135) */
     __device__ void derivs(const double *yy, double tt, double *d, bool keepB = false) {
         const DSpecies &sp = R.sp;
+        if (sp.q == 0 && R.prec == PT_PREC_FP32) {
+            derivs_neutral32(yy, tt, d, keepB);
+            return;
+        }
         double B[3] = {0, 0, 0}, dB[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, E[3] = {0, 0, 0}, V = 0;
         if (sp.q != 0 || (sp.mu != 0 && yy[7] != 0)) {
             bfield<true>(S, R.prec, yy[0], yy[1], yy[2], B, dB);
@@ -306,6 +310,46 @@ struct Lane {
             F1 += yy[7] * sp.mu * g1;
             F2 += yy[7] * sp.mu * g2;
         }
+        double v2 = yy[3] * yy[3] + yy[4] * yy[4] + yy[5] * yy[5];
+        double ig = sqrt(1 - v2 * PT_INV_C0_SQ);
+        double vF = (yy[3] * F0 + yy[4] * F1 + yy[5] * F2) * PT_INV_C0_SQ;
+        double s = ig * sp.inv_mkg;
+        d[3] = s * (F0 - yy[3] * vF);
+        d[4] = s * (F1 - yy[4] * vF);
+        d[5] = s * (F2 - yy[5] * vF);
+        d[6] = ig;
+        d[7] = 0;
+        d[8] = sqrt(v2);
+    }
+
+    /* The neutral-particle equation of motion in the FP32 field mode: B,
+     * grad B and the magnetic gradient force pol mu grad|B| in FP32 (relative
+     * error ~1e-7 of a force well below gravity), gravity, the relativistic
+     * factors and the state derivative in FP64. */
+    __device__ void derivs_neutral32(const double *yy, double tt, double *d, bool keepB) {
+        const DSpecies &sp = R.sp;
+        double F0 = 0, F1 = 0, F2 = sp.fgrav;
+        if (sp.mu != 0 && yy[7] != 0) {
+            float B[3], dB[3][3];
+            bfield32<true>(S, yy[0], yy[1], yy[2], B, dB);
+            ++lc.fields;
+            if (keepB) {
+                const double Bd[3] = {B[0], B[1], B[2]};
+                bc_put(yy[0], yy[1], yy[2], tt, Bd);
+            }
+            if (B[0] != 0 || B[1] != 0 || B[2] != 0) {
+                const float bb = fmaf(B[2], B[2], fmaf(B[1], B[1], B[0] * B[0]));
+                const float s = (float)yy[7] * sp.muf / sqrtf(bb);
+                const float g0 = fmaf(B[2], dB[2][0], fmaf(B[1], dB[1][0], B[0] * dB[0][0]));
+                const float g1 = fmaf(B[2], dB[2][1], fmaf(B[1], dB[1][1], B[0] * dB[0][1]));
+                const float g2 = fmaf(B[2], dB[2][2], fmaf(B[1], dB[1][2], B[0] * dB[0][2]));
+                F0 += (double)(s * g0);
+                F1 += (double)(s * g1);
+                F2 += (double)(s * g2);
+            }
+        }
+        ++lc.rhs;
+        d[0] = yy[3]; d[1] = yy[4]; d[2] = yy[5];
         double v2 = yy[3] * yy[3] + yy[4] * yy[4] + yy[5] * yy[5];
         double ig = sqrt(1 - v2 * PT_INV_C0_SQ);
         double vF = (yy[3] * F0 + yy[4] * F1 + yy[5] * F2) * PT_INV_C0_SQ;

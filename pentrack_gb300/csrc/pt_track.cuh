@@ -364,39 +364,38 @@ __device__ void hermite_cell(const T *__restrict__ nodes, int ncomp, int c0, int
  * ~1e-7 of a small quantity and the force is smooth to the 1e-9 step-size
  * controller. */
 template <bool GRAD>
-__device__ void tab3_mixed(const DField &f, int c0, int nc, double x, double y, double z, double *F, double (*dF)[3]) {
+__device__ void tab3_f32(const DField &f, int c0, int nc, float x, float y, float z, float *F, float (*dF)[3]) {
     int ix, iy, iz;
-    double u, v, w;
+    float u, v, w;
     {
-        const double r[3] = {x, y, z};
+        const float r[3] = {x, y, z};
         int idx[3];
-        double loc[3];
+        float loc[3];
         for (int a = 0; a < 3; ++a) {
-            const double *ax = f.ax[a];
+            const float *ax = f.ax32[a];
             const int n = f.n[a];
-            double g = (r[a] - f.a0[a]) * f.inv_h[a];
+            const float g = (r[a] - f.a0f[a]) * f.inv_hf[a];
             int k;
-            if (!(g > -1.0)) k = 0;
-            else if (!(g < (double)n)) k = n;
-            else k = (int)floor(g) + 1;
+            if (!(g > -1.0f)) k = 0;
+            else if (!(g < (float)n)) k = n;
+            else k = (int)floorf(g) + 1;
             while (k < n && ax[k] <= r[a]) ++k;
             while (k > 0 && ax[k - 1] > r[a]) --k;
             if (k >= n || k == 0) return;
             idx[a] = k - 1;
-            loc[a] = (r[a] - ax[k - 1]) * f.inv_w[a][k - 1];
+            loc[a] = (r[a] - ax[k - 1]) * f.inv_w32[a][k - 1];
         }
         ix = idx[0]; iy = idx[1]; iz = idx[2];
         u = loc[0]; v = loc[1]; w = loc[2];
     }
-    const double hx = f.ax[0][ix + 1] - f.ax[0][ix], hy = f.ax[1][iy + 1] - f.ax[1][iy], hz = f.ax[2][iz + 1] - f.ax[2][iz];
     Herm<float> U, V, W;
-    U.set((float)u, (float)hx, (float)f.inv_w[0][ix]);
-    V.set((float)v, (float)hy, (float)f.inv_w[1][iy]);
-    W.set((float)w, (float)hz, (float)f.inv_w[2][iz]);
+    U.set(u, f.ax32[0][ix + 1] - f.ax32[0][ix], f.inv_w32[0][ix]);
+    V.set(v, f.ax32[1][iy + 1] - f.ax32[1][iy], f.inv_w32[1][iy]);
+    W.set(w, f.ax32[2][iz + 1] - f.ax32[2][iz], f.inv_w32[2][iz]);
     const int64_t cell = ((int64_t)ix * (f.n[1] - 1) + iy) * (f.n[2] - 1) + iz;
     const float *cd = f.cell32 + cell * f.ncomp * 64;
-    const double *cb = f.cell64 + cell * f.ncomp * 4;
-    const double dx = x - f.ax[0][ix], dy = y - f.ax[1][iy], dz = z - f.ax[2][iz];
+    const float *cb = f.cellb32 + cell * f.ncomp * 4;
+    const float dx = x - f.ax32[0][ix], dy = y - f.ax32[1][iy], dz = z - f.ax32[2][iz];
     const int dtab[2][2][2] = {{{0, 3}, {2, 6}}, {{1, 5}, {4, 7}}};
     for (int c = c0; c < c0 + nc; ++c) {
         const float *cc = cd + c * 64;
@@ -432,23 +431,20 @@ __device__ void tab3_mixed(const DField &f, int c0, int nc, double x, double y, 
                     fz = fmaf(tzp, U.w[p], fz);
                 }
             }
-        const double *b = cb + c * 4;
-        F[c - c0] = fma(b[3], dz, fma(b[2], dy, fma(b[1], dx, b[0]))) + (double)fr;
+        /* linear base of the cell plus the Hermite remainder */
+        const float *b = cb + c * 4;
+        F[c - c0] = fmaf(b[3], dz, fmaf(b[2], dy, fmaf(b[1], dx, b[0]))) + fr;
         if (GRAD) {
-            dF[c - c0][0] = b[1] + (double)fx;
-            dF[c - c0][1] = b[2] + (double)fy;
-            dF[c - c0][2] = b[3] + (double)fz;
+            dF[c - c0][0] = b[1] + fx;
+            dF[c - c0][1] = b[2] + fy;
+            dF[c - c0][2] = b[3] + fz;
         }
     }
 }
 
 /* TabField3 B (and gradient) of one field; outputs untouched outside the grid */
 template <bool GRAD>
-__device__ void tab3_b(const DField &f, int prec, double x, double y, double z, double B[3], double (*dB)[3]) {
-    if (prec == PT_PREC_FP32 && f.cell32) {
-        tab3_mixed<GRAD>(f, 0, 3, x, y, z, B, dB);
-        return;
-    }
+__device__ void tab3_b(const DField &f, double x, double y, double z, double B[3], double (*dB)[3]) {
     int ix, iy, iz;
     double u, v, w, hx, hy, hz;
     if (!locate(f, 0, x, ix, u, hx) || !locate(f, 1, y, iy, v, hy) || !locate(f, 2, z, iz, w, hz)) return;
@@ -465,7 +461,10 @@ __device__ void tab3_b(const DField &f, int prec, double x, double y, double z, 
 __device__ void tab3_v(const DField &f, int prec, double x, double y, double z, double &Vv, double E[3]) {
     double F[1] = {Vv}, dF[1][3] = {{0, 0, 0}};
     if (prec == PT_PREC_FP32 && f.cell32) {
-        tab3_mixed<true>(f, 3, 1, x, y, z, F, dF);
+        float F32[1] = {(float)Vv}, dF32[1][3] = {{0, 0, 0}};
+        tab3_f32<true>(f, 3, 1, (float)x, (float)y, (float)z, F32, dF32);
+        F[0] = F32[0];
+        for (int k = 0; k < 3; ++k) dF[0][k] = dF32[0][k];
     } else {
         int ix, iy, iz;
         double u, v, w, hx, hy, hz;
@@ -508,9 +507,10 @@ __device__ void harmonic_b(const DField &f, double x, double y, double z, double
     }
 }
 
-/* TFieldManager::BField (src/fields.cpp:139-164) over TFieldContainer::BField (src/field.cpp:139-155) */
+/* TFieldManager::BField (src/fields.cpp:139-164) over TFieldContainer::BField
+ * (src/field.cpp:139-155) in FP64 */
 template <bool GRAD>
-__device__ void bfield(const DScene &S, int prec, double x, double y, double z, double B[3], double (*dB)[3]) {
+__device__ void bfield64(const DScene &S, double x, double y, double z, double B[3], double (*dB)[3]) {
     B[0] = B[1] = B[2] = 0;
     if (GRAD)
         for (int i = 0; i < 3; ++i) dB[i][0] = dB[i][1] = dB[i][2] = 0;
@@ -519,7 +519,7 @@ __device__ void bfield(const DScene &S, int prec, double x, double y, double z, 
         if (!f.has_b) continue;
         if (!fbox_in(f, x, y, z) || f.bscale == 0.) continue;
         double Bt[3] = {0, 0, 0}, dBt[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-        if (f.type == PT_FIELD_TAB3D) tab3_b<GRAD>(f, prec, x, y, z, Bt, dBt);
+        if (f.type == PT_FIELD_TAB3D) tab3_b<GRAD>(f, x, y, z, Bt, dBt);
         else if (f.type == PT_FIELD_HARMONIC) harmonic_b<GRAD>(f, x, y, z, Bt, dBt);
         for (int i = 0; i < 3; ++i) {
             Bt[i] *= f.bscale;
@@ -531,6 +531,66 @@ __device__ void bfield(const DScene &S, int prec, double x, double y, double z, 
             if (GRAD) for (int j = 0; j < 3; ++j) dB[i][j] += dBt[i][j];
         }
     }
+}
+
+/* The same superposition in the FP32 field mode: tables without a smoothing
+ * band are evaluated in FP32 from the cell's FP32 linear base plus the FP32
+ * Hermite remainder (relative error ~1e-7 in B and grad B, no cancellation
+ * since the base gradient is stored); every other field is evaluated in FP64
+ * and rounded. */
+template <bool GRAD>
+__device__ void bfield32(const DScene &S, double x, double y, double z, float B[3], float (*dB)[3]) {
+    B[0] = B[1] = B[2] = 0;
+    if (GRAD)
+        for (int i = 0; i < 3; ++i) dB[i][0] = dB[i][1] = dB[i][2] = 0;
+    for (int fi = 0; fi < S.n_fields; ++fi) {
+        const DField &f = S.fields[fi];
+        if (!f.has_b) continue;
+        if (!fbox_in(f, x, y, z) || f.bscale == 0.) continue;
+        float Bt[3] = {0, 0, 0}, dBt[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        if (f.type == PT_FIELD_TAB3D && f.cell32 && !(f.bw > 0 && fbox_has(f))) {
+            tab3_f32<GRAD>(f, 0, 3, (float)x, (float)y, (float)z, Bt, dBt);
+            if (f.bscale != 1.0) {
+                const float sc = (float)f.bscale;
+                for (int i = 0; i < 3; ++i) {
+                    Bt[i] *= sc;
+                    if (GRAD) for (int j = 0; j < 3; ++j) dBt[i][j] *= sc;
+                }
+            }
+        } else {
+            double Bd[3] = {0, 0, 0}, dBd[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            if (f.type == PT_FIELD_TAB3D) tab3_b<GRAD>(f, x, y, z, Bd, dBd);
+            else if (f.type == PT_FIELD_HARMONIC) harmonic_b<GRAD>(f, x, y, z, Bd, dBd);
+            for (int i = 0; i < 3; ++i) {
+                Bd[i] *= f.bscale;
+                if (GRAD) for (int j = 0; j < 3; ++j) dBd[i][j] *= f.bscale;
+            }
+            for (int i = 0; i < 3; ++i) scale_at_bounds(f, x, y, z, Bd[i], GRAD ? dBd[i] : nullptr);
+            for (int i = 0; i < 3; ++i) {
+                Bt[i] = (float)Bd[i];
+                if (GRAD) for (int j = 0; j < 3; ++j) dBt[i][j] = (float)dBd[i][j];
+            }
+        }
+        for (int i = 0; i < 3; ++i) {
+            B[i] += Bt[i];
+            if (GRAD) for (int j = 0; j < 3; ++j) dB[i][j] += dBt[i][j];
+        }
+    }
+}
+
+/* B (and grad B) in the requested field precision */
+template <bool GRAD>
+__device__ void bfield(const DScene &S, int prec, double x, double y, double z, double B[3], double (*dB)[3]) {
+    if (prec == PT_PREC_FP32) {
+        float Bf[3], dBf[3][3];
+        bfield32<GRAD>(S, x, y, z, Bf, dBf);
+        for (int i = 0; i < 3; ++i) {
+            B[i] = Bf[i];
+            if (GRAD) for (int j = 0; j < 3; ++j) dB[i][j] = dBf[i][j];
+        }
+        return;
+    }
+    bfield64<GRAD>(S, x, y, z, B, dB);
 }
 
 /* TFieldManager::EField (src/fields.cpp:167-182) */
