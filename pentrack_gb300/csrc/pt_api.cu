@@ -106,7 +106,7 @@ __global__ void k_zero_counts(int32_t *count, int a, int b, int c) {
 
 /* Batched form, phase 1: exactly one Dormand-Prince try for every active
  * particle (all lanes execute the same instruction stream). */
-__global__ void __launch_bounds__(128) k_try(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out) {
+__global__ void __launch_bounds__(128, 3) k_try(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out) {
     const int n = b.count[in];
     const int32_t *lin = b.list[in];
     Lane L(S, R);

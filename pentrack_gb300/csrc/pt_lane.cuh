@@ -1099,6 +1099,9 @@ struct Lane {
                 if (!check_segment(S, P.cya, P.y2)) { stop = PT_ID_HIT_BOUNDARIES; ch = true; P.stage = PS_CHECK_DONE; continue; }
                 if (P.x2 == P.cx1) { ch = false; P.stage = PS_CHECK_DONE; continue; }
                 P.cs = cur_solid();
+                /* the candidate triangles of the chord's stretch of curve serve
+                 * this query and the bisection that follows a hit */
+                if (ncand < 0 && P.cx1 >= to && P.x2 <= tn) prepare_candidates(P.cx1, P.x2);
                 int h = any_hit(P.cya, P.y2);
                 if (h < 0) { stop = PT_ID_CGAL_ERROR; ch = true; P.stage = PS_CHECK_DONE; continue; }
                 if (!h) {
@@ -1107,7 +1110,6 @@ struct Lane {
                     P.stage = PS_CHECK_DONE;
                     continue;
                 }
-                if (ncand < 0 && P.cx1 >= to && P.x2 <= tn) prepare_candidates(P.cx1, P.x2);
                 P.stage = PS_AFTER_BISECT;
                 return 1; /* TTracker::iterate_collision on (cx1, cya) -> (x2, y2) */
             } else if (P.stage == PS_AFTER_BISECT) {

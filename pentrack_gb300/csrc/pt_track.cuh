@@ -675,50 +675,58 @@ __device__ __forceinline__ bool tri_box_touch(const DTri &t, const double *p, co
 /* Separating-axis overlap test of a triangle and an axis-aligned box given by
  * centre c and half sizes e (Akenine-Moeller, "Fast 3D triangle-box overlap
  * testing", 2001): box axes, triangle normal, and the nine edge x axis
- * cross products.  Used with a box enlarged by a safety margin, so FP64
- * rounding can only add candidates, never drop one. */
-__device__ bool tri_box_overlap(const DTri &t, const double *c, const double *e) {
-    double v0[3], v1[3], v2[3];
+ * cross products, in FP32 on the triangle's FP32 copy.  Every axis the test
+ * uses is the FP32 vector it computes, taken as exact; the vertices' FP32
+ * rounding (<= 2^-24 of the coordinate each for the vertex and the centre)
+ * and the arithmetic of a projection (<= 3 x 2^-24 of its terms) move a
+ * projection by at most |axis|_1 x 10 x 2^-24 x M, M the largest coordinate
+ * magnitude involved; the caller widens e by that much per unit axis, so
+ * separation is only reported where it exactly holds.  A candidate set built
+ * with it can only be too large, never miss a triangle. */
+__device__ bool tri_box_overlap32(const DTri32 &t, const float *c, const float *e) {
+    float v0[3], v1[3], v2[3];
     for (int k = 0; k < 3; ++k) { v0[k] = t.a[k] - c[k]; v1[k] = t.b[k] - c[k]; v2[k] = t.c[k] - c[k]; }
     for (int k = 0; k < 3; ++k) {
-        double mn = fmin(v0[k], fmin(v1[k], v2[k])), mx = fmax(v0[k], fmax(v1[k], v2[k]));
+        const float mn = fminf(v0[k], fminf(v1[k], v2[k])), mx = fmaxf(v0[k], fmaxf(v1[k], v2[k]));
         if (mn > e[k] || mx < -e[k]) return false;
     }
-    double f[3][3];
+    float f[3][3];
     for (int k = 0; k < 3; ++k) { f[0][k] = v1[k] - v0[k]; f[1][k] = v2[k] - v1[k]; f[2][k] = v0[k] - v2[k]; }
-    const double *vv[3] = {v0, v1, v2};
+    const float *vv[3] = {v0, v1, v2};
+#pragma unroll
     for (int i = 0; i < 3; ++i)       /* edge i */
+#pragma unroll
         for (int a = 0; a < 3; ++a) { /* box axis a: axis = e_a x f_i */
-            double ax[3] = {0, 0, 0};
             const int a1 = (a + 1) % 3, a2 = (a + 2) % 3;
-            ax[a1] = -f[i][a2];
-            ax[a2] = f[i][a1];
-            double pmin = 1e300, pmax = -1e300;
+            const float x1 = -f[i][a2], x2 = f[i][a1];
+            float pmin = 3e38f, pmax = -3e38f;
             for (int v = 0; v < 3; ++v) {
-                double pr = ax[0] * vv[v][0] + ax[1] * vv[v][1] + ax[2] * vv[v][2];
-                pmin = fmin(pmin, pr);
-                pmax = fmax(pmax, pr);
+                const float pr = x1 * vv[v][a1] + x2 * vv[v][a2];
+                pmin = fminf(pmin, pr);
+                pmax = fmaxf(pmax, pr);
             }
-            double r = e[0] * fabs(ax[0]) + e[1] * fabs(ax[1]) + e[2] * fabs(ax[2]);
+            const float r = (e[a1] * fabsf(x1) + e[a2] * fabsf(x2)) * 1.0000005f;
             if (pmin > r || pmax < -r) return false;
         }
     /* plane of the triangle */
-    double d = t.n[0] * v0[0] + t.n[1] * v0[1] + t.n[2] * v0[2];
-    double r = e[0] * fabs(t.n[0]) + e[1] * fabs(t.n[1]) + e[2] * fabs(t.n[2]);
+    const float d = t.n[0] * v0[0] + t.n[1] * v0[1] + t.n[2] * v0[2];
+    const float r = (e[0] * fabsf(t.n[0]) + e[1] * fabsf(t.n[1]) + e[2] * fabsf(t.n[2])) * 1.0000005f;
     if (d > r || d < -r) return false;
     return true;
 }
 
 /* indices of the triangles that may touch the box [lo, hi]; -1 if more than maxc */
 __device__ int collect_candidates(const DScene &S, const double *lo, const double *hi, int *cand, int maxc, QueryStats &qs) {
-    float flo[3], fhi[3];
-    double c[3], e[3];
+    float flo[3], fhi[3], c[3], e[3];
+    double m = 0;
     for (int k = 0; k < 3; ++k) {
         flo[k] = __double2float_rd(lo[k]);
         fhi[k] = __double2float_ru(hi[k]);
-        c[k] = 0.5 * (lo[k] + hi[k]);
-        e[k] = 0.5 * (hi[k] - lo[k]);
+        c[k] = (float)(0.5 * (lo[k] + hi[k]));
+        m = fmax(m, fmax(fabs(lo[k]), fabs(hi[k])));
     }
+    const float M = __double2float_ru(m);
+    for (int k = 0; k < 3; ++k) e[k] = __double2float_ru(0.5 * (hi[k] - lo[k]));
     int nc = 0;
     int i = 0;
     while (i < S.n_nodes) {
@@ -730,7 +738,11 @@ __device__ int collect_candidates(const DScene &S, const double *lo, const doubl
         if (nd.leaf < 0) { ++i; continue; }
         int first = nd.leaf >> 3, cnt = nd.leaf & 7;
         for (int j = first; j < first + cnt; ++j) {
-            if (!tri_box_overlap(S.tris[j], c, e)) continue;
+            const DTri32 &t = S.tri32[j];
+            /* widen the box by the FP32 error bound of the test (per unit axis) */
+            const float w = 1.3e-6f * fmaxf(M, t.m) + 1e-30f;
+            const float ew[3] = {e[0] + w, e[1] + w, e[2] + w};
+            if (!tri_box_overlap32(t, c, ew)) continue;
             if (nc >= maxc) return -1;
             cand[nc++] = j;
         }
