@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(128) k_post(const __grid_constant__ DScene S, 
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const int i = lp[k];
         L.load(b, i);
-        L.load_dense(b, i);
+        L.load_try_end(b, i);
         L.load_bc(b, i);
         const double t0 = L.t;
         if (L.fast_post()) {

@@ -129,6 +129,14 @@ struct Lane {
         }
         tn = b.tn[i];
     }
+    /* what the fast completion reads of the accepted try: its end point and
+     * end derivative (no stage vectors: it never evaluates the dense output) */
+    __device__ void load_try_end(const DBatch &b, int64_t i) {
+        const int64_t n = b.n;
+        to = t;
+        for (int c = 0; c < 9; ++c) { xo[c] = y[c]; dxo[c] = dydt[c]; yn[c] = b.yn[c * n + i]; dyn[c] = b.dyn[c * n + i]; }
+        tn = b.tn[i];
+    }
     /* global B caches: slot 0 holds B at the committed point (t, y), slot 1 B
      * at the end point of the last accepted try (tn, yn) */
     __device__ void load_bc(const DBatch &b, int64_t i) {
