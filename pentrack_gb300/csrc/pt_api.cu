@@ -551,15 +551,10 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
             o.node64 = dupload(c->allocs, nd.data(), nd.size(), e);
             if (e) return ck(c, e, "upload table"), PT_ERR_CUDA;
             {
-                std::vector<double> base;
-                std::vector<float> rem;
-                pth::mixed_cells(ax, nd, o.ncomp, base, rem);
-                std::vector<float> basef(base.begin(), base.end());
-                o.cellb32 = dupload(c->allocs, basef.data(), basef.size(), e);
-                if (e) return ck(c, e, "upload cell table"), PT_ERR_CUDA;
-                o.cell32 = dupload(c->allocs, rem.data(), rem.size(), e);
-                if (e) return ck(c, e, "upload cell table"), PT_ERR_CUDA;
-                o.node32 = nullptr;
+                std::vector<float> n32;
+                o.node32_stride = pth::node_table32(nd, o.ncomp, n32);
+                o.node32 = dupload(c->allocs, n32.data(), n32.size(), e);
+                if (e) return ck(c, e, "upload FP32 node table"), PT_ERR_CUDA;
             }
             int n3[3] = {f.nx, f.ny, f.nz};
             for (int a = 0; a < 3; ++a) {

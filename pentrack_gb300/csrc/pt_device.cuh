@@ -90,12 +90,12 @@ struct DField {
     const double *ax[3];
     double a0[3], inv_h[3];
     const double *node64;  /* [node][comp][8]: f, fx, fy, fz, fxy, fxz, fyz, fxyz */
+    /* FP32 node table of the FP32 field mode: per node, for each component,
+     * the value split into FP32 high and low parts and the seven derivative
+     * values (fx, fy, fz, fxy, fxz, fyz, fxyz); node32_stride floats per node */
     const float *node32;
-    /* mixed-precision cell table: per cell and component a linear base
-     * (f at the cell's first corner, gradient g) in FP64 and the Hermite data
-     * of the remainder f - base at the 8 corners in FP32 */
-    const float *cellb32;  /* [cell][comp][4]: f0, gx, gy, gz */
-    const float *cell32;   /* [cell][comp][corner][8] */
+    int node32_stride;
+    int pad2;
     const double *inv_w[3]; /* 1 / cell width per axis interval */
     const float *ax32[3];   /* FP32 copies of the axes and widths for the FP32 field mode */
     const float *inv_w32[3];

@@ -189,41 +189,20 @@ void hermite_nodes(const std::vector<double> ax[3], const double *tabp, int comp
         for (int k = 0; k < 8; ++k) out[i * stride + comp * 8 + k] = (*src[k])[i];
 }
 
-void mixed_cells(const std::vector<double> ax[3], const std::vector<double> &nodes, int ncomp, std::vector<double> &base,
-                 std::vector<float> &rem) {
-    const size_t n[3] = {ax[0].size(), ax[1].size(), ax[2].size()};
-    const size_t nc = (n[0] - 1) * (n[1] - 1) * (n[2] - 1);
-    base.assign(nc * ncomp * 4, 0.0);
-    rem.assign(nc * ncomp * 64, 0.0f);
-    const size_t stride = (size_t)ncomp * 8;
-    for (size_t ix = 0; ix + 1 < n[0]; ++ix)
-        for (size_t iy = 0; iy + 1 < n[1]; ++iy)
-            for (size_t iz = 0; iz + 1 < n[2]; ++iz) {
-                const size_t cell = (ix * (n[1] - 1) + iy) * (n[2] - 1) + iz;
-                for (int c = 0; c < ncomp; ++c) {
-                    const double *node[8];
-                    for (int k = 0; k < 8; ++k) {
-                        size_t i = ix + (k & 1), j = iy + ((k >> 1) & 1), l = iz + ((k >> 2) & 1);
-                        node[k] = &nodes[((i * n[1] + j) * n[2] + l) * stride + c * 8];
-                    }
-                    double f0 = node[0][0], g[3] = {0, 0, 0};
-                    for (int k = 0; k < 8; ++k)
-                        for (int a = 0; a < 3; ++a) g[a] += node[k][1 + a];
-                    for (int a = 0; a < 3; ++a) g[a] *= 0.125;
-                    double *b = &base[(cell * ncomp + c) * 4];
-                    b[0] = f0; b[1] = g[0]; b[2] = g[1]; b[3] = g[2];
-                    for (int k = 0; k < 8; ++k) {
-                        double d[3] = {ax[0][ix + (k & 1)] - ax[0][ix], ax[1][iy + ((k >> 1) & 1)] - ax[1][iy],
-                                       ax[2][iz + ((k >> 2) & 1)] - ax[2][iz]};
-                        float *r = &rem[((cell * ncomp + c) * 8 + k) * 8];
-                        r[0] = (float)(node[k][0] - (f0 + g[0] * d[0] + g[1] * d[1] + g[2] * d[2]));
-                        r[1] = (float)(node[k][1] - g[0]);
-                        r[2] = (float)(node[k][2] - g[1]);
-                        r[3] = (float)(node[k][3] - g[2]);
-                        for (int m = 4; m < 8; ++m) r[m] = (float)node[k][m];
-                    }
-                }
-            }
+int node_table32(const std::vector<double> &nodes, int ncomp, std::vector<float> &out) {
+    const int stride = (ncomp * 9 + 3) / 4 * 4;
+    const size_t nn = nodes.size() / (size_t)(ncomp * 8);
+    out.assign(nn * stride, 0.0f);
+    for (size_t i = 0; i < nn; ++i)
+        for (int c = 0; c < ncomp; ++c) {
+            const double *src = &nodes[(i * ncomp + c) * 8];
+            float *dst = &out[i * stride + c * 9];
+            const float hi = (float)src[0];
+            dst[0] = hi;
+            dst[1] = (float)(src[0] - (double)hi);
+            for (int k = 1; k < 8; ++k) dst[k + 1] = (float)src[k];
+        }
+    return stride;
 }
 
 /* ---------------------------------------------------------------- harmonic */

@@ -31,13 +31,11 @@ void spline_derivs(int n, const double *x, const double *y, double *d);
  * (src/field_3d.cpp:374-381).  out[node*stride + comp*8 + k]. */
 void hermite_nodes(const std::vector<double> ax[3], const double *tab, int comp, int stride, std::vector<double> &out);
 
-/* Mixed-precision cell table from per-node Hermite data (stride ncomp*8):
- * per cell and component a linear base (value at the cell's first corner and
- * the mean of the 8 corner gradients) in FP64, and the Hermite data of the
- * remainder (value minus base, first derivatives minus the base gradient,
- * cross derivatives unchanged) at the 8 corners in FP32. */
-void mixed_cells(const std::vector<double> ax[3], const std::vector<double> &nodes, int ncomp, std::vector<double> &base,
-                 std::vector<float> &rem);
+/* FP32 node table from per-node Hermite data (stride ncomp*8): per node and
+ * component 9 floats -- the value as FP32 high part and FP32 rounding of the
+ * rest, then fx, fy, fz, fxy, fxz, fyz, fxyz rounded to FP32 -- with the
+ * node record padded to a multiple of 4 floats.  Returns the floats per node. */
+int node_table32(const std::vector<double> &nodes, int ncomp, std::vector<float> &out);
 
 /* Harmonic expansion (HarmonicExpandedBField, src/harmonicfields.cpp:50-829)
  * written as one scalar polynomial Phi with B = grad Phi.  Each G(l,m) adds

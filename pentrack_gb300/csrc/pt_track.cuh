@@ -392,13 +392,22 @@ __device__ void tab3_f32(const DField &f, int c0, int nc, float x, float y, floa
     U.set(u, f.ax32[0][ix + 1] - f.ax32[0][ix], f.inv_w32[0][ix]);
     V.set(v, f.ax32[1][iy + 1] - f.ax32[1][iy], f.inv_w32[1][iy]);
     W.set(w, f.ax32[2][iz + 1] - f.ax32[2][iz], f.inv_w32[2][iz]);
-    const int64_t cell = ((int64_t)ix * (f.n[1] - 1) + iy) * (f.n[2] - 1) + iz;
-    const float *cd = f.cell32 + cell * f.ncomp * 64;
-    const float *cb = f.cellb32 + cell * f.ncomp * 4;
-    const float dx = x - f.ax32[0][ix], dy = y - f.ax32[1][iy], dz = z - f.ax32[2][iz];
+    /* Node records of the cell's corners.  The tricubic is evaluated as the
+     * linear function L = f0 + g0 . (r - r0) of corner (0, 0, 0) (value f0 from
+     * its FP32 high/low parts, gradient g0 from its derivative data) plus the
+     * interpolant of f - L, which cubic Hermite interpolation reproduces
+     * exactly.  The data of f - L are curvature-sized, so FP32 accumulation
+     * keeps B and grad B to ~1e-7 relative instead of cancelling. */
+    const int S = f.node32_stride;
+    const int64_t nz = f.n[2], nyz = (int64_t)f.n[1] * nz;
+    const float *T0 = f.node32 + (((int64_t)ix * f.n[1] + iy) * nz + iz) * S;
+    const float hx = f.ax32[0][ix + 1] - f.ax32[0][ix], hy = f.ax32[1][iy + 1] - f.ax32[1][iy],
+                hz = f.ax32[2][iz + 1] - f.ax32[2][iz];
+    const float rx = x - f.ax32[0][ix], ry = y - f.ax32[1][iy], rz = z - f.ax32[2][iz];
     const int dtab[2][2][2] = {{{0, 3}, {2, 6}}, {{1, 5}, {4, 7}}};
     for (int c = c0; c < c0 + nc; ++c) {
-        const float *cc = cd + c * 64;
+        const float h0 = T0[c * 9], l0 = T0[c * 9 + 1];
+        const float g[3] = {T0[c * 9 + 2], T0[c * 9 + 3], T0[c * 9 + 4]};
         float fr = 0, fx = 0, fy = 0, fz = 0;
 #pragma unroll
         for (int cx = 0; cx < 2; ++cx)
@@ -408,13 +417,31 @@ __device__ void tab3_f32(const DField &f, int c0, int nc, float x, float y, floa
                 float tp = 0, typ = 0, tzp = 0;
 #pragma unroll
                 for (int cy = 0; cy < 2; ++cy) {
-                    const float *n0 = cc + (cx + 2 * cy) * 8;  /* corner (cx, cy, 0) */
-                    const float *n1 = n0 + 4 * 8;             /* corner (cx, cy, 1) */
+                    const float *n0 = T0 + (cx * nyz + cy * nz) * S + c * 9; /* corner (cx, cy, 0) */
+                    const float *n1 = n0 + S;                               /* corner (cx, cy, 1) */
+                    const float lxy = fmaf(g[1], cy ? hy : 0.0f, g[0] * (cx ? hx : 0.0f)); /* L - f0 at (cx, cy, 0) */
 #pragma unroll
                     for (int ay = 0; ay < 2; ++ay) {
                         const int q = cy + 2 * ay;
                         const int d0 = dtab[ax_][ay][0], d1 = dtab[ax_][ay][1];
-                        const float v0 = n0[d0], v1 = n1[d0], v2 = n0[d1], v3 = n1[d1];
+                        float v0, v1, v2, v3;
+                        if (d0 == 0) {
+                            v0 = ((n0[0] - h0) + (n0[1] - l0)) - lxy;
+                            v1 = ((n1[0] - h0) + (n1[1] - l0)) - fmaf(g[2], hz, lxy);
+                        } else if (d0 <= 3) {
+                            v0 = n0[d0 + 1] - g[d0 - 1];
+                            v1 = n1[d0 + 1] - g[d0 - 1];
+                        } else {
+                            v0 = n0[d0 + 1];
+                            v1 = n1[d0 + 1];
+                        }
+                        if (d1 <= 3) {
+                            v2 = n0[d1 + 1] - g[d1 - 1];
+                            v3 = n1[d1 + 1] - g[d1 - 1];
+                        } else {
+                            v2 = n0[d1 + 1];
+                            v3 = n1[d1 + 1];
+                        }
                         const float sv = fmaf(v3, W.w[3], fmaf(v2, W.w[2], fmaf(v1, W.w[1], v0 * W.w[0])));
                         tp = fmaf(sv, V.w[q], tp);
                         if (GRAD) {
@@ -431,13 +458,11 @@ __device__ void tab3_f32(const DField &f, int c0, int nc, float x, float y, floa
                     fz = fmaf(tzp, U.w[p], fz);
                 }
             }
-        /* linear base of the cell plus the Hermite remainder */
-        const float *b = cb + c * 4;
-        F[c - c0] = fmaf(b[3], dz, fmaf(b[2], dy, fmaf(b[1], dx, b[0]))) + fr;
+        F[c - c0] = h0 + (l0 + (fmaf(g[2], rz, fmaf(g[1], ry, g[0] * rx)) + fr));
         if (GRAD) {
-            dF[c - c0][0] = b[1] + fx;
-            dF[c - c0][1] = b[2] + fy;
-            dF[c - c0][2] = b[3] + fz;
+            dF[c - c0][0] = g[0] + fx;
+            dF[c - c0][1] = g[1] + fy;
+            dF[c - c0][2] = g[2] + fz;
         }
     }
 }
@@ -460,7 +485,7 @@ __device__ void tab3_b(const DField &f, double x, double y, double z, double B[3
 /* TabField3 potential V and E = -grad V */
 __device__ void tab3_v(const DField &f, int prec, double x, double y, double z, double &Vv, double E[3]) {
     double F[1] = {Vv}, dF[1][3] = {{0, 0, 0}};
-    if (prec == PT_PREC_FP32 && f.cell32) {
+    if (prec == PT_PREC_FP32 && f.node32) {
         float F32[1] = {(float)Vv}, dF32[1][3] = {{0, 0, 0}};
         tab3_f32<true>(f, 3, 1, (float)x, (float)y, (float)z, F32, dF32);
         F[0] = F32[0];
@@ -548,7 +573,7 @@ __device__ void bfield32(const DScene &S, double x, double y, double z, float B[
         if (!f.has_b) continue;
         if (!fbox_in(f, x, y, z) || f.bscale == 0.) continue;
         float Bt[3] = {0, 0, 0}, dBt[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-        if (f.type == PT_FIELD_TAB3D && f.cell32 && !(f.bw > 0 && fbox_has(f))) {
+        if (f.type == PT_FIELD_TAB3D && f.node32 && !(f.bw > 0 && fbox_has(f))) {
             tab3_f32<GRAD>(f, 0, 3, (float)x, (float)y, (float)z, Bt, dBt);
             if (f.bscale != 1.0) {
                 const float sc = (float)f.bscale;
