@@ -124,11 +124,12 @@ def algorithmic_work(st, precision):
 
 
 def setup_ours(args, rank):
-    from pentrack_gb300 import Engine, _abi as A, workloads
+    from pentrack_gb300 import Engine, _abi as A, replicas, workloads
     device = int(os.environ.get("LOCAL_RANK", 0))
     scene = workloads.field_storage_scene()
     engine = Engine(scene, device=device)
-    _, params, parts = workloads.field_storage(n=args.n, engine=engine, first_id=rank * args.n)
+    first, count = replicas.shard(args.n, rank)
+    _, params, parts = workloads.field_storage(n=count, engine=engine, first_id=first)
     params.field_precision = A.PREC_FP32 if args.precision == "fp32" else A.PREC_FP64
     params.mode = A.MODE_BATCHED if args.mode == "batched" else A.MODE_PLAIN
     return engine, params, parts, device
@@ -284,12 +285,8 @@ def run_ours(args, rank, world):
     psec = agg["particle_seconds"]
     device_ms = agg["span_ms"]
     if dist:
-        t = torch.tensor([device_ms / 1e3, psec], dtype=torch.float64, device=f"cuda:{device}")
-        tmax = t[0:1].clone()
-        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
-        tot = t[1:2].clone()
-        torch.distributed.all_reduce(tot, op=torch.distributed.ReduceOp.SUM)
-        device_s, psec_all = float(tmax[0]), float(tot[0])
+        from pentrack_gb300 import replicas
+        device_s, psec_all = replicas.reduce_timing(device_ms / 1e3, psec, device=f"cuda:{device}")
         torch.distributed.barrier()
     else:
         device_s, psec_all = device_ms / 1e3, psec

@@ -11,7 +11,8 @@ STATUS = {
     0: "PT_OK", -1: "PT_ERR_INVALID", -2: "PT_ERR_UNSUPPORTED", -3: "PT_ERR_OOM", -4: "PT_ERR_CUDA",
     -5: "PT_ERR_TIMEOUT", -6: "PT_ERR_CANCELLED", -7: "PT_ERR_IO", -8: "PT_ERR_NO_DEVICE",
 }
-PT_ERR_CANCELLED = -6
+PT_ERR_INVALID, PT_ERR_UNSUPPORTED, PT_ERR_OOM, PT_ERR_CUDA, PT_ERR_TIMEOUT = -1, -2, -3, -4, -5
+PT_ERR_CANCELLED, PT_ERR_IO, PT_ERR_NO_DEVICE = -6, -7, -8
 
 # stop IDs: include/globals.h:13-23 of the reference
 ID_UNKNOWN, ID_NOT_FINISH, ID_HIT_BOUNDARIES, ID_ODEINT_ERROR, ID_DECAYED = 0, -1, -2, -3, -4

@@ -246,7 +246,7 @@ class Engine:
         out = particles.copy()
         stats = A.Stats()
         pin, pout = particles.abi(outputs=False), out.abi()
-        self._check(lib().pt_integrate(self.h, C.byref(params), C.byref(pin), C.byref(pout), C.byref(stats)))
+        self.last_status = self._check(lib().pt_integrate(self.h, C.byref(params), C.byref(pin), C.byref(pout), C.byref(stats)))
         return out, stats.as_dict()
 
     def batch(self, params, particles):
