@@ -273,6 +273,29 @@ pt_status pt_point_solids(pt_ctx *ctx, int64_t n, const double *p, uint64_t *mas
  * a dependent-chain DFMA kernel over all SMs (TFLOP/s, 2 flops per FMA). */
 pt_status pt_probe_fp64(pt_ctx *ctx, double *tflops);
 
+/* ---- config.in front end (the reference's host inputs) ----
+ * TConfig::ReadFromFile (src/config.cpp:14-53) plus TGeometry(TConfig&)
+ * (src/geometry.cpp:93-137) and TFieldManager(TConfig&) (src/fields.cpp:19-136):
+ * builds a pt_scene_desc from a config.in with its [GEOMETRY], [MATERIALS] or
+ * materials_file, [FIELDS] (OPERA3D, 3Dtable, HarmonicExpansionBField,
+ * EDMStaticEField with constant scales) and [FORMULAS] sections; STL and table
+ * paths are relative to the config file.  The scene owns every array its
+ * descriptor points to until pt_config_free.  Errors: PT_ERR_IO (files),
+ * PT_ERR_INVALID (malformed entries), PT_ERR_UNSUPPORTED (field types, scale
+ * formulas or options the device path does not implement); message in
+ * pt_config_error(). */
+typedef struct pt_config_scene pt_config_scene;
+pt_status pt_config_load(const char *config_path, pt_config_scene **out);
+const pt_scene_desc *pt_config_scene_desc(const pt_config_scene *scene);
+void pt_config_free(pt_config_scene *scene);
+/* [GLOBAL] simtime and the particle options of [PARTICLES] overridden by the
+ * species section (tau, tmax, lmax, Bmax, spintimes, flipspin;
+ * src/tracking.cpp:19-60); spintimes are copied into the caller's buffer of
+ * max_spintimes doubles, which out->spintimes then points to. */
+pt_status pt_config_run_params(const char *config_path, const char *species, pt_run_params *out, double *spintimes,
+                               int32_t max_spintimes);
+const char *pt_config_error(void);
+
 /* Library version string. */
 const char *pt_version(void);
 

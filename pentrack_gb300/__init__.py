@@ -6,6 +6,6 @@ evaluation, BVH segment-mesh queries and wall physics.  This package is the
 Python host binding over that ABI plus synthetic-workload helpers.
 """
 from . import _abi as abi  # noqa: F401
-from .engine import Batch, Engine, EngineError, ParticleSet, Scene, lib, run_params  # noqa: F401
+from .engine import ConfigScene, config_run_params, Batch, Engine, EngineError, ParticleSet, Scene, lib, run_params  # noqa: F401
 
-__all__ = ["abi", "Batch", "Engine", "EngineError", "ParticleSet", "Scene", "lib", "run_params"]
+__all__ = ["abi", "Batch", "ConfigScene", "Engine", "EngineError", "ParticleSet", "Scene", "config_run_params", "lib", "run_params"]

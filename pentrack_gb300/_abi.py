@@ -124,6 +124,11 @@ def declare(lib):
         "pt_point_solids": (C.c_int32, [vp, C.c_int64, c_double_p, c_uint64_p]),
         "pt_probe_fp64": (C.c_int32, [vp, c_double_p]),
         "pt_version": (C.c_char_p, []),
+        "pt_config_load": (C.c_int32, [C.c_char_p, P(vp)]),
+        "pt_config_scene_desc": (P(SceneDesc), [vp]),
+        "pt_config_free": (None, [vp]),
+        "pt_config_run_params": (C.c_int32, [C.c_char_p, C.c_char_p, P(RunParams), c_double_p, C.c_int32]),
+        "pt_config_error": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -1,0 +1,543 @@
+/*
+ * pt_host.cpp -- config.in front end of the GPU path (see pt_host.hpp).
+ */
+#include "pt_host.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <filesystem>
+#include <fstream>
+#include <sstream>
+
+namespace fs = std::filesystem;
+
+namespace pth {
+
+namespace {
+
+std::string trim(const std::string &s) {
+    const char *ws = " \t\r\n";
+    size_t a = s.find_first_not_of(ws);
+    if (a == std::string::npos) return "";
+    size_t b = s.find_last_not_of(ws);
+    return s.substr(a, b - a + 1);
+}
+
+bool parse_number(const std::string &s, double &v) {
+    std::string t = trim(s);
+    if (t.empty()) return false;
+    char *end = nullptr;
+    v = std::strtod(t.c_str(), &end);
+    return end && *end == '\0';
+}
+
+/* ResolveFormula (src/field.cpp) restricted to constants: a [FORMULAS] name is
+ * replaced by its expression, which must then be a plain number */
+bool constant_scale(const std::string &tok, const Config &cfg, double &v, std::string &err) {
+    std::string e = tok;
+    auto f = cfg.find("FORMULAS");
+    if (f != cfg.end()) {
+        auto it = f->second.find(tok);
+        if (it != f->second.end()) e = it->second;
+    }
+    if (parse_number(e, v)) return true;
+    err = "field scale '" + tok + "' is not a constant; time-dependent field scaling is not implemented on the device path";
+    return false;
+}
+
+const std::map<std::string, std::string> &section(const Config &cfg, const char *name) {
+    static const std::map<std::string, std::string> empty;
+    auto it = cfg.find(name);
+    return it == cfg.end() ? empty : it->second;
+}
+
+fs::path relative_to(const std::string &config_path, const std::string &file) {
+    fs::path p(file);
+    if (p.is_absolute()) return p;
+    return fs::absolute(fs::path(config_path)).parent_path() / p;
+}
+
+} // namespace
+
+bool read_config(const std::string &path, Config &cfg, std::string &err) {
+    std::ifstream in(path);
+    if (!in) {
+        err = "Could not open " + path + "!";
+        return false;
+    }
+    std::string line, sec;
+    while (std::getline(in, line)) {
+        size_t p = line.find_first_not_of(" \t\r");
+        if (p == std::string::npos) continue;
+        const char c = line[p];
+        if (c == '[') {
+            if (p + 1 < line.size() && line[p + 1] == '/') {
+                sec.clear();
+            } else {
+                size_t q = line.find(']', p + 1);
+                sec = line.substr(p + 1, q == std::string::npos ? std::string::npos : q - p - 1);
+                cfg[sec];
+            }
+            continue;
+        }
+        if (c == '#' || sec.empty()) continue;
+        size_t ke = line.find_first_of(" \t\r", p);
+        std::string key = line.substr(p, ke == std::string::npos ? std::string::npos : ke - p);
+        std::string rest = ke == std::string::npos ? "" : line.substr(ke);
+        size_t h = rest.find('#');
+        if (h != std::string::npos) rest = rest.substr(0, h);
+        auto &m = cfg[sec];
+        if (m.count(key)) {
+            err = "Variable " + key + " in config file is ambiguous!";
+            return false;
+        }
+        m[key] = rest;
+    }
+    return true;
+}
+
+bool read_stl(const std::string &path, std::vector<double> &tris, std::string &err) {
+    std::ifstream in(path, std::ios::binary);
+    if (!in) {
+        err = "Could not open " + path;
+        return false;
+    }
+    char header[80];
+    uint32_t n = 0;
+    if (!in.read(header, 80) || !in.read(reinterpret_cast<char *>(&n), 4)) {
+        err = path + " is not a binary STL file";
+        return false;
+    }
+    if (n == 0) {
+        err = path + " contains no triangles";
+        return false;
+    }
+    tris.resize((size_t)n * 9);
+    for (uint32_t i = 0; i < n; ++i) {
+        unsigned char rec[50];
+        if (!in.read(reinterpret_cast<char *>(rec), 50)) {
+            err = path + " should contain " + std::to_string(n) + " triangles but read " + std::to_string(i);
+            return false;
+        }
+        for (int k = 0; k < 9; ++k) {
+            float f;
+            std::memcpy(&f, rec + 12 + 4 * k, 4); /* little-endian, as the STL format defines */
+            double v = f;
+            if (std::fabs(v) < 1e-8) v = 0.0;
+            tris[(size_t)i * 9 + k] = v;
+        }
+    }
+    return true;
+}
+
+bool read_opera3d(const std::string &path, double lengthconv, Table3 &t, std::string &err) {
+    const std::string ext = fs::path(path).extension().string();
+    if (ext == ".gz" || ext == ".bz2") {
+        err = path + ": compressed tables are not supported; decompress the file first";
+        return false;
+    }
+    std::ifstream in(path);
+    if (!in) {
+        err = "Could not open " + path;
+        return false;
+    }
+    long xl = 0, yl = 0, zl = 0;
+    std::string line;
+    if (!std::getline(in, line) || !(std::istringstream(line) >> xl >> yl >> zl) || xl < 2 || yl < 2 || zl < 2) {
+        err = path + ": bad table header";
+        return false;
+    }
+    /* column lines " i NAME [UNIT]" up to " 0" */
+    std::vector<std::string> cols;
+    while (std::getline(in, line)) {
+        std::istringstream ss(line);
+        int idx = -1;
+        std::string name;
+        ss >> idx;
+        if (idx == 0) break;
+        ss >> name;
+        cols.push_back(name);
+    }
+    if (cols.size() < 3) {
+        err = path + " not found or corrupt";
+        return false;
+    }
+    const size_t ncol = cols.size(), npts = (size_t)xl * yl * zl;
+    std::vector<double> data;
+    data.reserve(npts * ncol);
+    double v;
+    while (in >> v) data.push_back(v);
+    if (data.size() != npts * ncol) {
+        err = "The header says the size is " + std::to_string(npts) + ", actually it is " + std::to_string(data.size() / ncol) + "!";
+        return false;
+    }
+    for (int a = 0; a < 3; ++a) {
+        std::vector<double> &ax = t.ax[a];
+        ax.resize(npts);
+        for (size_t i = 0; i < npts; ++i) ax[i] = data[i * ncol + a] * lengthconv;
+        std::sort(ax.begin(), ax.end());
+        ax.erase(std::unique(ax.begin(), ax.end()), ax.end());
+    }
+    if (t.ax[0].size() != (size_t)xl || t.ax[1].size() != (size_t)yl || t.ax[2].size() != (size_t)zl) {
+        err = path + ": the grid is not rectilinear with the header's dimensions";
+        return false;
+    }
+    auto index = [](const std::vector<double> &ax, double x) { return (size_t)(std::lower_bound(ax.begin(), ax.end(), x) - ax.begin()); };
+    std::vector<double> *dst[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (size_t c = 3; c < ncol; ++c) {
+        std::string nme = cols[c];
+        std::transform(nme.begin(), nme.end(), nme.begin(), ::toupper);
+        std::vector<double> *d = nme == "BX" ? &t.bx : nme == "BY" ? &t.by : nme == "BZ" ? &t.bz : nme == "V" ? &t.v : nullptr;
+        if (d) d->assign(npts, 0.0);
+        dst[std::min<size_t>(c - 3, 3)] = d;
+        if (c - 3 > 3) {
+            err = path + ": more than four field columns";
+            return false;
+        }
+    }
+    for (size_t i = 0; i < npts; ++i) {
+        const size_t ix = index(t.ax[0], data[i * ncol] * lengthconv), iy = index(t.ax[1], data[i * ncol + 1] * lengthconv),
+                     iz = index(t.ax[2], data[i * ncol + 2] * lengthconv);
+        const size_t o = (ix * yl + iy) * zl + iz;
+        for (size_t c = 3; c < ncol; ++c)
+            if (dst[c - 3]) (*dst[c - 3])[o] = data[i * ncol + c];
+    }
+    return true;
+}
+
+pt_status load_scene(const std::string &config_path, SceneStore &S, std::string &err) {
+    Config cfg;
+    if (!read_config(config_path, cfg, err)) return PT_ERR_IO;
+    /* materials: [MATERIALS] of the config, or of [GLOBAL] materials_file */
+    std::string matfile;
+    {
+        auto &g = section(cfg, "GLOBAL");
+        auto it = g.find("materials_file");
+        if (it != g.end()) matfile = trim(it->second);
+    }
+    Config matcfg;
+    if (!matfile.empty()) {
+        if (!read_config(relative_to(config_path, matfile).string(), matcfg, err)) return PT_ERR_IO;
+    }
+    const auto &mats = matfile.empty() ? section(cfg, "MATERIALS") : section(matcfg, "MATERIALS");
+    std::map<std::string, pt_material> known;
+    for (auto &kv : mats) {
+        std::istringstream ss(kv.second);
+        pt_material m{};
+        if (!(ss >> m.fermi_real >> m.fermi_imag >> m.diff_prob >> m.spinflip_prob >> m.rms_roughness >> m.correl_length)) {
+            err = "Could not read material " + kv.first + "!";
+            return PT_ERR_INVALID;
+        }
+        if (!(ss >> m.internal_bfield)) m.internal_bfield = 0;
+        if (!(ss >> m.modified_lambert_prob)) m.modified_lambert_prob = 0;
+        if (!(ss >> m.loss_per_bounce)) m.loss_per_bounce = 0;
+        if (m.diff_prob < 0 || m.diff_prob > 1 || m.spinflip_prob < 0 || m.spinflip_prob > 1 || m.modified_lambert_prob < 0 ||
+            m.modified_lambert_prob > 1 || m.loss_per_bounce < 0 || m.loss_per_bounce > 1) {
+            err = "You set a probability outside range 0..1 for material " + kv.first + "!";
+            return PT_ERR_INVALID;
+        }
+        known[kv.first] = m;
+    }
+    auto material_index = [&](const std::string &name, int &idx) -> bool {
+        auto it = known.find(name);
+        if (it == known.end()) return false;
+        for (size_t k = 0; k < S.material_names.size(); ++k)
+            if (S.material_names[k] == name) { idx = (int)k; return true; }
+        S.material_names.push_back(name);
+        S.materials.push_back(it->second);
+        idx = (int)S.materials.size() - 1;
+        return true;
+    };
+    /* solids: the default solid (ID 1) first, then every other line in map order */
+    const auto &geo = section(cfg, "GEOMETRY");
+    bool have_default = false;
+    S.solids.assign(1, pt_solid{});
+    S.solid_ids.assign(1, 1);
+    S.ignore.assign(1, std::vector<double>());
+    for (auto &kv : geo) {
+        long id = 0;
+        if (!(std::istringstream(kv.first) >> id) || id < 1) {
+            err = "invalid solid ID " + kv.first;
+            return PT_ERR_INVALID;
+        }
+        std::istringstream ss(kv.second);
+        std::string file, matname;
+        if (!(ss >> file >> matname)) {
+            err = "Could not load solid with ID " + std::to_string(id) + "! Did you define invalid parameters?";
+            return PT_ERR_INVALID;
+        }
+        std::vector<double> ign;
+        double a, b;
+        char dash;
+        while (ss >> a) {
+            if (!(ss >> dash >> b) || dash != '-') {
+                err = "Invalid ignoretimes for solid " + std::to_string(id);
+                return PT_ERR_INVALID;
+            }
+            ign.push_back(a);
+            ign.push_back(b);
+        }
+        int mi = -1;
+        if (!material_index(matname, mi)) {
+            err = "Material " + matname + " used but not defined!";
+            return PT_ERR_INVALID;
+        }
+        pt_solid so{};
+        so.id = (uint32_t)id;
+        so.material = mi;
+        if (id == 1) {
+            have_default = true;
+            S.solids[0] = so;
+            S.ignore[0] = ign;
+            continue;
+        }
+        if (std::find(S.solid_ids.begin() + 1, S.solid_ids.end(), (uint32_t)id) != S.solid_ids.end()) {
+            err = "You defined solids with identical ID! IDs have to be unique!";
+            return PT_ERR_INVALID;
+        }
+        std::vector<double> tr;
+        if (!read_stl(relative_to(config_path, file).string(), tr, err)) return PT_ERR_IO;
+        const int32_t sidx = (int32_t)S.solids.size();
+        S.solids.push_back(so);
+        S.solid_ids.push_back((uint32_t)id);
+        S.ignore.push_back(ign);
+        S.triangles.insert(S.triangles.end(), tr.begin(), tr.end());
+        S.triangle_solid.insert(S.triangle_solid.end(), tr.size() / 9, sidx);
+    }
+    if (!have_default) {
+        err = "the [GEOMETRY] section needs the default solid with ID 1";
+        return PT_ERR_INVALID;
+    }
+    for (size_t k = 0; k < S.solids.size(); ++k) {
+        S.solids[k].n_ignore = (int32_t)(S.ignore[k].size() / 2);
+        S.solids[k].ignore_times = S.ignore[k].empty() ? nullptr : S.ignore[k].data();
+    }
+    /* fields */
+    const auto &fl = section(cfg, "FIELDS");
+    for (auto &kv : fl) {
+        std::istringstream ss(kv.second);
+        std::string type;
+        ss >> type;
+        pt_field f{};
+        f.xmax = f.xmin = f.ymax = f.ymin = f.zmax = f.zmin = 0;
+        if (type == "OPERA3D" || type == "3Dtable") {
+            std::string file, bs, es;
+            double bw = 0, lconv = 1;
+            if (!(ss >> file >> bs >> es >> bw) || (type == "OPERA3D" && !(ss >> lconv))) {
+                err = "Could not read all required parameters for field " + type + "!";
+                return PT_ERR_INVALID;
+            }
+            double b = 0, e = 0;
+            if (!constant_scale(bs, cfg, b, err) || !constant_scale(es, cfg, e, err)) return PT_ERR_UNSUPPORTED;
+            if (type == "3Dtable") { /* centimetres, gauss and volt per centimetre */
+                b *= 0.0001;
+                e *= 100;
+                lconv = 0.01;
+            }
+            auto t = std::make_unique<Table3>();
+            if (!read_opera3d(relative_to(config_path, file).string(), lconv, *t, err)) return PT_ERR_IO;
+            f.type = PT_FIELD_TAB3D;
+            f.b_scale = b;
+            f.e_scale = e;
+            f.boundary_width = bw;
+            f.nx = (int32_t)t->ax[0].size(); f.ny = (int32_t)t->ax[1].size(); f.nz = (int32_t)t->ax[2].size();
+            f.x = t->ax[0].data(); f.y = t->ax[1].data(); f.z = t->ax[2].data();
+            f.bx = t->bx.empty() ? nullptr : t->bx.data();
+            f.by = t->by.empty() ? nullptr : t->by.data();
+            f.bz = t->bz.empty() ? nullptr : t->bz.data();
+            f.v = t->v.empty() ? nullptr : t->v.data();
+            /* the container box is the table's extent (src/field_3d.cpp:308) */
+            f.xmax = t->ax[0].back(); f.xmin = t->ax[0].front();
+            f.ymax = t->ax[1].back(); f.ymin = t->ax[1].front();
+            f.zmax = t->ax[2].back(); f.zmin = t->ax[2].front();
+            S.tables.push_back(std::move(t));
+        } else if (type == "HarmonicExpansionBField") {
+            std::string bs;
+            double bw;
+            if (!(ss >> f.offset[0] >> f.offset[1] >> f.offset[2] >> bw >> f.xmax >> f.xmin >> f.ymax >> f.ymin >> f.zmax >> f.zmin >> bs)) {
+                err = "Could not read all required parameters for field " + type + "!";
+                return PT_ERR_INVALID;
+            }
+            double b;
+            if (!constant_scale(bs, cfg, b, err)) return PT_ERR_UNSUPPORTED;
+            std::vector<int32_t> L, M;
+            std::vector<double> G;
+            int l, m;
+            double g;
+            while (ss >> l >> m >> g) { L.push_back(l); M.push_back(m); G.push_back(g); }
+            f.type = PT_FIELD_HARMONIC;
+            f.b_scale = b;
+            f.e_scale = 0;
+            f.boundary_width = bw;
+            S.hl.push_back(L);
+            S.hm.push_back(M);
+            S.hg.push_back(G);
+            f.n_coeff = (int32_t)G.size();
+            f.l = S.hl.back().data();
+            f.m = S.hm.back().data();
+            f.g = S.hg.back().data();
+        } else if (type == "EDMStaticEField") {
+            std::string es;
+            if (!(ss >> f.e[0] >> f.e[1] >> f.e[2] >> es)) {
+                err = "Could not read all required parameters for field " + type + "!";
+                return PT_ERR_INVALID;
+            }
+            double e;
+            if (!constant_scale(es, cfg, e, err)) return PT_ERR_UNSUPPORTED;
+            f.type = PT_FIELD_UNIFORM_E;
+            f.b_scale = 0;
+            f.e_scale = e;
+        } else {
+            err = "field type " + type + " is not implemented on the device path";
+            return PT_ERR_UNSUPPORTED;
+        }
+        S.fields.push_back(f);
+    }
+    /* the harmonic coefficient vectors moved while growing: point again */
+    for (size_t k = 0, h = 0; k < S.fields.size(); ++k)
+        if (S.fields[k].type == PT_FIELD_HARMONIC) {
+            S.fields[k].l = S.hl[h].data();
+            S.fields[k].m = S.hm[h].data();
+            S.fields[k].g = S.hg[h].data();
+            ++h;
+        }
+    pt_scene_desc &d = S.desc;
+    d = pt_scene_desc{};
+    d.n_triangles = (int64_t)(S.triangles.size() / 9);
+    d.triangles = S.triangles.empty() ? nullptr : S.triangles.data();
+    d.triangle_solid = S.triangle_solid.empty() ? nullptr : S.triangle_solid.data();
+    d.n_solids = (int32_t)S.solids.size();
+    d.solids = S.solids.data();
+    d.n_materials = (int32_t)S.materials.size();
+    d.materials = S.materials.data();
+    d.n_fields = (int32_t)S.fields.size();
+    d.fields = S.fields.empty() ? nullptr : S.fields.data();
+    return PT_OK;
+}
+
+pt_status load_run_params(const std::string &config_path, const std::string &species, pt_run_params &p,
+                          std::vector<double> &spintimes, std::string &err) {
+    Config cfg;
+    if (!read_config(config_path, cfg, err)) return PT_ERR_IO;
+    p = pt_run_params{};
+    if (species == "neutron") p.species = PT_NEUTRON;
+    else if (species == "proton") p.species = PT_PROTON;
+    else if (species == "electron") p.species = PT_ELECTRON;
+    else {
+        err = "particle type " + species + " is not implemented on the device path";
+        return PT_ERR_UNSUPPORTED;
+    }
+    auto opt = [&](const char *key) -> std::string {
+        auto &sp = section(cfg, species.c_str());
+        auto it = sp.find(key);
+        if (it != sp.end()) return it->second;
+        auto &all = section(cfg, "PARTICLES");
+        it = all.find(key);
+        return it != all.end() ? it->second : std::string();
+    };
+    auto num = [&](const std::string &s, double dflt) {
+        double v;
+        return (std::istringstream(s) >> v) ? v : dflt;
+    };
+    {
+        auto &g = section(cfg, "GLOBAL");
+        auto it = g.find("simtime");
+        p.simtime = it != g.end() ? num(it->second, 0) : 0;
+    }
+    p.tau = num(opt("tau"), 0);
+    p.tmax = num(opt("tmax"), 0);
+    p.lmax = num(opt("lmax"), 0);
+    p.bmax = num(opt("Bmax"), 0);
+    p.flipspin = (int32_t)num(opt("flipspin"), 0);
+    if (num(opt("interpolatefields"), 0) != 0) {
+        err = "interpolatefields 1 is not implemented on the device path";
+        return PT_ERR_UNSUPPORTED;
+    }
+    spintimes.clear();
+    {
+        std::istringstream ss(opt("spintimes"));
+        double t;
+        while (ss >> t) spintimes.push_back(t);
+    }
+    p.n_spintimes = (int32_t)spintimes.size();
+    p.spintimes = spintimes.empty() ? nullptr : spintimes.data();
+    p.mode = PT_MODE_BATCHED;
+    p.field_precision = PT_PREC_FP64;
+    p.seed = 1;
+    return PT_OK;
+}
+
+TTrackerGPU::TTrackerGPU(const std::string &config_path, int device) : path_(config_path) {
+    pt_status st = load_scene(config_path, store_, err_);
+    if (st != PT_OK) return;
+    if (pt_create(&store_.desc, device, &ctx_) != PT_OK) {
+        err_ = pt_last_error(nullptr);
+        ctx_ = nullptr;
+    }
+}
+
+TTrackerGPU::~TTrackerGPU() {
+    if (ctx_) pt_destroy(ctx_);
+}
+
+pt_status TTrackerGPU::IntegrateParticles(const std::string &species, const pt_particles &in, pt_particles &out, pt_stats &stats,
+                                          int mode, uint64_t seed) {
+    if (!ctx_) return PT_ERR_INVALID;
+    pt_run_params p;
+    std::vector<double> spintimes;
+    pt_status st = load_run_params(path_, species, p, spintimes, err_);
+    if (st != PT_OK) return st;
+    p.mode = mode;
+    p.seed = seed;
+    st = pt_integrate(ctx_, &p, &in, &out, &stats);
+    if (st != PT_OK && st != PT_ERR_CANCELLED) err_ = pt_last_error(ctx_);
+    return st;
+}
+
+} // namespace pth
+
+/* ---------------- C ABI of the config front end ---------------- */
+struct pt_config_scene {
+    pth::SceneStore store;
+};
+
+namespace {
+thread_local std::string g_config_err;
+}
+
+extern "C" {
+
+pt_status pt_config_load(const char *config_path, pt_config_scene **out) {
+    if (!config_path || !out) return PT_ERR_INVALID;
+    *out = nullptr;
+    auto s = std::make_unique<pt_config_scene>();
+    pt_status st = pth::load_scene(config_path, s->store, g_config_err);
+    if (st != PT_OK) return st;
+    *out = s.release();
+    return PT_OK;
+}
+
+const pt_scene_desc *pt_config_scene_desc(const pt_config_scene *s) { return s ? &s->store.desc : nullptr; }
+
+void pt_config_free(pt_config_scene *s) { delete s; }
+
+pt_status pt_config_run_params(const char *config_path, const char *species, pt_run_params *out, double *spintimes,
+                               int32_t max_spintimes) {
+    if (!config_path || !species || !out) return PT_ERR_INVALID;
+    std::vector<double> st;
+    pt_status r = pth::load_run_params(config_path, species, *out, st, g_config_err);
+    if (r != PT_OK) return r;
+    if ((int32_t)st.size() > max_spintimes || (!spintimes && !st.empty())) {
+        g_config_err = "spintimes needs " + std::to_string(st.size()) + " values";
+        return PT_ERR_INVALID;
+    }
+    for (size_t k = 0; k < st.size(); ++k) spintimes[k] = st[k];
+    out->spintimes = st.empty() ? nullptr : spintimes;
+    return PT_OK;
+}
+
+const char *pt_config_error(void) { return g_config_err.c_str(); }
+
+} // extern "C"

@@ -213,6 +213,39 @@ def run_params(species=A.NEUTRON, simtime=100.0, tau=0.0, tmax=9e99, lmax=9e99, 
     return p
 
 
+class ConfigScene:
+    """The scene of a PENTrack config.in as the library's config front end
+    reads it (pt_config_load: [GEOMETRY], [MATERIALS] / materials_file,
+    [FIELDS], [FORMULAS]; files relative to the config)."""
+
+    def __init__(self, path):
+        h = C.c_void_p()
+        st = lib().pt_config_load(os.fsencode(str(path)), C.byref(h))
+        if st != A.PT_OK:
+            raise EngineError(st, lib().pt_config_error().decode())
+        self.h = h
+        self.path = str(path)
+
+    def desc(self):
+        return lib().pt_config_scene_desc(self.h).contents, self
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().pt_config_free(self.h)
+            self.h = None
+
+
+def config_run_params(path, species="neutron", max_spintimes=64):
+    """pt_run_params from [GLOBAL] simtime and the species' particle options."""
+    p = A.RunParams()
+    buf = np.zeros(max_spintimes)
+    st = lib().pt_config_run_params(os.fsencode(str(path)), species.encode(), C.byref(p), _dp(buf), max_spintimes)
+    if st != A.PT_OK:
+        raise EngineError(st, lib().pt_config_error().decode())
+    p._keep = buf
+    return p
+
+
 class Engine:
     """One device context: the scene on the GPU plus the tracking kernels."""
 
