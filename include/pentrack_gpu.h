@@ -203,6 +203,7 @@ typedef struct pt_stats {
     int64_t tri32_tests;       /* FP32 certified segment-triangle tests */
     double bisect_ms;          /* batched form: device time of the bisection kernel */
     int64_t bisect_dead;       /* bisection intervals abandoned because neither half collides */
+    int64_t spin_steps;        /* accepted steps of the spin (Bloch) integration */
 } pt_stats;
 
 typedef struct pt_ctx pt_ctx;

@@ -4,6 +4,9 @@
  * cites the reference code it restates.
  */
 #include "pto.h"
+
+/* spin steps of one trajectory step before the particle stops with ID_ODEINT_ERROR */
+#define PTO_MAX_SPIN_STEPS (1 << 22)
 #include "../include/pt_constants.h"
 #include "../include/pt_detmath.h"
 
@@ -727,6 +730,41 @@ struct Tracker {
         (void)t;
     }
 
+    /* TParticle::SpinPrecessionAxis (src/particle.cpp:148-175): BMT precession
+     * in the relativistically distorted field plus Thomas precession; 1/c^2
+     * as the reciprocal constant, as in the equation of motion */
+    void spin_axis(const double B[3], const double E[3], const double *dydt, double W[3]) const {
+        const double v2 = dydt[0] * dydt[0] + dydt[1] * dydt[1] + dydt[2] * dydt[2];
+        const double gr = 1. / std::sqrt(1. - v2 * PT_INV_C0_SQ);
+        const double Bdotv = B[0] * dydt[0] + B[1] * dydt[1] + B[2] * dydt[2];
+        double Bpar[3], vxE[3], axv[3];
+        for (int j = 0; j < 3; ++j) Bpar[j] = Bdotv * dydt[j] / v2;
+        vxE[0] = dydt[1] * E[2] - dydt[2] * E[1];
+        vxE[1] = dydt[2] * E[0] - dydt[0] * E[2];
+        vxE[2] = dydt[0] * E[1] - dydt[1] * E[0];
+        axv[0] = dydt[4] * dydt[2] - dydt[5] * dydt[1];
+        axv[1] = dydt[5] * dydt[0] - dydt[3] * dydt[2];
+        axv[2] = dydt[3] * dydt[1] - dydt[4] * dydt[0];
+        const double cb = -sp.gamma / gr, ct = gr * gr / (gr + 1) * PT_INV_C0_SQ;
+        for (int j = 0; j < 3; ++j)
+            W[j] = cb * ((1 - gr) * Bpar[j] + gr * B[j] - gr * vxE[j] * PT_INV_C0_SQ) + ct * axv[j];
+    }
+    /* TParticle::SpinDerivs (src/particle.cpp:178-193) along the trajectory's
+     * dense output: dS/dt = Omega x S, integrated time, integrated phase */
+    void spin_derivs(const double *S, double *dS, double t) {
+        double y[9], dydt[9], B[3], dB[3][3], V, E[3], W[3];
+        st.calc_state(t, y);
+        bfield(y[0], y[1], y[2], t, B, dB);
+        efield(y[0], y[1], y[2], t, V, E);
+        eom(y, dydt, B, dB, E);
+        spin_axis(B, E, dydt, W);
+        dS[0] = W[1] * S[2] - W[2] * S[1];
+        dS[1] = W[2] * S[0] - W[0] * S[2];
+        dS[2] = W[0] * S[1] - W[1] * S[0];
+        dS[3] = 1.;
+        dS[4] = std::sqrt(W[0] * W[0] + W[1] * W[1] + W[2] * W[2]);
+    }
+
     /* TParticle::derivs + EquationOfMotion (src/particle.cpp:96-135) */
     void derivs(const double *y, double *dydx, double x) {
         double B[3] = {0, 0, 0}, dB[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, E[3] = {0, 0, 0}, V = 0;
@@ -1099,8 +1137,27 @@ struct Tracker {
                 i2 |= (x2 >= P.spintimes[i] && x2 < P.spintimes[i + 1]);
             }
             if (i1 || i2) {
-                stopID = PT_ID_ODEINT_ERROR; /* Bloch integration not restated */
-                return y1[7];
+                /* LOOP D: a fresh dopri5 dense-output stepper (abs = rel = 1e-12)
+                 * started with half a Larmor turn as its step */
+                if (spin[0] == 0 && spin[1] == 0 && spin[2] == 0)
+                    for (int k = 0; k < 3; ++k) spin[k] = B1[k] * y1[7] / Babs1;
+                Dense5<5> ss(1e-12, 1e-12);
+                ss.initialize(spin, x1, std::fabs(PT_PI / sp.gamma / Babs1));
+                auto sys = [this](const double *S, double *dS, double t) { spin_derivs(S, dS, t); };
+                int64_t rej = 0;
+                for (int64_t steps = 0;; ++steps) {
+                    if (steps >= PTO_MAX_SPIN_STEPS) throw OdeintError();
+                    ss.do_step(sys, rej);
+                    double t = ss.t;
+                    if (t > x2) {
+                        t = x2;
+                        ss.calc_state(t, spin);
+                    } else {
+                        std::copy(ss.x, ss.x + 5, spin);
+                    }
+                    if (stats) stats->spin_steps++;
+                    if (t >= x2) break;
+                }
             } else if (spin[0] != 0 || spin[1] != 0 || spin[2] != 0) {
                 double proj = (spin[0] * B1[0] + spin[1] * B1[1] + spin[2] * B1[2]) / Babs1 /
                               std::sqrt(spin[0] * spin[0] + spin[1] * spin[1] + spin[2] * spin[2]);
@@ -1189,7 +1246,12 @@ struct Tracker {
                 stopID = PT_ID_CGAL_ERROR;
             }
             {
-                double sproj = integrate_spin(spin, x, y);
+                double sproj = st.xo[7];
+                try {
+                    sproj = integrate_spin(spin, x, y);
+                } catch (OdeintError &) {
+                    stopID = PT_ID_ODEINT_ERROR;
+                }
                 bool flipped = st.xo[7] != y[7];
                 if (sproj != st.xo[7]) {
                     /* TParticle::DoPolarize (src/particle.cpp:225-234) */
@@ -1335,7 +1397,7 @@ int pto_track(pto_ctx *ctx, const pt_run_params *params, const pt_particles *in,
         std::memset(stats, 0, sizeof(*stats));
         for (auto &s : st) {
             stats->rk_accepted += s.rk_accepted; stats->rk_rejected += s.rk_rejected; stats->rhs_evals += s.rhs_evals;
-            stats->hits += s.hits; stats->bisection_levels += s.bisection_levels; stats->bisect_dead += s.bisect_dead; stats->subsegments += s.subsegments;
+            stats->hits += s.hits; stats->bisection_levels += s.bisection_levels; stats->bisect_dead += s.bisect_dead; stats->spin_steps += s.spin_steps; stats->subsegments += s.subsegments;
             stats->bvh_nodes += s.bvh_nodes; stats->particle_seconds += s.particle_seconds;
         }
         stats->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

@@ -34,22 +34,22 @@ template <class T> __device__ __forceinline__ T warp_sum(unsigned mask, T v) {
 
 __device__ __forceinline__ void flush_counters(DCounters *C, const LaneCounters &lc, double psec, bool active) {
     /* warp-aggregated atomics over the lanes that reach this point */
-    unsigned long long v[16] = {lc.rk_acc, lc.rk_rej, lc.rhs, lc.fields, lc.hits, lc.bisect, lc.nodes, lc.tris, lc.subseg, lc.dense,
-                                active ? 1ull : 0ull, lc.cand_calls, lc.cand_overflow, lc.cand_sum, lc.tri32, lc.dead};
+    unsigned long long v[17] = {lc.rk_acc, lc.rk_rej, lc.rhs, lc.fields, lc.hits, lc.bisect, lc.nodes, lc.tris, lc.subseg, lc.dense,
+                                active ? 1ull : 0ull, lc.cand_calls, lc.cand_overflow, lc.cand_sum, lc.tri32, lc.dead, lc.spin};
     const unsigned mask = __activemask();
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(mask) - 1;
-    for (int k = 0; k < 16; ++k) v[k] = warp_sum(mask, v[k]);
+    for (int k = 0; k < 17; ++k) v[k] = warp_sum(mask, v[k]);
     double ps = warp_sum(mask, psec);
     unsigned bm = lc.bisect_max;
     for (unsigned m = mask; m; m &= m - 1) bm = max(bm, __shfl_sync(mask, lc.bisect_max, __ffs(m) - 1));
     if (lane == leader && bm) atomicMax(&C->bisect_max, bm);
     if (lane == leader) {
-        unsigned long long *dst[16] = {&C->rk_accepted, &C->rk_rejected, &C->rhs_evals, &C->field_evals, &C->hits,
+        unsigned long long *dst[17] = {&C->rk_accepted, &C->rk_rejected, &C->rhs_evals, &C->field_evals, &C->hits,
                                        &C->bisection_levels, &C->bvh_nodes, &C->tri_tests, &C->subsegments,
                                        &C->dense_evals, &C->active, &C->cand_calls, &C->cand_overflow, &C->cand_sum,
-                                       &C->tri32, &C->bisect_dead};
-        for (int k = 0; k < 16; ++k) if (v[k]) atomicAdd(dst[k], v[k]);
+                                       &C->tri32, &C->bisect_dead, &C->spin_steps};
+        for (int k = 0; k < 17; ++k) if (v[k]) atomicAdd(dst[k], v[k]);
         if (ps != 0) atomicAdd(&C->particle_seconds, ps);
     }
 }
@@ -610,7 +610,7 @@ void add_counters(pt_stats &acc, const DCounters &k) {
     acc.bvh_nodes += k.bvh_nodes; acc.tri_tests += k.tri_tests; acc.subsegments += k.subsegments;
     acc.dense_evals += k.dense_evals; acc.particle_seconds += k.particle_seconds;
     acc.bisect_max = std::max<int64_t>(acc.bisect_max, k.bisect_max);
-    acc.cand_calls += k.cand_calls; acc.cand_overflow += k.cand_overflow; acc.cand_sum += k.cand_sum; acc.tri32_tests += k.tri32; acc.bisect_dead += k.bisect_dead;
+    acc.cand_calls += k.cand_calls; acc.cand_overflow += k.cand_overflow; acc.cand_sum += k.cand_sum; acc.tri32_tests += k.tri32; acc.bisect_dead += k.bisect_dead; acc.spin_steps += k.spin_steps;
 }
 
 int persistent_grid(pt_ctx *c, const void *fn, int block) {

@@ -30,6 +30,7 @@
 #define PT_MAX_SUBSEGMENTS (1 << 20) /* chord pieces of one RK step */
 #define PT_MAX_HITS_PER_SEGMENT 64   /* surfaces crossed by one chord piece */
 #define PT_MAX_CAND 16               /* candidate triangles kept for a bisection */
+#define PT_MAX_SPIN_STEPS (1 << 22)  /* spin (Bloch) steps within one trajectory step */
 
 /* lane flags */
 #define PT_F_DERIV 1u   /* FSAL derivative valid */
@@ -175,5 +176,5 @@ struct DCounters {
     unsigned long long bvh_nodes, tri_tests, subsegments, dense_evals, active, paused;
     double particle_seconds;
     unsigned int bisect_max;
-    unsigned long long cand_calls, cand_overflow, cand_sum, tri32, bisect_dead;
+    unsigned long long cand_calls, cand_overflow, cand_sum, tri32, bisect_dead, spin_steps;
 };

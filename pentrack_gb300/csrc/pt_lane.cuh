@@ -15,7 +15,7 @@ namespace ptd {
 struct LaneCounters {
     unsigned rk_acc, rk_rej, rhs, fields, hits, bisect, subseg, dense;
     unsigned nodes, tris, bisect_max;
-    unsigned cand_calls, cand_overflow, cand_sum, tri32, dead;
+    unsigned cand_calls, cand_overflow, cand_sum, tri32, dead, spin;
 };
 
 /* Resumable state of one post-step (the remainder of LOOP A after an accepted
@@ -302,6 +302,12 @@ struct Lane {
         }
         if (sp.q != 0) efield(S, R.prec, yy[0], yy[1], yy[2], V, E);
         ++lc.rhs;
+        eom_fields(yy, B, dB, E, d);
+    }
+
+    /* TParticle::EquationOfMotion (src/particle.cpp:105-135) with given fields */
+    __device__ __forceinline__ void eom_fields(const double *yy, const double B[3], const double (*dB)[3], const double E[3], double *d) const {
+        const DSpecies &sp = R.sp;
         d[0] = yy[3]; d[1] = yy[4]; d[2] = yy[5];
         double F0 = 0, F1 = 0, F2 = sp.fgrav;
         if (sp.q != 0) {
@@ -328,6 +334,124 @@ struct Lane {
         d[6] = ig;
         d[7] = 0;
         d[8] = sqrt(v2);
+    }
+
+    /* TParticle::SpinPrecessionAxis (src/particle.cpp:148-175) */
+    __device__ void spin_axis(const double B[3], const double E[3], const double *dydt, double W[3]) const {
+        const double v2 = dydt[0] * dydt[0] + dydt[1] * dydt[1] + dydt[2] * dydt[2];
+        const double gr = 1. / sqrt(1. - v2 * PT_INV_C0_SQ);
+        const double Bdotv = B[0] * dydt[0] + B[1] * dydt[1] + B[2] * dydt[2];
+        double Bpar[3], vxE[3], axv[3];
+        for (int j = 0; j < 3; ++j) Bpar[j] = Bdotv * dydt[j] / v2;
+        vxE[0] = dydt[1] * E[2] - dydt[2] * E[1];
+        vxE[1] = dydt[2] * E[0] - dydt[0] * E[2];
+        vxE[2] = dydt[0] * E[1] - dydt[1] * E[0];
+        axv[0] = dydt[4] * dydt[2] - dydt[5] * dydt[1];
+        axv[1] = dydt[5] * dydt[0] - dydt[3] * dydt[2];
+        axv[2] = dydt[3] * dydt[1] - dydt[4] * dydt[0];
+        const double cb = -R.sp.gamma / gr, ct = gr * gr / (gr + 1) * PT_INV_C0_SQ;
+        for (int j = 0; j < 3; ++j) W[j] = cb * ((1 - gr) * Bpar[j] + gr * B[j] - gr * vxE[j] * PT_INV_C0_SQ) + ct * axv[j];
+    }
+    /* TParticle::SpinDerivs (src/particle.cpp:178-193) along the trajectory's dense output */
+    __device__ void spin_derivs(const double *Sv, double *dS, double tt) {
+        double yy[9], dydt[9], B[3], dB[3][3], V, E[3], W[3];
+        calc_state(tt, yy);
+        bfield<true>(S, R.prec, yy[0], yy[1], yy[2], B, dB);
+        efield(S, R.prec, yy[0], yy[1], yy[2], V, E);
+        ++lc.fields;
+        eom_fields(yy, B, dB, E, dydt);
+        spin_axis(B, E, dydt, W);
+        dS[0] = W[1] * Sv[2] - W[2] * Sv[1];
+        dS[1] = W[2] * Sv[0] - W[0] * Sv[2];
+        dS[2] = W[0] * Sv[1] - W[1] * Sv[0];
+        dS[3] = 1.;
+        dS[4] = sqrt(W[0] * W[0] + W[1] * W[1] + W[2] * W[2]);
+    }
+
+    /* LOOP D of TTracker::IntegrateSpin (src/tracking.cpp:423-446): a fresh
+     * dopri5 dense-output stepper with abs = rel = 1e-12 from (x1, spin) to
+     * x2, the same controller and arithmetic as the trajectory's; false when
+     * a step fails (500 tries) or the step count bound is reached */
+    __device__ __noinline__ bool bloch(double x1, double x2, double dt0) {
+        const double a2 = 1.0 / 5, a3 = 3.0 / 10, a4 = 4.0 / 5, a5 = 8.0 / 9;
+        const double b21 = 1.0 / 5;
+        const double b31 = 3.0 / 40, b32 = 9.0 / 40;
+        const double b41 = 44.0 / 45, b42 = -56.0 / 15, b43 = 32.0 / 9;
+        const double b51 = 19372.0 / 6561, b52 = -25360.0 / 2187, b53 = 64448.0 / 6561, b54 = -212.0 / 729;
+        const double b61 = 9017.0 / 3168, b62 = -355.0 / 33, b63 = 46732.0 / 5247, b64 = 49.0 / 176, b65 = -5103.0 / 18656;
+        const double c1 = 35.0 / 384, c3 = 500.0 / 1113, c4 = 125.0 / 192, c5 = -2187.0 / 6784, c6 = 11.0 / 84;
+        const double dc1 = c1 - 5179.0 / 57600, dc3 = c3 - 7571.0 / 16695, dc4 = c4 - 393.0 / 640,
+                     dc5 = c5 - (-92097.0) / 339200, dc6 = c6 - 187.0 / 2100, dc7 = -1.0 / 40;
+        const double eps = 1e-12;
+        double x[5], dxdt[5], xo5[5], dxo5[5], k2_[5], k3_[5], k4_[5], k5_[5], k6_[5], xt[5], out[5], dout[5];
+        for (int i = 0; i < 5; ++i) x[i] = spin[i];
+        double ts = x1, dt_ = dt0, tso = x1;
+        spin_derivs(x, dxdt, ts);
+        for (long steps = 0;; ++steps) {
+            if (steps >= PT_MAX_SPIN_STEPS) return false;
+            tso = ts;
+            for (int tries = 1;; ++tries) {
+                if (tries > PT_MAX_TRIES) return false;
+                for (int i = 0; i < 5; ++i) xt[i] = fma(dt_ * b21, dxdt[i], x[i]);
+                spin_derivs(xt, k2_, ts + dt_ * a2);
+                for (int i = 0; i < 5; ++i) xt[i] = fma(dt_ * b32, k2_[i], fma(dt_ * b31, dxdt[i], x[i]));
+                spin_derivs(xt, k3_, ts + dt_ * a3);
+                for (int i = 0; i < 5; ++i) xt[i] = fma(dt_ * b43, k3_[i], fma(dt_ * b42, k2_[i], fma(dt_ * b41, dxdt[i], x[i])));
+                spin_derivs(xt, k4_, ts + dt_ * a4);
+                for (int i = 0; i < 5; ++i)
+                    xt[i] = fma(dt_ * b54, k4_[i], fma(dt_ * b53, k3_[i], fma(dt_ * b52, k2_[i], fma(dt_ * b51, dxdt[i], x[i]))));
+                spin_derivs(xt, k5_, ts + dt_ * a5);
+                for (int i = 0; i < 5; ++i)
+                    xt[i] = fma(dt_ * b65, k5_[i], fma(dt_ * b64, k4_[i], fma(dt_ * b63, k3_[i], fma(dt_ * b62, k2_[i], fma(dt_ * b61, dxdt[i], x[i])))));
+                spin_derivs(xt, k6_, ts + dt_);
+                for (int i = 0; i < 5; ++i)
+                    out[i] = fma(dt_ * c6, k6_[i], fma(dt_ * c5, k5_[i], fma(dt_ * c4, k4_[i], fma(dt_ * c3, k3_[i], fma(dt_ * c1, dxdt[i], x[i])))));
+                spin_derivs(out, dout, ts + dt_);
+                double adt = fabs(dt_), m = 0;
+                for (int i = 0; i < 5; ++i) {
+                    const double er = fma(dt_ * dc7, dout[i], fma(dt_ * dc6, k6_[i], fma(dt_ * dc5, k5_[i], fma(dt_ * dc4, k4_[i],
+                                      fma(dt_ * dc3, k3_[i], (dt_ * dc1) * dxdt[i])))));
+                    const double e = fabs(er) / (eps + eps * (1.0 * fabs(x[i]) + adt * fabs(dxdt[i])));
+                    m = (m < e) ? e : m;
+                }
+                if (m > 1.0) {
+                    dt_ *= fmax(0.9 * ptdm_pow(m, -1.0 / 3.0), 0.2);
+                    continue;
+                }
+                ts += dt_;
+                if (m < 0.5) {
+                    m = fmax(0.00032, m);
+                    dt_ *= 0.9 * ptdm_pow(m, -1.0 / 5.0);
+                }
+                for (int i = 0; i < 5; ++i) { xo5[i] = x[i]; dxo5[i] = dxdt[i]; x[i] = out[i]; dxdt[i] = dout[i]; }
+                break;
+            }
+            ++lc.spin;
+            if (ts > x2) { /* overshoot: the continuous extension at x2 */
+                const double W_[6][5] = {
+                    {1.0, -2.8605386690370884, 3.099577878709121, -1.1618105836403092, 0.013917207301610328},
+                    {0.0, 4.047141499642786, -6.345354046938926, 2.795465086414005, -0.04801624082496286},
+                    {0.0, -3.941160071112659, 10.904003027940295, -6.729317509209278, 0.4175162190483098},
+                    {0.0, 2.8419447015870345, -7.547675862959386, 4.957636724931253, -0.5742817428041846},
+                    {0.0, -1.6109886359167997, 4.218915839039518, -2.950103865566732, 0.47312904339639456},
+                    {0.0, 1.523601174836727, -4.329466835790622, 3.0881301470710616, -0.2822644861171672}};
+                const double h = ts - tso, th = (x2 - tso) / h;
+                double hb[6];
+                for (int k = 0; k < 6; ++k) {
+                    double p = W_[k][4];
+                    p = fma(p, th, W_[k][3]);
+                    p = fma(p, th, W_[k][2]);
+                    p = fma(p, th, W_[k][1]);
+                    p = fma(p, th, W_[k][0]);
+                    hb[k] = h * (p * th);
+                }
+                for (int i = 0; i < 5; ++i)
+                    spin[i] = fma(hb[5], dxdt[i], fma(hb[4], k6_[i], fma(hb[3], k5_[i], fma(hb[2], k4_[i], fma(hb[1], k3_[i], fma(hb[0], dxo5[i], xo5[i]))))));
+                return true;
+            }
+            for (int i = 0; i < 5; ++i) spin[i] = x[i];
+            if (ts >= x2) return true;
+        }
     }
 
     /* The neutral-particle equation of motion in the FP32 field mode: B,
@@ -977,6 +1101,9 @@ struct Lane {
     }
 
     /* TTracker::IntegrateSpin decision logic (src/tracking.cpp:373-483) */
+    /* BLOCH = false compiles the variant without the Bloch integration, for
+     * callers that have checked spin_integrates() first */
+    template <bool BLOCH = true>
     __device__ double integrate_spin(double x2, const double *y2) {
         double B1[3], B2[3];
         bonly(xo[0], xo[1], xo[2], to, B1);
@@ -997,8 +1124,12 @@ struct Lane {
                 i2 |= (x2 >= R.spintimes[i] && x2 < R.spintimes[i + 1]);
             }
             if (i1 || i2) {
-                stop = PT_ID_ODEINT_ERROR; /* Bloch integration (LOOP D) is not on the device path */
-                return xo[7];
+                if (spin[0] == 0 && spin[1] == 0 && spin[2] == 0)
+                    for (int k = 0; k < 3; ++k) spin[k] = B1[k] * xo[7] / Babs1;
+                if (!BLOCH || !bloch(to, x2, fabs(PT_PI / R.sp.gamma / Babs1))) {
+                    stop = PT_ID_ODEINT_ERROR;
+                    return xo[7];
+                }
             } else if (spin[0] != 0 || spin[1] != 0 || spin[2] != 0) {
                 double proj = (spin[0] * B1[0] + spin[1] * B1[1] + spin[2] * B1[2]) / Babs1 /
                               sqrt(spin[0] * spin[0] + spin[1] * spin[1] + spin[2] * spin[2]);
@@ -1019,6 +1150,24 @@ struct Lane {
             return proj;
         }
         return xo[7];
+    }
+
+    /* whether integrate_spin(x2, y2) would run the Bloch integration */
+    __device__ bool spin_integrates(double x2, const double *y2) {
+        if (R.sp.gamma == 0 || R.n_spintimes < 2 || !(x2 > to)) return false;
+        bool i1 = false, i2 = false;
+        for (int i = 0; i + 1 < R.n_spintimes; i += 2) {
+            i1 |= (to >= R.spintimes[i] && to < R.spintimes[i + 1]);
+            i2 |= (x2 >= R.spintimes[i] && x2 < R.spintimes[i + 1]);
+        }
+        if (!(i1 || i2)) return false;
+        double B1[3], B2[3];
+        bonly(xo[0], xo[1], xo[2], to, B1);
+        bonly(y2[0], y2[1], y2[2], x2, B2);
+        const double Babs1 = sqrt(B1[0] * B1[0] + B1[1] * B1[1] + B1[2] * B1[2]);
+        const double Babs2 = sqrt(B2[0] * B2[0] + B2[1] * B2[1] + B2[2] * B2[2]);
+        if (Babs2 == 0 || Babs1 == 0) return false;
+        return Babs1 < R.bmax || Babs2 < R.bmax;
     }
 
     /* first-call setup: IntegrateParticle's prologue (src/tracking.cpp:19-69)
@@ -1172,8 +1321,9 @@ struct Lane {
 
     /* IntegrateSpin + polarisation bookkeeping + stop checks
      * (src/tracking.cpp:128-147), then commit the loop state. */
+    template <bool BLOCH = true>
     __device__ void finish_step(double x, double *yl, bool reset) {
-        double sproj = integrate_spin(x, yl);
+        double sproj = integrate_spin<BLOCH>(x, yl);
         bool flipped = xo[7] != yl[7];
         if (sproj != xo[7]) {
             double flipprob = 0.5 * (1 - yl[7] * sproj);
@@ -1225,10 +1375,11 @@ struct Lane {
         const DMat &m = S.mats[S.solids[cs].mat];
         if (R.sp.kind == PT_NEUTRON ? (m.fermi_imag > 0) : (S.solids[cs].id > 1)) return false; /* OnStep may act */
         if (any_hit(xo, yn) != 0) return false;
+        if (spin_integrates(tn, yn)) return false; /* the Bloch integration runs in the full post-step */
         double x2 = tn, y2[9];
         for (int i = 0; i < 9; ++i) y2[i] = yn[i];
         do_step(to, xo, x2, y2, cs); /* cannot alter the step here */
-        finish_step(tn, y2, false);
+        finish_step<false>(tn, y2, false);
         return true;
     }
 

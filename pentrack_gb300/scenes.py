@@ -23,6 +23,7 @@ M_E = float.fromhex("0x1.901732cb621c3p-38")
 MU_N = float.fromhex("-0x1.7ec4036197f3ap-87")
 ELE_E = float.fromhex("0x1.7a4da04a6daf5p-63")
 GRAV = float.fromhex("0x1.39d013a92a305p+3")
+GAMMA_N = float.fromhex("-0x1.5d842a2000000p+27")
 MASS = {A.NEUTRON: M_N, A.PROTON: M_P, A.ELECTRON: M_E}
 
 SOURCE_STREAM = np.uint64(1) << np.uint64(63)
