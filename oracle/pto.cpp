@@ -9,6 +9,7 @@
 #define PTO_MAX_SPIN_STEPS (1 << 22)
 #include "../include/pt_constants.h"
 #include "../include/pt_detmath.h"
+#include "harmonic_terms.h"
 
 #include <algorithm>
 #include <atomic>
@@ -269,6 +270,10 @@ struct Field {
     double xmax = 0, xmin = 0, ymax = 0, ymin = 0, zmax = 0, zmin = 0, bw = 0;
     Tab3 tab;
     double e[3] = {0, 0, 0};
+    /* HarmonicExpandedBField (src/harmonicfields.cpp:50-829): (l, m, G) terms and offset */
+    std::vector<int> hl, hm;
+    std::vector<double> hg;
+    double offset[3] = {0, 0, 0};
 
     /* TFieldBoundaryBox (src/field.cpp:48-125) */
     bool has_bounds() const { return xmin < xmax && ymin < ymax && zmin < zmax; }
@@ -314,8 +319,12 @@ struct Field {
         if (!in_bounds(x, y, z) || bscale == 0.) return;
         if (type == PT_FIELD_TAB3D) {
             for (int i = 0; i < 3; ++i) tab.interpolate(x, y, z, tab.coeff[i], B[i], dB ? dB[i] : nullptr);
+        } else if (type == PT_FIELD_HARMONIC) {
+            const double xo = x + offset[0], yo = y + offset[1], zo = z + offset[2];
+            for (size_t k = 0; k < hg.size(); ++k)
+                if (hg[k] != 0.) harmonic_term(hl[k], hm[k], hg[k], xo, yo, zo, B, dB);
         } else {
-            return; /* uniform E field has no B; harmonic handled elsewhere */
+            return; /* the uniform E field has no B */
         }
         for (int i = 0; i < 3; ++i) { /* TFieldScaler::scaleVectorField (src/field.cpp:12-32) */
             B[i] *= bscale;
@@ -1356,6 +1365,14 @@ int pto_create(const pt_scene_desc *d, pto_ctx **out) {
             F.bw = f.boundary_width;
             if (f.type == PT_FIELD_TAB3D) F.tab.build(f);
             else if (f.type == PT_FIELD_UNIFORM_E) { F.e[0] = f.e[0]; F.e[1] = f.e[1]; F.e[2] = f.e[2]; }
+            else if (f.type == PT_FIELD_HARMONIC) {
+                for (int k = 0; k < f.n_coeff; ++k) {
+                    if (f.l[k] < 0 || f.l[k] > 5 || f.m[k] < -f.l[k] - 1 || f.m[k] > f.l[k] + 1)
+                        throw std::runtime_error("harmonic term out of range");
+                    F.hl.push_back(f.l[k]); F.hm.push_back(f.m[k]); F.hg.push_back(f.g[k]);
+                }
+                for (int k = 0; k < 3; ++k) F.offset[k] = f.offset[k];
+            }
             else throw std::runtime_error("field type not supported by the oracle");
             sc.fields.push_back(std::move(F));
         }

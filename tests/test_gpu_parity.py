@@ -71,7 +71,7 @@ def test_tab3_field_matches_oracle(eng, oracle_mod, kind):
     gscale = max(np.abs(dBo).max(), 1e-30)
     assert np.max(np.abs(B - Bo)) <= 1e-12 * scale
     assert np.max(np.abs(dB - dBo)) <= 1e-11 * gscale
-    # mixed precision: corner values in FP64, corner derivatives in FP32
+    # FP32 field mode: FP32 node table, corner-linear base split off
     B32, dB32, _, _ = e.field(q, precision=A.PREC_FP32)
     assert np.max(np.abs(B32 - Bo)) <= 1e-6 * scale
     assert np.max(np.abs(dB32 - dBo)) <= 1e-6 * gscale
@@ -120,6 +120,32 @@ def test_harmonic_field_closed_forms(eng):
         qm[:, k] -= h
         fd = (eng(sc).field(qp)[0] - eng(sc).field(qm)[0]) / (2 * h)
         assert np.max(np.abs(fd - dB[:, :, k])) < 1e-6
+
+
+def test_harmonic_field_matches_oracle(eng, oracle_mod):
+    """Every HarmonicExpansionBField term up to l = 5 (random G), with offset,
+    box, smoothing band and scale: device polynomial vs the oracle's terms
+    derived symbolically (oracle/gen_harmonic.py)."""
+    from pentrack_gb300 import Scene, scenes
+    rng = np.random.default_rng(12)
+    coeffs = [(l, m, float(rng.normal()) * 10.0 ** -l) for l in range(6) for m in range(-l - 1, l + 2)]
+    sc = Scene()
+    sc.add_material("m", 0.0)
+    sc.add_solid(1, 0)
+    sc.add_solid(2, 0, scenes.box_mesh((-1, -1, -1), (1, 1, 1)))
+    sc.add_harmonic(coeffs, offset=(0.02, -0.01, 0.03), b_scale=0.8, boundary_width=0.05,
+                    box=(0.3, -0.3, 0.3, -0.3, 0.25, -0.25))
+    p = rng.uniform(-0.35, 0.35, (3000, 3))
+    q = np.column_stack([p, np.zeros(len(p))])
+    B, dB, _, _ = eng(sc).field(q)
+    Bo, dBo, _, _ = oracle_mod.Oracle(sc).field(q)
+    scale, gscale = np.abs(Bo).max(), np.abs(dBo).max()
+    assert np.max(np.abs(B - Bo)) <= 1e-12 * scale
+    assert np.max(np.abs(dB - dBo)) <= 1e-11 * gscale
+    B32, dB32, _, _ = eng(sc).field(q, precision=A.PREC_FP32)
+    assert np.max(np.abs(B32 - Bo)) <= 1e-6 * scale
+    inside = np.abs(Bo).sum(1) > 0
+    assert inside.sum() > 1000 and (~inside).sum() > 100
 
 
 @pytest.mark.parametrize("mesh", ["cylinder", "hollow"])

@@ -115,3 +115,37 @@ def test_synthetic_fixtures_replicate_reference_files(oracle_mod):
     f = sc.fields[0]
     assert np.allclose(f["x"], g["tab_x"]) and np.allclose(f["z"], g["tab_z"])
     assert np.allclose(f["bz"].reshape(6, 6, 6), g["tab_bz"])
+
+
+def test_oracle_harmonic_terms_match_reference_closed_forms(oracle_mod):
+    """The oracle's harmonic terms (derived symbolically from the expansion's
+    definition) against the reference's closed forms for l <= 2
+    (src/harmonicfields.cpp:76-288), with offset and scale."""
+    from pentrack_gb300 import Scene, scenes
+    rng = np.random.default_rng(5)
+    coeffs = [(0, -1, 0.3), (0, 0, 1e-6), (0, 1, -0.2), (1, -2, 7.5), (1, -1, 0.4), (1, 0, -1.1), (1, 1, 0.9),
+              (1, 2, 0.5), (2, -3, 1.7), (2, -2, -0.6), (2, -1, 0.8), (2, 0, 1.2), (2, 1, -0.3), (2, 2, 0.25), (2, 3, 2.0)]
+    sc = Scene()
+    sc.add_material("m", 0.0)
+    sc.add_solid(1, 0)
+    sc.add_solid(2, 0, scenes.box_mesh((-1, -1, -1), (1, 1, 1)))
+    off = (0.01, -0.02, 0.03)
+    sc.add_harmonic(coeffs, offset=off, b_scale=2.0)
+    p = rng.uniform(-0.3, 0.3, (400, 3))
+    B, dB, _, _ = oracle_mod.Oracle(sc).field(np.column_stack([p, np.zeros(len(p))]))
+    x, y, z = (p[:, k] + off[k] for k in range(3))
+    o = 0 * x
+    forms = {
+        (0, -1): (o, 1 + o, o), (0, 0): (o, o, 1 + o), (0, 1): (1 + o, o, o),
+        (1, -2): (y, x, o), (1, -1): (o, z, y), (1, 0): (-x / 2, -y / 2, z), (1, 1): (z, o, x), (1, 2): (x, -y, o),
+        (2, -3): (2 * x * y, (x - y) * (x + y), o), (2, -2): (2 * y * z, 2 * x * z, 2 * x * y),
+        (2, -1): (-x * y / 2, -x * x / 4 - 3 * y * y / 4 + z * z, 2 * y * z), (2, 0): (-x * z, -y * z, -x * x / 2 - y * y / 2 + z * z),
+        (2, 1): (-3 * x * x / 4 - y * y / 4 + z * z, -x * y / 2, 2 * x * z), (2, 2): (2 * x * z, -2 * y * z, (x - y) * (x + y)),
+        (2, 3): ((x - y) * (x + y), -2 * x * y, o),
+    }
+    ref = np.zeros((len(p), 3))
+    for l, m, g in coeffs:
+        ref += 2.0 * g * np.column_stack(forms[(l, m)])
+    assert np.max(np.abs(B - ref)) < 1e-13 * np.abs(ref).max()
+    assert np.max(np.abs(np.trace(dB, axis1=1, axis2=2))) < 1e-12
+    assert np.max(np.abs(dB - np.transpose(dB, (0, 2, 1)))) < 1e-12
