@@ -66,7 +66,9 @@ enum { PT_NEUTRON = 0, PT_PROTON = 1, PT_ELECTRON = 2 };
 enum {
     PT_FIELD_TAB3D = 1,     /* OPERA3D / 3Dtable / COMSOL: TabField3, tricubic  (src/field_3d.cpp:417-529) */
     PT_FIELD_HARMONIC = 2,  /* HarmonicExpansionBField, l <= 5        (src/harmonicfields.cpp:50-829) */
-    PT_FIELD_UNIFORM_E = 3  /* EDMStaticEField                        (src/edmfields.cpp:181-187) */
+    PT_FIELD_UNIFORM_E = 3, /* EDMStaticEField                        (src/edmfields.cpp:181-187) */
+    PT_FIELD_SOLENOID = 4   /* finite ideal solenoid along z, closed form (no reference counterpart:
+                               the reference approximates it with Conductor segments, src/conductor.cpp) */
 };
 
 /* scheduling form of the tracking kernels */
@@ -123,6 +125,9 @@ typedef struct pt_field {
     const double *g;
     /* PT_FIELD_UNIFORM_E: E [V/m]; potential V = e[2]*z as in src/edmfields.cpp:186 */
     double e[3];
+    /* PT_FIELD_SOLENOID: centre = offset, radius [m], half length [m] and the
+     * field at the centre [T] of a sheet current on the cylinder */
+    double sol_radius, sol_half_length, sol_bcenter;
 } pt_field;
 
 typedef struct pt_scene_desc {

@@ -10,6 +10,7 @@
 #include "../include/pt_constants.h"
 #include "../include/pt_detmath.h"
 #include "harmonic_terms.h"
+#include "../include/pt_solenoid.h"
 
 #include <algorithm>
 #include <atomic>
@@ -274,6 +275,7 @@ struct Field {
     std::vector<int> hl, hm;
     std::vector<double> hg;
     double offset[3] = {0, 0, 0};
+    double sol_a = 0, sol_b = 0, sol_B0 = 0; /* finite solenoid (include/pt_solenoid.h) */
 
     /* TFieldBoundaryBox (src/field.cpp:48-125) */
     bool has_bounds() const { return xmin < xmax && ymin < ymax && zmin < zmax; }
@@ -319,6 +321,8 @@ struct Field {
         if (!in_bounds(x, y, z) || bscale == 0.) return;
         if (type == PT_FIELD_TAB3D) {
             for (int i = 0; i < 3; ++i) tab.interpolate(x, y, z, tab.coeff[i], B[i], dB ? dB[i] : nullptr);
+        } else if (type == PT_FIELD_SOLENOID) {
+            pts_solenoid_field(sol_a, sol_b, sol_B0, x - offset[0], y - offset[1], z - offset[2], B, dB);
         } else if (type == PT_FIELD_HARMONIC) {
             const double xo = x + offset[0], yo = y + offset[1], zo = z + offset[2];
             for (size_t k = 0; k < hg.size(); ++k)
@@ -777,7 +781,7 @@ struct Tracker {
     /* TParticle::derivs + EquationOfMotion (src/particle.cpp:96-135) */
     void derivs(const double *y, double *dydx, double x) {
         double B[3] = {0, 0, 0}, dB[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, E[3] = {0, 0, 0}, V = 0;
-        if (sp.q != 0 || (sp.mu != 0 && y[7] != 0)) bfield(y[0], y[1], y[2], x, B, dB);
+        if (sp.q != 0 || (sp.mu != 0 && y[7] != 0)) bfield(y[0], y[1], y[2], x, B, (sp.mu != 0 && y[7] != 0) ? dB : nullptr);
         if (sp.q != 0) efield(y[0], y[1], y[2], x, V, E);
         if (stats) stats->rhs_evals++;
         eom(y, dydx, B, dB, E);
@@ -1371,6 +1375,13 @@ int pto_create(const pt_scene_desc *d, pto_ctx **out) {
                         throw std::runtime_error("harmonic term out of range");
                     F.hl.push_back(f.l[k]); F.hm.push_back(f.m[k]); F.hg.push_back(f.g[k]);
                 }
+                for (int k = 0; k < 3; ++k) F.offset[k] = f.offset[k];
+            }
+            else if (f.type == PT_FIELD_SOLENOID) {
+                F.sol_a = f.sol_radius;
+                F.sol_b = f.sol_half_length;
+                F.sol_B0 = f.sol_bcenter * std::sqrt(f.sol_radius * f.sol_radius + f.sol_half_length * f.sol_half_length) /
+                           (PT_PI * f.sol_half_length);
                 for (int k = 0; k < 3; ++k) F.offset[k] = f.offset[k];
             }
             else throw std::runtime_error("field type not supported by the oracle");

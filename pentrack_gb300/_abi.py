@@ -20,7 +20,7 @@ ID_INITIAL_NOT_FOUND, ID_CGAL_ERROR, ID_GEOMETRY_ERROR = -5, -6, -7
 ID_ABSORBED_IN_MATERIAL, ID_ABSORBED_ON_SURFACE = 1, 2
 
 NEUTRON, PROTON, ELECTRON = 0, 1, 2
-FIELD_TAB3D, FIELD_HARMONIC, FIELD_UNIFORM_E = 1, 2, 3
+FIELD_TAB3D, FIELD_HARMONIC, FIELD_UNIFORM_E, FIELD_SOLENOID = 1, 2, 3, 4
 MODE_PLAIN, MODE_BATCHED = 0, 1
 PREC_FP64, PREC_FP32 = 0, 1
 
@@ -48,6 +48,7 @@ class Field(C.Structure):
         ("offset", C.c_double * 3), ("n_coeff", C.c_int32), ("reserved2", C.c_int32),
         ("l", c_int32_p), ("m", c_int32_p), ("g", c_double_p),
         ("e", C.c_double * 3),
+        ("sol_radius", C.c_double), ("sol_half_length", C.c_double), ("sol_bcenter", C.c_double),
     ]
 
 

@@ -589,6 +589,14 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
         } else if (f.type == PT_FIELD_UNIFORM_E) {
             o.has_v = 1;
             for (int k = 0; k < 3; ++k) o.e[k] = f.e[k];
+        } else if (f.type == PT_FIELD_SOLENOID) {
+            if (!(f.sol_radius > 0) || !(f.sol_half_length > 0)) { err = "solenoid needs a positive radius and half length"; return PT_ERR_INVALID; }
+            o.has_b = 1;
+            o.sol_a = f.sol_radius;
+            o.sol_b = f.sol_half_length;
+            o.sol_B0 = f.sol_bcenter * std::sqrt(f.sol_radius * f.sol_radius + f.sol_half_length * f.sol_half_length) /
+                       (PT_PI * f.sol_half_length);
+            for (int k = 0; k < 3; ++k) o.offset[k] = f.offset[k];
         } else {
             err = "unsupported field type";
             return PT_ERR_UNSUPPORTED;

@@ -107,7 +107,8 @@ struct DField {
     int pad1;
     const double *mono_c;  /* coefficient of each monomial */
     const int *mono_e;     /* packed exponents i | j<<4 | k<<8 */
-    double offset[3];
+    double offset[3];      /* harmonic: added to the coordinates; solenoid: its centre */
+    double sol_a, sol_b, sol_B0; /* solenoid radius, half length, mu0 n I / pi */
 };
 
 struct DScene {

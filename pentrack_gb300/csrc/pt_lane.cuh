@@ -294,7 +294,9 @@ struct Lane {
         }
         double B[3] = {0, 0, 0}, dB[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, E[3] = {0, 0, 0}, V = 0;
         if (sp.q != 0 || (sp.mu != 0 && yy[7] != 0)) {
-            bfield<true>(S, R.prec, yy[0], yy[1], yy[2], B, dB);
+            /* the Jacobian only feeds the magnetic-moment force */
+            if (sp.mu != 0 && yy[7] != 0) bfield<true>(S, R.prec, yy[0], yy[1], yy[2], B, dB);
+            else bfield<false>(S, R.prec, yy[0], yy[1], yy[2], B, nullptr);
             ++lc.fields;
             /* the value part of the gradient evaluation is bit-identical to a
              * B-only evaluation, so it can serve later B-only queries */
@@ -353,7 +355,7 @@ struct Lane {
         for (int j = 0; j < 3; ++j) W[j] = cb * ((1 - gr) * Bpar[j] + gr * B[j] - gr * vxE[j] * PT_INV_C0_SQ) + ct * axv[j];
     }
     /* TParticle::SpinDerivs (src/particle.cpp:178-193) along the trajectory's dense output */
-    __device__ void spin_derivs(const double *Sv, double *dS, double tt) {
+    __device__ __noinline__ void spin_derivs(const double *Sv, double *dS, double tt) {
         double yy[9], dydt[9], B[3], dB[3][3], V, E[3], W[3];
         calc_state(tt, yy);
         bfield<true>(S, R.prec, yy[0], yy[1], yy[2], B, dB);

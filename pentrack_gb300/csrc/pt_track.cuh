@@ -19,6 +19,7 @@
  */
 #pragma once
 #include "pt_device.cuh"
+#include "../../include/pt_solenoid.h"
 
 namespace ptd {
 
@@ -506,6 +507,12 @@ __device__ void tab3_v(const DField &f, int prec, double x, double y, double z, 
     E[2] = -dF[0][2];
 }
 
+/* finite solenoid (include/pt_solenoid.h); one out-of-line copy: its
+ * elliptic-integral loops would otherwise be inlined at every field call */
+__device__ __noinline__ void solenoid_b(const DField &f, double x, double y, double z, double B[3], double (*dB)[3]) {
+    pts_solenoid_field(f.sol_a, f.sol_b, f.sol_B0, x - f.offset[0], y - f.offset[1], z - f.offset[2], B, dB);
+}
+
 /* harmonic expansion: B = grad Phi of a polynomial Phi (offset applied) */
 template <bool GRAD>
 __device__ void harmonic_b(const DField &f, double x, double y, double z, double B[3], double (*dB)[3]) {
@@ -546,6 +553,7 @@ __device__ void bfield64(const DScene &S, double x, double y, double z, double B
         double Bt[3] = {0, 0, 0}, dBt[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
         if (f.type == PT_FIELD_TAB3D) tab3_b<GRAD>(f, x, y, z, Bt, dBt);
         else if (f.type == PT_FIELD_HARMONIC) harmonic_b<GRAD>(f, x, y, z, Bt, dBt);
+        else if (f.type == PT_FIELD_SOLENOID) solenoid_b(f, x, y, z, Bt, GRAD ? dBt : nullptr);
         for (int i = 0; i < 3; ++i) {
             Bt[i] *= f.bscale;
             if (GRAD) for (int j = 0; j < 3; ++j) dBt[i][j] *= f.bscale;
@@ -586,6 +594,7 @@ __device__ void bfield32(const DScene &S, double x, double y, double z, float B[
             double Bd[3] = {0, 0, 0}, dBd[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
             if (f.type == PT_FIELD_TAB3D) tab3_b<GRAD>(f, x, y, z, Bd, dBd);
             else if (f.type == PT_FIELD_HARMONIC) harmonic_b<GRAD>(f, x, y, z, Bd, dBd);
+            else if (f.type == PT_FIELD_SOLENOID) solenoid_b(f, x, y, z, Bd, GRAD ? dBd : nullptr);
             for (int i = 0; i < 3; ++i) {
                 Bd[i] *= f.bscale;
                 if (GRAD) for (int j = 0; j < 3; ++j) dBd[i][j] *= f.bscale;

@@ -109,6 +109,15 @@ class Scene:
         self.fields.append({"type": A.FIELD_HARMONIC, "l": l, "m": m, "g": g, "offset": offset, "b_scale": b_scale,
                             "e_scale": 0.0, "boundary_width": boundary_width, "box": box})
 
+    def add_solenoid(self, radius, half_length, b_center, center=(0.0, 0.0, 0.0), b_scale=1.0, boundary_width=0.0,
+                     box=(0, 0, 0, 0, 0, 0)):
+        """Finite ideal solenoid along z (closed form, include/pt_solenoid.h):
+        sheet current on rho = radius, |z - zc| <= half_length, field b_center
+        [T] at its centre."""
+        self.fields.append({"type": A.FIELD_SOLENOID, "offset": center, "radius": radius, "half_length": half_length,
+                            "b_center": b_center, "b_scale": b_scale, "e_scale": 0.0, "boundary_width": boundary_width,
+                            "box": box})
+
     def add_uniform_e(self, ex, ey, ez, e_scale=1.0):
         """EDMStaticEField (src/edmfields.cpp:181-187): no box, B scale 0."""
         self.fields.append({"type": A.FIELD_UNIFORM_E, "e": (ex, ey, ez), "b_scale": 0.0, "e_scale": e_scale,
@@ -150,6 +159,9 @@ class Scene:
                 keep += [f["l"], f["m"], f["g"]]
             elif f["type"] == A.FIELD_UNIFORM_E:
                 F.e[:] = f["e"]
+            elif f["type"] == A.FIELD_SOLENOID:
+                F.offset[:] = f["offset"]
+                F.sol_radius, F.sol_half_length, F.sol_bcenter = f["radius"], f["half_length"], f["b_center"]
             flds[i] = F
         d = A.SceneDesc(len(T), _dp(T), _ip(S), len(self.solids), len(self.materials), sol, mats, len(self.fields), 0,
                         flds)
