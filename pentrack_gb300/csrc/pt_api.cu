@@ -1,6 +1,7 @@
 /*
- * pt_api.cu -- kernels and the C ABI of the GB300 tracking engine
- * (declared in include/pentrack_gpu.h).
+ * pt_api.cu -- host side of the GB300 tracking engine: scene upload, the
+ * batched scheduler and the C ABI declared in include/pentrack_gpu.h (the
+ * kernels are in pt_k_*.cu).
  */
 #include <cuda_runtime.h>
 
@@ -15,269 +16,11 @@
 #include <string>
 #include <vector>
 
-#include "pt_lane.cuh"
+#include "pt_kernels.cuh"
 #include "pt_scene.hpp"
 
-using namespace ptd;
+using namespace ptk;
 
-/* ================================================================== */
-/* kernels                                                            */
-/* ================================================================== */
-namespace {
-
-/* sum of v over the lanes in `mask` (any subset of the warp) */
-template <class T> __device__ __forceinline__ T warp_sum(unsigned mask, T v) {
-    T s = 0;
-    for (unsigned m = mask; m; m &= m - 1) s += __shfl_sync(mask, v, __ffs(m) - 1);
-    return s;
-}
-
-__device__ __forceinline__ void flush_counters(DCounters *C, const LaneCounters &lc, double psec, bool active) {
-    /* warp-aggregated atomics over the lanes that reach this point */
-    unsigned long long v[17] = {lc.rk_acc, lc.rk_rej, lc.rhs, lc.fields, lc.hits, lc.bisect, lc.nodes, lc.tris, lc.subseg, lc.dense,
-                                active ? 1ull : 0ull, lc.cand_calls, lc.cand_overflow, lc.cand_sum, lc.tri32, lc.dead, lc.spin};
-    const unsigned mask = __activemask();
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(mask) - 1;
-    for (int k = 0; k < 17; ++k) v[k] = warp_sum(mask, v[k]);
-    double ps = warp_sum(mask, psec);
-    unsigned bm = lc.bisect_max;
-    for (unsigned m = mask; m; m &= m - 1) bm = max(bm, __shfl_sync(mask, lc.bisect_max, __ffs(m) - 1));
-    if (lane == leader && bm) atomicMax(&C->bisect_max, bm);
-    if (lane == leader) {
-        unsigned long long *dst[17] = {&C->rk_accepted, &C->rk_rejected, &C->rhs_evals, &C->field_evals, &C->hits,
-                                       &C->bisection_levels, &C->bvh_nodes, &C->tri_tests, &C->subsegments,
-                                       &C->dense_evals, &C->active, &C->cand_calls, &C->cand_overflow, &C->cand_sum,
-                                       &C->tri32, &C->bisect_dead, &C->spin_steps};
-        for (int k = 0; k < 17; ++k) if (v[k]) atomicAdd(dst[k], v[k]);
-        if (ps != 0) atomicAdd(&C->particle_seconds, ps);
-    }
-}
-
-__global__ void __launch_bounds__(128) k_init(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.n) return;
-    Lane L(S, R);
-    const int64_t n = b.n;
-    L.id = b.id[i];
-    L.t = b.t[i];
-    for (int c = 0; c < 9; ++c) { L.y[c] = b.y[c * n + i]; L.dydt[c] = 0; }
-    for (int c = 0; c < 5; ++c) L.spin[c] = b.spin[c * n + i];
-    L.stop = PT_ID_UNKNOWN;
-    QueryStats qs{0, 0};
-    L.init(qs);
-    L.store_bc_commit(b, i);
-    L.store(b, i);
-    b.hstart[i] = L.hmax;
-    b.t_last[i] = L.t;
-}
-
-/* append v to a work list (warp-aggregated atomic) */
-__device__ __forceinline__ void list_push(int32_t *list, int32_t *count, int32_t v) {
-    const unsigned m = __activemask();
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(m) - 1;
-    const int rank = __popc(m & ((1u << lane) - 1));
-    int base = 0;
-    if (lane == leader) base = atomicAdd(count, __popc(m));
-    base = __shfl_sync(m, base, leader);
-    list[base + rank] = v;
-}
-
-/* active list of a batch: particles not stopped and before t_pause */
-__global__ void k_gather(const __grid_constant__ DBatch b, double t_pause, int32_t *list, int32_t *count) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.n) return;
-    if (b.stop_id[i] != PT_ID_UNKNOWN) return;
-    b.nacc0[i] = b.nacc[i];
-    if (b.flags[i] & PT_F_PENDING) list_push(b.list[3], &b.count[3], (int32_t)i); /* resume a deferred post-step */
-    else if (b.t[i] < t_pause) list_push(list, count, (int32_t)i);
-}
-
-/* a committed particle keeps stepping in this advance call */
-__device__ __forceinline__ bool keeps_going(const DRun &R, const DBatch &b, const Lane &L, int i) {
-    if (L.stop != PT_ID_UNKNOWN || !(L.t < R.t_pause)) return false;
-    return R.max_steps <= 0 || L.nacc - b.nacc0[i] < R.max_steps;
-}
-
-__global__ void k_zero_counts(int32_t *count, int a, int b, int c) {
-    if (threadIdx.x == 0) { count[a] = 0; count[b] = 0; count[c] = 0; }
-}
-
-/* Batched form, phase 1: exactly one Dormand-Prince try for every active
- * particle (all lanes execute the same instruction stream). */
-__global__ void __launch_bounds__(128, 3) k_try(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out) {
-    const int n = b.count[in];
-    const int32_t *lin = b.list[in];
-    Lane L(S, R);
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const int i = lin[k];
-        L.load_try_input(b, i);
-        int r = L.rk_try();
-        L.store_try_output(b, i, r == 1);
-        if (r == 1) {
-            uint32_t f = b.flags[i];
-            L.flags = f;
-            L.store_bc_try(b, i);
-            b.flags[i] = L.flags;
-            list_push(b.list[2], &b.count[2], i);
-        } else if (r == 0) {
-            list_push(b.list[out], &b.count[out], i);
-        } else {
-            b.stop_id[i] = PT_ID_ODEINT_ERROR;
-        }
-    }
-    flush_counters(C, L.lc, 0.0, false);
-}
-
-/* Batched form, phase 2: the common step completion (no clip, no split, no
- * collision); other steps are queued for phase 3. */
-__global__ void __launch_bounds__(128) k_post(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out) {
-    const int n = b.count[2];
-    const int32_t *lp = b.list[2];
-    Lane L(S, R);
-    double ps = 0;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const int i = lp[k];
-        L.load(b, i);
-        L.load_try_end(b, i);
-        L.load_bc(b, i);
-        const double t0 = L.t;
-        if (L.fast_post()) {
-            ps += L.t - t0;
-            L.store_bc_commit(b, i);
-            L.store(b, i);
-            if (keeps_going(R, b, L, i)) list_push(b.list[out], &b.count[out], i);
-        } else {
-            b.flags[i] |= PT_F_PENDING;
-            list_push(b.list[3], &b.count[3], i);
-        }
-    }
-    flush_counters(C, L.lc, ps, false);
-}
-
-/* Batched form, phase 3: the full post-step logic (chord split, CheckHit,
- * hit physics, clipping) for the queued steps, run until the step completes
- * or needs a bisection; those post-steps are suspended and queued for k_bisect. */
-__global__ void __launch_bounds__(128) k_slow(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out) {
-    const int n = b.count[3];
-    const int32_t *ls = b.list[3];
-    Lane L(S, R);
-    double ps = 0;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const int i = ls[k];
-        L.load(b, i);
-        L.load_dense(b, i);
-        L.load_bc(b, i);
-        if (L.flags & PT_F_SUSPENDED) L.load_post(b, i);
-        else L.ps.stage = PS_BEGIN;
-        L.flags &= ~(PT_F_PENDING | PT_F_SUSPENDED);
-        const double t0 = L.t;
-        if (L.post_resume()) {
-            L.flags |= PT_F_PENDING | PT_F_SUSPENDED;
-            L.store_post(b, i);
-            L.store(b, i);
-            list_push(b.list[4], &b.count[4], i);
-            continue;
-        }
-        ps += L.t - t0;
-        L.store_bc_commit(b, i);
-        L.store(b, i);
-        if (keeps_going(R, b, L, i)) list_push(b.list[out], &b.count[out], i);
-    }
-    flush_counters(C, L.lc, ps, false);
-}
-
-/* Batched form, phase 4: the bisections (TTracker::iterate_collision) that
- * suspended post-steps asked for; every lane runs the same search loop.  The
- * post-steps go back to the slow list. */
-__global__ void __launch_bounds__(128, 4) k_bisect(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C) {
-    const int n = b.count[4];
-    const int32_t *lq = b.list[4];
-    Lane L(S, R);
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const int i = lq[k];
-        L.load_bisect_request(b, i);
-        L.ps.bres = L.bisect(L.ps.cx1, L.ps.cya, L.ps.x2, L.ps.y2, L.ps.bxa, L.ps.bao, L.ps.bxb, L.ps.bbo);
-        L.store_bisect_result(b, i);
-        list_push(b.list[3], &b.count[3], i);
-    }
-    flush_counters(C, L.lc, 0.0, false);
-}
-
-/* Plain form: every lane advances its particle by up to `steps` LOOP-A
- * iterations, then the launch ends and the host relaunches. */
-__global__ void __launch_bounds__(128) k_plain(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int steps) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.n) return;
-    if (b.stop_id[i] != PT_ID_UNKNOWN || b.t[i] >= R.t_pause) return;
-    Lane L(S, R);
-    L.load(b, i);
-    const double t0 = L.t;
-    if (R.max_steps > 0) steps = R.max_steps;
-    for (int s = 0; s < steps; ++s) {
-        L.step();
-        if (L.stop != PT_ID_UNKNOWN || L.t >= R.t_pause) break;
-        if (*R.cancel) break;
-    }
-    L.store(b, i);
-    bool active = (L.stop == PT_ID_UNKNOWN && L.t < R.t_pause);
-    flush_counters(C, L.lc, L.t - t0, active);
-}
-
-/* FP64 throughput probe: 8 independent dependent-FMA chains per thread */
-__global__ void k_fp64_probe(double *out, int iters, double a, double b) {
-    double x0 = threadIdx.x * 1e-9, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
-    for (int i = 0; i < iters; ++i) {
-        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
-        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
-    }
-    double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
-    if (s == 1.2345) out[0] = s;
-}
-
-__global__ void k_field(const __grid_constant__ DScene S, int prec, int64_t n, const double *xyzt, double *B, double *dB, double *V, double *E) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double *q = xyzt + 4 * i;
-    double b[3], db[3][3], v, e[3];
-    bfield<true>(S, prec, q[0], q[1], q[2], b, db);
-    efield(S, prec, q[0], q[1], q[2], v, e);
-    if (B) for (int k = 0; k < 3; ++k) B[3 * i + k] = b[k];
-    if (dB) for (int k = 0; k < 9; ++k) dB[9 * i + k] = db[k / 3][k % 3];
-    if (V) V[i] = v;
-    if (E) for (int k = 0; k < 3; ++k) E[3 * i + k] = e[k];
-}
-
-__global__ void k_collisions(const __grid_constant__ DScene S, int64_t n, const double *seg, int maxh, int *count, double *s, double *nrm, int *sid,
-                             double *dn) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    Coll c[PT_MAX_COLLS];
-    QueryStats qs{0, 0};
-    bool cp;
-    int h = mesh_query<1>(S, seg + 6 * i, seg + 6 * i + 3, 0.0, 1.0, c, PT_MAX_COLLS, nullptr, qs, cp);
-    if (cp) { count[i] = -1; return; }
-    count[i] = h;
-    int k = h < maxh ? h : maxh;
-    if (k > PT_MAX_COLLS) k = PT_MAX_COLLS;
-    for (int j = 0; j < k; ++j) {
-        int64_t o = i * maxh + j;
-        s[o] = c[j].s;
-        for (int a = 0; a < 3; ++a) nrm[3 * o + a] = c[j].n[a];
-        sid[o] = (int)c[j].id;
-        dn[o] = c[j].dn;
-    }
-}
-
-__global__ void k_point_solids(const __grid_constant__ DScene S, int64_t n, const double *p, unsigned long long *mask) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    QueryStats qs{0, 0};
-    mask[i] = point_solids(S, p + 3 * i, qs);
-}
-
-} // namespace
 
 /* ================================================================== */
 /* host side                                                          */

@@ -1,0 +1,75 @@
+/*
+ * pt_k_phase.cu -- batched form: active lists, one RK try per particle, fast step completion.
+ */
+#include "pt_kcommon.cuh"
+#include "pt_kernels.cuh"
+
+namespace ptk {
+
+/* active list of a batch: particles not stopped and before t_pause */
+__global__ void k_gather(const __grid_constant__ DBatch b, double t_pause, int32_t *list, int32_t *count) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.n) return;
+    if (b.stop_id[i] != PT_ID_UNKNOWN) return;
+    b.nacc0[i] = b.nacc[i];
+    if (b.flags[i] & PT_F_PENDING) list_push(b.list[3], &b.count[3], (int32_t)i); /* resume a deferred post-step */
+    else if (b.t[i] < t_pause) list_push(list, count, (int32_t)i);
+}
+
+__global__ void k_zero_counts(int32_t *count, int a, int b, int c) {
+    if (threadIdx.x == 0) { count[a] = 0; count[b] = 0; count[c] = 0; }
+}
+
+/* Batched form, phase 1: exactly one Dormand-Prince try for every active
+ * particle (all lanes execute the same instruction stream). */
+__global__ void __launch_bounds__(128, 3) k_try(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out) {
+    const int n = b.count[in];
+    const int32_t *lin = b.list[in];
+    Lane L(S, R);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = lin[k];
+        L.load_try_input(b, i);
+        int r = L.rk_try();
+        L.store_try_output(b, i, r == 1);
+        if (r == 1) {
+            uint32_t f = b.flags[i];
+            L.flags = f;
+            L.store_bc_try(b, i);
+            b.flags[i] = L.flags;
+            list_push(b.list[2], &b.count[2], i);
+        } else if (r == 0) {
+            list_push(b.list[out], &b.count[out], i);
+        } else {
+            b.stop_id[i] = PT_ID_ODEINT_ERROR;
+        }
+    }
+    flush_counters(C, L.lc, 0.0, false);
+}
+
+/* Batched form, phase 2: the common step completion (no clip, no split, no
+ * collision); other steps are queued for phase 3. */
+__global__ void __launch_bounds__(128) k_post(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out) {
+    const int n = b.count[2];
+    const int32_t *lp = b.list[2];
+    Lane L(S, R);
+    double ps = 0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = lp[k];
+        L.load(b, i);
+        L.load_try_end(b, i);
+        L.load_bc(b, i);
+        const double t0 = L.t;
+        if (L.fast_post()) {
+            ps += L.t - t0;
+            L.store_bc_commit(b, i);
+            L.store(b, i);
+            if (keeps_going(R, b, L, i)) list_push(b.list[out], &b.count[out], i);
+        } else {
+            b.flags[i] |= PT_F_PENDING;
+            list_push(b.list[3], &b.count[3], i);
+        }
+    }
+    flush_counters(C, L.lc, ps, false);
+}
+
+} // namespace ptk

@@ -1,0 +1,58 @@
+/*
+ * pt_k_slow.cu -- batched form: the full post-step state machine and the bisections.
+ */
+#include "pt_kcommon.cuh"
+#include "pt_kernels.cuh"
+
+namespace ptk {
+
+/* Batched form, phase 3: the full post-step logic (chord split, CheckHit,
+ * hit physics, clipping) for the queued steps, run until the step completes
+ * or needs a bisection; those post-steps are suspended and queued for k_bisect. */
+__global__ void __launch_bounds__(128) k_slow(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out) {
+    const int n = b.count[3];
+    const int32_t *ls = b.list[3];
+    Lane L(S, R);
+    double ps = 0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = ls[k];
+        L.load(b, i);
+        L.load_dense(b, i);
+        L.load_bc(b, i);
+        if (L.flags & PT_F_SUSPENDED) L.load_post(b, i);
+        else L.ps.stage = PS_BEGIN;
+        L.flags &= ~(PT_F_PENDING | PT_F_SUSPENDED);
+        const double t0 = L.t;
+        if (L.post_resume()) {
+            L.flags |= PT_F_PENDING | PT_F_SUSPENDED;
+            L.store_post(b, i);
+            L.store(b, i);
+            list_push(b.list[4], &b.count[4], i);
+            continue;
+        }
+        ps += L.t - t0;
+        L.store_bc_commit(b, i);
+        L.store(b, i);
+        if (keeps_going(R, b, L, i)) list_push(b.list[out], &b.count[out], i);
+    }
+    flush_counters(C, L.lc, ps, false);
+}
+
+/* Batched form, phase 4: the bisections (TTracker::iterate_collision) that
+ * suspended post-steps asked for; every lane runs the same search loop.  The
+ * post-steps go back to the slow list. */
+__global__ void __launch_bounds__(128, 4) k_bisect(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C) {
+    const int n = b.count[4];
+    const int32_t *lq = b.list[4];
+    Lane L(S, R);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = lq[k];
+        L.load_bisect_request(b, i);
+        L.ps.bres = L.bisect(L.ps.cx1, L.ps.cya, L.ps.x2, L.ps.y2, L.ps.bxa, L.ps.bao, L.ps.bxb, L.ps.bbo);
+        L.store_bisect_result(b, i);
+        list_push(b.list[3], &b.count[3], i);
+    }
+    flush_counters(C, L.lc, 0.0, false);
+}
+
+} // namespace ptk

@@ -1,0 +1,24 @@
+/*
+ * pt_kernels.cuh -- the engine's kernels, defined in pt_k_*.cu and launched
+ * from the host code in pt_api.cu.
+ */
+#pragma once
+#include "pt_device.cuh"
+
+namespace ptk {
+
+__global__ void k_init(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C);
+__global__ void k_gather(const __grid_constant__ DBatch b, double t_pause, int32_t *list, int32_t *count);
+__global__ void k_zero_counts(int32_t *count, int a, int b, int c);
+__global__ void k_try(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out);
+__global__ void k_post(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out);
+__global__ void k_slow(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out);
+__global__ void k_bisect(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C);
+__global__ void k_plain(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int steps);
+__global__ void k_fp64_probe(double *out, int iters, double a, double b);
+__global__ void k_field(const __grid_constant__ DScene S, int prec, int64_t n, const double *xyzt, double *B, double *dB, double *V, double *E);
+__global__ void k_collisions(const __grid_constant__ DScene S, int64_t n, const double *seg, int maxh, int *count, double *s, double *nrm, int *sid,
+                             double *dn);
+__global__ void k_point_solids(const __grid_constant__ DScene S, int64_t n, const double *p, unsigned long long *mask);
+
+} // namespace ptk

@@ -22,6 +22,8 @@
 #include "../../include/pt_solenoid.h"
 
 namespace ptd {
+/* internal linkage: every kernel translation unit has its own copy */
+namespace {
 
 /* ---------------------------------------------------------------- */
 /* Philox4x32-10 stream keyed by (seed, particle id)                 */
@@ -865,4 +867,5 @@ __device__ uint64_t point_solids(const DScene &S, const double *p, QueryStats &q
     return mask;
 }
 
+} // namespace
 } // namespace ptd
