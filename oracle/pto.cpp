@@ -610,10 +610,10 @@ template <int N> struct Dense5 {
             double adt = std::fabs(dt), m = 0;
             for (int i = 0; i < N; ++i) {
                 double e = std::fabs(err[i]) / (eps_abs + eps_rel * (1.0 * std::fabs(x[i]) + adt * std::fabs(dxdt[i])));
-                m = (m < e) ? e : m;
+                m = (m < e || e != e) ? e : m; /* a NaN estimate sticks and rejects the step */
             }
-            if (m > 1.0) {
-                dt *= std::max(0.9 * det_pow(m, -1.0 / 3.0), 0.2);
+            if (!(m <= 1.0)) {
+                dt *= std::fmax(0.9 * (m < 1e300 ? det_pow(m, -1.0 / 3.0) : 0.0), 0.2);
                 ++n_rej;
                 continue;
             }

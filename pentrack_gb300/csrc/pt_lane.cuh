@@ -414,10 +414,10 @@ struct Lane {
                     const double er = fma(dt_ * dc7, dout[i], fma(dt_ * dc6, k6_[i], fma(dt_ * dc5, k5_[i], fma(dt_ * dc4, k4_[i],
                                       fma(dt_ * dc3, k3_[i], (dt_ * dc1) * dxdt[i])))));
                     const double e = fabs(er) / (eps + eps * (1.0 * fabs(x[i]) + adt * fabs(dxdt[i])));
-                    m = (m < e) ? e : m;
+                    m = (m < e || e != e) ? e : m;
                 }
-                if (m > 1.0) {
-                    dt_ *= fmax(0.9 * ptdm_pow(m, -1.0 / 3.0), 0.2);
+                if (!(m <= 1.0)) {
+                    dt_ *= fmax(0.9 * (m < 1e300 ? ptdm_pow(m, -1.0 / 3.0) : 0.0), 0.2);
                     continue;
                 }
                 ts += dt_;
@@ -581,9 +581,9 @@ struct Lane {
         for (int i = 0; i < 9; ++i) {
             double e = fma(h * dc7, dyn[i], fma(h * dc6, k6[i], fma(h * dc5, k5[i], fma(h * dc4, k4[i], fma(h * dc3, k3[i], (h * dc1) * dydt[i])))));
             double r = fabs(e) / (1e-9 + 1e-9 * (fabs(y[i]) + adt * fabs(dydt[i])));
-            m = (m < r) ? r : m;
+            m = (m < r || r != r) ? r : m; /* a NaN estimate sticks and rejects the step */
         }
-        if (m > 1.0) {
+        if (!(m <= 1.0)) {
             dt *= fmax(0.9 * (m < 1e300 ? ptdm_pow(m, -1.0 / 3.0) : 0.0), 0.2);
             ++nrej;
             ++lc.rk_rej;

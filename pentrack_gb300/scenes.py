@@ -265,6 +265,37 @@ def source_cylinder(seed, ids, rmin, rmax, zmin, zmax, emin, emax, theta=(0.0, P
     return pos, _kinematics(seed, ids, emin, emax, theta, phi, polarization, spectrum)
 
 
+def electron_beta_spectrum(E):
+    """ElectronBetaSpectrum (src/globals.cpp:96-101): relative intensity (< 1)
+    of neutron-decay electrons at kinetic energy E [eV] (0 <= E <= 782 keV)."""
+    q = 0.782
+    e = np.asarray(E, dtype=np.float64) * 1e-6
+    mec2 = M_E * C0 * C0 / ELE_E * 1e-6
+    return 8.2 * np.sqrt(e * e + 2 * e * mec2) * (q - e) ** 2 * (e + mec2)
+
+
+def spectrum_sampler(f, emin, emax, tries=256, first_draw=1000):
+    """Rejection sampling of the spectrum f (max < 1) on [emin, emax], as the
+    reference's source does for its spectrum formula; draw pairs come from the
+    particle's own Philox stream, so samples do not depend on the batch."""
+    def sample(seed, ids):
+        ids = np.asarray(ids, dtype=np.int64)
+        E = np.full(len(ids), np.nan)
+        todo = np.ones(len(ids), bool)
+        for k in range(tries):
+            if not todo.any():
+                break
+            e = emin + _draw(seed, ids, first_draw + 2 * k) * (emax - emin)
+            u = _draw(seed, ids, first_draw + 2 * k + 1)
+            acc = todo & (u < f(e))
+            E[acc] = e[acc]
+            todo &= ~acc
+        if todo.any():
+            raise RuntimeError(f"spectrum sampling did not converge for {int(todo.sum())} particles")
+        return E
+    return sample
+
+
 def _kinematics(seed, ids, emin, emax, theta, phi, polarization, spectrum=None):
     u = _draw(seed, ids, 3)
     pol = np.where(u < 0.5 * (polarization + 1), 1.0, -1.0)  # polarization_distribution (include/mc.h:22-48)

@@ -128,3 +128,46 @@ def integration_test_acceleration(grad=0.5):
     """a = -g - |mu_n| dBz/dz / m_n, the analytic answer the reference's
     showintegrationresult.cxx checks (-15.5754762729 m/s^2 for 1 T/m)."""
     return -S.GRAV - abs(S.MU_N) * grad / (S.M_N * S.ELE_E)
+
+
+def mixed_species_scene(nseg=160):
+    """Configuration 3's geometry and fields: a cylinder R = 0.3 m, z in
+    [-0.5, 0.5] whose wall is a closed 1 cm shell (solid 2) with a detector
+    disc at the top (solid 3, z in [0.495, 0.4999]); particles move in the
+    default medium (solid 1) and charged OnStep absorbs them as soon as they
+    are in a solid with ID > 1 (src/proton.cpp:25-33).  Fields: a 1 T finite
+    solenoid (radius 0.5 m, length 2 m) and E = (0, 0, 3e4 V/m) with the
+    reference's V = Ez z.  3 x 4 x nseg triangles (1,920 for nseg = 160)."""
+    sc = Scene()
+    sc.add_material("vacuum", 0.0)
+    sc.add_material("wall", 0.0)
+    sc.add_material("detector", 0.0)
+    sc.add_solid(1, "vacuum")
+    outer = S.cylinder_mesh(0.31, -0.51, 0.51, nseg)
+    inner = S.cylinder_mesh(0.3, -0.5, 0.5, nseg).reshape(-1, 3, 3)[:, [0, 2, 1], :].reshape(-1, 9)  # facing inwards
+    sc.add_solid(2, "wall", np.vstack([outer, inner]))
+    sc.add_solid(3, "detector", S.cylinder_mesh(0.299, 0.495, 0.4999, nseg))
+    sc.add_solenoid(0.5, 1.0, 1.0)
+    sc.add_uniform_e(0.0, 0.0, 3e4)
+    return sc
+
+
+def mixed_species(n_protons=100_000, n_electrons=100_000, seed=1003, tmax=1e-3):
+    """Configuration 3: decay protons (E ~ U[0, 750] eV) and electrons (beta
+    spectrum on [0, 782] keV), isotropic, uniform in the cylinder; tracked up
+    to 1 ms proper time (tmax, which the reference reports as ID_DECAYED).
+    Returns the scene and per-species (params, particles) pairs; the species
+    run as two calls (the C ABI takes one species per run).  Polarisation 0:
+    no magnetic-moment force on the charged particles."""
+    sc = mixed_species_scene()
+    out = {}
+    spec_e = S.spectrum_sampler(S.electron_beta_spectrum, 0.0, 782e3)
+    first = 0
+    for species, n, emax, spec in ((A.PROTON, n_protons, 750.0, None), (A.ELECTRON, n_electrons, 782e3, spec_e)):
+        ids = np.arange(first, first + n, dtype=np.int64)
+        first += n
+        pos, (E, ph, th, pol) = S.source_cylinder(seed, ids, 0.0, 0.3, -0.5, 0.5, 0.0, emax, polarization=0.0, spectrum=spec)
+        parts = S.make_particles(seed, ids, pos, E, ph, th, np.zeros(n), species=species)
+        params = run_params(species, simtime=1.0, tau=0.0, tmax=tmax, lmax=9e99, bmax=0.0, spintimes=(), seed=seed)
+        out[species] = (params, parts)
+    return sc, out

@@ -32,3 +32,25 @@ def test_field_storage_distributions_match_oracle(built, oracle_mod):
         fg, fo = np.mean(gout.stop_id == sid), np.mean(oout.stop_id == sid)
         se = np.sqrt(max(fo * (1 - fo), 1.0 / n) / n)
         assert abs(fg - fo) <= 3 * np.sqrt(2) * se + 1.0 / n, (sid, fg, fo)
+
+
+@pytest.mark.parametrize("species", [A.PROTON, A.ELECTRON])
+def test_mixed_species_distributions_match_oracle(built, oracle_mod, species):
+    """Configuration 3 (decay protons / beta electrons in a 1 T solenoid plus a
+    30 kV/m field, absorbing wall and detector): end time, end z and the
+    fractions of particles absorbed in the wall and on the detector."""
+    stats = pytest.importorskip("scipy.stats")
+    from pentrack_gb300 import Engine, workloads
+    sc, runs = workloads.mixed_species(n_protons=2000, n_electrons=2000)
+    params, parts = runs[species]
+    oout, _ = oracle_mod.Oracle(sc).integrate(params, parts)
+    params.mode = A.MODE_BATCHED
+    gout, gst = Engine(sc).integrate(params, parts)
+    assert np.all(gout.stop_id == A.ID_ABSORBED_IN_MATERIAL) and np.all(oout.stop_id == A.ID_ABSORBED_IN_MATERIAL)
+    for name, g, o in (("t_end", gout.t, oout.t), ("z", gout.y[2], oout.y[2])):
+        p = stats.ks_2samp(g, o).pvalue
+        assert p > 0.01, (name, p)
+    n = len(parts.t)
+    for sid in (2, 3):
+        fg, fo = np.mean(gout.solid == sid), np.mean(oout.solid == sid)
+        assert abs(fg - fo) <= 3 * np.sqrt(2 * max(fo * (1 - fo), 1.0 / n) / n) + 1.0 / n, (sid, fg, fo)
