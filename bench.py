@@ -227,7 +227,7 @@ def e2e_run(args, engine, params, rank, T):
         return p, parts
 
     h2d = d2h = 0
-    total_ps, total_s = 0.0, 0.0
+    total_ps, total_s, dev_ms = 0.0, 0.0, 0.0
     for k in range(1 + args.e2e_steps):
         p, parts = pinned_set(10_000_000 * (k + 1) + rank * n)
         p.field_precision, p.mode = params.field_precision, params.mode
@@ -238,10 +238,12 @@ def e2e_run(args, engine, params, rank, T):
             continue
         total_ps += st["particle_seconds"]
         total_s += dt
+        dev_ms += st["span_ms"]
         h2d = n * (8 + 8 + 72 + 40)
         d2h = n * (8 + 8 + 72 + 40 + 4 * 4 + 8 * 6)
     return {"value": total_ps / total_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-            "steps": args.e2e_steps, "call": "pt_integrate (host buffers, full H2D/D2H per step)"}
+            "steps": args.e2e_steps, "call": "pt_integrate (host buffers, full H2D/D2H per step)",
+            "ms_per_step": total_s * 1e3 / args.e2e_steps, "tracking_device_ms_per_step": dev_ms / args.e2e_steps}
 
 
 def load_traffic():

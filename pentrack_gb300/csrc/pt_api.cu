@@ -14,6 +14,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "pt_kernels.cuh"
@@ -46,6 +47,10 @@ struct pt_ctx {
     DCounters *counters = nullptr;
     DCounters *counters_host = nullptr;
     int sm_count = 0;
+    /* device arena kept between pt_integrate calls (their batches are
+     * created and destroyed inside the call) */
+    void *arena = nullptr;
+    size_t arena_bytes = 0;
 };
 
 /* Scratch of pt_segment_collisions_noalloc: a fixed device array in the
@@ -81,7 +86,7 @@ struct pt_batch {
     DBatch b{};
     DRun run{};
     std::vector<double> spintimes;
-    std::vector<void *> allocs;
+    std::vector<void *> allocs;   /* owned device memory (one arena) */
     int max_launches = 0;
     double timeout_s = 0;
 };
@@ -522,6 +527,7 @@ void pt_destroy(pt_ctx *c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_list(c->allocs);
+    if (c->arena) cudaFree(c->arena);
     if (c->counters) cudaFree(c->counters);
     if (c->counters_host) cudaFreeHost(c->counters_host);
     if (c->cancel_host) cudaFreeHost(c->cancel_host);
@@ -539,7 +545,44 @@ pt_status pt_cancel(pt_ctx *c) {
     return PT_OK;
 }
 
-pt_status pt_batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles *in, pt_batch **out) {
+} // extern "C"
+
+namespace {
+
+/* Places every DBatch array in one arena (256-byte aligned blocks); with
+ * base == nullptr only the size is computed. */
+size_t batch_layout(DBatch &b, int64_t n, unsigned char *base) {
+    size_t off = 0;
+    auto take = [&](auto *&ptr, size_t count) {
+        using T = std::remove_pointer_t<std::remove_reference_t<decltype(ptr)>>;
+        off = (off + 255) & ~(size_t)255;
+        ptr = base ? (T *)(base + off) : nullptr;
+        off += std::max<size_t>(count, 1) * sizeof(T);
+    };
+    const size_t m = (size_t)n;
+    take(b.id, m); take(b.t, m); take(b.y, 9 * m); take(b.dydt, 9 * m); take(b.dt, m);
+    take(b.spin, 5 * m); take(b.tau, m); take(b.hmax, m); take(b.noflip, m); take(b.hstart, m);
+    take(b.t_last, m); take(b.stop_id, m); take(b.nhit, m); take(b.nstep, m);
+    take(b.nspinflip, m); take(b.nsol, m); take(b.flags, m); take(b.stack, m);
+    take(b.rng_n, m); take(b.nacc, m); take(b.nrej, m); take(b.ntry, m);
+    take(b.yn, 9 * m); take(b.dyn, 9 * m); take(b.kst, 36 * m); take(b.tn, m);
+    take(b.bc, 14 * m); take(b.count, 8); take(b.nacc0, m);
+    take(b.ps_d, 42 * m); take(b.ps_i, (7 + PT_MAX_CAND) * m);
+    for (int k = 0; k < 5; ++k) take(b.list[k], m);
+    return (off + 255) & ~(size_t)255;
+}
+
+pt_status batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles *in, pt_batch **out, bool use_ctx_arena);
+
+} // namespace
+
+extern "C" pt_status pt_batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles *in, pt_batch **out) {
+    return batch_create(c, p, in, out, false);
+}
+
+namespace {
+
+pt_status batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles *in, pt_batch **out, bool use_ctx_arena) {
     if (!c || !p || !in || !out || in->n < 0 || !in->id || !in->t || !in->y) return PT_ERR_INVALID;
     cudaSetDevice(c->device);
     *out = nullptr;
@@ -566,17 +609,24 @@ pt_status pt_batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles 
     DBatch &b = B->b;
     b.n = n;
     cudaError_t e = cudaSuccess;
-#define ALLOC(field, T, cnt) b.field = dalloc<T>(B->allocs, (size_t)(cnt), e); if (e) { free_list(B->allocs); return ck(c, e, "batch alloc"), PT_ERR_OOM; }
-    ALLOC(id, int64_t, n) ALLOC(t, double, n) ALLOC(y, double, 9 * n) ALLOC(dydt, double, 9 * n) ALLOC(dt, double, n)
-    ALLOC(spin, double, 5 * n) ALLOC(tau, double, n) ALLOC(hmax, double, n) ALLOC(noflip, double, n) ALLOC(hstart, double, n)
-    ALLOC(t_last, double, n) ALLOC(stop_id, int32_t, n) ALLOC(nhit, int32_t, n) ALLOC(nstep, int32_t, n)
-    ALLOC(nspinflip, int32_t, n) ALLOC(nsol, int32_t, n) ALLOC(flags, uint32_t, n) ALLOC(stack, uint64_t, n)
-    ALLOC(rng_n, uint64_t, n) ALLOC(nacc, int64_t, n) ALLOC(nrej, int64_t, n) ALLOC(ntry, int32_t, n)
-    ALLOC(yn, double, 9 * n) ALLOC(dyn, double, 9 * n) ALLOC(kst, double, 36 * n) ALLOC(tn, double, n)
-    ALLOC(bc, double, 14 * n) ALLOC(count, int32_t, 8) ALLOC(nacc0, int64_t, n)
-    ALLOC(ps_d, double, 42 * n) ALLOC(ps_i, int32_t, (7 + PT_MAX_CAND) * n)
-    for (int k = 0; k < 5; ++k) { b.list[k] = dalloc<int32_t>(B->allocs, (size_t)n, e); if (e) { free_list(B->allocs); return ck(c, e, "batch alloc"), PT_ERR_OOM; } }
-#undef ALLOC
+    const size_t bytes = batch_layout(b, n, nullptr);
+    unsigned char *base = nullptr;
+    if (use_ctx_arena) { /* pt_integrate: reuse the context's arena when it is large enough */
+        if (c->arena_bytes < bytes) {
+            if (c->arena) cudaFree(c->arena);
+            c->arena = nullptr;
+            c->arena_bytes = 0;
+            if ((e = cudaMalloc(&c->arena, bytes))) { c->arena = nullptr; return ck(c, e, "batch alloc"), PT_ERR_OOM; }
+            c->arena_bytes = bytes;
+        }
+        base = (unsigned char *)c->arena;
+    } else {
+        void *a = nullptr;
+        if ((e = cudaMalloc(&a, bytes))) return ck(c, e, "batch alloc"), PT_ERR_OOM;
+        B->allocs.push_back(a);
+        base = (unsigned char *)a;
+    }
+    batch_layout(b, n, base);
     if (n > 0) {
         if ((e = cudaMemcpyAsync(b.id, in->id, n * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream)) ||
             (e = cudaMemcpyAsync(b.t, in->t, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) ||
@@ -596,6 +646,10 @@ pt_status pt_batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles 
     *out = B.release();
     return PT_OK;
 }
+
+} // namespace
+
+extern "C" {
 
 void pt_batch_destroy(pt_batch *B) {
     if (!B) return;
@@ -710,7 +764,7 @@ pt_status pt_integrate(pt_ctx *c, const pt_run_params *p, const pt_particles *in
     if (!c || !p || !in || !out) return PT_ERR_INVALID;
     auto w0 = std::chrono::steady_clock::now();
     pt_batch *B = nullptr;
-    pt_status st = pt_batch_create(c, p, in, &B);
+    pt_status st = batch_create(c, p, in, &B, true);
     if (st != PT_OK) return st;
     pt_stats s;
     std::memset(&s, 0, sizeof(s));
