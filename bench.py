@@ -306,7 +306,7 @@ def run_ours(args, rank, world):
         try_f64 = tries * (650 + 6 * 60) + (0 if args.precision == "fp32" else tries * 6 * field_per_rhs)
         try_f64 += tries * 6 * 128 if args.precision == "fp32" else 0  # FP64 corner-value terms of the mixed field
         launches = max(1, agg["dominant_launches"])
-        kern = {"k_try": agg["try_ms"], "k_post": agg["post_ms"], "k_slow": agg["slow_ms"], "k_bisect": agg["bisect_ms"]}
+        kern = {"k_try": agg["try_ms"], "k_post": agg["post_ms"], "k_slow": agg["slow_ms"], "k_bisect": agg["bisect_ms"], "k_plain_tail": agg["tail_ms"]}
         dom = max(kern, key=kern.get)
         avg_launch_s = kern[dom] / 1e3 / launches
         achieved = (try_f64 if dom == "k_try" else f64) / launches / avg_launch_s / 1e12
@@ -349,7 +349,7 @@ def run_ours(args, rank, world):
                                         "bisection_levels", "bvh_nodes", "tri_tests", "subsegments", "dense_evals",
                                         "bisect_max", "bisect_dead", "cand_calls", "cand_overflow", "cand_sum", "tri32_tests")},
         "live_particles": int(agg["active"]),
-        "phase_ms": {"k_try": agg["try_ms"], "k_post": agg["post_ms"], "k_slow": agg["slow_ms"], "k_bisect": agg["bisect_ms"]},
+        "phase_ms": {"k_try": agg["try_ms"], "k_post": agg["post_ms"], "k_slow": agg["slow_ms"], "k_bisect": agg["bisect_ms"], "k_plain_tail": agg["tail_ms"]},
     }
     if not args.no_plain and args.mode == "batched":
         line["plain_form"] = plain_run(args, rank)

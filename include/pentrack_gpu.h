@@ -209,6 +209,7 @@ typedef struct pt_stats {
     double bisect_ms;          /* batched form: device time of the bisection kernel */
     int64_t bisect_dead;       /* bisection intervals abandoned because neither half collides */
     int64_t spin_steps;        /* accepted steps of the spin (Bloch) integration */
+    double tail_ms;            /* batched form: device time of the plain-form tail launches */
 } pt_stats;
 
 typedef struct pt_ctx pt_ctx;

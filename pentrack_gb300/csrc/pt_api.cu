@@ -376,6 +376,44 @@ int persistent_grid(pt_ctx *c, const void *fn, int block) {
     return per_sm * c->sm_count;
 }
 
+/* Plain form: k_plain launches (one lane per particle, up to steps_per_launch
+ * LOOP-A iterations or the step budget) until no particle is active; also the
+ * tail of the batched form (budgets counted from the call's start). */
+pt_status advance_plain(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc, std::chrono::steady_clock::time_point w0,
+                        bool &cancelled, bool &timed_out, bool from_nacc0) {
+    cudaError_t e;
+    const int steps = R.steps_per_launch, block = 128;
+    const int64_t n = B->b.n;
+    const int max_steps = R.max_steps;
+    for (int launch = 0;; ++launch) {
+        if ((e = cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream))) return ck(c, e, "memset"), PT_ERR_CUDA;
+        cudaEventRecord(c->ev0, c->stream);
+        k_plain<<<grid_for(n, block), block, 0, c->stream>>>(c->scene, R, B->b, c->counters, steps, from_nacc0 ? 1 : 0);
+        cudaEventRecord(c->ev1, c->stream);
+        if ((e = cudaGetLastError())) return ck(c, e, "k_plain launch"), PT_ERR_CUDA;
+        if ((e = cudaMemcpyAsync(c->counters_host, c->counters, sizeof(DCounters), cudaMemcpyDeviceToHost, c->stream)))
+            return ck(c, e, "counters"), PT_ERR_CUDA;
+        if ((e = cudaStreamSynchronize(c->stream))) return ck(c, e, "k_plain"), PT_ERR_CUDA;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        const DCounters &k = *c->counters_host;
+        acc.kernel_ms += ms;
+        acc.dominant_kernel_ms += ms;
+        acc.dominant_launches += 1;
+        acc.launches += 1;
+        add_counters(acc, k);
+        acc.active = (int64_t)k.active;
+        if (*(volatile int *)c->cancel_host) { cancelled = true; break; }
+        if (k.active == 0 || max_steps > 0) break; /* a step budget is one fixed step-batch launch */
+        if (B->max_launches > 0 && launch + 1 >= B->max_launches) { timed_out = true; break; }
+        if (B->timeout_s > 0 && std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count() > B->timeout_s) {
+            timed_out = true;
+            break;
+        }
+    }
+    return PT_OK;
+}
+
 /* Batched (phase-split) form: per iteration one RK try for every active
  * particle (k_try), the common completion (k_post) and the full post-step
  * logic for queued steps (k_slow), over work lists in device memory. */
@@ -405,6 +443,11 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
      * particle still executes its own operations in its own order, so the
      * results equal the plain form's bit for bit. */
     int64_t l_slow = 0;
+    /* Once few particles remain, iterations cost mostly launch latency: the
+     * queue is drained and the rest runs as plain-form lanes (same
+     * per-particle arithmetic, so the same bits). */
+    const int tail = (int)std::max<int64_t>(2048, n / 50);
+    bool to_plain = false;
     for (int it = 0;; ++it) {
         const int in = it & 1, out = in ^ 1;
         if ((e = cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream))) { st = ck(c, e, "memset"), PT_ERR_CUDA; break; }
@@ -427,7 +470,7 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
         int active = hcount[out], slow = hcount[3];
         /* rounds of k_slow (each queued post-step runs to its end or to its
          * next bisection) and k_bisect, while the queue fills the GPU */
-        while (slow > 0 && (slow >= std::max(2048, active / 4) || active == 0)) {
+        while (slow > 0 && (slow >= std::max(2048, active / 4) || active == 0 || active <= tail)) {
             cudaEventRecord(ev[3], c->stream);
             k_slow<<<g_slow, block, 0, c->stream>>>(c->scene, R, b, c->counters, out);
             cudaEventRecord(ev[4], c->stream);
@@ -455,6 +498,7 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
         acc.active = active + slow;
         if (*(volatile int *)c->cancel_host) { cancelled = true; break; }
         if (active == 0 && slow == 0) break;
+        if (active <= tail && slow == 0) { to_plain = true; break; }
         if (B->max_launches > 0 && acc.launches >= B->max_launches) { timed_out = true; break; }
         if (B->timeout_s > 0 && std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count() > B->timeout_s) {
             timed_out = true;
@@ -463,6 +507,11 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
     }
     for (int k = 0; k < 6; ++k) cudaEventDestroy(ev[k]);
     cudaFreeHost(hcount);
+    if (st == PT_OK && to_plain && !cancelled && !timed_out) {
+        const double k0 = acc.kernel_ms;
+        st = advance_plain(c, B, R, acc, w0, cancelled, timed_out, true);
+        acc.tail_ms = acc.kernel_ms - k0;
+    }
     const char *name = "k_try";
     double dom = t_try;
     if (t_post > dom) { dom = t_post; name = "k_post"; }
@@ -683,31 +732,9 @@ pt_status pt_batch_advance_steps(pt_ctx *c, pt_batch *B, double t_pause, int32_t
         st = advance_batched(c, B, R, acc, w0, cancelled, timed_out);
         if (st != PT_OK) return st;
     }
-    for (int launch = 0; n > 0 && R.mode != PT_MODE_BATCHED; ++launch) {
-        if ((e = cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream))) return ck(c, e, "memset"), PT_ERR_CUDA;
-        cudaEventRecord(c->ev0, c->stream);
-        k_plain<<<grid_for(n, block), block, 0, c->stream>>>(c->scene, R, B->b, c->counters, steps);
-        cudaEventRecord(c->ev1, c->stream);
-        if ((e = cudaGetLastError())) return ck(c, e, "k_plain launch"), PT_ERR_CUDA;
-        if ((e = cudaMemcpyAsync(c->counters_host, c->counters, sizeof(DCounters), cudaMemcpyDeviceToHost, c->stream)))
-            return ck(c, e, "counters"), PT_ERR_CUDA;
-        if ((e = cudaStreamSynchronize(c->stream))) return ck(c, e, "k_plain"), PT_ERR_CUDA;
-        float ms = 0;
-        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-        const DCounters &k = *c->counters_host;
-        acc.kernel_ms += ms;
-        acc.dominant_kernel_ms += ms;
-        acc.dominant_launches += 1;
-        acc.launches += 1;
-        add_counters(acc, k);
-        acc.active = (int64_t)k.active;
-        if (*(volatile int *)c->cancel_host) { cancelled = true; break; }
-        if (k.active == 0 || max_steps > 0) break; /* a step budget is one fixed step-batch launch */
-        if (B->max_launches > 0 && launch + 1 >= B->max_launches) { timed_out = true; break; }
-        if (B->timeout_s > 0 && std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count() > B->timeout_s) {
-            timed_out = true;
-            break;
-        }
+    if (R.mode != PT_MODE_BATCHED && n > 0) {
+        st = advance_plain(c, B, R, acc, w0, cancelled, timed_out, false);
+        if (st != PT_OK) return st;
     }
     cudaEventRecord(c->evs1, c->stream);
     cudaEventSynchronize(c->evs1);
