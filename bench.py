@@ -217,22 +217,28 @@ def e2e_run(args, engine, params, rank, T):
     import torch
     n = args.n
 
+    def pinned(a):
+        tt = torch.empty(a.shape, dtype=torch.from_numpy(a).dtype, pin_memory=True)
+        tt.numpy()[...] = a
+        return tt.numpy()
+
     def pinned_set(seed_first):
+        from pentrack_gb300 import ParticleSet
         _, p, parts = workloads.field_storage(n=n, simtime=T, engine=engine, first_id=seed_first)
         for k in ("id", "t", "y", "spin"):
-            a = getattr(parts, k)
-            tt = torch.empty(a.shape, dtype=torch.from_numpy(a).dtype, pin_memory=True)
-            tt.numpy()[...] = a
-            setattr(parts, k, tt.numpy())
-        return p, parts
+            setattr(parts, k, pinned(getattr(parts, k)))
+        out = ParticleSet.empty(n)  # caller-owned pinned output buffers
+        for k in ("id", "t", "y", "spin") + tuple(f for f, _ in ParticleSet.OUT_FIELDS):
+            setattr(out, k, pinned(getattr(out, k)))
+        return p, parts, out
 
     h2d = d2h = 0
     total_ps, total_s, dev_ms = 0.0, 0.0, 0.0
     for k in range(1 + args.e2e_steps):
-        p, parts = pinned_set(10_000_000 * (k + 1) + rank * n)
+        p, parts, dst = pinned_set(10_000_000 * (k + 1) + rank * n)
         p.field_precision, p.mode = params.field_precision, params.mode
         t0 = time.perf_counter()
-        out, st = engine.integrate(p, parts)
+        out, st = engine.integrate(p, parts, out=dst)
         dt = time.perf_counter() - t0
         if k == 0:
             continue

@@ -186,6 +186,19 @@ class ParticleSet:
         for name, dt in self.OUT_FIELDS:
             setattr(self, name, np.zeros(n, dtype=dt))
 
+    @classmethod
+    def empty(cls, n):
+        """A set with uninitialised arrays (every field is an output of pt_batch_read)."""
+        p = cls.__new__(cls)
+        p.n = int(n)
+        p.id = np.empty(n, np.int64)
+        p.t = np.empty(n)
+        p.y = np.empty((9, n))
+        p.spin = np.empty((5, n))
+        for name, dt in cls.OUT_FIELDS:
+            setattr(p, name, np.empty(n, dtype=dt))
+        return p
+
     def copy(self):
         p = ParticleSet(self.n, self.id.copy(), self.t.copy(), self.y.copy(), self.spin.copy())
         for name, _ in self.OUT_FIELDS:
@@ -286,9 +299,14 @@ class Engine:
             raise EngineError(st, lib().pt_last_error(self.h).decode())
         return st
 
-    def integrate(self, params, particles):
-        """Track every particle to its stop ID (host arrays in and out)."""
-        out = particles.copy()
+    def integrate(self, params, particles, out=None):
+        """Track every particle to its stop ID (host arrays in and out).  `out`
+        (a ParticleSet of the same size, e.g. with pinned arrays) receives the
+        end states; by default fresh arrays are allocated."""
+        if out is None:
+            out = ParticleSet.empty(particles.n)
+        elif out.n != particles.n:
+            raise ValueError("output set has a different size")
         stats = A.Stats()
         pin, pout = particles.abi(outputs=False), out.abi()
         self.last_status = self._check(lib().pt_integrate(self.h, C.byref(params), C.byref(pin), C.byref(pout), C.byref(stats)))
