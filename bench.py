@@ -43,7 +43,9 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--n", type=int, default=1_000_000, help="particles per GPU")
+    p.add_argument("--n", type=int, default=None, help="particles per GPU (default 1e6; 1e7 for large_mesh)")
+    p.add_argument("--workload", default="field_storage", choices=["field_storage", "large_mesh"],
+                   help="field_storage: the headline configuration; large_mesh: the 200k-triangle, 128^3 scale-up")
     p.add_argument("--batch-steps", type=int, default=32, help="accepted RK steps per particle per bench step")
     p.add_argument("--precision", default="fp32", choices=["fp64", "fp32"],
                    help="field evaluation: fp64, or fp32 = mixed (corner values FP64, derivative terms FP32)")
@@ -123,13 +125,26 @@ def algorithmic_work(st, precision):
     return other64 + field_flops, 0
 
 
+def make_workload(args, n, engine=None, first_id=0, simtime=None, scene=None):
+    from pentrack_gb300 import workloads
+    kw = {} if simtime is None else {"simtime": simtime}
+    if args.workload == "large_mesh":
+        return workloads.large_mesh(n=n, engine=engine, first_id=first_id, scene=scene, **kw)
+    return workloads.field_storage(n=n, engine=engine, first_id=first_id, **kw)
+
+
+def make_scene(args):
+    from pentrack_gb300 import workloads
+    return workloads.large_mesh_scene() if args.workload == "large_mesh" else workloads.field_storage_scene()
+
+
 def setup_ours(args, rank):
-    from pentrack_gb300 import Engine, _abi as A, replicas, workloads
+    from pentrack_gb300 import Engine, _abi as A, replicas
     device = int(os.environ.get("LOCAL_RANK", 0))
-    scene = workloads.field_storage_scene()
+    scene = make_scene(args)
     engine = Engine(scene, device=device)
     first, count = replicas.shard(args.n, rank)
-    _, params, parts = workloads.field_storage(n=count, engine=engine, first_id=first)
+    _, params, parts = make_workload(args, count, engine=engine, first_id=first, scene=scene)
     params.field_precision = A.PREC_FP32 if args.precision == "fp32" else A.PREC_FP64
     params.mode = A.MODE_BATCHED if args.mode == "batched" else A.MODE_PLAIN
     return engine, params, parts, device
@@ -162,7 +177,7 @@ def cpu_baseline(args, T, n_hint=2048):
     from oracle import pyoracle
     from pentrack_gb300 import Engine, workloads
     cores = os.cpu_count()
-    scene = workloads.field_storage_scene()
+    scene = make_scene(args)
     orc = pyoracle.Oracle(scene)
     eng = None
     try:
@@ -172,7 +187,7 @@ def cpu_baseline(args, T, n_hint=2048):
     m = n_hint
     total_ps, total_s = 0.0, 0.0
     while True:
-        _, params, parts = workloads.field_storage(n=m, simtime=T, engine=eng)
+        _, params, parts = make_workload(args, m, engine=eng, simtime=T, scene=scene)
         t0 = time.perf_counter()
         out, st = orc.integrate(params, parts, nthreads=cores)
         dt = time.perf_counter() - t0
@@ -224,7 +239,7 @@ def e2e_run(args, engine, params, rank, T):
 
     def pinned_set(seed_first):
         from pentrack_gb300 import ParticleSet
-        _, p, parts = workloads.field_storage(n=n, simtime=T, engine=engine, first_id=seed_first)
+        _, p, parts = make_workload(args, n, engine=engine, first_id=seed_first, simtime=T)
         for k in ("id", "t", "y", "spin"):
             setattr(parts, k, pinned(getattr(parts, k)))
         out = ParticleSet.empty(n)  # caller-owned pinned output buffers
@@ -335,8 +350,11 @@ def run_ours(args, rank, world):
         "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f64 state, f32 field",
         "data": "synthetic (seeded Philox sources; analytic quadrupole table)",
-        "config": {"workload": f"field storage: {args.n} UCN/GPU, cylinder R=0.2 m H=0.1 m (1024 triangles), "
-                               f"64^3 tricubic quadrupole, 250 neV walls 5% Lambert 1e-4 loss, tau 880 s",
+        "config": {"workload": (f"field storage: {args.n} UCN/GPU, cylinder R=0.2 m H=0.1 m (1024 triangles), "
+                                f"64^3 tricubic quadrupole, 250 neV walls 5% Lambert 1e-4 loss, tau 880 s")
+                               if args.workload == "field_storage" else
+                               (f"large mesh: {args.n} UCN/GPU, noisy torus R=1 m r=0.1 m + sphere R=0.5 m (200,000 "
+                                f"triangles), 128^3 tricubic multipole, 10% Lambert 3e-5 loss, tau 880 s"),
                    "step": f"one step-batch: every live particle advances {args.batch_steps} accepted RK steps",
                    "form": args.mode, "field_precision": args.precision,
                    "l2": "per-step particle state > L2 (350 B x 1e6); field table L2-resident by design",
@@ -404,6 +422,8 @@ def run_reference(args, rank, world):
 
 def main():
     args = parse()
+    if args.n is None:
+        args.n = 10_000_000 if args.workload == "large_mesh" else 1_000_000
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if world > 1:

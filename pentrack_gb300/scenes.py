@@ -133,6 +133,48 @@ def cylinder_mesh(r, z0, z1, nseg, cx=0.0, cy=0.0):
     return as_stl_precision(np.array(tris, dtype=np.float64))
 
 
+def torus_mesh(R, r, nu, nv, noise=0.0, seed=0):
+    """Closed torus about the z axis (major radius R, tube radius r) on an
+    nu x nv vertex grid, 2 nu nv outward-wound triangles; each vertex moves
+    along its tube normal by noise * r * (2u - 1) with u from the vertex's own
+    Philox draw, so the mesh stays watertight."""
+    iu, iv = np.meshgrid(np.arange(nu), np.arange(nv), indexing="ij")
+    a, b = 2 * np.pi * iu / nu, 2 * np.pi * iv / nv
+    vid = (iu * nv + iv).astype(np.int64).ravel()
+    rr = r * (1.0 + noise * (2.0 * uniform(seed, vid, 0) - 1.0)).reshape(nu, nv)
+    P = np.stack([(R + rr * np.cos(b)) * np.cos(a), (R + rr * np.cos(b)) * np.sin(a), rr * np.sin(b)], -1)
+    tris = []
+    for i in range(nu):
+        i1 = (i + 1) % nu
+        for j in range(nv):
+            j1 = (j + 1) % nv
+            p00, p10, p11, p01 = P[i, j], P[i1, j], P[i1, j1], P[i, j1]
+            tris.append(np.concatenate([p00, p10, p11]))
+            tris.append(np.concatenate([p00, p11, p01]))
+    return as_stl_precision(np.array(tris))
+
+
+def sphere_mesh(R, nlat, nlon, center=(0.0, 0.0, 0.0)):
+    """Closed UV sphere, outward winding: pole fans plus quads split in two
+    (2 nlon (nlat - 1) triangles)."""
+    c = np.asarray(center, dtype=np.float64)
+    th = np.pi * np.arange(1, nlat) / nlat
+    ph = 2 * np.pi * np.arange(nlon) / nlon
+    ring = c + R * np.stack([np.sin(th)[:, None] * np.cos(ph)[None, :], np.sin(th)[:, None] * np.sin(ph)[None, :],
+                             np.cos(th)[:, None] * np.ones(nlon)[None, :]], -1)
+    top, bot = c + np.array([0, 0, R]), c - np.array([0, 0, R])
+    tris = []
+    for j in range(nlon):
+        j1 = (j + 1) % nlon
+        tris.append(np.concatenate([top, ring[0, j], ring[0, j1]]))
+        tris.append(np.concatenate([bot, ring[-1, j1], ring[-1, j]]))
+        for i in range(nlat - 2):
+            a, b, cc, d = ring[i, j], ring[i + 1, j], ring[i + 1, j1], ring[i, j1]
+            tris.append(np.concatenate([a, b, cc]))
+            tris.append(np.concatenate([a, cc, d]))
+    return as_stl_precision(np.array(tris))
+
+
 # ----------------------------------------------------------------------------
 # OPERA3D tables
 def read_opera3d(path, lengthconv=1.0):

@@ -171,3 +171,61 @@ def mixed_species(n_protons=100_000, n_electrons=100_000, seed=1003, tmax=1e-3):
         params = run_params(species, simtime=1.0, tau=0.0, tmax=tmax, lmax=9e99, bmax=0.0, spintimes=(), seed=seed)
         out[species] = (params, parts)
     return sc, out
+
+
+def multipole_table(n=128, lo=(-1.15, -1.15, -0.55), hi=(1.15, 1.15, 0.55), g1=0.43, g2=0.22, b0=0.05):
+    """n^3 grid of the curl- and divergence-free multipole
+    B = (g1 y + 2 g2 x y, g1 x + g2 (x^2 - y^2), b0) = grad(g1 x y + g2 (x^2 y - y^3/3) + b0 z),
+    |B| <= 1 T over the box."""
+    ax = tuple(np.linspace(lo[k], hi[k], n) for k in range(3))
+    X, Y, Z = np.meshgrid(*ax, indexing="ij")
+    return ax, (g1 * Y + 2 * g2 * X * Y, g1 * X + g2 * (X * X - Y * Y), np.full_like(X, b0))
+
+
+def large_mesh_scene(table_n=128, nu=500, nv=160, nlat=101, nlon=200):
+    """Configuration 5's scene: a noise-perturbed torus (R = 1 m, r = 0.1 m,
+    2 nu nv triangles) as the guide and a sphere (R = 0.5 m at the origin,
+    2 nlon (nlat - 1) triangles) as the bottle, both closed vacuum solids in a
+    wall of 10 % diffuse reflection and 3e-5 loss per bounce (200,000
+    triangles by default), with gravity and the multipole table.  The two
+    volumes are separate closed meshes (a seamless fusion would need a mesh
+    boolean the workload generator does not have)."""
+    sc = Scene()
+    sc.add_material("wall", 250.0, 0.0, 0.1, 0.0, 0.0, 0.0, 0.0, 0.0, 3e-5)
+    sc.add_material("vacuum", 0.0)
+    sc.add_solid(1, "wall")
+    sc.add_solid(2, "vacuum", S.torus_mesh(1.0, 0.1, nu, nv, noise=0.05, seed=1005))
+    sc.add_solid(3, "vacuum", S.sphere_mesh(0.5, nlat, nlon))
+    ax, comps = multipole_table(table_n)
+    sc.add_table3d(*ax, *comps)
+    return sc
+
+
+def large_mesh(n=10_000_000, seed=1005, simtime=100.0, table_n=128, scene=None, engine=None, first_id=0):
+    """Configuration 5: UCN with E ~ U[0, 300] neV, isotropic, half of them
+    uniform in the bottle (r < 0.45 m) and half uniform in the guide's tube
+    (within 0.08 m of its centre circle), tau 880 s, 100 s."""
+    sc = scene if scene is not None else large_mesh_scene(table_n)
+    ids = np.arange(first_id, first_id + n, dtype=np.int64)
+    u0, u1, u2 = (S.uniform(seed, ids, S.SOURCE_STREAM + np.uint64(50 + k)) for k in range(3))
+    in_ball = (ids % 2) == 0
+    # ball: radius by the cube root, direction uniform on the sphere
+    rb = 0.45 * np.cbrt(u0)
+    ct = 2 * u1 - 1
+    st = np.sqrt(1 - ct * ct)
+    pb = np.vstack([rb * st * np.cos(2 * np.pi * u2), rb * st * np.sin(2 * np.pi * u2), rb * ct])
+    # tube: position along the ring uniform, uniform disc of radius 0.08 in the cross-section
+    a = 2 * np.pi * u0
+    rd = 0.08 * np.sqrt(u1)
+    b = 2 * np.pi * u2
+    pt = np.vstack([(1.0 + rd * np.cos(b)) * np.cos(a), (1.0 + rd * np.cos(b)) * np.sin(a), rd * np.sin(b)])
+    pos = np.where(in_ball[None, :], pb, pt)
+    E, ph, th, pol = S._kinematics(seed, ids, 0.0, 300e-9, (0.0, S.PI), (0.0, 2 * S.PI), 0.0)
+    bf = None
+    if engine is not None:
+        def bf(p):
+            q = np.column_stack([p, np.zeros(len(p))])
+            return engine.field(q)[0]
+    parts = S.make_particles(seed, ids, pos, E, ph, th, pol, spinprojection=0.0, bfield=bf)
+    params = run_params(A.NEUTRON, simtime=simtime, tau=880.0, tmax=9e99, lmax=9e99, bmax=0.1, spintimes=(0, 0), seed=seed)
+    return sc, params, parts
