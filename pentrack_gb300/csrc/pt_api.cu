@@ -616,7 +616,7 @@ size_t batch_layout(DBatch &b, int64_t n, unsigned char *base) {
     take(b.rng_n, m); take(b.nacc, m); take(b.nrej, m); take(b.ntry, m);
     take(b.yn, 9 * m); take(b.dyn, 9 * m); take(b.kst, 36 * m); take(b.tn, m);
     take(b.bc, 14 * m); take(b.count, 8); take(b.nacc0, m);
-    take(b.ps_d, 42 * m); take(b.ps_i, (7 + PT_MAX_CAND) * m);
+    take(b.ps_d, 45 * m); take(b.ps_i, (7 + PT_MAX_CAND) * m);
     for (int k = 0; k < 5; ++k) take(b.list[k], m);
     return (off + 255) & ~(size_t)255;
 }

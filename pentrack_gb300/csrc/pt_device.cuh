@@ -158,7 +158,7 @@ struct DBatch {
     /* phase-split form: result of the last accepted try and B-value caches */
     double *yn, *dyn, *kst, *tn; /* yn, dyn: 9n; kst: k3..k6, 36n; tn: n */
     double *bc;                  /* 2 slots x (x, y, z, t, Bx, By, Bz): 14n */
-    /* suspended post-steps: 42 doubles and 7 + PT_MAX_CAND ints per particle */
+    /* suspended post-steps: 45 doubles and 7 + PT_MAX_CAND ints per particle */
     double *ps_d;
     int32_t *ps_i;
     /* work lists of particle indices and their counts */

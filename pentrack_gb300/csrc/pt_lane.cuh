@@ -57,6 +57,9 @@ struct Lane {
      * (ncand < 0: not available, use the full BVH query) */
     int cand[PT_MAX_CAND];
     int ncand;
+    /* the candidates serve chords whose end times lie in [cand_ta, cand_tb];
+     * cand_span is the length of the last interval a set was built for */
+    double cand_ta, cand_tb, cand_span;
     PostState ps;
     LaneCounters lc;
 
@@ -65,6 +68,8 @@ struct Lane {
         bc_next = 0;
         ntry = 0;
         ncand = -1;
+        cand_ta = cand_tb = 0;
+        cand_span = INFINITY;
         lc = LaneCounters{};
     }
 
@@ -195,6 +200,7 @@ struct Lane {
         ps.reset = fl & 1; ps.bao = (fl >> 1) & 1; ps.bbo = (fl >> 2) & 1;
         ncand = q[6 * n + i];
         for (int k = 0; k < PT_MAX_CAND; ++k) cand[k] = q[(7 + k) * n + i];
+        cand_ta = d[42 * n + i]; cand_tb = d[43 * n + i]; cand_span = d[44 * n + i];
     }
     __device__ void store_post(const DBatch &b, int64_t i) const {
         const int64_t n = b.n;
@@ -212,6 +218,7 @@ struct Lane {
         q[5 * n + i] = (ps.reset ? 1 : 0) | (ps.bao ? 2 : 0) | (ps.bbo ? 4 : 0);
         q[6 * n + i] = ncand;
         for (int k = 0; k < PT_MAX_CAND; ++k) q[(7 + k) * n + i] = cand[k];
+        d[42 * n + i] = cand_ta; d[43 * n + i] = cand_tb; d[44 * n + i] = cand_span;
     }
     /* what a bisection of a suspended post-step reads: the dense data of the
      * accepted try and the interval (cx1, cya) -> (x2, y2) (positions only)
@@ -239,6 +246,7 @@ struct Lane {
         const int32_t *q = b.ps_i;
         ncand = q[6 * n + i];
         for (int k = 0; k < PT_MAX_CAND; ++k) cand[k] = q[(7 + k) * n + i];
+        cand_ta = d[42 * n + i]; cand_tb = d[43 * n + i]; cand_span = d[44 * n + i];
     }
     __device__ void store_bisect_result(const DBatch &b, int64_t i) const {
         const int64_t n = b.n;
@@ -248,6 +256,10 @@ struct Lane {
         q[4 * n + i] = ps.bres;
         q[5 * n + i] = (q[5 * n + i] & 1) | (ps.bao ? 2 : 0) | (ps.bbo ? 4 : 0);
         q[0 * n + i] = PS_AFTER_BISECT;
+        /* the bisection may have narrowed the candidate set */
+        q[6 * n + i] = ncand;
+        for (int k = 0; k < PT_MAX_CAND; ++k) q[(7 + k) * n + i] = cand[k];
+        b.ps_d[42 * n + i] = cand_ta; b.ps_d[43 * n + i] = cand_tb; b.ps_d[44 * n + i] = cand_span;
     }
     __device__ void store(const DBatch &b, int64_t i) const {
         const int64_t n = b.n;
@@ -641,9 +653,12 @@ struct Lane {
     }
 
     /* ---------------- geometry wrappers ---------------- */
+    __device__ bool cand_cover(double ta, double tb) const { return ncand >= 0 && ta >= cand_ta && tb <= cand_tb; }
     /* any collision on segment p->q; returns -1 on a coplanar (CGAL error) case */
-    __device__ int any_hit(const double *p, const double *q) {
-        if (ncand >= 0) {
+    __device__ int any_hit(const double *p, const double *q) { return any_hit(p, q, NAN, NAN); }
+    /* the same for a chord between the dense-output points at tp and tq */
+    __device__ int any_hit(const double *p, const double *q, double tp, double tq) {
+        if (cand_cover(tp, tq)) {
             bool cp = false;
             Seg32 s32;
             seg32_make(p, q, s32);
@@ -675,7 +690,7 @@ struct Lane {
         return cp ? -1 : 0;
     }
     __device__ int all_hits(double x1, const double *p, double x2, const double *q, Coll *c) {
-        if (ncand >= 0) {
+        if (cand_cover(x1, x2)) {
             int nh = 0;
             for (int j = 0; j < ncand; ++j) {
                 const DTri &t = S.tris[cand[j]];
@@ -762,6 +777,7 @@ struct Lane {
     }
     /* set up the candidate triangles for chord pieces within [ta, tb] */
     __device__ void prepare_candidates(double ta, double tb) {
+        cand_span = tb - ta;
         double lo[3], hi[3];
         curve_box(ta, tb, lo, hi);
         bool ok = true;
@@ -772,7 +788,18 @@ struct Lane {
         lc.nodes += qs.nodes;
         ++lc.cand_calls;
         if (ncand < 0) ++lc.cand_overflow;
-        else lc.cand_sum += ncand;
+        else { lc.cand_sum += ncand; cand_ta = ta; cand_tb = tb; }
+    }
+    /* candidates for [ta, tb] when the current set does not cover it and the
+     * interval is at most a quarter of the last one tried (a set that
+     * overflowed is retried once the search has narrowed) */
+    __device__ void refresh_candidates(double ta, double tb) {
+        if (cand_cover(ta, tb) || !(tb - ta <= 0.25 * cand_span) || ta < to || tb > tn) return;
+        prepare_candidates(ta, tb);
+    }
+    __device__ void reset_candidates() {
+        ncand = -1;
+        cand_span = INFINITY;
     }
 
     /* ---------------- RotateVector (src/globals.cpp:40-64) ---------------- */
@@ -977,6 +1004,7 @@ struct Lane {
                 ++lc.bisect;
                 stA[level] = A;
                 stB[level] = B;
+                refresh_candidates(A, B);
                 xc = A + (B - A) * 0.5;
                 calc_pos(xc, pc);
             } else if (phase == RESUME) {
@@ -1002,7 +1030,7 @@ struct Lane {
                 Q[k] = first ? pc[k] : pB[k];
             }
             if (++work > PT_MAX_BISECT_WORK) { lc.bisect_max = max(lc.bisect_max, (unsigned)work); return -1; }
-            const int h = any_hit(P, Q);
+            const int h = any_hit(P, Q, first ? A : xc, first ? xc : B);
             if (h < 0) { lc.bisect_max = max(lc.bisect_max, (unsigned)work); return -1; }
             if (phase == RESUME) setbit(tr0, tr1, level, true);
             if (h) {
@@ -1248,7 +1276,7 @@ struct Lane {
                 }
                 /* TTracker::CheckHit (src/tracking.cpp:176-226) on (x1, y1) -> (x2, y2);
                  * its tail recursion is the PS_CHECK loop */
-                ncand = -1;
+                reset_candidates();
                 P.cx1 = P.x1;
                 for (int i = 0; i < 9; ++i) P.cya[i] = P.y1[i];
                 P.pass = 0;
@@ -1260,11 +1288,11 @@ struct Lane {
                 P.cs = cur_solid();
                 /* the candidate triangles of the chord's stretch of curve serve
                  * this query and the bisection that follows a hit */
-                if (ncand < 0 && P.cx1 >= to && P.x2 <= tn) prepare_candidates(P.cx1, P.x2);
-                int h = any_hit(P.cya, P.y2);
+                refresh_candidates(P.cx1, P.x2);
+                int h = any_hit(P.cya, P.y2, P.cx1, P.x2);
                 if (h < 0) { stop = PT_ID_CGAL_ERROR; ch = true; P.stage = PS_CHECK_DONE; continue; }
                 if (!h) {
-                    ncand = -1;
+                    reset_candidates();
                     ch = do_step(P.cx1, P.cya, P.x2, P.y2, P.cs);
                     P.stage = PS_CHECK_DONE;
                     continue;
@@ -1299,7 +1327,7 @@ struct Lane {
                 for (int i = 0; i < 9; ++i) P.cya[i] = yc2[i];
                 P.stage = PS_CHECK;
             } else { /* PS_CHECK_DONE: back in the chord-piece loop */
-                ncand = -1;
+                reset_candidates();
                 P.reset = ch;
                 if (P.reset) {
                     P.x = P.x2;
