@@ -806,11 +806,39 @@ __device__ int mesh_query(const DScene &S, const double *p, const double *q, dou
     const int nn = S.n_nodes;
     Seg32 s32;
     seg32_make(p, q, s32);
+    /* Slab test of the segment against a node's box, for segments whose box is
+     * loose (long diagonal chords).  The FP32 segment o + t d, t in [0, 1], is
+     * within eps of the FP64 one everywhere, so boxes are widened by eps with
+     * outward rounding; the t interval is computed as in Ize, "Robust BVH Ray
+     * Traversal" (JCGT 2, 2013), and a node is skipped only when the interval
+     * is empty by more than 1e-6, above the FP32 error of t near [0, 1]. */
+    float so[3], sinv[3];
+    double sm = 0, sd = 0;
+    for (int k = 0; k < 3; ++k) {
+        const double dk = q[k] - p[k];
+        so[k] = (float)p[k];
+        const float d32 = (float)dk;
+        sinv[k] = d32 != 0.0f ? 1.0f / d32 : 0.0f;
+        sm = fmax(sm, fabs(p[k]));
+        sd = fmax(sd, fabs(dk));
+    }
+    const float seps = __double2float_ru(1.2e-7 * (sm + sd) + 1e-30);
+    const bool slab = (MODE != 2) && sd > 2e-3;
     while (i < nn) {
         const DNode nd = S.nodes[i];
         ++qs.nodes;
         bool ov = !(nd.lo[0] > hi[0] || nd.hi[0] < lo[0] || nd.lo[1] > hi[1] || nd.hi[1] < lo[1] || nd.lo[2] > hi[2] ||
                     nd.hi[2] < lo[2]);
+        if (ov && slab) {
+            float t0 = 0.0f, t1 = 1.0f;
+            for (int k = 0; k < 3; ++k) {
+                if (sinv[k] == 0.0f) continue; /* parallel to this slab: the box test above decides */
+                const float a = (__fsub_rd(nd.lo[k], seps) - so[k]) * sinv[k], b = (__fadd_ru(nd.hi[k], seps) - so[k]) * sinv[k];
+                t0 = fmaxf(t0, fminf(a, b));
+                t1 = fminf(t1, fmaxf(a, b));
+            }
+            ov = !(t0 > t1 + 1e-6f); /* both ends lie in [0, 1] when close: an absolute slack above 2 gamma_3 */
+        }
         if (!ov) { i = nd.skip; continue; }
         if (nd.leaf < 0) { ++i; continue; }
         int first = nd.leaf >> 3, cnt = nd.leaf & 7;
