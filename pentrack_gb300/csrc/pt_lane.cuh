@@ -78,69 +78,69 @@ struct Lane {
     /* ---------------- persistence ---------------- */
     __device__ void load(const DBatch &b, int64_t i) {
         const int64_t n = b.n;
-        id = b.id[i];
-        t = b.t[i];
-        for (int c = 0; c < 9; ++c) { y[c] = b.y[c * n + i]; dydt[c] = b.dydt[c * n + i]; }
-        dt = b.dt[i];
-        flags = b.flags[i];
-        for (int c = 0; c < 5; ++c) spin[c] = b.spin[c * n + i];
-        tau = b.tau[i]; hmax = b.hmax[i]; noflip = b.noflip[i];
-        stop = b.stop_id[i]; nhit = b.nhit[i]; nstep = b.nstep[i]; nspinflip = b.nspinflip[i]; nsol = b.nsol[i];
-        uint64_t st = b.stack[i];
+        id = __ldcs(&b.id[i]);
+        t = __ldcs(&b.t[i]);
+        for (int c = 0; c < 9; ++c) { y[c] = __ldcs(&b.y[c * n + i]); dydt[c] = __ldcs(&b.dydt[c * n + i]); }
+        dt = __ldcs(&b.dt[i]);
+        flags = __ldcs(&b.flags[i]);
+        for (int c = 0; c < 5; ++c) spin[c] = __ldcs(&b.spin[c * n + i]);
+        tau = __ldcs(&b.tau[i]); hmax = __ldcs(&b.hmax[i]); noflip = __ldcs(&b.noflip[i]);
+        stop = __ldcs(&b.stop_id[i]); nhit = __ldcs(&b.nhit[i]); nstep = __ldcs(&b.nstep[i]); nspinflip = __ldcs(&b.nspinflip[i]); nsol = __ldcs(&b.nsol[i]);
+        uint64_t st = __ldcs(&b.stack[i]);
         for (int k = 0; k < PT_MAX_STACK; ++k) {
             uint8_t v = (uint8_t)(st >> (8 * k));
             sidx[k] = v & 63;
             sign[k] = (v >> 7) & 1;
         }
-        rn = b.rng_n[i];
-        nacc = b.nacc[i]; nrej = b.nrej[i];
-        ntry = b.ntry[i];
+        rn = __ldcs(&b.rng_n[i]);
+        nacc = __ldcs(&b.nacc[i]); nrej = __ldcs(&b.nrej[i]);
+        ntry = __ldcs(&b.ntry[i]);
     }
     /* the committed step state only (what one RK try needs) */
     __device__ void load_try_input(const DBatch &b, int64_t i) {
         const int64_t n = b.n;
-        t = b.t[i];
-        for (int c = 0; c < 9; ++c) { y[c] = b.y[c * n + i]; dydt[c] = b.dydt[c * n + i]; }
-        dt = b.dt[i];
-        ntry = b.ntry[i];
-        nacc = b.nacc[i]; nrej = b.nrej[i];
+        t = __ldcs(&b.t[i]);
+        for (int c = 0; c < 9; ++c) { y[c] = __ldcs(&b.y[c * n + i]); dydt[c] = __ldcs(&b.dydt[c * n + i]); }
+        dt = __ldcs(&b.dt[i]);
+        ntry = __ldcs(&b.ntry[i]);
+        nacc = __ldcs(&b.nacc[i]); nrej = __ldcs(&b.nrej[i]);
     }
     __device__ void store_try_output(const DBatch &b, int64_t i, bool accepted) const {
         const int64_t n = b.n;
-        b.dt[i] = dt;
-        b.ntry[i] = ntry;
-        b.nacc[i] = nacc; b.nrej[i] = nrej;
+        __stcs(&b.dt[i], dt);
+        __stcs(&b.ntry[i], ntry);
+        __stcs(&b.nacc[i], nacc); __stcs(&b.nrej[i], nrej);
         if (accepted) {
-            for (int c = 0; c < 9; ++c) { b.yn[c * n + i] = yn[c]; b.dyn[c * n + i] = dyn[c]; }
+            for (int c = 0; c < 9; ++c) { __stcs(&b.yn[c * n + i], yn[c]); __stcs(&b.dyn[c * n + i], dyn[c]); }
             for (int c = 0; c < 9; ++c) {
-                b.kst[(0 * 9 + c) * n + i] = k3[c];
-                b.kst[(1 * 9 + c) * n + i] = k4[c];
-                b.kst[(2 * 9 + c) * n + i] = k5[c];
-                b.kst[(3 * 9 + c) * n + i] = k6[c];
+                __stcs(&b.kst[(0 * 9 + c) * n + i], k3[c]);
+                __stcs(&b.kst[(1 * 9 + c) * n + i], k4[c]);
+                __stcs(&b.kst[(2 * 9 + c) * n + i], k5[c]);
+                __stcs(&b.kst[(3 * 9 + c) * n + i], k6[c]);
             }
-            b.tn[i] = tn;
+            __stcs(&b.tn[i], tn);
         }
     }
     /* dense data of the accepted try (start = committed state) */
     __device__ void load_dense(const DBatch &b, int64_t i) {
         const int64_t n = b.n;
         to = t;
-        for (int c = 0; c < 9; ++c) { xo[c] = y[c]; dxo[c] = dydt[c]; yn[c] = b.yn[c * n + i]; dyn[c] = b.dyn[c * n + i]; }
+        for (int c = 0; c < 9; ++c) { xo[c] = y[c]; dxo[c] = dydt[c]; yn[c] = __ldcs(&b.yn[c * n + i]); dyn[c] = __ldcs(&b.dyn[c * n + i]); }
         for (int c = 0; c < 9; ++c) {
-            k3[c] = b.kst[(0 * 9 + c) * n + i];
-            k4[c] = b.kst[(1 * 9 + c) * n + i];
-            k5[c] = b.kst[(2 * 9 + c) * n + i];
-            k6[c] = b.kst[(3 * 9 + c) * n + i];
+            k3[c] = __ldcs(&b.kst[(0 * 9 + c) * n + i]);
+            k4[c] = __ldcs(&b.kst[(1 * 9 + c) * n + i]);
+            k5[c] = __ldcs(&b.kst[(2 * 9 + c) * n + i]);
+            k6[c] = __ldcs(&b.kst[(3 * 9 + c) * n + i]);
         }
-        tn = b.tn[i];
+        tn = __ldcs(&b.tn[i]);
     }
     /* what the fast completion reads of the accepted try: its end point and
      * end derivative (no stage vectors: it never evaluates the dense output) */
     __device__ void load_try_end(const DBatch &b, int64_t i) {
         const int64_t n = b.n;
         to = t;
-        for (int c = 0; c < 9; ++c) { xo[c] = y[c]; dxo[c] = dydt[c]; yn[c] = b.yn[c * n + i]; dyn[c] = b.dyn[c * n + i]; }
-        tn = b.tn[i];
+        for (int c = 0; c < 9; ++c) { xo[c] = y[c]; dxo[c] = dydt[c]; yn[c] = __ldcs(&b.yn[c * n + i]); dyn[c] = __ldcs(&b.dyn[c * n + i]); }
+        tn = __ldcs(&b.tn[i]);
     }
     /* global B caches: slot 0 holds B at the committed point (t, y), slot 1 B
      * at the end point of the last accepted try (tn, yn) */
@@ -149,8 +149,8 @@ struct Lane {
         bc_ok[0] = (flags & PT_F_BC0) != 0;
         bc_ok[1] = (flags & PT_F_BC1) != 0;
         for (int k = 0; k < 2; ++k) {
-            for (int c = 0; c < 4; ++c) bc_p[k][c] = b.bc[(k * 7 + c) * n + i];
-            for (int c = 0; c < 3; ++c) bc_B[k][c] = b.bc[(k * 7 + 4 + c) * n + i];
+            for (int c = 0; c < 4; ++c) bc_p[k][c] = __ldcs(&b.bc[(k * 7 + c) * n + i]);
+            for (int c = 0; c < 3; ++c) bc_B[k][c] = __ldcs(&b.bc[(k * 7 + 4 + c) * n + i]);
         }
         bc_next = 0;
     }
@@ -161,8 +161,8 @@ struct Lane {
     }
     __device__ void bc_write(const DBatch &b, int64_t i, int slot, int k) const {
         const int64_t n = b.n;
-        for (int c = 0; c < 4; ++c) b.bc[(slot * 7 + c) * n + i] = bc_p[k][c];
-        for (int c = 0; c < 3; ++c) b.bc[(slot * 7 + 4 + c) * n + i] = bc_B[k][c];
+        for (int c = 0; c < 4; ++c) __stcs(&b.bc[(slot * 7 + c) * n + i], bc_p[k][c]);
+        for (int c = 0; c < 3; ++c) __stcs(&b.bc[(slot * 7 + 4 + c) * n + i], bc_B[k][c]);
     }
     /* after a commit: keep B at the new committed point (flags stored by store()) */
     __device__ void store_bc_commit(const DBatch &b, int64_t i) {
@@ -263,19 +263,19 @@ struct Lane {
     }
     __device__ void store(const DBatch &b, int64_t i) const {
         const int64_t n = b.n;
-        b.t[i] = t;
-        for (int c = 0; c < 9; ++c) { b.y[c * n + i] = y[c]; b.dydt[c * n + i] = dydt[c]; }
-        b.dt[i] = dt;
-        b.flags[i] = flags;
-        for (int c = 0; c < 5; ++c) b.spin[c * n + i] = spin[c];
-        b.tau[i] = tau; b.hmax[i] = hmax; b.noflip[i] = noflip;
-        b.stop_id[i] = stop; b.nhit[i] = nhit; b.nstep[i] = nstep; b.nspinflip[i] = nspinflip; b.nsol[i] = nsol;
+        __stcs(&b.t[i], t);
+        for (int c = 0; c < 9; ++c) { __stcs(&b.y[c * n + i], y[c]); __stcs(&b.dydt[c * n + i], dydt[c]); }
+        __stcs(&b.dt[i], dt);
+        __stcs(&b.flags[i], flags);
+        for (int c = 0; c < 5; ++c) __stcs(&b.spin[c * n + i], spin[c]);
+        __stcs(&b.tau[i], tau); __stcs(&b.hmax[i], hmax); __stcs(&b.noflip[i], noflip);
+        __stcs(&b.stop_id[i], stop); __stcs(&b.nhit[i], nhit); __stcs(&b.nstep[i], nstep); __stcs(&b.nspinflip[i], nspinflip); __stcs(&b.nsol[i], nsol);
         uint64_t st = 0;
         for (int k = 0; k < PT_MAX_STACK; ++k) st |= (uint64_t)(sidx[k] | (sign[k] ? 128 : 0)) << (8 * k);
-        b.stack[i] = st;
-        b.rng_n[i] = rn;
-        b.nacc[i] = nacc; b.nrej[i] = nrej;
-        b.ntry[i] = ntry;
+        __stcs(&b.stack[i], st);
+        __stcs(&b.rng_n[i], rn);
+        __stcs(&b.nacc[i], nacc); __stcs(&b.nrej[i], nrej);
+        __stcs(&b.ntry[i], ntry);
     }
 
     /* ---------------- fields and equation of motion ---------------- */
