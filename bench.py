@@ -359,7 +359,7 @@ def run_ours(args, rank, world):
                    "form": args.mode, "field_precision": args.precision,
                    "l2": "per-step particle state > L2 (350 B x 1e6); field table L2-resident by design",
                    "parallelism": f"replicas x{world}", "lab_time_per_step_s": span_step},
-        "gpu_launches": int(agg["launches"]),
+        "gpu_launches": int(agg["launches"] + agg["aux_launches"]),
         "wall_s": elapsed,
         "clocks": clk,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",

@@ -210,6 +210,7 @@ typedef struct pt_stats {
     int64_t bisect_dead;       /* bisection intervals abandoned because neither half collides */
     int64_t spin_steps;        /* accepted steps of the spin (Bloch) integration */
     double tail_ms;            /* batched form: device time of the plain-form tail launches */
+    int64_t aux_launches;      /* bookkeeping kernel launches (work-list gathers, list-count resets) */
 } pt_stats;
 
 typedef struct pt_ctx pt_ctx;

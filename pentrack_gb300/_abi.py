@@ -91,7 +91,7 @@ class Stats(C.Structure):
         ("try_ms", C.c_double), ("post_ms", C.c_double), ("slow_ms", C.c_double),
         ("bisect_max", C.c_int64),
         ("cand_calls", C.c_int64), ("cand_overflow", C.c_int64), ("cand_sum", C.c_int64), ("tri32_tests", C.c_int64),
-        ("bisect_ms", C.c_double), ("bisect_dead", C.c_int64), ("spin_steps", C.c_int64), ("tail_ms", C.c_double),
+        ("bisect_ms", C.c_double), ("bisect_dead", C.c_int64), ("spin_steps", C.c_int64), ("tail_ms", C.c_double), ("aux_launches", C.c_int64),
     ]
 
     def as_dict(self):

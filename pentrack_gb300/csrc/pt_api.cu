@@ -430,6 +430,7 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
     if ((e = cudaMemsetAsync(b.count, 0, 8 * sizeof(int32_t), c->stream))) return ck(c, e, "counts"), PT_ERR_CUDA;
     k_gather<<<grid_for(n, 256), 256, 0, c->stream>>>(b, R.t_pause, b.list[0], &b.count[0]);
     if ((e = cudaGetLastError())) return ck(c, e, "gather"), PT_ERR_CUDA;
+    acc.aux_launches += 1;
     cudaEvent_t ev[6];
     for (int k = 0; k < 6; ++k) cudaEventCreate(&ev[k]);
     double t_try = 0, t_post = 0, t_slow = 0, t_bisect = 0;
@@ -451,7 +452,13 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
     for (int it = 0;; ++it) {
         const int in = it & 1, out = in ^ 1;
         if ((e = cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream))) { st = ck(c, e, "memset"), PT_ERR_CUDA; break; }
+        if (it > 0) {
+            k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, in, in, in);
+            k_regather<<<grid_for(n, 256), 256, 0, c->stream>>>(b, R.t_pause, R.max_steps, b.list[in], &b.count[in]);
+            acc.aux_launches += 2;
+        }
         k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, out, 2, 2);
+        acc.aux_launches += 1;
         cudaEventRecord(ev[0], c->stream);
         k_try<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, in, out);
         cudaEventRecord(ev[1], c->stream);
@@ -478,6 +485,7 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
             k_bisect<<<g_bisect, block, 0, c->stream>>>(c->scene, R, b, c->counters);
             cudaEventRecord(ev[5], c->stream);
             k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 4, 4, 4);
+            acc.aux_launches += 2;
             if ((e = cudaGetLastError())) { st = ck(c, e, "k_slow launch"), PT_ERR_CUDA; break; }
             cudaMemcpyAsync(hcount, b.count, 8 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
             if ((e = cudaStreamSynchronize(c->stream))) { st = ck(c, e, "k_slow"), PT_ERR_CUDA; break; }

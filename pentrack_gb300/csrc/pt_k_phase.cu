@@ -16,6 +16,21 @@ __global__ void k_gather(const __grid_constant__ DBatch b, double t_pause, int32
     else if (b.t[i] < t_pause) list_push(list, count, (int32_t)i);
 }
 
+/* The next iteration's active list rebuilt from the particle states: the same
+ * set the previous iteration appended (not stopped, no post-step pending,
+ * before t_pause, within the step budget), but every warp appends its active
+ * particles among 32 consecutive ones in index order.  The lanes of a warp in
+ * k_try then read and write neighbouring entries of the state arrays, where
+ * the appends of the previous iteration had scattered them over separate
+ * memory sectors. */
+__global__ void k_regather(const __grid_constant__ DBatch b, double t_pause, int max_steps, int32_t *list, int32_t *count) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.n) return;
+    if (b.stop_id[i] != PT_ID_UNKNOWN || (b.flags[i] & PT_F_PENDING) || !(b.t[i] < t_pause)) return;
+    if (max_steps > 0 && b.nacc[i] - b.nacc0[i] >= max_steps) return;
+    list_push(list, count, (int32_t)i);
+}
+
 __global__ void k_zero_counts(int32_t *count, int a, int b, int c) {
     if (threadIdx.x == 0) { count[a] = 0; count[b] = 0; count[c] = 0; }
 }

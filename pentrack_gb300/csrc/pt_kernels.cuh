@@ -9,6 +9,7 @@ namespace ptk {
 
 __global__ void k_init(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C);
 __global__ void k_gather(const __grid_constant__ DBatch b, double t_pause, int32_t *list, int32_t *count);
+__global__ void k_regather(const __grid_constant__ DBatch b, double t_pause, int max_steps, int32_t *list, int32_t *count);
 __global__ void k_zero_counts(int32_t *count, int a, int b, int c);
 __global__ void k_try(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out);
 __global__ void k_post(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out);

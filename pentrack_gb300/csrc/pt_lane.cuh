@@ -159,10 +159,14 @@ struct Lane {
             if (bc_ok[k] && bc_p[k][0] == x && bc_p[k][1] == yy && bc_p[k][2] == z && bc_p[k][3] == tt) return k;
         return -1;
     }
-    __device__ void bc_write(const DBatch &b, int64_t i, int slot, int k) const {
+    template <int K> __device__ void bc_write_from(const DBatch &b, int64_t i, int slot) const {
         const int64_t n = b.n;
-        for (int c = 0; c < 4; ++c) __stcs(&b.bc[(slot * 7 + c) * n + i], bc_p[k][c]);
-        for (int c = 0; c < 3; ++c) __stcs(&b.bc[(slot * 7 + 4 + c) * n + i], bc_B[k][c]);
+        for (int c = 0; c < 4; ++c) __stcs(&b.bc[(slot * 7 + c) * n + i], bc_p[K][c]);
+        for (int c = 0; c < 3; ++c) __stcs(&b.bc[(slot * 7 + 4 + c) * n + i], bc_B[K][c]);
+    }
+    __device__ void bc_write(const DBatch &b, int64_t i, int slot, int k) const {
+        if (k == 0) bc_write_from<0>(b, i, slot);
+        else bc_write_from<1>(b, i, slot);
     }
     /* after a commit: keep B at the new committed point (flags stored by store()) */
     __device__ void store_bc_commit(const DBatch &b, int64_t i) {
@@ -279,12 +283,16 @@ struct Lane {
     }
 
     /* ---------------- fields and equation of motion ---------------- */
+    /* the slot index is a template constant so that the caches stay in registers */
+    template <int K> __device__ void bc_set(double x, double yy, double z, double tt, const double B[3]) {
+        bc_p[K][0] = x; bc_p[K][1] = yy; bc_p[K][2] = z; bc_p[K][3] = tt;
+        bc_B[K][0] = B[0]; bc_B[K][1] = B[1]; bc_B[K][2] = B[2];
+        bc_ok[K] = true;
+    }
     __device__ void bc_put(double x, double yy, double z, double tt, const double B[3]) {
-        int k = bc_next;
+        if (bc_next == 0) bc_set<0>(x, yy, z, tt, B);
+        else bc_set<1>(x, yy, z, tt, B);
         bc_next ^= 1;
-        bc_p[k][0] = x; bc_p[k][1] = yy; bc_p[k][2] = z; bc_p[k][3] = tt;
-        bc_B[k][0] = B[0]; bc_B[k][1] = B[1]; bc_B[k][2] = B[2];
-        bc_ok[k] = true;
     }
     __device__ void bonly(double x, double yy, double z, double tt, double B[3]) {
         for (int k = 0; k < 2; ++k)

@@ -358,39 +358,32 @@ __device__ void hermite_cell(const T *__restrict__ nodes, int ncomp, int c0, int
     }
 }
 
-/* Mixed-precision cell evaluation (PT_PREC_FP32).  Within a cell the field is
- * split exactly into a linear base L(x) = f0 + g.(x - x0) (f0: value at the
- * cell's first corner, g: mean corner gradient), evaluated in FP64, and the
- * remainder f - L, whose corner Hermite data were formed in FP64 on the host
- * and stored in FP32; its tricubic is evaluated in FP32.  The remainder is
- * O(h^2 f'') small (zero for a linear field), so the FP32 rounding stays
- * ~1e-7 of a small quantity and the force is smooth to the 1e-9 step-size
- * controller. */
-template <bool GRAD>
-__device__ void tab3_f32(const DField &f, int c0, int nc, float x, float y, float z, float *F, float (*dF)[3]) {
+/* Cell lookup on one axis of the FP32 node table: the cell index and the
+ * local coordinate, false outside the grid. */
+__device__ __forceinline__ bool locate32(const DField &f, int a, float r, int &idx, float &loc) {
+    const float *ax = f.ax32[a];
+    const int n = f.n[a];
+    const float g = (r - f.a0f[a]) * f.inv_hf[a];
+    int k;
+    if (!(g > -1.0f)) k = 0;
+    else if (!(g < (float)n)) k = n;
+    else k = (int)floorf(g) + 1;
+    while (k < n && ax[k] <= r) ++k;
+    while (k > 0 && ax[k - 1] > r) --k;
+    if (k >= n || k == 0) return false;
+    idx = k - 1;
+    loc = (r - ax[k - 1]) * f.inv_w32[a][k - 1];
+    return true;
+}
+
+/* FP32 field mode: tricubic value (+ gradient) of components C0 .. C0+NC-1
+ * from the FP32 node table.  The component range is a template constant so
+ * that the outputs stay in registers. */
+template <bool GRAD, int C0, int NC>
+__device__ void tab3_f32(const DField &f, float x, float y, float z, float *F, float (*dF)[3]) {
     int ix, iy, iz;
     float u, v, w;
-    {
-        const float r[3] = {x, y, z};
-        int idx[3];
-        float loc[3];
-        for (int a = 0; a < 3; ++a) {
-            const float *ax = f.ax32[a];
-            const int n = f.n[a];
-            const float g = (r[a] - f.a0f[a]) * f.inv_hf[a];
-            int k;
-            if (!(g > -1.0f)) k = 0;
-            else if (!(g < (float)n)) k = n;
-            else k = (int)floorf(g) + 1;
-            while (k < n && ax[k] <= r[a]) ++k;
-            while (k > 0 && ax[k - 1] > r[a]) --k;
-            if (k >= n || k == 0) return;
-            idx[a] = k - 1;
-            loc[a] = (r[a] - ax[k - 1]) * f.inv_w32[a][k - 1];
-        }
-        ix = idx[0]; iy = idx[1]; iz = idx[2];
-        u = loc[0]; v = loc[1]; w = loc[2];
-    }
+    if (!locate32(f, 0, x, ix, u) || !locate32(f, 1, y, iy, v) || !locate32(f, 2, z, iz, w)) return;
     Herm<float> U, V, W;
     U.set(u, f.ax32[0][ix + 1] - f.ax32[0][ix], f.inv_w32[0][ix]);
     V.set(v, f.ax32[1][iy + 1] - f.ax32[1][iy], f.inv_w32[1][iy]);
@@ -408,7 +401,8 @@ __device__ void tab3_f32(const DField &f, int c0, int nc, float x, float y, floa
                 hz = f.ax32[2][iz + 1] - f.ax32[2][iz];
     const float rx = x - f.ax32[0][ix], ry = y - f.ax32[1][iy], rz = z - f.ax32[2][iz];
     const int dtab[2][2][2] = {{{0, 3}, {2, 6}}, {{1, 5}, {4, 7}}};
-    for (int c = c0; c < c0 + nc; ++c) {
+#pragma unroll
+    for (int c = C0; c < C0 + NC; ++c) {
         const float h0 = T0[c * 9], l0 = T0[c * 9 + 1];
         const float g[3] = {T0[c * 9 + 2], T0[c * 9 + 3], T0[c * 9 + 4]};
         float fr = 0, fx = 0, fy = 0, fz = 0;
@@ -461,11 +455,11 @@ __device__ void tab3_f32(const DField &f, int c0, int nc, float x, float y, floa
                     fz = fmaf(tzp, U.w[p], fz);
                 }
             }
-        F[c - c0] = h0 + (l0 + (fmaf(g[2], rz, fmaf(g[1], ry, g[0] * rx)) + fr));
+        F[c - C0] = h0 + (l0 + (fmaf(g[2], rz, fmaf(g[1], ry, g[0] * rx)) + fr));
         if (GRAD) {
-            dF[c - c0][0] = g[0] + fx;
-            dF[c - c0][1] = g[1] + fy;
-            dF[c - c0][2] = g[2] + fz;
+            dF[c - C0][0] = g[0] + fx;
+            dF[c - C0][1] = g[1] + fy;
+            dF[c - C0][2] = g[2] + fz;
         }
     }
 }
@@ -490,7 +484,7 @@ __device__ void tab3_v(const DField &f, int prec, double x, double y, double z, 
     double F[1] = {Vv}, dF[1][3] = {{0, 0, 0}};
     if (prec == PT_PREC_FP32 && f.node32) {
         float F32[1] = {(float)Vv}, dF32[1][3] = {{0, 0, 0}};
-        tab3_f32<true>(f, 3, 1, (float)x, (float)y, (float)z, F32, dF32);
+        tab3_f32<true, 3, 1>(f, (float)x, (float)y, (float)z, F32, dF32);
         F[0] = F32[0];
         for (int k = 0; k < 3; ++k) dF[0][k] = dF32[0][k];
     } else {
@@ -584,7 +578,7 @@ __device__ void bfield32(const DScene &S, double x, double y, double z, float B[
         if (!fbox_in(f, x, y, z) || f.bscale == 0.) continue;
         float Bt[3] = {0, 0, 0}, dBt[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
         if (f.type == PT_FIELD_TAB3D && f.node32 && !(f.bw > 0 && fbox_has(f))) {
-            tab3_f32<GRAD>(f, 0, 3, (float)x, (float)y, (float)z, Bt, dBt);
+            tab3_f32<GRAD, 0, 3>(f, (float)x, (float)y, (float)z, Bt, dBt);
             if (f.bscale != 1.0) {
                 const float sc = (float)f.bscale;
                 for (int i = 0; i < 3; ++i) {
