@@ -481,7 +481,7 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
             cudaEventRecord(ev[3], c->stream);
             k_slow<<<g_slow, block, 0, c->stream>>>(c->scene, R, b, c->counters, out);
             cudaEventRecord(ev[4], c->stream);
-            k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 3, 3, 3);
+            k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 3, 5, 5);
             k_bisect<<<g_bisect, block, 0, c->stream>>>(c->scene, R, b, c->counters);
             cudaEventRecord(ev[5], c->stream);
             k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 4, 4, 4);

@@ -39,18 +39,33 @@ __global__ void __launch_bounds__(128) k_slow(const __grid_constant__ DScene S, 
 }
 
 /* Batched form, phase 4: the bisections (TTracker::iterate_collision) that
- * suspended post-steps asked for; every lane runs the same search loop.  The
- * post-steps go back to the slow list. */
+ * suspended post-steps asked for.  Every loop iteration runs one step (one
+ * chord query) of the lane's current bisection; a lane whose bisection ends
+ * stores the result and takes the next request from the list, so the lanes of
+ * a warp stay on the same code while bisections of very different lengths
+ * run.  The post-steps go back to the slow list.  count[5] (zero at launch) is
+ * the take cursor of the request list. */
 __global__ void __launch_bounds__(128, 4) k_bisect(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C) {
     const int n = b.count[4];
     const int32_t *lq = b.list[4];
     Lane L(S, R);
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const int i = lq[k];
-        L.load_bisect_request(b, i);
-        L.ps.bres = L.bisect(L.ps.cx1, L.ps.cya, L.ps.x2, L.ps.y2, L.ps.bxa, L.ps.bao, L.ps.bxb, L.ps.bbo);
-        L.store_bisect_result(b, i);
-        list_push(b.list[3], &b.count[3], i);
+    BisectState bs;
+    int i = -1;
+    for (;;) {
+        if (i < 0) {
+            const int k = atomicAdd(&b.count[5], 1);
+            if (k >= n) break;
+            i = lq[k];
+            L.load_bisect_request(b, i);
+            L.bisect_begin(bs, L.ps.cx1, L.ps.cya, L.ps.x2, L.ps.y2);
+        }
+        const int r = L.bisect_step(bs, L.ps.bxa, L.ps.bao, L.ps.bxb, L.ps.bbo);
+        if (r != BISECT_RUNNING) {
+            L.ps.bres = r;
+            L.store_bisect_result(b, i);
+            list_push(b.list[3], &b.count[3], i);
+            i = -1;
+        }
     }
     flush_counters(C, L.lc, 0.0, false);
 }

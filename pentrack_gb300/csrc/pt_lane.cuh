@@ -31,6 +31,21 @@ struct PostState {
 };
 enum { PS_BEGIN = 0, PS_OUTER = 1, PS_CHECK = 2, PS_AFTER_BISECT = 3, PS_CHECK_DONE = 4 };
 
+/* State of one bisection between its steps: the current interval [A, B] with
+ * its end positions and origin flags, the midpoint, the stack of interval
+ * ends per level, the choice and tried bits per level, the query count and
+ * the phase of the current level (ENTER: first half next, SECOND: second
+ * half next, RESUME: back at a stacked level after a dead end). */
+struct BisectState {
+    enum { ENTER, SECOND, RESUME };
+    double stA[PT_MAX_BISECT_LEVELS + 1], stB[PT_MAX_BISECT_LEVELS + 1];
+    uint64_t ch0, ch1, tr0, tr1;
+    double A, B, pA[3], pB[3], p2[3], xc, pc[3];
+    int level, work, phase;
+    bool Ao, Bo;
+};
+enum { BISECT_RUNNING = 2 };
+
 struct Lane {
     const DScene &S;
     const DRun &R;
@@ -974,100 +989,118 @@ struct Lane {
         return !same;
     }
 
+    /* One bisection as a resumable state machine: bisect_begin sets it up and
+     * each bisect_step runs one iteration of the search (at most one chord
+     * query), so a kernel can interleave the bisections of several particles
+     * on one lane and keep the lanes of a warp on the same iteration. */
+    __device__ void bisect_begin(BisectState &bs, double x1, const double *p1, double x2, const double *p2) const {
+        bs.ch0 = bs.ch1 = bs.tr0 = bs.tr1 = 0;
+        bs.level = 0;
+        bs.A = x1;
+        bs.B = x2;
+        for (int k = 0; k < 3; ++k) {
+            bs.pA[k] = p1[k];
+            bs.pB[k] = p2[k];
+            bs.p2[k] = p2[k];
+            bs.pc[k] = 0;
+        }
+        bs.xc = 0;
+        bs.Ao = bs.Bo = true;
+        bs.work = 0;
+        bs.phase = BisectState::ENTER;
+    }
+    /* BISECT_RUNNING while the search goes on, else bisect()'s result */
+    __device__ int bisect_step(BisectState &bs, double &xa, bool &aorig, double &xb, bool &borig) {
+        auto getbit = [](uint64_t a, uint64_t b, int l) -> bool { return l < 64 ? ((a >> l) & 1) : ((b >> (l - 64)) & 1); };
+        auto setbit = [](uint64_t &a, uint64_t &b, int l, bool v) {
+            if (l < 64) { if (v) a |= (1ull << l); else a &= ~(1ull << l); }
+            else { if (v) b |= (1ull << (l - 64)); else b &= ~(1ull << (l - 64)); }
+        };
+        if (bs.phase == BisectState::ENTER) {
+            /* termination tests at the entry of iterate_collision */
+            double dx = bs.pB[0] - bs.pA[0], dy = bs.pB[1] - bs.pA[1], dz = bs.pB[2] - bs.pA[2];
+            if (dx * dx + dy * dy + dz * dz < PT_REFLECT_TOLERANCE * PT_REFLECT_TOLERANCE ||
+                bs.B - bs.A < 4 * (bs.A + bs.B) * 2.220446049250313e-16 || bs.level >= PT_MAX_BISECT_LEVELS) {
+                xa = bs.A; aorig = bs.Ao; xb = bs.B; borig = bs.Bo;
+                lc.bisect_max = max(lc.bisect_max, (unsigned)bs.work);
+                return 1;
+            }
+            ++lc.bisect;
+            bs.stA[bs.level] = bs.A;
+            bs.stB[bs.level] = bs.B;
+            refresh_candidates(bs.A, bs.B);
+            bs.xc = bs.A + (bs.B - bs.A) * 0.5;
+            calc_pos(bs.xc, bs.pc);
+        } else if (bs.phase == BisectState::RESUME) {
+            /* second half of a stacked level: the start is the input start
+             * iff every choice above took the first half, the end is the
+             * input end iff every choice took the second half */
+            bs.A = bs.stA[bs.level];
+            bs.B = bs.stB[bs.level];
+            bool allsecond = true;
+            for (int l = 0; l < bs.level; ++l) allsecond = allsecond && getbit(bs.ch0, bs.ch1, l);
+            bs.Bo = allsecond;
+            if (bs.Bo) { bs.pB[0] = bs.p2[0]; bs.pB[1] = bs.p2[1]; bs.pB[2] = bs.p2[2]; }
+            else calc_pos(bs.B, bs.pB);
+            bs.xc = bs.A + (bs.B - bs.A) * 0.5;
+            calc_pos(bs.xc, bs.pc);
+        }
+        /* the one chord query of this iteration: first half (A, xc) on
+         * entering a level, else second half (xc, B) */
+        const bool first = (bs.phase == BisectState::ENTER);
+        double P[3], Q[3];
+        for (int k = 0; k < 3; ++k) {
+            P[k] = first ? bs.pA[k] : bs.pc[k];
+            Q[k] = first ? bs.pc[k] : bs.pB[k];
+        }
+        if (++bs.work > PT_MAX_BISECT_WORK) { lc.bisect_max = max(lc.bisect_max, (unsigned)bs.work); return -1; }
+        const int h = any_hit(P, Q, first ? bs.A : bs.xc, first ? bs.xc : bs.B);
+        if (h < 0) { lc.bisect_max = max(lc.bisect_max, (unsigned)bs.work); return -1; }
+        if (bs.phase == BisectState::RESUME) setbit(bs.tr0, bs.tr1, bs.level, true);
+        if (h) {
+            setbit(bs.ch0, bs.ch1, bs.level, !first);
+            if (bs.phase == BisectState::ENTER) setbit(bs.tr0, bs.tr1, bs.level, false);
+            if (bs.phase == BisectState::SECOND) setbit(bs.tr0, bs.tr1, bs.level, true);
+            if (first) { bs.B = bs.xc; bs.pB[0] = bs.pc[0]; bs.pB[1] = bs.pc[1]; bs.pB[2] = bs.pc[2]; bs.Bo = false; }
+            else { bs.A = bs.xc; bs.pA[0] = bs.pc[0]; bs.pA[1] = bs.pc[1]; bs.pA[2] = bs.pc[2]; bs.Ao = false; }
+            ++bs.level;
+            bs.phase = BisectState::ENTER;
+            return BISECT_RUNNING;
+        }
+        if (bs.phase == BisectState::ENTER) { bs.phase = BisectState::SECOND; return BISECT_RUNNING; }
+        /* neither half of this level leads to a collision: a dead end;
+         * back up to the nearest level whose second half is untried */
+        ++lc.dead;
+        bool found = false;
+        while (bs.level > 0) {
+            --bs.level;
+            if (getbit(bs.tr0, bs.tr1, bs.level)) { ++lc.dead; continue; } /* both halves of this level done */
+            found = true;
+            break;
+        }
+        if (!found) {
+            lc.bisect_max = max(lc.bisect_max, (unsigned)bs.work);
+            return 0;
+        }
+        bs.phase = BisectState::RESUME;
+        return BISECT_RUNNING;
+    }
     /* TTracker::iterate_collision (src/tracking.cpp:228-265) without recursion:
      * a depth-first search over halves with an explicit stack of interval
      * times (positions of stacked interval ends are recomputed from the dense
-     * output, which is deterministic).  Every loop iteration makes exactly one
-     * chord query from one call site, so lanes of a warp that bisect at the
+     * output, which is deterministic).  Every step (bisect_step) makes at most one
+     * chord query, from one call site, so lanes of a warp that bisect at the
      * same time stay converged whichever half they are in.  Returns 1 with the
      * final bracket [xa, xb] (aorig/borig: the bracket end is an input end), 0
      * when no sub-chord collides, -1 on a CGAL-error case or when the search
      * exceeds its work bound. */
     __device__ int bisect(double x1, const double *p1, double x2, const double *p2, double &xa, bool &aorig, double &xb,
                           bool &borig) {
-        enum { ENTER, SECOND, RESUME };
-        double stA[PT_MAX_BISECT_LEVELS + 1], stB[PT_MAX_BISECT_LEVELS + 1];
-        uint64_t ch0 = 0, ch1 = 0; /* choice bit per level: 1 = second half */
-        uint64_t tr0 = 0, tr1 = 0; /* second half already tried at this level */
-        int level = 0;
-        double A = x1, B = x2, pA[3] = {p1[0], p1[1], p1[2]}, pB[3] = {p2[0], p2[1], p2[2]};
-        double xc = 0, pc[3] = {0, 0, 0};
-        bool Ao = true, Bo = true;
-        int work = 0, phase = ENTER;
-        auto getbit = [](uint64_t a, uint64_t b, int l) -> bool { return l < 64 ? ((a >> l) & 1) : ((b >> (l - 64)) & 1); };
-        auto setbit = [](uint64_t &a, uint64_t &b, int l, bool v) {
-            if (l < 64) { if (v) a |= (1ull << l); else a &= ~(1ull << l); }
-            else { if (v) b |= (1ull << (l - 64)); else b &= ~(1ull << (l - 64)); }
-        };
-        while (true) {
-            if (phase == ENTER) {
-                /* termination tests at the entry of iterate_collision */
-                double dx = pB[0] - pA[0], dy = pB[1] - pA[1], dz = pB[2] - pA[2];
-                if (dx * dx + dy * dy + dz * dz < PT_REFLECT_TOLERANCE * PT_REFLECT_TOLERANCE ||
-                    B - A < 4 * (A + B) * 2.220446049250313e-16 || level >= PT_MAX_BISECT_LEVELS) {
-                    xa = A; aorig = Ao; xb = B; borig = Bo;
-                    lc.bisect_max = max(lc.bisect_max, (unsigned)work);
-                    return 1;
-                }
-                ++lc.bisect;
-                stA[level] = A;
-                stB[level] = B;
-                refresh_candidates(A, B);
-                xc = A + (B - A) * 0.5;
-                calc_pos(xc, pc);
-            } else if (phase == RESUME) {
-                /* second half of a stacked level: the start is the input start
-                 * iff every choice above took the first half, the end is the
-                 * input end iff every choice took the second half */
-                A = stA[level];
-                B = stB[level];
-                bool allsecond = true;
-                for (int l = 0; l < level; ++l) allsecond = allsecond && getbit(ch0, ch1, l);
-                Bo = allsecond;
-                if (Bo) { pB[0] = p2[0]; pB[1] = p2[1]; pB[2] = p2[2]; }
-                else calc_pos(B, pB);
-                xc = A + (B - A) * 0.5;
-                calc_pos(xc, pc);
-            }
-            /* the one chord query of this iteration: first half (A, xc) on
-             * entering a level, else second half (xc, B) */
-            const bool first = (phase == ENTER);
-            double P[3], Q[3];
-            for (int k = 0; k < 3; ++k) {
-                P[k] = first ? pA[k] : pc[k];
-                Q[k] = first ? pc[k] : pB[k];
-            }
-            if (++work > PT_MAX_BISECT_WORK) { lc.bisect_max = max(lc.bisect_max, (unsigned)work); return -1; }
-            const int h = any_hit(P, Q, first ? A : xc, first ? xc : B);
-            if (h < 0) { lc.bisect_max = max(lc.bisect_max, (unsigned)work); return -1; }
-            if (phase == RESUME) setbit(tr0, tr1, level, true);
-            if (h) {
-                setbit(ch0, ch1, level, !first);
-                if (phase == ENTER) setbit(tr0, tr1, level, false);
-                if (phase == SECOND) setbit(tr0, tr1, level, true);
-                if (first) { B = xc; pB[0] = pc[0]; pB[1] = pc[1]; pB[2] = pc[2]; Bo = false; }
-                else { A = xc; pA[0] = pc[0]; pA[1] = pc[1]; pA[2] = pc[2]; Ao = false; }
-                ++level;
-                phase = ENTER;
-                continue;
-            }
-            if (phase == ENTER) { phase = SECOND; continue; }
-            /* neither half of this level leads to a collision: a dead end;
-             * back up to the nearest level whose second half is untried */
-            ++lc.dead;
-            bool found = false;
-            while (level > 0) {
-                --level;
-                if (getbit(tr0, tr1, level)) { ++lc.dead; continue; } /* both halves of this level done */
-                found = true;
-                break;
-            }
-            if (!found) {
-                lc.bisect_max = max(lc.bisect_max, (unsigned)work);
-                return 0;
-            }
-            phase = RESUME;
-        }
+        BisectState bs;
+        bisect_begin(bs, x1, p1, x2, p2);
+        int r;
+        while ((r = bisect_step(bs, xa, aorig, xb, borig)) == BISECT_RUNNING) {}
+        return r;
     }
 
     /* TTracker::DoHit (src/tracking.cpp:280-365) */
