@@ -369,9 +369,9 @@ void add_counters(pt_stats &acc, const DCounters &k) {
     acc.cand_calls += k.cand_calls; acc.cand_overflow += k.cand_overflow; acc.cand_sum += k.cand_sum; acc.tri32_tests += k.tri32; acc.bisect_dead += k.bisect_dead; acc.spin_steps += k.spin_steps;
 }
 
-int persistent_grid(pt_ctx *c, const void *fn, int block) {
+int persistent_grid(pt_ctx *c, const void *fn, int block, size_t smem = 0) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, smem);
     if (per_sm < 1) per_sm = 1;
     return per_sm * c->sm_count;
 }
@@ -423,7 +423,17 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
     DBatch &b = B->b;
     const int64_t n = b.n;
     const int block = 128;
-    const int g_try = persistent_grid(c, (const void *)k_try, block);
+    /* k_try without the general right-hand side when every magnetic field is
+     * an FP32 table and the species is neutral in the FP32 field mode (the
+     * same branch bfield32 takes per field) */
+    bool tab_only = R.sp.q == 0 && R.prec == PT_PREC_FP32;
+    for (int fi = 0; fi < c->scene.n_fields; ++fi) {
+        const DField &f = c->scene.fields[fi];
+        const bool box = f.xmin < f.xmax && f.ymin < f.ymax && f.zmin < f.zmax;
+        if (f.has_b && !(f.type == PT_FIELD_TAB3D && f.node32 && !(f.bw > 0 && box))) tab_only = false;
+    }
+    const void *try_fn = tab_only ? (const void *)k_try_tab32 : (const void *)k_try;
+    const int g_try = persistent_grid(c, try_fn, block);
     const int g_post = persistent_grid(c, (const void *)k_post, block);
     const int g_slow = persistent_grid(c, (const void *)k_slow, block);
     const int g_bisect = persistent_grid(c, (const void *)k_bisect, block);
@@ -451,7 +461,7 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
     bool to_plain = false;
     for (int it = 0;; ++it) {
         const int in = it & 1, out = in ^ 1;
-        if ((e = cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream))) { st = ck(c, e, "memset"), PT_ERR_CUDA; break; }
+        if ((e = cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream))) { ck(c, e, "memset"); st = PT_ERR_CUDA; break; }
         if (it > 0) {
             k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, in, in, in);
             k_regather<<<grid_for(n, 256), 256, 0, c->stream>>>(b, R.t_pause, R.max_steps, b.list[in], &b.count[in]);
@@ -460,13 +470,14 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
         k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, out, 2, 2);
         acc.aux_launches += 1;
         cudaEventRecord(ev[0], c->stream);
-        k_try<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, in, out);
+        if (tab_only) k_try_tab32<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, in, out);
+        else k_try<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, in, out);
         cudaEventRecord(ev[1], c->stream);
         k_post<<<g_post, block, 0, c->stream>>>(c->scene, R, b, c->counters, out);
         cudaEventRecord(ev[2], c->stream);
-        if ((e = cudaGetLastError())) { st = ck(c, e, "batched launch"), PT_ERR_CUDA; break; }
+        if ((e = cudaGetLastError())) { ck(c, e, "batched launch"); st = PT_ERR_CUDA; break; }
         cudaMemcpyAsync(hcount, b.count, 8 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
-        if ((e = cudaStreamSynchronize(c->stream))) { st = ck(c, e, "batched iteration"), PT_ERR_CUDA; break; }
+        if ((e = cudaStreamSynchronize(c->stream))) { ck(c, e, "batched iteration"); st = PT_ERR_CUDA; break; }
         float a = 0, bb = 0;
         cudaEventElapsedTime(&a, ev[0], ev[1]);
         cudaEventElapsedTime(&bb, ev[1], ev[2]);
@@ -486,9 +497,9 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
             cudaEventRecord(ev[5], c->stream);
             k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 4, 4, 4);
             acc.aux_launches += 2;
-            if ((e = cudaGetLastError())) { st = ck(c, e, "k_slow launch"), PT_ERR_CUDA; break; }
+            if ((e = cudaGetLastError())) { ck(c, e, "k_slow launch"); st = PT_ERR_CUDA; break; }
             cudaMemcpyAsync(hcount, b.count, 8 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
-            if ((e = cudaStreamSynchronize(c->stream))) { st = ck(c, e, "k_slow"), PT_ERR_CUDA; break; }
+            if ((e = cudaStreamSynchronize(c->stream))) { ck(c, e, "k_slow"); st = PT_ERR_CUDA; break; }
             float cc = 0, cb = 0;
             cudaEventElapsedTime(&cc, ev[3], ev[4]);
             cudaEventElapsedTime(&cb, ev[4], ev[5]);
@@ -520,7 +531,7 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
         st = advance_plain(c, B, R, acc, w0, cancelled, timed_out, true);
         acc.tail_ms = acc.kernel_ms - k0;
     }
-    const char *name = "k_try";
+    const char *name = tab_only ? "k_try_tab32" : "k_try";
     double dom = t_try;
     if (t_post > dom) { dom = t_post; name = "k_post"; }
     if (t_slow > dom) { dom = t_slow; name = "k_slow"; }

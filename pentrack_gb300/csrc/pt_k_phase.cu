@@ -36,16 +36,22 @@ __global__ void k_zero_counts(int32_t *count, int a, int b, int c) {
 }
 
 /* Batched form, phase 1: exactly one Dormand-Prince try for every active
- * particle (all lanes execute the same instruction stream). */
-__global__ void __launch_bounds__(128, 3) k_try(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out) {
+ * particle (all lanes execute the same instruction stream).  k_try_tab32 is
+ * the instance with the FP32-table-only right-hand side (neutral species,
+ * FP32 field mode, magnetic fields all FP32 tables): without the code of the
+ * other field types it needs no local memory at 168 registers. */
+template <bool TAB_ONLY>
+static __device__ __forceinline__ void try_phase(const DScene &S, const DRun &R, const DBatch &b, DCounters *C, int in, int out) {
     const int n = b.count[in];
     const int32_t *lin = b.list[in];
     Lane L(S, R);
+    double ksr[5][9];
+    const Lane::KReg ks{ksr, L.y, L.dydt};
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const int i = lin[k];
-        L.load_try_input(b, i);
-        int r = L.rk_try();
-        L.store_try_output(b, i, r == 1);
+        L.load_try_input(b, i, ks);
+        int r = L.rk_try_with<TAB_ONLY>(ks);
+        L.store_try_output(b, i, r == 1, ks);
         if (r == 1) {
             uint32_t f = b.flags[i];
             L.flags = f;
@@ -59,6 +65,13 @@ __global__ void __launch_bounds__(128, 3) k_try(const __grid_constant__ DScene S
         }
     }
     flush_counters(C, L.lc, 0.0, false);
+}
+
+__global__ void __launch_bounds__(128, PT_TRY_BLOCKS_PER_SM) k_try(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out) {
+    try_phase<false>(S, R, b, C, in, out);
+}
+__global__ void __launch_bounds__(128, PT_TRY_BLOCKS_PER_SM) k_try_tab32(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out) {
+    try_phase<true>(S, R, b, C, in, out);
 }
 
 /* Batched form, phase 2: the common step completion (no clip, no split, no

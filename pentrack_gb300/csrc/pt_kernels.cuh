@@ -5,6 +5,9 @@
 #pragma once
 #include "pt_device.cuh"
 
+/* k_try: resident blocks of 128 per SM (register budget 168) */
+#define PT_TRY_BLOCKS_PER_SM 3
+
 namespace ptk {
 
 __global__ void k_init(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C);
@@ -12,6 +15,7 @@ __global__ void k_gather(const __grid_constant__ DBatch b, double t_pause, int32
 __global__ void k_regather(const __grid_constant__ DBatch b, double t_pause, int max_steps, int32_t *list, int32_t *count);
 __global__ void k_zero_counts(int32_t *count, int a, int b, int c);
 __global__ void k_try(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out);
+__global__ void k_try_tab32(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out);
 __global__ void k_post(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out);
 __global__ void k_slow(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out);
 __global__ void k_bisect(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C);

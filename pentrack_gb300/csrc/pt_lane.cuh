@@ -46,6 +46,57 @@ struct BisectState {
 };
 enum { BISECT_RUNNING = 2 };
 
+/* TParticle::EquationOfMotion (src/particle.cpp:105-135) with given fields */
+static __device__ __forceinline__ void eom(const DSpecies &sp, const double *yy, const double B[3], const double (*dB)[3],
+                                           const double E[3], double *d) {
+    d[0] = yy[3]; d[1] = yy[4]; d[2] = yy[5];
+    double F0 = 0, F1 = 0, F2 = sp.fgrav;
+    if (sp.q != 0) {
+        F0 += sp.q * (E[0] + yy[4] * B[2] - yy[5] * B[1]);
+        F1 += sp.q * (E[1] + yy[5] * B[0] - yy[3] * B[2]);
+        F2 += sp.q * (E[2] + yy[3] * B[1] - yy[4] * B[0]);
+    }
+    if (sp.mu != 0 && yy[7] != 0 && (B[0] != 0 || B[1] != 0 || B[2] != 0)) {
+        double inv = 1.0 / sqrt(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
+        double g0 = (B[0] * dB[0][0] + B[1] * dB[1][0] + B[2] * dB[2][0]) * inv;
+        double g1 = (B[0] * dB[0][1] + B[1] * dB[1][1] + B[2] * dB[2][1]) * inv;
+        double g2 = (B[0] * dB[0][2] + B[1] * dB[1][2] + B[2] * dB[2][2]) * inv;
+        F0 += yy[7] * sp.mu * g0;
+        F1 += yy[7] * sp.mu * g1;
+        F2 += yy[7] * sp.mu * g2;
+    }
+    double v2 = yy[3] * yy[3] + yy[4] * yy[4] + yy[5] * yy[5];
+    double ig = sqrt(1 - v2 * PT_INV_C0_SQ);
+    double vF = (yy[3] * F0 + yy[4] * F1 + yy[5] * F2) * PT_INV_C0_SQ;
+    double s = ig * sp.inv_mkg;
+    d[3] = s * (F0 - yy[3] * vF);
+    d[4] = s * (F1 - yy[4] * vF);
+    d[5] = s * (F2 - yy[5] * vF);
+    d[6] = ig;
+    d[7] = 0;
+    d[8] = sqrt(v2);
+}
+
+/* TParticle::derivs (src/particle.cpp:105-135) for every species and field
+ * mode but the FP32 neutral one: B (with its Jacobian when the
+ * magnetic-moment force needs it), E, then the equation of motion.  Returns
+ * whether B was evaluated (its value in B). */
+static __device__ __forceinline__ bool rhs_general(const DScene &S, const DRun &R, const double *yy, double *d, double B[3]) {
+    const DSpecies &sp = R.sp;
+    double dB[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, E[3] = {0, 0, 0}, V = 0;
+    B[0] = B[1] = B[2] = 0;
+    bool have = false;
+    if (sp.q != 0 || (sp.mu != 0 && yy[7] != 0)) {
+        /* the Jacobian only feeds the magnetic-moment force */
+        if (sp.mu != 0 && yy[7] != 0) bfield<true>(S, R.prec, yy[0], yy[1], yy[2], B, dB);
+        else bfield<false>(S, R.prec, yy[0], yy[1], yy[2], B, nullptr);
+        have = true;
+    }
+    if (sp.q != 0) efield(S, R.prec, yy[0], yy[1], yy[2], V, E);
+    eom(sp, yy, B, dB, E, d);
+    return have;
+}
+
 struct Lane {
     const DScene &S;
     const DRun &R;
@@ -120,7 +171,17 @@ struct Lane {
         ntry = __ldcs(&b.ntry[i]);
         nacc = __ldcs(&b.nacc[i]); nrej = __ldcs(&b.nrej[i]);
     }
-    __device__ void store_try_output(const DBatch &b, int64_t i, bool accepted) const {
+    /* the same with y and dydt into ks's state slots */
+    template <class K> __device__ void load_try_input(const DBatch &b, int64_t i, const K &ks) {
+        const int64_t n = b.n;
+        t = __ldcs(&b.t[i]);
+        for (int c = 0; c < 9; ++c) { ks.y(c) = __ldcs(&b.y[c * n + i]); ks.dy(c) = __ldcs(&b.dydt[c * n + i]); }
+        dt = __ldcs(&b.dt[i]);
+        ntry = __ldcs(&b.ntry[i]);
+        nacc = __ldcs(&b.nacc[i]); nrej = __ldcs(&b.nrej[i]);
+    }
+    /* the try's outputs; stage vectors k3 .. k6 from ks(1 .. 4, c) */
+    template <class K> __device__ void store_try_output(const DBatch &b, int64_t i, bool accepted, const K &ks) const {
         const int64_t n = b.n;
         __stcs(&b.dt[i], dt);
         __stcs(&b.ntry[i], ntry);
@@ -128,10 +189,10 @@ struct Lane {
         if (accepted) {
             for (int c = 0; c < 9; ++c) { __stcs(&b.yn[c * n + i], yn[c]); __stcs(&b.dyn[c * n + i], dyn[c]); }
             for (int c = 0; c < 9; ++c) {
-                __stcs(&b.kst[(0 * 9 + c) * n + i], k3[c]);
-                __stcs(&b.kst[(1 * 9 + c) * n + i], k4[c]);
-                __stcs(&b.kst[(2 * 9 + c) * n + i], k5[c]);
-                __stcs(&b.kst[(3 * 9 + c) * n + i], k6[c]);
+                __stcs(&b.kst[(0 * 9 + c) * n + i], ks(1, c));
+                __stcs(&b.kst[(1 * 9 + c) * n + i], ks(2, c));
+                __stcs(&b.kst[(2 * 9 + c) * n + i], ks(3, c));
+                __stcs(&b.kst[(3 * 9 + c) * n + i], ks(4, c));
             }
             __stcs(&b.tn[i], tn);
         }
@@ -321,58 +382,28 @@ struct Lane {
     }
 
     /* TParticle::derivs + EquationOfMotion (src/particle.cpp:96-135) */
-    __device__ void derivs(const double *yy, double tt, double *d, bool keepB = false) {
-        const DSpecies &sp = R.sp;
-        if (sp.q == 0 && R.prec == PT_PREC_FP32) {
-            derivs_neutral32(yy, tt, d, keepB);
+    /* TAB_ONLY: a neutral species in the FP32 field mode whose magnetic
+     * fields are all FP32 tables (the host selects it), the other paths
+     * compiled out */
+    template <bool TAB_ONLY = false> __device__ void derivs(const double *yy, double tt, double *d, bool keepB = false) {
+        if (TAB_ONLY || (R.sp.q == 0 && R.prec == PT_PREC_FP32)) {
+            derivs_neutral32<TAB_ONLY>(yy, tt, d, keepB);
             return;
         }
-        double B[3] = {0, 0, 0}, dB[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, E[3] = {0, 0, 0}, V = 0;
-        if (sp.q != 0 || (sp.mu != 0 && yy[7] != 0)) {
-            /* the Jacobian only feeds the magnetic-moment force */
-            if (sp.mu != 0 && yy[7] != 0) bfield<true>(S, R.prec, yy[0], yy[1], yy[2], B, dB);
-            else bfield<false>(S, R.prec, yy[0], yy[1], yy[2], B, nullptr);
+        double B[3];
+        if (rhs_general(S, R, yy, d, B)) {
             ++lc.fields;
             /* the value part of the gradient evaluation is bit-identical to a
              * B-only evaluation, so it can serve later B-only queries */
             if (keepB) bc_put(yy[0], yy[1], yy[2], tt, B);
         }
-        if (sp.q != 0) efield(S, R.prec, yy[0], yy[1], yy[2], V, E);
         ++lc.rhs;
-        eom_fields(yy, B, dB, E, d);
     }
 
     /* TParticle::EquationOfMotion (src/particle.cpp:105-135) with given fields */
     __device__ __forceinline__ void eom_fields(const double *yy, const double B[3], const double (*dB)[3], const double E[3], double *d) const {
-        const DSpecies &sp = R.sp;
-        d[0] = yy[3]; d[1] = yy[4]; d[2] = yy[5];
-        double F0 = 0, F1 = 0, F2 = sp.fgrav;
-        if (sp.q != 0) {
-            F0 += sp.q * (E[0] + yy[4] * B[2] - yy[5] * B[1]);
-            F1 += sp.q * (E[1] + yy[5] * B[0] - yy[3] * B[2]);
-            F2 += sp.q * (E[2] + yy[3] * B[1] - yy[4] * B[0]);
-        }
-        if (sp.mu != 0 && yy[7] != 0 && (B[0] != 0 || B[1] != 0 || B[2] != 0)) {
-            double inv = 1.0 / sqrt(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
-            double g0 = (B[0] * dB[0][0] + B[1] * dB[1][0] + B[2] * dB[2][0]) * inv;
-            double g1 = (B[0] * dB[0][1] + B[1] * dB[1][1] + B[2] * dB[2][1]) * inv;
-            double g2 = (B[0] * dB[0][2] + B[1] * dB[1][2] + B[2] * dB[2][2]) * inv;
-            F0 += yy[7] * sp.mu * g0;
-            F1 += yy[7] * sp.mu * g1;
-            F2 += yy[7] * sp.mu * g2;
-        }
-        double v2 = yy[3] * yy[3] + yy[4] * yy[4] + yy[5] * yy[5];
-        double ig = sqrt(1 - v2 * PT_INV_C0_SQ);
-        double vF = (yy[3] * F0 + yy[4] * F1 + yy[5] * F2) * PT_INV_C0_SQ;
-        double s = ig * sp.inv_mkg;
-        d[3] = s * (F0 - yy[3] * vF);
-        d[4] = s * (F1 - yy[4] * vF);
-        d[5] = s * (F2 - yy[5] * vF);
-        d[6] = ig;
-        d[7] = 0;
-        d[8] = sqrt(v2);
+        eom(R.sp, yy, B, dB, E, d);
     }
-
     /* TParticle::SpinPrecessionAxis (src/particle.cpp:148-175) */
     __device__ void spin_axis(const double B[3], const double E[3], const double *dydt, double W[3]) const {
         const double v2 = dydt[0] * dydt[0] + dydt[1] * dydt[1] + dydt[2] * dydt[2];
@@ -495,12 +526,12 @@ struct Lane {
      * grad B and the magnetic gradient force pol mu grad|B| in FP32 (relative
      * error ~1e-7 of a force well below gravity), gravity, the relativistic
      * factors and the state derivative in FP64. */
-    __device__ void derivs_neutral32(const double *yy, double tt, double *d, bool keepB) {
+    template <bool TAB_ONLY = false> __device__ void derivs_neutral32(const double *yy, double tt, double *d, bool keepB) {
         const DSpecies &sp = R.sp;
         double F0 = 0, F1 = 0, F2 = sp.fgrav;
         if (sp.mu != 0 && yy[7] != 0) {
             float B[3], dB[3][3];
-            bfield32<true>(S, yy[0], yy[1], yy[2], B, dB);
+            bfield32<true, TAB_ONLY>(S, yy[0], yy[1], yy[2], B, dB);
             ++lc.fields;
             if (keepB) {
                 const double Bd[3] = {B[0], B[1], B[2]};
@@ -577,12 +608,26 @@ struct Lane {
     __device__ int cur_solid() const { return current_solid(nsol, sidx, sign); }
 
     /* ---------------- Dormand-Prince 5(4) with odeint's controller ---------------- */
+    /* Storage of one try's vectors: ks(s, i) is component i of stage s + 2
+     * (k2 .. k6), ks.y(i) / ks.dy(i) of the committed state and its
+     * derivative.  KReg keeps the stages in a local array and the state in the
+     * lane's members (registers). */
+    struct KReg {
+        double (*a)[9];
+        double *ys, *dys;
+        __device__ __forceinline__ double &operator()(int s, int i) const { return a[s][i]; }
+        __device__ __forceinline__ double &y(int i) const { return ys[i]; }
+        __device__ __forceinline__ double &dy(int i) const { return dys[i]; }
+    };
+
     /* One try of controlled_runge_kutta::try_step on the committed state
      * (t, y, dydt).  Returns 1 when accepted (dense data set, dt grown), 0
      * when rejected (dt shrunk), -1 after 500 consecutive rejections (odeint's
      * failed_step_checker).  The stage sums are explicit fused multiply-add
-     * chains in tableau order, the same chains the oracle evaluates. */
-    __device__ int rk_try() {
+     * chains in tableau order, the same chains the oracle evaluates; the
+     * stage vectors live wherever `ks` puts them, which changes no operation.
+     * On acceptance yn and dyn are set; the caller takes k3 .. k6 from ks. */
+    template <bool TAB_ONLY = false, class K> __device__ __forceinline__ int rk_try_with(const K &ks) {
         const double a2 = 1.0 / 5, a3 = 3.0 / 10, a4 = 4.0 / 5, a5 = 8.0 / 9;
         const double b21 = 1.0 / 5;
         const double b31 = 3.0 / 40, b32 = 9.0 / 40;
@@ -594,28 +639,33 @@ struct Lane {
                      dc5 = c5 - (-92097.0) / 339200, dc6 = c6 - 187.0 / 2100, dc7 = -1.0 / 40;
         if (ntry >= PT_MAX_TRIES) return -1;
         ++ntry;
-        double k2[9], xt[9];
+        double xt[9], d[9];
         const double h = dt;
-        for (int i = 0; i < 9; ++i) xt[i] = fma(h * b21, dydt[i], y[i]);
-        derivs(xt, t + h * a2, k2);
-        for (int i = 0; i < 9; ++i) xt[i] = fma(h * b32, k2[i], fma(h * b31, dydt[i], y[i]));
-        derivs(xt, t + h * a3, k3);
-        for (int i = 0; i < 9; ++i) xt[i] = fma(h * b43, k3[i], fma(h * b42, k2[i], fma(h * b41, dydt[i], y[i])));
-        derivs(xt, t + h * a4, k4);
+        for (int i = 0; i < 9; ++i) xt[i] = fma(h * b21, ks.dy(i), ks.y(i));
+        derivs<TAB_ONLY>(xt, t + h * a2, d);
+        for (int i = 0; i < 9; ++i) ks(0, i) = d[i];
+        for (int i = 0; i < 9; ++i) xt[i] = fma(h * b32, ks(0, i), fma(h * b31, ks.dy(i), ks.y(i)));
+        derivs<TAB_ONLY>(xt, t + h * a3, d);
+        for (int i = 0; i < 9; ++i) ks(1, i) = d[i];
+        for (int i = 0; i < 9; ++i) xt[i] = fma(h * b43, ks(1, i), fma(h * b42, ks(0, i), fma(h * b41, ks.dy(i), ks.y(i))));
+        derivs<TAB_ONLY>(xt, t + h * a4, d);
+        for (int i = 0; i < 9; ++i) ks(2, i) = d[i];
         for (int i = 0; i < 9; ++i)
-            xt[i] = fma(h * b54, k4[i], fma(h * b53, k3[i], fma(h * b52, k2[i], fma(h * b51, dydt[i], y[i]))));
-        derivs(xt, t + h * a5, k5);
+            xt[i] = fma(h * b54, ks(2, i), fma(h * b53, ks(1, i), fma(h * b52, ks(0, i), fma(h * b51, ks.dy(i), ks.y(i)))));
+        derivs<TAB_ONLY>(xt, t + h * a5, d);
+        for (int i = 0; i < 9; ++i) ks(3, i) = d[i];
         for (int i = 0; i < 9; ++i)
-            xt[i] = fma(h * b65, k5[i], fma(h * b64, k4[i], fma(h * b63, k3[i], fma(h * b62, k2[i], fma(h * b61, dydt[i], y[i])))));
-        derivs(xt, t + h, k6);
+            xt[i] = fma(h * b65, ks(3, i), fma(h * b64, ks(2, i), fma(h * b63, ks(1, i), fma(h * b62, ks(0, i), fma(h * b61, ks.dy(i), ks.y(i))))));
+        derivs<TAB_ONLY>(xt, t + h, d);
+        for (int i = 0; i < 9; ++i) ks(4, i) = d[i];
         for (int i = 0; i < 9; ++i)
-            yn[i] = fma(h * c6, k6[i], fma(h * c5, k5[i], fma(h * c4, k4[i], fma(h * c3, k3[i], fma(h * c1, dydt[i], y[i])))));
-        derivs(yn, t + h, dyn, true);
+            yn[i] = fma(h * c6, ks(4, i), fma(h * c5, ks(3, i), fma(h * c4, ks(2, i), fma(h * c3, ks(1, i), fma(h * c1, ks.dy(i), ks.y(i))))));
+        derivs<TAB_ONLY>(yn, t + h, dyn, true);
         const double adt = fabs(h);
         double m = 0;
         for (int i = 0; i < 9; ++i) {
-            double e = fma(h * dc7, dyn[i], fma(h * dc6, k6[i], fma(h * dc5, k5[i], fma(h * dc4, k4[i], fma(h * dc3, k3[i], (h * dc1) * dydt[i])))));
-            double r = fabs(e) / (1e-9 + 1e-9 * (fabs(y[i]) + adt * fabs(dydt[i])));
+            double e = fma(h * dc7, dyn[i], fma(h * dc6, ks(4, i), fma(h * dc5, ks(3, i), fma(h * dc4, ks(2, i), fma(h * dc3, ks(1, i), (h * dc1) * ks.dy(i))))));
+            double r = fabs(e) / (1e-9 + 1e-9 * (fabs(ks.y(i)) + adt * fabs(ks.dy(i))));
             m = (m < r || r != r) ? r : m; /* a NaN estimate sticks and rejects the step */
         }
         if (!(m <= 1.0)) {
@@ -630,11 +680,19 @@ struct Lane {
             m = fmax(0.00032, m); /* 5^-5 */
             dt *= 0.9 * ptdm_pow(m, -1.0 / 5.0);
         }
-        for (int i = 0; i < 9; ++i) { xo[i] = y[i]; dxo[i] = dydt[i]; }
+        for (int i = 0; i < 9; ++i) { xo[i] = ks.y(i); dxo[i] = ks.dy(i); }
         ntry = 0;
         ++nacc;
         ++lc.rk_acc;
         return 1;
+    }
+    /* rk_try with the stage vectors in registers; k3 .. k6 kept for the dense output */
+    __device__ int rk_try() {
+        double ks[5][9];
+        const int r = rk_try_with(KReg{ks, y, dydt});
+        if (r == 1)
+            for (int i = 0; i < 9; ++i) { k3[i] = ks[1][i]; k4[i] = ks[2][i]; k5[i] = ks[3][i]; k6[i] = ks[4][i]; }
+        return r;
     }
 
     /* runge_kutta_dopri5::calc_state: continuous extension on [to, tn]; the

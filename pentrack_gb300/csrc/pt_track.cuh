@@ -562,12 +562,31 @@ __device__ void bfield64(const DScene &S, double x, double y, double z, double B
     }
 }
 
+/* One field of a type without an FP32 table, evaluated in FP64 and rounded */
+template <bool GRAD>
+__device__ __forceinline__ void bfield_other32(const DField &f, double x, double y, double z, float Bt[3], float (*dBt)[3]) {
+    double Bd[3] = {0, 0, 0}, dBd[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    if (f.type == PT_FIELD_TAB3D) tab3_b<GRAD>(f, x, y, z, Bd, dBd);
+    else if (f.type == PT_FIELD_HARMONIC) harmonic_b<GRAD>(f, x, y, z, Bd, dBd);
+    else if (f.type == PT_FIELD_SOLENOID) solenoid_b(f, x, y, z, Bd, GRAD ? dBd : nullptr);
+    for (int i = 0; i < 3; ++i) {
+        Bd[i] *= f.bscale;
+        if (GRAD) for (int j = 0; j < 3; ++j) dBd[i][j] *= f.bscale;
+    }
+    for (int i = 0; i < 3; ++i) scale_at_bounds(f, x, y, z, Bd[i], GRAD ? dBd[i] : nullptr);
+    for (int i = 0; i < 3; ++i) {
+        Bt[i] = (float)Bd[i];
+        if (GRAD) for (int j = 0; j < 3; ++j) dBt[i][j] = (float)dBd[i][j];
+    }
+}
+
 /* The same superposition in the FP32 field mode: tables without a smoothing
  * band are evaluated in FP32 from the cell's FP32 linear base plus the FP32
  * Hermite remainder (relative error ~1e-7 in B and grad B, no cancellation
  * since the base gradient is stored); every other field is evaluated in FP64
- * and rounded. */
-template <bool GRAD>
+ * and rounded.  TAB_ONLY: the scene's magnetic fields are all such tables
+ * (checked on the host), so the other field types are compiled out. */
+template <bool GRAD, bool TAB_ONLY = false>
 __device__ void bfield32(const DScene &S, double x, double y, double z, float B[3], float (*dB)[3]) {
     B[0] = B[1] = B[2] = 0;
     if (GRAD)
@@ -586,20 +605,8 @@ __device__ void bfield32(const DScene &S, double x, double y, double z, float B[
                     if (GRAD) for (int j = 0; j < 3; ++j) dBt[i][j] *= sc;
                 }
             }
-        } else {
-            double Bd[3] = {0, 0, 0}, dBd[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-            if (f.type == PT_FIELD_TAB3D) tab3_b<GRAD>(f, x, y, z, Bd, dBd);
-            else if (f.type == PT_FIELD_HARMONIC) harmonic_b<GRAD>(f, x, y, z, Bd, dBd);
-            else if (f.type == PT_FIELD_SOLENOID) solenoid_b(f, x, y, z, Bd, GRAD ? dBd : nullptr);
-            for (int i = 0; i < 3; ++i) {
-                Bd[i] *= f.bscale;
-                if (GRAD) for (int j = 0; j < 3; ++j) dBd[i][j] *= f.bscale;
-            }
-            for (int i = 0; i < 3; ++i) scale_at_bounds(f, x, y, z, Bd[i], GRAD ? dBd[i] : nullptr);
-            for (int i = 0; i < 3; ++i) {
-                Bt[i] = (float)Bd[i];
-                if (GRAD) for (int j = 0; j < 3; ++j) dBt[i][j] = (float)dBd[i][j];
-            }
+        } else if (!TAB_ONLY) {
+            bfield_other32<GRAD>(f, x, y, z, Bt, dBt);
         }
         for (int i = 0; i < 3; ++i) {
             B[i] += Bt[i];
