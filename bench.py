@@ -267,8 +267,10 @@ def e2e_run(args, engine, params, rank, T):
             "ms_per_step": total_s * 1e3 / args.e2e_steps, "tracking_device_ms_per_step": dev_ms / args.e2e_steps}
 
 
-def load_traffic():
-    path = os.path.join(ROOT, "profiles", "k_plain_field_storage_traffic.json")
+def load_traffic(kernel):
+    """DRAM bytes per RK try of the try kernel, from the committed ncu capture
+    (profiles/<kernel>_field_storage_traffic.json); None when absent."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_field_storage_traffic.json")
     if os.path.exists(path):
         with open(path) as f:
             return json.load(f)
@@ -334,14 +336,30 @@ def run_ours(args, rank, world):
         kern = {"k_try": agg["try_ms"], "k_post": agg["post_ms"], "k_slow": agg["slow_ms"], "k_bisect": agg["bisect_ms"], "k_plain_tail": agg["tail_ms"]}
         dom = max(kern, key=kern.get)
         avg_launch_s = kern[dom] / 1e3 / launches
-        achieved = (try_f64 if dom == "k_try" else f64) / launches / avg_launch_s / 1e12
+        dom_f64 = try_f64 if dom == "k_try" else f64
+        dom_f32 = (tries * 6 * field_per_rhs if args.precision == "fp32" else 0) if dom == "k_try" else f32
+        achieved = dom_f64 / launches / avg_launch_s / 1e12
         # the try phase runs k_try_tab32 when every field is an FP32 table
         agg["dominant_kernel"] = try_kernel if dom == "k_try" else dom
     else:
         launches = max(1, agg["dominant_launches"])
         avg_launch_s = agg["dominant_kernel_ms"] / 1e3 / launches
         achieved = f64 / launches / avg_launch_s / 1e12
-    traffic = load_traffic()
+        dom_f64, dom_f32 = f64, f32
+    traffic = None
+    if args.mode == "batched" and args.workload == "field_storage" and agg["dominant_kernel"].startswith("k_try"):
+        t = load_traffic(agg["dominant_kernel"])
+        if t:
+            # per launch like `achieved`: bytes per try x tries per average launch
+            traffic = (t["dram_read_bytes_per_try"] + t["dram_write_bytes_per_try"]) * tries / launches
+    state_bytes = None
+    if args.mode == "batched":
+        # per-particle state a try must move: reads t, y, dydt, dt, ntry, nacc,
+        # nrej, list entry (188 B), writes dt, ntry, nacc, nrej (28 B); an
+        # accepted try also writes yn, dyn, k3..k6, tn, flags, the B cache slot
+        # and a list entry (504 B), a rejected one a list entry (4 B)
+        acc = agg["rk_accepted"] / max(1, tries)
+        state_bytes = (188 + 28 + 504 * acc + 4 * (1 - acc)) * tries / launches
     line = {
         "metric": METRIC,
         "value": psec_all / device_s,
@@ -370,10 +388,10 @@ def run_ours(args, rank, world):
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                      "frac": achieved / peak.value if peak.value else None,
                      "peak_source": "measured: pt_probe_fp64 DFMA kernel on this GPU",
-                     "traffic": traffic.get("bytes_per_launch") if traffic else None,
+                     "traffic": traffic, "state_bytes_per_launch": state_bytes,
                      "kernel": agg["dominant_kernel"], "launches": int(launches),
                      "avg_launch_ms": avg_launch_s * 1e3,
-                     "fp64_flops_per_launch": f64 / launches, "fp32_flops_per_launch": f32 / launches},
+                     "fp64_flops_per_launch": dom_f64 / launches, "fp32_flops_per_launch": dom_f32 / launches},
         "events": {k: agg[k] for k in ("rk_accepted", "rk_rejected", "rhs_evals", "field_evals", "hits",
                                         "bisection_levels", "bvh_nodes", "tri_tests", "subsegments", "dense_evals",
                                         "bisect_max", "bisect_dead", "cand_calls", "cand_overflow", "cand_sum", "tri32_tests")},
