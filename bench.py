@@ -48,7 +48,7 @@ def parse():
                    help="field_storage: the headline configuration; large_mesh: the 200k-triangle, 128^3 scale-up")
     p.add_argument("--batch-steps", type=int, default=32, help="accepted RK steps per particle per bench step")
     p.add_argument("--precision", default="fp32", choices=["fp64", "fp32"],
-                   help="field evaluation: fp64, or fp32 = mixed (corner values FP64, derivative terms FP32)")
+                   help="field evaluation: fp64, or fp32 = FP32 node table (linear base + FP32 Hermite remainder)")
     p.add_argument("--mode", default="batched", choices=["plain", "batched"])
     p.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison run")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
