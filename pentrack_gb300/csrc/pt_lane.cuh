@@ -46,6 +46,21 @@ struct BisectState {
 };
 enum { BISECT_RUNNING = 2 };
 
+/* Entries of a packed current-solids list (one byte each: solid index in
+ * bits 0-5, ignored flag in bit 7). */
+static __device__ __forceinline__ int stk_idx(uint64_t s, int k) { return (int)((s >> (8 * k)) & 63); }
+static __device__ __forceinline__ bool stk_ign(uint64_t s, int k) { return (s >> (8 * k + 7)) & 1; }
+static __device__ __forceinline__ uint64_t stk_put(uint64_t s, int k, int idx, bool ign) {
+    const int sh = 8 * k;
+    return (s & ~(0xFFull << sh)) | ((uint64_t)(idx | (ign ? 128 : 0)) << sh);
+}
+/* remove entry k of the n entries: entries k+1 .. n-1 move down one place,
+ * entry n-1 keeps its old value (as the element-wise shift leaves it) */
+static __device__ __forceinline__ uint64_t stk_erase(uint64_t s, int k, int n) {
+    for (int i = k; i + 1 < n; ++i) s = stk_put(s, i, stk_idx(s, i + 1), stk_ign(s, i + 1));
+    return s;
+}
+
 /* TParticle::EquationOfMotion (src/particle.cpp:105-135) with given fields */
 static __device__ __forceinline__ void eom(const DSpecies &sp, const double *yy, const double B[3], const double (*dB)[3],
                                            const double E[3], double *d) {
@@ -107,8 +122,10 @@ struct Lane {
     double spin[5];
     double tau, hmax, noflip;
     int stop, nhit, nstep, nspinflip, nsol;
-    uint8_t sidx[PT_MAX_STACK];
-    bool sign[PT_MAX_STACK];
+    /* current-solids list packed one byte per entry (solid index | ignored
+     * << 7), entry k in bits 8k .. 8k+7: bit operations keep it in a register
+     * where indexed arrays would put the whole lane in local memory */
+    uint64_t stk;
     uint64_t rn;
     int64_t nacc, nrej;
     int ntry;           /* consecutive rejected tries of the current step */
@@ -152,12 +169,7 @@ struct Lane {
         for (int c = 0; c < 5; ++c) spin[c] = __ldcs(&b.spin[c * n + i]);
         tau = __ldcs(&b.tau[i]); hmax = __ldcs(&b.hmax[i]); noflip = __ldcs(&b.noflip[i]);
         stop = __ldcs(&b.stop_id[i]); nhit = __ldcs(&b.nhit[i]); nstep = __ldcs(&b.nstep[i]); nspinflip = __ldcs(&b.nspinflip[i]); nsol = __ldcs(&b.nsol[i]);
-        uint64_t st = __ldcs(&b.stack[i]);
-        for (int k = 0; k < PT_MAX_STACK; ++k) {
-            uint8_t v = (uint8_t)(st >> (8 * k));
-            sidx[k] = v & 63;
-            sign[k] = (v >> 7) & 1;
-        }
+        stk = __ldcs(&b.stack[i]) & 0xBFBFBFBFBFBFBFBFull;
         rn = __ldcs(&b.rng_n[i]);
         nacc = __ldcs(&b.nacc[i]); nrej = __ldcs(&b.nrej[i]);
         ntry = __ldcs(&b.ntry[i]);
@@ -350,9 +362,7 @@ struct Lane {
         for (int c = 0; c < 5; ++c) __stcs(&b.spin[c * n + i], spin[c]);
         __stcs(&b.tau[i], tau); __stcs(&b.hmax[i], hmax); __stcs(&b.noflip[i], noflip);
         __stcs(&b.stop_id[i], stop); __stcs(&b.nhit[i], nhit); __stcs(&b.nstep[i], nstep); __stcs(&b.nspinflip[i], nspinflip); __stcs(&b.nsol[i], nsol);
-        uint64_t st = 0;
-        for (int k = 0; k < PT_MAX_STACK; ++k) st |= (uint64_t)(sidx[k] | (sign[k] ? 128 : 0)) << (8 * k);
-        __stcs(&b.stack[i], st);
+        __stcs(&b.stack[i], stk);
         __stcs(&b.rng_n[i], rn);
         __stcs(&b.nacc[i], nacc); __stcs(&b.nrej[i], nrej);
         __stcs(&b.ntry[i], ntry);
@@ -597,15 +607,15 @@ struct Lane {
 
     /* ---------------- solids ---------------- */
     /* TTracker::GetCurrentsolid (src/tracking.cpp:367-370) */
-    __device__ int current_solid(int n, const uint8_t *ix, const bool *ig) const {
+    __device__ int current_solid(int n, uint64_t st) const {
         int best = 0;
         for (int i = 1; i < n; ++i) {
-            bool less = ig[best] || (!ig[i] && S.solids[ix[best]].id < S.solids[ix[i]].id);
+            bool less = stk_ign(st, best) || (!stk_ign(st, i) && S.solids[stk_idx(st, best)].id < S.solids[stk_idx(st, i)].id);
             if (less) best = i;
         }
-        return ix[best];
+        return stk_idx(st, best);
     }
-    __device__ int cur_solid() const { return current_solid(nsol, sidx, sign); }
+    __device__ int cur_solid() const { return current_solid(nsol, stk); }
 
     /* ---------------- Dormand-Prince 5(4) with odeint's controller ---------------- */
     /* Storage of one try's vectors: ks(s, i) is component i of stage s + 2
@@ -884,7 +894,7 @@ struct Lane {
     }
 
     /* ---------------- RotateVector (src/globals.cpp:40-64) ---------------- */
-    __device__ static void rotate_vector(double v[3], const double n[3], const double *x) {
+    __device__ __forceinline__ static void rotate_vector(double v[3], const double n[3], const double *x) {
         double nn = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
         double xv[3];
         bool use_base = (x == nullptr);
@@ -1168,28 +1178,26 @@ struct Lane {
         int nc = all_hits(x1, y1, x2, y2, colls);
         if (nc <= 0) { stop = PT_ID_CGAL_ERROR; return true; }
         int nn = nsol;
-        uint8_t ni[PT_MAX_STACK];
-        bool ng[PT_MAX_STACK];
-        for (int i = 0; i < nn; ++i) { ni[i] = sidx[i]; ng[i] = sign[i]; }
+        uint64_t ns = stk; /* the new list, same packing */
         for (int c = 0; c < nc; ++c) {
             const Coll &cl = colls[c];
             int found = -1;
-            for (int i = 0; i < nn; ++i) if (S.solids[ni[i]].id == cl.id) { found = i; break; }
+            for (int i = 0; i < nn; ++i) if (S.solids[stk_idx(ns, i)].id == cl.id) { found = i; break; }
             if (cl.dn < 0) {
                 if (found >= 0) {
                     if (cl.s > 0) {
                         if (nn >= PT_MAX_STACK) { stop = PT_ID_GEOMETRY_ERROR; return true; }
-                        ni[nn] = (uint8_t)cl.solid; ng[nn] = ng[found]; ++nn;
+                        ns = stk_put(ns, nn, cl.solid, stk_ign(ns, found)); ++nn;
                     }
                 } else {
                     if (nn >= PT_MAX_STACK) { stop = PT_ID_GEOMETRY_ERROR; return true; }
-                    ni[nn] = (uint8_t)cl.solid; ng[nn] = cl.ign; ++nn;
+                    ns = stk_put(ns, nn, cl.solid, cl.ign); ++nn;
                 }
             } else if (cl.dn > 0) {
                 if (found < 0) {
                     if (cl.s > 0) { stop = PT_ID_GEOMETRY_ERROR; return true; }
                 } else {
-                    for (int i = found; i + 1 < nn; ++i) { ni[i] = ni[i + 1]; ng[i] = ng[i + 1]; }
+                    ns = stk_erase(ns, found, nn);
                     --nn;
                 }
             } else {
@@ -1200,7 +1208,7 @@ struct Lane {
         int leaving = cur_solid();
         int entering = 0;
         for (int i = 0; i < nn; ++i)
-            if (!ng[i] && S.solids[ni[i]].id > S.solids[entering].id) entering = ni[i];
+            if (!stk_ign(ns, i) && S.solids[stk_idx(ns, i)].id > S.solids[entering].id) entering = stk_idx(ns, i);
         if (S.solids[leaving].id != S.solids[entering].id) {
             int ci = -1;
             for (int c = 0; c < nc; ++c)
@@ -1224,7 +1232,7 @@ struct Lane {
         }
         if (traversed) {
             nsol = nn;
-            for (int i = 0; i < nn; ++i) { sidx[i] = ni[i]; sign[i] = ng[i]; }
+            stk = ns;
         }
         return altered || stop != PT_ID_UNKNOWN;
     }
@@ -1306,14 +1314,13 @@ struct Lane {
         if (R.tau > 0) tau = -log(1 - u01()) * R.tau;
         else tau = R.tmax;
         nsol = 1;
-        sidx[0] = 0; sign[0] = false;
+        stk = 0; /* entry 0: solid 0, not ignored */
         uint64_t m = point_solids(S, y, qs);
         for (int s = 1; s < S.n_solids; ++s)
             if (m & (1ull << s)) {
-                if (nsol < PT_MAX_STACK) { sidx[nsol] = (uint8_t)s; sign[nsol] = solid_ignored(S.solids[s], t); ++nsol; }
+                if (nsol < PT_MAX_STACK) { stk = stk_put(stk, nsol, s, solid_ignored(S.solids[s], t)); ++nsol; }
                 else stop = PT_ID_GEOMETRY_ERROR;
             }
-        for (int k = nsol; k < PT_MAX_STACK; ++k) { sidx[k] = 0; sign[k] = false; }
         double h0 = ekin(&y[3]) + epot(t, y, cur_solid());
         hmax = h0;
         noflip = 1;
