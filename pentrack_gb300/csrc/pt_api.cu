@@ -457,7 +457,7 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
     /* Once few particles remain, iterations cost mostly launch latency: the
      * queue is drained and the rest runs as plain-form lanes (same
      * per-particle arithmetic, so the same bits). */
-    const int tail = (int)std::max<int64_t>(2048, n / 50);
+    const int tail = (int)std::max<int64_t>(2048, n / 1000);
     bool to_plain = false;
     for (int it = 0;; ++it) {
         const int in = it & 1, out = in ^ 1;
