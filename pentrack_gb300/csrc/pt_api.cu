@@ -369,9 +369,9 @@ void add_counters(pt_stats &acc, const DCounters &k) {
     acc.cand_calls += k.cand_calls; acc.cand_overflow += k.cand_overflow; acc.cand_sum += k.cand_sum; acc.tri32_tests += k.tri32; acc.bisect_dead += k.bisect_dead; acc.spin_steps += k.spin_steps;
 }
 
-int persistent_grid(pt_ctx *c, const void *fn, int block, size_t smem = 0) {
+int persistent_grid(pt_ctx *c, const void *fn, int block) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, 0);
     if (per_sm < 1) per_sm = 1;
     return per_sm * c->sm_count;
 }
