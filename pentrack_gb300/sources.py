@@ -163,3 +163,84 @@ def phase_space_volume_source(seed, ids, random_point, potential, emin, emax, sp
     parts = S.make_particles(seed, ids, pos, ekin, ph, th, pol, species=species)
     parts.t[:] = t0
     return parts, vmin
+
+
+_SURF_BASE = 3000        # surface points: triangle, two barycentric draws per round
+REFLECT_TOLERANCE = 1e-8  # include/trianglemesh.h:39
+
+
+def cylinder_region(rmin, rmax, zmin, zmax, phimin=-S.PI, phimax=S.PI):
+    """InSourceVolume of TCylindricalSurfaceSource (include/source.h:279-283)
+    and its bounding box (include/source.h:272-274)"""
+    def inside(p):
+        r = np.sqrt(p[:, 0] * p[:, 0] + p[:, 1] * p[:, 1])
+        ph = np.arctan2(p[:, 1], p[:, 0])
+        return (r > rmin) & (r < rmax) & (ph > phimin) & (ph < phimax) & (p[:, 2] > zmin) & (p[:, 2] < zmax)
+    return inside, ((-rmax, -rmax, zmin), (rmax, rmax, zmax))
+
+
+def surface_source(seed, ids, scene, in_volume, bbox, emin, emax, enormal=0.0, polarization=0.0, t_range=(0.0, 0.0),
+                   spectrum=None, species=A.NEUTRON, max_rounds=100_000):
+    """TSurfaceSource::CreateParticle (src/source.cpp:102-131): a point on the
+    scene's surfaces (TTriangleMesh::RandomPointOnSurface,
+    include/trianglemesh.h:210-232: a solid's mesh by area among those whose
+    bounding box meets the source box, a triangle by area, a uniform point on
+    it) redrawn until `in_volume(points)` holds, moved off the surface by
+    REFLECT_TOLERANCE along the unit face normal; a cos(theta) sin(theta)
+    direction about that normal, the normal energy raised by `enormal`.
+    `bbox` = ((xmin, ymin, zmin), (xmax, ymax, zmax)) of the source region."""
+    ids = np.asarray(ids, dtype=np.int64)
+    n = len(ids)
+    lo, hi = np.asarray(bbox[0], np.float64), np.asarray(bbox[1], np.float64)
+    tris, weights = [], []
+    for block, solid in scene.tri_blocks:
+        t = np.asarray(block, np.float64).reshape(-1, 3, 3)
+        mlo, mhi = t.min(axis=(0, 1)), t.max(axis=(0, 1))
+        if np.any(mhi < lo) or np.any(mlo > hi):
+            continue  # the reference redraws meshes whose box misses the source box
+        tris.append(t)
+        weights.append(0.5 * np.sqrt((np.cross(t[:, 1] - t[:, 0], t[:, 2] - t[:, 0]) ** 2).sum(1)))
+    if not tris:
+        raise ValueError("no surface of the scene meets the source region")
+    tris, weights = np.concatenate(tris), np.concatenate(weights)
+    cum = np.cumsum(weights)
+    pos, nrm = np.full((3, n), np.nan), np.full((3, n), np.nan)
+    todo = np.arange(n)
+    for r in range(max_rounds):
+        if len(todo) == 0:
+            break
+        k = _SURF_BASE + r * _ROUND_STRIDE
+        sid = ids[todo]
+        j = np.minimum(np.searchsorted(cum, S._draw(seed, sid, k) * cum[-1], side="right"), len(cum) - 1)
+        a, b = S._draw(seed, sid, k + 1), S._draw(seed, sid, k + 2)
+        flip = a + b > 1
+        a, b = np.where(flip, 1 - a, a), np.where(flip, 1 - b, b)
+        t = tris[j]
+        p = t[:, 0] + a[:, None] * (t[:, 1] - t[:, 0]) + b[:, None] * (t[:, 2] - t[:, 0])
+        ok = np.asarray(in_volume(p), dtype=bool)
+        nv = np.cross(t[:, 1] - t[:, 0], t[:, 2] - t[:, 0])
+        nv /= np.sqrt((nv ** 2).sum(1))[:, None]
+        sel = todo[ok]
+        pos[:, sel], nrm[:, sel] = p[ok].T, nv[ok].T
+        todo = todo[~ok]
+    if len(todo):
+        raise RuntimeError(f"no surface point in the source region for {len(todo)} particles")
+    pos = pos + nrm * REFLECT_TOLERANCE
+    if spectrum is None:
+        E = emin + S._draw(seed, ids, 4) * (emax - emin)
+    else:
+        E = spectrum(seed, ids)
+    ph = 2.0 * S.PI * S._draw(seed, ids, 5)
+    th = np.arccos(np.sqrt(1.0 - S._draw(seed, ids, 6)))  # sincos_distribution(0, pi/2), include/mc.h:163-175
+    if enormal > 0:
+        vn = np.sqrt(E * np.cos(th) * np.cos(th) + enormal)
+        vt = np.sqrt(E) * np.sin(th)
+        th = np.arctan2(vt, vn)
+        E = vn * vn + vt * vt
+    v = np.vstack([np.cos(ph) * np.sin(th), np.sin(ph) * np.sin(th), np.cos(th)])
+    v = S.rotate_vector(v, nrm)
+    ph, th = np.arctan2(v[1], v[0]), np.arccos(np.clip(v[2], -1.0, 1.0))
+    pol = np.where(S._draw(seed, ids, 3) < 0.5 * (polarization + 1), 1.0, -1.0)
+    parts = S.make_particles(seed, ids, pos, E, ph, th, pol, species=species)
+    parts.t[:] = t_range[0] + S._draw(seed, ids, 7) * (t_range[1] - t_range[0])
+    return parts

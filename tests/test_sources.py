@@ -70,3 +70,27 @@ def test_phase_space_weighting_in_gravity(oracle_mod):
     p2, _ = sources.phase_space_volume_source(1001, np.arange(300, 600), pts, V, 0.0, 60e-9, n_min_samples=20000)
     p12, _ = sources.phase_space_volume_source(1001, np.arange(600), pts, V, 0.0, 60e-9, n_min_samples=20000)
     assert np.array_equal(np.hstack([p1.y, p2.y]), p12.y)
+
+
+def test_surface_source_on_a_face():
+    """TSurfaceSource on the top face of the storage cube: points on the face
+    inside the source cylinder, 1e-8 m off along the outward normal, Lambert
+    (cos theta sin theta) directions about it, uniform over the face, and
+    the normal energy raised by Enormal."""
+    from pentrack_gb300 import workloads, logger
+    sc, _, _ = workloads.cube_storage(n=1)
+    inside, box = sources.cylinder_region(0.0, 0.3, 0.49, 0.51)
+    ids = np.arange(5000)
+    p = sources.surface_source(5, ids, sc, inside, box, 0.0, 100e-9)
+    assert np.allclose(p.y[2], 0.5 + 1e-8, rtol=0, atol=1e-15)
+    r2 = p.y[0] ** 2 + p.y[1] ** 2
+    assert np.all(r2 < 0.09)
+    assert ks_uniform_p(r2 / 0.09) > 1e-3
+    v = np.sqrt((p.y[3:6] ** 2).sum(0))
+    cz = p.y[5] / v
+    assert np.all(cz > 0) and ks_uniform_p(cz ** 2) > 1e-3
+    e0 = logger.kinetic_energy(A.NEUTRON, p.y[3:6])
+    q = sources.surface_source(5, ids, sc, inside, box, 0.0, 100e-9, enormal=20e-9)
+    e1 = logger.kinetic_energy(A.NEUTRON, q.y[3:6])
+    np.testing.assert_allclose(e1, e0 + 20e-9, rtol=1e-9)
+    assert np.array_equal(q.y[0:3], p.y[0:3])
