@@ -101,16 +101,21 @@ def rest_energy_potential(scene, kind, field, point_solids):
 
 def phase_space_volume_source(seed, ids, random_point, potential, emin, emax, spectrum=None, polarization=0.0,
                               t_range=(0.0, 0.0), theta=(0.0, S.PI), phi=(0.0, 2 * S.PI), species=A.NEUTRON,
-                              n_min_samples=100_000, max_rounds=100_000):
+                              n_min_samples=100_000, max_rounds=100_000, direction=None, times=None):
     """TVolumeSource with PhaseSpaceWeighting.  `random_point(seed, ids, base)`
     gives points (3, n) in the source volume from draws at counter `base` on,
     `potential(t, pos, pol)` the potential energy there (rest_energy_potential),
-    `spectrum(seed, ids)` total energies (default uniform on [emin, emax]).
-    Returns (ParticleSet, Vmin)."""
+    `spectrum(seed, ids)` total energies (default uniform on [emin, emax]);
+    `direction(seed, ids)` -> (phi, theta) and `times(seed, ids, counter)`
+    replace the default uniform azimuth, sine-distributed polar angle and
+    uniform start time on t_range.  Returns (ParticleSet, Vmin)."""
     ids = np.asarray(ids, dtype=np.int64)
     n = len(ids)
+    time_of = times
 
     def times(sel_ids, k):
+        if time_of is not None:
+            return time_of(seed, sel_ids, k)
         return t_range[0] + S._draw(seed, sel_ids, k) * (t_range[1] - t_range[0])
 
     def pols(sel_ids, k):
@@ -157,9 +162,12 @@ def phase_space_volume_source(seed, ids, random_point, potential, emin, emax, sp
         todo = todo[~ok]
     if len(todo):
         raise RuntimeError(f"no accepted start point for {len(todo)} particles after {max_rounds} rounds")
-    ph = phi[0] + S._draw(seed, ids, 5) * (phi[1] - phi[0])
-    u = S._draw(seed, ids, 6)
-    th = np.arccos(np.cos(theta[0]) - u * (np.cos(theta[0]) - np.cos(theta[1])))
+    if direction is not None:
+        ph, th = direction(seed, ids)
+    else:
+        ph = phi[0] + S._draw(seed, ids, 5) * (phi[1] - phi[0])
+        u = S._draw(seed, ids, 6)
+        th = np.arccos(np.cos(theta[0]) - u * (np.cos(theta[0]) - np.cos(theta[1])))
     parts = S.make_particles(seed, ids, pos, ekin, ph, th, pol, species=species)
     parts.t[:] = t0
     return parts, vmin
