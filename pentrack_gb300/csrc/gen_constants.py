@@ -3,9 +3,9 @@
 PENTrack defines its constants as ``long double`` (src/globals.cpp:13-32) and
 derives the particle masses in eV/c^2 by a long-double division by the
 elementary charge.  On x86-64 that is 80-bit extended arithmetic.  Device code
-has no long double, and the GPU machine is aarch64 where ``long double`` is IEEE
-quad, so the values are evaluated once here with numpy's x86 extended type,
-rounded to double, and written as hex-float literals.  The oracle and the CUDA
+has no long double, and on aarch64 hosts ``long double`` is IEEE quad, so
+the values are evaluated once here with numpy's x86 extended type, rounded
+to double, and written as hex-float literals.  The oracle and the CUDA
 kernels include the same header, so both see bit-identical constants.
 
 Run on an x86-64 host:  python pentrack_gb300/csrc/gen_constants.py

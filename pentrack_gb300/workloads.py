@@ -131,7 +131,7 @@ def integration_test_acceleration(grad=0.5):
 
 
 def mixed_species_scene(nseg=160):
-    """Configuration 3's geometry and fields: a cylinder R = 0.3 m, z in
+    """The mixed-species scene: a cylinder R = 0.3 m, z in
     [-0.5, 0.5] whose wall is a closed 1 cm shell (solid 2) with a detector
     disc at the top (solid 3, z in [0.495, 0.4999]); particles move in the
     default medium (solid 1) and charged OnStep absorbs them as soon as they
@@ -153,7 +153,7 @@ def mixed_species_scene(nseg=160):
 
 
 def mixed_species(n_protons=100_000, n_electrons=100_000, seed=1003, tmax=1e-3):
-    """Configuration 3: decay protons (E ~ U[0, 750] eV) and electrons (beta
+    """The mixed-species workload: decay protons (E ~ U[0, 750] eV) and electrons (beta
     spectrum on [0, 782] keV), isotropic, uniform in the cylinder; tracked up
     to 1 ms proper time (tmax, which the reference reports as ID_DECAYED).
     Returns the scene and per-species (params, particles) pairs; the species
@@ -183,7 +183,7 @@ def multipole_table(n=128, lo=(-1.15, -1.15, -0.55), hi=(1.15, 1.15, 0.55), g1=0
 
 
 def large_mesh_scene(table_n=128, nu=500, nv=160, nlat=101, nlon=200):
-    """Configuration 5's scene: a noise-perturbed torus (R = 1 m, r = 0.1 m,
+    """The large-mesh scene: a noise-perturbed torus (R = 1 m, r = 0.1 m,
     2 nu nv triangles) as the guide and a sphere (R = 0.5 m at the origin,
     2 nlon (nlat - 1) triangles) as the bottle, both closed vacuum solids in a
     wall of 10 % diffuse reflection and 3e-5 loss per bounce (200,000
@@ -202,7 +202,7 @@ def large_mesh_scene(table_n=128, nu=500, nv=160, nlat=101, nlon=200):
 
 
 def large_mesh(n=10_000_000, seed=1005, simtime=100.0, table_n=128, scene=None, engine=None, first_id=0):
-    """Configuration 5: UCN with E ~ U[0, 300] neV, isotropic, half of them
+    """The large-mesh workload: UCN with E ~ U[0, 300] neV, isotropic, half of them
     uniform in the bottle (r < 0.45 m) and half uniform in the guide's tube
     (within 0.08 m of its centre circle), tau 880 s, 100 s."""
     sc = scene if scene is not None else large_mesh_scene(table_n)

@@ -1,4 +1,4 @@
-"""Configuration 5's geometry (needs a GB300): the 200,000-triangle
+"""The large-mesh geometry (needs a GB300): the 200,000-triangle
 noise-perturbed torus and sphere with a tricubic multipole (32^3 here, so the
 oracle's reference-layout table stays small), GPU vs oracle over 0.5 s.
 

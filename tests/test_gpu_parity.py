@@ -192,8 +192,8 @@ def compare_states(gpu, orc, pos_tol=1e-6, vel_tol=1e-6):
 
 
 def test_cube_storage_parity(eng, oracle_mod):
-    """BASELINE configuration 1 (closed unit cube, gravity, specular 335 neV
-    walls, 0-200 neV): per-particle end states within 1e-6 of the oracle."""
+    """The closed unit cube (gravity, specular 335 neV walls, 0-200 neV UCN):
+    per-particle end states within 1e-6 of the oracle."""
     from pentrack_gb300 import workloads
     sc, params, parts = workloads.cube_storage(n=2000, simtime=100.0)
     gout, gst = eng(sc).integrate(params, parts)
@@ -248,7 +248,7 @@ def test_integration_test_known_answer_gpu(eng):
 
 
 def test_field_storage_short_parity(eng, oracle_mod):
-    """BASELINE configuration 2 physics (tricubic quadrupole, +-mu grad|B|,
+    """Field-storage physics (tricubic quadrupole, +-mu grad|B|,
     Fermi walls with Lambert diffuse and loss, decay) over 0.5 s: the same
     Philox stream drives both, so end states agree particle by particle."""
     from pentrack_gb300 import workloads

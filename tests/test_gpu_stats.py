@@ -36,7 +36,7 @@ def test_field_storage_distributions_match_oracle(built, oracle_mod):
 
 @pytest.mark.parametrize("species", [A.PROTON, A.ELECTRON])
 def test_mixed_species_distributions_match_oracle(built, oracle_mod, species):
-    """Configuration 3 (decay protons / beta electrons in a 1 T solenoid plus a
+    """The mixed-species workload (decay protons / beta electrons in a 1 T solenoid plus a
     30 kV/m field, absorbing wall and detector): end time, end z and the
     fractions of particles absorbed in the wall and on the detector."""
     stats = pytest.importorskip("scipy.stats")
