@@ -55,3 +55,31 @@ def test_create_without_device_fails_cleanly(built):
         assert e.value.status in (-8, -4)
     else:
         pytest.skip("a GPU is present")
+
+
+def test_ctypes_layout_equals_the_c_compilers(tmp_path):
+    """Every field offset and struct size of the ctypes mirror equals what a C
+    compiler computes from include/pentrack_gpu.h."""
+    import shutil
+    import subprocess
+    from pentrack_gb300 import _abi as A
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"pt_material": A.Material, "pt_solid": A.Solid, "pt_field": A.Field, "pt_scene_desc": A.SceneDesc,
+               "pt_run_params": A.RunParams, "pt_particles": A.Particles, "pt_stats": A.Stats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "pentrack_gpu.h"', "int main(void) {"]
+    expect = []
+    for cname, cls in structs.items():
+        lines.append(f'printf("%zu\\n", sizeof({cname}));')
+        expect.append(ctypes.sizeof(cls))
+        for f in cls._fields_:
+            lines.append(f'printf("%zu\\n", offsetof({cname}, {f[0]}));')
+            expect.append(getattr(cls, f[0]).offset)
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert got == expect
