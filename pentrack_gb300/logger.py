@@ -165,3 +165,18 @@ def write_endlog(directory, scene, kind, start, end, field, point_solids, jobnum
     if unknown:
         raise ValueError(f"end log variables not available (formulas are not evaluated): {unknown}")
     return write_log(directory, jobnumber, SPECIES_NAME[kind], "end", titles, [v[t] for t in titles])
+
+
+def log_settings(config_path, particle_name, suffix="end"):
+    """(enabled, logvars) of one log from a config.in: `<suffix>log` and
+    `<suffix>logvars` of [PARTICLES], overridden by the particle's own
+    section (as TTracker reads the particle options, src/tracking.cpp:19-60);
+    logvars None means the default columns."""
+    from .config_source import read_config
+    cfg = read_config(config_path)
+    opts = dict(cfg.get("PARTICLES", {}))
+    opts.update(cfg.get(particle_name, {}))
+    on = opts.get(suffix + "log", "0").split()
+    names = opts.get(suffix + "logvars", "").split()
+    return bool(on) and float(on[0]) != 0, (names or None)
+

@@ -59,3 +59,54 @@ def test_cylindrical_volume_and_surface_sources(tmp_path):
     p.write_text("[SOURCE]\nsourcemode sphere\n")
     with pytest.raises(ValueError):
         cs.source_from_config(str(p), 10, 9)
+
+
+INTEGRATION_TEST_CONFIG = """[GLOBAL]
+simtype 1
+simcount 1000
+simtime 10
+
+[SOURCE]
+sourcemode boxvolume
+parameters 0.1	0.1	0.5	0.5		0.01	0.01
+particle neutron
+ActiveTime 0
+PhaseSpaceWeighting 0
+Emin 10e-9
+Emax 150e-9
+spectrum 1
+phi_v_min 0
+phi_v_max 0
+phi_v 1
+theta_v_min 5
+theta_v_max 5
+theta_v 1
+polarization 1
+
+[PARTICLES]
+tau 0
+endlog 1
+endlogvars xstart ystart zstart xend yend zend vxstart vystart vzstart vxend vyend vzend
+hitlog 0
+"""
+
+
+def test_reference_integration_test_source(tmp_path):
+    """The source and end-log settings of the reference's integration test
+    (test/IntegrationTest/config.in): every neutron starts at (0.1, 0.5, 0.01)
+    with azimuth 0 and polar angle 5 degrees, 10-150 neV, polarisation +1; the
+    end log is on with its twelve columns."""
+    from pentrack_gb300 import logger
+    p = tmp_path / "config.in"
+    p.write_text(INTEGRATION_TEST_CONFIG)
+    kind, parts = cs.source_from_config(str(p), 1000, 3)
+    assert kind == A.NEUTRON
+    assert np.all(parts.y[0] == 0.1) and np.all(parts.y[1] == 0.5) and np.all(parts.y[2] == 0.01)
+    v = np.sqrt((parts.y[3:6] ** 2).sum(0))
+    np.testing.assert_allclose(parts.y[5] / v, np.cos(5 * np.pi / 180), rtol=1e-12)
+    assert np.all(parts.y[4] == 0) and np.all(parts.y[3] > 0) and np.all(parts.y[7] == 1) and np.all(parts.t == 0)
+    e = logger.kinetic_energy(A.NEUTRON, parts.y[3:6])
+    assert np.all((e > 10e-9 * (1 - 1e-9)) & (e < 150e-9 * (1 + 1e-9))) and e.std() > 30e-9
+    on, names = logger.log_settings(str(p), "neutron")
+    assert on and names[:3] == ["xstart", "ystart", "zstart"] and len(names) == 12
+    assert logger.log_settings(str(p), "neutron", "hit") == (False, None)
