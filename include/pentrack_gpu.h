@@ -304,6 +304,31 @@ pt_status pt_config_run_params(const char *config_path, const char *species, pt_
                                int32_t max_spintimes);
 const char *pt_config_error(void);
 
+/* The end log of one species' particles in the reference's text layout
+ * (TLogger::Print with suffix "end", src/logger.cpp:42-126, written as
+ * TTextLogger::DoLog does, src/logger.cpp:314-334): the file
+ * <directory>/<jobnumber, 12 digits><particle>end.out with a header of the
+ * variable names and one line per particle, values at 15 significant
+ * digits, each followed by a space.  No reference counterpart as a function:
+ * the reference writes the line per particle from TTracker.  `start` holds
+ * the tracked inputs, `end` pt_integrate's outputs (n = start->n); the caller
+ * passes B (3 per particle, row-major) and V at the start and end points and
+ * the index into scene->solids of the solid each point is in
+ * (pt_field_eval, pt_point_solids).  `logvars` (space-separated names, the
+ * config's endlogvars) selects columns, NULL or "" the default 43; formulas
+ * are refused with PT_ERR_UNSUPPORTED.  Errors: PT_ERR_INVALID, PT_ERR_IO;
+ * message in pt_config_error(). */
+/* The solid index each point is in, from its pt_point_solids mask at time t:
+ * the default solid plus the masked solids in index order, the highest ID
+ * not ignored at t winning (TTracker::GetCurrentsolid, src/tracking.cpp:
+ * 367-370, over TGeometry::GetSolids, src/geometry.cpp:151-158).  Host only. */
+pt_status pt_current_solid(const pt_scene_desc *scene, int64_t n, const uint64_t *masks, const double *t,
+                           int32_t *solid_index);
+pt_status pt_endlog_write(const char *directory, int64_t jobnumber, int32_t species, const pt_scene_desc *scene,
+                          const pt_particles *start, const pt_particles *end, const double *b_start,
+                          const double *v_start, const int32_t *solid_start, const double *b_end, const double *v_end,
+                          const int32_t *solid_end, const char *logvars);
+
 /* Library version string. */
 const char *pt_version(void);
 

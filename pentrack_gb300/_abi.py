@@ -130,6 +130,10 @@ def declare(lib):
         "pt_config_free": (None, [vp]),
         "pt_config_run_params": (C.c_int32, [C.c_char_p, C.c_char_p, P(RunParams), c_double_p, C.c_int32]),
         "pt_config_error": (C.c_char_p, []),
+        "pt_current_solid": (C.c_int32, [P(SceneDesc), C.c_int64, c_uint64_p, c_double_p, c_int32_p]),
+        "pt_endlog_write": (C.c_int32, [C.c_char_p, C.c_int64, C.c_int32, P(SceneDesc), P(Particles), P(Particles),
+                                        c_double_p, c_double_p, c_int32_p, c_double_p, c_double_p, c_int32_p,
+                                        C.c_char_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -2,6 +2,7 @@
  * pt_host.cpp -- config.in front end of the GPU path (see pt_host.hpp).
  */
 #include "pt_host.hpp"
+#include "../../include/pt_constants.h"
 
 #include <algorithm>
 #include <cmath>
@@ -9,6 +10,7 @@
 #include <cstring>
 #include <filesystem>
 #include <fstream>
+#include <iomanip>
 #include <sstream>
 
 namespace fs = std::filesystem;
@@ -496,6 +498,109 @@ pt_status TTrackerGPU::IntegrateParticles(const std::string &species, const pt_p
     return st;
 }
 
+
+/* ---------------- end log ---------------- */
+const SpeciesConstants *species_constants(int kind) {
+    static const SpeciesConstants table[3] = {
+        {"neutron", PT_NEUTRON, PT_NEUTRON_M, PT_NEUTRON_Q, PT_NEUTRON_MU, PT_NEUTRON_MU_OVER_E, PT_NEUTRON_Q_OVER_E,
+         PT_NEUTRON_MC2, PT_NEUTRON_MG},
+        {"proton", PT_PROTON, PT_PROTON_M, PT_PROTON_Q, PT_PROTON_MU, PT_PROTON_MU_OVER_E, PT_PROTON_Q_OVER_E,
+         PT_PROTON_MC2, PT_PROTON_MG},
+        {"electron", PT_ELECTRON, PT_ELECTRON_M, PT_ELECTRON_Q, PT_ELECTRON_MU, PT_ELECTRON_MU_OVER_E,
+         PT_ELECTRON_Q_OVER_E, PT_ELECTRON_MC2, PT_ELECTRON_MG}};
+    return kind >= 0 && kind < 3 ? &table[kind] : nullptr;
+}
+
+double kinetic_energy(const SpeciesConstants &sp, const double v[3]) {
+    const double beta2 = (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) / PT_C0_SQ;
+    const double b4 = beta2 * beta2;
+    double gm1;
+    if (b4 * b4 * beta2 < 2.220446049250313e-16)
+        gm1 = (0.5 + (3.0 / 8.0 + (5.0 / 16.0 + 35.0 / 128.0 * beta2) * beta2) * beta2) * beta2;
+    else
+        gm1 = 1.0 / std::sqrt(1.0 - beta2) - 1.0;
+    return sp.mc2 * gm1;
+}
+
+double potential_energy(const SpeciesConstants &sp, const pt_scene_desc &scene, const double y[9], const double B[3],
+                        double V, int solid) {
+    double r = 0;
+    if (sp.mu != 0) r += -y[7] * sp.mu_over_e * std::sqrt(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
+    if (sp.q != 0) r += sp.q_over_e * V;
+    r += sp.mg * y[2];
+    if (sp.kind == PT_NEUTRON) {
+        const pt_material &m = scene.materials[scene.solids[solid].material];
+        r += m.fermi_real * 1e-9 - m.internal_bfield * sp.mu_over_e * y[7];
+    }
+    return r;
+}
+
+const char *const END_TITLES[43] = {
+    "jobnumber", "particle", "tstart", "xstart", "ystart", "zstart", "vxstart", "vystart", "vzstart", "polstart",
+    "Sxstart", "Systart", "Szstart", "Hstart", "Estart", "Bstart", "Ustart", "solidstart", "tend", "xend", "yend",
+    "zend", "vxend", "vyend", "vzend", "polend", "Sxend", "Syend", "Szend", "Hend", "Eend", "Bend", "Uend",
+    "solidend", "stopID", "Nspinflip", "spinflipprob", "Nhit", "Nstep", "propert", "trajlength", "Hmax", "wL"};
+
+bool end_variable_known(const std::string &name) {
+    if (name == "m" || name == "q" || name == "mu") return true;
+    for (const char *t : END_TITLES)
+        if (name == t) return true;
+    return false;
+}
+
+EndRow end_row(const SpeciesConstants &sp, const pt_scene_desc &scene, const pt_particles &start, const pt_particles &end,
+               int64_t i, const double *b0, double v0, int s0, const double *b1, double v1, int s1, int64_t jobnumber) {
+    const int64_t n = start.n;
+    double ys[9], ye[9];
+    for (int c = 0; c < 9; ++c) {
+        ys[c] = start.y[c * n + i];
+        ye[c] = end.y[c * n + i];
+    }
+    const double es = kinetic_energy(sp, &ys[3]), ee = kinetic_energy(sp, &ye[3]);
+    EndRow r;
+    auto &v = r.v;
+    v["jobnumber"] = (double)jobnumber;
+    v["particle"] = (double)(start.id[i] + 1);
+    v["m"] = sp.m;
+    v["q"] = sp.q;
+    v["mu"] = sp.mu;
+    v["tstart"] = start.t[i];
+    v["tend"] = end.t[i];
+    const char *pos[6] = {"x", "y", "z", "vx", "vy", "vz"};
+    for (int c = 0; c < 6; ++c) {
+        v[std::string(pos[c]) + "start"] = ys[c];
+        v[std::string(pos[c]) + "end"] = ye[c];
+    }
+    v["polstart"] = ys[7];
+    v["polend"] = ye[7];
+    const char *sn[3] = {"Sx", "Sy", "Sz"};
+    for (int c = 0; c < 3; ++c) {
+        v[std::string(sn[c]) + "start"] = start.spin ? start.spin[c * n + i] : 0.0;
+        v[std::string(sn[c]) + "end"] = end.spin ? end.spin[c * n + i] : 0.0;
+    }
+    v["Hstart"] = es + potential_energy(sp, scene, ys, b0, v0, s0);
+    v["Estart"] = es;
+    v["Bstart"] = std::sqrt(b0[0] * b0[0] + b0[1] * b0[1] + b0[2] * b0[2]);
+    v["Ustart"] = v0;
+    v["solidstart"] = (double)scene.solids[s0].id;
+    v["Hend"] = ee + potential_energy(sp, scene, ye, b1, v1, s1);
+    v["Eend"] = ee;
+    v["Bend"] = std::sqrt(b1[0] * b1[0] + b1[1] * b1[1] + b1[2] * b1[2]);
+    v["Uend"] = v1;
+    v["solidend"] = (double)scene.solids[s1].id;
+    v["stopID"] = (double)end.stop_id[i];
+    v["Nspinflip"] = (double)end.n_spinflip[i];
+    v["spinflipprob"] = 1 - end.noflip_prob[i];
+    v["Nhit"] = (double)end.n_hit[i];
+    v["Nstep"] = (double)end.n_step[i];
+    v["propert"] = ye[6];
+    v["trajlength"] = ye[8];
+    v["Hmax"] = end.h_max[i];
+    const double s3 = end.spin ? end.spin[3 * n + i] : 0.0, s4 = end.spin ? end.spin[4 * n + i] : 0.0;
+    v["wL"] = s3 > 0 ? s4 / s3 : 0.0;
+    return r;
+}
+
 } // namespace pth
 
 /* ---------------- C ABI of the config front end ---------------- */
@@ -539,5 +644,89 @@ pt_status pt_config_run_params(const char *config_path, const char *species, pt_
 }
 
 const char *pt_config_error(void) { return g_config_err.c_str(); }
+
+pt_status pt_current_solid(const pt_scene_desc *scene, int64_t n, const uint64_t *masks, const double *t,
+                           int32_t *solid_index) {
+    if (!scene || n < 0 || (n > 0 && (!masks || !t || !solid_index)) || scene->n_solids < 1 || scene->n_solids > 64) {
+        g_config_err = "pt_current_solid: invalid arguments";
+        return PT_ERR_INVALID;
+    }
+    auto ignored = [&](int s, double tt) {
+        const pt_solid &so = scene->solids[s];
+        for (int k = 0; k < so.n_ignore; ++k)
+            if (tt >= so.ignore_times[2 * k] && tt < so.ignore_times[2 * k + 1]) return true;
+        return false;
+    };
+    for (int64_t i = 0; i < n; ++i) {
+        int best = 0;
+        bool best_ign = false;
+        for (int s = 1; s < scene->n_solids; ++s) {
+            if (!((masks[i] >> s) & 1)) continue;
+            const bool ign = ignored(s, t[i]);
+            if (best_ign || (!ign && scene->solids[best].id < scene->solids[s].id)) {
+                best = s;
+                best_ign = ign;
+            }
+        }
+        solid_index[i] = best;
+    }
+    return PT_OK;
+}
+
+pt_status pt_endlog_write(const char *directory, int64_t jobnumber, int32_t species, const pt_scene_desc *scene,
+                          const pt_particles *start, const pt_particles *end, const double *b_start,
+                          const double *v_start, const int32_t *solid_start, const double *b_end, const double *v_end,
+                          const int32_t *solid_end, const char *logvars) {
+    if (!directory || !scene || !start || !end || !b_start || !v_start || !solid_start || !b_end || !v_end ||
+        !solid_end || start->n != end->n || !end->stop_id || !end->n_hit || !end->n_step || !end->n_spinflip ||
+        !end->h_max || !end->noflip_prob) {
+        g_config_err = "pt_endlog_write: missing arrays or start and end of different size";
+        return PT_ERR_INVALID;
+    }
+    const pth::SpeciesConstants *sp = pth::species_constants(species);
+    if (!sp) {
+        g_config_err = "pt_endlog_write: unknown species";
+        return PT_ERR_INVALID;
+    }
+    const int64_t n = start->n;
+    for (int64_t i = 0; i < n; ++i)
+        if (solid_start[i] < 0 || solid_start[i] >= scene->n_solids || solid_end[i] < 0 || solid_end[i] >= scene->n_solids) {
+            g_config_err = "pt_endlog_write: solid index out of range";
+            return PT_ERR_INVALID;
+        }
+    std::vector<std::string> titles;
+    if (logvars && *logvars) {
+        std::istringstream ls(logvars);
+        for (std::string t; ls >> t;) titles.push_back(t);
+    }
+    if (titles.empty()) titles.assign(std::begin(pth::END_TITLES), std::end(pth::END_TITLES));
+    for (const auto &t : titles)
+        if (!pth::end_variable_known(t)) {
+            g_config_err = "pt_endlog_write: end log variable '" + t + "' is not available (formulas are not evaluated)";
+            return PT_ERR_UNSUPPORTED;
+        }
+    char name[64];
+    std::snprintf(name, sizeof(name), "%012lld%send.out", (long long)jobnumber, sp->name);
+    const std::string path = (std::filesystem::path(directory) / name).string();
+    std::ofstream f(path);
+    if (!f) {
+        g_config_err = "Could not open " + path;
+        return PT_ERR_IO;
+    }
+    f << std::setprecision(15);
+    for (const auto &t : titles) f << t << ' ';
+    f << '\n';
+    for (int64_t i = 0; i < n; ++i) {
+        const pth::EndRow row = pth::end_row(*sp, *scene, *start, *end, i, b_start + 3 * i, v_start[i], solid_start[i],
+                                             b_end + 3 * i, v_end[i], solid_end[i], jobnumber);
+        for (const auto &t : titles) f << row.get(t) << ' ';
+        f << '\n';
+    }
+    if (!f) {
+        g_config_err = "write error on " + path;
+        return PT_ERR_IO;
+    }
+    return PT_OK;
+}
 
 } // extern "C"

@@ -67,6 +67,30 @@ pt_status load_scene(const std::string &config_path, SceneStore &store, std::str
 pt_status load_run_params(const std::string &config_path, const std::string &species, pt_run_params &p,
                           std::vector<double> &spintimes, std::string &err);
 
+/* ---- end log (TLogger::Print "end", src/logger.cpp:42-126) ---- */
+struct SpeciesConstants {
+    const char *name;
+    int kind;
+    double m, q, mu, mu_over_e, q_over_e, mc2, mg;
+};
+/* the constants the kernels use (include/pt_constants.h); nullptr for an unknown kind */
+const SpeciesConstants *species_constants(int kind);
+/* TParticle::GetKineticEnergy (src/particle.cpp:237-251) and GetPotentialEnergy
+ * (src/particle.cpp:254-269) + TNeutron's material potential, with the
+ * kernels' operations */
+double kinetic_energy(const SpeciesConstants &sp, const double v[3]);
+double potential_energy(const SpeciesConstants &sp, const pt_scene_desc &scene, const double y[9], const double B[3],
+                        double V, int solid);
+extern const char *const END_TITLES[43];
+bool end_variable_known(const std::string &name);
+/* one particle's end-log variables */
+struct EndRow {
+    std::map<std::string, double> v;
+    double get(const std::string &k) const { return v.at(k); }
+};
+EndRow end_row(const SpeciesConstants &sp, const pt_scene_desc &scene, const pt_particles &start, const pt_particles &end,
+               int64_t i, const double *b0, double v0, int s0, const double *b1, double v1, int s1, int64_t jobnumber);
+
 /* C++ front end with the reference's construction from a config file. */
 class TTrackerGPU {
 public:

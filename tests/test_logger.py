@@ -81,3 +81,66 @@ def test_endlog_start_energy_matches_oracle(oracle_mod):
     live = out.stop_id == A.ID_NOT_FINISH
     assert live.sum() > 100
     assert np.max(np.abs(v["Hend"][live] - v["Hstart"][live])) < 1e-13
+
+
+def test_cpp_endlog_writer_matches_python_byte_for_byte(built, oracle_mod, tmp_path):
+    """pt_endlog_write (the C ABI's end-log writer, C++ streams at precision
+    15) and logger.write_endlog write the same file, given the same fields and
+    solids: the C++ writer's formatting and energies are the Python ones."""
+    import ctypes as C
+    from pentrack_gb300 import workloads, engine
+    sc, params, parts = workloads.field_storage(n=300, simtime=0.02, table_n=16)
+    orc = oracle_mod.Oracle(sc)
+    out, _ = orc.integrate(params, parts)
+
+    def fields_solids(s):
+        B, _, V, _ = orc.field(np.column_stack([s.y[0], s.y[1], s.y[2], s.t]))
+        idx = logger.current_solid(sc, orc.point_solids(np.ascontiguousarray(s.y[0:3].T)), s.t)
+        return np.ascontiguousarray(B), np.ascontiguousarray(V), np.ascontiguousarray(idx.astype(np.int32))
+
+    B0, V0, S0 = fields_solids(parts)
+    B1, V1, S1 = fields_solids(out)
+    d_py, d_cpp = tmp_path / "py", tmp_path / "cpp"
+    d_py.mkdir()
+    d_cpp.mkdir()
+    py = logger.write_endlog(str(d_py), sc, A.NEUTRON, parts, out, orc.field, orc.point_solids, jobnumber=12)
+    L = engine.lib()
+    desc, keep = sc.desc()
+    dp = lambda a: a.ctypes.data_as(A.c_double_p)
+    ip = lambda a: a.ctypes.data_as(A.c_int32_p)
+    pin, pout = parts.abi(outputs=False), out.abi()
+    for logvars in (None, b"particle Hstart Hend stopID wL"):
+        st = L.pt_endlog_write(str(d_cpp).encode(), 12, A.NEUTRON, C.byref(desc), C.byref(pin), C.byref(pout),
+                               dp(B0), dp(V0), ip(S0), dp(B1), dp(V1), ip(S1), logvars)
+        assert st == A.PT_OK, L.pt_config_error()
+        if logvars is None:
+            assert open(d_cpp / "000000000012neutronend.out").read() == open(py).read()
+    sub = logger.write_endlog(str(d_py), sc, A.NEUTRON, parts, out, orc.field, orc.point_solids, jobnumber=12,
+                              logvars=["particle", "Hstart", "Hend", "stopID", "wL"])
+    assert open(d_cpp / "000000000012neutronend.out").read() == open(sub).read()
+    st = L.pt_endlog_write(str(d_cpp).encode(), 12, A.NEUTRON, C.byref(desc), C.byref(pin), C.byref(pout),
+                           dp(B0), dp(V0), ip(S0), dp(B1), dp(V1), ip(S1), b"Hend-Hstart")
+    assert st == A.PT_ERR_UNSUPPORTED
+
+
+def test_cpp_current_solid_matches_python(built):
+    """pt_current_solid picks the same solid as logger.current_solid, with
+    ignore times and overlapping solids of different priority."""
+    import ctypes as C
+    from pentrack_gb300 import Scene, engine, scenes
+    sc = Scene()
+    sc.add_material("a", 100.0)
+    sc.add_solid(1, "a")
+    sc.add_solid(5, "a", scenes.box_mesh((-1, -1, -1), (1, 1, 1)), ignore=[(2.0, 3.0)])
+    sc.add_solid(3, "a", scenes.box_mesh((-2, -2, -2), (2, 2, 2)))
+    sc.add_solid(7, "a", scenes.box_mesh((0, 0, 0), (1, 1, 1)), ignore=[(0.0, 1.0), (4.0, 5.0)])
+    rng = np.random.default_rng(8)
+    n = 5000
+    masks = rng.integers(0, 16, n).astype(np.uint64) & ~np.uint64(1)
+    t = rng.uniform(-1, 6, n)
+    desc, keep = sc.desc()
+    out = np.zeros(n, np.int32)
+    st = engine.lib().pt_current_solid(C.byref(desc), n, masks.ctypes.data_as(A.c_uint64_p),
+                                       t.ctypes.data_as(A.c_double_p), out.ctypes.data_as(A.c_int32_p))
+    assert st == A.PT_OK
+    assert np.array_equal(out, logger.current_solid(sc, masks, t))
