@@ -498,6 +498,43 @@ pt_status TTrackerGPU::IntegrateParticles(const std::string &species, const pt_p
     return st;
 }
 
+pt_status TTrackerGPU::WriteEndLog(const std::string &species, const pt_particles &in, const pt_particles &out,
+                                   const std::string &directory, int64_t jobnumber, const char *logvars) {
+    if (!ctx_) return PT_ERR_INVALID;
+    const int kind = species == "neutron" ? PT_NEUTRON : species == "proton" ? PT_PROTON : species == "electron" ? PT_ELECTRON : -1;
+    if (kind < 0 || in.n != out.n) {
+        err_ = "WriteEndLog: unknown species or batches of different size";
+        return PT_ERR_INVALID;
+    }
+    const int64_t n = in.n;
+    std::vector<double> q(4 * n), p(3 * n), B[2], dB(9 * n), V[2], E(3 * n);
+    std::vector<uint64_t> masks(n);
+    std::vector<int32_t> solid[2];
+    const pt_particles *set[2] = {&in, &out};
+    for (int k = 0; k < 2; ++k) {
+        for (int64_t i = 0; i < n; ++i) {
+            for (int c = 0; c < 3; ++c) q[4 * i + c] = p[3 * i + c] = set[k]->y[c * n + i];
+            q[4 * i + 3] = set[k]->t[i];
+        }
+        B[k].resize(3 * n);
+        V[k].resize(n);
+        solid[k].resize(n);
+        pt_status st = pt_field_eval(ctx_, n, q.data(), PT_PREC_FP64, B[k].data(), dB.data(), V[k].data(), E.data());
+        if (st == PT_OK) st = pt_point_solids(ctx_, n, p.data(), masks.data());
+        if (st != PT_OK) {
+            err_ = pt_last_error(ctx_);
+            return st;
+        }
+        if ((st = pt_current_solid(&store_.desc, n, masks.data(), set[k]->t, solid[k].data())) != PT_OK) {
+            err_ = pt_config_error();
+            return st;
+        }
+    }
+    pt_status st = pt_endlog_write(directory.c_str(), jobnumber, kind, &store_.desc, &in, &out, B[0].data(), V[0].data(),
+                                   solid[0].data(), B[1].data(), V[1].data(), solid[1].data(), logvars);
+    if (st != PT_OK) err_ = pt_config_error();
+    return st;
+}
 
 /* ---------------- end log ---------------- */
 const SpeciesConstants *species_constants(int kind) {

@@ -101,6 +101,10 @@ public:
     /* pt_integrate over host SoA arrays with the config's options for `species` */
     pt_status IntegrateParticles(const std::string &species, const pt_particles &in, pt_particles &out, pt_stats &stats,
                                  int mode = PT_MODE_BATCHED, uint64_t seed = 1);
+    /* the end log of a tracked batch (pt_endlog_write): fields and solids at
+     * the start and end points from this context's device queries */
+    pt_status WriteEndLog(const std::string &species, const pt_particles &in, const pt_particles &out,
+                          const std::string &directory, int64_t jobnumber = 0, const char *logvars = nullptr);
     const std::string &error() const { return err_; }
     pt_ctx *context() const { return ctx_; }
 
