@@ -56,3 +56,35 @@ def test_cube_storage_energy_conservation_oracle(oracle_mod):
     assert np.max(dh) < 1e-13, np.max(dh)  # eV, i.e. < 1e-4 neV
     assert np.all(out.n_hit > 0)
     assert np.all(out.solid == 2)
+
+
+def test_absorption_per_bounce_matches_the_complex_potential_step(oracle_mod):
+    """TNeutron::OnHit for total reflection (src/neutron.cpp:219-256): a UCN
+    bouncing vertically on a floor with Fermi potential 250 - 20i neV and
+    1e-3 loss per bounce is absorbed with probability
+    1 - |(k1 - k2)/(k1 + k2)|^2 + loss per hit, k = sqrt(E_normal - U).  The
+    number of hits to absorption is geometric: n / sum(hits) estimates it."""
+    from pentrack_gb300 import Scene, scenes, workloads
+    sc = Scene()
+    sc.add_material("floor", 250.0, fermi_imag=20.0, loss_per_bounce=1e-3)
+    sc.add_material("vacuum", 0.0)
+    sc.add_solid(1, "floor")
+    sc.add_solid(2, "vacuum", scenes.box_mesh((-0.5, -0.5, -0.5), (0.5, 0.5, 0.5)))
+    n = 3000
+    ids = np.arange(n, dtype=np.int64)
+    e0 = 30e-9
+    pos = np.zeros((3, n))
+    pos[0], pos[1] = 0.1, 0.13  # off the box's face diagonals, which a ray from the centre would graze
+    parts = scenes.make_particles(1, ids, pos, np.full(n, e0), np.zeros(n), np.full(n, np.pi), np.ones(n))
+    params = workloads.run_params(A.NEUTRON, simtime=300.0, tau=0.0, tmax=9e99, lmax=9e99, bmax=0.0,
+                                  spintimes=(0, 0), seed=1)
+    out, _ = oracle_mod.Oracle(sc).integrate(params, parts)
+    assert np.all(out.stop_id == A.ID_ABSORBED_ON_SURFACE)
+    v0 = np.sqrt((parts.y[3:6, 0] ** 2).sum())
+    en = 0.5 * scenes.M_N * (v0 * v0 + 2 * scenes.GRAV * 0.5)  # normal energy at the floor
+    k1 = np.sqrt(complex(en, 0.0))
+    k2 = np.sqrt(complex(en - 250e-9, -20e-9))
+    p = 1 - abs((k1 - k2) / (k1 + k2)) ** 2 + 1e-3
+    p_hat = n / out.n_hit.sum()
+    sigma = p * np.sqrt((1 - p) / n)
+    assert abs(p_hat - p) < 4 * sigma, (p_hat, p, sigma)
