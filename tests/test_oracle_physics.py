@@ -88,3 +88,58 @@ def test_absorption_per_bounce_matches_the_complex_potential_step(oracle_mod):
     p_hat = n / out.n_hit.sum()
     sigma = p * np.sqrt((1 - p) / n)
     assert abs(p_hat - p) < 4 * sigma, (p_hat, p, sigma)
+
+
+def _floor_drop(oracle_mod, fermi, diff_prob=0.0, n=3000, simtime=0.6, e0=30e-9):
+    """UCN falling vertically from (0.1, 0.13, 0) onto the floor of a 1 m box
+    whose outside (the default solid) has the given Fermi potential.  A UCN
+    leaving the box moves along its outward normal, so the surface properties
+    that apply are the box's own (OnHit takes the leaving solid's material
+    then, src/neutron.cpp:191): the diffuse probability is set there."""
+    from pentrack_gb300 import Scene, scenes, workloads
+    sc = Scene()
+    sc.add_material("floor", fermi)
+    sc.add_material("vacuum", 0.0, diff_prob=diff_prob)
+    sc.add_solid(1, "floor")
+    sc.add_solid(2, "vacuum", scenes.box_mesh((-0.5, -0.5, -0.5), (0.5, 0.5, 0.5)))
+    ids = np.arange(n, dtype=np.int64)
+    pos = np.zeros((3, n))
+    pos[0], pos[1] = 0.1, 0.13
+    parts = scenes.make_particles(2, ids, pos, np.full(n, e0), np.zeros(n), np.full(n, np.pi), np.ones(n))
+    params = workloads.run_params(A.NEUTRON, simtime=simtime, tau=0.0, tmax=9e99, lmax=9e99, bmax=0.0,
+                                  spintimes=(0, 0), seed=2)
+    out, _ = oracle_mod.Oracle(sc).integrate(params, parts)
+    v0 = np.sqrt((parts.y[3:6, 0] ** 2).sum())
+    return parts, out, v0 * v0 + 2 * scenes.GRAV * 0.5  # squared speed at the floor
+
+
+def test_transmission_probability_above_the_potential_step(oracle_mod):
+    """Enormal > Estep (src/neutron.cpp:221-240): reflection with probability
+    |(k1 - k2)/(k1 + k2)|^2 for real k, otherwise transmission into the floor."""
+    from pentrack_gb300 import scenes
+    parts, out, vf2 = _floor_drop(oracle_mod, 50.0)
+    en = 0.5 * scenes.M_N * vf2
+    k1, k2 = np.sqrt(en), np.sqrt(en - 50e-9)
+    R = ((k1 - k2) / (k1 + k2)) ** 2
+    # transmitted UCN fall through the floor and leave the geometry's bounding
+    # box (ID_HIT_BOUNDARIES, CheckSegment); reflected ones are still flying
+    refl = (out.stop_id == A.ID_NOT_FINISH).mean()
+    assert np.all(out.n_hit == 1) and np.all(np.isin(out.stop_id, (A.ID_NOT_FINISH, A.ID_HIT_BOUNDARIES)))
+    assert np.all(out.y[2][out.stop_id == A.ID_NOT_FINISH] > -0.5)
+    assert abs(refl - R) < 4 * np.sqrt(R * (1 - R) / parts.n), (refl, R)
+
+
+def test_lambert_reflection_directions(oracle_mod):
+    """DiffProb 1 (ReflectLambert, src/neutron.cpp:150-183): the outgoing
+    direction about the normal has density cos(theta) sin(theta), so
+    cos^2(theta) is uniform; horizontal velocity is conserved in flight, so
+    sin^2(theta) = v_horizontal^2 / v_floor^2 at the end."""
+    from scipy import stats
+    from pentrack_gb300 import scenes
+    v0 = scenes.speed_from_energy(np.array([30e-9]), scenes.M_N)[0]
+    t1 = (-v0 + np.sqrt(v0 * v0 + scenes.GRAV)) / scenes.GRAV  # the fall of 0.5 m to the floor
+    # stop 1 ms after the bounce: a second floor hit within 1 ms needs cos(theta) < 0.002
+    parts, out, vf2 = _floor_drop(oracle_mod, 250.0, diff_prob=1.0, simtime=t1 + 1e-3)
+    assert (out.n_hit == 1).mean() > 0.998
+    c2 = 1 - (out.y[3] ** 2 + out.y[4] ** 2) / vf2
+    assert stats.kstest(c2, "uniform").pvalue > 1e-3
