@@ -143,3 +143,30 @@ def test_lambert_reflection_directions(oracle_mod):
     assert (out.n_hit == 1).mean() > 0.998
     c2 = 1 - (out.y[3] ** 2 + out.y[4] ** 2) / vf2
     assert stats.kstest(c2, "uniform").pvalue > 1e-3
+
+
+def test_spinflip_per_hit_and_decay_fraction(oracle_mod):
+    """SpinflipProb flips the polarisation at a hit with that probability
+    (src/neutron.cpp:193-196, counted in Nspinflip); with tau the particle
+    decays at an exponentially distributed proper time
+    (src/tracking.cpp:19-26, 144-155)."""
+    from pentrack_gb300 import Scene, scenes, workloads
+    sc = Scene()
+    sc.add_material("wall", 335.0)
+    sc.add_material("vacuum", 0.0, spinflip_prob=0.3)
+    sc.add_solid(1, "wall")
+    sc.add_solid(2, "vacuum", scenes.box_mesh((-0.5, -0.5, -0.5), (0.5, 0.5, 0.5)))
+    n = 3000
+    ids = np.arange(n, dtype=np.int64)
+    pos, (E, ph, th, pol) = scenes.source_box(3, ids, (-0.45, -0.45, -0.45), (0.45, 0.45, 0.45), 0.0, 100e-9)
+    parts = scenes.make_particles(3, ids, pos, E, ph, th, pol)
+    params = workloads.run_params(A.NEUTRON, simtime=5.0, tau=10.0, tmax=9e99, lmax=9e99, bmax=0.0,
+                                  spintimes=(0, 0), seed=3)
+    out, _ = oracle_mod.Oracle(sc).integrate(params, parts)
+    hits = out.n_hit.sum()
+    p = out.n_spinflip.sum() / hits
+    assert hits > 20000 and abs(p - 0.3) < 4 * np.sqrt(0.3 * 0.7 / hits), p
+    dec = (out.stop_id == A.ID_DECAYED).mean()
+    q = 1 - np.exp(-5.0 / 10.0)  # proper time = lab time to 1e-16 for UCN
+    assert np.all(np.isin(out.stop_id, (A.ID_DECAYED, A.ID_NOT_FINISH)))
+    assert abs(dec - q) < 4 * np.sqrt(q * (1 - q) / n), (dec, q)
