@@ -170,3 +170,37 @@ def test_spinflip_per_hit_and_decay_fraction(oracle_mod):
     q = 1 - np.exp(-5.0 / 10.0)  # proper time = lab time to 1e-16 for UCN
     assert np.all(np.isin(out.stop_id, (A.ID_DECAYED, A.ID_NOT_FINISH)))
     assert abs(dec - q) < 4 * np.sqrt(q * (1 - q) / n), (dec, q)
+
+
+def test_cyclotron_orbits_close_after_whole_periods(oracle_mod):
+    """TParticle::EquationOfMotion's Lorentz force with the relativistic factors
+    (src/particle.cpp:105-135): in a uniform 1 T field a 500 eV proton and a
+    500 keV electron started perpendicular to B return to their start point
+    after whole periods 2 pi gamma m / (q B)."""
+    from pentrack_gb300 import Scene, scenes, workloads
+    sc = Scene()
+    sc.add_material("vacuum", 0.0)
+    sc.add_material("detector", 0.0)
+    # charged particles fly in the default solid (any other solid absorbs
+    # them); two small cubes at opposite corners span the geometry's box
+    sc.add_solid(1, "vacuum")
+    corners = np.vstack([scenes.box_mesh((-1, -1, -1), (-0.9, -0.9, -0.9)), scenes.box_mesh((0.9, 0.9, 0.9), (1, 1, 1))])
+    sc.add_solid(2, "detector", corners)
+    sc.add_harmonic([(0, 0, 1.0)])
+    for species, E, m in ((A.PROTON, 500.0, scenes.M_P), (A.ELECTRON, 500e3, scenes.M_E)):
+        ids = np.arange(4, dtype=np.int64)
+        pos = np.tile(np.array([[0.1], [0.13], [0.05]]), (1, 4))
+        parts = scenes.make_particles(4, ids, pos, np.full(4, E), np.linspace(0, 1.5, 4), np.full(4, np.pi / 2),
+                                      np.ones(4), species=species)
+        gamma = 1 + E / (m * scenes.C0 ** 2)
+        period = 2 * np.pi * gamma * m / 1.0  # m in eV s^2/m^2, so q B / m in units of e: omega = B / (gamma m)
+        params = workloads.run_params(species, simtime=5 * period, tau=0.0, tmax=9e99, lmax=9e99, bmax=0.0,
+                                      spintimes=(0, 0), seed=4)
+        out, _ = oracle_mod.Oracle(sc).integrate(params, parts)
+        assert np.all(out.stop_id == A.ID_NOT_FINISH)
+        v = np.sqrt((parts.y[3:6] ** 2).sum(0))
+        r = gamma * m * v / 1.0
+        assert 1e-3 < r[0] < 1e-2
+        dpos = np.sqrt(((out.y[0:3] - parts.y[0:3]) ** 2).sum(0))
+        assert np.all(dpos < 1e-5 * r), (species, dpos / r)
+        np.testing.assert_allclose(np.sqrt((out.y[3:6] ** 2).sum(0)), v, rtol=1e-7)
