@@ -204,3 +204,31 @@ def test_cyclotron_orbits_close_after_whole_periods(oracle_mod):
         dpos = np.sqrt(((out.y[0:3] - parts.y[0:3]) ** 2).sum(0))
         assert np.all(dpos < 1e-5 * r), (species, dpos / r)
         np.testing.assert_allclose(np.sqrt((out.y[3:6] ** 2).sum(0)), v, rtol=1e-7)
+
+
+def test_exb_drift_is_a_straight_line(oracle_mod):
+    """The Lorentz force with a uniform E (EDMStaticEField) and B: a proton
+    moving at the drift velocity E x B / B^2 feels no net force and keeps its
+    velocity (src/particle.cpp:105-135)."""
+    from pentrack_gb300 import Scene, scenes, workloads
+    sc = Scene()
+    sc.add_material("vacuum", 0.0)
+    sc.add_material("detector", 0.0)
+    sc.add_solid(1, "vacuum")
+    corners = np.vstack([scenes.box_mesh((-1, -1, -1), (-0.9, -0.9, -0.9)), scenes.box_mesh((0.9, 0.9, 0.9), (1, 1, 1))])
+    sc.add_solid(2, "detector", corners)
+    sc.add_harmonic([(0, 0, 1.0)])
+    sc.add_uniform_e(1e4, 0.0, 0.0)
+    n = 3
+    pos = np.tile(np.array([[0.1], [0.13], [0.05]]), (1, n))
+    parts = scenes.make_particles(5, np.arange(n, dtype=np.int64), pos, np.full(n, 1.0), np.zeros(n),
+                                  np.full(n, np.pi / 2), np.ones(n), species=A.PROTON)
+    parts.y[3:6] = np.array([[0.0], [-1e4], [0.0]])
+    params = workloads.run_params(A.PROTON, simtime=1e-6, tau=0.0, tmax=9e99, lmax=9e99, bmax=0.0,
+                                  spintimes=(0, 0), seed=5)
+    out, _ = oracle_mod.Oracle(sc).integrate(params, parts)
+    assert np.all(out.stop_id == A.ID_NOT_FINISH)
+    dt = out.t - parts.t
+    np.testing.assert_allclose(out.y[1], parts.y[1] - 1e4 * dt, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(out.y[0], parts.y[0], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(out.y[3:6], parts.y[3:6], rtol=0, atol=1e-3)
