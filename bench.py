@@ -59,14 +59,32 @@ def parse():
 
 
 # ----------------------------------------------------------------------------
+def pci_bus_id(device):
+    """PCI bus ID of CUDA device `device` (cudaDeviceGetPCIBusId, read-only):
+    nvidia-smi numbers GPUs in PCI order and ignores CUDA_VISIBLE_DEVICES, so
+    the clock sampler selects the GPU by bus ID."""
+    import ctypes
+    for name in ("libcudart.so", "libcudart.so.13", "/usr/local/cuda/lib64/libcudart.so"):
+        try:
+            rt = ctypes.CDLL(name)
+        except OSError:
+            continue
+        buf = ctypes.create_string_buffer(64)
+        if rt.cudaDeviceGetPCIBusId(buf, 64, int(device)) == 0:
+            return buf.value.decode()
+    return None
+
+
 class Clocks:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """nvidia-smi clock / throttle sampling during the timed region, on the
+    GPU with the CUDA device's PCI bus ID."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device):
         self.device = device
+        self.bus_id = pci_bus_id(device)
         self.proc = None
         self.path = None
 
@@ -74,13 +92,14 @@ class Clocks:
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+            sel = self.bus_id if self.bus_id else str(self.device)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", sel, f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
                                           "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
     def stop(self):
-        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "pci_bus_id": self.bus_id}
         if self.proc is None:
             return out
         time.sleep(0.25)

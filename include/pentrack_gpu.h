@@ -262,9 +262,11 @@ pt_status pt_segment_collisions(pt_ctx *ctx, int64_t n, const double *seg, int32
  * reference (an addition for callers that must not allocate device memory
  * per call).  Same arguments, results and
  * errors as pt_segment_collisions; device scratch is a fixed 8 MiB array in
- * the library's module, addressed with cudaGetSymbolAddress on the first call
- * on each device (that device current), so make the first call before any
- * stream capture.  Scratch needed: 48 n + 4 n + 44 n max_hits bytes plus
+ * the library's module, addressed with cudaGetSymbolAddress (that device
+ * current) on the first call after each pt_create on the device, so make that
+ * first call before any stream capture.  A cudaDeviceReset invalidates every
+ * context on the device (their scene memory) and with them that address:
+ * create a new context before calling again.  Scratch needed: 48 n + 4 n + 44 n max_hits bytes plus
  * 256-byte alignment per block; larger requests return PT_ERR_INVALID with the
  * sizes in pt_last_error (n = 16384, max_hits = 8 fits).  Not reentrant: every
  * context on a device shares the one scratch array, so calls on the same

@@ -1125,9 +1125,8 @@ struct Tracker {
         return false;
     }
 
-    /* TTracker::IntegrateSpin decision logic (src/tracking.cpp:373-483).  The
-     * Bloch integration itself (LOOP D) is not part of this restatement yet:
-     * particles that would need it stop with ID_ODEINT_ERROR. */
+    /* TTracker::IntegrateSpin decision logic (src/tracking.cpp:373-483); the
+     * Bloch integration (LOOP D) is bloch() below. */
     double integrate_spin(double *spin, double x2, const double *y2) {
         double x1 = st.to;
         const double *y1 = st.xo;
@@ -1490,6 +1489,8 @@ void pto_tricubic_eval(const double *a, double x, double y, double z, int derx, 
 void pto_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) { philox(ctr, key, out); }
 
 double pto_uniform(uint64_t seed, int64_t id, uint64_t draw) { return uniform_draw(seed, id, draw); }
+
+double pto_detpow(double x, double p) { return ptdm_pow(x, p); }
 
 int pto_dopri5_selftest(double t0, const double *y0, double dt0, int nsteps, double *t_out, double *y_out) {
     struct Osc {

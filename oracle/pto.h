@@ -56,6 +56,8 @@ void pto_tricubic_coeff(const double *stacked64, double *a64);
 void pto_tricubic_eval(const double *a64, double x, double y, double z, int derx, int dery, int derz, double *out);
 void pto_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 double pto_uniform(uint64_t seed, int64_t id, uint64_t draw);
+/* the step adjuster's deterministic x^p (include/pt_detmath.h) */
+double pto_detpow(double x, double p);
 /* dopri5 dense-output evaluation of one accepted step of dy/dt = f on a
  * fixed test system (harmonic oscillator with drag); for unit tests. */
 int pto_dopri5_selftest(double t0, const double *y0, double dt0, int nsteps, double *t_out, double *y_out);

@@ -39,6 +39,8 @@ def lib():
         L.pto_philox4x32_10.argtypes = [P(C.c_uint32), P(C.c_uint32), P(C.c_uint32)]
         L.pto_uniform.argtypes = [C.c_uint64, C.c_int64, C.c_uint64]
         L.pto_uniform.restype = C.c_double
+        L.pto_detpow.argtypes = [C.c_double, C.c_double]
+        L.pto_detpow.restype = C.c_double
         L.pto_dopri5_selftest.argtypes = [C.c_double, dp, C.c_double, C.c_int, dp, dp]
         _LIB = L
     return _LIB

@@ -58,6 +58,14 @@ def build_engine(force=False, verbose=False):
     return LIB
 
 
+def reference_tree():
+    """The reference source tree the oracle recipe compiles ALGLIB/libtricubic
+    from: $PENTRACK_REFERENCE, else the read-only mount of the build container;
+    None when absent (as on a machine that only runs the prebuilt checker)."""
+    path = os.environ.get("PENTRACK_REFERENCE", "/root/reference")
+    return path if os.path.isdir(path) else None
+
+
 def build_oracle(force=False):
     """Compile the CPU oracle (test infrastructure) and, when the reference
     tree is present, the reference's ALGLIB/libtricubic under oracle/_ref."""
@@ -66,8 +74,9 @@ def build_oracle(force=False):
     if force:
         args.insert(3, "-B")
     _run(args)
-    if os.path.isdir("/root/reference"):
-        _run(["make", "-C", odir, "-j8", "ref"])
+    ref = reference_tree()
+    if ref:
+        _run(["make", "-C", odir, "-j8", "ref", f"REF={ref}"])
 
 
 if __name__ == "__main__":

@@ -191,7 +191,7 @@ def source_from_config(config_path, n, seed, first_id=0, inside_stl=None, scene=
                               float(get("pulseGap", "0") or 0) if "pulseWidth" in sc and "pulseGap" in sc else 0.0,
                               float(get("pulseWidth", "0") or 0) if "pulseWidth" in sc and "pulseGap" in sc else 0.0)
     draw = lambda k, sel=ids: S._draw(seed, sel, k)
-    spectrum = lambda sd, sel: spec(S._draw(sd, sel, 4))
+    spectrum = lambda sd, sel, k=4: spec(S._draw(sd, sel, k))
     stl = None
     if mode in ("STLvolume", "STLsurface"):
         path = get("STLfile").split()[0]

@@ -63,10 +63,17 @@ struct pt_ctx {
 static __device__ __align__(256) unsigned char g_noalloc_scratch[PT_NOALLOC_SCRATCH_BYTES];
 
 namespace {
-/* device address of g_noalloc_scratch, resolved once per device with that
- * device current */
+/* device address of g_noalloc_scratch, resolved with that device current on
+ * the first no-alloc call after a pt_create on the device (pt_create clears
+ * the entry: a context created after a cudaDeviceReset must not inherit the
+ * address of the module's previous load) */
 std::mutex g_noalloc_mu;
 unsigned char *g_noalloc_addr[64] = {};
+void noalloc_forget(int device) {
+    if (device < 0 || device >= 64) return;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    g_noalloc_addr[device] = nullptr;
+}
 cudaError_t noalloc_scratch(int device, unsigned char **out) {
     if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
@@ -132,6 +139,33 @@ DSpecies make_species(int s) {
     return d;
 }
 
+/* Host-side checks of the materials (the reference's operator>> for
+ * material, src/geometry.cpp:10-52): probabilities in 0..1 and at most one
+ * diffuse-reflection model (Lambert, MicroRoughness, modified Lambert); run
+ * by pt_create before it touches a device. */
+pt_status validate_materials(const pt_scene_desc *d, std::string &err) {
+    if (!d || d->n_materials < 0 || (d->n_materials > 0 && !d->materials)) { err = "materials missing"; return PT_ERR_INVALID; }
+    for (int i = 0; i < d->n_materials; ++i) {
+        const pt_material &m = d->materials[i];
+        if (m.diff_prob < 0 || m.diff_prob > 1 || m.spinflip_prob < 0 || m.spinflip_prob > 1 || m.modified_lambert_prob < 0 ||
+            m.modified_lambert_prob > 1 || m.loss_per_bounce < 0 || m.loss_per_bounce > 1) {
+            err = "material " + std::to_string(i) + ": probability outside 0..1";
+            return PT_ERR_INVALID;
+        }
+        const int models = (m.diff_prob != 0) + (m.rms_roughness != 0 || m.correl_length != 0) + (m.modified_lambert_prob != 0);
+        if (models > 1) {
+            err = "You have set parameters for more than one diffuse-reflection model for material " + std::to_string(i) +
+                  "! Now I don't know which to use.";
+            return PT_ERR_INVALID;
+        }
+        if (m.rms_roughness != 0 || m.correl_length != 0) {
+            err = "material " + std::to_string(i) + ": MicroRoughness materials are not implemented on the device path";
+            return PT_ERR_UNSUPPORTED;
+        }
+    }
+    return PT_OK;
+}
+
 pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
     cudaError_t e = cudaSuccess;
     std::string &err = c->err;
@@ -143,10 +177,6 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
     std::vector<DMat> mats(d->n_materials);
     for (int i = 0; i < d->n_materials; ++i) {
         const pt_material &m = d->materials[i];
-        if (m.rms_roughness != 0 || m.correl_length != 0) { err = "MicroRoughness materials are not implemented on the device path"; return PT_ERR_UNSUPPORTED; }
-        if (m.diff_prob < 0 || m.diff_prob > 1 || m.spinflip_prob < 0 || m.spinflip_prob > 1 || m.loss_per_bounce < 0 || m.loss_per_bounce > 1) {
-            err = "material probability outside 0..1"; return PT_ERR_INVALID;
-        }
         mats[i] = DMat{m.fermi_real, m.fermi_imag, m.diff_prob, m.spinflip_prob, m.internal_bfield, m.modified_lambert_prob, m.loss_per_bounce};
     }
     /* solids */
@@ -557,6 +587,10 @@ const char *pt_last_error(const pt_ctx *ctx) { return ctx ? ctx->err.c_str() : g
 pt_status pt_create(const pt_scene_desc *scene, int32_t device, pt_ctx **out) {
     if (!out) return PT_ERR_INVALID;
     *out = nullptr;
+    {
+        pt_status vs = validate_materials(scene, g_create_err);
+        if (vs != PT_OK) return vs;
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         g_create_err = "no CUDA device";
@@ -566,6 +600,7 @@ pt_status pt_create(const pt_scene_desc *scene, int32_t device, pt_ctx **out) {
     std::unique_ptr<pt_ctx> c(new pt_ctx());
     c->device = device;
     if (!ck(nullptr, cudaSetDevice(device), "cudaSetDevice")) return PT_ERR_CUDA;
+    noalloc_forget(device);
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     pt_status st = build_scene(c.get(), scene);
     if (st != PT_OK) {

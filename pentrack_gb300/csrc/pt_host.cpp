@@ -240,6 +240,11 @@ pt_status load_scene(const std::string &config_path, SceneStore &S, std::string 
             err = "You set a probability outside range 0..1 for material " + kv.first + "!";
             return PT_ERR_INVALID;
         }
+        if ((m.diff_prob != 0) + (m.rms_roughness != 0 || m.correl_length != 0) + (m.modified_lambert_prob != 0) > 1) {
+            err = "You have set parameters for more than one diffuse-reflection model for material " + kv.first +
+                  "! Now I don't know which to use.";
+            return PT_ERR_INVALID;
+        }
         known[kv.first] = m;
     }
     auto material_index = [&](const std::string &name, int &idx) -> bool {

@@ -319,8 +319,10 @@ def electron_beta_spectrum(E):
 def spectrum_sampler(f, emin, emax, tries=256, first_draw=1000):
     """Rejection sampling of the spectrum f (max < 1) on [emin, emax], as the
     reference's source does for its spectrum formula; draw pairs come from the
-    particle's own Philox stream, so samples do not depend on the batch."""
-    def sample(seed, ids):
+    particle's own Philox stream, so samples do not depend on the batch.
+    The sampler's draws start at counter `first_draw` and use at most
+    2 x `tries` counters."""
+    def sample(seed, ids, first_draw=first_draw):
         ids = np.asarray(ids, dtype=np.int64)
         E = np.full(len(ids), np.nan)
         todo = np.ones(len(ids), bool)

@@ -29,6 +29,8 @@ _ROUND_STRIDE = 16
 _VOL_BASE = 2000        # STL-volume points: 3 coordinates per round
 _H_BASE = 1 << 20       # total-energy rounds
 _PS_BASE = 1 << 22      # phase-space rounds: time, polarisation, acceptance
+_SPEC_BASE = 1 << 60    # spectrum redraws of the total-energy rounds ...
+_SPEC_STRIDE = 1 << 12  # ... each round's draws in its own counter block
 
 
 def _point_base(r):
@@ -105,7 +107,9 @@ def phase_space_volume_source(seed, ids, random_point, potential, emin, emax, sp
     """TVolumeSource with PhaseSpaceWeighting.  `random_point(seed, ids, base)`
     gives points (3, n) in the source volume from draws at counter `base` on,
     `potential(t, pos, pol)` the potential energy there (rest_energy_potential),
-    `spectrum(seed, ids)` total energies (default uniform on [emin, emax]);
+    `spectrum(seed, ids, counter)` total energies from draws at `counter` on
+    (default uniform on [emin, emax]; round r redraws at _SPEC_BASE +
+    r _SPEC_STRIDE, keeping the particle's own id and stream);
     `direction(seed, ids)` -> (phi, theta) and `times(seed, ids, counter)`
     replace the default uniform azimuth, sine-distributed polar angle and
     uniform start time on t_range.  Returns (ParticleSet, Vmin)."""
@@ -137,7 +141,7 @@ def phase_space_volume_source(seed, ids, random_point, potential, emin, emax, sp
         if spectrum is None:
             h = emin + S._draw(seed, ids[todo], k) * (emax - emin)
         else:
-            h = spectrum(seed, ids[todo] + (np.int64(r) << np.int64(40)))
+            h = spectrum(seed, ids[todo], _SPEC_BASE + r * _SPEC_STRIDE)
         ok = h >= vmin
         H[todo[ok]] = h[ok]
         todo = todo[~ok]

@@ -1,7 +1,7 @@
 """Generate the golden vectors under tests/golden from the reference's own code.
 
-Run here, where the reference tree exists:  python tests/golden/gen_golden.py
-It builds oracle/_ref/libptref.so (`make -C oracle ref`), i.e. the vendored
+Run where the reference tree exists:  python tests/golden/gen_golden.py [REFERENCE_TREE]
+(default: $PENTRACK_REFERENCE, else the build container's read-only mount).  It builds oracle/_ref/libptref.so (`make -C oracle ref`), i.e. the vendored
 ALGLIB 3.15.0 and libtricubic sources of the reference compiled in place, and
 records:
   alglib_spline.npz   spline1dgriddiffcubic(x, y) on uniform and random grids
@@ -24,7 +24,11 @@ sys.path.insert(0, ROOT)
 
 
 def main():
-    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref"], check=True)
+    from pentrack_gb300.build import reference_tree
+    tree = sys.argv[1] if len(sys.argv) > 1 else reference_tree()
+    if not tree or not os.path.isdir(tree):
+        sys.exit("reference tree not found: pass its path or set PENTRACK_REFERENCE")
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref", f"REF={tree}"], check=True)
     from oracle import pyoracle
     from pentrack_gb300 import scenes
 
@@ -61,7 +65,7 @@ def main():
             ev[i, j] = R.ref_tricubic_eval(dp(a), pts[i, 0], pts[i, 1], pts[i, 2], *der)
     np.savez_compressed(os.path.join(HERE, "tricubic.npz"), x=X, a=Acoef, pts=pts, eval=ev)
 
-    ref = "/root/reference/test"
+    ref = os.path.join(tree, "test")
     hollow = scenes.read_stl(os.path.join(ref, "HollowUnitCube.STL"))
     cube = scenes.read_stl(os.path.join(ref, "UnitCubeCenteredOn(0,0,0).STL"))
     axes, comps = scenes.read_opera3d(os.path.join(ref, "VerticalLinearGradientField3D.tab"), 0.01)

@@ -45,7 +45,7 @@ MATERIALS = """[MATERIALS]
 default 250 0 0.05 0 0 0 0 0 1e-4
 vacuum  0 0 0 0 0 0
 wall    183 0.0852 0.1 1e-5 0 0 0 0 0
-unused  54 0.003 0.2 1e-5 2.6e-9 20e-9 0 0 0
+unused  54 0.003 0 1e-5 2.6e-9 20e-9 0 0 0
 """
 
 
@@ -134,6 +134,41 @@ def test_config_errors(built, tmp_path):
     bad.write_text(CONFIG.replace("block.STL    wall", "block.STL    nosuch"))
     with pytest.raises(EngineError, match="not defined"):
         ConfigScene(bad)
+    # at most one diffuse-reflection model per material (src/geometry.cpp:40-47)
+    (tmp_path / "materials.in").write_text(MATERIALS.replace("wall    183 0.0852 0.1 1e-5 0 0 0 0 0",
+                                                            "wall    183 0.0852 0.1 1e-5 0 0 0 0.2 0"))
+    with pytest.raises(EngineError, match="more than one diffuse-reflection model") as ex:
+        ConfigScene(tmp_path / "config.in")
+    assert ex.value.status == A.PT_ERR_INVALID
+    (tmp_path / "materials.in").write_text(MATERIALS.replace("wall    183 0.0852 0.1 1e-5 0 0 0 0 0",
+                                                            "wall    183 0.0852 0.1 1e-5 0 0 0 1.5 0"))
+    with pytest.raises(EngineError, match="outside range 0..1"):
+        ConfigScene(tmp_path / "config.in")
+
+
+@pytest.mark.parametrize("change,status,match", [
+    ({"diff_prob": 0.1, "modified_lambert_prob": 0.2}, A.PT_ERR_INVALID, "more than one diffuse-reflection model"),
+    ({"diff_prob": 0.1, "rms_roughness": 1e-9}, A.PT_ERR_INVALID, "more than one diffuse-reflection model"),
+    ({"modified_lambert_prob": 1.5}, A.PT_ERR_INVALID, "outside 0..1"),
+    ({"modified_lambert_prob": -0.1}, A.PT_ERR_INVALID, "outside 0..1"),
+    ({"rms_roughness": 1e-9, "correl_length": 2e-8}, A.PT_ERR_UNSUPPORTED, "MicroRoughness"),
+])
+def test_pt_create_rejects_invalid_materials(built, change, status, match):
+    """pt_create checks the materials on the host before it looks for a
+    device, so these rejections hold with or without a GPU."""
+    from pentrack_gb300 import Engine, Scene, scenes
+    from pentrack_gb300.engine import EngineError
+    cols = {"fermi_real": 250.0, "fermi_imag": 0.0, "diff_prob": 0.0, "spinflip_prob": 0.0, "rms_roughness": 0.0,
+            "correl_length": 0.0, "internal_bfield": 0.0, "modified_lambert_prob": 0.0, "loss_per_bounce": 0.0}
+    cols.update(change)
+    sc = Scene()
+    sc.add_material("wall", *cols.values())
+    sc.add_material("vacuum", 0.0)
+    sc.add_solid(1, "wall")
+    sc.add_solid(2, "vacuum", scenes.box_mesh((-0.5, -0.5, -0.5), (0.5, 0.5, 0.5)))
+    with pytest.raises(EngineError, match=match) as ex:
+        Engine(sc)
+    assert ex.value.status == status
 
 
 def test_3dtable_units(built, tmp_path):
