@@ -54,6 +54,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-fp64-line", action="store_true", help="skip the FP64-field batched sub-record")
     p.add_argument("--e2e-steps", type=int, default=2)
     return p.parse_args()
 
@@ -189,6 +190,29 @@ def plain_run(args, rank):
             "events": {"rk_accepted": st["rk_accepted"], "hits": st["hits"]}}
 
 
+def field_fp64_run(args, rank):
+    """The batched form in the FP64 field mode (the tricubic evaluated in FP64
+    as the reference does) on the same workload: the FP32 field mode's gain
+    made visible in the same line."""
+    from pentrack_gb300 import _abi as A
+    import torch
+    engine, params, parts, device = setup_ours(args, rank)
+    params.field_precision = A.PREC_FP64
+    batch = engine.batch(params, parts)
+    for _ in range(args.warmup):
+        batch.advance(max_steps=args.batch_steps)
+    torch.cuda.synchronize(device)
+    psec = ms = 0.0
+    steps = max(3, args.steps // 2)
+    for _ in range(steps):
+        st = batch.advance(max_steps=args.batch_steps)
+        psec += st["particle_seconds"]
+        ms += st["span_ms"]
+    out = batch.read()
+    return {"value": psec / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps, "steps": steps,
+            "energy_drift": energy_drift(engine.field, parts, out)}
+
+
 def cpu_baseline(args, T, n_hint=2048):
     """The oracle (FP64 CPU restatement of the reference path) on all host cores,
     on the first ids of the same workload tracked over 0-T s, T the lab-time
@@ -216,12 +240,15 @@ def cpu_baseline(args, T, n_hint=2048):
         m = int(min(1 << 20, m * max(2.0, args.cpu_seconds / max(dt, 1e-3))))
     return {"value": total_ps / total_s, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"oracle on {cores} threads: first {m} UCN of the workload tracked over 0-{T:g} s "
-                      f"({total_ps:.4g} particle-s in {total_s:.2f} s)"}
+                      f"({total_ps:.4g} particle-s in {total_s:.2f} s)",
+            "energy_drift": energy_drift(orc.field, parts, out)}
 
 
-def energy_drift(engine, parts, out):
+def energy_drift(field, parts, out):
     """(H_end - H_start)/(t_end - t_start) per particle [eV/s] for particles
-    still stored: H = Ekin + m g z - pol mu |B| (+ Fermi potential, 0 inside)."""
+    still stored: H = Ekin + m g z - pol mu |B| (+ Fermi potential, 0 inside);
+    `field` evaluates B at (x, y, z, t) rows (the engine's FP64 field, or the
+    oracle's for the oracle's own run)."""
     from pentrack_gb300 import scenes
     live = out.stop_id == 0
     if live.sum() == 0:
@@ -233,7 +260,7 @@ def energy_drift(engine, parts, out):
     def H(t, y):
         v2 = (y[3:6] ** 2).sum(0)
         q = np.column_stack([y[0], y[1], y[2], t])
-        B = engine.field(q)[0]
+        B = field(q)[0]
         return 0.5 * m * v2 * (1 + 0.75 * v2 / c2) + m * scenes.GRAV * y[2] - y[7] * (scenes.MU_N / scenes.ELE_E) * np.sqrt((B ** 2).sum(1))
 
     h0 = H(parts.t[idx], parts.y[:, idx])
@@ -419,7 +446,9 @@ def run_ours(args, rank, world):
     }
     if not args.no_plain and args.mode == "batched":
         line["plain_form"] = plain_run(args, rank)
-    line["energy_drift"] = energy_drift(engine, parts, out_state)
+    line["energy_drift"] = energy_drift(engine.field, parts, out_state)
+    if not args.no_fp64_line and args.precision == "fp32" and args.mode == "batched":
+        line["field_fp64"] = field_fp64_run(args, rank)
     if not args.no_e2e:
         try:
             line["e2e"] = e2e_run(args, engine, params, rank, span_step)
@@ -427,6 +456,9 @@ def run_ours(args, rank, world):
             line["e2e"] = {"error": str(ex)}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, span_total)
+        # the energy drift of the FP64 CPU oracle over the same lab-time span, beside the GPU's
+        line["energy_drift"] = {"gpu": line["energy_drift"], "oracle": line["cpu_baseline"]["energy_drift"],
+                                "unit": "eV/s per particle, |H_end - H_start| / (t_end - t_start), stored UCN"}
     return line
 
 

@@ -5,10 +5,16 @@ cube_storage        closed 1 m cube (12 triangles) centred at the origin, gravit
 field_storage       closed cylinder R = 0.2 m, z in [-0.05, 0.05] m, 256 segments
                     (1,024 triangles), 64^3 OPERA3D-style table of the quadrupole
                     B = (7.5 y, 7.5 x, 1e-5) T padded by one cell, 250 neV walls with
-                    5 % Lambert and 1e-4 loss per bounce, tau = 880 s, 0-250 neV,
-                    50/50 spin states, 200 s
+                    5 % Lambert and 1e-4 loss per bounce (surface columns on the
+                    cylinder's vacuum material, where the reference's OnHit reads
+                    them), tau = 880 s, 0-250 neV, 50/50 spin states, 200 s
 integration_test    the reference's test/IntegrationTest with the 3D table only:
                     linear gradient dBz/dz = 0.5 T/m in a hollow unit cube
+adjoint_spin        closed cylinder R = 0.2 m, z in [-0.06, 0.06] m, 512 segments
+                    (2,048 triangles), B0 = 1 uT along z plus 8 harmonic terms
+                    (l <= 2, G ~ N(0, (1e-10 T/m^l)^2)), E = 1e6 V/m along z,
+                    specular 335 neV walls, 0-200 neV UCN with spins along x,
+                    100 s of Bloch integration
 """
 import numpy as np
 
@@ -62,10 +68,20 @@ def quadrupole_table(n=64, r=0.2, h=0.1, grad=7.5, b0=1e-5):
     return (x, x.copy(), z), (grad * Y, grad * X, np.full_like(X, b0))
 
 
+def storage_vacuum(diff_prob, loss_per_bounce):
+    """The material of a vacuum solid whose surface is a storage wall.  The
+    reference applies the surface columns (diffuse probability, loss per
+    bounce, spin flip) of the solid whose surface is hit (TNeutron::OnHit,
+    src/neutron.cpp:192): a particle inside the vacuum solid hits that
+    solid's own surface, so the wall's surface properties sit on the vacuum
+    material while the default medium supplies the Fermi potential step."""
+    return ("vacuum", 0.0, 0.0, diff_prob, 0.0, 0.0, 0.0, 0.0, 0.0, loss_per_bounce)
+
+
 def field_storage_scene(table_n=64, nseg=256):
     sc = Scene()
     sc.add_material("wall", 250.0, 0.0, 0.05, 0.0, 0.0, 0.0, 0.0, 0.0, 1e-4)
-    sc.add_material("vacuum", 0.0)
+    sc.add_material(*storage_vacuum(0.05, 1e-4))
     sc.add_solid(1, "wall")
     sc.add_solid(2, "vacuum", S.cylinder_mesh(0.2, -0.05, 0.05, nseg))
     (x, y, z), (bx, by, bz) = quadrupole_table(table_n)
@@ -173,6 +189,49 @@ def mixed_species(n_protons=100_000, n_electrons=100_000, seed=1003, tmax=1e-3):
     return sc, out
 
 
+def harmonic_terms_l2(seed=1004, n_terms=8, sigma=1e-10):
+    """Eight (l, m) slots of the fifteen with l <= 2, picked deterministically
+    from the seed, with coefficients G ~ N(0, (sigma T/m^l)^2)."""
+    slots = [(l, m) for l in range(3) for m in range(-l - 1, l + 2)]
+    rng = np.random.default_rng(seed)
+    pick = sorted(rng.choice(len(slots), n_terms, replace=False))
+    return [(slots[k][0], slots[k][1], float(rng.normal(0.0, sigma))) for k in pick]
+
+
+def adjoint_spin_scene(nseg=512, terms=None, b0=1e-6, ez=1e6):
+    """The adjoint-spin scene: closed cylinder R = 0.2 m, z in [-0.06, 0.06]
+    (nseg azimuthal segments, 4 nseg triangles), 335 neV specular walls, a
+    uniform B0 along z (the harmonic l = 0, m = 0 term, field 0), the harmonic
+    terms whose coefficients the gradients are taken with respect to (field 1)
+    and the uniform E = (0, 0, ez) (EDMStaticEField)."""
+    sc = Scene()
+    sc.add_material("wall", 335.0)
+    sc.add_material("vacuum", 0.0)
+    sc.add_solid(1, "wall")
+    sc.add_solid(2, "vacuum", S.cylinder_mesh(0.2, -0.06, 0.06, nseg))
+    sc.add_harmonic([(0, 0, b0)])
+    sc.add_harmonic(harmonic_terms_l2() if terms is None else terms)
+    sc.add_uniform_e(0.0, 0.0, ez)
+    return sc
+
+
+def adjoint_spin(n=10_000, seed=1004, simtime=100.0, terms=None, first_id=0, nseg=512):
+    """The adjoint-spin workload: UCN uniform in the cylinder (r < 0.19 m,
+    |z| < 0.05 m), 0-200 neV isotropic, polarisation +1, spins along +x
+    (the configuration's override of the reference's random azimuth about
+    B), Bloch integration over the whole run (spintimes 0 simtime, Bmax 1 T),
+    no decay."""
+    sc = adjoint_spin_scene(nseg=nseg, terms=terms)
+    ids = np.arange(first_id, first_id + n, dtype=np.int64)
+    pos, (E, ph, th, pol) = S.source_cylinder(seed, ids, 0.0, 0.19, -0.05, 0.05, 0.0, 200e-9, polarization=1.0)
+    parts = S.make_particles(seed, ids, pos, E, ph, th, pol)
+    parts.spin[:] = 0.0
+    parts.spin[0] = 1.0
+    params = run_params(A.NEUTRON, simtime=simtime, tau=0.0, tmax=9e99, lmax=9e99, bmax=1.0, spintimes=(0.0, simtime),
+                        seed=seed)
+    return sc, params, parts
+
+
 def multipole_table(n=128, lo=(-1.15, -1.15, -0.55), hi=(1.15, 1.15, 0.55), g1=0.43, g2=0.22, b0=0.05):
     """n^3 grid of the curl- and divergence-free multipole
     B = (g1 y + 2 g2 x y, g1 x + g2 (x^2 - y^2), b0) = grad(g1 x y + g2 (x^2 y - y^3/3) + b0 z),
@@ -192,7 +251,7 @@ def large_mesh_scene(table_n=128, nu=500, nv=160, nlat=101, nlon=200):
     boolean the workload generator does not have)."""
     sc = Scene()
     sc.add_material("wall", 250.0, 0.0, 0.1, 0.0, 0.0, 0.0, 0.0, 0.0, 3e-5)
-    sc.add_material("vacuum", 0.0)
+    sc.add_material(*storage_vacuum(0.1, 3e-5))
     sc.add_solid(1, "wall")
     sc.add_solid(2, "vacuum", S.torus_mesh(1.0, 0.1, nu, nv, noise=0.05, seed=1005))
     sc.add_solid(3, "vacuum", S.sphere_mesh(0.5, nlat, nlon))

@@ -192,10 +192,11 @@ def compare_states(gpu, orc, pos_tol=1e-6, vel_tol=1e-6):
 
 
 def test_cube_storage_parity(eng, oracle_mod):
-    """The closed unit cube (gravity, specular 335 neV walls, 0-200 neV UCN):
+    """The plain-method configuration at its stated size: 10,000 UCN in the
+    closed unit cube (gravity, specular 335 neV walls, 0-200 neV) for 100 s,
     per-particle end states within 1e-6 of the oracle."""
     from pentrack_gb300 import workloads
-    sc, params, parts = workloads.cube_storage(n=2000, simtime=100.0)
+    sc, params, parts = workloads.cube_storage(n=10_000, simtime=100.0)
     gout, gst = eng(sc).integrate(params, parts)
     oout, ost = oracle_mod.Oracle(sc).integrate(params, parts)
     dpos, dvel = compare_states(gout, oout)
