@@ -49,8 +49,10 @@ def parse():
     p.add_argument("--batch-steps", type=int, default=32, help="accepted RK steps per particle per bench step")
     p.add_argument("--precision", default="fp32", choices=["fp64", "fp32"],
                    help="field evaluation: fp64, or fp32 = FP32 node table (linear base + FP32 Hermite remainder)")
-    p.add_argument("--mode", default="batched", choices=["plain", "batched"])
+    p.add_argument("--mode", default="batched", choices=["plain", "batched", "phased"],
+                   help="batched: persistent lanes + device-scheduled CUDA graph; phased: host-driven phase split")
     p.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison run")
+    p.add_argument("--no-phased", action="store_true", help="skip the host-driven phase-split comparison run")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -166,7 +168,7 @@ def setup_ours(args, rank):
     first, count = replicas.shard(args.n, rank)
     _, params, parts = make_workload(args, count, engine=engine, first_id=first, scene=scene)
     params.field_precision = A.PREC_FP32 if args.precision == "fp32" else A.PREC_FP64
-    params.mode = A.MODE_BATCHED if args.mode == "batched" else A.MODE_PLAIN
+    params.mode = {"batched": A.MODE_BATCHED, "phased": A.MODE_PHASED, "plain": A.MODE_PLAIN}[args.mode]
     return engine, params, parts, device
 
 
@@ -188,6 +190,29 @@ def plain_run(args, rank):
         ms += st["span_ms"]
     return {"value": psec / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / args.steps,
             "events": {"rk_accepted": st["rk_accepted"], "hits": st["hits"]}}
+
+
+def form_run(args, rank, mode):
+    """Another scheduling form on the same workload and precision (the
+    host-driven phase split), timed like the headline."""
+    from pentrack_gb300 import _abi as A
+    import torch
+    engine, params, parts, device = setup_ours(args, rank)
+    params.mode = {"phased": A.MODE_PHASED, "plain": A.MODE_PLAIN, "batched": A.MODE_BATCHED}[mode]
+    batch = engine.batch(params, parts)
+    for _ in range(args.warmup):
+        batch.advance(max_steps=args.batch_steps)
+    torch.cuda.synchronize(device)
+    psec = ms = 0.0
+    steps = max(3, args.steps // 2)
+    launches = 0
+    for _ in range(steps):
+        st = batch.advance(max_steps=args.batch_steps)
+        psec += st["particle_seconds"]
+        ms += st["span_ms"]
+        launches += st["launches"] + st["aux_launches"]
+    return {"value": psec / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps, "steps": steps,
+            "gpu_launches_per_step_batch": launches / steps}
 
 
 def field_fp64_run(args, rank):
@@ -340,11 +365,11 @@ def run_ours(args, rank, world):
     clocks = Clocks(device)
     clocks.start()
     agg = None
-    try_kernel = "k_try"
+    try_kernel = "k_run" if args.mode == "batched" else "k_try"
     t0 = time.perf_counter()
     for _ in range(args.steps):
         st = batch.advance(max_steps=args.batch_steps)
-        if str(st["dominant_kernel"]).startswith("k_try"):
+        if str(st["dominant_kernel"]).startswith(("k_try", "k_run")):
             try_kernel = st["dominant_kernel"]
         if agg is None:
             agg = dict(st)
@@ -371,41 +396,51 @@ def run_ours(args, rank, world):
     span_total = float(np.median(out_state.t[live] - parts.t[live])) if live.any() else 1.0
     span_step = span_total / (args.warmup + args.steps)
     f64, f32 = algorithmic_work(agg, args.precision)
-    if args.mode == "batched":
-        # dominant kernel of the batched form is k_try: one RK try per particle
-        tries = agg["rk_accepted"] + agg["rk_rejected"]
-        field_per_rhs = 1248
-        # FP32 field mode: the table is evaluated entirely in FP32, so only the
-        # RK stage algebra and the equation of motion count as FP64 work
-        try_f64 = tries * (650 + 6 * 60) + (0 if args.precision == "fp32" else tries * 6 * field_per_rhs)
-        launches = max(1, agg["dominant_launches"])
-        kern = {"k_try": agg["try_ms"], "k_post": agg["post_ms"], "k_slow": agg["slow_ms"], "k_bisect": agg["bisect_ms"], "k_plain_tail": agg["tail_ms"]}
+    tries = agg["rk_accepted"] + agg["rk_rejected"]
+    field_per_rhs = 1248
+    # one RK try: stage algebra, error norm and step control (650) plus six
+    # equations of motion (60 each) in FP64; the tricubic B and grad B (1,248
+    # per right-hand side) in FP64 or, in the FP32 field mode, in FP32
+    try_f64 = tries * (650 + 6 * 60) + (0 if args.precision == "fp32" else tries * 6 * field_per_rhs)
+    try_f32 = tries * 6 * field_per_rhs if args.precision == "fp32" else 0
+    state_bytes = None
+    if args.mode in ("batched", "phased"):
+        first = "k_run" if args.mode == "batched" else "k_try"
+        kern = {first: agg["try_ms"], "k_post": agg["post_ms"], "k_slow": agg["slow_ms"], "k_bisect": agg["bisect_ms"],
+                "k_plain_tail": agg["tail_ms"]}
         dom = max(kern, key=kern.get)
+        if dom == first:
+            launches = max(1, agg["sched_outer_iters"] if args.mode == "batched" else agg["dominant_launches"])
+        elif dom in ("k_slow", "k_bisect"):
+            launches = max(1, agg["sched_inner_iters"] if args.mode == "batched" else agg["dominant_launches"])
+        else:
+            launches = max(1, agg["dominant_launches"])
         avg_launch_s = kern[dom] / 1e3 / launches
-        dom_f64 = try_f64 if dom == "k_try" else f64
-        dom_f32 = (tries * 6 * field_per_rhs if args.precision == "fp32" else 0) if dom == "k_try" else f32
+        # k_run: its tries are counted (a lower bound on its work: the fast
+        # step completion and its BVH query add to it); k_try: exactly its tries
+        dom_f64 = try_f64 if dom == first else f64
+        dom_f32 = try_f32 if dom == first else f32
         achieved = dom_f64 / launches / avg_launch_s / 1e12
-        # the try phase runs k_try_tab32 when every field is an FP32 table
-        agg["dominant_kernel"] = try_kernel if dom == "k_try" else dom
+        # the FP32-table-only instances are k_run_tab32 / k_try_tab32
+        agg["dominant_kernel"] = try_kernel if dom == first else dom
+        if args.mode == "phased":
+            # per-particle state a try must move: reads t, y, dydt, dt, ntry, nacc,
+            # nrej, list entry (188 B), writes dt, ntry, nacc, nrej (28 B); an
+            # accepted try also writes yn, dyn, k3..k6, tn, flags, the B cache slot
+            # and a list entry (504 B), a rejected one a list entry (4 B)
+            acc = agg["rk_accepted"] / max(1, tries)
+            state_bytes = (188 + 28 + 504 * acc + 4 * (1 - acc)) * tries / launches
     else:
         launches = max(1, agg["dominant_launches"])
         avg_launch_s = agg["dominant_kernel_ms"] / 1e3 / launches
         achieved = f64 / launches / avg_launch_s / 1e12
         dom_f64, dom_f32 = f64, f32
     traffic = None
-    if args.mode == "batched" and args.workload == "field_storage" and agg["dominant_kernel"].startswith("k_try"):
+    if args.workload == "field_storage" and agg["dominant_kernel"].startswith(("k_try", "k_run")):
         t = load_traffic(agg["dominant_kernel"])
         if t:
             # per launch like `achieved`: bytes per try x tries per average launch
             traffic = (t["dram_read_bytes_per_try"] + t["dram_write_bytes_per_try"]) * tries / launches
-    state_bytes = None
-    if args.mode == "batched":
-        # per-particle state a try must move: reads t, y, dydt, dt, ntry, nacc,
-        # nrej, list entry (188 B), writes dt, ntry, nacc, nrej (28 B); an
-        # accepted try also writes yn, dyn, k3..k6, tn, flags, the B cache slot
-        # and a list entry (504 B), a rejected one a list entry (4 B)
-        acc = agg["rk_accepted"] / max(1, tries)
-        state_bytes = (188 + 28 + 504 * acc + 4 * (1 - acc)) * tries / launches
     line = {
         "metric": METRIC,
         "value": psec_all / device_s,
@@ -429,6 +464,11 @@ def run_ours(args, rank, world):
                    "l2": "per-step particle state > L2 (350 B x 1e6); field table L2-resident by design",
                    "parallelism": f"replicas x{world}", "lab_time_per_step_s": span_step},
         "gpu_launches": int(agg["launches"] + agg["aux_launches"]),
+        "gpu_launches_detail": {"timed_kernels": int(agg["launches"]), "bookkeeping_kernels": int(agg["aux_launches"]),
+                                "graph_launches": int(agg["graph_launches"]),
+                                "scheduler_iterations": int(agg["sched_outer_iters"]),
+                                "slow_rounds": int(agg["sched_inner_iters"]),
+                                "per_step_batch": (agg["launches"] + agg["aux_launches"]) / args.steps},
         "wall_s": elapsed,
         "clocks": clk,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
@@ -442,10 +482,13 @@ def run_ours(args, rank, world):
                                         "bisection_levels", "bvh_nodes", "tri_tests", "subsegments", "dense_evals",
                                         "bisect_max", "bisect_dead", "cand_calls", "cand_overflow", "cand_sum", "tri32_tests")},
         "live_particles": int(agg["active"]),
-        "phase_ms": {"k_try": agg["try_ms"], "k_post": agg["post_ms"], "k_slow": agg["slow_ms"], "k_bisect": agg["bisect_ms"], "k_plain_tail": agg["tail_ms"]},
+        "phase_ms": {("k_run" if args.mode == "batched" else "k_try"): agg["try_ms"], "k_post": agg["post_ms"],
+                     "k_slow": agg["slow_ms"], "k_bisect": agg["bisect_ms"], "k_plain_tail": agg["tail_ms"]},
     }
     if not args.no_plain and args.mode == "batched":
         line["plain_form"] = plain_run(args, rank)
+    if not args.no_phased and args.mode == "batched":
+        line["phased_form"] = form_run(args, rank, "phased")
     line["energy_drift"] = energy_drift(engine.field, parts, out_state)
     if not args.no_fp64_line and args.precision == "fp32" and args.mode == "batched":
         line["field_fp64"] = field_fp64_run(args, rank)

@@ -74,7 +74,11 @@ enum {
 /* scheduling form of the tracking kernels */
 enum {
     PT_MODE_PLAIN = 0,   /* fixed step-batch launches: one lane per particle, K accepted steps per launch */
-    PT_MODE_BATCHED = 1  /* phase-split: converged RK-try launches + hit-resolution launches over work queues */
+    PT_MODE_BATCHED = 1, /* persistent: lanes refilled from a device work queue run the steps without hits
+                            (k_run), hit resolution in work-list launches (k_slow, k_bisect); the whole loop
+                            is a CUDA graph whose iterations the device schedules */
+    PT_MODE_PHASED = 2   /* host-driven phase split: one RK-try launch and one completion launch per
+                            iteration over work lists, the host reading the list counts in between */
 };
 
 /* arithmetic of the field evaluation (the state update, step control and
@@ -162,6 +166,8 @@ typedef struct pt_run_params {
     int32_t block_size;        /* 0 = autotuned */
     int32_t max_launches;      /* 0 = unlimited */
     double timeout_s;          /* host wait limit per call (0 = none) */
+    int32_t max_run;           /* batched form: consecutive steps a lane keeps one particle (0 = step budget only) */
+    int32_t period_iters;      /* batched form: scheduler iterations per graph launch (0 = 64) */
 } pt_run_params;
 
 /* structure-of-arrays particle batch (host memory).  y and spin are
@@ -202,7 +208,8 @@ typedef struct pt_stats {
     double dominant_kernel_ms; /* summed device time of the dominant kernel */
     int64_t dominant_launches;
     char dominant_kernel[48];
-    double try_ms, post_ms, slow_ms; /* batched form: device time per phase kernel */
+    double try_ms, post_ms, slow_ms; /* batched forms: device time per phase kernel (try_ms: k_run in the
+                                        persistent form, k_try in the phased one) */
     int64_t bisect_max;        /* largest number of collision queries of one bisection */
     int64_t cand_calls, cand_overflow, cand_sum; /* candidate-triangle sets built for bisections */
     int64_t tri32_tests;       /* FP32 certified segment-triangle tests */
@@ -211,6 +218,9 @@ typedef struct pt_stats {
     int64_t spin_steps;        /* accepted steps of the spin (Bloch) integration */
     double tail_ms;            /* batched form: device time of the plain-form tail launches */
     int64_t aux_launches;      /* bookkeeping kernel launches (work-list gathers, list-count resets) */
+    int64_t graph_launches;    /* batched form: CUDA graph launches (periods) of the call */
+    int64_t sched_outer_iters; /* batched form: scheduler iterations (k_run launches) */
+    int64_t sched_inner_iters; /* batched form: slow rounds (k_slow + k_bisect launches) */
 } pt_stats;
 
 typedef struct pt_ctx pt_ctx;

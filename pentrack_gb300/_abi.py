@@ -21,7 +21,7 @@ ID_ABSORBED_IN_MATERIAL, ID_ABSORBED_ON_SURFACE = 1, 2
 
 NEUTRON, PROTON, ELECTRON = 0, 1, 2
 FIELD_TAB3D, FIELD_HARMONIC, FIELD_UNIFORM_E, FIELD_SOLENOID = 1, 2, 3, 4
-MODE_PLAIN, MODE_BATCHED = 0, 1
+MODE_PLAIN, MODE_BATCHED, MODE_PHASED = 0, 1, 2
 PREC_FP64, PREC_FP32 = 0, 1
 
 
@@ -67,6 +67,7 @@ class RunParams(C.Structure):
         ("simtime", C.c_double), ("tau", C.c_double), ("tmax", C.c_double), ("lmax", C.c_double), ("bmax", C.c_double),
         ("n_spintimes", C.c_int32), ("steps_per_launch", C.c_int32), ("spintimes", c_double_p),
         ("seed", C.c_uint64), ("block_size", C.c_int32), ("max_launches", C.c_int32), ("timeout_s", C.c_double),
+        ("max_run", C.c_int32), ("period_iters", C.c_int32),
     ]
 
 
@@ -92,6 +93,7 @@ class Stats(C.Structure):
         ("bisect_max", C.c_int64),
         ("cand_calls", C.c_int64), ("cand_overflow", C.c_int64), ("cand_sum", C.c_int64), ("tri32_tests", C.c_int64),
         ("bisect_ms", C.c_double), ("bisect_dead", C.c_int64), ("spin_steps", C.c_int64), ("tail_ms", C.c_double), ("aux_launches", C.c_int64),
+        ("graph_launches", C.c_int64), ("sched_outer_iters", C.c_int64), ("sched_inner_iters", C.c_int64),
     ]
 
     def as_dict(self):

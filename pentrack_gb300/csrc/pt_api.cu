@@ -46,6 +46,7 @@ struct pt_ctx {
     int *cancel_dev = nullptr;
     DCounters *counters = nullptr;
     DCounters *counters_host = nullptr;
+    DSched *sched_host = nullptr;   /* pinned copy of a batch's scheduler state */
     int sm_count = 0;
     /* device arena kept between pt_integrate calls (their batches are
      * created and destroyed inside the call) */
@@ -96,6 +97,8 @@ struct pt_batch {
     std::vector<void *> allocs;   /* owned device memory (one arena) */
     int max_launches = 0;
     double timeout_s = 0;
+    int period_iters = 0;   /* persistent form: outer iterations per graph launch (0 = 64) */
+    int max_run = 0;        /* persistent form: consecutive steps per lane and particle (0 = budget only) */
 };
 
 namespace {
@@ -520,10 +523,10 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
          * next bisection) and k_bisect, while the queue fills the GPU */
         while (slow > 0 && (slow >= std::max(2048, active / 4) || active == 0 || active <= tail)) {
             cudaEventRecord(ev[3], c->stream);
-            k_slow<<<g_slow, block, 0, c->stream>>>(c->scene, R, b, c->counters, out);
+            k_slow<<<g_slow, block, 0, c->stream>>>(c->scene, R, b, c->counters, out, nullptr);
             cudaEventRecord(ev[4], c->stream);
             k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 3, 5, 5);
-            k_bisect<<<g_bisect, block, 0, c->stream>>>(c->scene, R, b, c->counters);
+            k_bisect<<<g_bisect, block, 0, c->stream>>>(c->scene, R, b, c->counters, nullptr);
             cudaEventRecord(ev[5], c->stream);
             k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 4, 4, 4);
             acc.aux_launches += 2;
@@ -576,6 +579,172 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
     return st;
 }
 
+/* Adds a conditional node of `type` to the graph the stream is capturing,
+ * after the captured work so far, and continues the capture after it;
+ * returns the node's body graph. */
+cudaError_t capture_conditional(cudaStream_t s, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type, cudaGraph_t *body) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    const cudaGraphEdgeData *edges = nullptr;
+    size_t nd = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, &edges, &nd);
+    if (e) return e;
+    if (cs != cudaStreamCaptureStatusActive) return cudaErrorIllegalState;
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = type;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    if ((e = cudaGraphAddNode(&node, g, deps, edges, nd, &p))) return e;
+    *body = p.conditional.phGraph_out[0];
+    return cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+}
+
+/* kernel executions of the graph's iterations: sched_begin, regather, run,
+ * after_run, end per outer iteration; slow, zero, bisect, zero, after_slow
+ * per slow round */
+constexpr int PT_GRAPH_OUTER_KERNELS = 5, PT_GRAPH_INNER_KERNELS = 5;
+
+/* Persistent batched form: one CUDA graph per advance call whose outer WHILE
+ * node runs iterations of { rebuild the active list, k_run (lanes refilled
+ * from the list), slow rounds (inner WHILE node: k_slow + k_bisect while
+ * post-steps are queued) }, every decision taken by one-thread scheduling
+ * kernels on the device.  The host launches the graph once per period of at
+ * most `period_iters` iterations (checking cancellation, launch and time
+ * limits between periods) and finishes the last few particles as
+ * plain-form lanes. */
+pt_status advance_persistent(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc, std::chrono::steady_clock::time_point w0,
+                             bool &cancelled, bool &timed_out) {
+    cudaError_t e = cudaSuccess;
+    DBatch &b = B->b;
+    const int64_t n = b.n;
+    const int block = 128;
+    bool tab_only = R.sp.q == 0 && R.prec == PT_PREC_FP32;
+    for (int fi = 0; fi < c->scene.n_fields; ++fi) {
+        const DField &f = c->scene.fields[fi];
+        const bool box = f.xmin < f.xmax && f.ymin < f.ymax && f.zmin < f.zmax;
+        if (f.has_b && !(f.type == PT_FIELD_TAB3D && f.node32 && !(f.bw > 0 && box))) tab_only = false;
+    }
+    const void *run_fn = tab_only ? (const void *)k_run_tab32 : (const void *)k_run;
+    const int g_run = persistent_grid(c, run_fn, block);
+    const int g_slow = persistent_grid(c, (const void *)k_slow, block);
+    const int g_bisect = persistent_grid(c, (const void *)k_bisect, block);
+    const int tail = (int)std::max<int64_t>(2048, n / 1000);
+    const int period_iters = B->period_iters > 0 ? B->period_iters : 64;
+    const int max_run = B->max_run;
+    /* scheduler state and counters */
+    DSched &hs = *c->sched_host;
+    std::memset(&hs, 0, sizeof(hs));
+    for (int k = 0; k < PT_SPANS; ++k) hs.t0[k] = ~0ull;
+    hs.tail = tail;
+    hs.max_iters = period_iters;
+    if ((e = cudaMemcpyAsync(b.sched, &hs, sizeof(DSched), cudaMemcpyHostToDevice, c->stream)) ||
+        (e = cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream)) ||
+        (e = cudaMemsetAsync(b.count, 0, 8 * sizeof(int32_t), c->stream)))
+        return ck(c, e, "persistent setup"), PT_ERR_CUDA;
+    /* budgets count from here; suspended post-steps of an earlier call go to list 3 */
+    k_gather<<<grid_for(n, 256), 256, 0, c->stream>>>(b, R.t_pause, b.list[0], &b.count[0]);
+    acc.aux_launches += 1;
+    /* the graph */
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t gx = nullptr;
+    pt_status st = PT_OK;
+    auto fail = [&](const char *what) {
+        ck(c, e, what);
+        st = PT_ERR_CUDA;
+    };
+    do {
+        if ((e = cudaGraphCreate(&g, 0))) { fail("graph create"); break; }
+        cudaGraphConditionalHandle h_outer, h_slow;
+        if ((e = cudaGraphConditionalHandleCreate(&h_outer, g, 1, cudaGraphCondAssignDefault)) ||
+            (e = cudaGraphConditionalHandleCreate(&h_slow, g, 0, 0))) { fail("graph handles"); break; }
+        cudaGraph_t body_outer = nullptr, body_slow = nullptr;
+        if ((e = cudaStreamBeginCaptureToGraph(c->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal))) { fail("capture"); break; }
+        k_sched_period<<<1, 32, 0, c->stream>>>(b.sched);
+        e = capture_conditional(c->stream, h_outer, cudaGraphCondTypeWhile, &body_outer);
+        cudaGraph_t tmp = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(c->stream, &tmp);
+        if (e || (e = e2)) { fail("capture period"); break; }
+        /* outer body: one iteration */
+        if ((e = cudaStreamBeginCaptureToGraph(c->stream, body_outer, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal))) { fail("capture"); break; }
+        k_sched_begin<<<1, 32, 0, c->stream>>>(b, b.sched);
+        k_regather<<<grid_for(n, 256), 256, 0, c->stream>>>(b, R.t_pause, R.max_steps, b.list[0], &b.count[0]);
+        if (tab_only) k_run_tab32<<<g_run, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched, max_run);
+        else k_run<<<g_run, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched, max_run);
+        k_sched_after_run<<<1, 32, 0, c->stream>>>(b, b.sched, h_slow);
+        e = capture_conditional(c->stream, h_slow, cudaGraphCondTypeWhile, &body_slow);
+        if (!e) k_sched_end<<<1, 32, 0, c->stream>>>(b, b.sched, R, h_outer);
+        e2 = cudaStreamEndCapture(c->stream, &tmp);
+        if (e || (e = e2)) { fail("capture iteration"); break; }
+        /* inner body: one slow round */
+        if ((e = cudaStreamBeginCaptureToGraph(c->stream, body_slow, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal))) { fail("capture"); break; }
+        k_slow<<<g_slow, block, 0, c->stream>>>(c->scene, R, b, c->counters, 1, b.sched);
+        k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 3, 5, 5);
+        k_bisect<<<g_bisect, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched);
+        k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 4, 4, 4);
+        k_sched_after_slow<<<1, 32, 0, c->stream>>>(b, b.sched, R, h_slow);
+        if ((e = cudaStreamEndCapture(c->stream, &tmp))) { fail("capture slow round"); break; }
+        if ((e = cudaGraphInstantiate(&gx, g, 0))) { fail("graph instantiate"); break; }
+    } while (false);
+    if (st == PT_OK) {
+        for (int period = 0;; ++period) {
+            if ((e = cudaGraphLaunch(gx, c->stream))) { fail("graph launch"); break; }
+            acc.graph_launches += 1;
+            if ((e = cudaMemcpyAsync(c->sched_host, b.sched, sizeof(DSched), cudaMemcpyDeviceToHost, c->stream)) ||
+                (e = cudaStreamSynchronize(c->stream))) { fail("persistent period"); break; }
+            if (hs.error) {
+                c->err = "batched scheduler: a slow-round loop exceeded its round limit";
+                st = PT_ERR_CUDA;
+                break;
+            }
+            if (*(volatile int *)c->cancel_host) { cancelled = true; break; }
+            if (hs.last_going <= tail) break;
+            const int64_t kernels = (int64_t)hs.outer_iters * PT_GRAPH_OUTER_KERNELS + (int64_t)hs.inner_iters * PT_GRAPH_INNER_KERNELS;
+            if (B->max_launches > 0 && kernels >= B->max_launches) { timed_out = true; break; }
+            if (B->timeout_s > 0 && std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count() > B->timeout_s) {
+                timed_out = true;
+                break;
+            }
+        }
+    }
+    if (gx) cudaGraphExecDestroy(gx);
+    if (g) cudaGraphDestroy(g);
+    if (st != PT_OK) return st;
+    if ((e = cudaMemcpy(c->counters_host, c->counters, sizeof(DCounters), cudaMemcpyDeviceToHost))) return ck(c, e, "counters"), PT_ERR_CUDA;
+    add_counters(acc, *c->counters_host);
+    const double run_ms = hs.ns[PT_SPAN_RUN] * 1e-6, slow_ms = hs.ns[PT_SPAN_SLOW] * 1e-6, bisect_ms = hs.ns[PT_SPAN_BISECT] * 1e-6;
+    acc.kernel_ms += run_ms + slow_ms + bisect_ms;
+    /* kernel executions inside the graph: the timed kernels (one k_run per
+     * iteration, k_slow + k_bisect per slow round) and the bookkeeping ones
+     * (scheduling kernels, list rebuild, count resets, one per period) */
+    acc.launches += (int64_t)hs.outer_iters + 2 * (int64_t)hs.inner_iters;
+    acc.aux_launches += (int64_t)hs.outer_iters * (PT_GRAPH_OUTER_KERNELS - 1) + (int64_t)hs.inner_iters * (PT_GRAPH_INNER_KERNELS - 2) +
+                        acc.graph_launches;
+    acc.sched_outer_iters = hs.outer_iters;
+    acc.sched_inner_iters = hs.inner_iters;
+    acc.active = hs.last_going;
+    if (!cancelled && !timed_out && hs.last_going > 0) {
+        const double k0 = acc.kernel_ms;
+        st = advance_plain(c, B, R, acc, w0, cancelled, timed_out, true);
+        acc.tail_ms = acc.kernel_ms - k0;
+    }
+    const char *name = tab_only ? "k_run_tab32" : "k_run";
+    double dom = run_ms;
+    int64_t dl = hs.outer_iters;
+    if (slow_ms > dom) { dom = slow_ms; name = "k_slow"; dl = hs.inner_iters; }
+    if (bisect_ms > dom) { dom = bisect_ms; name = "k_bisect"; dl = hs.inner_iters; }
+    acc.dominant_kernel_ms = dom;
+    acc.dominant_launches = dl;
+    std::snprintf(acc.dominant_kernel, sizeof(acc.dominant_kernel), "%s", name);
+    acc.try_ms = run_ms;
+    acc.post_ms = 0;
+    acc.slow_ms = slow_ms;
+    acc.bisect_ms = bisect_ms;
+    return st;
+}
+
 } // namespace
 
 extern "C" {
@@ -615,7 +784,8 @@ pt_status pt_create(const pt_scene_desc *scene, int32_t device, pt_ctx **out) {
         (e = cudaHostAlloc((void **)&c->cancel_host, sizeof(int), cudaHostAllocMapped)) != cudaSuccess ||
         (e = cudaHostGetDevicePointer((void **)&c->cancel_dev, c->cancel_host, 0)) != cudaSuccess ||
         (e = cudaMalloc((void **)&c->counters, sizeof(DCounters))) != cudaSuccess ||
-        (e = cudaHostAlloc((void **)&c->counters_host, sizeof(DCounters), 0)) != cudaSuccess) {
+        (e = cudaHostAlloc((void **)&c->counters_host, sizeof(DCounters), 0)) != cudaSuccess ||
+        (e = cudaHostAlloc((void **)&c->sched_host, sizeof(DSched), 0)) != cudaSuccess) {
         g_create_err = std::string("context setup: ") + cudaGetErrorString(e);
         free_list(c->allocs);
         return PT_ERR_CUDA;
@@ -633,6 +803,7 @@ void pt_destroy(pt_ctx *c) {
     if (c->arena) cudaFree(c->arena);
     if (c->counters) cudaFree(c->counters);
     if (c->counters_host) cudaFreeHost(c->counters_host);
+    if (c->sched_host) cudaFreeHost(c->sched_host);
     if (c->cancel_host) cudaFreeHost(c->cancel_host);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -672,6 +843,7 @@ size_t batch_layout(DBatch &b, int64_t n, unsigned char *base) {
     take(b.bc, 14 * m); take(b.count, 8); take(b.nacc0, m);
     take(b.ps_d, 45 * m); take(b.ps_i, (7 + PT_MAX_CAND) * m);
     for (int k = 0; k < 5; ++k) take(b.list[k], m);
+    take(b.sched, 1);
     return (off + 255) & ~(size_t)255;
 }
 
@@ -691,10 +863,14 @@ pt_status batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles *in
     *out = nullptr;
     if (p->n_spintimes > PT_MAX_SPINTIMES) { c->err = "at most 8 spintimes intervals"; return PT_ERR_UNSUPPORTED; }
     if (p->species < PT_NEUTRON || p->species > PT_ELECTRON) { c->err = "unknown species"; return PT_ERR_INVALID; }
+    if (p->mode != PT_MODE_PLAIN && p->mode != PT_MODE_BATCHED && p->mode != PT_MODE_PHASED) { c->err = "unknown mode"; return PT_ERR_INVALID; }
+    if (p->max_run < 0 || p->period_iters < 0) { c->err = "negative tuning parameter"; return PT_ERR_INVALID; }
     std::unique_ptr<pt_batch> B(new pt_batch());
     B->ctx = c;
     B->max_launches = p->max_launches;
     B->timeout_s = p->timeout_s;
+    B->max_run = p->max_run;
+    B->period_iters = p->period_iters;
     DRun &R = B->run;
     std::memset(&R, 0, sizeof(R));
     R.sp = make_species(p->species);
@@ -783,10 +959,14 @@ pt_status pt_batch_advance_steps(pt_ctx *c, pt_batch *B, double t_pause, int32_t
     pt_status st = PT_OK;
     cudaEventRecord(c->evs0, c->stream);
     if (R.mode == PT_MODE_BATCHED && n > 0) {
+        st = advance_persistent(c, B, R, acc, w0, cancelled, timed_out);
+        if (st != PT_OK) return st;
+    }
+    if (R.mode == PT_MODE_PHASED && n > 0) {
         st = advance_batched(c, B, R, acc, w0, cancelled, timed_out);
         if (st != PT_OK) return st;
     }
-    if (R.mode != PT_MODE_BATCHED && n > 0) {
+    if (R.mode == PT_MODE_PLAIN && n > 0) {
         st = advance_plain(c, B, R, acc, w0, cancelled, timed_out, false);
         if (st != PT_OK) return st;
     }

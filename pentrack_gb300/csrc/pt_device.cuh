@@ -164,12 +164,30 @@ struct DBatch {
     /* work lists of particle indices and their counts */
     int32_t *list[5];            /* 0/1: active (ping-pong), 2: post, 3: slow, 4: bisection */
     int32_t *count;              /* counts of the lists */
+    struct DSched *sched;        /* scheduler state of the persistent batched form */
 };
 
 #define PT_F_BC0 8u   /* cache slot 0 valid */
 #define PT_F_BC1 16u  /* cache slot 1 valid */
 #define PT_F_PENDING 32u /* an accepted try waits for the full post-step logic */
 #define PT_F_SUSPENDED 64u /* that post-step is suspended at a bisection (state in ps_d/ps_i) */
+
+/* Device-side state of the batched form's scheduler (one per batch): loop
+ * counts, the period's iteration cap and tail threshold, and the device time
+ * of the timed kernels (k_run, k_slow, k_bisect) measured on %globaltimer
+ * inside the CUDA graph, where no event can be recorded. */
+enum { PT_SPAN_RUN = 0, PT_SPAN_SLOW = 1, PT_SPAN_BISECT = 2, PT_SPANS = 3 };
+/* Slow rounds of one scheduler iteration before the device loop gives up
+ * with an error (every post-step completes after a bounded number of rounds:
+ * bisections and chord pieces are bounded, see PT_MAX_*; the cap keeps a
+ * logic error from looping on the device). */
+#define PT_MAX_SLOW_ROUNDS (1 << 16)
+struct DSched {
+    int outer_iters, inner_iters, period_start, max_iters;
+    int tail, last_going, last_active, inner_this; /* inner_this: slow rounds of the current iteration */
+    int error, pad2;                                /* error: the slow-round cap was reached */
+    unsigned long long t0[PT_SPANS], t1[PT_SPANS], ns[PT_SPANS], launches[PT_SPANS];
+};
 
 /* device event counters (one set per launch, summed with atomics per block) */
 struct DCounters {

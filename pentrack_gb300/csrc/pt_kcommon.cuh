@@ -49,6 +49,33 @@ static __device__ __forceinline__ void list_push(int32_t *list, int32_t *count, 
     list[base + rank] = v;
 }
 
+/* Device time of the timed kernels inside the batched form's graph: every
+ * block records its start and end on %globaltimer (nanoseconds); the
+ * scheduling kernel after a launch adds max(end) - min(start) to the
+ * kernel's total.  sc == nullptr (host-driven loops, timed with events)
+ * skips it. */
+static __device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+static __device__ __forceinline__ void span_begin(DSched *sc, int k) {
+    if (sc && threadIdx.x == 0) atomicMin(&sc->t0[k], gtimer());
+}
+static __device__ __forceinline__ void span_end(DSched *sc, int k) {
+    if (!sc) return;
+    __syncthreads();
+    if (threadIdx.x == 0) atomicMax(&sc->t1[k], gtimer());
+}
+static __device__ __forceinline__ void span_close(DSched *sc, int k) {
+    if (sc->t1[k] > sc->t0[k] && sc->t0[k] != ~0ull) {
+        sc->ns[k] += sc->t1[k] - sc->t0[k];
+        sc->launches[k] += 1;
+    }
+    sc->t0[k] = ~0ull;
+    sc->t1[k] = 0;
+}
+
 /* a committed particle keeps stepping in this advance call */
 static __device__ __forceinline__ bool keeps_going(const DRun &R, const DBatch &b, const Lane &L, int i) {
     if (L.stop != PT_ID_UNKNOWN || !(L.t < R.t_pause)) return false;

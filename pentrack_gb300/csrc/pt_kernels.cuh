@@ -7,6 +7,10 @@
 
 /* k_try: resident blocks of 128 per SM (register budget 168) */
 #define PT_TRY_BLOCKS_PER_SM 3
+/* k_run: resident blocks of 128 per SM */
+#ifndef PT_RUN_BLOCKS_PER_SM
+#define PT_RUN_BLOCKS_PER_SM 3
+#endif
 
 namespace ptk {
 
@@ -17,8 +21,21 @@ __global__ void k_zero_counts(int32_t *count, int a, int b, int c);
 __global__ void k_try(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out);
 __global__ void k_try_tab32(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out);
 __global__ void k_post(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out);
-__global__ void k_slow(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out);
-__global__ void k_bisect(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C);
+__global__ void k_slow(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out,
+                       DSched *sc);
+__global__ void k_bisect(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C,
+                         DSched *sc);
+__global__ void k_run(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, DSched *sc,
+                      int max_run);
+__global__ void k_run_tab32(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C,
+                            DSched *sc, int max_run);
+__global__ void k_sched_begin(const __grid_constant__ DBatch b, DSched *sc);
+__global__ void k_sched_after_run(const __grid_constant__ DBatch b, DSched *sc, cudaGraphConditionalHandle slow);
+__global__ void k_sched_after_slow(const __grid_constant__ DBatch b, DSched *sc, const __grid_constant__ DRun R,
+                                   cudaGraphConditionalHandle slow);
+__global__ void k_sched_end(const __grid_constant__ DBatch b, DSched *sc, const __grid_constant__ DRun R,
+                            cudaGraphConditionalHandle outer);
+__global__ void k_sched_period(DSched *sc);
 __global__ void k_plain(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int steps,
                         int budget_from_nacc0);
 __global__ void k_fp64_probe(double *out, int iters, double a, double b);

@@ -265,6 +265,21 @@ struct Lane {
             flags |= PT_F_BC0;
         }
     }
+    /* hand-off of an accepted try to the full post-step (persistent form):
+     * slot 0 keeps B at the committed point, slot 1 B at the try's end
+     * point, whichever the lane's cache holds (flags stored by store()) */
+    __device__ void store_bc_handoff(const DBatch &b, int64_t i) {
+        const int k0 = bc_find(y[0], y[1], y[2], t), k1 = bc_find(yn[0], yn[1], yn[2], tn);
+        flags &= ~(PT_F_BC0 | PT_F_BC1);
+        if (k0 >= 0) {
+            bc_write(b, i, 0, k0);
+            flags |= PT_F_BC0;
+        }
+        if (k1 >= 0) {
+            bc_write(b, i, 1, k1);
+            flags |= PT_F_BC1;
+        }
+    }
     /* after an accepted try: keep B at its end point (flags stored separately) */
     __device__ void store_bc_try(const DBatch &b, int64_t i) {
         int k = bc_find(yn[0], yn[1], yn[2], tn);

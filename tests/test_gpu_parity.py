@@ -293,20 +293,50 @@ def test_pause_and_resume_is_bit_identical(eng):
         assert np.array_equal(getattr(one, k), getattr(win, k)), k
 
 
+@pytest.mark.parametrize("mode", [A.MODE_BATCHED, A.MODE_PHASED])
 @pytest.mark.parametrize("precision", [A.PREC_FP64, A.PREC_FP32])
-def test_plain_and_batched_forms_are_bit_identical(eng, precision):
-    """The phase-split batched form schedules the same per-particle arithmetic
-    as the plain form, so every output is bit-identical."""
+def test_plain_and_batched_forms_are_bit_identical(eng, precision, mode):
+    """The batched forms (persistent lanes refilled from a device queue inside
+    a device-scheduled CUDA graph; host-driven phase split) schedule the same
+    per-particle arithmetic as the plain form, so every output is
+    bit-identical."""
     from pentrack_gb300 import workloads
     sc, params, parts = workloads.field_storage(n=4096, simtime=0.4)
     e = eng(sc)
     params.field_precision = precision
     params.mode = A.MODE_PLAIN
     plain, sp = e.integrate(params, parts)
-    params.mode = A.MODE_BATCHED
+    params.mode = mode
     batched, sb = e.integrate(params, parts)
     for k in ("t", "y", "spin", "stop_id", "n_hit", "n_step", "n_spinflip", "h_max", "noflip_prob", "n_accepted",
               "n_rejected", "solid"):
         assert np.array_equal(getattr(plain, k), getattr(batched, k)), k
     assert sp["rk_accepted"] == sb["rk_accepted"]
     assert sb["try_ms"] > 0
+    if mode == A.MODE_BATCHED:
+        assert sb["graph_launches"] >= 1 and sb["sched_outer_iters"] >= 1
+
+
+@pytest.mark.parametrize("max_run,period", [(0, 0), (3, 2), (1, 1)])
+def test_persistent_form_tuning_is_bit_identical(eng, max_run, period):
+    """Hand-back after max_run consecutive steps and short graph periods only
+    change which lane runs a particle when: the results stay the plain
+    form's, in step budgets as the bench uses them."""
+    from pentrack_gb300 import workloads
+    sc, params, parts = workloads.field_storage(n=6000, simtime=0.3)
+    e = eng(sc)
+    params.field_precision = A.PREC_FP32
+    params.mode = A.MODE_PLAIN
+    pb = e.batch(params, parts)
+    for _ in range(3):
+        pb.advance(max_steps=16)
+    plain = pb.read()
+    params.mode = A.MODE_BATCHED
+    params.max_run, params.period_iters = max_run, period
+    bb = e.batch(params, parts)
+    for _ in range(3):
+        st = bb.advance(max_steps=16)
+    batched = bb.read()
+    for k in ("t", "y", "stop_id", "n_hit", "n_step", "h_max", "n_accepted", "n_rejected"):
+        assert np.array_equal(getattr(plain, k), getattr(batched, k)), k
+    assert st["graph_launches"] >= 1
