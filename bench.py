@@ -275,7 +275,8 @@ def energy_drift(field, parts, out):
     `field` evaluates B at (x, y, z, t) rows (the engine's FP64 field, or the
     oracle's for the oracle's own run)."""
     from pentrack_gb300 import scenes
-    live = out.stop_id == 0
+    # stored to the end of the window: still active (0) or stopped at the window's end (ID_NOT_FINISH)
+    live = (out.stop_id == 0) | (out.stop_id == -1)
     if live.sum() == 0:
         return None
     idx = np.nonzero(live)[0][:20000]

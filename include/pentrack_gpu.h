@@ -221,6 +221,8 @@ typedef struct pt_stats {
     int64_t graph_launches;    /* batched form: CUDA graph launches (periods) of the call */
     int64_t sched_outer_iters; /* batched form: scheduler iterations (k_run launches) */
     int64_t sched_inner_iters; /* batched form: slow rounds (k_slow + k_bisect launches) */
+    double adj_forward_ms;     /* pt_adjoint: device time of the recording forward pass(es) */
+    double adj_reverse_ms;     /* pt_adjoint: device time of the reverse sweep */
 } pt_stats;
 
 typedef struct pt_ctx pt_ctx;
@@ -284,6 +286,31 @@ pt_status pt_segment_collisions(pt_ctx *ctx, int64_t n, const double *seg, int32
 pt_status pt_segment_collisions_noalloc(pt_ctx *ctx, int64_t n, const double *seg, int32_t max_hits,
                                         int32_t *count, double *s, double *normal, int32_t *solid_id,
                                         double *distnormal);
+
+/* Gradient of a scalar loss L of the particles' end states with respect to
+ * the coefficients G_k of harmonic field `field` of the scene: the adjoint
+ * (reverse mode) of the whole tracking path of TTracker::IntegrateParticle
+ * with IntegrateSpin (src/tracking.cpp:17-173, 373-483), taken pathwise
+ * along each particle's fixed sequence of specular hits (TNeutron::Reflect,
+ * src/neutron.cpp:99-115): the Dormand-Prince trajectory steps with their
+ * dense output, the reflection map, and the Bloch integration of the spin
+ * (SpinDerivs / SpinPrecessionAxis, src/particle.cpp:141-193) in the
+ * harmonic field (src/harmonicfields.cpp:50-829), with every accepted step
+ * size and bisection bracket frozen (the derivative of the discrete map).
+ * The call runs the forward pass (its end states go to `out` when not
+ * NULL), recording every trajectory step and a Bloch checkpoint every
+ * `checkpoint_interval` accepted spin steps, then the reverse sweep, which
+ * recomputes each chunk of checkpoint_interval spin steps from its
+ * checkpoint.  dL_dspin (5n, component-major like pt_particles.spin) and
+ * dL_dy (9n like pt_particles.y, or NULL) are dL/d(end state) per particle;
+ * dL_dG receives the field's n_coeff derivatives summed over particles.
+ * Supported: neutrons, FP64 field mode, scenes of harmonic expansions and
+ * uniform E fields without boxes, at most 16 coefficients, walls that
+ * reflect specularly (a diffuse reflection or transmission on a path gives
+ * PT_ERR_UNSUPPORTED).  No counterpart in the reference, which has no
+ * derivatives. */
+pt_status pt_adjoint(pt_ctx *ctx, const pt_run_params *params, const pt_particles *in, int32_t field, int32_t checkpoint_interval,
+                     const double *dL_dspin, const double *dL_dy, double *dL_dG, pt_particles *out, pt_stats *stats);
 
 /* IDs of solids containing each point by +z ray parity (TTriangleMesh::GetSolids,
  * include/trianglemesh.h:181-188) as a bit mask over scene solid indices. */

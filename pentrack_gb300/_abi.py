@@ -94,6 +94,7 @@ class Stats(C.Structure):
         ("cand_calls", C.c_int64), ("cand_overflow", C.c_int64), ("cand_sum", C.c_int64), ("tri32_tests", C.c_int64),
         ("bisect_ms", C.c_double), ("bisect_dead", C.c_int64), ("spin_steps", C.c_int64), ("tail_ms", C.c_double), ("aux_launches", C.c_int64),
         ("graph_launches", C.c_int64), ("sched_outer_iters", C.c_int64), ("sched_inner_iters", C.c_int64),
+        ("adj_forward_ms", C.c_double), ("adj_reverse_ms", C.c_double),
     ]
 
     def as_dict(self):
@@ -122,6 +123,8 @@ def declare(lib):
         "pt_field_eval": (C.c_int32, [vp, C.c_int64, c_double_p, C.c_int32, c_double_p, c_double_p, c_double_p, c_double_p]),
         "pt_segment_collisions": (C.c_int32, [vp, C.c_int64, c_double_p, C.c_int32, c_int32_p, c_double_p, c_double_p,
                                               c_int32_p, c_double_p]),
+        "pt_adjoint": (C.c_int32, [vp, P(RunParams), P(Particles), C.c_int32, C.c_int32, c_double_p, c_double_p,
+                                   c_double_p, P(Particles), P(Stats)]),
         "pt_segment_collisions_noalloc": (C.c_int32, [vp, C.c_int64, c_double_p, C.c_int32, c_int32_p, c_double_p,
                                                       c_double_p, c_int32_p, c_double_p]),
         "pt_point_solids": (C.c_int32, [vp, C.c_int64, c_double_p, c_uint64_p]),

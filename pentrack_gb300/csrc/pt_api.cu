@@ -20,6 +20,12 @@
 #include "pt_kernels.cuh"
 #include "pt_scene.hpp"
 
+/* record layout of the adjoint's tapes (doubles per record; see pt_adjoint.cuh) */
+namespace {
+constexpr int SEG_DOUBLES = 108, CK_DOUBLES = 12, STEP_DOUBLES = 26, PT_ADJ_MAX_COEF = 16;
+enum { ADJ_OVF_SEG = 1, ADJ_OVF_CK = 2, ADJ_CANCELLED = 64, ADJ_UNSUPPORTED = 8 };
+}
+
 using namespace ptk;
 
 
@@ -99,6 +105,7 @@ struct pt_batch {
     double timeout_s = 0;
     int period_iters = 0;   /* persistent form: outer iterations per graph launch (0 = 64) */
     int max_run = 0;        /* persistent form: consecutive steps per lane and particle (0 = budget only) */
+    int run_blocks = 3;     /* persistent form: resident k_run blocks per SM (3: 168 registers, 2: 255) */
 };
 
 namespace {
@@ -366,6 +373,25 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
             if (e) return ck(c, e, "upload harmonic"), PT_ERR_CUDA;
             o.mono_e = dupload(c->allocs, expo.data(), expo.size(), e);
             if (e) return ck(c, e, "upload harmonic"), PT_ERR_CUDA;
+            {
+                /* one potential per coefficient with G = 1: the basis fields of the adjoint */
+                std::vector<double> bc;
+                std::vector<int> be, start(1, 0);
+                for (int k = 0; k < f.n_coeff; ++k) {
+                    std::vector<double> ck1;
+                    std::vector<int> ek1;
+                    const double one = 1.0;
+                    if (!pth::harmonic_polynomial(1, f.l + k, f.m + k, &one, ck1, ek1, err)) return PT_ERR_INVALID;
+                    bc.insert(bc.end(), ck1.begin(), ck1.end());
+                    be.insert(be.end(), ek1.begin(), ek1.end());
+                    start.push_back((int)bc.size());
+                }
+                o.n_terms = f.n_coeff;
+                o.term_start = dupload(c->allocs, start.data(), start.size(), e);
+                if (!e) o.basis_c = dupload(c->allocs, bc.data(), bc.size(), e);
+                if (!e) o.basis_e = dupload(c->allocs, be.data(), be.size(), e);
+                if (e) return ck(c, e, "upload harmonic basis"), PT_ERR_CUDA;
+            }
             for (int k = 0; k < 3; ++k) o.offset[k] = f.offset[k];
         } else if (f.type == PT_FIELD_UNIFORM_E) {
             o.has_v = 1;
@@ -409,6 +435,10 @@ int persistent_grid(pt_ctx *c, const void *fn, int block) {
     return per_sm * c->sm_count;
 }
 
+/* whether a run can integrate spins (IntegrateSpin's Bloch integration):
+ * a species with a gyromagnetic ratio and spin-integration windows */
+bool spin_run(const DRun &R) { return R.sp.gamma != 0 && R.n_spintimes >= 2; }
+
 /* Plain form: k_plain launches (one lane per particle, up to steps_per_launch
  * LOOP-A iterations or the step budget) until no particle is active; also the
  * tail of the batched form (budgets counted from the call's start). */
@@ -421,7 +451,8 @@ pt_status advance_plain(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc, st
     for (int launch = 0;; ++launch) {
         if ((e = cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream))) return ck(c, e, "memset"), PT_ERR_CUDA;
         cudaEventRecord(c->ev0, c->stream);
-        k_plain<<<grid_for(n, block), block, 0, c->stream>>>(c->scene, R, B->b, c->counters, steps, from_nacc0 ? 1 : 0);
+        if (spin_run(R)) k_plain_spin<<<grid_for(n, block), block, 0, c->stream>>>(c->scene, R, B->b, c->counters, steps, from_nacc0 ? 1 : 0);
+        else k_plain<<<grid_for(n, block), block, 0, c->stream>>>(c->scene, R, B->b, c->counters, steps, from_nacc0 ? 1 : 0);
         cudaEventRecord(c->ev1, c->stream);
         if ((e = cudaGetLastError())) return ck(c, e, "k_plain launch"), PT_ERR_CUDA;
         if ((e = cudaMemcpyAsync(c->counters_host, c->counters, sizeof(DCounters), cudaMemcpyDeviceToHost, c->stream)))
@@ -627,7 +658,9 @@ pt_status advance_persistent(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &ac
         const bool box = f.xmin < f.xmax && f.ymin < f.ymax && f.zmin < f.zmax;
         if (f.has_b && !(f.type == PT_FIELD_TAB3D && f.node32 && !(f.bw > 0 && box))) tab_only = false;
     }
-    const void *run_fn = tab_only ? (const void *)k_run_tab32 : (const void *)k_run;
+    const bool wide = B->run_blocks == 2; /* the 255-register instance */
+    const void *run_fn = wide ? (tab_only ? (const void *)k_run2_tab32 : (const void *)k_run2)
+                              : (tab_only ? (const void *)k_run_tab32 : (const void *)k_run);
     const int g_run = persistent_grid(c, run_fn, block);
     const int g_slow = persistent_grid(c, (const void *)k_slow, block);
     const int g_bisect = persistent_grid(c, (const void *)k_bisect, block);
@@ -671,7 +704,9 @@ pt_status advance_persistent(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &ac
         if ((e = cudaStreamBeginCaptureToGraph(c->stream, body_outer, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal))) { fail("capture"); break; }
         k_sched_begin<<<1, 32, 0, c->stream>>>(b, b.sched);
         k_regather<<<grid_for(n, 256), 256, 0, c->stream>>>(b, R.t_pause, R.max_steps, b.list[0], &b.count[0]);
-        if (tab_only) k_run_tab32<<<g_run, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched, max_run);
+        if (wide && tab_only) k_run2_tab32<<<g_run, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched, max_run);
+        else if (wide) k_run2<<<g_run, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched, max_run);
+        else if (tab_only) k_run_tab32<<<g_run, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched, max_run);
         else k_run<<<g_run, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched, max_run);
         k_sched_after_run<<<1, 32, 0, c->stream>>>(b, b.sched, h_slow);
         e = capture_conditional(c->stream, h_slow, cudaGraphCondTypeWhile, &body_slow);
@@ -730,7 +765,7 @@ pt_status advance_persistent(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &ac
         st = advance_plain(c, B, R, acc, w0, cancelled, timed_out, true);
         acc.tail_ms = acc.kernel_ms - k0;
     }
-    const char *name = tab_only ? "k_run_tab32" : "k_run";
+    const char *name = wide ? (tab_only ? "k_run2_tab32" : "k_run2") : (tab_only ? "k_run_tab32" : "k_run");
     double dom = run_ms;
     int64_t dl = hs.outer_iters;
     if (slow_ms > dom) { dom = slow_ms; name = "k_slow"; dl = hs.inner_iters; }
@@ -871,6 +906,7 @@ pt_status batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles *in
     B->timeout_s = p->timeout_s;
     B->max_run = p->max_run;
     B->period_iters = p->period_iters;
+    B->run_blocks = p->block_size == 2 ? 2 : 3;
     DRun &R = B->run;
     std::memset(&R, 0, sizeof(R));
     R.sp = make_species(p->species);
@@ -958,7 +994,14 @@ pt_status pt_batch_advance_steps(pt_ctx *c, pt_batch *B, double t_pause, int32_t
     bool cancelled = false, timed_out = false;
     pt_status st = PT_OK;
     cudaEventRecord(c->evs0, c->stream);
-    if (R.mode == PT_MODE_BATCHED && n > 0) {
+    /* Runs that integrate spins spend nearly all their time in the Bloch
+     * integration, and every trajectory step of such a run needs the full
+     * post-step: the batched form runs them as the warp-synchronous
+     * plain-form lanes of k_plain_spin. */
+    if (R.mode == PT_MODE_BATCHED && n > 0 && spin_run(R)) {
+        st = advance_plain(c, B, R, acc, w0, cancelled, timed_out, false);
+        if (st != PT_OK) return st;
+    } else if (R.mode == PT_MODE_BATCHED && n > 0) {
         st = advance_persistent(c, B, R, acc, w0, cancelled, timed_out);
         if (st != PT_OK) return st;
     }
@@ -1126,6 +1169,148 @@ pt_status pt_segment_collisions_noalloc(pt_ctx *c, int64_t n, const double *seg,
     if (!e) e = cudaStreamSynchronize(c->stream);
     if (e) return ck(c, e, "noalloc collisions"), PT_ERR_CUDA;
     return PT_OK;
+}
+
+pt_status pt_adjoint(pt_ctx *c, const pt_run_params *p, const pt_particles *in, int32_t field, int32_t K, const double *dl_dspin,
+                     const double *dl_dy, double *dl_dg, pt_particles *out, pt_stats *stats) {
+    if (!c || !p || !in || !dl_dg || K < 1 || K > (1 << 20)) return PT_ERR_INVALID;
+    const DScene &S = c->scene;
+    if (field < 0 || field >= S.n_fields || S.fields[field].type != PT_FIELD_HARMONIC) {
+        c->err = "pt_adjoint: field must index a harmonic-expansion field of the scene";
+        return PT_ERR_INVALID;
+    }
+    const int nc = S.fields[field].n_terms;
+    if (nc < 1 || nc > PT_ADJ_MAX_COEF) { c->err = "pt_adjoint: 1 to 16 coefficients"; return PT_ERR_UNSUPPORTED; }
+    if (p->species != PT_NEUTRON || p->field_precision != PT_PREC_FP64) {
+        c->err = "pt_adjoint: neutrons in the FP64 field mode only";
+        return PT_ERR_UNSUPPORTED;
+    }
+    for (int fi = 0; fi < S.n_fields; ++fi) {
+        const DField &f = S.fields[fi];
+        const bool box = f.xmin < f.xmax && f.ymin < f.ymax && f.zmin < f.zmax;
+        if ((f.type != PT_FIELD_HARMONIC && f.type != PT_FIELD_UNIFORM_E) || box || f.bw > 0) {
+            c->err = "pt_adjoint: the scene's fields must be harmonic expansions and uniform E fields without a box";
+            return PT_ERR_UNSUPPORTED;
+        }
+    }
+    cudaSetDevice(c->device);
+    const int64_t n = in->n;
+    if (n <= 0) {
+        for (int k = 0; k < nc; ++k) dl_dg[k] = 0;
+        return PT_OK;
+    }
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const double budget = std::min((double)free_b * 0.6, 120e9);
+    const double tape_b = (double)n * K * STEP_DOUBLES * 8;
+    if (tape_b > 0.5 * budget) { c->err = "pt_adjoint: the chunk tapes (n K 208 B) exceed the device memory budget"; return PT_ERR_OOM; }
+    auto clampi = [](double v, double lo, double hi) { return (int)std::max(lo, std::min(hi, v)); };
+    int cap_seg = clampi((budget - tape_b) * 0.7 / ((double)n * SEG_DOUBLES * 8), 64, 1 << 20);
+    int cap_ck = clampi((budget - tape_b) * 0.3 / ((double)n * CK_DOUBLES * 8), 64, 1 << 22);
+    pt_stats acc;
+    std::memset(&acc, 0, sizeof(acc));
+    std::snprintf(acc.dominant_kernel, sizeof(acc.dominant_kernel), "k_adj_reverse");
+    auto w0 = std::chrono::steady_clock::now();
+    pt_status st = PT_OK;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        pt_batch *B = nullptr;
+        pt_run_params q = *p;
+        q.mode = PT_MODE_PLAIN;
+        if ((st = batch_create(c, &q, in, &B, false)) != PT_OK) return st;
+        DRun R = B->run;
+        R.t_pause = INFINITY;
+        R.max_steps = 0;
+        std::vector<void *> mem;
+        cudaError_t e = cudaSuccess;
+        DAdj A{};
+        A.seg = dalloc<double>(mem, (size_t)n * cap_seg * SEG_DOUBLES, e);
+        if (!e) A.ck = dalloc<double>(mem, (size_t)n * cap_ck * CK_DOUBLES, e);
+        if (!e) A.tape = dalloc<double>(mem, (size_t)n * K * STEP_DOUBLES, e);
+        if (!e) A.nseg = dalloc<int>(mem, n, e);
+        if (!e) A.status = dalloc<int>(mem, n, e);
+        if (!e) A.dl_dg = dalloc<double>(mem, (size_t)n * nc, e);
+        double *dspin = nullptr, *dy = nullptr;
+        if (!e && dl_dspin) dspin = dupload(mem, dl_dspin, 5 * (size_t)n, e);
+        if (!e && dl_dy) dy = dupload(mem, dl_dy, 9 * (size_t)n, e);
+        if (e) { free_list(mem); pt_batch_destroy(B); return ck(c, e, "pt_adjoint alloc"), PT_ERR_OOM; }
+        A.cap_seg = cap_seg; A.cap_ck = cap_ck; A.K = K; A.field = field; A.ncoef = nc;
+        A.dl_dspin = dspin; A.dl_dy = dy;
+        std::vector<int> hstat(n);
+        float fms = 0, rms = 0;
+        cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream);
+        cudaEventRecord(c->ev0, c->stream);
+        k_adj_forward<<<grid_for(n, 128), 128, 0, c->stream>>>(S, R, B->b, c->counters, A);
+        cudaEventRecord(c->ev1, c->stream);
+        if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(hstat.data(), A.status, n * sizeof(int), cudaMemcpyDeviceToHost, c->stream)) ||
+            (e = cudaStreamSynchronize(c->stream))) {
+            free_list(mem); pt_batch_destroy(B);
+            return ck(c, e, "pt_adjoint forward"), PT_ERR_CUDA;
+        }
+        cudaEventElapsedTime(&fms, c->ev0, c->ev1);
+        cudaMemcpy(c->counters_host, c->counters, sizeof(DCounters), cudaMemcpyDeviceToHost);
+        add_counters(acc, *c->counters_host);
+        acc.adj_forward_ms += fms;
+        int any = 0;
+        for (int64_t i = 0; i < n; ++i) any |= hstat[i];
+        if (any & ADJ_CANCELLED) {
+            free_list(mem); pt_batch_destroy(B);
+            *(volatile int *)c->cancel_host = 0;
+            return PT_ERR_CANCELLED;
+        }
+        if (any & (ADJ_OVF_SEG | ADJ_OVF_CK)) { /* the tapes were too short: grow and run again */
+            free_list(mem); pt_batch_destroy(B);
+            if (any & ADJ_OVF_SEG) cap_seg = std::min(cap_seg * 4, 1 << 22);
+            if (any & ADJ_OVF_CK) cap_ck = std::min(cap_ck * 4, 1 << 24);
+            st = PT_ERR_OOM;
+            c->err = "pt_adjoint: the forward tapes did not fit the device memory budget";
+            continue;
+        }
+        if (any) {
+            free_list(mem); pt_batch_destroy(B);
+            c->err = "pt_adjoint: the forward pass failed";
+            return PT_ERR_CUDA;
+        }
+        cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream);
+        cudaEventRecord(c->ev0, c->stream);
+        k_adj_reverse<<<grid_for(n, 128), 128, 0, c->stream>>>(S, R, B->b, c->counters, A);
+        cudaEventRecord(c->ev1, c->stream);
+        std::vector<double> g((size_t)n * nc);
+        if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(hstat.data(), A.status, n * sizeof(int), cudaMemcpyDeviceToHost, c->stream)) ||
+            (e = cudaMemcpyAsync(g.data(), A.dl_dg, g.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream)) ||
+            (e = cudaStreamSynchronize(c->stream))) {
+            free_list(mem); pt_batch_destroy(B);
+            return ck(c, e, "pt_adjoint reverse"), PT_ERR_CUDA;
+        }
+        cudaEventElapsedTime(&rms, c->ev0, c->ev1);
+        acc.adj_reverse_ms += rms;
+        any = 0;
+        for (int64_t i = 0; i < n; ++i) any |= hstat[i];
+        st = PT_OK;
+        if (any & ADJ_UNSUPPORTED) {
+            c->err = "pt_adjoint: a particle's path has a diffuse reflection or a transmission; the adjoint follows specular reflections only";
+            st = PT_ERR_UNSUPPORTED;
+        } else if (any) {
+            c->err = "pt_adjoint: a recomputed Bloch chunk differs from the forward pass";
+            st = PT_ERR_CUDA;
+        }
+        if (st == PT_OK) {
+            /* per-particle gradients summed in particle order (deterministic) */
+            for (int k = 0; k < nc; ++k) {
+                double sum = 0;
+                for (int64_t i = 0; i < n; ++i) sum += g[(size_t)k * n + i];
+                dl_dg[k] = sum;
+            }
+            if (out) st = pt_batch_read(c, B, out);
+        }
+        free_list(mem);
+        pt_batch_destroy(B);
+        break;
+    }
+    acc.kernel_ms = acc.adj_forward_ms + acc.adj_reverse_ms;
+    acc.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+    acc.launches = 2;
+    if (stats) *stats = acc;
+    return st;
 }
 
 pt_status pt_probe_fp64(pt_ctx *c, double *tflops) {

@@ -108,6 +108,13 @@ struct DField {
     const double *mono_c;  /* coefficient of each monomial */
     const int *mono_e;     /* packed exponents i | j<<4 | k<<8 */
     double offset[3];      /* harmonic: added to the coordinates; solenoid: its centre */
+    /* harmonic: the potential of each coefficient with G = 1 (the basis
+     * fields dB/dG_k the adjoint uses), terms term_start[k] .. term_start[k+1]-1 */
+    int n_terms;
+    int pad3;
+    const int *term_start;
+    const double *basis_c;
+    const int *basis_e;
     double sol_a, sol_b, sol_B0; /* solenoid radius, half length, mu0 n I / pi */
 };
 
@@ -187,6 +194,17 @@ struct DSched {
     int tail, last_going, last_active, inner_this; /* inner_this: slow rounds of the current iteration */
     int error, pad2;                                /* error: the slow-round cap was reached */
     unsigned long long t0[PT_SPANS], t1[PT_SPANS], ns[PT_SPANS], launches[PT_SPANS];
+};
+
+/* Device buffers of one pt_adjoint call (per particle i: segment records
+ * at seg + i cap_seg SEG_DOUBLES, Bloch checkpoints at ck + i cap_ck
+ * CK_DOUBLES, one chunk tape of K steps at tape + i K STEP_DOUBLES) */
+struct DAdj {
+    double *seg, *ck, *tape;
+    int cap_seg, cap_ck, K, field, ncoef, pad;
+    int *nseg, *status;
+    const double *dl_dspin, *dl_dy; /* 5n, 9n component-major (dl_dy may be null) */
+    double *dl_dg;                  /* ncoef x n */
 };
 
 /* device event counters (one set per launch, summed with atomics per block) */

@@ -30,4 +30,68 @@ __global__ void __launch_bounds__(128) k_plain(const __grid_constant__ DScene S,
     flush_counters(C, L.lc, L.t - t0, active);
 }
 
+/* The plain form for runs that integrate the spin (IntegrateSpin's Bloch
+ * integration, LOOP D): the same LOOP-A iterations as k_plain, but a lane
+ * whose step reaches its Bloch integration runs it one accepted Bloch step
+ * per loop iteration, and every lane of the warp stays in the loop and is
+ * re-synchronised at its top.  The lanes in their Bloch integration -- almost
+ * all of them, since it takes hundreds of Bloch steps per trajectory step --
+ * then execute each Bloch step as one converged pass, where calling it per
+ * lane lets the warp split into groups that run it separately. */
+__global__ void __launch_bounds__(128) k_plain_spin(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C,
+                                                    int steps, int budget_from_nacc0) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool done = i >= b.n;
+    if (!done) {
+        if (b.stop_id[i] != PT_ID_UNKNOWN || b.t[i] >= R.t_pause) done = true;
+        else if (R.max_steps > 0) steps = budget_from_nacc0 ? (int)(R.max_steps - (b.nacc[i] - b.nacc0[i])) : R.max_steps;
+        if (steps <= 0) done = true;
+    }
+    Lane L(S, R);
+    double t0 = 0;
+    const bool had = !done;
+    if (had) {
+        L.load(b, i);
+        t0 = L.t;
+    }
+    int s = 0;
+    bool inbloch = false;
+    for (;;) {
+        __syncwarp();
+        if (__all_sync(0xffffffffu, done)) break;
+        if (done) continue;
+        bool ended = false;
+        if (inbloch) {
+            const int r = L.bloch_run(L.bst, L.bx2, 1);
+            if (r == 0) continue;
+            L.bloch_finish(r);
+            inbloch = false;
+            ended = true;
+        } else {
+            int r;
+            do { r = L.rk_try(); } while (r == 0);
+            if (r < 0) {
+                L.stop = PT_ID_ODEINT_ERROR;
+                ended = true;
+            } else {
+                L.ps.stage = PS_BEGIN;
+                int q;
+                while ((q = L.post_resume<true>()) == 1)
+                    L.ps.bres = L.bisect(L.ps.cx1, L.ps.cya, L.ps.x2, L.ps.y2, L.ps.bxa, L.ps.bao, L.ps.bxb, L.ps.bbo);
+                if (q == 2) inbloch = true;
+                else ended = true;
+            }
+        }
+        if (ended) {
+            ++s;
+            if (L.stop != PT_ID_UNKNOWN || L.t >= R.t_pause || s >= steps || *R.cancel) done = true;
+        }
+    }
+    if (had) {
+        L.store(b, i);
+        const bool active = (L.stop == PT_ID_UNKNOWN && L.t < R.t_pause);
+        flush_counters(C, L.lc, L.t - t0, active);
+    }
+}
+
 } // namespace ptk

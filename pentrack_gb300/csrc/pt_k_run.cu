@@ -93,13 +93,23 @@ static __device__ __forceinline__ void run_phase(const DScene &S, const DRun &R,
     span_end(sc, PT_SPAN_RUN);
 }
 
-__global__ void __launch_bounds__(128, PT_RUN_BLOCKS_PER_SM) k_run(const __grid_constant__ DScene S, const __grid_constant__ DRun R,
-                                                                  const __grid_constant__ DBatch b, DCounters *C, DSched *sc, int max_run) {
+/* instances: general / FP32-table-only right-hand side, at 3 resident
+ * blocks of 128 per SM (168 registers) or 2 (255 registers, fewer spills of
+ * the lane state the kernel keeps across steps); the host picks one */
+__global__ void __launch_bounds__(128, 3) k_run(const __grid_constant__ DScene S, const __grid_constant__ DRun R,
+                                               const __grid_constant__ DBatch b, DCounters *C, DSched *sc, int max_run) {
     run_phase<false>(S, R, b, C, sc, max_run);
 }
-__global__ void __launch_bounds__(128, PT_RUN_BLOCKS_PER_SM) k_run_tab32(const __grid_constant__ DScene S, const __grid_constant__ DRun R,
-                                                                        const __grid_constant__ DBatch b, DCounters *C, DSched *sc,
-                                                                        int max_run) {
+__global__ void __launch_bounds__(128, 3) k_run_tab32(const __grid_constant__ DScene S, const __grid_constant__ DRun R,
+                                                     const __grid_constant__ DBatch b, DCounters *C, DSched *sc, int max_run) {
+    run_phase<true>(S, R, b, C, sc, max_run);
+}
+__global__ void __launch_bounds__(128, 2) k_run2(const __grid_constant__ DScene S, const __grid_constant__ DRun R,
+                                                const __grid_constant__ DBatch b, DCounters *C, DSched *sc, int max_run) {
+    run_phase<false>(S, R, b, C, sc, max_run);
+}
+__global__ void __launch_bounds__(128, 2) k_run2_tab32(const __grid_constant__ DScene S, const __grid_constant__ DRun R,
+                                                      const __grid_constant__ DBatch b, DCounters *C, DSched *sc, int max_run) {
     run_phase<true>(S, R, b, C, sc, max_run);
 }
 

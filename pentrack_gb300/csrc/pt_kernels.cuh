@@ -7,10 +7,6 @@
 
 /* k_try: resident blocks of 128 per SM (register budget 168) */
 #define PT_TRY_BLOCKS_PER_SM 3
-/* k_run: resident blocks of 128 per SM */
-#ifndef PT_RUN_BLOCKS_PER_SM
-#define PT_RUN_BLOCKS_PER_SM 3
-#endif
 
 namespace ptk {
 
@@ -29,6 +25,10 @@ __global__ void k_run(const __grid_constant__ DScene S, const __grid_constant__ 
                       int max_run);
 __global__ void k_run_tab32(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C,
                             DSched *sc, int max_run);
+__global__ void k_run2(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, DSched *sc,
+                       int max_run);
+__global__ void k_run2_tab32(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C,
+                             DSched *sc, int max_run);
 __global__ void k_sched_begin(const __grid_constant__ DBatch b, DSched *sc);
 __global__ void k_sched_after_run(const __grid_constant__ DBatch b, DSched *sc, cudaGraphConditionalHandle slow);
 __global__ void k_sched_after_slow(const __grid_constant__ DBatch b, DSched *sc, const __grid_constant__ DRun R,
@@ -36,8 +36,14 @@ __global__ void k_sched_after_slow(const __grid_constant__ DBatch b, DSched *sc,
 __global__ void k_sched_end(const __grid_constant__ DBatch b, DSched *sc, const __grid_constant__ DRun R,
                             cudaGraphConditionalHandle outer);
 __global__ void k_sched_period(DSched *sc);
+__global__ void k_adj_forward(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C,
+                              const __grid_constant__ DAdj A);
+__global__ void k_adj_reverse(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C,
+                              const __grid_constant__ DAdj A);
 __global__ void k_plain(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int steps,
                         int budget_from_nacc0);
+__global__ void k_plain_spin(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int steps,
+                             int budget_from_nacc0);
 __global__ void k_fp64_probe(double *out, int iters, double a, double b);
 __global__ void k_field(const __grid_constant__ DScene S, int prec, int64_t n, const double *xyzt, double *B, double *dB, double *V, double *E);
 __global__ void k_collisions(const __grid_constant__ DScene S, int64_t n, const double *seg, int maxh, int *count, double *s, double *nrm, int *sid,

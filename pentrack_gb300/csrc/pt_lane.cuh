@@ -112,9 +112,34 @@ static __device__ __forceinline__ bool rhs_general(const DScene &S, const DRun &
     return have;
 }
 
-struct Lane {
+/* State of a Bloch (LOOP D) integration between its steps: time, step
+ * size, spin state, its FSAL derivative and the precession axis at it, and
+ * the accepted steps so far. */
+struct BlochState {
+    double ts, dt, x[5], dxdt[5], w[3];
+    long steps;
+};
+
+/* Recording hooks of a lane.  The production kernels use NoTape, whose
+ * hooks are empty and compile away; the adjoint's taped forward and its
+ * chunk recomputation (pt_k_adjoint.cu) record the trajectory segments and
+ * the accepted Bloch steps through them, so both run exactly the
+ * arithmetic of the production lane. */
+struct NoTape {
+    static constexpr bool kSpinStages = false; /* whether bloch collects the precession axis of every stage */
+    template <class L> __device__ __forceinline__ void on_accept(L &, const double *) {}
+    template <class L> __device__ __forceinline__ void on_segment(L &, double, const double *, bool) {}
+    template <class L> __device__ __forceinline__ void on_bloch_start(L &, double, double, double) {}
+    template <class L> __device__ __forceinline__ bool on_spin_step(L &, double, double, const double *, const double (*)[3]) { return true; }
+    template <class L> __device__ __forceinline__ bool on_step_top(L &, const BlochState &) { return true; }
+    template <class L> __device__ __forceinline__ void on_reflect(L &, double, double, const double *) {}
+    template <class L> __device__ __forceinline__ void on_other(L &) {} /* a diffuse reflection or a transmission */
+};
+
+template <class Tape> struct LaneT {
     const DScene &S;
     const DRun &R;
+    Tape tp;
     /* persistent state */
     int64_t id;
     double t, y[9], dydt[9], dt;
@@ -145,8 +170,14 @@ struct Lane {
     double cand_ta, cand_tb, cand_span;
     PostState ps;
     LaneCounters lc;
+    /* a pending Bloch integration (spin_begin / finish_begin): its stepper,
+     * end time, B at the step's end point and the finish_step arguments */
+    BlochState bst;
+    double bx2, sBabs2, sB2[3], fx;
+    double *fyl;
+    bool freset;
 
-    __device__ Lane(const DScene &s, const DRun &r) : S(s), R(r) {
+    __device__ LaneT(const DScene &s, const DRun &r) : S(s), R(r) {
         bc_ok[0] = bc_ok[1] = false;
         bc_next = 0;
         ntry = 0;
@@ -446,7 +477,7 @@ struct Lane {
         for (int j = 0; j < 3; ++j) W[j] = cb * ((1 - gr) * Bpar[j] + gr * B[j] - gr * vxE[j] * PT_INV_C0_SQ) + ct * axv[j];
     }
     /* TParticle::SpinDerivs (src/particle.cpp:178-193) along the trajectory's dense output */
-    __device__ __noinline__ void spin_derivs(const double *Sv, double *dS, double tt) {
+    __device__ __noinline__ void spin_derivs(const double *Sv, double *dS, double tt, double *Wout = nullptr) {
         double yy[9], dydt[9], B[3], dB[3][3], V, E[3], W[3];
         calc_state(tt, yy);
         bfield<true>(S, R.prec, yy[0], yy[1], yy[2], B, dB);
@@ -459,6 +490,7 @@ struct Lane {
         dS[2] = W[0] * Sv[1] - W[1] * Sv[0];
         dS[3] = 1.;
         dS[4] = sqrt(W[0] * W[0] + W[1] * W[1] + W[2] * W[2]);
+        if (Wout) { Wout[0] = W[0]; Wout[1] = W[1]; Wout[2] = W[2]; }
     }
 
     /* LOOP D of TTracker::IntegrateSpin (src/tracking.cpp:423-446): a fresh
@@ -466,6 +498,27 @@ struct Lane {
      * x2, the same controller and arithmetic as the trajectory's; false when
      * a step fails (500 tries) or the step count bound is reached */
     __device__ __noinline__ bool bloch(double x1, double x2, double dt0) {
+        BlochState bs;
+        bloch_begin(bs, x1, x2, dt0);
+        return bloch_run(bs, x2, -1) == 1;
+    }
+    /* the stepper's start: spin state, first step size and FSAL derivative */
+    __device__ void bloch_begin(BlochState &bs, double x1, double x2, double dt0) {
+        tp.on_bloch_start(*this, x1, x2, dt0);
+        for (int i = 0; i < 5; ++i) bs.x[i] = spin[i];
+        bs.ts = x1;
+        bs.dt = dt0;
+        bs.steps = 0;
+        spin_derivs(bs.x, bs.dxdt, bs.ts, Tape::kSpinStages ? bs.w : nullptr);
+    }
+    /* Runs the stepper from `bs` towards x2 for at most max_steps accepted
+     * steps (< 0: no limit).  Returns 1 when x2 is reached (the spin at x2 in
+     * spin[]), 0 when max_steps steps are done (state in bs, spin[] = the
+     * state after the last step), -1 on a failed step or the step bound.
+     * The hooks see the top of every step and every accepted step: its start
+     * time, step size, start state and (kSpinStages) the precession axis at
+     * each of its seven stages (the last is the FSAL point). */
+    __device__ __noinline__ int bloch_run(BlochState &bs, double x2, long max_steps) {
         const double a2 = 1.0 / 5, a3 = 3.0 / 10, a4 = 4.0 / 5, a5 = 8.0 / 9;
         const double b21 = 1.0 / 5;
         const double b31 = 3.0 / 40, b32 = 9.0 / 40;
@@ -476,30 +529,36 @@ struct Lane {
         const double dc1 = c1 - 5179.0 / 57600, dc3 = c3 - 7571.0 / 16695, dc4 = c4 - 393.0 / 640,
                      dc5 = c5 - (-92097.0) / 339200, dc6 = c6 - 187.0 / 2100, dc7 = -1.0 / 40;
         const double eps = 1e-12;
-        double x[5], dxdt[5], xo5[5], dxo5[5], k2_[5], k3_[5], k4_[5], k5_[5], k6_[5], xt[5], out[5], dout[5];
-        for (int i = 0; i < 5; ++i) x[i] = spin[i];
-        double ts = x1, dt_ = dt0, tso = x1;
-        spin_derivs(x, dxdt, ts);
-        for (long steps = 0;; ++steps) {
-            if (steps >= PT_MAX_SPIN_STEPS) return false;
+        double *x = bs.x, *dxdt = bs.dxdt;
+        double xo5[5], dxo5[5], k2_[5], k3_[5], k4_[5], k5_[5], k6_[5], xt[5], out[5], dout[5];
+        double wst[7][3]; /* precession axis per stage (kSpinStages only) */
+        double &ts = bs.ts, &dt_ = bs.dt;
+        double tso = ts;
+        for (long done = 0;; ++done) {
+            if (bs.steps >= PT_MAX_SPIN_STEPS) return -1;
+            if (max_steps >= 0 && done >= max_steps) {
+                for (int i = 0; i < 5; ++i) spin[i] = x[i];
+                return 0;
+            }
+            if (!tp.on_step_top(*this, bs)) return -1;
             tso = ts;
             for (int tries = 1;; ++tries) {
-                if (tries > PT_MAX_TRIES) return false;
+                if (tries > PT_MAX_TRIES) return -1;
                 for (int i = 0; i < 5; ++i) xt[i] = fma(dt_ * b21, dxdt[i], x[i]);
-                spin_derivs(xt, k2_, ts + dt_ * a2);
+                spin_derivs(xt, k2_, ts + dt_ * a2, Tape::kSpinStages ? wst[1] : nullptr);
                 for (int i = 0; i < 5; ++i) xt[i] = fma(dt_ * b32, k2_[i], fma(dt_ * b31, dxdt[i], x[i]));
-                spin_derivs(xt, k3_, ts + dt_ * a3);
+                spin_derivs(xt, k3_, ts + dt_ * a3, Tape::kSpinStages ? wst[2] : nullptr);
                 for (int i = 0; i < 5; ++i) xt[i] = fma(dt_ * b43, k3_[i], fma(dt_ * b42, k2_[i], fma(dt_ * b41, dxdt[i], x[i])));
-                spin_derivs(xt, k4_, ts + dt_ * a4);
+                spin_derivs(xt, k4_, ts + dt_ * a4, Tape::kSpinStages ? wst[3] : nullptr);
                 for (int i = 0; i < 5; ++i)
                     xt[i] = fma(dt_ * b54, k4_[i], fma(dt_ * b53, k3_[i], fma(dt_ * b52, k2_[i], fma(dt_ * b51, dxdt[i], x[i]))));
-                spin_derivs(xt, k5_, ts + dt_ * a5);
+                spin_derivs(xt, k5_, ts + dt_ * a5, Tape::kSpinStages ? wst[4] : nullptr);
                 for (int i = 0; i < 5; ++i)
                     xt[i] = fma(dt_ * b65, k5_[i], fma(dt_ * b64, k4_[i], fma(dt_ * b63, k3_[i], fma(dt_ * b62, k2_[i], fma(dt_ * b61, dxdt[i], x[i])))));
-                spin_derivs(xt, k6_, ts + dt_);
+                spin_derivs(xt, k6_, ts + dt_, Tape::kSpinStages ? wst[5] : nullptr);
                 for (int i = 0; i < 5; ++i)
                     out[i] = fma(dt_ * c6, k6_[i], fma(dt_ * c5, k5_[i], fma(dt_ * c4, k4_[i], fma(dt_ * c3, k3_[i], fma(dt_ * c1, dxdt[i], x[i])))));
-                spin_derivs(out, dout, ts + dt_);
+                spin_derivs(out, dout, ts + dt_, Tape::kSpinStages ? wst[6] : nullptr);
                 double adt = fabs(dt_), m = 0;
                 for (int i = 0; i < 5; ++i) {
                     const double er = fma(dt_ * dc7, dout[i], fma(dt_ * dc6, k6_[i], fma(dt_ * dc5, k5_[i], fma(dt_ * dc4, k4_[i],
@@ -511,6 +570,11 @@ struct Lane {
                     dt_ *= fmax(0.9 * (m < 1e300 ? ptdm_pow(m, -1.0 / 3.0) : 0.0), 0.2);
                     continue;
                 }
+                if (Tape::kSpinStages) {
+                    wst[0][0] = bs.w[0]; wst[0][1] = bs.w[1]; wst[0][2] = bs.w[2];
+                    bs.w[0] = wst[6][0]; bs.w[1] = wst[6][1]; bs.w[2] = wst[6][2];
+                }
+                if (!tp.on_spin_step(*this, tso, dt_, x, wst)) return -1;
                 ts += dt_;
                 if (m < 0.5) {
                     m = fmax(0.00032, m);
@@ -520,6 +584,7 @@ struct Lane {
                 break;
             }
             ++lc.spin;
+            ++bs.steps;
             if (ts > x2) { /* overshoot: the continuous extension at x2 */
                 const double W_[6][5] = {
                     {1.0, -2.8605386690370884, 3.099577878709121, -1.1618105836403092, 0.013917207301610328},
@@ -540,10 +605,10 @@ struct Lane {
                 }
                 for (int i = 0; i < 5; ++i)
                     spin[i] = fma(hb[5], dxdt[i], fma(hb[4], k6_[i], fma(hb[3], k5_[i], fma(hb[2], k4_[i], fma(hb[1], k3_[i], fma(hb[0], dxo5[i], xo5[i]))))));
-                return true;
+                return 1;
             }
             for (int i = 0; i < 5; ++i) spin[i] = x[i];
-            if (ts >= x2) return true;
+            if (ts >= x2) return 1;
         }
     }
 
@@ -715,8 +780,10 @@ struct Lane {
     __device__ int rk_try() {
         double ks[5][9];
         const int r = rk_try_with(KReg{ks, y, dydt});
-        if (r == 1)
+        if (r == 1) {
             for (int i = 0; i < 9; ++i) { k3[i] = ks[1][i]; k4[i] = ks[2][i]; k5[i] = ks[3][i]; k6[i] = ks[4][i]; }
+            tp.on_accept(*this, ks[0]);
+        }
         return r;
     }
 
@@ -938,6 +1005,7 @@ struct Lane {
 
     /* ---------------- neutron wall physics (src/neutron.cpp) ---------------- */
     __device__ void reflect(double x1, const double *y1, double &x2, double *y2, const double *n) {
+        tp.on_reflect(*this, x1, x2, n);
         double vn = y1[3] * n[0] + y1[4] * n[1] + y1[5] * n[2];
         x2 = x1;
         y2[0] = y1[0]; y2[1] = y1[1]; y2[2] = y1[2];
@@ -950,6 +1018,7 @@ struct Lane {
         return acos(sqrt(u * (cb * cb - ca * ca) + ca * ca));
     }
     __device__ void reflect_lambert(double x1, const double *y1, double &x2, double *y2, const double *normal, const DMat &mat) {
+        tp.on_other(*this);
         double vn = y1[3] * normal[0] + y1[4] * normal[1] + y1[5] * normal[2];
         double n[3] = {normal[0], normal[1], normal[2]};
         if (vn > 0) { vn *= -1; n[0] *= -1; n[1] *= -1; n[2] *= -1; }
@@ -973,12 +1042,14 @@ struct Lane {
         y2[6] = y1[6]; y2[8] = y1[8];
     }
     __device__ void transmit(const double *y1, double *y2, const double *n, double Estep) {
+        tp.on_other(*this);
         double vn = y1[3] * n[0] + y1[4] * n[1] + y1[5] * n[2];
         double En = 0.5 * R.sp.m * vn * vn;
         double k1 = sqrt(En), k2 = sqrt(En - Estep);
         for (int i = 0; i < 3; i++) y2[i + 3] += (k2 / k1 - 1) * (n[i] * vn);
     }
     __device__ void transmit_lambert(const double *y1, double *y2, const double *normal, double Estep, const DMat &mat) {
+        tp.on_other(*this);
         double vn = y1[3] * normal[0] + y1[4] * normal[1] + y1[5] * normal[2];
         double n[3] = {normal[0], normal[1], normal[2]};
         if (vn < 0) { vn *= -1; n[0] *= -1; n[1] *= -1; n[2] *= -1; }
@@ -1252,11 +1323,16 @@ struct Lane {
         return altered || stop != PT_ID_UNKNOWN;
     }
 
-    /* TTracker::IntegrateSpin decision logic (src/tracking.cpp:373-483) */
-    /* BLOCH = false compiles the variant without the Bloch integration, for
-     * callers that have checked spin_integrates() first */
+    /* TTracker::IntegrateSpin decision logic (src/tracking.cpp:373-483), in
+     * two parts around the Bloch integration so that a kernel can run the
+     * latter one step at a time: spin_begin returns 1 when the Bloch
+     * integration is to run (its stepper set up in bst, towards bx2), 0 when
+     * IntegrateSpin is complete (its result in sproj); spin_end(r) finishes
+     * it after bloch_run returned r.  BLOCH = false compiles the variant
+     * without the Bloch integration, for callers that have checked
+     * spin_integrates() first. */
     template <bool BLOCH = true>
-    __device__ double integrate_spin(double x2, const double *y2) {
+    __device__ int spin_begin(double x2, const double *y2, double &sproj) {
         double B1[3], B2[3];
         bonly(xo[0], xo[1], xo[2], to, B1);
         bonly(y2[0], y2[1], y2[2], x2, B2);
@@ -1264,11 +1340,13 @@ struct Lane {
         double Babs2 = sqrt(B2[0] * B2[0] + B2[1] * B2[1] + B2[2] * B2[2]);
         if (R.sp.gamma == 0 || Babs2 == 0) {
             for (int k = 0; k < 5; ++k) spin[k] = 0;
-            return xo[7];
+            sproj = xo[7];
+            return 0;
         } else if (Babs1 == 0 && Babs2 > 0) {
             double s = (u01() < 0.5 ? 0 : 1) * 2 - 1;
             for (int k = 0; k < 5; ++k) spin[k] = 0;
-            return s;
+            sproj = s;
+            return 0;
         } else if (x2 > to && (Babs1 < R.bmax || Babs2 < R.bmax)) {
             bool i1 = false, i2 = false;
             for (int i = 0; i + 1 < R.n_spintimes; i += 2) {
@@ -1278,10 +1356,16 @@ struct Lane {
             if (i1 || i2) {
                 if (spin[0] == 0 && spin[1] == 0 && spin[2] == 0)
                     for (int k = 0; k < 3; ++k) spin[k] = B1[k] * xo[7] / Babs1;
-                if (!BLOCH || !bloch(to, x2, fabs(PT_PI / R.sp.gamma / Babs1))) {
+                if (!BLOCH) {
                     stop = PT_ID_ODEINT_ERROR;
-                    return xo[7];
+                    sproj = xo[7];
+                    return 0;
                 }
+                sBabs2 = Babs2;
+                for (int k = 0; k < 3; ++k) sB2[k] = B2[k];
+                bx2 = x2;
+                bloch_begin(bst, to, x2, fabs(PT_PI / R.sp.gamma / Babs1));
+                return 1;
             } else if (spin[0] != 0 || spin[1] != 0 || spin[2] != 0) {
                 double proj = (spin[0] * B1[0] + spin[1] * B1[1] + spin[2] * B1[2]) / Babs1 /
                               sqrt(spin[0] * spin[0] + spin[1] * spin[1] + spin[2] * spin[2]);
@@ -1295,6 +1379,11 @@ struct Lane {
                 rotate_vector(spin, B2, nullptr);
             }
         }
+        sproj = spin_tail(Babs2, B2);
+        return 0;
+    }
+    /* the end of IntegrateSpin: projection onto B where |B| exceeds Bmax */
+    __device__ double spin_tail(double Babs2, const double *B2) {
         if (Babs2 > R.bmax && (spin[0] != 0 || spin[1] != 0 || spin[2] != 0)) {
             double proj = (spin[0] * B2[0] + spin[1] * B2[1] + spin[2] * B2[2]) / Babs2 /
                           sqrt(spin[0] * spin[0] + spin[1] * spin[1] + spin[2] * spin[2]);
@@ -1302,6 +1391,19 @@ struct Lane {
             return proj;
         }
         return xo[7];
+    }
+    __device__ double spin_end(int r) {
+        if (r != 1) {
+            stop = PT_ID_ODEINT_ERROR;
+            return xo[7];
+        }
+        return spin_tail(sBabs2, sB2);
+    }
+    template <bool BLOCH = true>
+    __device__ double integrate_spin(double x2, const double *y2) {
+        double sp;
+        if (spin_begin<BLOCH>(x2, y2, sp)) return spin_end(bloch_run(bst, bx2, -1));
+        return sp;
     }
 
     /* whether integrate_spin(x2, y2) would run the Bloch integration */
@@ -1353,7 +1455,10 @@ struct Lane {
      * bisection, spin and stop checks, commit -- as a resumable state machine.
      * Returns 1 when it needs the bisection of (ps.cx1, ps.cya) -> (ps.x2,
      * ps.y2) (result expected in ps.bres/bxa/bxb/bao/bbo, then call again), 0
-     * when the step is finished.  Call with ps.stage = PS_BEGIN first. */
+     * when the step is finished; with SPLIT, 2 when only its Bloch
+     * integration is left (run bloch_run on bst, then bloch_finish).  Call
+     * with ps.stage = PS_BEGIN first. */
+    template <bool SPLIT = false>
     __device__ int post_resume() {
         PostState &P = ps;
         bool ch = false;
@@ -1459,6 +1564,12 @@ struct Lane {
                 P.stage = PS_OUTER;
             }
         }
+        if (SPLIT) { /* return 2 with the Bloch integration pending (see finish_begin) */
+            double sp;
+            if (finish_begin<true>(P.x, P.yl, P.reset, sp)) return 2;
+            finish_end(P.x, P.yl, P.reset, sp);
+            return 0;
+        }
         finish_step(P.x, P.yl, P.reset);
         return 0;
     }
@@ -1474,7 +1585,25 @@ struct Lane {
      * (src/tracking.cpp:128-147), then commit the loop state. */
     template <bool BLOCH = true>
     __device__ void finish_step(double x, double *yl, bool reset) {
-        double sproj = integrate_spin<BLOCH>(x, yl);
+        double sp;
+        if (finish_begin<BLOCH>(x, yl, reset, sp)) sp = spin_end(bloch_run(bst, bx2, -1));
+        finish_end(x, yl, reset, sp);
+    }
+    /* finish_step up to its Bloch integration: true when that is to run
+     * (then bloch_finish(bloch_run's result) completes the step) */
+    template <bool BLOCH = true>
+    __device__ bool finish_begin(double x, double *yl, bool reset, double &sproj) {
+        tp.on_segment(*this, x, yl, reset);
+        if (spin_begin<BLOCH>(x, yl, sproj)) {
+            fx = x;
+            fyl = yl;
+            freset = reset;
+            return true;
+        }
+        return false;
+    }
+    __device__ void bloch_finish(int r) { finish_end(fx, fyl, freset, spin_end(r)); }
+    __device__ void finish_end(double x, double *yl, bool reset, double sproj) {
         bool flipped = xo[7] != yl[7];
         if (sproj != xo[7]) {
             double flipprob = 0.5 * (1 - yl[7] * sproj);
@@ -1542,5 +1671,7 @@ struct Lane {
         post_step();
     }
 };
+
+using Lane = LaneT<NoTape>;
 
 } // namespace ptd

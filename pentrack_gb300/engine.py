@@ -276,6 +276,7 @@ class Engine:
 
     def __init__(self, scene, device=0):
         L = lib()
+        self._scene_fields = list(scene.fields)
         self._desc, self._keep = scene.desc()
         h = C.c_void_p()
         st = L.pt_create(C.byref(self._desc), device, C.byref(h))
@@ -314,6 +315,29 @@ class Engine:
 
     def batch(self, params, particles):
         return Batch(self, params, particles)
+
+    def adjoint(self, params, particles, field, dl_dspin, dl_dy=None, checkpoint_interval=1024, out=None):
+        """pt_adjoint: dL/dG for the coefficients of harmonic field `field`,
+        given dL/d(end spin) (5, n) and optionally dL/d(end state) (9, n) per
+        particle.  Returns (dL_dG, end states of the forward pass, stats)."""
+        n = particles.n
+        dsp = np.ascontiguousarray(dl_dspin, dtype=np.float64).reshape(5, n)
+        dy = None if dl_dy is None else np.ascontiguousarray(dl_dy, dtype=np.float64).reshape(9, n)
+        nc = len(self._field_coeffs(field))
+        g = np.zeros(nc)
+        if out is None:
+            out = ParticleSet.empty(n)
+        stats = A.Stats()
+        pin, pout = particles.abi(outputs=False), out.abi()
+        self._check(lib().pt_adjoint(self.h, C.byref(params), C.byref(pin), field, checkpoint_interval, _dp(dsp),
+                                     _dp(dy) if dy is not None else None, _dp(g), C.byref(pout), C.byref(stats)))
+        return g, out, stats.as_dict()
+
+    def _field_coeffs(self, field):
+        f = self._scene_fields[field]
+        if f["type"] != A.FIELD_HARMONIC:
+            raise ValueError("pt_adjoint differentiates a harmonic-expansion field")
+        return f["g"]
 
     def field(self, xyzt, precision=A.PREC_FP64):
         q = np.ascontiguousarray(xyzt, dtype=np.float64).reshape(-1, 4)
