@@ -57,6 +57,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64-line", action="store_true", help="skip the FP64-field batched sub-record")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-spin forward / adjoint cost sub-record")
     p.add_argument("--e2e-steps", type=int, default=2)
     return p.parse_args()
 
@@ -213,6 +214,33 @@ def form_run(args, rank, mode):
         launches += st["launches"] + st["aux_launches"]
     return {"value": psec / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps, "steps": steps,
             "gpu_launches_per_step_batch": launches / steps}
+
+
+def adjoint_run(args, rank, n=1024, simtime=0.5, K=1024):
+    """The adjoint-spin configuration (B0 = 1 uT + eight l <= 2 harmonic terms,
+    E = 1e6 V/m, specular walls, spins along x) on a subset: the forward
+    pass (pt_integrate, FP64 field, Bloch integration) and the adjoint
+    (pt_adjoint, gradient of the mean phase with respect to the eight
+    coefficients, checkpoints every K Bloch steps), each timed on the device;
+    the cost ratio adjoint / forward is the configuration's figure."""
+    from pentrack_gb300 import Engine, _abi as A, workloads, spin_gradients as SG
+    device = int(os.environ.get("LOCAL_RANK", 0))
+    terms = workloads.harmonic_terms_l2()
+    sc, params, parts = workloads.adjoint_spin(n=n, simtime=simtime, terms=terms, first_id=rank * n)
+    e = Engine(sc, device=device)
+    params.mode = A.MODE_PLAIN
+    params.field_precision = A.PREC_FP64
+    e.integrate(params, parts)  # warm-up
+    out, st = e.integrate(params, parts)
+    fwd_ms = st["kernel_ms"]
+    g, _, ast = e.adjoint(params, parts, 1, SG.observable_cotangents(out, "phase"), checkpoint_interval=K)
+    adj_ms = ast["adj_forward_ms"] + ast["adj_reverse_ms"]
+    return {"workload": f"adjoint spin: {n} UCN x {simtime} s, cylinder R=0.2 m H=0.12 m (2048 triangles), "
+                        f"B0 1 uT + 8 harmonic terms l<=2, E 1e6 V/m, spins along x",
+            "checkpoint_interval": K, "forward_ms": fwd_ms, "adjoint_ms": adj_ms,
+            "adjoint_forward_pass_ms": ast["adj_forward_ms"], "adjoint_reverse_ms": ast["adj_reverse_ms"],
+            "cost_ratio": adj_ms / fwd_ms, "spin_steps": st["spin_steps"],
+            "spin_steps_per_s": st["spin_steps"] / (fwd_ms / 1e3), "dphase_dG": [float(x) for x in g]}
 
 
 def field_fp64_run(args, rank):
@@ -493,6 +521,8 @@ def run_ours(args, rank, world):
     line["energy_drift"] = energy_drift(engine.field, parts, out_state)
     if not args.no_fp64_line and args.precision == "fp32" and args.mode == "batched":
         line["field_fp64"] = field_fp64_run(args, rank)
+    if not args.no_adjoint:
+        line["adjoint_spin"] = adjoint_run(args, rank)
     if not args.no_e2e:
         try:
             line["e2e"] = e2e_run(args, engine, params, rank, span_step)

@@ -28,26 +28,30 @@ enum {
     SEG_XA = 7, SEG_XB = 8, SEG_N = 9,                           /* reflection: bracket [xa, xb], normal */
     SEG_XO = 12, SEG_DXO = 21, SEG_K2 = 30, SEG_K3 = 39, SEG_K4 = 48, SEG_K5 = 57, SEG_K6 = 66,
     SEG_YN = 75, SEG_DYN = 84, SEG_YL = 93, SEG_SPIN = 102,
+    SEG_FIRST = 107,                                             /* particle-wide index of its first Bloch step */
     SEG_DOUBLES = 108
 };
 enum { SEGF_BLOCH = 1, SEGF_REFLECT = 2, SEGF_RESET = 4, SEGF_OTHER = 8 };
-/* Bloch checkpoint: ts, dt, x[5], dxdt[5] */
-enum { CK_DOUBLES = 12 };
-/* chunk record: step start, step size, start spin (3), precession axis at the 7 stages */
-enum { STEP_DOUBLES = 26 };
+/* Bloch checkpoint at particle-wide Bloch step c K: segment index, ts, dt,
+ * x[5], dxdt[5], the segment's Bloch steps before it */
+enum { CK_SEG = 0, CK_TS = 1, CK_DT = 2, CK_X = 3, CK_DXDT = 8, CK_STEPS = 13, CK_DOUBLES = 14 };
+/* chunk record: step start, step size, start spin (3), precession axis at
+ * the 7 stages, segment index */
+enum { STEP_SEG = 26, STEP_DOUBLES = 27 };
 
 /* per-lane status bits of the adjoint kernels */
 enum { ADJ_OVF_SEG = 1, ADJ_OVF_CK = 2, ADJ_OVF_TAPE = 4, ADJ_UNSUPPORTED = 8, ADJ_MISMATCH = 16, ADJ_FAILED = 32, ADJ_CANCELLED = 64 };
 
 /* The forward pass's recording hooks: a segment record per accepted
- * trajectory try, a Bloch checkpoint at the top of every K-th spin step of a
- * segment. */
+ * trajectory try, a Bloch checkpoint at the top of every K-th Bloch step of
+ * the particle (counted across segments). */
 struct FwdTape {
     static constexpr bool kSpinStages = false;
     double *seg = nullptr, *ck = nullptr;
     int cap_seg = 0, cap_ck = 0, K = 1;
     int nseg = 0, nck = 0, status = 0;
     long nspin = 0;                    /* accepted spin steps of the current segment */
+    long nspin_tot = 0;                /* accepted spin steps of the particle */
     double k2[9];
     double rx[2] = {0, 0}, rn[3] = {0, 0, 0}; /* reflection of the current step: bracket and normal */
     int reflected = 0, other = 0;
@@ -74,6 +78,7 @@ struct FwdTape {
             r[SEG_YN + c] = l.yn[c]; r[SEG_DYN + c] = l.dyn[c]; r[SEG_YL + c] = yl[c];
         }
         for (int c = 0; c < 5; ++c) r[SEG_SPIN + c] = l.spin[c];
+        r[SEG_FIRST] = (double)nspin_tot;
         ++nseg;
         nspin = 0;
         reflected = other = 0;
@@ -85,17 +90,19 @@ struct FwdTape {
         r[SEG_FLAGS] = (double)((int)r[SEG_FLAGS] | SEGF_BLOCH);
     }
     template <class L> __device__ bool on_step_top(L &, const BlochState &bs) {
-        if (nspin > 0 && nspin % K == 0) {
+        if (nspin_tot % K == 0) {
             if (nck >= cap_ck) { status |= ADJ_OVF_CK; return true; }
             double *c = ck + (size_t)nck * CK_DOUBLES;
-            c[0] = bs.ts; c[1] = bs.dt;
-            for (int i = 0; i < 5; ++i) { c[2 + i] = bs.x[i]; c[7 + i] = bs.dxdt[i]; }
+            c[CK_SEG] = nseg - 1; c[CK_TS] = bs.ts; c[CK_DT] = bs.dt;
+            for (int i = 0; i < 5; ++i) { c[CK_X + i] = bs.x[i]; c[CK_DXDT + i] = bs.dxdt[i]; }
+            c[CK_STEPS] = (double)bs.steps;
             ++nck;
         }
         return true;
     }
     template <class L> __device__ bool on_spin_step(L &, double, double, const double *, const double (*)[3]) {
         ++nspin;
+        ++nspin_tot;
         if (nseg > 0 && !(status & ADJ_OVF_SEG)) seg[(size_t)(nseg - 1) * SEG_DOUBLES + SEG_NSPIN] = (double)nspin;
         return true;
     }
@@ -107,6 +114,7 @@ struct RecTape {
     static constexpr bool kSpinStages = true;
     double *tape = nullptr;
     int cap = 0, n = 0, overflow = 0;
+    int seg_idx = 0; /* segment of the steps being recorded */
     template <class L> __device__ __forceinline__ void on_accept(L &, const double *) {}
     template <class L> __device__ __forceinline__ void on_reflect(L &, double, double, const double *) {}
     template <class L> __device__ __forceinline__ void on_other(L &) {}
@@ -119,6 +127,7 @@ struct RecTape {
         r[0] = tso; r[1] = h; r[2] = x[0]; r[3] = x[1]; r[4] = x[2];
         for (int s = 0; s < 7; ++s)
             for (int k = 0; k < 3; ++k) r[5 + 3 * s + k] = w[s][k];
+        r[STEP_SEG] = seg_idx;
         ++n;
         return true;
     }

@@ -22,7 +22,7 @@
 
 /* record layout of the adjoint's tapes (doubles per record; see pt_adjoint.cuh) */
 namespace {
-constexpr int SEG_DOUBLES = 108, CK_DOUBLES = 12, STEP_DOUBLES = 26, PT_ADJ_MAX_COEF = 16;
+constexpr int SEG_DOUBLES = 108, CK_DOUBLES = 14, STEP_DOUBLES = 27, PT_ADJ_MAX_COEF = 16;
 enum { ADJ_OVF_SEG = 1, ADJ_OVF_CK = 2, ADJ_CANCELLED = 64, ADJ_UNSUPPORTED = 8 };
 }
 
@@ -374,6 +374,56 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
             o.mono_e = dupload(c->allocs, expo.data(), expo.size(), e);
             if (e) return ck(c, e, "upload harmonic"), PT_ERR_CUDA;
             {
+                /* B = grad Phi and its Jacobian as polynomials over the
+                 * monomials of degree <= deg (deg = the degree of B) */
+                int deg = 0;
+                for (int ex : expo) deg = std::max(deg, (ex & 15) + ((ex >> 4) & 15) + ((ex >> 8) & 15) - 1);
+                deg = std::max(deg, 0);
+                std::vector<int> mon;
+                for (int d = 0; d <= deg; ++d)
+                    for (int a = d; a >= 0; --a)
+                        for (int bb = d - a; bb >= 0; --bb) mon.push_back(a | bb << 4 | (d - a - bb) << 8);
+                int n1 = 0;
+                for (int ex : mon) n1 += ((ex & 15) + ((ex >> 4) & 15) + ((ex >> 8) & 15)) <= deg - 1;
+                const int nm = (int)mon.size();
+                std::vector<double> hc(9 * (size_t)nm, 0.0);
+                auto slot = [&](int a, int bb, int cc) {
+                    const int key = a | bb << 4 | cc << 8;
+                    for (int k = 0; k < nm; ++k) if (mon[k] == key) return k;
+                    return -1;
+                };
+                for (size_t t = 0; t < coef.size(); ++t) {
+                    const int ex = expo[t], ea = ex & 15, eb = (ex >> 4) & 15, ec = (ex >> 8) & 15;
+                    const int E[3] = {ea, eb, ec};
+                    for (int i = 0; i < 3; ++i) { /* dPhi/dx_i */
+                        if (E[i] == 0) continue;
+                        int D[3] = {ea, eb, ec};
+                        D[i] -= 1;
+                        const int k = slot(D[0], D[1], D[2]);
+                        if (k >= 0) hc[(size_t)i * nm + k] += coef[t] * E[i];
+                    }
+                    const int pairs[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+                    for (int q = 0; q < 6; ++q) { /* d2Phi/dx_i dx_j */
+                        const int i = pairs[q][0], j = pairs[q][1];
+                        int D[3] = {ea, eb, ec};
+                        double fct = D[i];
+                        D[i] -= 1;
+                        if (D[i] < 0) continue;
+                        fct *= D[j];
+                        D[j] -= 1;
+                        if (D[j] < 0) continue;
+                        const int k = slot(D[0], D[1], D[2]);
+                        if (k >= 0) hc[(size_t)(3 + q) * nm + k] += coef[t] * fct;
+                    }
+                }
+                o.hp_deg = deg;
+                o.hp_n = nm;
+                o.hp_n1 = n1;
+                o.hp_c = dupload(c->allocs, hc.data(), hc.size(), e);
+                if (!e) o.hp_e = dupload(c->allocs, mon.data(), mon.size(), e);
+                if (e) return ck(c, e, "upload harmonic polynomials"), PT_ERR_CUDA;
+            }
+            {
                 /* one potential per coefficient with G = 1: the basis fields of the adjoint */
                 std::vector<double> bc;
                 std::vector<int> be, start(1, 0);
@@ -436,8 +486,14 @@ int persistent_grid(pt_ctx *c, const void *fn, int block) {
 }
 
 /* whether a run can integrate spins (IntegrateSpin's Bloch integration):
- * a species with a gyromagnetic ratio and spin-integration windows */
-bool spin_run(const DRun &R) { return R.sp.gamma != 0 && R.n_spintimes >= 2; }
+ * a species with a gyromagnetic ratio and a non-empty spin-integration
+ * window [start, end) */
+bool spin_run(const DRun &R) {
+    if (R.sp.gamma == 0) return false;
+    for (int i = 0; i + 1 < R.n_spintimes; i += 2)
+        if (R.spintimes[i] < R.spintimes[i + 1]) return true;
+    return false;
+}
 
 /* Plain form: k_plain launches (one lane per particle, up to steps_per_launch
  * LOOP-A iterations or the step budget) until no particle is active; also the
@@ -1227,6 +1283,7 @@ pt_status pt_adjoint(pt_ctx *c, const pt_run_params *p, const pt_particles *in, 
         if (!e) A.ck = dalloc<double>(mem, (size_t)n * cap_ck * CK_DOUBLES, e);
         if (!e) A.tape = dalloc<double>(mem, (size_t)n * K * STEP_DOUBLES, e);
         if (!e) A.nseg = dalloc<int>(mem, n, e);
+        if (!e) A.nck = dalloc<int>(mem, n, e);
         if (!e) A.status = dalloc<int>(mem, n, e);
         if (!e) A.dl_dg = dalloc<double>(mem, (size_t)n * nc, e);
         double *dspin = nullptr, *dy = nullptr;

@@ -108,6 +108,14 @@ struct DField {
     const double *mono_c;  /* coefficient of each monomial */
     const int *mono_e;     /* packed exponents i | j<<4 | k<<8 */
     double offset[3];      /* harmonic: added to the coordinates; solenoid: its centre */
+    /* harmonic: B and its Jacobian as polynomials over the monomials
+     * x^a y^b z^c of total degree <= hp_deg in graded order (hp_e packed
+     * a | b << 4 | c << 8): hp_c holds 9 rows of hp_n coefficients, B_x,
+     * B_y, B_z, then dB_xx, dB_xy, dB_xz, dB_yy, dB_yz, dB_zz, which use the
+     * first hp_n1 monomials (degree <= hp_deg - 1) */
+    int hp_deg, hp_n, hp_n1, pad4;
+    const double *hp_c;
+    const int *hp_e;
     /* harmonic: the potential of each coefficient with G = 1 (the basis
      * fields dB/dG_k the adjoint uses), terms term_start[k] .. term_start[k+1]-1 */
     int n_terms;
@@ -202,7 +210,7 @@ struct DSched {
 struct DAdj {
     double *seg, *ck, *tape;
     int cap_seg, cap_ck, K, field, ncoef, pad;
-    int *nseg, *status;
+    int *nseg, *nck, *status;
     const double *dl_dspin, *dl_dy; /* 5n, 9n component-major (dl_dy may be null) */
     double *dl_dg;                  /* ncoef x n */
 };

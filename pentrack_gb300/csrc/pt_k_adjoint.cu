@@ -23,27 +23,66 @@ namespace ptk {
 
 /* ---------------- forward pass with recording ---------------- */
 
+/* One lane per particle, warp-synchronous like k_plain_spin: a lane whose
+ * step reaches its Bloch integration runs it one Bloch step per loop
+ * iteration, every lane stays in the loop and the warp is re-synchronised at
+ * its top; the FwdTape hooks record the segments and the checkpoints. */
 __global__ void __launch_bounds__(128) k_adj_forward(const __grid_constant__ DScene S, const __grid_constant__ DRun R,
                                                      const __grid_constant__ DBatch b, DCounters *C, const __grid_constant__ DAdj A) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.n) return;
+    const bool have = i < b.n;
     LaneT<FwdTape> L(S, R);
-    L.tp.seg = A.seg + (size_t)i * A.cap_seg * SEG_DOUBLES;
-    L.tp.cap_seg = A.cap_seg;
-    L.tp.ck = A.ck + (size_t)i * A.cap_ck * CK_DOUBLES;
-    L.tp.cap_ck = A.cap_ck;
-    L.tp.K = A.K;
-    L.load(b, i);
-    const double t0 = L.t;
-    while (L.stop == PT_ID_UNKNOWN) {
-        L.step();
-        if (L.tp.status) break;
-        if (*R.cancel) { L.tp.status |= ADJ_CANCELLED; break; }
+    double t0 = 0;
+    bool done = !have, inbloch = false;
+    if (have) {
+        L.tp.seg = A.seg + (size_t)i * A.cap_seg * SEG_DOUBLES;
+        L.tp.cap_seg = A.cap_seg;
+        L.tp.ck = A.ck + (size_t)i * A.cap_ck * CK_DOUBLES;
+        L.tp.cap_ck = A.cap_ck;
+        L.tp.K = A.K;
+        L.load(b, i);
+        t0 = L.t;
+        done = L.stop != PT_ID_UNKNOWN;
     }
-    L.store(b, i);
-    A.nseg[i] = L.tp.nseg;
-    A.status[i] = L.tp.status;
-    flush_counters(C, L.lc, L.t - t0, false);
+    for (;;) {
+        __syncwarp();
+        if (__all_sync(0xffffffffu, done)) break;
+        if (done) continue;
+        bool ended = false;
+        if (inbloch) {
+            const int r = L.bloch_run(L.bst, L.bx2, 1);
+            if (r == 0) continue;
+            L.bloch_finish(r);
+            inbloch = false;
+            ended = true;
+        } else {
+            int r;
+            do { r = L.rk_try(); } while (r == 0);
+            if (r < 0) {
+                L.stop = PT_ID_ODEINT_ERROR;
+                ended = true;
+            } else {
+                L.ps.stage = PS_BEGIN;
+                int q;
+                while ((q = L.post_resume<true>()) == 1)
+                    L.ps.bres = L.bisect(L.ps.cx1, L.ps.cya, L.ps.x2, L.ps.y2, L.ps.bxa, L.ps.bao, L.ps.bxb, L.ps.bbo);
+                if (q == 2) inbloch = true;
+                else ended = true;
+            }
+        }
+        if (L.tp.status) done = true;
+        else if (ended) {
+            if (L.stop != PT_ID_UNKNOWN) done = true;
+            else if (*R.cancel) { L.tp.status |= ADJ_CANCELLED; done = true; }
+        }
+    }
+    if (have) {
+        L.store(b, i);
+        A.nseg[i] = L.tp.nseg;
+        A.nck[i] = L.tp.nck;
+        A.status[i] = L.tp.status;
+        flush_counters(C, L.lc, L.t - t0, false);
+    }
 }
 
 /* ---------------- reverse sweep ---------------- */
@@ -308,106 +347,186 @@ static __device__ void traj_step_adj(const DScene &S, const DRun &R, const DFiel
     for (int c = 0; c < 6; ++c) lY[c] = lYn[c] + tmp[c];
 }
 
+/* The reverse sweep of one particle per lane over its Bloch steps in chunks
+ * of K: chunk c starts at the particle's Bloch step c K (its checkpoint) and
+ * holds K steps (the last one the rest), across segment boundaries.  For
+ * every chunk, from the last, the warp recomputes the chunk one Bloch step
+ * per lane and iteration (recording the stage precession axes), then sweeps
+ * it backwards one step per lane and iteration; both phases end together for
+ * the whole warp, so the lanes stay converged whatever their segments look
+ * like.  Between Bloch steps of different segments the sweep finishes the
+ * later segment (the adjoint of its trajectory step) and opens the earlier
+ * one (the adjoint of how it ended: next step, reflection or stop). */
+struct RevState {
+    int j;              /* segment being swept */
+    double lS[5], lK1n[5], lY[6], lyn[6];
+    SegAdj a;
+};
+
+static __device__ void load_seg_dense(RLane &L, const double *r) {
+    L.to = r[SEG_TO];
+    L.tn = r[SEG_TN];
+    for (int c = 0; c < 9; ++c) {
+        L.xo[c] = r[SEG_XO + c]; L.dxo[c] = r[SEG_DXO + c];
+        L.k3[c] = r[SEG_K3 + c]; L.k4[c] = r[SEG_K4 + c]; L.k5[c] = r[SEG_K5 + c]; L.k6[c] = r[SEG_K6 + c];
+        L.yn[c] = r[SEG_YN + c]; L.dyn[c] = r[SEG_DYN + c];
+    }
+}
+
+/* open segment j for the sweep: its dense data in L, zero cotangents, and
+ * the adjoint of how it ended applied to the cotangent lY of what followed */
+static __device__ int seg_enter(RLane &L, const double *segb, int j, RevState &v) {
+    const double *r = segb + (size_t)j * SEG_DOUBLES;
+    load_seg_dense(L, r);
+    v.j = j;
+    for (int c = 0; c < 6; ++c) {
+        v.a.lxo[c] = 0;
+        v.lyn[c] = 0;
+        for (int k = 0; k < 7; ++k) v.a.lK[k][c] = 0;
+    }
+    for (int c = 0; c < 5; ++c) v.lK1n[c] = 0;
+    const int flags = (int)r[SEG_FLAGS];
+    if (flags & SEGF_OTHER) return ADJ_UNSUPPORTED;
+    const double xend = r[SEG_XEND];
+    if (flags & SEGF_REFLECT) {
+        /* TNeutron::Reflect: position at xa, velocity at xb minus 2 (v(xa).n) n */
+        const double *nn = r + SEG_N;
+        const double ln = nn[0] * v.lY[3] + nn[1] * v.lY[4] + nn[2] * v.lY[5];
+        const double la[6] = {v.lY[0], v.lY[1], v.lY[2], -2 * ln * nn[0], -2 * ln * nn[1], -2 * ln * nn[2]};
+        const double lb[6] = {0, 0, 0, v.lY[3], v.lY[4], v.lY[5]};
+        dense_adj(L, r[SEG_XA], la, v.a);
+        dense_adj(L, r[SEG_XB], lb, v.a);
+        return 0;
+    }
+    bool normal = !(flags & SEGF_RESET) && xend == L.tn;
+    for (int c = 0; c < 9; ++c) normal = normal && r[SEG_YL + c] == L.yn[c];
+    if (normal) { /* the next segment starts from yn */
+        for (int c = 0; c < 6; ++c) v.lyn[c] = v.lY[c];
+        return 0;
+    }
+    double yd[9]; /* stopped at a point of the dense output */
+    L.calc_state(xend, yd);
+    bool same = true;
+    for (int c = 0; c < 9; ++c) same = same && yd[c] == r[SEG_YL + c];
+    if (!same) return ADJ_UNSUPPORTED;
+    dense_adj(L, xend, v.lY, v.a);
+    return 0;
+}
+
 __global__ void __launch_bounds__(128) k_adj_reverse(const __grid_constant__ DScene S, const __grid_constant__ DRun R,
                                                      const __grid_constant__ DBatch b, DCounters *C, const __grid_constant__ DAdj A) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.n) return;
+    const bool have = i < b.n;
     const int64_t n = b.n;
     const DField &F = S.fields[A.field];
     const int nc = A.ncoef;
+    const int K = A.K;
     RLane L(S, R);
-    L.tp.tape = A.tape + (size_t)i * A.K * STEP_DOUBLES;
-    L.tp.cap = A.K;
-    double lS[5], lY[6], lG[PT_ADJ_MAX_COEF];
-    for (int c = 0; c < 5; ++c) lS[c] = A.dl_dspin ? A.dl_dspin[c * n + i] : 0.0;
-    for (int c = 0; c < 6; ++c) lY[c] = A.dl_dy ? A.dl_dy[c * n + i] : 0.0;
+    RevState v;
+    double lG[PT_ADJ_MAX_COEF];
     for (int k = 0; k < PT_ADJ_MAX_COEF; ++k) lG[k] = 0;
-    int status = A.status[i];
-    const double *segb = A.seg + (size_t)i * A.cap_seg * SEG_DOUBLES;
-    const double *ckb = A.ck + (size_t)i * A.cap_ck * CK_DOUBLES;
-    const int nseg = status ? 0 : A.nseg[i];
-    for (int j = nseg - 1; j >= 0 && !status; --j) {
-        const double *r = segb + (size_t)j * SEG_DOUBLES;
-        L.to = r[SEG_TO];
-        L.tn = r[SEG_TN];
-        for (int c = 0; c < 9; ++c) {
-            L.xo[c] = r[SEG_XO + c]; L.dxo[c] = r[SEG_DXO + c];
-            L.k3[c] = r[SEG_K3 + c]; L.k4[c] = r[SEG_K4 + c]; L.k5[c] = r[SEG_K5 + c]; L.k6[c] = r[SEG_K6 + c];
-            L.yn[c] = r[SEG_YN + c]; L.dyn[c] = r[SEG_DYN + c];
+    int status = have ? A.status[i] : 0;
+    const double *segb = A.seg + (size_t)(have ? i : 0) * A.cap_seg * SEG_DOUBLES;
+    const double *ckb = A.ck + (size_t)(have ? i : 0) * A.cap_ck * CK_DOUBLES;
+    const int nseg = (have && !status) ? A.nseg[i] : 0;
+    int ch = -1;          /* current chunk */
+    long total = 0;       /* Bloch steps of the particle */
+    if (nseg > 0) {
+        for (int c = 0; c < 5; ++c) v.lS[c] = A.dl_dspin ? A.dl_dspin[c * n + i] : 0.0;
+        for (int c = 0; c < 6; ++c) v.lY[c] = A.dl_dy ? A.dl_dy[c * n + i] : 0.0;
+        const double *rl = segb + (size_t)(nseg - 1) * SEG_DOUBLES;
+        total = (long)rl[SEG_FIRST] + (long)rl[SEG_NSPIN];
+        ch = (int)((total + K - 1) / K) - 1;
+        if (A.nck[i] != ch + 1) status |= ADJ_MISMATCH;
+        status |= seg_enter(L, segb, nseg - 1, v);
+    }
+    L.tp.tape = A.tape + (size_t)(have ? i : 0) * K * STEP_DOUBLES;
+    L.tp.cap = K;
+    for (;;) { /* one chunk per pass */
+        const bool act = !status && ch >= 0;
+        if (!__any_sync(0xffffffffu, act)) break;
+        const long c0 = (long)ch * K;
+        const long len = act ? min((long)K, total - c0) : 0;
+        /* recompute phase */
+        BlochState bs;
+        int jr = 0;
+        double x2 = 0;
+        long left = len;
+        if (act) {
+            const double *q = ckb + (size_t)ch * CK_DOUBLES;
+            jr = (int)q[CK_SEG];
+            const double *r = segb + (size_t)jr * SEG_DOUBLES;
+            load_seg_dense(L, r);
+            x2 = r[SEG_XEND];
+            bs.ts = q[CK_TS];
+            bs.dt = q[CK_DT];
+            for (int c = 0; c < 5; ++c) { bs.x[c] = q[CK_X + c]; bs.dxdt[c] = q[CK_DXDT + c]; }
+            bs.steps = (long)q[CK_STEPS];
+            double tmp[5];
+            L.spin_derivs(bs.x, tmp, bs.ts, bs.w);
+            L.tp.n = 0;
+            L.tp.seg_idx = jr;
         }
-        const int flags = (int)r[SEG_FLAGS];
-        if (flags & SEGF_OTHER) { status |= ADJ_UNSUPPORTED; break; }
-        SegAdj a;
-        for (int c = 0; c < 6; ++c) {
-            a.lxo[c] = 0;
-            for (int k = 0; k < 7; ++k) a.lK[k][c] = 0;
-        }
-        double lyn[6] = {0, 0, 0, 0, 0, 0};
-        const double xend = r[SEG_XEND];
-        /* how the segment ended: the next segment starts from yn (no reset),
-         * from the reflected state at the bracket start, or the particle
-         * stopped at a point of the dense output */
-        if (flags & SEGF_REFLECT) {
-            /* TNeutron::Reflect: position at xa, velocity at xb minus 2 (v(xa).n) n */
-            const double *nn = r + SEG_N;
-            const double ln = nn[0] * lY[3] + nn[1] * lY[4] + nn[2] * lY[5];
-            const double la[6] = {lY[0], lY[1], lY[2], -2 * ln * nn[0], -2 * ln * nn[1], -2 * ln * nn[2]};
-            const double lb[6] = {0, 0, 0, lY[3], lY[4], lY[5]};
-            dense_adj(L, r[SEG_XA], la, a);
-            dense_adj(L, r[SEG_XB], lb, a);
-        } else {
-            bool normal = !(flags & SEGF_RESET) && xend == L.tn;
-            for (int c = 0; c < 9; ++c) normal = normal && r[SEG_YL + c] == L.yn[c];
-            if (normal) {
-                for (int c = 0; c < 6; ++c) lyn[c] = lY[c];
-            } else {
-                double yd[9];
-                L.calc_state(xend, yd);
-                bool same = true;
-                for (int c = 0; c < 9; ++c) same = same && yd[c] == r[SEG_YL + c];
-                if (!same) { status |= ADJ_UNSUPPORTED; break; }
-                dense_adj(L, xend, lY, a);
+        for (;;) {
+            __syncwarp();
+            const bool busy = act && left > 0 && !status;
+            if (!__any_sync(0xffffffffu, busy)) break;
+            if (!busy) continue;
+            const int rr = L.bloch_run(bs, x2, 1);
+            --left;
+            if (rr < 0 || L.tp.overflow) { status |= ADJ_MISMATCH; continue; }
+            if (rr == 1 && left > 0) { /* this segment's Bloch integration ended: the next one with Bloch steps */
+                int jn = jr + 1;
+                while (jn < nseg && !(((int)segb[(size_t)jn * SEG_DOUBLES + SEG_FLAGS] & SEGF_BLOCH) &&
+                                      segb[(size_t)jn * SEG_DOUBLES + SEG_NSPIN] > 0))
+                    ++jn;
+                if (jn >= nseg) { status |= ADJ_MISMATCH; continue; }
+                jr = jn;
+                const double *r = segb + (size_t)jr * SEG_DOUBLES;
+                load_seg_dense(L, r);
+                x2 = r[SEG_XEND];
+                for (int c = 0; c < 5; ++c) L.spin[c] = r[SEG_SPIN + c];
+                L.bloch_begin(bs, L.to, x2, r[SEG_DT0]);
+                L.tp.seg_idx = jr;
             }
         }
-        /* the segment's Bloch integration, chunk by chunk from the last */
-        const long nspin = (long)r[SEG_NSPIN];
-        if ((flags & SEGF_BLOCH) && nspin > 0) {
-            const int K = A.K;
-            const long nch = (nspin + K - 1) / K;
-            double lK1n[5] = {0, 0, 0, 0, 0};
-            for (long ch = nch - 1; ch >= 0 && !status; --ch) {
-                BlochState bs;
-                if (ch == 0) {
-                    for (int c = 0; c < 5; ++c) L.spin[c] = r[SEG_SPIN + c];
-                    L.bloch_begin(bs, L.to, xend, r[SEG_DT0]);
-                } else {
-                    const double *q = ckb + ((size_t)r[SEG_CK] + ch - 1) * CK_DOUBLES;
-                    bs.ts = q[0];
-                    bs.dt = q[1];
-                    for (int c = 0; c < 5; ++c) { bs.x[c] = q[2 + c]; bs.dxdt[c] = q[7 + c]; }
-                    bs.steps = ch * K;
-                    double tmp[5];
-                    L.spin_derivs(bs.x, tmp, bs.ts, bs.w);
-                }
-                const long nst = min((long)K, nspin - ch * K);
-                L.tp.n = 0;
-                const int rr = L.bloch_run(bs, xend, nst);
-                const bool lastch = (ch == nch - 1);
-                if (L.tp.overflow) { status |= ADJ_OVF_TAPE; break; }
-                if (L.tp.n != nst || (lastch ? rr != 1 : rr != 0)) { status |= ADJ_MISMATCH; break; }
-                for (long t = nst - 1; t >= 0; --t) {
-                    const double *rec = L.tp.tape + (size_t)t * STEP_DOUBLES;
-                    spin_step_adj(L, F, nc, rec, lastch && t == nst - 1, ch == 0 && t == 0, xend, lS, lK1n, lG, a);
-                }
+        if (act && !status && L.tp.n != len) status |= ADJ_MISMATCH;
+        /* sweep phase */
+        if (act && !status) load_seg_dense(L, segb + (size_t)v.j * SEG_DOUBLES);
+        long t = len - 1;
+        for (;;) {
+            __syncwarp();
+            const bool busy = act && t >= 0 && !status;
+            if (!__any_sync(0xffffffffu, busy)) break;
+            if (!busy) continue;
+            const double *rec = L.tp.tape + (size_t)t * STEP_DOUBLES;
+            const int js = (int)rec[STEP_SEG];
+            while (v.j > js && !status) { /* finish the later segment, open the earlier one */
+                traj_step_adj(S, R, F, nc, segb + (size_t)v.j * SEG_DOUBLES, v.lyn, v.a, v.lY, lG);
+                status |= seg_enter(L, segb, v.j - 1, v);
             }
+            if (status) continue;
+            const double *r = segb + (size_t)js * SEG_DOUBLES;
+            const long gi = c0 + t, first = (long)r[SEG_FIRST], last = first + (long)r[SEG_NSPIN] - 1;
+            spin_step_adj(L, F, nc, rec, gi == last, gi == first, r[SEG_XEND], v.lS, v.lK1n, lG, v.a);
+            --t;
+        }
+        --ch;
+    }
+    /* the segments before the first Bloch step and the trajectory steps of the rest */
+    if (nseg > 0 && !status) {
+        for (;;) {
+            traj_step_adj(S, R, F, nc, segb + (size_t)v.j * SEG_DOUBLES, v.lyn, v.a, v.lY, lG);
+            if (v.j == 0) break;
+            status |= seg_enter(L, segb, v.j - 1, v);
             if (status) break;
         }
-        /* the segment's trajectory step */
-        traj_step_adj(S, R, F, nc, r, lyn, a, lY, lG);
     }
-    for (int k = 0; k < nc; ++k) A.dl_dg[(size_t)k * n + i] = lG[k];
-    A.status[i] = status;
-    flush_counters(C, L.lc, 0.0, false);
+    if (have) {
+        for (int k = 0; k < nc; ++k) A.dl_dg[(size_t)k * n + i] = lG[k];
+        A.status[i] = status;
+        flush_counters(C, L.lc, 0.0, false);
+    }
 }
 
 } // namespace ptk

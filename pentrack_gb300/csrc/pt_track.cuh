@@ -509,29 +509,43 @@ __device__ __noinline__ void solenoid_b(const DField &f, double x, double y, dou
     pts_solenoid_field(f.sol_a, f.sol_b, f.sol_B0, x - f.offset[0], y - f.offset[1], z - f.offset[2], B, dB);
 }
 
-/* harmonic expansion: B = grad Phi of a polynomial Phi (offset applied) */
+/* harmonic expansion: B = grad Phi of a polynomial Phi (offset applied),
+ * evaluated from the precomputed polynomials of B and of its Jacobian over
+ * one set of monomials (each monomial value formed once, then one FMA per
+ * output) */
 template <bool GRAD>
 __device__ void harmonic_b(const DField &f, double x, double y, double z, double B[3], double (*dB)[3]) {
     x += f.offset[0];
     y += f.offset[1];
     z += f.offset[2];
-    double px[8], py[8], pz[8];
+    double px[7], py[7], pz[7];
     px[0] = py[0] = pz[0] = 1.0;
-    for (int i = 1; i < 8; ++i) { px[i] = px[i - 1] * x; py[i] = py[i - 1] * y; pz[i] = pz[i - 1] * z; }
-    for (int m = 0; m < f.n_mono; ++m) {
-        double c = f.mono_c[m];
-        int e = f.mono_e[m], i = e & 15, j = (e >> 4) & 15, k = (e >> 8) & 15;
-        if (i > 0) B[0] += c * i * px[i - 1] * py[j] * pz[k];
-        if (j > 0) B[1] += c * j * px[i] * py[j - 1] * pz[k];
-        if (k > 0) B[2] += c * k * px[i] * py[j] * pz[k - 1];
-        if (GRAD) {
-            if (i > 1) dB[0][0] += c * i * (i - 1) * px[i - 2] * py[j] * pz[k];
-            if (j > 1) dB[1][1] += c * j * (j - 1) * px[i] * py[j - 2] * pz[k];
-            if (k > 1) dB[2][2] += c * k * (k - 1) * px[i] * py[j] * pz[k - 2];
-            if (i > 0 && j > 0) { double h = c * i * j * px[i - 1] * py[j - 1] * pz[k]; dB[0][1] += h; dB[1][0] += h; }
-            if (i > 0 && k > 0) { double h = c * i * k * px[i - 1] * py[j] * pz[k - 1]; dB[0][2] += h; dB[2][0] += h; }
-            if (j > 0 && k > 0) { double h = c * j * k * px[i] * py[j - 1] * pz[k - 1]; dB[1][2] += h; dB[2][1] += h; }
+    for (int i = 1; i <= f.hp_deg; ++i) { px[i] = px[i - 1] * x; py[i] = py[i - 1] * y; pz[i] = pz[i - 1] * z; }
+    const int n = f.hp_n, n1 = f.hp_n1;
+    const double *c = f.hp_c;
+    double b0 = 0, b1 = 0, b2 = 0, d00 = 0, d01 = 0, d02 = 0, d11 = 0, d12 = 0, d22 = 0;
+    for (int m = 0; m < n; ++m) {
+        const int e = f.hp_e[m];
+        const double v = px[e & 15] * py[(e >> 4) & 15] * pz[(e >> 8) & 15];
+        b0 = fma(c[m], v, b0);
+        b1 = fma(c[n + m], v, b1);
+        b2 = fma(c[2 * n + m], v, b2);
+        if (GRAD && m < n1) {
+            d00 = fma(c[3 * n + m], v, d00);
+            d01 = fma(c[4 * n + m], v, d01);
+            d02 = fma(c[5 * n + m], v, d02);
+            d11 = fma(c[6 * n + m], v, d11);
+            d12 = fma(c[7 * n + m], v, d12);
+            d22 = fma(c[8 * n + m], v, d22);
         }
+    }
+    B[0] += b0;
+    B[1] += b1;
+    B[2] += b2;
+    if (GRAD) {
+        dB[0][0] += d00; dB[0][1] += d01; dB[0][2] += d02;
+        dB[1][0] += d01; dB[1][1] += d11; dB[1][2] += d12;
+        dB[2][0] += d02; dB[2][1] += d12; dB[2][2] += d22;
     }
 }
 
