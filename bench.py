@@ -404,7 +404,7 @@ def run_ours(args, rank, world):
             agg = dict(st)
         else:
             for k, v in st.items():
-                if isinstance(v, (int, float)) and k != "active":
+                if isinstance(v, (int, float)) and k not in ("active", "scheduler"):
                     agg[k] += v
             agg["active"] = st["active"]
     torch.cuda.synchronize(device)
@@ -434,16 +434,11 @@ def run_ours(args, rank, world):
     try_f32 = tries * 6 * field_per_rhs if args.precision == "fp32" else 0
     state_bytes = None
     if args.mode in ("batched", "phased"):
-        first = "k_run" if args.mode == "batched" else "k_try"
+        first = "k_run" if str(agg["dominant_kernel"]).startswith("k_run") else "k_try"
         kern = {first: agg["try_ms"], "k_post": agg["post_ms"], "k_slow": agg["slow_ms"], "k_bisect": agg["bisect_ms"],
                 "k_plain_tail": agg["tail_ms"]}
         dom = max(kern, key=kern.get)
-        if dom == first:
-            launches = max(1, agg["sched_outer_iters"] if args.mode == "batched" else agg["dominant_launches"])
-        elif dom in ("k_slow", "k_bisect"):
-            launches = max(1, agg["sched_inner_iters"] if args.mode == "batched" else agg["dominant_launches"])
-        else:
-            launches = max(1, agg["dominant_launches"])
+        launches = max(1, agg["dominant_launches"])
         avg_launch_s = kern[dom] / 1e3 / launches
         # k_run: its tries are counted (a lower bound on its work: the fast
         # step completion and its BVH query add to it); k_try: exactly its tries
@@ -511,7 +506,10 @@ def run_ours(args, rank, world):
                                         "bisection_levels", "bvh_nodes", "tri_tests", "subsegments", "dense_evals",
                                         "bisect_max", "bisect_dead", "cand_calls", "cand_overflow", "cand_sum", "tri32_tests")},
         "live_particles": int(agg["active"]),
-        "phase_ms": {("k_run" if args.mode == "batched" else "k_try"): agg["try_ms"], "k_post": agg["post_ms"],
+        "scheduler": {"chosen": ["autotuning", "phase split", "persistent", "persistent (255 registers)"][int(st["scheduler"])],
+                      "autotune_ns_per_try": {"phase split": st["tune_ns_per_try"][0], "persistent": st["tune_ns_per_try"][1],
+                                              "persistent (255 registers)": st["tune_ns_per_try"][2]}},
+        "phase_ms": {("k_run" if str(agg["dominant_kernel"]).startswith("k_run") else "k_try"): agg["try_ms"], "k_post": agg["post_ms"],
                      "k_slow": agg["slow_ms"], "k_bisect": agg["bisect_ms"], "k_plain_tail": agg["tail_ms"]},
     }
     if not args.no_plain and args.mode == "batched":

@@ -74,9 +74,10 @@ enum {
 /* scheduling form of the tracking kernels */
 enum {
     PT_MODE_PLAIN = 0,   /* fixed step-batch launches: one lane per particle, K accepted steps per launch */
-    PT_MODE_BATCHED = 1, /* persistent: lanes refilled from a device work queue run the steps without hits
-                            (k_run), hit resolution in work-list launches (k_slow, k_bisect); the whole loop
-                            is a CUDA graph whose iterations the device schedules */
+    PT_MODE_BATCHED = 1, /* the loop is a CUDA graph whose iterations the device schedules; each iteration
+                            runs the steps without hits either as a phase split (k_try + k_post over work
+                            lists) or in persistent lanes refilled from a device work queue (k_run), hit
+                            resolution in work-list launches (k_slow, k_bisect); pt_run_params.scheduler */
     PT_MODE_PHASED = 2   /* host-driven phase split: one RK-try launch and one completion launch per
                             iteration over work lists, the host reading the list counts in between */
 };
@@ -166,9 +167,15 @@ typedef struct pt_run_params {
     int32_t block_size;        /* 0 = autotuned */
     int32_t max_launches;      /* 0 = unlimited */
     double timeout_s;          /* host wait limit per call (0 = none) */
-    int32_t max_run;           /* batched form: consecutive steps a lane keeps one particle (0 = step budget only) */
+    int32_t max_run;           /* batched form, persistent scheduler: consecutive steps a lane keeps one particle
+                                  (0 = step budget only) */
     int32_t period_iters;      /* batched form: scheduler iterations per graph launch (0 = 64) */
+    int32_t scheduler;         /* batched form: PT_SCHED_* (PT_SCHED_AUTO: measured on the batch's first periods) */
+    int32_t reserved3;
 } pt_run_params;
+
+/* schedulers of the batched form (results are the same bits with each) */
+enum { PT_SCHED_AUTO = 0, PT_SCHED_PHASED = 1, PT_SCHED_PERSISTENT = 2, PT_SCHED_PERSISTENT_WIDE = 3 };
 
 /* structure-of-arrays particle batch (host memory).  y and spin are
  * component-major: y[c*n + i] is component c of particle i.
@@ -223,6 +230,8 @@ typedef struct pt_stats {
     int64_t sched_inner_iters; /* batched form: slow rounds (k_slow + k_bisect launches) */
     double adj_forward_ms;     /* pt_adjoint: device time of the recording forward pass(es) */
     double adj_reverse_ms;     /* pt_adjoint: device time of the reverse sweep */
+    int64_t scheduler;         /* batched form: the scheduler that ran (PT_SCHED_*; 0 while still tuning) */
+    double tune_ns_per_try[3]; /* batched form: the autotuner's device ns per RK try of each scheduler (0 = untried) */
 } pt_stats;
 
 typedef struct pt_ctx pt_ctx;

@@ -23,6 +23,7 @@ NEUTRON, PROTON, ELECTRON = 0, 1, 2
 FIELD_TAB3D, FIELD_HARMONIC, FIELD_UNIFORM_E, FIELD_SOLENOID = 1, 2, 3, 4
 MODE_PLAIN, MODE_BATCHED, MODE_PHASED = 0, 1, 2
 PREC_FP64, PREC_FP32 = 0, 1
+SCHED_AUTO, SCHED_PHASED, SCHED_PERSISTENT, SCHED_PERSISTENT_WIDE = 0, 1, 2, 3
 
 
 class Material(C.Structure):
@@ -67,7 +68,7 @@ class RunParams(C.Structure):
         ("simtime", C.c_double), ("tau", C.c_double), ("tmax", C.c_double), ("lmax", C.c_double), ("bmax", C.c_double),
         ("n_spintimes", C.c_int32), ("steps_per_launch", C.c_int32), ("spintimes", c_double_p),
         ("seed", C.c_uint64), ("block_size", C.c_int32), ("max_launches", C.c_int32), ("timeout_s", C.c_double),
-        ("max_run", C.c_int32), ("period_iters", C.c_int32),
+        ("max_run", C.c_int32), ("period_iters", C.c_int32), ("scheduler", C.c_int32), ("reserved3", C.c_int32),
     ]
 
 
@@ -95,13 +96,18 @@ class Stats(C.Structure):
         ("bisect_ms", C.c_double), ("bisect_dead", C.c_int64), ("spin_steps", C.c_int64), ("tail_ms", C.c_double), ("aux_launches", C.c_int64),
         ("graph_launches", C.c_int64), ("sched_outer_iters", C.c_int64), ("sched_inner_iters", C.c_int64),
         ("adj_forward_ms", C.c_double), ("adj_reverse_ms", C.c_double),
+        ("scheduler", C.c_int64), ("tune_ns_per_try", C.c_double * 3),
     ]
 
     def as_dict(self):
         d = {}
         for name, _ in self._fields_:
             v = getattr(self, name)
-            d[name] = v.decode() if isinstance(v, bytes) else v
+            if isinstance(v, bytes):
+                v = v.decode()
+            elif hasattr(v, "_length_"):
+                v = list(v)
+            d[name] = v
         return d
 
 

@@ -53,6 +53,9 @@ struct pt_ctx {
     DCounters *counters = nullptr;
     DCounters *counters_host = nullptr;
     DSched *sched_host = nullptr;   /* pinned copy of a batch's scheduler state */
+    /* the autotuner's scores per kind of run (index: field precision x
+     * neutral FP32-table right-hand side), kept for later batches */
+    double tune_score[4][3] = {};
     int sm_count = 0;
     /* device arena kept between pt_integrate calls (their batches are
      * created and destroyed inside the call) */
@@ -104,8 +107,10 @@ struct pt_batch {
     int max_launches = 0;
     double timeout_s = 0;
     int period_iters = 0;   /* persistent form: outer iterations per graph launch (0 = 64) */
-    int max_run = 0;        /* persistent form: consecutive steps per lane and particle (0 = budget only) */
-    int run_blocks = 3;     /* persistent form: resident k_run blocks per SM (3: 168 registers, 2: 255) */
+    int max_run = 0;        /* persistent scheduler: consecutive steps per lane and particle (0 = budget only) */
+    int scheduler = 0;      /* batched form: 0 autotuned, else SCHED_* + 1 */
+    int sched_choice = 0;   /* the autotuner's choice for this batch (SCHED_* + 1; 0 = not tuned yet) */
+    double tune_score[3] = {0, 0, 0}; /* device ns per RK try measured for each scheduler */
 };
 
 namespace {
@@ -590,10 +595,10 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
         k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, out, 2, 2);
         acc.aux_launches += 1;
         cudaEventRecord(ev[0], c->stream);
-        if (tab_only) k_try_tab32<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, in, out);
-        else k_try<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, in, out);
+        if (tab_only) k_try_tab32<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, in, out, nullptr);
+        else k_try<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, in, out, nullptr);
         cudaEventRecord(ev[1], c->stream);
-        k_post<<<g_post, block, 0, c->stream>>>(c->scene, R, b, c->counters, out);
+        k_post<<<g_post, block, 0, c->stream>>>(c->scene, R, b, c->counters, out, nullptr);
         cudaEventRecord(ev[2], c->stream);
         if ((e = cudaGetLastError())) { ck(c, e, "batched launch"); st = PT_ERR_CUDA; break; }
         cudaMemcpyAsync(hcount, b.count, 8 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
@@ -689,41 +694,106 @@ cudaError_t capture_conditional(cudaStream_t s, cudaGraphConditionalHandle h, cu
     return cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
 }
 
-/* kernel executions of the graph's iterations: sched_begin, regather, run,
- * after_run, end per outer iteration; slow, zero, bisect, zero, after_slow
- * per slow round */
-constexpr int PT_GRAPH_OUTER_KERNELS = 5, PT_GRAPH_INNER_KERNELS = 5;
+/* The batched form's iteration bodies (schedulers), all run as a CUDA
+ * graph whose loops the device schedules:
+ *   SCHED_PHASED:  k_regather, k_try, k_post, slow rounds while the slow
+ *                  list fills the GPU
+ *   SCHED_RUN:     k_regather, k_run (persistent lanes refilled from the
+ *                  active list, 168 registers), slow rounds until the slow
+ *                  list is empty
+ *   SCHED_RUN_WIDE: the same with the 255-register instance of k_run
+ * Every body schedules each particle's own operations in its own order, so
+ * all give the plain form's results bit for bit. */
+enum { SCHED_PHASED = 0, SCHED_RUN = 1, SCHED_RUN_WIDE = 2, SCHED_VARIANTS = 3 };
+const char *const SCHED_NAMES[SCHED_VARIANTS] = {"phase split", "persistent", "persistent wide"};
 
-/* Persistent batched form: one CUDA graph per advance call whose outer WHILE
- * node runs iterations of { rebuild the active list, k_run (lanes refilled
- * from the list), slow rounds (inner WHILE node: k_slow + k_bisect while
- * post-steps are queued) }, every decision taken by one-thread scheduling
- * kernels on the device.  The host launches the graph once per period of at
- * most `period_iters` iterations (checking cancellation, launch and time
- * limits between periods) and finishes the last few particles as
- * plain-form lanes. */
-pt_status advance_persistent(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc, std::chrono::steady_clock::time_point w0,
-                             bool &cancelled, bool &timed_out) {
-    cudaError_t e = cudaSuccess;
+/* Builds the graph of one scheduler: a period kernel, then a WHILE node
+ * over iterations with an inner WHILE node over slow rounds. */
+cudaError_t build_graph(pt_ctx *c, pt_batch *B, const DRun &R, int v, bool tab_only, cudaGraph_t *gout, cudaGraphExec_t *xout) {
     DBatch &b = B->b;
     const int64_t n = b.n;
     const int block = 128;
+    cudaError_t e;
+    cudaGraph_t g = nullptr;
+    if ((e = cudaGraphCreate(&g, 0))) return e;
+    *gout = g;
+    cudaGraphConditionalHandle h_outer, h_slow;
+    if ((e = cudaGraphConditionalHandleCreate(&h_outer, g, 1, cudaGraphCondAssignDefault)) ||
+        (e = cudaGraphConditionalHandleCreate(&h_slow, g, 0, 0)))
+        return e;
+    cudaGraph_t body_outer = nullptr, body_slow = nullptr, tmp = nullptr;
+    if ((e = cudaStreamBeginCaptureToGraph(c->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal))) return e;
+    k_sched_period<<<1, 32, 0, c->stream>>>(b.sched);
+    e = capture_conditional(c->stream, h_outer, cudaGraphCondTypeWhile, &body_outer);
+    cudaError_t e2 = cudaStreamEndCapture(c->stream, &tmp);
+    if (e || (e = e2)) return e;
+    if ((e = cudaStreamBeginCaptureToGraph(c->stream, body_outer, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal))) return e;
+    k_sched_begin<<<1, 32, 0, c->stream>>>(b, b.sched);
+    k_regather<<<grid_for(n, 256), 256, 0, c->stream>>>(b, R.t_pause, R.max_steps, b.list[0], &b.count[0]);
+    if (v == SCHED_PHASED) {
+        const void *try_fn = tab_only ? (const void *)k_try_tab32 : (const void *)k_try;
+        const int g_try = persistent_grid(c, try_fn, block), g_post = persistent_grid(c, (const void *)k_post, block);
+        if (tab_only) k_try_tab32<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, 0, 1, b.sched);
+        else k_try<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, 0, 1, b.sched);
+        k_post<<<g_post, block, 0, c->stream>>>(c->scene, R, b, c->counters, 1, b.sched);
+        k_sched_after_post<<<1, 32, 0, c->stream>>>(b, b.sched, h_slow);
+    } else {
+        const bool wide = v == SCHED_RUN_WIDE;
+        const void *run_fn = wide ? (tab_only ? (const void *)k_run2_tab32 : (const void *)k_run2)
+                                  : (tab_only ? (const void *)k_run_tab32 : (const void *)k_run);
+        const int g_run = persistent_grid(c, run_fn, block);
+        if (wide && tab_only) k_run2_tab32<<<g_run, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched, B->max_run);
+        else if (wide) k_run2<<<g_run, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched, B->max_run);
+        else if (tab_only) k_run_tab32<<<g_run, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched, B->max_run);
+        else k_run<<<g_run, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched, B->max_run);
+        k_sched_after_run<<<1, 32, 0, c->stream>>>(b, b.sched, h_slow);
+    }
+    e = capture_conditional(c->stream, h_slow, cudaGraphCondTypeWhile, &body_slow);
+    if (!e) {
+        if (v == SCHED_PHASED) k_sched_end_phased<<<1, 32, 0, c->stream>>>(b, b.sched, R, h_outer);
+        else k_sched_end<<<1, 32, 0, c->stream>>>(b, b.sched, R, h_outer);
+    }
+    e2 = cudaStreamEndCapture(c->stream, &tmp);
+    if (e || (e = e2)) return e;
+    if ((e = cudaStreamBeginCaptureToGraph(c->stream, body_slow, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal))) return e;
+    const int g_slow = persistent_grid(c, (const void *)k_slow, block), g_bisect = persistent_grid(c, (const void *)k_bisect, block);
+    k_slow<<<g_slow, block, 0, c->stream>>>(c->scene, R, b, c->counters, 1, b.sched);
+    k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 3, 5, 5);
+    k_bisect<<<g_bisect, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched);
+    k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 4, 4, 4);
+    if (v == SCHED_PHASED) k_sched_after_slow_phased<<<1, 32, 0, c->stream>>>(b, b.sched, R, h_slow);
+    else k_sched_after_slow<<<1, 32, 0, c->stream>>>(b, b.sched, R, h_slow);
+    if ((e = cudaStreamEndCapture(c->stream, &tmp))) return e;
+    return cudaGraphInstantiate(xout, g, 0);
+}
+
+/* Batched form: the iterations run inside CUDA graphs (one launch per
+ * period of at most `period_iters` iterations; the host checks
+ * cancellation, launch and time limits between periods) and the last few
+ * particles finish as plain-form lanes.  The scheduler is the caller's
+ * choice or, when left to the autotuner, measured: the first periods of a
+ * batch run a short trial of each scheduler and the one with the least
+ * device time per RK try runs from then on (a choice kept by the batch). */
+pt_status advance_graph(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc, std::chrono::steady_clock::time_point w0, bool &cancelled,
+                        bool &timed_out) {
+    cudaError_t e = cudaSuccess;
+    DBatch &b = B->b;
+    const int64_t n = b.n;
     bool tab_only = R.sp.q == 0 && R.prec == PT_PREC_FP32;
     for (int fi = 0; fi < c->scene.n_fields; ++fi) {
         const DField &f = c->scene.fields[fi];
         const bool box = f.xmin < f.xmax && f.ymin < f.ymax && f.zmin < f.zmax;
         if (f.has_b && !(f.type == PT_FIELD_TAB3D && f.node32 && !(f.bw > 0 && box))) tab_only = false;
     }
-    const bool wide = B->run_blocks == 2; /* the 255-register instance */
-    const void *run_fn = wide ? (tab_only ? (const void *)k_run2_tab32 : (const void *)k_run2)
-                              : (tab_only ? (const void *)k_run_tab32 : (const void *)k_run);
-    const int g_run = persistent_grid(c, run_fn, block);
-    const int g_slow = persistent_grid(c, (const void *)k_slow, block);
-    const int g_bisect = persistent_grid(c, (const void *)k_bisect, block);
     const int tail = (int)std::max<int64_t>(2048, n / 1000);
     const int period_iters = B->period_iters > 0 ? B->period_iters : 64;
-    const int max_run = B->max_run;
-    /* scheduler state and counters */
+    const int trial_iters = 3;
+    /* a batch starts from the scores earlier batches of the same kind
+     * measured on this context (measured again only for untried schedulers) */
+    double *ctx_score = c->tune_score[(R.prec == PT_PREC_FP32 ? 2 : 0) + (tab_only ? 1 : 0)];
+    if (B->scheduler == 0 && B->sched_choice == 0)
+        for (int k = 0; k < SCHED_VARIANTS; ++k)
+            if (!(B->tune_score[k] > 0) && ctx_score[k] > 0) B->tune_score[k] = ctx_score[k];
     DSched &hs = *c->sched_host;
     std::memset(&hs, 0, sizeof(hs));
     for (int k = 0; k < PT_SPANS; ++k) hs.t0[k] = ~0ull;
@@ -732,105 +802,122 @@ pt_status advance_persistent(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &ac
     if ((e = cudaMemcpyAsync(b.sched, &hs, sizeof(DSched), cudaMemcpyHostToDevice, c->stream)) ||
         (e = cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream)) ||
         (e = cudaMemsetAsync(b.count, 0, 8 * sizeof(int32_t), c->stream)))
-        return ck(c, e, "persistent setup"), PT_ERR_CUDA;
+        return ck(c, e, "batched setup"), PT_ERR_CUDA;
     /* budgets count from here; suspended post-steps of an earlier call go to list 3 */
     k_gather<<<grid_for(n, 256), 256, 0, c->stream>>>(b, R.t_pause, b.list[0], &b.count[0]);
     acc.aux_launches += 1;
-    /* the graph */
-    cudaGraph_t g = nullptr;
-    cudaGraphExec_t gx = nullptr;
+    cudaGraph_t gr[SCHED_VARIANTS] = {};
+    cudaGraphExec_t gx[SCHED_VARIANTS] = {};
     pt_status st = PT_OK;
-    auto fail = [&](const char *what) {
-        ck(c, e, what);
-        st = PT_ERR_CUDA;
-    };
-    do {
-        if ((e = cudaGraphCreate(&g, 0))) { fail("graph create"); break; }
-        cudaGraphConditionalHandle h_outer, h_slow;
-        if ((e = cudaGraphConditionalHandleCreate(&h_outer, g, 1, cudaGraphCondAssignDefault)) ||
-            (e = cudaGraphConditionalHandleCreate(&h_slow, g, 0, 0))) { fail("graph handles"); break; }
-        cudaGraph_t body_outer = nullptr, body_slow = nullptr;
-        if ((e = cudaStreamBeginCaptureToGraph(c->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal))) { fail("capture"); break; }
-        k_sched_period<<<1, 32, 0, c->stream>>>(b.sched);
-        e = capture_conditional(c->stream, h_outer, cudaGraphCondTypeWhile, &body_outer);
-        cudaGraph_t tmp = nullptr;
-        cudaError_t e2 = cudaStreamEndCapture(c->stream, &tmp);
-        if (e || (e = e2)) { fail("capture period"); break; }
-        /* outer body: one iteration */
-        if ((e = cudaStreamBeginCaptureToGraph(c->stream, body_outer, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal))) { fail("capture"); break; }
-        k_sched_begin<<<1, 32, 0, c->stream>>>(b, b.sched);
-        k_regather<<<grid_for(n, 256), 256, 0, c->stream>>>(b, R.t_pause, R.max_steps, b.list[0], &b.count[0]);
-        if (wide && tab_only) k_run2_tab32<<<g_run, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched, max_run);
-        else if (wide) k_run2<<<g_run, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched, max_run);
-        else if (tab_only) k_run_tab32<<<g_run, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched, max_run);
-        else k_run<<<g_run, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched, max_run);
-        k_sched_after_run<<<1, 32, 0, c->stream>>>(b, b.sched, h_slow);
-        e = capture_conditional(c->stream, h_slow, cudaGraphCondTypeWhile, &body_slow);
-        if (!e) k_sched_end<<<1, 32, 0, c->stream>>>(b, b.sched, R, h_outer);
-        e2 = cudaStreamEndCapture(c->stream, &tmp);
-        if (e || (e = e2)) { fail("capture iteration"); break; }
-        /* inner body: one slow round */
-        if ((e = cudaStreamBeginCaptureToGraph(c->stream, body_slow, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal))) { fail("capture"); break; }
-        k_slow<<<g_slow, block, 0, c->stream>>>(c->scene, R, b, c->counters, 1, b.sched);
-        k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 3, 5, 5);
-        k_bisect<<<g_bisect, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched);
-        k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 4, 4, 4);
-        k_sched_after_slow<<<1, 32, 0, c->stream>>>(b, b.sched, R, h_slow);
-        if ((e = cudaStreamEndCapture(c->stream, &tmp))) { fail("capture slow round"); break; }
-        if ((e = cudaGraphInstantiate(&gx, g, 0))) { fail("graph instantiate"); break; }
-    } while (false);
-    if (st == PT_OK) {
-        for (int period = 0;; ++period) {
-            if ((e = cudaGraphLaunch(gx, c->stream))) { fail("graph launch"); break; }
-            acc.graph_launches += 1;
-            if ((e = cudaMemcpyAsync(c->sched_host, b.sched, sizeof(DSched), cudaMemcpyDeviceToHost, c->stream)) ||
-                (e = cudaStreamSynchronize(c->stream))) { fail("persistent period"); break; }
-            if (hs.error) {
-                c->err = "batched scheduler: a slow-round loop exceeded its round limit";
+    int64_t iters_of[SCHED_VARIANTS] = {0, 0, 0};
+    unsigned long long prev_tries = 0, prev_ns = 0;
+    int prev_outer = 0;
+    for (int period = 0;; ++period) {
+        /* the scheduler of this period */
+        int v;
+        bool trial = false;
+        if (B->scheduler > 0) v = B->scheduler - 1;
+        else if (B->sched_choice > 0) v = B->sched_choice - 1;
+        else {
+            v = -1;
+            for (int k = 0; k < SCHED_VARIANTS && v < 0; ++k)
+                if (!(B->tune_score[k] > 0)) v = k;
+            trial = v >= 0;
+            if (!trial) {
+                v = 0;
+                for (int k = 1; k < SCHED_VARIANTS; ++k)
+                    if (B->tune_score[k] < B->tune_score[v]) v = k;
+                B->sched_choice = v + 1;
+            }
+        }
+        if (!gx[v]) {
+            e = build_graph(c, B, R, v, tab_only, &gr[v], &gx[v]);
+            if (e) {
+                cudaStreamCaptureStatus cs;
+                if (cudaStreamIsCapturing(c->stream, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+                    cudaGraph_t junk = nullptr;
+                    cudaStreamEndCapture(c->stream, &junk);
+                    if (junk) cudaGraphDestroy(junk);
+                }
+                ck(c, e, "batched graph");
                 st = PT_ERR_CUDA;
                 break;
             }
-            if (*(volatile int *)c->cancel_host) { cancelled = true; break; }
-            if (hs.last_going <= tail) break;
-            const int64_t kernels = (int64_t)hs.outer_iters * PT_GRAPH_OUTER_KERNELS + (int64_t)hs.inner_iters * PT_GRAPH_INNER_KERNELS;
-            if (B->max_launches > 0 && kernels >= B->max_launches) { timed_out = true; break; }
-            if (B->timeout_s > 0 && std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count() > B->timeout_s) {
-                timed_out = true;
-                break;
-            }
+        }
+        const int iters = trial ? trial_iters : period_iters;
+        if ((e = cudaMemcpyAsync(&b.sched->max_iters, &iters, sizeof(int), cudaMemcpyHostToDevice, c->stream)) ||
+            (e = cudaGraphLaunch(gx[v], c->stream))) { ck(c, e, "graph launch"); st = PT_ERR_CUDA; break; }
+        acc.graph_launches += 1;
+        if ((e = cudaMemcpyAsync(c->sched_host, b.sched, sizeof(DSched), cudaMemcpyDeviceToHost, c->stream)) ||
+            (e = cudaMemcpyAsync(c->counters_host, c->counters, sizeof(DCounters), cudaMemcpyDeviceToHost, c->stream)) ||
+            (e = cudaStreamSynchronize(c->stream))) { ck(c, e, "batched period"); st = PT_ERR_CUDA; break; }
+        unsigned long long ns = 0;
+        for (int k = 0; k < PT_SPANS; ++k) ns += hs.ns[k];
+        const unsigned long long tries = c->counters_host->rk_accepted + c->counters_host->rk_rejected;
+        iters_of[v] += hs.outer_iters - prev_outer;
+        if (trial && tries > prev_tries) ctx_score[v] = B->tune_score[v] = (double)(ns - prev_ns) / (double)(tries - prev_tries);
+        else if (trial) B->tune_score[v] = 1e300; /* nothing to measure: not a candidate for this batch */
+        prev_tries = tries;
+        prev_ns = ns;
+        prev_outer = hs.outer_iters;
+        if (hs.error) {
+            c->err = "batched scheduler: a slow-round loop exceeded its round limit";
+            st = PT_ERR_CUDA;
+            break;
+        }
+        if (*(volatile int *)c->cancel_host) { cancelled = true; break; }
+        const bool finished = hs.last_going == 0 && hs.last_slow == 0;
+        if (finished || (hs.last_going <= tail && hs.last_slow == 0)) break;
+        const int64_t kernels = (int64_t)hs.outer_iters * 5 + (int64_t)hs.inner_iters * 5;
+        if (B->max_launches > 0 && kernels >= B->max_launches) { timed_out = true; break; }
+        if (B->timeout_s > 0 && std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count() > B->timeout_s) {
+            timed_out = true;
+            break;
         }
     }
-    if (gx) cudaGraphExecDestroy(gx);
-    if (g) cudaGraphDestroy(g);
+    for (int k = 0; k < SCHED_VARIANTS; ++k) {
+        if (gx[k]) cudaGraphExecDestroy(gx[k]);
+        if (gr[k]) cudaGraphDestroy(gr[k]);
+    }
     if (st != PT_OK) return st;
-    if ((e = cudaMemcpy(c->counters_host, c->counters, sizeof(DCounters), cudaMemcpyDeviceToHost))) return ck(c, e, "counters"), PT_ERR_CUDA;
     add_counters(acc, *c->counters_host);
-    const double run_ms = hs.ns[PT_SPAN_RUN] * 1e-6, slow_ms = hs.ns[PT_SPAN_SLOW] * 1e-6, bisect_ms = hs.ns[PT_SPAN_BISECT] * 1e-6;
-    acc.kernel_ms += run_ms + slow_ms + bisect_ms;
-    /* kernel executions inside the graph: the timed kernels (one k_run per
-     * iteration, k_slow + k_bisect per slow round) and the bookkeeping ones
-     * (scheduling kernels, list rebuild, count resets, one per period) */
-    acc.launches += (int64_t)hs.outer_iters + 2 * (int64_t)hs.inner_iters;
-    acc.aux_launches += (int64_t)hs.outer_iters * (PT_GRAPH_OUTER_KERNELS - 1) + (int64_t)hs.inner_iters * (PT_GRAPH_INNER_KERNELS - 2) +
-                        acc.graph_launches;
+    const double run_ms = hs.ns[PT_SPAN_RUN] * 1e-6, try_ms = hs.ns[PT_SPAN_TRY] * 1e-6, post_ms = hs.ns[PT_SPAN_POST] * 1e-6,
+                 slow_ms = hs.ns[PT_SPAN_SLOW] * 1e-6, bisect_ms = hs.ns[PT_SPAN_BISECT] * 1e-6;
+    acc.kernel_ms += run_ms + try_ms + post_ms + slow_ms + bisect_ms;
+    /* kernel executions inside the graphs: the timed kernels (k_run, or k_try
+     * and k_post, per iteration; k_slow + k_bisect per slow round) and the
+     * bookkeeping ones (scheduling kernels, list rebuild, count resets, one
+     * per period) */
+    const int64_t run_it = iters_of[SCHED_RUN] + iters_of[SCHED_RUN_WIDE], ph_it = iters_of[SCHED_PHASED];
+    acc.launches += run_it + 2 * ph_it + 2 * (int64_t)hs.inner_iters;
+    acc.aux_launches += (run_it + ph_it) * 4 + (int64_t)hs.inner_iters * 3 + acc.graph_launches;
     acc.sched_outer_iters = hs.outer_iters;
     acc.sched_inner_iters = hs.inner_iters;
-    acc.active = hs.last_going;
-    if (!cancelled && !timed_out && hs.last_going > 0) {
+    acc.scheduler = B->scheduler > 0 ? B->scheduler : B->sched_choice;
+    for (int k = 0; k < SCHED_VARIANTS; ++k) acc.tune_ns_per_try[k] = B->tune_score[k] < 1e299 ? B->tune_score[k] : 0;
+    acc.active = hs.last_going + hs.last_slow;
+    if (!cancelled && !timed_out && (hs.last_going > 0 || hs.last_slow > 0)) {
         const double k0 = acc.kernel_ms;
         st = advance_plain(c, B, R, acc, w0, cancelled, timed_out, true);
         acc.tail_ms = acc.kernel_ms - k0;
     }
-    const char *name = wide ? (tab_only ? "k_run2_tab32" : "k_run2") : (tab_only ? "k_run_tab32" : "k_run");
-    double dom = run_ms;
-    int64_t dl = hs.outer_iters;
+    /* the dominant kernel and its launches */
+    const char *name = tab_only ? "k_try_tab32" : "k_try";
+    double dom = try_ms;
+    int64_t dl = ph_it;
+    if (run_ms > dom) {
+        dom = run_ms;
+        dl = run_it;
+        name = iters_of[SCHED_RUN_WIDE] > iters_of[SCHED_RUN] ? (tab_only ? "k_run2_tab32" : "k_run2") : (tab_only ? "k_run_tab32" : "k_run");
+    }
+    if (post_ms > dom) { dom = post_ms; name = "k_post"; dl = ph_it; }
     if (slow_ms > dom) { dom = slow_ms; name = "k_slow"; dl = hs.inner_iters; }
     if (bisect_ms > dom) { dom = bisect_ms; name = "k_bisect"; dl = hs.inner_iters; }
     acc.dominant_kernel_ms = dom;
     acc.dominant_launches = dl;
     std::snprintf(acc.dominant_kernel, sizeof(acc.dominant_kernel), "%s", name);
-    acc.try_ms = run_ms;
-    acc.post_ms = 0;
+    acc.try_ms = run_ms + try_ms;
+    acc.post_ms = post_ms;
     acc.slow_ms = slow_ms;
     acc.bisect_ms = bisect_ms;
     return st;
@@ -956,13 +1043,14 @@ pt_status batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles *in
     if (p->species < PT_NEUTRON || p->species > PT_ELECTRON) { c->err = "unknown species"; return PT_ERR_INVALID; }
     if (p->mode != PT_MODE_PLAIN && p->mode != PT_MODE_BATCHED && p->mode != PT_MODE_PHASED) { c->err = "unknown mode"; return PT_ERR_INVALID; }
     if (p->max_run < 0 || p->period_iters < 0) { c->err = "negative tuning parameter"; return PT_ERR_INVALID; }
+    if (p->scheduler < 0 || p->scheduler > 3) { c->err = "unknown scheduler"; return PT_ERR_INVALID; }
     std::unique_ptr<pt_batch> B(new pt_batch());
     B->ctx = c;
     B->max_launches = p->max_launches;
     B->timeout_s = p->timeout_s;
     B->max_run = p->max_run;
     B->period_iters = p->period_iters;
-    B->run_blocks = p->block_size == 2 ? 2 : 3;
+    B->scheduler = p->scheduler;
     DRun &R = B->run;
     std::memset(&R, 0, sizeof(R));
     R.sp = make_species(p->species);
@@ -1058,7 +1146,7 @@ pt_status pt_batch_advance_steps(pt_ctx *c, pt_batch *B, double t_pause, int32_t
         st = advance_plain(c, B, R, acc, w0, cancelled, timed_out, false);
         if (st != PT_OK) return st;
     } else if (R.mode == PT_MODE_BATCHED && n > 0) {
-        st = advance_persistent(c, B, R, acc, w0, cancelled, timed_out);
+        st = advance_graph(c, B, R, acc, w0, cancelled, timed_out);
         if (st != PT_OK) return st;
     }
     if (R.mode == PT_MODE_PHASED && n > 0) {

@@ -191,7 +191,7 @@ struct DBatch {
  * counts, the period's iteration cap and tail threshold, and the device time
  * of the timed kernels (k_run, k_slow, k_bisect) measured on %globaltimer
  * inside the CUDA graph, where no event can be recorded. */
-enum { PT_SPAN_RUN = 0, PT_SPAN_SLOW = 1, PT_SPAN_BISECT = 2, PT_SPANS = 3 };
+enum { PT_SPAN_RUN = 0, PT_SPAN_SLOW = 1, PT_SPAN_BISECT = 2, PT_SPAN_TRY = 3, PT_SPAN_POST = 4, PT_SPANS = 5 };
 /* Slow rounds of one scheduler iteration before the device loop gives up
  * with an error (every post-step completes after a bounded number of rounds:
  * bisections and chord pieces are bounded, see PT_MAX_*; the cap keeps a
@@ -200,7 +200,7 @@ enum { PT_SPAN_RUN = 0, PT_SPAN_SLOW = 1, PT_SPAN_BISECT = 2, PT_SPANS = 3 };
 struct DSched {
     int outer_iters, inner_iters, period_start, max_iters;
     int tail, last_going, last_active, inner_this; /* inner_this: slow rounds of the current iteration */
-    int error, pad2;                                /* error: the slow-round cap was reached */
+    int error, last_slow;                           /* error: the slow-round cap was reached; post-steps left queued */
     unsigned long long t0[PT_SPANS], t1[PT_SPANS], ns[PT_SPANS], launches[PT_SPANS];
 };
 

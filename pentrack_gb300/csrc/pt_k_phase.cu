@@ -41,7 +41,8 @@ __global__ void k_zero_counts(int32_t *count, int a, int b, int c) {
  * FP32 field mode, magnetic fields all FP32 tables): without the code of the
  * other field types it needs no local memory at 168 registers. */
 template <bool TAB_ONLY>
-static __device__ __forceinline__ void try_phase(const DScene &S, const DRun &R, const DBatch &b, DCounters *C, int in, int out) {
+static __device__ __forceinline__ void try_phase(const DScene &S, const DRun &R, const DBatch &b, DCounters *C, int in, int out, DSched *sc) {
+    span_begin(sc, PT_SPAN_TRY);
     const int n = b.count[in];
     const int32_t *lin = b.list[in];
     Lane L(S, R);
@@ -65,18 +66,23 @@ static __device__ __forceinline__ void try_phase(const DScene &S, const DRun &R,
         }
     }
     flush_counters(C, L.lc, 0.0, false);
+    span_end(sc, PT_SPAN_TRY);
 }
 
-__global__ void __launch_bounds__(128, PT_TRY_BLOCKS_PER_SM) k_try(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out) {
-    try_phase<false>(S, R, b, C, in, out);
+__global__ void __launch_bounds__(128, PT_TRY_BLOCKS_PER_SM) k_try(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out,
+                                                                  DSched *sc) {
+    try_phase<false>(S, R, b, C, in, out, sc);
 }
-__global__ void __launch_bounds__(128, PT_TRY_BLOCKS_PER_SM) k_try_tab32(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out) {
-    try_phase<true>(S, R, b, C, in, out);
+__global__ void __launch_bounds__(128, PT_TRY_BLOCKS_PER_SM) k_try_tab32(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out,
+                                                                        DSched *sc) {
+    try_phase<true>(S, R, b, C, in, out, sc);
 }
 
 /* Batched form, phase 2: the common step completion (no clip, no split, no
  * collision); other steps are queued for phase 3. */
-__global__ void __launch_bounds__(128) k_post(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out) {
+__global__ void __launch_bounds__(128) k_post(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out,
+                                              DSched *sc) {
+    span_begin(sc, PT_SPAN_POST);
     const int n = b.count[2];
     const int32_t *lp = b.list[2];
     Lane L(S, R);
@@ -98,6 +104,7 @@ __global__ void __launch_bounds__(128) k_post(const __grid_constant__ DScene S, 
         }
     }
     flush_counters(C, L.lc, ps, false);
+    span_end(sc, PT_SPAN_POST);
 }
 
 } // namespace ptk

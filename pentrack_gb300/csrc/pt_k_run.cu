@@ -126,6 +126,7 @@ __global__ void k_sched_begin(const __grid_constant__ DBatch b, DSched *sc) {
     if (threadIdx.x != 0) return;
     b.count[0] = 0;
     b.count[1] = 0;
+    b.count[2] = 0;
     b.count[6] = 0;
     sc->outer_iters += 1;
     sc->inner_this = 0;
@@ -163,6 +164,48 @@ __global__ void k_sched_end(const __grid_constant__ DBatch b, DSched *sc, const 
     sc->last_going = going;
     const bool more = going > sc->tail && (sc->outer_iters - sc->period_start) < sc->max_iters && *R.cancel == 0 &&
                       b.count[3] == 0 && !sc->error;
+    cudaGraphSetConditional(outer, more ? 1u : 0u);
+}
+
+/* ---- the phase-split iteration in the same graph form ----
+ * k_regather, k_try (one RK try per active particle), k_post (the common
+ * completion), then slow rounds while the slow list fills the GPU: the
+ * decisions the host-driven phase split takes between its launches, taken
+ * here on the device (count[1]: particles that keep stepping, count[3]:
+ * queued post-steps) */
+static __device__ __forceinline__ bool slow_rounds_due(const DBatch &b, const DSched *sc) {
+    const int active = b.count[1], slow = b.count[3];
+    return slow > 0 && (slow >= max(2048, active / 4) || active == 0 || active <= sc->tail);
+}
+
+__global__ void k_sched_after_post(const __grid_constant__ DBatch b, DSched *sc, cudaGraphConditionalHandle slow) {
+    if (threadIdx.x != 0) return;
+    span_close(sc, PT_SPAN_TRY);
+    span_close(sc, PT_SPAN_POST);
+    sc->last_active = b.count[0];
+    cudaGraphSetConditional(slow, slow_rounds_due(b, sc) ? 1u : 0u);
+}
+
+__global__ void k_sched_after_slow_phased(const __grid_constant__ DBatch b, DSched *sc, const __grid_constant__ DRun R,
+                                          cudaGraphConditionalHandle slow) {
+    if (threadIdx.x != 0) return;
+    span_close(sc, PT_SPAN_SLOW);
+    span_close(sc, PT_SPAN_BISECT);
+    sc->inner_iters += 1;
+    if (++sc->inner_this >= PT_MAX_SLOW_ROUNDS && b.count[3] > 0) sc->error = 1;
+    const bool more = slow_rounds_due(b, sc) && *R.cancel == 0 && !sc->error;
+    cudaGraphSetConditional(slow, more ? 1u : 0u);
+}
+
+__global__ void k_sched_end_phased(const __grid_constant__ DBatch b, DSched *sc, const __grid_constant__ DRun R,
+                                   cudaGraphConditionalHandle outer) {
+    if (threadIdx.x != 0) return;
+    const int going = b.count[1], slow = b.count[3];
+    sc->last_going = going;
+    sc->last_slow = slow;
+    const bool finished = going == 0 && slow == 0;
+    const bool tail = going <= sc->tail && slow == 0;
+    const bool more = !finished && !tail && (sc->outer_iters - sc->period_start) < sc->max_iters && *R.cancel == 0 && !sc->error;
     cudaGraphSetConditional(outer, more ? 1u : 0u);
 }
 

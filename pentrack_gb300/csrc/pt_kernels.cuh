@@ -14,9 +14,17 @@ __global__ void k_init(const __grid_constant__ DScene S, const __grid_constant__
 __global__ void k_gather(const __grid_constant__ DBatch b, double t_pause, int32_t *list, int32_t *count);
 __global__ void k_regather(const __grid_constant__ DBatch b, double t_pause, int max_steps, int32_t *list, int32_t *count);
 __global__ void k_zero_counts(int32_t *count, int a, int b, int c);
-__global__ void k_try(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out);
-__global__ void k_try_tab32(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out);
-__global__ void k_post(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out);
+__global__ void k_try(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out,
+                      DSched *sc);
+__global__ void k_try_tab32(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in,
+                            int out, DSched *sc);
+__global__ void k_post(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out,
+                       DSched *sc);
+__global__ void k_sched_after_post(const __grid_constant__ DBatch b, DSched *sc, cudaGraphConditionalHandle slow);
+__global__ void k_sched_after_slow_phased(const __grid_constant__ DBatch b, DSched *sc, const __grid_constant__ DRun R,
+                                          cudaGraphConditionalHandle slow);
+__global__ void k_sched_end_phased(const __grid_constant__ DBatch b, DSched *sc, const __grid_constant__ DRun R,
+                                   cudaGraphConditionalHandle outer);
 __global__ void k_slow(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out,
                        DSched *sc);
 __global__ void k_bisect(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C,

@@ -276,7 +276,6 @@ class Engine:
 
     def __init__(self, scene, device=0):
         L = lib()
-        self._scene_fields = list(scene.fields)
         self._desc, self._keep = scene.desc()
         h = C.c_void_p()
         st = L.pt_create(C.byref(self._desc), device, C.byref(h))
@@ -334,10 +333,10 @@ class Engine:
         return g, out, stats.as_dict()
 
     def _field_coeffs(self, field):
-        f = self._scene_fields[field]
-        if f["type"] != A.FIELD_HARMONIC:
+        f = self._desc.fields[field]
+        if f.type != A.FIELD_HARMONIC:
             raise ValueError("pt_adjoint differentiates a harmonic-expansion field")
-        return f["g"]
+        return [f.g[k] for k in range(f.n_coeff)]
 
     def field(self, xyzt, precision=A.PREC_FP64):
         q = np.ascontiguousarray(xyzt, dtype=np.float64).reshape(-1, 4)

@@ -18,9 +18,9 @@ import numpy as np
 
 
 def observables(out):
-    """mean phase, mean S.x and |<S>| of a tracked set"""
+    """mean phase, mean S.x, mean S.y and |<S>| of a tracked set"""
     s = out.spin
-    return {"phase": float(np.mean(s[4])), "sx": float(np.mean(s[0])),
+    return {"phase": float(np.mean(s[4])), "sx": float(np.mean(s[0])), "sy": float(np.mean(s[1])),
             "polarisation": float(np.sqrt((np.mean(s[0:3], axis=1) ** 2).sum()))}
 
 
@@ -61,6 +61,8 @@ def observable_cotangents(out, name):
         d[4] = 1.0 / n
     elif name == "sx":
         d[0] = 1.0 / n
+    elif name == "sy":
+        d[1] = 1.0 / n
     elif name == "polarisation":
         m = np.mean(s[0:3], axis=1)
         p = np.sqrt((m ** 2).sum())
@@ -71,7 +73,7 @@ def observable_cotangents(out, name):
     return d
 
 
-def adjoint_gradients(engine, params, particles, field=1, names=("phase", "sx", "polarisation"), checkpoint_interval=1024):
+def adjoint_gradients(engine, params, particles, field=1, names=("phase", "sx", "sy", "polarisation"), checkpoint_interval=1024):
     """(observables, {name: dL/dG over the coefficients of harmonic field
     `field`}) from one forward pass and one pt_adjoint call per observable on
     the GPU (FP64 field mode)."""

@@ -317,9 +317,13 @@ def test_plain_and_batched_forms_are_bit_identical(eng, precision, mode):
         assert sb["graph_launches"] >= 1 and sb["sched_outer_iters"] >= 1
 
 
-@pytest.mark.parametrize("max_run,period", [(0, 0), (3, 2), (1, 1)])
-def test_persistent_form_tuning_is_bit_identical(eng, max_run, period):
-    """Hand-back after max_run consecutive steps and short graph periods only
+@pytest.mark.parametrize("scheduler,max_run,period", [(A.SCHED_PHASED, 0, 0), (A.SCHED_PHASED, 0, 1), (A.SCHED_PERSISTENT, 0, 0),
+                                                      (A.SCHED_PERSISTENT, 3, 2), (A.SCHED_PERSISTENT_WIDE, 1, 1),
+                                                      (A.SCHED_AUTO, 0, 2)])
+def test_batched_schedulers_are_bit_identical(eng, scheduler, max_run, period):
+    """Every scheduler of the batched form (phase split or persistent lanes in
+    the device-scheduled graph, the autotuner switching between them), a
+    hand-back after max_run consecutive steps and short graph periods only
     change which lane runs a particle when: the results stay the plain
     form's, in step budgets as the bench uses them."""
     from pentrack_gb300 import workloads
@@ -332,7 +336,7 @@ def test_persistent_form_tuning_is_bit_identical(eng, max_run, period):
         pb.advance(max_steps=16)
     plain = pb.read()
     params.mode = A.MODE_BATCHED
-    params.max_run, params.period_iters = max_run, period
+    params.max_run, params.period_iters, params.scheduler = max_run, period, scheduler
     bb = e.batch(params, parts)
     for _ in range(3):
         st = bb.advance(max_steps=16)
@@ -340,3 +344,8 @@ def test_persistent_form_tuning_is_bit_identical(eng, max_run, period):
     for k in ("t", "y", "stop_id", "n_hit", "n_step", "h_max", "n_accepted", "n_rejected"):
         assert np.array_equal(getattr(plain, k), getattr(batched, k)), k
     assert st["graph_launches"] >= 1
+    if scheduler == A.SCHED_AUTO:  # the trials ran, one scheduler was chosen
+        assert st["scheduler"] in (A.SCHED_PHASED, A.SCHED_PERSISTENT, A.SCHED_PERSISTENT_WIDE)
+        assert all(x > 0 for x in st["tune_ns_per_try"])
+    else:
+        assert st["scheduler"] == scheduler
