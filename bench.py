@@ -44,7 +44,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=None, help="particles per GPU (default 1e6; 1e7 for large_mesh)")
-    p.add_argument("--workload", default="field_storage", choices=["field_storage", "large_mesh"],
+    p.add_argument("--workload", default="field_storage", choices=["field_storage", "large_mesh", "adjoint_spin"],
                    help="field_storage: the headline configuration; large_mesh: the 200k-triangle, 128^3 scale-up")
     p.add_argument("--batch-steps", type=int, default=32, help="accepted RK steps per particle per bench step")
     p.add_argument("--precision", default="fp32", choices=["fp64", "fp32"],
@@ -59,6 +59,8 @@ def parse():
     p.add_argument("--no-fp64-line", action="store_true", help="skip the FP64-field batched sub-record")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-spin forward / adjoint cost sub-record")
     p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--spin-window", type=float, default=0.2,
+                   help="adjoint_spin workload: lab time every particle advances per bench step (s)")
     return p.parse_args()
 
 
@@ -153,6 +155,8 @@ def make_workload(args, n, engine=None, first_id=0, simtime=None, scene=None):
     kw = {} if simtime is None else {"simtime": simtime}
     if args.workload == "large_mesh":
         return workloads.large_mesh(n=n, engine=engine, first_id=first_id, scene=scene, **kw)
+    if args.workload == "adjoint_spin":
+        return workloads.adjoint_spin(n=n, first_id=first_id, **kw)
     return workloads.field_storage(n=n, engine=engine, first_id=first_id, **kw)
 
 
@@ -534,6 +538,95 @@ def run_ours(args, rank, world):
     return line
 
 
+# Bloch (LOOP D) work per accepted Bloch step, FP64 flops: six precession-axis
+# evaluations (dense-output coefficients 36 + trajectory state 108 + the two
+# harmonic polynomials of B and grad B 140 + equation of motion 60 + BMT and
+# Thomas axis 70 + spin derivative 20) and the stage algebra and error norm
+# (about 290)
+BLOCH_FLOPS = 6 * 434 + 290
+
+
+def run_spin(args, rank, world):
+    """--workload adjoint_spin: the adjoint-spin configuration at its stated
+    size (10,000 UCN per GPU in the cylinder R = 0.2 m, H = 0.12 m of 512
+    segments; B0 = 1 uT + eight l <= 2 harmonic terms; E = 1e6 V/m; specular
+    walls; spins along x; Bloch integration along every trajectory step, FP64
+    field) in bounded steps: each bench step advances every particle by
+    --spin-window s of its 100 s (pt_batch_advance_steps with a lab-time
+    pause), timed with CUDA events on the engine's stream.  Reports
+    particle-s/s, Bloch steps/s and the FP64 roofline of k_plain_spin."""
+    import torch
+    import ctypes
+    from pentrack_gb300 import Engine, _abi as A, workloads, lib
+    device = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(device)
+    sc, params, parts = workloads.adjoint_spin(n=args.n, simtime=100.0, first_id=rank * args.n)
+    e = Engine(sc, device=device)
+    params.mode = A.MODE_PLAIN
+    params.field_precision = A.PREC_FP64
+    peak = ctypes.c_double(0)
+    lib().pt_probe_fp64(e.h, ctypes.byref(peak))
+    batch = e.batch(params, parts)
+    w = args.spin_window
+    for k in range(args.warmup):
+        batch.advance(t_pause=(k + 1) * w)
+    dist = world > 1
+    if dist:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(device)
+    clocks = Clocks(device)
+    clocks.start()
+    psec = ms = 0.0
+    spin = launches = 0
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        st = batch.advance(t_pause=(args.warmup + k + 1) * w)
+        psec += st["particle_seconds"]
+        ms += st["kernel_ms"]
+        spin += st["spin_steps"]
+        launches += st["launches"]
+    torch.cuda.synchronize(device)
+    elapsed = time.perf_counter() - t0
+    clk = clocks.stop()
+    device_s = ms / 1e3
+    if dist:
+        from pentrack_gb300 import replicas
+        device_s, psec_all = replicas.reduce_timing(device_s, psec, device=f"cuda:{device}")
+        torch.distributed.barrier()
+    else:
+        psec_all = psec
+    if rank != 0:
+        return None
+    achieved = spin * BLOCH_FLOPS / (ms / 1e3) / 1e12
+    line = {
+        "metric": "particle-s tracked/s with Bloch spin integration, 1 GB300", "value": psec_all / device_s,
+        "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": device_s * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded Philox sources; harmonic coefficients drawn N(0, 1e-10 T/m^l))",
+        "config": {"workload": f"adjoint spin: {args.n} UCN/GPU x 100 s, cylinder R=0.2 m H=0.12 m (2048 triangles), "
+                               "B0 1 uT + 8 harmonic terms l<=2, E 1e6 V/m, specular walls, spins along x",
+                   "step": f"every particle advances {w:g} s of lab time with Bloch integration",
+                   "form": "plain (k_plain_spin)", "field_precision": "fp64",
+                   "l2": "state 1.6 KB x 1e4 particles is L2-resident; the kernel is FP64-pipe bound",
+                   "parallelism": f"replicas x{world}"},
+        "bloch_steps_per_s": spin / (ms / 1e3), "bloch_steps": int(spin),
+        "gpu_launches": int(launches), "wall_s": elapsed, "clocks": clk,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+                     "frac": achieved / peak.value if peak.value else None,
+                     "peak_source": "measured: pt_probe_fp64 DFMA kernel on this GPU",
+                     "kernel": "k_plain_spin", "fp64_flops_per_bloch_step": BLOCH_FLOPS, "traffic": None},
+    }
+    if not args.no_e2e:
+        try:
+            line["e2e"] = e2e_run(args, e, params, rank, w)
+        except Exception as ex:  # report, never hide
+            line["e2e"] = {"error": str(ex)}
+    if not args.no_cpu_baseline:
+        ref = run_reference_spin(argparse.Namespace(warmup=0, steps=2), 1, os.cpu_count())
+        line["cpu_baseline"] = dict(ref["cpu_baseline"], bloch_steps_per_s=ref["bloch_steps_per_s"])
+    return line
+
+
 def run_reference(args, rank, world):
     """The reference path's CPU implementation (the oracle port: the reference
     itself cannot be built without Boost/CGAL) on all host cores."""
@@ -542,6 +635,8 @@ def run_reference(args, rank, world):
     from oracle import pyoracle
     from pentrack_gb300 import workloads
     cores = os.cpu_count()
+    if args.workload == "adjoint_spin":
+        return run_reference_spin(args, world, cores)
     scene = workloads.field_storage_scene()
     orc = pyoracle.Oracle(scene)
     m = 4096
@@ -566,10 +661,42 @@ def run_reference(args, rank, world):
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_reference_spin(args, world, cores):
+    """The oracle on the adjoint-spin configuration: per step a fresh 512 UCN
+    of the workload tracked with Bloch integration over 0-1 s on all host
+    threads."""
+    from oracle import pyoracle
+    from pentrack_gb300 import workloads
+    m, T = 512, 1.0
+    total_ps = total_s = 0.0
+    spin = 0
+    orc = None
+    for k in range(args.warmup + args.steps):
+        sc, params, parts = workloads.adjoint_spin(n=m, simtime=T, first_id=k * m)
+        orc = orc or pyoracle.Oracle(sc)
+        t0 = time.perf_counter()
+        out, st = orc.integrate(params, parts, nthreads=cores)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            total_ps += st["particle_seconds"]
+            total_s += dt
+            spin += st["spin_steps"]
+    value = total_ps / total_s
+    sample = f"{args.steps} x {m} UCN over 0-{T:g} s with Bloch integration on {cores} threads"
+    return {"metric": "particle-s tracked/s with Bloch spin integration, 1 GB300", "value": value, "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Philox sources; harmonic coefficients drawn N(0, 1e-10 T/m^l))", "impl": "reference",
+            "config": {"workload": "adjoint spin (same scene); " + sample, "parallelism": f"{cores} host threads"},
+            "bloch_steps_per_s": spin / total_s,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def main():
     args = parse()
     if args.n is None:
-        args.n = 10_000_000 if args.workload == "large_mesh" else 1_000_000
+        args.n = {"large_mesh": 10_000_000, "adjoint_spin": 10_000}.get(args.workload, 1_000_000)
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if world > 1:
@@ -580,7 +707,12 @@ def main():
     if args.impl == "ours":
         build.build_engine()
     build.build_oracle()
-    line = run_reference(args, rank, world) if args.impl == "reference" else run_ours(args, rank, world)
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    elif args.workload == "adjoint_spin":
+        line = run_spin(args, rank, world)
+    else:
+        line = run_ours(args, rank, world)
     if rank == 0 and line is not None:
         print(json.dumps(line))
     if world > 1:

@@ -474,6 +474,17 @@ void free_list(std::vector<void *> &l) {
 
 int grid_for(int64_t n, int block) { return (int)((n + block - 1) / block); }
 
+/* Threads per block of the one-lane-per-particle kernels (k_plain,
+ * k_plain_spin, k_adj_*): 128, halved down to 32 while the grid would leave
+ * SMs without a block.  A small batch then spreads over the SMs one warp or
+ * two per SM instead of crowding a few, which matters for the spin kernels:
+ * their Bloch steps are FP64 arithmetic, and the FP64 pipes are per SM. */
+int lane_block(const pt_ctx *c, int64_t n) {
+    int b = 128;
+    while (b > 32 && grid_for(n, b) < c->sm_count) b >>= 1;
+    return b;
+}
+
 void add_counters(pt_stats &acc, const DCounters &k) {
     acc.rk_accepted += k.rk_accepted; acc.rk_rejected += k.rk_rejected; acc.rhs_evals += k.rhs_evals;
     acc.field_evals += k.field_evals; acc.hits += k.hits; acc.bisection_levels += k.bisection_levels;
@@ -506,8 +517,8 @@ bool spin_run(const DRun &R) {
 pt_status advance_plain(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc, std::chrono::steady_clock::time_point w0,
                         bool &cancelled, bool &timed_out, bool from_nacc0) {
     cudaError_t e;
-    const int steps = R.steps_per_launch, block = 128;
     const int64_t n = B->b.n;
+    const int steps = R.steps_per_launch, block = lane_block(c, n);
     const int max_steps = R.max_steps;
     for (int launch = 0;; ++launch) {
         if ((e = cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream))) return ck(c, e, "memset"), PT_ERR_CUDA;
@@ -1347,7 +1358,7 @@ pt_status pt_adjoint(pt_ctx *c, const pt_run_params *p, const pt_particles *in, 
     cudaMemGetInfo(&free_b, &total_b);
     const double budget = std::min((double)free_b * 0.6, 120e9);
     const double tape_b = (double)n * K * STEP_DOUBLES * 8;
-    if (tape_b > 0.5 * budget) { c->err = "pt_adjoint: the chunk tapes (n K 208 B) exceed the device memory budget"; return PT_ERR_OOM; }
+    if (tape_b > 0.5 * budget) { c->err = "pt_adjoint: the chunk tapes (n K 216 B) exceed the device memory budget"; return PT_ERR_OOM; }
     auto clampi = [](double v, double lo, double hi) { return (int)std::max(lo, std::min(hi, v)); };
     int cap_seg = clampi((budget - tape_b) * 0.7 / ((double)n * SEG_DOUBLES * 8), 64, 1 << 20);
     int cap_ck = clampi((budget - tape_b) * 0.3 / ((double)n * CK_DOUBLES * 8), 64, 1 << 22);
@@ -1384,7 +1395,7 @@ pt_status pt_adjoint(pt_ctx *c, const pt_run_params *p, const pt_particles *in, 
         float fms = 0, rms = 0;
         cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream);
         cudaEventRecord(c->ev0, c->stream);
-        k_adj_forward<<<grid_for(n, 128), 128, 0, c->stream>>>(S, R, B->b, c->counters, A);
+        k_adj_forward<<<grid_for(n, lane_block(c, n)), lane_block(c, n), 0, c->stream>>>(S, R, B->b, c->counters, A);
         cudaEventRecord(c->ev1, c->stream);
         if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(hstat.data(), A.status, n * sizeof(int), cudaMemcpyDeviceToHost, c->stream)) ||
             (e = cudaStreamSynchronize(c->stream))) {
@@ -1417,7 +1428,7 @@ pt_status pt_adjoint(pt_ctx *c, const pt_run_params *p, const pt_particles *in, 
         }
         cudaMemsetAsync(c->counters, 0, sizeof(DCounters), c->stream);
         cudaEventRecord(c->ev0, c->stream);
-        k_adj_reverse<<<grid_for(n, 128), 128, 0, c->stream>>>(S, R, B->b, c->counters, A);
+        k_adj_reverse<<<grid_for(n, lane_block(c, n)), lane_block(c, n), 0, c->stream>>>(S, R, B->b, c->counters, A);
         cudaEventRecord(c->ev1, c->stream);
         std::vector<double> g((size_t)n * nc);
         if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(hstat.data(), A.status, n * sizeof(int), cudaMemcpyDeviceToHost, c->stream)) ||
