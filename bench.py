@@ -34,6 +34,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-s tracked/s at stated energy drift: batched vs plain GPU form, 1 GB300"
+SCHED_NAMES = ["autotuning", "phase split (168 registers)", "persistent (168 registers)", "persistent (255 registers)",
+               "phase split (255 registers)"]
 UNIT = "particle-s/s"
 
 
@@ -51,6 +53,9 @@ def parse():
                    help="field evaluation: fp64, or fp32 = FP32 node table (linear base + FP32 Hermite remainder)")
     p.add_argument("--mode", default="batched", choices=["plain", "batched", "phased"],
                    help="batched: persistent lanes + device-scheduled CUDA graph; phased: host-driven phase split")
+    p.add_argument("--scheduler", type=int, default=0, choices=[0, 1, 2, 3, 4],
+                   help="batched/phased forms: 0 autotuned, 1 phase split, 2 persistent, 3 persistent (255 registers), "
+                        "4 phase split (255 registers); the phased form uses the 255-register try kernel for 4")
     p.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison run")
     p.add_argument("--no-phased", action="store_true", help="skip the host-driven phase-split comparison run")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
@@ -59,7 +64,10 @@ def parse():
     p.add_argument("--no-fp64-line", action="store_true", help="skip the FP64-field batched sub-record")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-spin forward / adjoint cost sub-record")
     p.add_argument("--e2e-steps", type=int, default=2)
-    p.add_argument("--spin-window", type=float, default=0.2,
+    p.add_argument("--full-run", action="store_true",
+                   help="field_storage: track --n UCN over the whole 200 s in the batched and the plain form (one call "
+                        "each, to completion) instead of step-batches")
+    p.add_argument("--spin-window", type=float, default=0.5,
                    help="adjoint_spin workload: lab time every particle advances per bench step (s)")
     return p.parse_args()
 
@@ -174,6 +182,7 @@ def setup_ours(args, rank):
     _, params, parts = make_workload(args, count, engine=engine, first_id=first, scene=scene)
     params.field_precision = A.PREC_FP32 if args.precision == "fp32" else A.PREC_FP64
     params.mode = {"batched": A.MODE_BATCHED, "phased": A.MODE_PHASED, "plain": A.MODE_PLAIN}[args.mode]
+    params.scheduler = args.scheduler
     return engine, params, parts, device
 
 
@@ -510,9 +519,8 @@ def run_ours(args, rank, world):
                                         "bisection_levels", "bvh_nodes", "tri_tests", "subsegments", "dense_evals",
                                         "bisect_max", "bisect_dead", "cand_calls", "cand_overflow", "cand_sum", "tri32_tests")},
         "live_particles": int(agg["active"]),
-        "scheduler": {"chosen": ["autotuning", "phase split", "persistent", "persistent (255 registers)"][int(st["scheduler"])],
-                      "autotune_ns_per_try": {"phase split": st["tune_ns_per_try"][0], "persistent": st["tune_ns_per_try"][1],
-                                              "persistent (255 registers)": st["tune_ns_per_try"][2]}},
+        "scheduler": {"chosen": SCHED_NAMES[int(st["scheduler"])],
+                      "autotune_ns_per_try": {SCHED_NAMES[k + 1]: st["tune_ns_per_try"][k] for k in range(4)}},
         "phase_ms": {("k_run" if str(agg["dominant_kernel"]).startswith("k_run") else "k_try"): agg["try_ms"], "k_post": agg["post_ms"],
                      "k_slow": agg["slow_ms"], "k_bisect": agg["bisect_ms"], "k_plain_tail": agg["tail_ms"]},
     }
@@ -627,6 +635,50 @@ def run_spin(args, rank, world):
     return line
 
 
+def run_full(args, rank, world):
+    """--full-run: the field-storage workload over its whole 200 s, every UCN
+    tracked to its end (decay, absorption, loss through the boundary or the
+    end of the run) in one pt_integrate call per form, the regime where
+    trajectory lengths are most uneven (absorbed UCN within ms, stored ones
+    the full 200 s).  Device time of each call (CUDA events / %globaltimer
+    spans on the engine's stream) and wall time; particle-s/s of each form."""
+    import torch
+    from pentrack_gb300 import Engine, _abi as A, workloads
+    device = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(device)
+    sc = workloads.field_storage_scene()
+    e = Engine(sc, device=device)
+    res = {}
+    for form, mode in (("batched", A.MODE_BATCHED), ("plain", A.MODE_PLAIN)):
+        _, params, parts = workloads.field_storage(n=args.n, simtime=200.0, first_id=rank * args.n, engine=e)
+        params.field_precision = A.PREC_FP32 if args.precision == "fp32" else A.PREC_FP64
+        params.mode = mode
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        out, st = e.integrate(params, parts)
+        torch.cuda.synchronize(device)
+        wall = time.perf_counter() - t0
+        dev_s = st["span_ms"] / 1e3
+        ids, counts = np.unique(out.stop_id, return_counts=True)
+        res[form] = {"value": st["particle_seconds"] / dev_s, "unit": UNIT, "device_s": dev_s, "wall_s": wall,
+                     "particle_seconds": st["particle_seconds"], "rk_steps": int(st["rk_accepted"]),
+                     "stop_ids": {int(k): int(c) for k, c in zip(ids, counts)},
+                     "gpu_launches": int(st["launches"] + st["aux_launches"])}
+        if form == "batched":
+            res[form]["scheduler"] = SCHED_NAMES[int(st["scheduler"])]
+    if rank != 0:
+        return None
+    return {"metric": METRIC, "value": res["batched"]["value"], "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
+            "ms_per_step": res["batched"]["device_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64 state, f32 field",
+            "data": "synthetic (seeded Philox sources; analytic quadrupole table)",
+            "config": {"workload": f"field storage, full run: {args.n} UCN/GPU over 0-200 s, every UCN to its end",
+                       "step": "one pt_integrate call per form", "field_precision": args.precision,
+                       "parallelism": f"replicas x{world}"},
+            "batched": res["batched"], "plain": res["plain"],
+            "batched_over_plain": res["batched"]["value"] / res["plain"]["value"]}
+
+
 def run_reference(args, rank, world):
     """The reference path's CPU implementation (the oracle port: the reference
     itself cannot be built without Boost/CGAL) on all host cores."""
@@ -711,6 +763,8 @@ def main():
         line = run_reference(args, rank, world)
     elif args.workload == "adjoint_spin":
         line = run_spin(args, rank, world)
+    elif args.full_run:
+        line = run_full(args, rank, world)
     else:
         line = run_ours(args, rank, world)
     if rank == 0 and line is not None:

@@ -175,7 +175,7 @@ typedef struct pt_run_params {
 } pt_run_params;
 
 /* schedulers of the batched form (results are the same bits with each) */
-enum { PT_SCHED_AUTO = 0, PT_SCHED_PHASED = 1, PT_SCHED_PERSISTENT = 2, PT_SCHED_PERSISTENT_WIDE = 3 };
+enum { PT_SCHED_AUTO = 0, PT_SCHED_PHASED = 1, PT_SCHED_PERSISTENT = 2, PT_SCHED_PERSISTENT_WIDE = 3, PT_SCHED_PHASED_WIDE = 4 };
 
 /* structure-of-arrays particle batch (host memory).  y and spin are
  * component-major: y[c*n + i] is component c of particle i.
@@ -231,7 +231,7 @@ typedef struct pt_stats {
     double adj_forward_ms;     /* pt_adjoint: device time of the recording forward pass(es) */
     double adj_reverse_ms;     /* pt_adjoint: device time of the reverse sweep */
     int64_t scheduler;         /* batched form: the scheduler that ran (PT_SCHED_*; 0 while still tuning) */
-    double tune_ns_per_try[3]; /* batched form: the autotuner's device ns per RK try of each scheduler (0 = untried) */
+    double tune_ns_per_try[4]; /* batched form: the autotuner's device ns per RK try of each scheduler, PT_SCHED_* - 1 (0 = untried) */
 } pt_stats;
 
 typedef struct pt_ctx pt_ctx;

@@ -23,7 +23,7 @@ NEUTRON, PROTON, ELECTRON = 0, 1, 2
 FIELD_TAB3D, FIELD_HARMONIC, FIELD_UNIFORM_E, FIELD_SOLENOID = 1, 2, 3, 4
 MODE_PLAIN, MODE_BATCHED, MODE_PHASED = 0, 1, 2
 PREC_FP64, PREC_FP32 = 0, 1
-SCHED_AUTO, SCHED_PHASED, SCHED_PERSISTENT, SCHED_PERSISTENT_WIDE = 0, 1, 2, 3
+SCHED_AUTO, SCHED_PHASED, SCHED_PERSISTENT, SCHED_PERSISTENT_WIDE, SCHED_PHASED_WIDE = 0, 1, 2, 3, 4
 
 
 class Material(C.Structure):
@@ -96,7 +96,7 @@ class Stats(C.Structure):
         ("bisect_ms", C.c_double), ("bisect_dead", C.c_int64), ("spin_steps", C.c_int64), ("tail_ms", C.c_double), ("aux_launches", C.c_int64),
         ("graph_launches", C.c_int64), ("sched_outer_iters", C.c_int64), ("sched_inner_iters", C.c_int64),
         ("adj_forward_ms", C.c_double), ("adj_reverse_ms", C.c_double),
-        ("scheduler", C.c_int64), ("tune_ns_per_try", C.c_double * 3),
+        ("scheduler", C.c_int64), ("tune_ns_per_try", C.c_double * 4),
     ]
 
     def as_dict(self):

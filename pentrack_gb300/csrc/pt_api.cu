@@ -55,7 +55,7 @@ struct pt_ctx {
     DSched *sched_host = nullptr;   /* pinned copy of a batch's scheduler state */
     /* the autotuner's scores per kind of run (index: field precision x
      * neutral FP32-table right-hand side), kept for later batches */
-    double tune_score[4][3] = {};
+    double tune_score[4][4] = {};
     int sm_count = 0;
     /* device arena kept between pt_integrate calls (their batches are
      * created and destroyed inside the call) */
@@ -110,7 +110,7 @@ struct pt_batch {
     int max_run = 0;        /* persistent scheduler: consecutive steps per lane and particle (0 = budget only) */
     int scheduler = 0;      /* batched form: 0 autotuned, else SCHED_* + 1 */
     int sched_choice = 0;   /* the autotuner's choice for this batch (SCHED_* + 1; 0 = not tuned yet) */
-    double tune_score[3] = {0, 0, 0}; /* device ns per RK try measured for each scheduler */
+    double tune_score[4] = {0, 0, 0, 0}; /* device ns per RK try measured for each scheduler */
 };
 
 namespace {
@@ -568,7 +568,10 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
         const bool box = f.xmin < f.xmax && f.ymin < f.ymax && f.zmin < f.zmax;
         if (f.has_b && !(f.type == PT_FIELD_TAB3D && f.node32 && !(f.bw > 0 && box))) tab_only = false;
     }
-    const void *try_fn = tab_only ? (const void *)k_try_tab32 : (const void *)k_try;
+    /* the 255-register try kernel when the caller names that scheduler */
+    const bool wide = B->scheduler == PT_SCHED_PHASED_WIDE;
+    const void *try_fn = wide ? (tab_only ? (const void *)k_try_tab32_w : (const void *)k_try_w)
+                              : (tab_only ? (const void *)k_try_tab32 : (const void *)k_try);
     const int g_try = persistent_grid(c, try_fn, block);
     const int g_post = persistent_grid(c, (const void *)k_post, block);
     const int g_slow = persistent_grid(c, (const void *)k_slow, block);
@@ -606,7 +609,9 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
         k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, out, 2, 2);
         acc.aux_launches += 1;
         cudaEventRecord(ev[0], c->stream);
-        if (tab_only) k_try_tab32<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, in, out, nullptr);
+        if (wide && tab_only) k_try_tab32_w<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, in, out, nullptr);
+        else if (wide) k_try_w<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, in, out, nullptr);
+        else if (tab_only) k_try_tab32<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, in, out, nullptr);
         else k_try<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, in, out, nullptr);
         cudaEventRecord(ev[1], c->stream);
         k_post<<<g_post, block, 0, c->stream>>>(c->scene, R, b, c->counters, out, nullptr);
@@ -667,7 +672,7 @@ pt_status advance_batched(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc,
         st = advance_plain(c, B, R, acc, w0, cancelled, timed_out, true);
         acc.tail_ms = acc.kernel_ms - k0;
     }
-    const char *name = tab_only ? "k_try_tab32" : "k_try";
+    const char *name = tab_only ? (wide ? "k_try_tab32_w" : "k_try_tab32") : (wide ? "k_try_w" : "k_try");
     double dom = t_try;
     if (t_post > dom) { dom = t_post; name = "k_post"; }
     if (t_slow > dom) { dom = t_slow; name = "k_slow"; }
@@ -713,10 +718,11 @@ cudaError_t capture_conditional(cudaStream_t s, cudaGraphConditionalHandle h, cu
  *                  active list, 168 registers), slow rounds until the slow
  *                  list is empty
  *   SCHED_RUN_WIDE: the same with the 255-register instance of k_run
+ *   SCHED_PHASED_WIDE: SCHED_PHASED with the 255-register instance of k_try
  * Every body schedules each particle's own operations in its own order, so
  * all give the plain form's results bit for bit. */
-enum { SCHED_PHASED = 0, SCHED_RUN = 1, SCHED_RUN_WIDE = 2, SCHED_VARIANTS = 3 };
-const char *const SCHED_NAMES[SCHED_VARIANTS] = {"phase split", "persistent", "persistent wide"};
+enum { SCHED_PHASED = 0, SCHED_RUN = 1, SCHED_RUN_WIDE = 2, SCHED_PHASED_WIDE = 3, SCHED_VARIANTS = 4 };
+static bool sched_phased(int v) { return v == SCHED_PHASED || v == SCHED_PHASED_WIDE; }
 
 /* Builds the graph of one scheduler: a period kernel, then a WHILE node
  * over iterations with an inner WHILE node over slow rounds. */
@@ -741,10 +747,14 @@ cudaError_t build_graph(pt_ctx *c, pt_batch *B, const DRun &R, int v, bool tab_o
     if ((e = cudaStreamBeginCaptureToGraph(c->stream, body_outer, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal))) return e;
     k_sched_begin<<<1, 32, 0, c->stream>>>(b, b.sched);
     k_regather<<<grid_for(n, 256), 256, 0, c->stream>>>(b, R.t_pause, R.max_steps, b.list[0], &b.count[0]);
-    if (v == SCHED_PHASED) {
-        const void *try_fn = tab_only ? (const void *)k_try_tab32 : (const void *)k_try;
+    if (sched_phased(v)) {
+        const bool wide = v == SCHED_PHASED_WIDE;
+        const void *try_fn = wide ? (tab_only ? (const void *)k_try_tab32_w : (const void *)k_try_w)
+                                  : (tab_only ? (const void *)k_try_tab32 : (const void *)k_try);
         const int g_try = persistent_grid(c, try_fn, block), g_post = persistent_grid(c, (const void *)k_post, block);
-        if (tab_only) k_try_tab32<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, 0, 1, b.sched);
+        if (wide && tab_only) k_try_tab32_w<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, 0, 1, b.sched);
+        else if (wide) k_try_w<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, 0, 1, b.sched);
+        else if (tab_only) k_try_tab32<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, 0, 1, b.sched);
         else k_try<<<g_try, block, 0, c->stream>>>(c->scene, R, b, c->counters, 0, 1, b.sched);
         k_post<<<g_post, block, 0, c->stream>>>(c->scene, R, b, c->counters, 1, b.sched);
         k_sched_after_post<<<1, 32, 0, c->stream>>>(b, b.sched, h_slow);
@@ -761,7 +771,7 @@ cudaError_t build_graph(pt_ctx *c, pt_batch *B, const DRun &R, int v, bool tab_o
     }
     e = capture_conditional(c->stream, h_slow, cudaGraphCondTypeWhile, &body_slow);
     if (!e) {
-        if (v == SCHED_PHASED) k_sched_end_phased<<<1, 32, 0, c->stream>>>(b, b.sched, R, h_outer);
+        if (sched_phased(v)) k_sched_end_phased<<<1, 32, 0, c->stream>>>(b, b.sched, R, h_outer);
         else k_sched_end<<<1, 32, 0, c->stream>>>(b, b.sched, R, h_outer);
     }
     e2 = cudaStreamEndCapture(c->stream, &tmp);
@@ -772,7 +782,7 @@ cudaError_t build_graph(pt_ctx *c, pt_batch *B, const DRun &R, int v, bool tab_o
     k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 3, 5, 5);
     k_bisect<<<g_bisect, block, 0, c->stream>>>(c->scene, R, b, c->counters, b.sched);
     k_zero_counts<<<1, 32, 0, c->stream>>>(b.count, 4, 4, 4);
-    if (v == SCHED_PHASED) k_sched_after_slow_phased<<<1, 32, 0, c->stream>>>(b, b.sched, R, h_slow);
+    if (sched_phased(v)) k_sched_after_slow_phased<<<1, 32, 0, c->stream>>>(b, b.sched, R, h_slow);
     else k_sched_after_slow<<<1, 32, 0, c->stream>>>(b, b.sched, R, h_slow);
     if ((e = cudaStreamEndCapture(c->stream, &tmp))) return e;
     return cudaGraphInstantiate(xout, g, 0);
@@ -798,7 +808,10 @@ pt_status advance_graph(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc, st
     }
     const int tail = (int)std::max<int64_t>(2048, n / 1000);
     const int period_iters = B->period_iters > 0 ? B->period_iters : 64;
-    const int trial_iters = 3;
+    /* a trial spans several slow rounds of the phase split (one every few
+     * iterations), so its time per try is not decided by whether a round
+     * happened to fall inside it */
+    const int trial_iters = 12;
     /* a batch starts from the scores earlier batches of the same kind
      * measured on this context (measured again only for untried schedulers) */
     double *ctx_score = c->tune_score[(R.prec == PT_PREC_FP32 ? 2 : 0) + (tab_only ? 1 : 0)];
@@ -820,7 +833,7 @@ pt_status advance_graph(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc, st
     cudaGraph_t gr[SCHED_VARIANTS] = {};
     cudaGraphExec_t gx[SCHED_VARIANTS] = {};
     pt_status st = PT_OK;
-    int64_t iters_of[SCHED_VARIANTS] = {0, 0, 0};
+    int64_t iters_of[SCHED_VARIANTS] = {0, 0, 0, 0};
     unsigned long long prev_tries = 0, prev_ns = 0;
     int prev_outer = 0;
     for (int period = 0;; ++period) {
@@ -899,7 +912,7 @@ pt_status advance_graph(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc, st
      * and k_post, per iteration; k_slow + k_bisect per slow round) and the
      * bookkeeping ones (scheduling kernels, list rebuild, count resets, one
      * per period) */
-    const int64_t run_it = iters_of[SCHED_RUN] + iters_of[SCHED_RUN_WIDE], ph_it = iters_of[SCHED_PHASED];
+    const int64_t run_it = iters_of[SCHED_RUN] + iters_of[SCHED_RUN_WIDE], ph_it = iters_of[SCHED_PHASED] + iters_of[SCHED_PHASED_WIDE];
     acc.launches += run_it + 2 * ph_it + 2 * (int64_t)hs.inner_iters;
     acc.aux_launches += (run_it + ph_it) * 4 + (int64_t)hs.inner_iters * 3 + acc.graph_launches;
     acc.sched_outer_iters = hs.outer_iters;
@@ -913,7 +926,8 @@ pt_status advance_graph(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc, st
         acc.tail_ms = acc.kernel_ms - k0;
     }
     /* the dominant kernel and its launches */
-    const char *name = tab_only ? "k_try_tab32" : "k_try";
+    const bool try_wide = iters_of[SCHED_PHASED_WIDE] > iters_of[SCHED_PHASED];
+    const char *name = tab_only ? (try_wide ? "k_try_tab32_w" : "k_try_tab32") : (try_wide ? "k_try_w" : "k_try");
     double dom = try_ms;
     int64_t dl = ph_it;
     if (run_ms > dom) {
@@ -1054,7 +1068,7 @@ pt_status batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles *in
     if (p->species < PT_NEUTRON || p->species > PT_ELECTRON) { c->err = "unknown species"; return PT_ERR_INVALID; }
     if (p->mode != PT_MODE_PLAIN && p->mode != PT_MODE_BATCHED && p->mode != PT_MODE_PHASED) { c->err = "unknown mode"; return PT_ERR_INVALID; }
     if (p->max_run < 0 || p->period_iters < 0) { c->err = "negative tuning parameter"; return PT_ERR_INVALID; }
-    if (p->scheduler < 0 || p->scheduler > 3) { c->err = "unknown scheduler"; return PT_ERR_INVALID; }
+    if (p->scheduler < 0 || p->scheduler > PT_SCHED_PHASED_WIDE) { c->err = "unknown scheduler"; return PT_ERR_INVALID; }
     std::unique_ptr<pt_batch> B(new pt_batch());
     B->ctx = c;
     B->max_launches = p->max_launches;

@@ -24,7 +24,7 @@ namespace ptk {
 /* ---------------- forward pass with recording ---------------- */
 
 /* One lane per particle, warp-synchronous like k_plain_spin: a lane whose
- * step reaches its Bloch integration runs it one Bloch step per loop
+ * step reaches its Bloch integration runs one try of its Bloch step per loop
  * iteration, every lane stays in the loop and the warp is re-synchronised at
  * its top; the FwdTape hooks record the segments and the checkpoints. */
 __global__ void __launch_bounds__(128) k_adj_forward(const __grid_constant__ DScene S, const __grid_constant__ DRun R,
@@ -50,8 +50,8 @@ __global__ void __launch_bounds__(128) k_adj_forward(const __grid_constant__ DSc
         if (done) continue;
         bool ended = false;
         if (inbloch) {
-            const int r = L.bloch_run(L.bst, L.bx2, 1);
-            if (r == 0) continue;
+            const int r = L.bloch_try(L.bst, L.bx2);
+            if (r == 0 || r == 2) continue;
             L.bloch_finish(r);
             inbloch = false;
             ended = true;
@@ -462,6 +462,7 @@ __global__ void __launch_bounds__(128) k_adj_reverse(const __grid_constant__ DSc
             bs.dt = q[CK_DT];
             for (int c = 0; c < 5; ++c) { bs.x[c] = q[CK_X + c]; bs.dxdt[c] = q[CK_DXDT + c]; }
             bs.steps = (long)q[CK_STEPS];
+            bs.tries = 0;
             double tmp[5];
             L.spin_derivs(bs.x, tmp, bs.ts, bs.w);
             L.tp.n = 0;
@@ -472,7 +473,8 @@ __global__ void __launch_bounds__(128) k_adj_reverse(const __grid_constant__ DSc
             const bool busy = act && left > 0 && !status;
             if (!__any_sync(0xffffffffu, busy)) break;
             if (!busy) continue;
-            const int rr = L.bloch_run(bs, x2, 1);
+            const int rr = L.bloch_try(bs, x2);
+            if (rr == 2) continue; /* rejected: the step is retried in the next pass */
             --left;
             if (rr < 0 || L.tp.overflow) { status |= ADJ_MISMATCH; continue; }
             if (rr == 1 && left > 0) { /* this segment's Bloch integration ended: the next one with Bloch steps */

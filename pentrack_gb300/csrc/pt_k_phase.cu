@@ -38,8 +38,10 @@ __global__ void k_zero_counts(int32_t *count, int a, int b, int c) {
 /* Batched form, phase 1: exactly one Dormand-Prince try for every active
  * particle (all lanes execute the same instruction stream).  k_try_tab32 is
  * the instance with the FP32-table-only right-hand side (neutral species,
- * FP32 field mode, magnetic fields all FP32 tables): without the code of the
- * other field types it needs no local memory at 168 registers. */
+ * FP32 field mode, magnetic fields all FP32 tables).  At 3 blocks per SM
+ * (168 registers) both spill part of the stage vectors to local memory;
+ * the *_w instances at 2 blocks per SM (255 registers) trade a third of the
+ * resident warps for fewer spills, and the autotuner picks between them. */
 template <bool TAB_ONLY>
 static __device__ __forceinline__ void try_phase(const DScene &S, const DRun &R, const DBatch &b, DCounters *C, int in, int out, DSched *sc) {
     span_begin(sc, PT_SPAN_TRY);
@@ -75,6 +77,14 @@ __global__ void __launch_bounds__(128, PT_TRY_BLOCKS_PER_SM) k_try(const __grid_
 }
 __global__ void __launch_bounds__(128, PT_TRY_BLOCKS_PER_SM) k_try_tab32(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out,
                                                                         DSched *sc) {
+    try_phase<true>(S, R, b, C, in, out, sc);
+}
+__global__ void __launch_bounds__(128, 2) k_try_w(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out,
+                                                  DSched *sc) {
+    try_phase<false>(S, R, b, C, in, out, sc);
+}
+__global__ void __launch_bounds__(128, 2) k_try_tab32_w(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in,
+                                                        int out, DSched *sc) {
     try_phase<true>(S, R, b, C, in, out, sc);
 }
 

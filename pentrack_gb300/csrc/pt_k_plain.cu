@@ -32,12 +32,22 @@ __global__ void __launch_bounds__(128) k_plain(const __grid_constant__ DScene S,
 
 /* The plain form for runs that integrate the spin (IntegrateSpin's Bloch
  * integration, LOOP D): the same LOOP-A iterations as k_plain, but a lane
- * whose step reaches its Bloch integration runs it one accepted Bloch step
- * per loop iteration, and every lane of the warp stays in the loop and is
- * re-synchronised at its top.  The lanes in their Bloch integration -- almost
- * all of them, since it takes hundreds of Bloch steps per trajectory step --
- * then execute each Bloch step as one converged pass, where calling it per
- * lane lets the warp split into groups that run it separately. */
+ * whose step reaches its Bloch integration runs one try of its current
+ * Bloch step per loop iteration, and every lane of the warp stays in the
+ * loop and is re-synchronised at its top.  The lanes in their Bloch
+ * integration -- almost all of them, since it takes hundreds of Bloch steps
+ * per trajectory step -- then execute each try as one converged pass: a lane
+ * whose try is rejected retries in the next pass with the others' next
+ * tries, where retrying at once would leave the rest of the warp idle for a
+ * whole try, and calling the integration per lane would let the warp split
+ * into groups that run it separately.
+ * The launch's quota of `steps` trajectory steps is a per-warp one: a lane
+ * that reaches it keeps stepping until every lane of its warp has, then
+ * finishes the step it is in (the trajectory steps of a spin run hold
+ * hundreds of Bloch steps each, so lanes that stopped at their own quota
+ * would leave the warp waiting on its slowest lane for a large part of the
+ * launch).  An exact step budget (max_steps) and the pause time stay exact
+ * per particle, so the results do not depend on where launches end. */
 __global__ void __launch_bounds__(128) k_plain_spin(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C,
                                                     int steps, int budget_from_nacc0) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -55,15 +65,18 @@ __global__ void __launch_bounds__(128) k_plain_spin(const __grid_constant__ DSce
         t0 = L.t;
     }
     int s = 0;
-    bool inbloch = false;
+    const bool exact = R.max_steps > 0;
+    bool inbloch = false, quota = false, closing = false;
     for (;;) {
         __syncwarp();
-        if (__all_sync(0xffffffffu, done)) break;
-        if (done) continue;
+        closing = closing || __all_sync(0xffffffffu, done || quota);
+        const bool idle = done || (closing && !inbloch);
+        if (__all_sync(0xffffffffu, idle)) break;
+        if (idle) continue;
         bool ended = false;
         if (inbloch) {
-            const int r = L.bloch_run(L.bst, L.bx2, 1);
-            if (r == 0) continue;
+            const int r = L.bloch_try(L.bst, L.bx2);
+            if (r == 0 || r == 2) continue;
             L.bloch_finish(r);
             inbloch = false;
             ended = true;
@@ -84,7 +97,8 @@ __global__ void __launch_bounds__(128) k_plain_spin(const __grid_constant__ DSce
         }
         if (ended) {
             ++s;
-            if (L.stop != PT_ID_UNKNOWN || L.t >= R.t_pause || s >= steps || *R.cancel) done = true;
+            if (L.stop != PT_ID_UNKNOWN || L.t >= R.t_pause || (exact && s >= steps) || *R.cancel) done = true;
+            else if (s >= steps) quota = true;
         }
     }
     if (had) {

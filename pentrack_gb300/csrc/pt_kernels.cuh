@@ -18,6 +18,10 @@ __global__ void k_try(const __grid_constant__ DScene S, const __grid_constant__ 
                       DSched *sc);
 __global__ void k_try_tab32(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in,
                             int out, DSched *sc);
+__global__ void k_try_w(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in, int out,
+                        DSched *sc);
+__global__ void k_try_tab32_w(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int in,
+                              int out, DSched *sc);
 __global__ void k_post(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int out,
                        DSched *sc);
 __global__ void k_sched_after_post(const __grid_constant__ DBatch b, DSched *sc, cudaGraphConditionalHandle slow);

@@ -118,6 +118,7 @@ static __device__ __forceinline__ bool rhs_general(const DScene &S, const DRun &
 struct BlochState {
     double ts, dt, x[5], dxdt[5], w[3];
     long steps;
+    int tries; /* tries of the current step so far (0: at a step's top) */
 };
 
 /* Recording hooks of a lane.  The production kernels use NoTape, whose
@@ -479,7 +480,7 @@ template <class Tape> struct LaneT {
     /* TParticle::SpinDerivs (src/particle.cpp:178-193) along the trajectory's dense output */
     __device__ __noinline__ void spin_derivs(const double *Sv, double *dS, double tt, double *Wout = nullptr) {
         double yy[9], dydt[9], B[3], dB[3][3], V, E[3], W[3];
-        calc_state(tt, yy);
+        calc_spin_state(tt, yy);
         bfield<true>(S, R.prec, yy[0], yy[1], yy[2], B, dB);
         efield(S, R.prec, yy[0], yy[1], yy[2], V, E);
         ++lc.fields;
@@ -509,16 +510,36 @@ template <class Tape> struct LaneT {
         bs.ts = x1;
         bs.dt = dt0;
         bs.steps = 0;
+        bs.tries = 0;
         spin_derivs(bs.x, bs.dxdt, bs.ts, Tape::kSpinStages ? bs.w : nullptr);
     }
     /* Runs the stepper from `bs` towards x2 for at most max_steps accepted
      * steps (< 0: no limit).  Returns 1 when x2 is reached (the spin at x2 in
      * spin[]), 0 when max_steps steps are done (state in bs, spin[] = the
-     * state after the last step), -1 on a failed step or the step bound.
-     * The hooks see the top of every step and every accepted step: its start
-     * time, step size, start state and (kSpinStages) the precession axis at
-     * each of its seven stages (the last is the FSAL point). */
+     * state after the last step), -1 on a failed step or the step bound. */
     __device__ __noinline__ int bloch_run(BlochState &bs, double x2, long max_steps) {
+        for (long done = 0;;) {
+            if (max_steps >= 0 && done >= max_steps && bs.tries == 0) {
+                for (int i = 0; i < 5; ++i) spin[i] = bs.x[i];
+                return 0;
+            }
+            const int r = bloch_try(bs, x2);
+            if (r == 2) continue;
+            if (r != 0) return r;
+            ++done;
+        }
+    }
+    /* One try of the stepper's current step (the unit a warp runs
+     * converged: a lane whose try is rejected retries in the next call,
+     * together with the other lanes' next tries).  Returns 2 when the try is
+     * rejected (step size reduced), 0 when it is accepted and x2 is not yet
+     * reached (spin[] = the new state), 1 when x2 is reached (the spin at x2
+     * in spin[]), -1 on the step bound or the 500-try limit.  The hooks see
+     * the top of every step (before its first try) and every accepted step:
+     * its start time, step size, start state and (kSpinStages) the
+     * precession axis at each of its seven stages (the last is the FSAL
+     * point). */
+    __device__ __noinline__ int bloch_try(BlochState &bs, double x2) {
         const double a2 = 1.0 / 5, a3 = 3.0 / 10, a4 = 4.0 / 5, a5 = 8.0 / 9;
         const double b21 = 1.0 / 5;
         const double b31 = 3.0 / 40, b32 = 9.0 / 40;
@@ -533,83 +554,76 @@ template <class Tape> struct LaneT {
         double xo5[5], dxo5[5], k2_[5], k3_[5], k4_[5], k5_[5], k6_[5], xt[5], out[5], dout[5];
         double wst[7][3]; /* precession axis per stage (kSpinStages only) */
         double &ts = bs.ts, &dt_ = bs.dt;
-        double tso = ts;
-        for (long done = 0;; ++done) {
+        const double tso = ts;
+        if (bs.tries == 0) {
             if (bs.steps >= PT_MAX_SPIN_STEPS) return -1;
-            if (max_steps >= 0 && done >= max_steps) {
-                for (int i = 0; i < 5; ++i) spin[i] = x[i];
-                return 0;
-            }
             if (!tp.on_step_top(*this, bs)) return -1;
-            tso = ts;
-            for (int tries = 1;; ++tries) {
-                if (tries > PT_MAX_TRIES) return -1;
-                for (int i = 0; i < 5; ++i) xt[i] = fma(dt_ * b21, dxdt[i], x[i]);
-                spin_derivs(xt, k2_, ts + dt_ * a2, Tape::kSpinStages ? wst[1] : nullptr);
-                for (int i = 0; i < 5; ++i) xt[i] = fma(dt_ * b32, k2_[i], fma(dt_ * b31, dxdt[i], x[i]));
-                spin_derivs(xt, k3_, ts + dt_ * a3, Tape::kSpinStages ? wst[2] : nullptr);
-                for (int i = 0; i < 5; ++i) xt[i] = fma(dt_ * b43, k3_[i], fma(dt_ * b42, k2_[i], fma(dt_ * b41, dxdt[i], x[i])));
-                spin_derivs(xt, k4_, ts + dt_ * a4, Tape::kSpinStages ? wst[3] : nullptr);
-                for (int i = 0; i < 5; ++i)
-                    xt[i] = fma(dt_ * b54, k4_[i], fma(dt_ * b53, k3_[i], fma(dt_ * b52, k2_[i], fma(dt_ * b51, dxdt[i], x[i]))));
-                spin_derivs(xt, k5_, ts + dt_ * a5, Tape::kSpinStages ? wst[4] : nullptr);
-                for (int i = 0; i < 5; ++i)
-                    xt[i] = fma(dt_ * b65, k5_[i], fma(dt_ * b64, k4_[i], fma(dt_ * b63, k3_[i], fma(dt_ * b62, k2_[i], fma(dt_ * b61, dxdt[i], x[i])))));
-                spin_derivs(xt, k6_, ts + dt_, Tape::kSpinStages ? wst[5] : nullptr);
-                for (int i = 0; i < 5; ++i)
-                    out[i] = fma(dt_ * c6, k6_[i], fma(dt_ * c5, k5_[i], fma(dt_ * c4, k4_[i], fma(dt_ * c3, k3_[i], fma(dt_ * c1, dxdt[i], x[i])))));
-                spin_derivs(out, dout, ts + dt_, Tape::kSpinStages ? wst[6] : nullptr);
-                double adt = fabs(dt_), m = 0;
-                for (int i = 0; i < 5; ++i) {
-                    const double er = fma(dt_ * dc7, dout[i], fma(dt_ * dc6, k6_[i], fma(dt_ * dc5, k5_[i], fma(dt_ * dc4, k4_[i],
-                                      fma(dt_ * dc3, k3_[i], (dt_ * dc1) * dxdt[i])))));
-                    const double e = fabs(er) / (eps + eps * (1.0 * fabs(x[i]) + adt * fabs(dxdt[i])));
-                    m = (m < e || e != e) ? e : m;
-                }
-                if (!(m <= 1.0)) {
-                    dt_ *= fmax(0.9 * (m < 1e300 ? ptdm_pow(m, -1.0 / 3.0) : 0.0), 0.2);
-                    continue;
-                }
-                if (Tape::kSpinStages) {
-                    wst[0][0] = bs.w[0]; wst[0][1] = bs.w[1]; wst[0][2] = bs.w[2];
-                    bs.w[0] = wst[6][0]; bs.w[1] = wst[6][1]; bs.w[2] = wst[6][2];
-                }
-                if (!tp.on_spin_step(*this, tso, dt_, x, wst)) return -1;
-                ts += dt_;
-                if (m < 0.5) {
-                    m = fmax(0.00032, m);
-                    dt_ *= 0.9 * ptdm_pow(m, -1.0 / 5.0);
-                }
-                for (int i = 0; i < 5; ++i) { xo5[i] = x[i]; dxo5[i] = dxdt[i]; x[i] = out[i]; dxdt[i] = dout[i]; }
-                break;
-            }
-            ++lc.spin;
-            ++bs.steps;
-            if (ts > x2) { /* overshoot: the continuous extension at x2 */
-                const double W_[6][5] = {
-                    {1.0, -2.8605386690370884, 3.099577878709121, -1.1618105836403092, 0.013917207301610328},
-                    {0.0, 4.047141499642786, -6.345354046938926, 2.795465086414005, -0.04801624082496286},
-                    {0.0, -3.941160071112659, 10.904003027940295, -6.729317509209278, 0.4175162190483098},
-                    {0.0, 2.8419447015870345, -7.547675862959386, 4.957636724931253, -0.5742817428041846},
-                    {0.0, -1.6109886359167997, 4.218915839039518, -2.950103865566732, 0.47312904339639456},
-                    {0.0, 1.523601174836727, -4.329466835790622, 3.0881301470710616, -0.2822644861171672}};
-                const double h = ts - tso, th = (x2 - tso) / h;
-                double hb[6];
-                for (int k = 0; k < 6; ++k) {
-                    double p = W_[k][4];
-                    p = fma(p, th, W_[k][3]);
-                    p = fma(p, th, W_[k][2]);
-                    p = fma(p, th, W_[k][1]);
-                    p = fma(p, th, W_[k][0]);
-                    hb[k] = h * (p * th);
-                }
-                for (int i = 0; i < 5; ++i)
-                    spin[i] = fma(hb[5], dxdt[i], fma(hb[4], k6_[i], fma(hb[3], k5_[i], fma(hb[2], k4_[i], fma(hb[1], k3_[i], fma(hb[0], dxo5[i], xo5[i]))))));
-                return 1;
-            }
-            for (int i = 0; i < 5; ++i) spin[i] = x[i];
-            if (ts >= x2) return 1;
         }
+        if (++bs.tries > PT_MAX_TRIES) return -1;
+        for (int i = 0; i < 5; ++i) xt[i] = fma(dt_ * b21, dxdt[i], x[i]);
+        spin_derivs(xt, k2_, ts + dt_ * a2, Tape::kSpinStages ? wst[1] : nullptr);
+        for (int i = 0; i < 5; ++i) xt[i] = fma(dt_ * b32, k2_[i], fma(dt_ * b31, dxdt[i], x[i]));
+        spin_derivs(xt, k3_, ts + dt_ * a3, Tape::kSpinStages ? wst[2] : nullptr);
+        for (int i = 0; i < 5; ++i) xt[i] = fma(dt_ * b43, k3_[i], fma(dt_ * b42, k2_[i], fma(dt_ * b41, dxdt[i], x[i])));
+        spin_derivs(xt, k4_, ts + dt_ * a4, Tape::kSpinStages ? wst[3] : nullptr);
+        for (int i = 0; i < 5; ++i)
+            xt[i] = fma(dt_ * b54, k4_[i], fma(dt_ * b53, k3_[i], fma(dt_ * b52, k2_[i], fma(dt_ * b51, dxdt[i], x[i]))));
+        spin_derivs(xt, k5_, ts + dt_ * a5, Tape::kSpinStages ? wst[4] : nullptr);
+        for (int i = 0; i < 5; ++i)
+            xt[i] = fma(dt_ * b65, k5_[i], fma(dt_ * b64, k4_[i], fma(dt_ * b63, k3_[i], fma(dt_ * b62, k2_[i], fma(dt_ * b61, dxdt[i], x[i])))));
+        spin_derivs(xt, k6_, ts + dt_, Tape::kSpinStages ? wst[5] : nullptr);
+        for (int i = 0; i < 5; ++i)
+            out[i] = fma(dt_ * c6, k6_[i], fma(dt_ * c5, k5_[i], fma(dt_ * c4, k4_[i], fma(dt_ * c3, k3_[i], fma(dt_ * c1, dxdt[i], x[i])))));
+        spin_derivs(out, dout, ts + dt_, Tape::kSpinStages ? wst[6] : nullptr);
+        double adt = fabs(dt_), m = 0;
+        for (int i = 0; i < 5; ++i) {
+            const double er = fma(dt_ * dc7, dout[i], fma(dt_ * dc6, k6_[i], fma(dt_ * dc5, k5_[i], fma(dt_ * dc4, k4_[i],
+                              fma(dt_ * dc3, k3_[i], (dt_ * dc1) * dxdt[i])))));
+            const double e = fabs(er) / (eps + eps * (1.0 * fabs(x[i]) + adt * fabs(dxdt[i])));
+            m = (m < e || e != e) ? e : m;
+        }
+        if (!(m <= 1.0)) {
+            dt_ *= fmax(0.9 * (m < 1e300 ? ptdm_pow(m, -1.0 / 3.0) : 0.0), 0.2);
+            return 2;
+        }
+        if (Tape::kSpinStages) {
+            wst[0][0] = bs.w[0]; wst[0][1] = bs.w[1]; wst[0][2] = bs.w[2];
+            bs.w[0] = wst[6][0]; bs.w[1] = wst[6][1]; bs.w[2] = wst[6][2];
+        }
+        if (!tp.on_spin_step(*this, tso, dt_, x, wst)) return -1;
+        ts += dt_;
+        if (m < 0.5) {
+            m = fmax(0.00032, m);
+            dt_ *= 0.9 * ptdm_pow(m, -1.0 / 5.0);
+        }
+        for (int i = 0; i < 5; ++i) { xo5[i] = x[i]; dxo5[i] = dxdt[i]; x[i] = out[i]; dxdt[i] = dout[i]; }
+        bs.tries = 0;
+        ++lc.spin;
+        ++bs.steps;
+        if (ts > x2) { /* overshoot: the continuous extension at x2 */
+            const double W_[6][5] = {
+                {1.0, -2.8605386690370884, 3.099577878709121, -1.1618105836403092, 0.013917207301610328},
+                {0.0, 4.047141499642786, -6.345354046938926, 2.795465086414005, -0.04801624082496286},
+                {0.0, -3.941160071112659, 10.904003027940295, -6.729317509209278, 0.4175162190483098},
+                {0.0, 2.8419447015870345, -7.547675862959386, 4.957636724931253, -0.5742817428041846},
+                {0.0, -1.6109886359167997, 4.218915839039518, -2.950103865566732, 0.47312904339639456},
+                {0.0, 1.523601174836727, -4.329466835790622, 3.0881301470710616, -0.2822644861171672}};
+            const double h = ts - tso, th = (x2 - tso) / h;
+            double hb[6];
+            for (int k = 0; k < 6; ++k) {
+                double p = W_[k][4];
+                p = fma(p, th, W_[k][3]);
+                p = fma(p, th, W_[k][2]);
+                p = fma(p, th, W_[k][1]);
+                p = fma(p, th, W_[k][0]);
+                hb[k] = h * (p * th);
+            }
+            for (int i = 0; i < 5; ++i)
+                spin[i] = fma(hb[5], dxdt[i], fma(hb[4], k6_[i], fma(hb[3], k5_[i], fma(hb[2], k4_[i], fma(hb[1], k3_[i], fma(hb[0], dxo5[i], xo5[i]))))));
+            return 1;
+        }
+        for (int i = 0; i < 5; ++i) spin[i] = x[i];
+        return ts >= x2 ? 1 : 0;
     }
 
     /* The neutral-particle equation of motion in the FP32 field mode: B,
@@ -815,6 +829,20 @@ template <class Tape> struct LaneT {
         dense_coef(tt, b);
         for (int i = 0; i < 9; ++i)
             o[i] = fma(b[5], dyn[i], fma(b[4], k6[i], fma(b[3], k5[i], fma(b[2], k4[i], fma(b[1], k3[i], fma(b[0], dxo[i], xo[i]))))));
+        ++lc.dense;
+    }
+    /* the state the precession axis needs: position, velocity and the
+     * polarisation (component 7, constant along a step: its derivative is 0,
+     * so every stage adds an exact zero and calc_state returns xo[7]); the
+     * proper time and the path length are not needed (set to 0) */
+    __device__ void calc_spin_state(double tt, double *o) {
+        double b[6];
+        dense_coef(tt, b);
+        for (int i = 0; i < 6; ++i)
+            o[i] = fma(b[5], dyn[i], fma(b[4], k6[i], fma(b[3], k5[i], fma(b[2], k4[i], fma(b[1], k3[i], fma(b[0], dxo[i], xo[i]))))));
+        o[6] = 0;
+        o[7] = xo[7];
+        o[8] = 0;
         ++lc.dense;
     }
     __device__ void calc_pos(double tt, double *o) {

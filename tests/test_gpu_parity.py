@@ -319,6 +319,7 @@ def test_plain_and_batched_forms_are_bit_identical(eng, precision, mode):
 
 @pytest.mark.parametrize("scheduler,max_run,period", [(A.SCHED_PHASED, 0, 0), (A.SCHED_PHASED, 0, 1), (A.SCHED_PERSISTENT, 0, 0),
                                                       (A.SCHED_PERSISTENT, 3, 2), (A.SCHED_PERSISTENT_WIDE, 1, 1),
+                                                      (A.SCHED_PHASED_WIDE, 0, 0),
                                                       (A.SCHED_AUTO, 0, 2)])
 def test_batched_schedulers_are_bit_identical(eng, scheduler, max_run, period):
     """Every scheduler of the batched form (phase split or persistent lanes in
@@ -345,7 +346,7 @@ def test_batched_schedulers_are_bit_identical(eng, scheduler, max_run, period):
         assert np.array_equal(getattr(plain, k), getattr(batched, k)), k
     assert st["graph_launches"] >= 1
     if scheduler == A.SCHED_AUTO:  # the trials ran, one scheduler was chosen
-        assert st["scheduler"] in (A.SCHED_PHASED, A.SCHED_PERSISTENT, A.SCHED_PERSISTENT_WIDE)
+        assert st["scheduler"] in (A.SCHED_PHASED, A.SCHED_PERSISTENT, A.SCHED_PERSISTENT_WIDE, A.SCHED_PHASED_WIDE)
         assert all(x > 0 for x in st["tune_ns_per_try"])
     else:
         assert st["scheduler"] == scheduler
