@@ -325,6 +325,38 @@ pt_status pt_adjoint(pt_ctx *ctx, const pt_run_params *params, const pt_particle
  * include/trianglemesh.h:181-188) as a bit mask over scene solid indices. */
 pt_status pt_point_solids(pt_ctx *ctx, int64_t n, const double *p, uint64_t *mask);
 
+/* ---- volume particle sources on the device ----
+ * TVolumeSource::CreateParticle (src/source.cpp:102-194) for the cuboid,
+ * cylindrical and STL volumes (TCuboidVolumeSource, TCylindricalVolumeSource,
+ * TSTLVolumeSource: include/source.h:186-331), with or without
+ * PhaseSpaceWeighting, with a flat energy spectrum, the azimuth uniform and
+ * the polar angle sine-distributed, the start time uniform. */
+enum { PT_SOURCE_BOX = 0, PT_SOURCE_CYLINDER = 1, PT_SOURCE_SOLID = 2 };
+typedef struct pt_source_params {
+    int32_t species;
+    int32_t shape;             /* PT_SOURCE_* */
+    uint64_t seed;             /* keys every particle's stream with its id */
+    double lo[3], hi[3];       /* BOX: the box; SOLID: the box points are proposed in (the STL's bounding box) */
+    double rmin, rmax, phimin, phimax, zmin, zmax; /* CYLINDER [m, rad] */
+    int32_t solid;             /* SOLID: index (pt_scene_desc order) of the scene solid whose inside is the volume */
+    int32_t phase_space;       /* PhaseSpaceWeighting: emin/emax bound the total energy H; a point with potential V
+                                  is accepted with probability sqrt(H - V) / sqrt(H - Vmin), kinetic energy H - V */
+    double emin, emax;         /* eV: kinetic energy (or total, phase_space) */
+    double polarization;       /* probability of +1 is (1 + polarization) / 2 */
+    double tmin, tmax;         /* start time, uniform */
+    double thetamin, thetamax, phimin_v, phimax_v; /* velocity direction [rad] */
+    int64_t n_min_samples;     /* phase_space: points for the minimum potential Vmin (0: 100,000) */
+    int32_t max_rounds;        /* proposal rounds per particle (0: 100,000); STL points: 10,000 box proposals each */
+    int32_t reserved;
+} pt_source_params;
+
+/* n particles with ids `ids` from the source: out->id, t, y (9n) and spin
+ * (5n, zero) are written (host buffers); *vmin (may be NULL) receives the
+ * minimum potential of a phase-space weighted source.  PT_ERR_INVALID when
+ * the spectrum lies below that minimum or a particle's rounds run out. */
+pt_status pt_source_volume(pt_ctx *ctx, const pt_source_params *sp, int64_t n, const int64_t *ids, pt_particles *out,
+                           double *vmin);
+
 /* Calibration: FP64 fused-multiply-add throughput of this device measured by
  * a dependent-chain DFMA kernel over all SMs (TFLOP/s, 2 flops per FMA). */
 pt_status pt_probe_fp64(pt_ctx *ctx, double *tflops);

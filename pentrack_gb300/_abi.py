@@ -82,6 +82,22 @@ class Particles(C.Structure):
     ]
 
 
+SOURCE_BOX, SOURCE_CYLINDER, SOURCE_SOLID = 0, 1, 2
+
+
+class SourceParams(C.Structure):
+    _fields_ = [
+        ("species", C.c_int32), ("shape", C.c_int32), ("seed", C.c_uint64),
+        ("lo", C.c_double * 3), ("hi", C.c_double * 3),
+        ("rmin", C.c_double), ("rmax", C.c_double), ("phimin", C.c_double), ("phimax", C.c_double),
+        ("zmin", C.c_double), ("zmax", C.c_double),
+        ("solid", C.c_int32), ("phase_space", C.c_int32),
+        ("emin", C.c_double), ("emax", C.c_double), ("polarization", C.c_double), ("tmin", C.c_double),
+        ("tmax", C.c_double), ("thetamin", C.c_double), ("thetamax", C.c_double), ("phimin_v", C.c_double),
+        ("phimax_v", C.c_double), ("n_min_samples", C.c_int64), ("max_rounds", C.c_int32), ("reserved", C.c_int32),
+    ]
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("kernel_ms", C.c_double), ("span_ms", C.c_double), ("wall_ms", C.c_double), ("particle_seconds", C.c_double),
@@ -134,6 +150,7 @@ def declare(lib):
         "pt_segment_collisions_noalloc": (C.c_int32, [vp, C.c_int64, c_double_p, C.c_int32, c_int32_p, c_double_p,
                                                       c_double_p, c_int32_p, c_double_p]),
         "pt_point_solids": (C.c_int32, [vp, C.c_int64, c_double_p, c_uint64_p]),
+        "pt_source_volume": (C.c_int32, [vp, P(SourceParams), C.c_int64, c_int64_p, P(Particles), c_double_p]),
         "pt_probe_fp64": (C.c_int32, [vp, c_double_p]),
         "pt_version": (C.c_char_p, []),
         "pt_config_load": (C.c_int32, [C.c_char_p, P(vp)]),

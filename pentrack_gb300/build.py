@@ -18,7 +18,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", f"-I{os.path.join(ROOT, 'include')}"]
 
-SOURCES = ["pt_api.cu", "pt_k_phase.cu", "pt_k_run.cu", "pt_k_adjoint.cu", "pt_k_slow.cu", "pt_k_plain.cu", "pt_k_query.cu", "pt_scene.cpp", "pt_host.cpp"]
+SOURCES = ["pt_api.cu", "pt_k_phase.cu", "pt_k_run.cu", "pt_k_adjoint.cu", "pt_k_slow.cu", "pt_k_plain.cu", "pt_k_query.cu", "pt_k_source.cu", "pt_scene.cpp", "pt_host.cpp"]
 
 
 def _run(cmd):

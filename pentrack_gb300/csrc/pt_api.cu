@@ -111,6 +111,8 @@ struct pt_batch {
     int scheduler = 0;      /* batched form: 0 autotuned, else SCHED_* + 1 */
     int sched_choice = 0;   /* the autotuner's choice for this batch (SCHED_* + 1; 0 = not tuned yet) */
     double tune_score[4] = {0, 0, 0, 0}; /* device ns per RK try measured for each scheduler */
+    double tune_ns[4] = {0, 0, 0, 0}, tune_tries[4] = {0, 0, 0, 0}; /* trial sums per scheduler */
+    int tune_windows[4] = {0, 0, 0, 0};                               /* trial windows run per scheduler */
 };
 
 namespace {
@@ -808,10 +810,12 @@ pt_status advance_graph(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc, st
     }
     const int tail = (int)std::max<int64_t>(2048, n / 1000);
     const int period_iters = B->period_iters > 0 ? B->period_iters : 64;
-    /* a trial spans several slow rounds of the phase split (one every few
-     * iterations), so its time per try is not decided by whether a round
-     * happened to fall inside it */
-    const int trial_iters = 12;
+    /* Trials run in round robin, TRIAL_WINDOWS windows of trial_iters
+     * iterations per scheduler, and score the sums: each scheduler is then
+     * sampled over the same stretch of the batch (a step budget thins the
+     * active set towards its end, and the phase split's slow rounds, one
+     * every few iterations, fall into some windows and not others). */
+    const int trial_iters = 4, TRIAL_WINDOWS = 2;
     /* a batch starts from the scores earlier batches of the same kind
      * measured on this context (measured again only for untried schedulers) */
     double *ctx_score = c->tune_score[(R.prec == PT_PREC_FP32 ? 2 : 0) + (tab_only ? 1 : 0)];
@@ -844,10 +848,18 @@ pt_status advance_graph(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc, st
         else if (B->sched_choice > 0) v = B->sched_choice - 1;
         else {
             v = -1;
-            for (int k = 0; k < SCHED_VARIANTS && v < 0; ++k)
-                if (!(B->tune_score[k] > 0)) v = k;
+            for (int k = 0; k < SCHED_VARIANTS; ++k) /* the untried scheduler with the fewest windows */
+                if (!(B->tune_score[k] > 0) && B->tune_windows[k] < TRIAL_WINDOWS && (v < 0 || B->tune_windows[k] < B->tune_windows[v]))
+                    v = k;
             trial = v >= 0;
             if (!trial) {
+                for (int k = 0; k < SCHED_VARIANTS; ++k) {
+                    if (B->tune_score[k] > 0) continue;
+                    /* trials done: score the sums (a scheduler whose windows saw no
+                     * try is no candidate for this batch, and nothing is cached) */
+                    B->tune_score[k] = B->tune_tries[k] > 0 ? B->tune_ns[k] / B->tune_tries[k] : 1e300;
+                    if (B->tune_tries[k] > 0) ctx_score[k] = B->tune_score[k];
+                }
                 v = 0;
                 for (int k = 1; k < SCHED_VARIANTS; ++k)
                     if (B->tune_score[k] < B->tune_score[v]) v = k;
@@ -879,8 +891,11 @@ pt_status advance_graph(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc, st
         for (int k = 0; k < PT_SPANS; ++k) ns += hs.ns[k];
         const unsigned long long tries = c->counters_host->rk_accepted + c->counters_host->rk_rejected;
         iters_of[v] += hs.outer_iters - prev_outer;
-        if (trial && tries > prev_tries) ctx_score[v] = B->tune_score[v] = (double)(ns - prev_ns) / (double)(tries - prev_tries);
-        else if (trial) B->tune_score[v] = 1e300; /* nothing to measure: not a candidate for this batch */
+        if (trial) {
+            B->tune_ns[v] += (double)(ns - prev_ns);
+            B->tune_tries[v] += (double)(tries - prev_tries);
+            B->tune_windows[v] += 1;
+        }
         prev_tries = tries;
         prev_ns = ns;
         prev_outer = hs.outer_iters;
@@ -1500,6 +1515,74 @@ pt_status pt_probe_fp64(pt_ctx *c, double *tflops) {
     cudaFree(d);
     if (e) return ck(c, e, "probe"), PT_ERR_CUDA;
     *tflops = 2.0 * 8.0 * (double)iters * threads * blocks / (ms * 1e-3) / 1e12;
+    return PT_OK;
+}
+
+pt_status pt_source_volume(pt_ctx *c, const pt_source_params *sp, int64_t n, const int64_t *ids, pt_particles *out, double *vmin_out) {
+    if (!c || !sp || n < 0 || (n && (!ids || !out || !out->id || !out->t || !out->y || !out->spin))) return PT_ERR_INVALID;
+    if (sp->species < PT_NEUTRON || sp->species > PT_ELECTRON) { c->err = "pt_source_volume: unknown species"; return PT_ERR_INVALID; }
+    if (sp->shape < PT_SOURCE_BOX || sp->shape > PT_SOURCE_SOLID) { c->err = "pt_source_volume: unknown shape"; return PT_ERR_INVALID; }
+    if (sp->shape == PT_SOURCE_SOLID && (sp->solid < 1 || sp->solid >= c->scene.n_solids)) {
+        c->err = "pt_source_volume: solid must index a scene solid other than the default one";
+        return PT_ERR_INVALID;
+    }
+    DSourceSpec Q{};
+    Q.shape = sp->shape; Q.solid = sp->solid; Q.phase_space = sp->phase_space != 0;
+    Q.max_rounds = sp->max_rounds > 0 ? sp->max_rounds : 100000;
+    Q.seed = sp->seed;
+    for (int a = 0; a < 3; ++a) { Q.lo[a] = sp->lo[a]; Q.hi[a] = sp->hi[a]; }
+    Q.rmin = sp->rmin; Q.rmax = sp->rmax; Q.phimin = sp->phimin; Q.phimax = sp->phimax; Q.zmin = sp->zmin; Q.zmax = sp->zmax;
+    Q.emin = sp->emin; Q.emax = sp->emax; Q.polarization = sp->polarization; Q.tmin = sp->tmin; Q.tmax = sp->tmax;
+    Q.thetamin = sp->thetamin; Q.thetamax = sp->thetamax; Q.phimin_v = sp->phimin_v; Q.phimax_v = sp->phimax_v;
+    const DSpecies spc = make_species(sp->species);
+    cudaSetDevice(c->device);
+    std::vector<void *> tmp;
+    cudaError_t e = cudaSuccess;
+    double vmin = -INFINITY;
+    if (Q.phase_space) { /* FindPotentialMinimum over a fixed sample (src/source.cpp:136-156) */
+        const int64_t m = sp->n_min_samples > 0 ? sp->n_min_samples : 100000;
+        double *dv = dalloc<double>(tmp, m, e);
+        if (e) { free_list(tmp); return ck(c, e, "source alloc"), PT_ERR_OOM; }
+        k_source_vmin<<<grid_for(m, 128), 128, 0, c->stream>>>(c->scene, Q, spc, m, dv);
+        std::vector<double> hv(m);
+        e = cudaGetLastError();
+        if (!e) e = cudaMemcpyAsync(hv.data(), dv, m * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+        if (!e) e = cudaStreamSynchronize(c->stream);
+        if (e) { free_list(tmp); return ck(c, e, "source minimum potential"), PT_ERR_CUDA; }
+        vmin = INFINITY;
+        for (double x : hv) {
+            if (x != x) { free_list(tmp); c->err = "pt_source_volume: no point inside the source volume for a sample"; return PT_ERR_INVALID; }
+            vmin = std::min(vmin, x);
+        }
+        if (vmin > Q.emax) {
+            free_list(tmp);
+            c->err = "pt_source_volume: the spectrum is below the minimal potential energy in the source volume";
+            return PT_ERR_INVALID;
+        }
+    }
+    if (vmin_out) *vmin_out = vmin;
+    if (n == 0) { free_list(tmp); return PT_OK; }
+    const int64_t *dids = dupload(tmp, ids, n, e);
+    double *dt = dalloc<double>(tmp, n, e), *dy = dalloc<double>(tmp, 9 * n, e), *ds = dalloc<double>(tmp, 5 * n, e);
+    int *dst = dalloc<int>(tmp, n, e);
+    if (e) { free_list(tmp); return ck(c, e, "source alloc"), PT_ERR_OOM; }
+    k_source<<<grid_for(n, 128), 128, 0, c->stream>>>(c->scene, Q, spc, n, dids, vmin, dt, dy, ds, dst);
+    std::vector<int> hs(n);
+    e = cudaGetLastError();
+    if (!e) e = cudaMemcpyAsync(out->t, dt, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaMemcpyAsync(out->y, dy, 9 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaMemcpyAsync(out->spin, ds, 5 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaMemcpyAsync(hs.data(), dst, n * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaStreamSynchronize(c->stream);
+    free_list(tmp);
+    if (e) return ck(c, e, "source"), PT_ERR_CUDA;
+    if (out->id != ids) std::memcpy(out->id, ids, n * sizeof(int64_t));
+    int64_t bad = 0;
+    for (int64_t i = 0; i < n; ++i) bad += hs[i] != 0;
+    if (bad) {
+        c->err = "pt_source_volume: no accepted start point for " + std::to_string(bad) + " particles within the rounds";
+        return PT_ERR_INVALID;
+    }
     return PT_OK;
 }
 

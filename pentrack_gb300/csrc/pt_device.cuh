@@ -215,6 +215,16 @@ struct DAdj {
     double *dl_dg;                  /* ncoef x n */
 };
 
+/* a volume source on the device (pt_source_params, checked on the host) */
+struct DSourceSpec {
+    int shape, solid, phase_space, max_rounds;
+    uint64_t seed;
+    double lo[3], hi[3];
+    double rmin, rmax, phimin, phimax, zmin, zmax;
+    double emin, emax, polarization, tmin, tmax;
+    double thetamin, thetamax, phimin_v, phimax_v;
+};
+
 /* device event counters (one set per launch, summed with atomics per block) */
 struct DCounters {
     unsigned long long rk_accepted, rk_rejected, rhs_evals, field_evals, hits, bisection_levels;

@@ -1,0 +1,187 @@
+/*
+ * pt_k_source.cu -- volume particle sources on the device: the initial
+ * states of TVolumeSource::CreateParticle (src/source.cpp:102-194) for the
+ * cuboid, cylindrical and STL volumes (TCuboidVolumeSource,
+ * TCylindricalVolumeSource, TSTLVolumeSource: include/source.h:186-331),
+ * with or without PhaseSpaceWeighting, written straight into the particle
+ * arrays.
+ *
+ * Every particle draws from its own Philox stream (the source stream: bit
+ * 63 of the counter set, keyed by the seed and the particle id), one counter
+ * per draw, in the counter layout of the host-side sources
+ * (pentrack_gb300/sources.py), so a particle's start state does not depend
+ * on the batch it is made in and equals the host path's.
+ */
+#include "pt_kcommon.cuh"
+#include "pt_kernels.cuh"
+
+namespace ptk {
+
+namespace {
+
+constexpr uint64_t SRC_STREAM = 1ull << 63;
+constexpr uint64_t SRC_ROUND = 16;       /* counters per proposal round */
+constexpr uint64_t SRC_H = 1ull << 20;   /* total-energy rounds */
+constexpr uint64_t SRC_PS = 1ull << 22;  /* phase-space rounds: time, polarisation, acceptance */
+constexpr int SRC_STL_ROUNDS = 10000;    /* bounding-box proposals per STL point */
+
+__device__ __forceinline__ double sdraw(uint64_t seed, int64_t id, uint64_t k) { return uniform(seed, id, SRC_STREAM + k); }
+
+/* first counter of the volume point of phase-space round r (round 0: the
+ * minimum-potential samples and the points of unweighted sources) */
+__device__ __forceinline__ uint64_t point_base(int r) { return (uint64_t)(r + 1) << 24; }
+
+/* a point of the source volume from draws at `base` on; false when an STL
+ * volume's bounding-box proposals ran out (RandomPointInVolume,
+ * include/trianglemesh.h:241-265: uniform in the box, kept when inside) */
+__device__ bool volume_point(const DScene &S, const DSourceSpec &Q, uint64_t seed, int64_t id, uint64_t base, double p[3]) {
+    if (Q.shape == PT_SOURCE_BOX) {
+        for (int a = 0; a < 3; ++a) p[a] = Q.lo[a] + sdraw(seed, id, base + a) * (Q.hi[a] - Q.lo[a]);
+        return true;
+    }
+    if (Q.shape == PT_SOURCE_CYLINDER) { /* r from the linear distribution, azimuth and z uniform */
+        const double r = sqrt(sdraw(seed, id, base) * (Q.rmax * Q.rmax - Q.rmin * Q.rmin) + Q.rmin * Q.rmin);
+        const double ph = Q.phimin + sdraw(seed, id, base + 1) * (Q.phimax - Q.phimin);
+        p[0] = r * cos(ph);
+        p[1] = r * sin(ph);
+        p[2] = Q.zmin + sdraw(seed, id, base + 2) * (Q.zmax - Q.zmin);
+        return true;
+    }
+    for (int r = 0; r < SRC_STL_ROUNDS; ++r) {
+        const uint64_t k = base + (uint64_t)r * SRC_ROUND;
+        for (int a = 0; a < 3; ++a) p[a] = Q.lo[a] + sdraw(seed, id, k + a) * (Q.hi[a] - Q.lo[a]);
+        QueryStats qs{0, 0};
+        if ((point_solids(S, p, qs) >> Q.solid) & 1ull) return true;
+    }
+    return false;
+}
+
+/* TParticle::GetInitialTotalEnergy with zero kinetic energy at (t, p) with
+ * polarisation pol: the magnetic, electric and gravitational potential
+ * energies and, for neutrons, the Fermi potential and internal-field term of
+ * the material of the solid the point is in (the solid by
+ * TGeometry::GetSolid's rule: the highest ID among the solids containing the
+ * point that are not ignored at t) */
+__device__ double rest_potential(const DScene &S, const DSpecies &sp, double t, const double p[3], double pol) {
+    double B[3], dB[3][3], V = 0, E[3];
+    bfield<true>(S, PT_PREC_FP64, p[0], p[1], p[2], B, dB);
+    efield(S, PT_PREC_FP64, p[0], p[1], p[2], V, E);
+    double r = 0;
+    if (sp.mu != 0) r = r + (-pol * sp.mu_over_e) * sqrt(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
+    if (sp.q != 0) r = r + sp.q_over_e * V;
+    r = r + sp.mg * p[2];
+    if (sp.kind == PT_NEUTRON) {
+        QueryStats qs{0, 0};
+        const uint64_t mask = point_solids(S, p, qs);
+        int best = 0;
+        bool best_ign = false;
+        for (int s = 1; s < S.n_solids; ++s) {
+            if (!((mask >> s) & 1ull)) continue;
+            const DSolid &d = S.solids[s];
+            bool ign = false;
+            for (int k = 0; k < d.n_ign; ++k) ign = ign || (t >= d.ign[2 * k] && t < d.ign[2 * k + 1]);
+            if (best_ign || (!ign && S.solids[best].id < d.id)) {
+                best = s;
+                best_ign = ign;
+            }
+        }
+        const DMat &m = S.mats[S.solids[best].mat];
+        r = r + (m.fermi_real * 1e-9 - m.ibf * sp.mu_over_e * pol);
+    }
+    return r;
+}
+
+/* the TParticle constructor's speed from the kinetic energy
+ * (src/particle.cpp:45-52): beta^2 from E / mc^2, its series below round-off */
+__device__ double speed_of(double E, double m) {
+    const double Eom = E / m / PT_C0 / PT_C0;
+    const double series = ((((6.0 * Eom - 5.0) * Eom + 4.0) * Eom - 3.0) * Eom + 2.0) * Eom;
+    const double rel = 1.0 - 1.0 / (Eom + 1) / (Eom + 1);
+    const double beta2 = pow(Eom, 6.0) < 2 * 2.220446049250313e-16 ? series : rel;
+    return PT_C0 * sqrt(beta2);
+}
+
+} // namespace
+
+/* FindPotentialMinimum (src/source.cpp:136-156): the rest potential at the
+ * fixed sample points (ids 2^62 + k, k < n, start time and polarisation from
+ * the first phase-space counters), one per thread; NaN where an STL
+ * sample's proposals ran out */
+__global__ void k_source_vmin(const __grid_constant__ DScene S, const __grid_constant__ DSourceSpec Q, DSpecies sp, int64_t n, double *v) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int64_t id = (int64_t)(1ull << 62) + k;
+    const double t = Q.tmin + sdraw(Q.seed, id, SRC_PS + 1) * (Q.tmax - Q.tmin);
+    const double pol = sdraw(Q.seed, id, SRC_PS + 2) < 0.5 * (Q.polarization + 1) ? 1.0 : -1.0;
+    double p[3];
+    v[k] = volume_point(S, Q, Q.seed, id, point_base(0), p) ? rest_potential(S, sp, t, p, pol) : NAN;
+}
+
+/* One particle per thread: its initial time, state (position, velocity,
+ * polarisation) and zero spin.  Unweighted: the point from round 0, the
+ * polarisation, kinetic energy (uniform), azimuth (uniform) and polar angle
+ * (sine distribution) from draws 3-6, the start time from draw 7.
+ * PhaseSpaceWeighting: a total energy H >= vmin (uniform, redrawn), then
+ * rounds of (start time, polarisation, point) until the point's rest
+ * potential V <= H is accepted with probability sqrt(H - V) / sqrt(H - vmin);
+ * kinetic energy H - V.  status[i] = 1 when the rounds ran out. */
+__global__ void k_source(const __grid_constant__ DScene S, const __grid_constant__ DSourceSpec Q, DSpecies sp, int64_t n, const int64_t *ids,
+                         double vmin, double *t_out, double *y, double *spin, int *status) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t id = ids[i];
+    const uint64_t seed = Q.seed;
+    double p[3] = {0, 0, 0}, t0 = 0, pol = 0, ekin = 0;
+    int bad = 0;
+    if (!Q.phase_space) {
+        if (!volume_point(S, Q, seed, id, point_base(0), p)) bad = 1;
+        pol = sdraw(seed, id, 3) < 0.5 * (Q.polarization + 1) ? 1.0 : -1.0;
+        ekin = Q.emin + sdraw(seed, id, 4) * (Q.emax - Q.emin);
+        t0 = Q.tmin + sdraw(seed, id, 7) * (Q.tmax - Q.tmin);
+    } else {
+        double H = NAN;
+        for (int r = 0; r < Q.max_rounds; ++r) {
+            const double h = Q.emin + sdraw(seed, id, SRC_H + (uint64_t)r * SRC_ROUND) * (Q.emax - Q.emin);
+            if (h >= vmin) { H = h; break; }
+        }
+        bool ok = H == H;
+        if (!ok) bad = 1;
+        for (int r = 0; ok && r < Q.max_rounds; ++r) {
+            const uint64_t k = SRC_PS + (uint64_t)(r + 1) * SRC_ROUND;
+            const double tt = Q.tmin + sdraw(seed, id, k + 1) * (Q.tmax - Q.tmin);
+            const double pl = sdraw(seed, id, k + 2) < 0.5 * (Q.polarization + 1) ? 1.0 : -1.0;
+            double q[3];
+            if (!volume_point(S, Q, seed, id, point_base(r + 1), q)) { bad = 1; break; }
+            const double v = rest_potential(S, sp, tt, q, pl);
+            const double u = sdraw(seed, id, k + 3) * sqrt(H - vmin);
+            if (H >= v && sqrt(H - v) > u) {
+                p[0] = q[0]; p[1] = q[1]; p[2] = q[2];
+                t0 = tt;
+                pol = pl;
+                ekin = H - v;
+                ok = false; /* accepted */
+                bad = 0;
+                break;
+            }
+            if (r + 1 == Q.max_rounds) bad = 1;
+        }
+    }
+    const double ph = Q.phimin_v + sdraw(seed, id, 5) * (Q.phimax_v - Q.phimin_v);
+    const double u = sdraw(seed, id, 6);
+    const double th = acos(cos(Q.thetamin) - u * (cos(Q.thetamin) - cos(Q.thetamax)));
+    const double v = speed_of(ekin, sp.m);
+    t_out[i] = t0;
+    y[0 * n + i] = p[0];
+    y[1 * n + i] = p[1];
+    y[2 * n + i] = p[2];
+    y[3 * n + i] = v * cos(ph) * sin(th);
+    y[4 * n + i] = v * sin(ph) * sin(th);
+    y[5 * n + i] = v * cos(th);
+    y[6 * n + i] = 0;
+    y[7 * n + i] = pol;
+    y[8 * n + i] = 0;
+    for (int c = 0; c < 5; ++c) spin[c * n + i] = 0;
+    status[i] = bad;
+}
+
+} // namespace ptk

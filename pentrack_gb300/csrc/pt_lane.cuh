@@ -338,7 +338,7 @@ template <class Tape> struct LaneT {
         const int fl = q[5 * n + i];
         ps.reset = fl & 1; ps.bao = (fl >> 1) & 1; ps.bbo = (fl >> 2) & 1;
         ncand = q[6 * n + i];
-        for (int k = 0; k < PT_MAX_CAND; ++k) cand[k] = q[(7 + k) * n + i];
+        for (int k = 0; k < ncand; ++k) cand[k] = q[(7 + k) * n + i]; /* entries past ncand are never read */
         cand_ta = d[42 * n + i]; cand_tb = d[43 * n + i]; cand_span = d[44 * n + i];
     }
     __device__ void store_post(const DBatch &b, int64_t i) const {
@@ -356,7 +356,7 @@ template <class Tape> struct LaneT {
         q[0 * n + i] = ps.stage; q[1 * n + i] = ps.cs; q[2 * n + i] = ps.nsub; q[3 * n + i] = ps.pass; q[4 * n + i] = ps.bres;
         q[5 * n + i] = (ps.reset ? 1 : 0) | (ps.bao ? 2 : 0) | (ps.bbo ? 4 : 0);
         q[6 * n + i] = ncand;
-        for (int k = 0; k < PT_MAX_CAND; ++k) q[(7 + k) * n + i] = cand[k];
+        for (int k = 0; k < ncand; ++k) q[(7 + k) * n + i] = cand[k];
         d[42 * n + i] = cand_ta; d[43 * n + i] = cand_tb; d[44 * n + i] = cand_span;
     }
     /* what a bisection of a suspended post-step reads: the dense data of the
@@ -384,7 +384,7 @@ template <class Tape> struct LaneT {
         }
         const int32_t *q = b.ps_i;
         ncand = q[6 * n + i];
-        for (int k = 0; k < PT_MAX_CAND; ++k) cand[k] = q[(7 + k) * n + i];
+        for (int k = 0; k < ncand; ++k) cand[k] = q[(7 + k) * n + i]; /* entries past ncand are never read */
         cand_ta = d[42 * n + i]; cand_tb = d[43 * n + i]; cand_span = d[44 * n + i];
     }
     __device__ void store_bisect_result(const DBatch &b, int64_t i) const {
@@ -397,7 +397,7 @@ template <class Tape> struct LaneT {
         q[0 * n + i] = PS_AFTER_BISECT;
         /* the bisection may have narrowed the candidate set */
         q[6 * n + i] = ncand;
-        for (int k = 0; k < PT_MAX_CAND; ++k) q[(7 + k) * n + i] = cand[k];
+        for (int k = 0; k < ncand; ++k) q[(7 + k) * n + i] = cand[k];
         b.ps_d[42 * n + i] = cand_ta; b.ps_d[43 * n + i] = cand_tb; b.ps_d[44 * n + i] = cand_span;
     }
     __device__ void store(const DBatch &b, int64_t i) const {

@@ -364,6 +364,34 @@ class Engine:
         self._check(lib().pt_segment_collisions_noalloc(self.h, n, _dp(s), max_hits, _ip(cnt), _dp(ss), _dp(nn), _ip(sid), _dp(dn)))
         return cnt, ss, nn, sid, dn
 
+    def source_volume(self, ids, seed, species=A.NEUTRON, shape=A.SOURCE_BOX, lo=(0, 0, 0), hi=(0, 0, 0),
+                      cylinder=(0, 0, 0, 0, 0, 0), solid=0, phase_space=False, emin=0.0, emax=0.0, polarization=0.0,
+                      t_range=(0.0, 0.0), theta=(0.0, np.pi), phi=(0.0, 2 * np.pi), n_min_samples=100_000,
+                      max_rounds=100_000):
+        """pt_source_volume: initial states of the particles `ids` from a
+        cuboid (lo, hi), cylindrical (cylinder = rmin, rmax, phimin, phimax,
+        zmin, zmax) or STL volume (scene solid index `solid`, points proposed
+        in the box lo..hi), optionally phase-space weighted, generated on the
+        device.  Returns (ParticleSet, minimum potential or -inf)."""
+        ids = np.ascontiguousarray(ids, dtype=np.int64)
+        n = len(ids)
+        sp = A.SourceParams()
+        sp.species, sp.shape, sp.seed = species, shape, int(seed)
+        for a in range(3):
+            sp.lo[a], sp.hi[a] = lo[a], hi[a]
+        sp.rmin, sp.rmax, sp.phimin, sp.phimax, sp.zmin, sp.zmax = cylinder
+        sp.solid, sp.phase_space = solid, int(bool(phase_space))
+        sp.emin, sp.emax, sp.polarization = emin, emax, polarization
+        sp.tmin, sp.tmax = t_range
+        sp.thetamin, sp.thetamax = theta
+        sp.phimin_v, sp.phimax_v = phi
+        sp.n_min_samples, sp.max_rounds = n_min_samples, max_rounds
+        out = ParticleSet(n, ids.copy())
+        vmin = C.c_double(0)
+        P = out.abi(outputs=False)
+        self._check(lib().pt_source_volume(self.h, C.byref(sp), n, _lp(out.id), C.byref(P), C.byref(vmin)))
+        return out, vmin.value
+
     def point_solids(self, pts):
         p = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
         m = np.zeros(len(p), np.uint64)

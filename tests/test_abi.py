@@ -67,7 +67,8 @@ def test_ctypes_layout_equals_the_c_compilers(tmp_path):
     if cc is None:
         pytest.skip("no C compiler")
     structs = {"pt_material": A.Material, "pt_solid": A.Solid, "pt_field": A.Field, "pt_scene_desc": A.SceneDesc,
-               "pt_run_params": A.RunParams, "pt_particles": A.Particles, "pt_stats": A.Stats}
+               "pt_run_params": A.RunParams, "pt_particles": A.Particles, "pt_stats": A.Stats,
+               "pt_source_params": A.SourceParams}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "pentrack_gpu.h"', "int main(void) {"]
     expect = []
     for cname, cls in structs.items():

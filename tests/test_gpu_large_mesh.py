@@ -1,6 +1,6 @@
-"""The large-mesh geometry (needs a GB300): the 200,000-triangle
-noise-perturbed torus and sphere with a tricubic multipole (32^3 here, so the
-oracle's reference-layout table stays small), GPU vs oracle over 0.5 s.
+"""The large-mesh configuration (needs a GB300): the 200,000-triangle
+noise-perturbed torus and sphere with the tricubic multipole at the
+configuration's 128^3 (and at 32^3), 2,000 UCN, GPU vs oracle over 0.5 s.
 
 Tolerances as for the field-storage physics test: the device and the oracle
 evaluate the same tricubic in different exact forms, so force differences of
@@ -14,11 +14,12 @@ from pentrack_gb300 import _abi as A
 pytestmark = pytest.mark.gpu
 
 
-def test_large_mesh_short_parity(built, oracle_mod):
+@pytest.mark.parametrize("table_n", [32, 128])
+def test_large_mesh_short_parity(built, oracle_mod, table_n):
     from pentrack_gb300 import Engine, workloads
-    sc = workloads.large_mesh_scene(table_n=32)
+    sc = workloads.large_mesh_scene(table_n=table_n)
     e = Engine(sc)
-    _, params, parts = workloads.large_mesh(n=2000, simtime=0.5, table_n=32, scene=sc, engine=e)
+    _, params, parts = workloads.large_mesh(n=2000, simtime=0.5, table_n=table_n, scene=sc, engine=e)
     oout, ost = oracle_mod.Oracle(sc).integrate(params, parts)
     params.mode = A.MODE_BATCHED
     gout, gst = e.integrate(params, parts)
