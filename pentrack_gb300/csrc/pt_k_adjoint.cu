@@ -170,7 +170,7 @@ static __device__ void rhs_adj(RLane &L, const DField &F, int nc, double t, cons
     const double lW[3] = {Ss[1] * lk[2] - Ss[2] * lk[1] + q * W[0], Ss[2] * lk[0] - Ss[0] * lk[2] + q * W[1],
                           Ss[0] * lk[1] - Ss[1] * lk[0] + q * W[2]};
     double yt[9];
-    L.calc_state(t, yt);
+    L.calc_spin_state(t, yt); /* position and velocity as the forward's spin_derivs had them */
     const double *v = yt + 3;
     const double v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
     const double gr = 1. / sqrt(1. - v2 * PT_INV_C0_SQ);

@@ -96,4 +96,4 @@ def test_spectrum_below_minimum_is_refused(storage):
     sc, e = storage
     with pytest.raises(EngineError):
         e.source_volume(np.arange(16), SEED, shape=A.SOURCE_BOX, lo=(-0.1, -0.1, 0.03), hi=(0.1, 0.1, 0.04),
-                        phase_space=True, emin=0.0, emax=1e-12, polarization=-1.0, n_min_samples=1000)
+                        phase_space=True, emin=-2.0, emax=-1.0, n_min_samples=1000)
