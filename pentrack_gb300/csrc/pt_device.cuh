@@ -29,7 +29,7 @@
 #define PT_MAX_LAMBERT 10000
 #define PT_MAX_SUBSEGMENTS (1 << 20) /* chord pieces of one RK step */
 #define PT_MAX_HITS_PER_SEGMENT 64   /* surfaces crossed by one chord piece */
-#define PT_MAX_CAND 96               /* candidate triangles kept for a bisection */
+#define PT_MAX_CAND 48               /* candidate triangles kept for a bisection */
 #define PT_MAX_SPIN_STEPS (1 << 22)  /* spin (Bloch) steps within one trajectory step */
 
 /* lane flags */

@@ -990,7 +990,6 @@ template <class Tape> struct LaneT {
         ++lc.cand_calls;
         if (ncand < 0) {
             ++lc.cand_overflow;
-            cand_span = 2 * (tb - ta); /* retry once the search has halved the interval */
         } else {
             lc.cand_sum += ncand;
             cand_ta = ta;
@@ -998,8 +997,8 @@ template <class Tape> struct LaneT {
         }
     }
     /* candidates for [ta, tb] when the current set does not cover it and the
-     * interval is at most a quarter of the last one built for, or half of
-     * the last one that overflowed */
+     * interval is at most a quarter of the last one tried (a set that
+     * overflowed is retried once the search has narrowed) */
     __device__ void refresh_candidates(double ta, double tb) {
         if (cand_cover(ta, tb) || !(tb - ta <= 0.25 * cand_span) || ta < to || tb > tn) return;
         prepare_candidates(ta, tb);
