@@ -6,6 +6,10 @@
 
 namespace ptk {
 
+/* k_plain_spin's batching of trajectory work: lanes waiting before they run
+ * it together, and the passes a lane waits at most */
+constexpr int TRAJ_BATCH = 8, TRAJ_WAIT = 16;
+
 /* Plain form: every lane advances its particle by up to `steps` LOOP-A
  * iterations, then the launch ends and the host relaunches. */
 __global__ void __launch_bounds__(128) k_plain(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int steps,
@@ -64,42 +68,64 @@ __global__ void __launch_bounds__(128) k_plain_spin(const __grid_constant__ DSce
         L.load(b, i);
         t0 = L.t;
     }
-    int s = 0;
+    int s = 0, fin = 0, waited = 0;
     const bool exact = R.max_steps > 0;
     bool inbloch = false, quota = false, closing = false;
+    /* a trajectory step ended: count it; true when the lane stops here */
+    auto step_end = [&]() {
+        ++s;
+        if (L.stop != PT_ID_UNKNOWN || L.t >= R.t_pause || (exact && s >= steps) || *R.cancel) done = true;
+        else if (s >= steps) quota = true;
+        return done || (quota && closing);
+    };
     for (;;) {
         __syncwarp();
         closing = closing || __all_sync(0xffffffffu, done || quota);
-        const bool idle = done || (closing && !inbloch);
+        const bool idle = done || (closing && !inbloch && !fin);
         if (__all_sync(0xffffffffu, idle)) break;
+        /* The trajectory work (completing a finished Bloch integration and
+         * the next trajectory step with its collision checks and
+         * bisections) runs for the lanes that need it together: once
+         * TRAJ_BATCH of them wait, once one has waited TRAJ_WAIT passes, or
+         * when no lane is in its Bloch integration.  Run one lane at a time,
+         * it would hold the warp's other lanes for whole bisections. */
+        const bool traj = !idle && !inbloch;
+        const int ntraj = __popc(__ballot_sync(0xffffffffu, traj));
+        const bool go = ntraj >= TRAJ_BATCH || !__any_sync(0xffffffffu, !idle && inbloch) ||
+                        __any_sync(0xffffffffu, traj && waited >= TRAJ_WAIT);
         if (idle) continue;
-        bool ended = false;
         if (inbloch) {
             const int r = L.bloch_try(L.bst, L.bx2);
-            if (r == 0 || r == 2) continue;
-            L.bloch_finish(r);
-            inbloch = false;
-            ended = true;
-        } else {
-            int r;
-            do { r = L.rk_try(); } while (r == 0);
-            if (r < 0) {
-                L.stop = PT_ID_ODEINT_ERROR;
-                ended = true;
-            } else {
-                L.ps.stage = PS_BEGIN;
-                int q;
-                while ((q = L.post_resume<true>()) == 1)
-                    L.ps.bres = L.bisect(L.ps.cx1, L.ps.cya, L.ps.x2, L.ps.y2, L.ps.bxa, L.ps.bao, L.ps.bxb, L.ps.bbo);
-                if (q == 2) inbloch = true;
-                else ended = true;
+            if (r != 0 && r != 2) {
+                fin = r;
+                inbloch = false;
+                waited = 0;
             }
+            continue;
         }
-        if (ended) {
-            ++s;
-            if (L.stop != PT_ID_UNKNOWN || L.t >= R.t_pause || (exact && s >= steps) || *R.cancel) done = true;
-            else if (s >= steps) quota = true;
+        if (!go) {
+            ++waited;
+            continue;
         }
+        waited = 0;
+        if (fin) {
+            L.bloch_finish(fin);
+            fin = 0;
+            if (step_end()) continue;
+        }
+        int r;
+        do { r = L.rk_try(); } while (r == 0);
+        if (r < 0) {
+            L.stop = PT_ID_ODEINT_ERROR;
+            step_end();
+            continue;
+        }
+        L.ps.stage = PS_BEGIN;
+        int q;
+        while ((q = L.post_resume<true>()) == 1)
+            L.ps.bres = L.bisect(L.ps.cx1, L.ps.cya, L.ps.x2, L.ps.y2, L.ps.bxa, L.ps.bao, L.ps.bxb, L.ps.bbo);
+        if (q == 2) inbloch = true;
+        else step_end();
     }
     if (had) {
         L.store(b, i);
