@@ -201,6 +201,32 @@ __device__ void adj_bfield(const DScene &S, double x, double y, double z, double
     }
 }
 
+/* every basis field b_k = dB/dG_k (k < nc) of harmonic field f at a point,
+ * from the basis polynomials over the field's monomials (each monomial
+ * value formed once) */
+__device__ void adj_basis_all(const DField &f, int nc, double x, double y, double z, double (*b)[3]) {
+    x += f.offset[0];
+    y += f.offset[1];
+    z += f.offset[2];
+    double px[7], py[7], pz[7];
+    px[0] = py[0] = pz[0] = 1.0;
+    for (int i = 1; i <= f.hp_deg; ++i) { px[i] = px[i - 1] * x; py[i] = py[i - 1] * y; pz[i] = pz[i - 1] * z; }
+    const int n = f.hp_n;
+    for (int k = 0; k < nc; ++k) b[k][0] = b[k][1] = b[k][2] = 0;
+    for (int m = 0; m < n; ++m) {
+        const int e = f.hp_e[m];
+        const double v = px[e & 15] * py[(e >> 4) & 15] * pz[(e >> 8) & 15];
+        for (int k = 0; k < nc; ++k) {
+            const double *c = f.basis_hp + (size_t)k * 3 * n + m;
+            b[k][0] = fma(c[0], v, b[k][0]);
+            b[k][1] = fma(c[n], v, b[k][1]);
+            b[k][2] = fma(c[2 * n], v, b[k][2]);
+        }
+    }
+    for (int k = 0; k < nc; ++k)
+        for (int i = 0; i < 3; ++i) b[k][i] *= f.bscale;
+}
+
 /* basis field b_k = dB/dG_k of coefficient k of harmonic field f and, when
  * db != nullptr, its Jacobian */
 __device__ void adj_basis(const DField &f, int k, double x, double y, double z, double b[3], double (*db)[3]) {

@@ -434,11 +434,30 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
                 /* one potential per coefficient with G = 1: the basis fields of the adjoint */
                 std::vector<double> bc;
                 std::vector<int> be, start(1, 0);
+                /* and each basis field B_k = grad Phi_k over the field's monomials */
+                int deg = o.hp_deg;
+                std::vector<int> mon;
+                for (int d = 0; d <= deg; ++d)
+                    for (int a = d; a >= 0; --a)
+                        for (int bb = d - a; bb >= 0; --bb) mon.push_back(a | bb << 4 | (d - a - bb) << 8);
+                const int nm = (int)mon.size();
+                std::vector<double> bhp((size_t)f.n_coeff * 3 * nm, 0.0);
                 for (int k = 0; k < f.n_coeff; ++k) {
                     std::vector<double> ck1;
                     std::vector<int> ek1;
                     const double one = 1.0;
                     if (!pth::harmonic_polynomial(1, f.l + k, f.m + k, &one, ck1, ek1, err)) return PT_ERR_INVALID;
+                    for (size_t t = 0; t < ck1.size(); ++t) {
+                        const int E[3] = {ek1[t] & 15, (ek1[t] >> 4) & 15, (ek1[t] >> 8) & 15};
+                        for (int i = 0; i < 3; ++i) {
+                            if (E[i] == 0) continue;
+                            int D[3] = {E[0], E[1], E[2]};
+                            D[i] -= 1;
+                            const int key = D[0] | D[1] << 4 | D[2] << 8;
+                            for (int q = 0; q < nm; ++q)
+                                if (mon[q] == key) bhp[((size_t)k * 3 + i) * nm + q] += ck1[t] * E[i];
+                        }
+                    }
                     bc.insert(bc.end(), ck1.begin(), ck1.end());
                     be.insert(be.end(), ek1.begin(), ek1.end());
                     start.push_back((int)bc.size());
@@ -447,6 +466,7 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
                 o.term_start = dupload(c->allocs, start.data(), start.size(), e);
                 if (!e) o.basis_c = dupload(c->allocs, bc.data(), bc.size(), e);
                 if (!e) o.basis_e = dupload(c->allocs, be.data(), be.size(), e);
+                if (!e) o.basis_hp = dupload(c->allocs, bhp.data(), bhp.size(), e);
                 if (e) return ck(c, e, "upload harmonic basis"), PT_ERR_CUDA;
             }
             for (int k = 0; k < 3; ++k) o.offset[k] = f.offset[k];
@@ -847,10 +867,17 @@ pt_status advance_graph(pt_ctx *c, pt_batch *B, const DRun &R, pt_stats &acc, st
         if (B->scheduler > 0) v = B->scheduler - 1;
         else if (B->sched_choice > 0) v = B->sched_choice - 1;
         else {
+            /* the untried scheduler with the fewest windows, in index order in
+             * even rounds and in reverse order in odd ones (0 1 2 3 3 2 1 0), so
+             * that no scheduler's windows all fall late in a batch */
+            int wmin = TRIAL_WINDOWS;
+            for (int k = 0; k < SCHED_VARIANTS; ++k)
+                if (!(B->tune_score[k] > 0)) wmin = std::min(wmin, B->tune_windows[k]);
             v = -1;
-            for (int k = 0; k < SCHED_VARIANTS; ++k) /* the untried scheduler with the fewest windows */
-                if (!(B->tune_score[k] > 0) && B->tune_windows[k] < TRIAL_WINDOWS && (v < 0 || B->tune_windows[k] < B->tune_windows[v]))
-                    v = k;
+            for (int k = 0; k < SCHED_VARIANTS; ++k) {
+                const int kk = (wmin & 1) ? SCHED_VARIANTS - 1 - k : k;
+                if (v < 0 && !(B->tune_score[kk] > 0) && B->tune_windows[kk] == wmin && wmin < TRIAL_WINDOWS) v = kk;
+            }
             trial = v >= 0;
             if (!trial) {
                 for (int k = 0; k < SCHED_VARIANTS; ++k) {

@@ -123,6 +123,9 @@ struct DField {
     const int *term_start;
     const double *basis_c;
     const int *basis_e;
+    /* the basis fields themselves as polynomials over the hp monomials:
+     * n_terms x 3 rows of hp_n coefficients (b_k,x, b_k,y, b_k,z) */
+    const double *basis_hp;
     double sol_a, sol_b, sol_B0; /* solenoid radius, half length, mu0 n I / pi */
 };
 

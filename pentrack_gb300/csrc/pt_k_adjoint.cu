@@ -44,36 +44,57 @@ __global__ void __launch_bounds__(128) k_adj_forward(const __grid_constant__ DSc
         t0 = L.t;
         done = L.stop != PT_ID_UNKNOWN;
     }
-    for (;;) {
+    int fin = 0, waited = 0;
+    /* a trajectory step ended (or the tape ran out): whether the lane stops */
+    auto step_end = [&]() {
+        if (L.tp.status || L.stop != PT_ID_UNKNOWN) done = true;
+        else if (*R.cancel) { L.tp.status |= ADJ_CANCELLED; done = true; }
+        return done;
+    };
+    for (;;) { /* the passes of k_plain_spin, trajectory work batched the same way */
         __syncwarp();
         if (__all_sync(0xffffffffu, done)) break;
+        const bool traj = !done && !inbloch;
+        const int ntraj = __popc(__ballot_sync(0xffffffffu, traj));
+        const bool go = ntraj >= TRAJ_BATCH || !__any_sync(0xffffffffu, !done && inbloch) ||
+                        __any_sync(0xffffffffu, traj && waited >= TRAJ_WAIT);
         if (done) continue;
-        bool ended = false;
         if (inbloch) {
             const int r = L.bloch_try(L.bst, L.bx2);
-            if (r == 0 || r == 2) continue;
-            L.bloch_finish(r);
-            inbloch = false;
-            ended = true;
-        } else {
-            int r;
-            do { r = L.rk_try(); } while (r == 0);
-            if (r < 0) {
-                L.stop = PT_ID_ODEINT_ERROR;
-                ended = true;
-            } else {
-                L.ps.stage = PS_BEGIN;
-                int q;
-                while ((q = L.post_resume<true>()) == 1)
-                    L.ps.bres = L.bisect(L.ps.cx1, L.ps.cya, L.ps.x2, L.ps.y2, L.ps.bxa, L.ps.bao, L.ps.bxb, L.ps.bbo);
-                if (q == 2) inbloch = true;
-                else ended = true;
+            if (r != 0 && r != 2) {
+                fin = r;
+                inbloch = false;
+                waited = 0;
             }
+            if (L.tp.status) done = true;
+            continue;
         }
-        if (L.tp.status) done = true;
-        else if (ended) {
-            if (L.stop != PT_ID_UNKNOWN) done = true;
-            else if (*R.cancel) { L.tp.status |= ADJ_CANCELLED; done = true; }
+        if (!go) {
+            ++waited;
+            continue;
+        }
+        waited = 0;
+        if (fin) {
+            L.bloch_finish(fin);
+            fin = 0;
+            if (step_end()) continue;
+        }
+        int r;
+        do { r = L.rk_try(); } while (r == 0);
+        if (r < 0) {
+            L.stop = PT_ID_ODEINT_ERROR;
+            step_end();
+            continue;
+        }
+        L.ps.stage = PS_BEGIN;
+        int q;
+        while ((q = L.post_resume<true>()) == 1)
+            L.ps.bres = L.bisect(L.ps.cx1, L.ps.cya, L.ps.x2, L.ps.y2, L.ps.bxa, L.ps.bao, L.ps.bxb, L.ps.bbo);
+        if (q == 2) {
+            inbloch = true;
+            if (L.tp.status) done = true;
+        } else {
+            step_end();
         }
     }
     if (have) {
@@ -179,7 +200,7 @@ static __device__ void rhs_adj(RLane &L, const DField &F, int nc, double t, cons
     double lB[3];
     for (int k = 0; k < 3; ++k) lB[k] = cb * ((1 - gr) * vl * v[k] + gr * lW[k]);
     double B[3], dB[3][3];
-    adj_bfield(L.S, yt[0], yt[1], yt[2], B, dB, nullptr);
+    bfield64<true>(L.S, yt[0], yt[1], yt[2], B, dB); /* the forward's B polynomials */
     double V, E[3];
     efield(L.S, L.R.prec, yt[0], yt[1], yt[2], V, E);
     const double ce = cb * gr * PT_INV_C0_SQ;
@@ -188,11 +209,9 @@ static __device__ void rhs_adj(RLane &L, const DField &F, int nc, double t, cons
     lam[3] = ce * (lW[1] * E[2] - lW[2] * E[1]);
     lam[4] = ce * (lW[2] * E[0] - lW[0] * E[2]);
     lam[5] = ce * (lW[0] * E[1] - lW[1] * E[0]);
-    for (int k = 0; k < nc; ++k) {
-        double bk[3];
-        adj_basis(F, k, yt[0], yt[1], yt[2], bk, nullptr);
-        lG[k] += lB[0] * bk[0] + lB[1] * bk[1] + lB[2] * bk[2];
-    }
+    double bk[PT_ADJ_MAX_COEF][3];
+    adj_basis_all(F, nc, yt[0], yt[1], yt[2], bk);
+    for (int k = 0; k < nc; ++k) lG[k] += lB[0] * bk[k][0] + lB[1] * bk[k][1] + lB[2] * bk[k][2];
     dense_adj(L, t, lam, a);
 }
 

@@ -6,10 +6,6 @@
 
 namespace ptk {
 
-/* k_plain_spin's batching of trajectory work: lanes waiting before they run
- * it together, and the passes a lane waits at most */
-constexpr int TRAJ_BATCH = 8, TRAJ_WAIT = 16;
-
 /* Plain form: every lane advances its particle by up to `steps` LOOP-A
  * iterations, then the launch ends and the host relaunches. */
 __global__ void __launch_bounds__(128) k_plain(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int steps,

@@ -38,6 +38,13 @@ static __device__ __forceinline__ void flush_counters(DCounters *C, const LaneCo
 }
 
 /* append v to a work list (warp-aggregated atomic) */
+/* The warp-synchronous spin kernels' batching of trajectory work (completing
+ * a Bloch integration, the next trajectory step, its collision checks and
+ * bisections): lanes that need it wait until TRAJ_BATCH of them do, or one
+ * has waited TRAJ_WAIT passes, or no lane of the warp is in its Bloch
+ * integration, and then run it together. */
+constexpr int TRAJ_BATCH = 8, TRAJ_WAIT = 16;
+
 static __device__ __forceinline__ void list_push(int32_t *list, int32_t *count, int32_t v) {
     const unsigned m = __activemask();
     const int lane = threadIdx.x & 31;

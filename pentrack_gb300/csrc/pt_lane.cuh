@@ -461,20 +461,27 @@ template <class Tape> struct LaneT {
     __device__ __forceinline__ void eom_fields(const double *yy, const double B[3], const double (*dB)[3], const double E[3], double *d) const {
         eom(R.sp, yy, B, dB, E, d);
     }
-    /* TParticle::SpinPrecessionAxis (src/particle.cpp:148-175) */
+    /* TParticle::SpinPrecessionAxis (src/particle.cpp:148-175).  Three of
+     * its six divisions are folded (B.v / v^2 once for the three components
+     * of the parallel field, -gamma / gr as -gamma sqrt(1 - v^2/c^2)): on
+     * GB300 an FP64 division is a sequence of a dozen FP64-pipe
+     * instructions, and the axis is evaluated six times per Bloch step.
+     * The result differs from the unfolded expression by rounding only. */
     __device__ void spin_axis(const double B[3], const double E[3], const double *dydt, double W[3]) const {
         const double v2 = dydt[0] * dydt[0] + dydt[1] * dydt[1] + dydt[2] * dydt[2];
-        const double gr = 1. / sqrt(1. - v2 * PT_INV_C0_SQ);
+        const double sq = sqrt(1. - v2 * PT_INV_C0_SQ);
+        const double gr = 1. / sq;
         const double Bdotv = B[0] * dydt[0] + B[1] * dydt[1] + B[2] * dydt[2];
+        const double bv = Bdotv / v2;
         double Bpar[3], vxE[3], axv[3];
-        for (int j = 0; j < 3; ++j) Bpar[j] = Bdotv * dydt[j] / v2;
+        for (int j = 0; j < 3; ++j) Bpar[j] = bv * dydt[j];
         vxE[0] = dydt[1] * E[2] - dydt[2] * E[1];
         vxE[1] = dydt[2] * E[0] - dydt[0] * E[2];
         vxE[2] = dydt[0] * E[1] - dydt[1] * E[0];
         axv[0] = dydt[4] * dydt[2] - dydt[5] * dydt[1];
         axv[1] = dydt[5] * dydt[0] - dydt[3] * dydt[2];
         axv[2] = dydt[3] * dydt[1] - dydt[4] * dydt[0];
-        const double cb = -R.sp.gamma / gr, ct = gr * gr / (gr + 1) * PT_INV_C0_SQ;
+        const double cb = -R.sp.gamma * sq, ct = gr * gr / (gr + 1) * PT_INV_C0_SQ;
         for (int j = 0; j < 3; ++j) W[j] = cb * ((1 - gr) * Bpar[j] + gr * B[j] - gr * vxE[j] * PT_INV_C0_SQ) + ct * axv[j];
     }
     /* TParticle::SpinDerivs (src/particle.cpp:178-193) along the trajectory's dense output */
