@@ -172,7 +172,30 @@ typedef struct pt_run_params {
     int32_t period_iters;      /* batched form: scheduler iterations per graph launch (0 = 64) */
     int32_t scheduler;         /* batched form: PT_SCHED_* (PT_SCHED_AUTO: measured on the batch's first periods) */
     int32_t reserved3;
+    /* event logs (TLogger::PrintHit / PrintSnapshot, src/logger.cpp:128-235):
+     * hitlog: one record per wall hit that changes the particle's solid (after
+     * its OnHit); snapshotlog: at the first of the snapshot times in each
+     * trajectory step's [start, end), the dense-output state.  Records are read
+     * with pt_log_read after the call (pt_integrate) or the advances
+     * (pt_batch_*, collected from pt_batch_create on). */
+    int32_t hitlog, snapshotlog;
+    const double *snapshots;   /* snapshot times [s] (snapshotlog) */
+    int32_t n_snapshots;       /* at most PT_MAX_SNAPSHOTS */
+    int32_t reserved4;
+    int64_t log_capacity;      /* records kept per log (0: 1,000,000); later events are counted, not kept */
 } pt_run_params;
+
+enum { PT_LOG_HIT = 0, PT_LOG_SNAPSHOT = 1 };
+#define PT_MAX_SNAPSHOTS 1024
+/* hit record: particle, t, x, y, z, v1x, v1y, v1z, pol1, v2x, v2y, v2z, pol2,
+ * nx, ny, nz, solid1 (leaving), solid2 (entering) -- the reference's hit-log
+ * columns after jobnumber */
+#define PT_HIT_RECORD 18
+/* snapshot record: particle, t, y[9] (x, y, z, vx, vy, vz, proper time,
+ * polarisation, path length), spin[5], stopID, Nspinflip, no-flip
+ * probability, Nhit, Nstep, Hmax -- what TLogger::Print needs besides the
+ * particle's start and the fields */
+#define PT_SNAPSHOT_RECORD 22
 
 /* schedulers of the batched form (results are the same bits with each) */
 enum { PT_SCHED_AUTO = 0, PT_SCHED_PHASED = 1, PT_SCHED_PERSISTENT = 2, PT_SCHED_PERSISTENT_WIDE = 3, PT_SCHED_PHASED_WIDE = 4 };
@@ -263,6 +286,12 @@ pt_status pt_batch_advance(pt_ctx *ctx, pt_batch *batch, double t_pause, pt_stat
  * RK steps in this call (one fixed step-batch of the plain form; 0 = no limit). */
 pt_status pt_batch_advance_steps(pt_ctx *ctx, pt_batch *batch, double t_pause, int32_t max_steps, pt_stats *stats);
 pt_status pt_batch_read(pt_ctx *ctx, pt_batch *batch, pt_particles *out);
+/* The records of log `kind` (PT_LOG_HIT, PT_LOG_SNAPSHOT) collected by the
+ * last pt_integrate call or since the last pt_batch_create: *total receives the
+ * number of events, up to `cap` records (of PT_HIT_RECORD / PT_SNAPSHOT_RECORD
+ * doubles, in no particular order) are copied to `rec` (may be NULL with
+ * cap = 0 to ask for the count). */
+pt_status pt_log_read(pt_ctx *ctx, int32_t kind, int64_t cap, double *rec, int64_t *total);
 void pt_batch_destroy(pt_batch *batch);
 
 /* Field of the whole scene at n points (x,y,z,t interleaved, 4n doubles):

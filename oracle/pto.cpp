@@ -529,7 +529,12 @@ struct Scene {
 
 } // namespace
 
-struct pto_ctx { Scene sc; };
+/* the event logs of the last pto_track call (TLogger::PrintHit /
+ * PrintSnapshot records, the library's record layout) */
+struct pto_ctx {
+    Scene sc;
+    std::vector<double> hits, snaps;
+};
 
 /* ------------------------------------------------------------------ */
 /* Particle tracking                                                   */
@@ -716,6 +721,8 @@ struct Tracker {
     int64_t nacc = 0, nrej = 0;
     pt_stats *stats;
     std::vector<Coll> cbuf;
+    int64_t pid = 0;                        /* the particle being tracked */
+    std::vector<double> hitlog, snaplog;    /* records of this thread's particles */
 
     Tracker(const Scene &s, const pt_run_params &p, pt_stats *stt) : sc(s), P(p), sp(species_of(p.species)), st(1e-9, 1e-9), stats(stt) {}
 
@@ -1089,6 +1096,12 @@ struct Tracker {
                 else if (x2 == x1 && y2[0] == y1[0] && y2[1] == y1[1] && y2[2] == y1[2]) traversed = false;
                 else { stopID = PT_ID_GEOMETRY_ERROR; return true; }
             }
+            if (P.hitlog) { /* TLogger::PrintHit (src/logger.cpp:202-235) */
+                const double r[PT_HIT_RECORD] = {(double)pid, x1, y1[0], y1[1], y1[2], y1[3], y1[4], y1[5], y1[7], y2[3], y2[4], y2[5],
+                                                  y2[7], c->normal[0], c->normal[1], c->normal[2], (double)sc.solids[leaving].id,
+                                                  (double)sc.solids[entering].id};
+                hitlog.insert(hitlog.end(), r, r + PT_HIT_RECORD);
+            }
         }
         if (traversed) cur = ns;
         return altered || stopID != PT_ID_UNKNOWN;
@@ -1195,6 +1208,7 @@ struct Tracker {
     /* TTracker::IntegrateParticle (src/tracking.cpp:17-173) */
     void integrate(int64_t id, double t0, const double *ystart, const double *spinstart, pt_particles *out, int64_t i) {
         rng = Rng{P.seed, id, 0};
+        pid = id;
         stopID = PT_ID_UNKNOWN; Nhit = Nstep = Nspinflip = 0; noflip = 1; nacc = nrej = 0;
         double tau = 0;
         if (P.tau > 0) tau = -std::log(1 - rng.u()) * P.tau; /* exponential_distribution(1/tau) */
@@ -1257,6 +1271,19 @@ struct Tracker {
             } catch (...) {
                 stopID = PT_ID_CGAL_ERROR;
             }
+            if (P.snapshotlog) /* TLogger::PrintSnapshot (src/logger.cpp:128-141) */
+                for (int k = 0; k < P.n_snapshots; ++k) {
+                    const double ts = P.snapshots[k];
+                    if (!(st.to <= ts && ts < x)) continue;
+                    double ys[9];
+                    st.calc_state(ts, ys);
+                    double r[PT_SNAPSHOT_RECORD] = {(double)pid, ts};
+                    for (int c = 0; c < 9; ++c) r[2 + c] = ys[c];
+                    for (int c = 0; c < 5; ++c) r[11 + c] = spin[c];
+                    r[16] = stopID; r[17] = Nspinflip; r[18] = noflip; r[19] = Nhit; r[20] = Nstep; r[21] = Hmax;
+                    snaplog.insert(snaplog.end(), r, r + PT_SNAPSHOT_RECORD);
+                    break;
+                }
             {
                 double sproj = st.xo[7];
                 try {
@@ -1396,6 +1423,16 @@ int pto_create(const pt_scene_desc *d, pto_ctx **out) {
 
 void pto_destroy(pto_ctx *ctx) { delete ctx; }
 
+/* the records of the last pto_track call's log `kind` (PT_LOG_HIT,
+ * PT_LOG_SNAPSHOT): their number, and up to cap of them into rec */
+int64_t pto_log_read(pto_ctx *ctx, int32_t kind, int64_t cap, double *rec) {
+    const std::vector<double> &v = kind == PT_LOG_HIT ? ctx->hits : ctx->snaps;
+    const int w = kind == PT_LOG_HIT ? PT_HIT_RECORD : PT_SNAPSHOT_RECORD;
+    const int64_t n = (int64_t)v.size() / w;
+    if (rec) std::copy(v.begin(), v.begin() + std::min(n, cap) * w, rec);
+    return n;
+}
+
 int pto_track(pto_ctx *ctx, const pt_run_params *params, const pt_particles *in, pt_particles *out, int nthreads,
               pt_stats *stats) {
     if (!ctx || !params || !in || !out) return PT_ERR_INVALID;
@@ -1405,6 +1442,7 @@ int pto_track(pto_ctx *ctx, const pt_run_params *params, const pt_particles *in,
     std::vector<pt_stats> st(nthreads);
     std::memset(st.data(), 0, sizeof(pt_stats) * nthreads);
     std::atomic<int64_t> next{0};
+    std::vector<std::vector<double>> hits(nthreads), snaps(nthreads);
     auto work = [&](int w) {
         Tracker tr(ctx->sc, *params, &st[w]);
         double ys[9], ss[5];
@@ -1415,11 +1453,19 @@ int pto_track(pto_ctx *ctx, const pt_run_params *params, const pt_particles *in,
             for (int c = 0; c < 5; ++c) ss[c] = in->spin ? in->spin[c * n + i] : 0.0;
             tr.integrate(in->id[i], in->t[i], ys, ss, out, i);
         }
+        hits[w].swap(tr.hitlog);
+        snaps[w].swap(tr.snaplog);
     };
     std::vector<std::thread> th;
     for (int w = 1; w < nthreads; ++w) th.emplace_back(work, w);
     work(0);
     for (auto &t : th) t.join();
+    ctx->hits.clear();
+    ctx->snaps.clear();
+    for (int w = 0; w < nthreads; ++w) {
+        ctx->hits.insert(ctx->hits.end(), hits[w].begin(), hits[w].end());
+        ctx->snaps.insert(ctx->snaps.end(), snaps[w].begin(), snaps[w].end());
+    }
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         for (auto &s : st) {

@@ -42,6 +42,8 @@ def lib():
         L.pto_detpow.argtypes = [C.c_double, C.c_double]
         L.pto_detpow.restype = C.c_double
         L.pto_dopri5_selftest.argtypes = [C.c_double, dp, C.c_double, C.c_int, dp, dp]
+        L.pto_log_read.argtypes = [vp, C.c_int32, C.c_int64, dp]
+        L.pto_log_read.restype = C.c_int64
         _LIB = L
     return _LIB
 
@@ -87,6 +89,17 @@ class Oracle:
         lib().pto_track(self.h, C.byref(params), C.byref(particles.abi(outputs=False)), C.byref(out.abi()), nthreads,
                         C.byref(stats))
         return out, stats.as_dict()
+
+    def read_log(self, kind):
+        """records of the last integrate call's hit log (A.LOG_HIT) or snapshot
+        log (A.LOG_SNAPSHOT), sorted by particle and time"""
+        width = A.HIT_RECORD if kind == A.LOG_HIT else A.SNAPSHOT_RECORD
+        n = lib().pto_log_read(self.h, kind, 0, None)
+        rec = np.zeros((n, width))
+        if n:
+            lib().pto_log_read(self.h, kind, n, _dp(rec))
+        order = np.lexsort((rec[:, 1], rec[:, 0])) if n else np.arange(0)
+        return rec[order]
 
     def field(self, xyzt):
         q = np.ascontiguousarray(xyzt, dtype=np.float64).reshape(-1, 4)

@@ -69,6 +69,8 @@ class RunParams(C.Structure):
         ("n_spintimes", C.c_int32), ("steps_per_launch", C.c_int32), ("spintimes", c_double_p),
         ("seed", C.c_uint64), ("block_size", C.c_int32), ("max_launches", C.c_int32), ("timeout_s", C.c_double),
         ("max_run", C.c_int32), ("period_iters", C.c_int32), ("scheduler", C.c_int32), ("reserved3", C.c_int32),
+        ("hitlog", C.c_int32), ("snapshotlog", C.c_int32), ("snapshots", c_double_p), ("n_snapshots", C.c_int32),
+        ("reserved4", C.c_int32), ("log_capacity", C.c_int64),
     ]
 
 
@@ -83,6 +85,8 @@ class Particles(C.Structure):
 
 
 SOURCE_BOX, SOURCE_CYLINDER, SOURCE_SOLID = 0, 1, 2
+LOG_HIT, LOG_SNAPSHOT = 0, 1
+HIT_RECORD, SNAPSHOT_RECORD = 18, 22
 
 
 class SourceParams(C.Structure):
@@ -151,6 +155,7 @@ def declare(lib):
                                                       c_double_p, c_int32_p, c_double_p]),
         "pt_point_solids": (C.c_int32, [vp, C.c_int64, c_double_p, c_uint64_p]),
         "pt_source_volume": (C.c_int32, [vp, P(SourceParams), C.c_int64, c_int64_p, P(Particles), c_double_p]),
+        "pt_log_read": (C.c_int32, [vp, C.c_int32, C.c_int64, c_double_p, c_int64_p]),
         "pt_probe_fp64": (C.c_int32, [vp, c_double_p]),
         "pt_version": (C.c_char_p, []),
         "pt_config_load": (C.c_int32, [C.c_char_p, P(vp)]),

@@ -61,6 +61,11 @@ struct pt_ctx {
      * created and destroyed inside the call) */
     void *arena = nullptr;
     size_t arena_bytes = 0;
+    /* event logs of the last run that asked for them (pt_log_read) */
+    double *log_hit = nullptr, *log_snap = nullptr, *log_snap_t = nullptr;
+    unsigned long long *log_n = nullptr; /* [0] hits, [1] snapshots */
+    long long log_cap_hit = 0, log_cap_snap = 0, log_cap = 0;
+    bool log_hit_on = false, log_snap_on = false;
 };
 
 /* Scratch of pt_segment_collisions_noalloc: a fixed device array in the
@@ -1046,6 +1051,10 @@ void pt_destroy(pt_ctx *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_list(c->allocs);
     if (c->arena) cudaFree(c->arena);
+    if (c->log_hit) cudaFree(c->log_hit);
+    if (c->log_snap) cudaFree(c->log_snap);
+    if (c->log_snap_t) cudaFree(c->log_snap_t);
+    if (c->log_n) cudaFree(c->log_n);
     if (c->counters) cudaFree(c->counters);
     if (c->counters_host) cudaFreeHost(c->counters_host);
     if (c->sched_host) cudaFreeHost(c->sched_host);
@@ -1102,6 +1111,52 @@ extern "C" pt_status pt_batch_create(pt_ctx *c, const pt_run_params *p, const pt
 
 namespace {
 
+/* The event-log buffers of a run (context-owned, grown as asked, counts
+ * reset): R.log points at them, or is empty when no log is on. */
+pt_status setup_logs(pt_ctx *c, const pt_run_params *p, DRun &R) {
+    std::memset(&R.log, 0, sizeof(R.log));
+    c->log_hit_on = p->hitlog != 0;
+    c->log_snap_on = p->snapshotlog != 0 && p->n_snapshots > 0;
+    if (!c->log_hit_on && !c->log_snap_on) return PT_OK;
+    if (c->log_snap_on && (p->n_snapshots > PT_MAX_SNAPSHOTS || !p->snapshots)) {
+        c->err = "snapshotlog: 1 to 1024 snapshot times";
+        return PT_ERR_INVALID;
+    }
+    const long long cap = p->log_capacity > 0 ? p->log_capacity : 1000000;
+    cudaError_t e = cudaSuccess;
+    if (!c->log_n && (e = cudaMalloc((void **)&c->log_n, 2 * sizeof(unsigned long long)))) return ck(c, e, "log counts"), PT_ERR_OOM;
+    if (!c->log_snap_t && (e = cudaMalloc((void **)&c->log_snap_t, PT_MAX_SNAPSHOTS * sizeof(double)))) return ck(c, e, "log times"), PT_ERR_OOM;
+    if (c->log_hit_on && c->log_cap_hit < cap) {
+        if (c->log_hit) cudaFree(c->log_hit);
+        c->log_hit = nullptr;
+        c->log_cap_hit = 0;
+        if ((e = cudaMalloc((void **)&c->log_hit, (size_t)cap * PT_HIT_RECORD * sizeof(double)))) return ck(c, e, "hit log"), PT_ERR_OOM;
+        c->log_cap_hit = cap;
+    }
+    if (c->log_snap_on && c->log_cap_snap < cap) {
+        if (c->log_snap) cudaFree(c->log_snap);
+        c->log_snap = nullptr;
+        c->log_cap_snap = 0;
+        if ((e = cudaMalloc((void **)&c->log_snap, (size_t)cap * PT_SNAPSHOT_RECORD * sizeof(double)))) return ck(c, e, "snapshot log"), PT_ERR_OOM;
+        c->log_cap_snap = cap;
+    }
+    c->log_cap = cap;
+    if ((e = cudaMemsetAsync(c->log_n, 0, 2 * sizeof(unsigned long long), c->stream))) return ck(c, e, "log counts"), PT_ERR_CUDA;
+    if (c->log_snap_on &&
+        (e = cudaMemcpyAsync(c->log_snap_t, p->snapshots, p->n_snapshots * sizeof(double), cudaMemcpyHostToDevice, c->stream)))
+        return ck(c, e, "snapshot times"), PT_ERR_CUDA;
+    R.log.cap = cap;
+    R.log.hit_n = c->log_n;
+    R.log.snap_n = c->log_n + 1;
+    if (c->log_hit_on) R.log.hit = c->log_hit;
+    if (c->log_snap_on) {
+        R.log.snap = c->log_snap;
+        R.log.snap_t = c->log_snap_t;
+        R.log.n_snap = p->n_snapshots;
+    }
+    return PT_OK;
+}
+
 pt_status batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles *in, pt_batch **out, bool use_ctx_arena) {
     if (!c || !p || !in || !out || in->n < 0 || !in->id || !in->t || !in->y) return PT_ERR_INVALID;
     cudaSetDevice(c->device);
@@ -1131,6 +1186,7 @@ pt_status batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles *in
     R.seed = p->seed;
     R.t_pause = INFINITY;
     R.cancel = c->cancel_dev;
+    if (pt_status ls = setup_logs(c, p, R)) return ls;
     const int64_t n = in->n;
     DBatch &b = B->b;
     b.n = n;
@@ -1292,6 +1348,28 @@ pt_status pt_integrate(pt_ctx *c, const pt_run_params *p, const pt_particles *in
     s.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
     if (stats) *stats = s;
     return st;
+}
+
+pt_status pt_log_read(pt_ctx *c, int32_t kind, int64_t cap, double *rec, int64_t *total) {
+    if (!c || !total || cap < 0 || (cap > 0 && !rec) || (kind != PT_LOG_HIT && kind != PT_LOG_SNAPSHOT)) return PT_ERR_INVALID;
+    *total = 0;
+    const bool on = kind == PT_LOG_HIT ? c->log_hit_on : c->log_snap_on;
+    if (!on || !c->log_n) return PT_OK;
+    cudaSetDevice(c->device);
+    unsigned long long cnt = 0;
+    cudaError_t e = cudaMemcpyAsync(&cnt, c->log_n + (kind == PT_LOG_HIT ? 0 : 1), sizeof(cnt), cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaStreamSynchronize(c->stream);
+    if (e) return ck(c, e, "log count"), PT_ERR_CUDA;
+    *total = (int64_t)cnt;
+    const int64_t kept = std::min<int64_t>((int64_t)cnt, std::min<int64_t>(cap, c->log_cap));
+    const int width = kind == PT_LOG_HIT ? PT_HIT_RECORD : PT_SNAPSHOT_RECORD;
+    if (kept > 0) {
+        e = cudaMemcpyAsync(rec, kind == PT_LOG_HIT ? c->log_hit : c->log_snap, (size_t)kept * width * sizeof(double), cudaMemcpyDeviceToHost,
+                            c->stream);
+        if (!e) e = cudaStreamSynchronize(c->stream);
+        if (e) return ck(c, e, "log read"), PT_ERR_CUDA;
+    }
+    return PT_OK;
 }
 
 pt_status pt_field_eval(pt_ctx *c, int64_t n, const double *xyzt, int32_t prec, double *B, double *dB, double *V, double *E) {

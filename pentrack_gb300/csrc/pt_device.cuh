@@ -150,8 +150,19 @@ struct DSpecies {
     float pad2;
 };
 
+/* event-log buffers (null when the log is off): records appended at an
+ * atomic count; counts past the capacity are kept, records dropped */
+struct DLog {
+    double *hit, *snap;
+    unsigned long long *hit_n, *snap_n;
+    long long cap;
+    const double *snap_t;
+    int n_snap, pad;
+};
+
 struct DRun {
     DSpecies sp;
+    DLog log;
     double simtime, tau, tmax, lmax, bmax;
     double spintimes[PT_MAX_SPINTIMES];
     int n_spintimes, flipspin, prec, steps_per_launch;

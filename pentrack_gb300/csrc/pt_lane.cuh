@@ -1015,6 +1015,44 @@ template <class Tape> struct LaneT {
         cand_span = INFINITY;
     }
 
+    /* ---------------- event logs ---------------- */
+    /* TLogger::PrintHit (src/logger.cpp:202-235): time, state before and
+     * after OnHit, the hit surface's normal, the solids left and entered */
+    __device__ void log_hit(double x1, const double *y1, const double *y2, const double *nrm, uint32_t leaving, uint32_t entering) const {
+        const unsigned long long k = atomicAdd(R.log.hit_n, 1ull);
+        if ((long long)k >= R.log.cap) return;
+        double *r = R.log.hit + k * PT_HIT_RECORD;
+        const double v[PT_HIT_RECORD] = {(double)id, x1, y1[0], y1[1], y1[2], y1[3], y1[4], y1[5], y1[7],
+                                         y2[3], y2[4], y2[5], y2[7], nrm[0], nrm[1], nrm[2], (double)leaving, (double)entering};
+        for (int j = 0; j < PT_HIT_RECORD; ++j) r[j] = v[j];
+    }
+    /* TLogger::PrintSnapshot (src/logger.cpp:128-141): at the first
+     * snapshot time in [to, x), the dense-output state there with the spin
+     * and counters as they stand before the step's spin integration */
+    __device__ void log_snapshot(double x) {
+        for (int k = 0; k < R.log.n_snap; ++k) {
+            const double ts = R.log.snap_t[k];
+            if (!(to <= ts && ts < x)) continue;
+            double ys[9];
+            calc_state(ts, ys);
+            const unsigned long long j = atomicAdd(R.log.snap_n, 1ull);
+            if ((long long)j < R.log.cap) {
+                double *r = R.log.snap + j * PT_SNAPSHOT_RECORD;
+                r[0] = (double)id;
+                r[1] = ts;
+                for (int c = 0; c < 9; ++c) r[2 + c] = ys[c];
+                for (int c = 0; c < 5; ++c) r[11 + c] = spin[c];
+                r[16] = (double)stop;
+                r[17] = (double)nspinflip;
+                r[18] = noflip;
+                r[19] = (double)nhit;
+                r[20] = (double)nstep;
+                r[21] = hmax;
+            }
+            return;
+        }
+    }
+
     /* ---------------- RotateVector (src/globals.cpp:40-64) ---------------- */
     __device__ __forceinline__ static void rotate_vector(double v[3], const double n[3], const double *x) {
         double nn = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
@@ -1355,6 +1393,7 @@ template <class Tape> struct LaneT {
                 else if (x2 == x1 && y2[0] == y1[0] && y2[1] == y1[1] && y2[2] == y1[2]) traversed = false;
                 else { stop = PT_ID_GEOMETRY_ERROR; return true; }
             }
+            if (R.log.hit) log_hit(x1, y1, y2, colls[ci].n, S.solids[leaving].id, S.solids[entering].id);
         }
         if (traversed) {
             nsol = nn;
@@ -1634,6 +1673,7 @@ template <class Tape> struct LaneT {
     template <bool BLOCH = true>
     __device__ bool finish_begin(double x, double *yl, bool reset, double &sproj) {
         tp.on_segment(*this, x, yl, reset);
+        if (R.log.snap) log_snapshot(x);
         if (spin_begin<BLOCH>(x, yl, sproj)) {
             fx = x;
             fyl = yl;
@@ -1696,6 +1736,9 @@ template <class Tape> struct LaneT {
         if (R.sp.kind == PT_NEUTRON ? (m.fermi_imag > 0) : (S.solids[cs].id > 1)) return false; /* OnStep may act */
         if (any_hit(xo, yn) != 0) return false;
         if (spin_integrates(tn, yn)) return false; /* the Bloch integration runs in the full post-step */
+        if (R.log.snap) /* a snapshot needs the try's stages, which the full post-step loads */
+            for (int k = 0; k < R.log.n_snap; ++k)
+                if (to <= R.log.snap_t[k] && R.log.snap_t[k] < tn) return false;
         double x2 = tn, y2[9];
         for (int i = 0; i < 9; ++i) y2[i] = yn[i];
         do_step(to, xo, x2, y2, cs); /* cannot alter the step here */

@@ -238,6 +238,20 @@ def run_params(species=A.NEUTRON, simtime=100.0, tau=0.0, tmax=9e99, lmax=9e99, 
     return p
 
 
+def set_logs(p, hitlog=False, snapshots=None, capacity=0):
+    """Turn on the hit log and (with snapshot times) the snapshot log of a
+    run (the particle options hitlog, snapshotlog and snapshots of
+    src/logger.cpp:128-235); read them after the run with Engine.read_log."""
+    p.hitlog = int(bool(hitlog))
+    ts = np.ascontiguousarray(np.array(() if snapshots is None else snapshots, dtype=np.float64).reshape(-1))
+    p.snapshotlog = int(len(ts) > 0)
+    p.n_snapshots = len(ts)
+    p.snapshots = _dp(ts) if len(ts) else None
+    p.log_capacity = capacity
+    p._keep_snap = ts
+    return p
+
+
 class ConfigScene:
     """The scene of a PENTrack config.in as the library's config front end
     reads it (pt_config_load: [GEOMETRY], [MATERIALS] / materials_file,
@@ -391,6 +405,20 @@ class Engine:
         P = out.abi(outputs=False)
         self._check(lib().pt_source_volume(self.h, C.byref(sp), n, _lp(out.id), C.byref(P), C.byref(vmin)))
         return out, vmin.value
+
+    def read_log(self, kind):
+        """pt_log_read: the records of the last run's hit log (kind LOG_HIT,
+        columns of A.HIT_RECORD) or snapshot log (LOG_SNAPSHOT), sorted by
+        particle and time, as an (n, width) array; and the number of events
+        (more than n when the log's capacity was exceeded)."""
+        width = A.HIT_RECORD if kind == A.LOG_HIT else A.SNAPSHOT_RECORD
+        total = C.c_int64(0)
+        self._check(lib().pt_log_read(self.h, kind, 0, None, C.byref(total)))
+        rec = np.zeros((max(total.value, 0), width))
+        if total.value > 0:
+            self._check(lib().pt_log_read(self.h, kind, total.value, _dp(rec), C.byref(total)))
+        order = np.lexsort((rec[:, 1], rec[:, 0])) if len(rec) else np.arange(0)
+        return rec[order], int(total.value)
 
     def point_solids(self, pts):
         p = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)

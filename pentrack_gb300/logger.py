@@ -167,6 +167,49 @@ def write_endlog(directory, scene, kind, start, end, field, point_solids, jobnum
     return write_log(directory, jobnumber, SPECIES_NAME[kind], "end", titles, [v[t] for t in titles])
 
 
+HIT_TITLES = ("jobnumber", "particle", "t", "x", "y", "z", "v1x", "v1y", "v1z", "pol1", "v2x", "v2y", "v2z", "pol2",
+              "nx", "ny", "nz", "solid1", "solid2")
+
+
+def write_hitlog(directory, kind, records, jobnumber=0):
+    """The hit log (TLogger::PrintHit, src/logger.cpp:202-235) from the hit
+    records of Engine.read_log(LOG_HIT): one row per hit that changed the
+    particle's solid, in the order of the records (by particle, then time);
+    particle numbers as in the end log (id + 1).  Returns the path."""
+    r = np.asarray(records, dtype=np.float64).reshape(-1, 18)
+    cols = [np.full(len(r), float(jobnumber)), r[:, 0] + 1] + [r[:, k] for k in range(1, 18)]
+    return write_log(directory, jobnumber, SPECIES_NAME[kind], "hit", HIT_TITLES, cols)
+
+
+def snapshot_states(start, records):
+    """(start subset, ParticleSet at the snapshots) from snapshot records of
+    Engine.read_log(LOG_SNAPSHOT): for each record the particle's start state
+    and its state, spin and counters at the snapshot time."""
+    from .engine import ParticleSet
+    r = np.asarray(records, dtype=np.float64).reshape(-1, 22)
+    index = {int(i): k for k, i in enumerate(start.id)}
+    rows = np.array([index[int(i)] for i in r[:, 0]], dtype=np.int64)
+    st = start.subset(rows)
+    snap = ParticleSet(len(r), st.id.copy(), r[:, 1].copy(), r[:, 2:11].T.copy(), r[:, 11:16].T.copy())
+    snap.stop_id[:] = r[:, 16]
+    snap.n_spinflip[:] = r[:, 17]
+    snap.noflip_prob[:] = r[:, 18]
+    snap.n_hit[:] = r[:, 19]
+    snap.n_step[:] = r[:, 20]
+    snap.h_max[:] = r[:, 21]
+    return st, snap
+
+
+def write_snapshotlog(directory, scene, kind, start, records, field, point_solids, jobnumber=0, logvars=None):
+    """The snapshot log (TLogger::PrintSnapshot -> Print(..., "snapshot"),
+    src/logger.cpp:128-141): the end log's columns with the state at each
+    snapshot time in place of the end state.  Returns the path."""
+    st, snap = snapshot_states(start, records)
+    v = end_variables(scene, kind, st, snap, field, point_solids, jobnumber)
+    titles = tuple(logvars) if logvars else END_TITLES
+    return write_log(directory, jobnumber, SPECIES_NAME[kind], "snapshot", titles, [v[t] for t in titles])
+
+
 def log_settings(config_path, particle_name, suffix="end"):
     """(enabled, logvars) of one log from a config.in: `<suffix>log` and
     `<suffix>logvars` of [PARTICLES], overridden by the particle's own

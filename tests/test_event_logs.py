@@ -1,0 +1,67 @@
+"""Hit and snapshot logs (TLogger::PrintHit / PrintSnapshot,
+src/logger.cpp:128-235) on the oracle (CPU): in the closed cube every wall
+hit is a total reflection out of the vacuum solid into the default one, so
+each particle has one hit record per hit (n_hit of the end state) and each
+record's velocity after the hit is the specular image of the one before (to
+1e-6 m/s: the mirrored velocity is the one at the far end of the final
+1e-8 m bisection bracket); a
+snapshot is taken at each listed time a particle is still tracked, with the
+total energy of its start to 1e-5 (the end states' drift over these 4 s is
+3.6e-6); the
+writers produce the reference's columns."""
+import os
+
+import numpy as np
+import pytest
+
+from pentrack_gb300 import _abi as A
+
+SNAPSHOTS = (0.75, 2.25, 3.5)
+
+
+@pytest.fixture(scope="module")
+def cube_logs(oracle_mod):
+    from pentrack_gb300 import engine, workloads
+    sc, params, parts = workloads.cube_storage(n=200, simtime=4.0)
+    engine.set_logs(params, hitlog=True, snapshots=SNAPSHOTS)
+    orc = oracle_mod.Oracle(sc)
+    out, st = orc.integrate(params, parts, nthreads=4)
+    return sc, params, parts, out, orc.read_log(A.LOG_HIT), orc.read_log(A.LOG_SNAPSHOT), orc
+
+
+def test_hit_records_match_hits(cube_logs):
+    sc, params, parts, out, hits, snaps, orc = cube_logs
+    assert hits.shape[1] == A.HIT_RECORD
+    assert len(hits) == out.n_hit.sum() > 100
+    per = np.bincount(hits[:, 0].astype(np.int64), minlength=parts.n)
+    np.testing.assert_array_equal(per, out.n_hit)
+    # leaving the vacuum solid (ID 2) into the default solid (ID 1), reflected specularly
+    assert np.all(hits[:, 16] == 2) and np.all(hits[:, 17] == 1)
+    # Reflect (src/neutron.cpp:99-115) mirrors the velocity at the far end of
+    # the final bisection bracket (up to 1e-8 m on), v1 is the one at its start
+    n = hits[:, 13:16]
+    v1, v2 = hits[:, 5:8], hits[:, 9:12]
+    np.testing.assert_allclose(v2, v1 - 2 * (v1 * n).sum(1)[:, None] * n, rtol=0, atol=1e-6)
+    assert np.all(np.abs(hits[:, 2:5]) <= 0.5 + 1e-7)
+
+
+def test_snapshots_at_listed_times(cube_logs, tmp_path):
+    from pentrack_gb300 import logger
+    sc, params, parts, out, hits, snaps, orc = cube_logs
+    assert snaps.shape[1] == A.SNAPSHOT_RECORD
+    for ts in SNAPSHOTS:
+        alive = out.t > ts
+        got = snaps[snaps[:, 1] == ts]
+        assert len(got) == alive.sum()
+        assert np.all(np.abs(got[:, 2:5]) <= 0.5)
+    st, snap = logger.snapshot_states(parts, snaps)
+    v = logger.end_variables(sc, A.NEUTRON, st, snap, orc.field, orc.point_solids)
+    np.testing.assert_allclose(v["Hend"], v["Hstart"], rtol=1e-5, atol=0)  # as the end states' drift
+    p = logger.write_snapshotlog(str(tmp_path), sc, A.NEUTRON, parts, snaps, orc.field, orc.point_solids, jobnumber=3)
+    lines = open(p).read().splitlines()
+    assert os.path.basename(p) == "000000000003neutronsnapshot.out"
+    assert lines[0].split() == list(logger.END_TITLES) and len(lines) == 1 + len(snaps)
+    p = logger.write_hitlog(str(tmp_path), A.NEUTRON, hits, jobnumber=3)
+    lines = open(p).read().splitlines()
+    assert lines[0].split() == list(logger.HIT_TITLES) and len(lines) == 1 + len(hits)
+    assert float(lines[1].split()[1]) == hits[0, 0] + 1
