@@ -1018,7 +1018,7 @@ template <class Tape> struct LaneT {
     /* ---------------- event logs ---------------- */
     /* TLogger::PrintHit (src/logger.cpp:202-235): time, state before and
      * after OnHit, the hit surface's normal, the solids left and entered */
-    __device__ void log_hit(double x1, const double *y1, const double *y2, const double *nrm, uint32_t leaving, uint32_t entering) const {
+    __device__ __noinline__ void log_hit(double x1, const double *y1, const double *y2, const double *nrm, uint32_t leaving, uint32_t entering) const {
         const unsigned long long k = atomicAdd(R.log.hit_n, 1ull);
         if ((long long)k >= R.log.cap) return;
         double *r = R.log.hit + k * PT_HIT_RECORD;
@@ -1028,8 +1028,15 @@ template <class Tape> struct LaneT {
     }
     /* TLogger::PrintSnapshot (src/logger.cpp:128-141): at the first
      * snapshot time in [to, x), the dense-output state there with the spin
-     * and counters as they stand before the step's spin integration */
-    __device__ void log_snapshot(double x) {
+     * and counters as they stand before the step's spin integration.  The
+     * log functions stay out of line: inlined, they enlarge the fast step
+     * completion that runs without them. */
+    __device__ __noinline__ bool snapshot_due(double x) const {
+        for (int k = 0; k < R.log.n_snap; ++k)
+            if (to <= R.log.snap_t[k] && R.log.snap_t[k] < x) return true;
+        return false;
+    }
+    __device__ __noinline__ void log_snapshot(double x) {
         for (int k = 0; k < R.log.n_snap; ++k) {
             const double ts = R.log.snap_t[k];
             if (!(to <= ts && ts < x)) continue;
@@ -1736,9 +1743,7 @@ template <class Tape> struct LaneT {
         if (R.sp.kind == PT_NEUTRON ? (m.fermi_imag > 0) : (S.solids[cs].id > 1)) return false; /* OnStep may act */
         if (any_hit(xo, yn) != 0) return false;
         if (spin_integrates(tn, yn)) return false; /* the Bloch integration runs in the full post-step */
-        if (R.log.snap) /* a snapshot needs the try's stages, which the full post-step loads */
-            for (int k = 0; k < R.log.n_snap; ++k)
-                if (to <= R.log.snap_t[k] && R.log.snap_t[k] < tn) return false;
+        if (R.log.snap && snapshot_due(tn)) return false; /* a snapshot needs the try's stages, which the full post-step loads */
         double x2 = tn, y2[9];
         for (int i = 0; i < 9; ++i) y2[i] = yn[i];
         do_step(to, xo, x2, y2, cs); /* cannot alter the step here */
