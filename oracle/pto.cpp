@@ -533,7 +533,7 @@ struct Scene {
  * PrintSnapshot records, the library's record layout) */
 struct pto_ctx {
     Scene sc;
-    std::vector<double> hits, snaps;
+    std::vector<double> hits, snaps, tracks;
 };
 
 /* ------------------------------------------------------------------ */
@@ -722,7 +722,19 @@ struct Tracker {
     pt_stats *stats;
     std::vector<Coll> cbuf;
     int64_t pid = 0;                        /* the particle being tracked */
-    std::vector<double> hitlog, snaplog;    /* records of this thread's particles */
+    std::vector<double> hitlog, snaplog, tracklog; /* records of this thread's particles */
+
+    /* TLogger::PrintTrack (src/logger.cpp:143-200): at zero path length and
+     * when a step from path length l1 to y[8] crossed a multiple of the
+     * interval */
+    void log_track(double l1, double x, const double *y) {
+        const double iv = P.trackloginterval;
+        if (!P.tracklog || !(iv > 0)) return;
+        if (y[8] > 0 && (int)(l1 / iv) == (int)(y[8] / iv)) return;
+        const double r[PT_TRACK_RECORD] = {(double)pid, x, y[0], y[1], y[2], y[3], y[4], y[5], y[7],
+                                            (double)sc.solids[current_solid(cur)].id};
+        tracklog.insert(tracklog.end(), r, r + PT_TRACK_RECORD);
+    }
 
     Tracker(const Scene &s, const pt_run_params &p, pt_stats *stt) : sc(s), P(p), sp(species_of(p.species)), st(1e-9, 1e-9), stats(stt) {}
 
@@ -1224,6 +1236,7 @@ struct Tracker {
             Hmax = hstart;
         }
         bool reset = false;
+        log_track(y[8], x, y); /* the track log's first point (src/tracking.cpp:43) */
         if (x > tmax) stopID = PT_ID_NOT_FINISH;
         st.initialize(y, x, 10. * PT_MAX_TRACK_DEVIATION / std::sqrt(y[3] * y[3] + y[4] * y[4] + y[5] * y[5]));
         while (stopID == PT_ID_UNKNOWN) {
@@ -1306,6 +1319,7 @@ struct Tracker {
                     std::fill(spin, spin + 5, 0.0);
                 }
             }
+            log_track(st.xo[8], x, y); /* src/tracking.cpp:140 */
             if (stopID == PT_ID_UNKNOWN && y[6] >= tau) stopID = PT_ID_DECAYED;
             else if (stopID == PT_ID_UNKNOWN && (x >= tmax || y[8] >= maxtraj)) stopID = PT_ID_NOT_FINISH;
         }
@@ -1426,8 +1440,8 @@ void pto_destroy(pto_ctx *ctx) { delete ctx; }
 /* the records of the last pto_track call's log `kind` (PT_LOG_HIT,
  * PT_LOG_SNAPSHOT): their number, and up to cap of them into rec */
 int64_t pto_log_read(pto_ctx *ctx, int32_t kind, int64_t cap, double *rec) {
-    const std::vector<double> &v = kind == PT_LOG_HIT ? ctx->hits : ctx->snaps;
-    const int w = kind == PT_LOG_HIT ? PT_HIT_RECORD : PT_SNAPSHOT_RECORD;
+    const std::vector<double> &v = kind == PT_LOG_HIT ? ctx->hits : kind == PT_LOG_SNAPSHOT ? ctx->snaps : ctx->tracks;
+    const int w = kind == PT_LOG_HIT ? PT_HIT_RECORD : kind == PT_LOG_SNAPSHOT ? PT_SNAPSHOT_RECORD : PT_TRACK_RECORD;
     const int64_t n = (int64_t)v.size() / w;
     if (rec) std::copy(v.begin(), v.begin() + std::min(n, cap) * w, rec);
     return n;
@@ -1442,7 +1456,7 @@ int pto_track(pto_ctx *ctx, const pt_run_params *params, const pt_particles *in,
     std::vector<pt_stats> st(nthreads);
     std::memset(st.data(), 0, sizeof(pt_stats) * nthreads);
     std::atomic<int64_t> next{0};
-    std::vector<std::vector<double>> hits(nthreads), snaps(nthreads);
+    std::vector<std::vector<double>> hits(nthreads), snaps(nthreads), tracks(nthreads);
     auto work = [&](int w) {
         Tracker tr(ctx->sc, *params, &st[w]);
         double ys[9], ss[5];
@@ -1455,6 +1469,7 @@ int pto_track(pto_ctx *ctx, const pt_run_params *params, const pt_particles *in,
         }
         hits[w].swap(tr.hitlog);
         snaps[w].swap(tr.snaplog);
+        tracks[w].swap(tr.tracklog);
     };
     std::vector<std::thread> th;
     for (int w = 1; w < nthreads; ++w) th.emplace_back(work, w);
@@ -1462,9 +1477,11 @@ int pto_track(pto_ctx *ctx, const pt_run_params *params, const pt_particles *in,
     for (auto &t : th) t.join();
     ctx->hits.clear();
     ctx->snaps.clear();
+    ctx->tracks.clear();
     for (int w = 0; w < nthreads; ++w) {
         ctx->hits.insert(ctx->hits.end(), hits[w].begin(), hits[w].end());
         ctx->snaps.insert(ctx->snaps.end(), snaps[w].begin(), snaps[w].end());
+        ctx->tracks.insert(ctx->tracks.end(), tracks[w].begin(), tracks[w].end());
     }
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));

@@ -71,6 +71,7 @@ class RunParams(C.Structure):
         ("max_run", C.c_int32), ("period_iters", C.c_int32), ("scheduler", C.c_int32), ("reserved3", C.c_int32),
         ("hitlog", C.c_int32), ("snapshotlog", C.c_int32), ("snapshots", c_double_p), ("n_snapshots", C.c_int32),
         ("reserved4", C.c_int32), ("log_capacity", C.c_int64),
+        ("tracklog", C.c_int32), ("reserved5", C.c_int32), ("trackloginterval", C.c_double),
     ]
 
 
@@ -85,8 +86,8 @@ class Particles(C.Structure):
 
 
 SOURCE_BOX, SOURCE_CYLINDER, SOURCE_SOLID = 0, 1, 2
-LOG_HIT, LOG_SNAPSHOT = 0, 1
-HIT_RECORD, SNAPSHOT_RECORD = 18, 22
+LOG_HIT, LOG_SNAPSHOT, LOG_TRACK = 0, 1, 2
+HIT_RECORD, SNAPSHOT_RECORD, TRACK_RECORD = 18, 22, 10
 
 
 class SourceParams(C.Structure):

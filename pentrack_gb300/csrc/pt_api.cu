@@ -62,10 +62,10 @@ struct pt_ctx {
     void *arena = nullptr;
     size_t arena_bytes = 0;
     /* event logs of the last run that asked for them (pt_log_read) */
-    double *log_hit = nullptr, *log_snap = nullptr, *log_snap_t = nullptr;
-    unsigned long long *log_n = nullptr; /* [0] hits, [1] snapshots */
-    long long log_cap_hit = 0, log_cap_snap = 0, log_cap = 0;
-    bool log_hit_on = false, log_snap_on = false;
+    double *log_hit = nullptr, *log_snap = nullptr, *log_track = nullptr, *log_snap_t = nullptr;
+    unsigned long long *log_n = nullptr; /* [0] hits, [1] snapshots, [2] track points */
+    long long log_cap_hit = 0, log_cap_snap = 0, log_cap_track = 0, log_cap = 0;
+    bool log_hit_on = false, log_snap_on = false, log_track_on = false;
 };
 
 /* Scratch of pt_segment_collisions_noalloc: a fixed device array in the
@@ -1053,6 +1053,7 @@ void pt_destroy(pt_ctx *c) {
     if (c->arena) cudaFree(c->arena);
     if (c->log_hit) cudaFree(c->log_hit);
     if (c->log_snap) cudaFree(c->log_snap);
+    if (c->log_track) cudaFree(c->log_track);
     if (c->log_snap_t) cudaFree(c->log_snap_t);
     if (c->log_n) cudaFree(c->log_n);
     if (c->counters) cudaFree(c->counters);
@@ -1117,14 +1118,15 @@ pt_status setup_logs(pt_ctx *c, const pt_run_params *p, DRun &R) {
     std::memset(&R.log, 0, sizeof(R.log));
     c->log_hit_on = p->hitlog != 0;
     c->log_snap_on = p->snapshotlog != 0 && p->n_snapshots > 0;
-    if (!c->log_hit_on && !c->log_snap_on) return PT_OK;
+    c->log_track_on = p->tracklog != 0 && p->trackloginterval > 0;
+    if (!c->log_hit_on && !c->log_snap_on && !c->log_track_on) return PT_OK;
     if (c->log_snap_on && (p->n_snapshots > PT_MAX_SNAPSHOTS || !p->snapshots)) {
         c->err = "snapshotlog: 1 to 1024 snapshot times";
         return PT_ERR_INVALID;
     }
     const long long cap = p->log_capacity > 0 ? p->log_capacity : 1000000;
     cudaError_t e = cudaSuccess;
-    if (!c->log_n && (e = cudaMalloc((void **)&c->log_n, 2 * sizeof(unsigned long long)))) return ck(c, e, "log counts"), PT_ERR_OOM;
+    if (!c->log_n && (e = cudaMalloc((void **)&c->log_n, 3 * sizeof(unsigned long long)))) return ck(c, e, "log counts"), PT_ERR_OOM;
     if (!c->log_snap_t && (e = cudaMalloc((void **)&c->log_snap_t, PT_MAX_SNAPSHOTS * sizeof(double)))) return ck(c, e, "log times"), PT_ERR_OOM;
     if (c->log_hit_on && c->log_cap_hit < cap) {
         if (c->log_hit) cudaFree(c->log_hit);
@@ -1140,15 +1142,27 @@ pt_status setup_logs(pt_ctx *c, const pt_run_params *p, DRun &R) {
         if ((e = cudaMalloc((void **)&c->log_snap, (size_t)cap * PT_SNAPSHOT_RECORD * sizeof(double)))) return ck(c, e, "snapshot log"), PT_ERR_OOM;
         c->log_cap_snap = cap;
     }
+    if (c->log_track_on && c->log_cap_track < cap) {
+        if (c->log_track) cudaFree(c->log_track);
+        c->log_track = nullptr;
+        c->log_cap_track = 0;
+        if ((e = cudaMalloc((void **)&c->log_track, (size_t)cap * PT_TRACK_RECORD * sizeof(double)))) return ck(c, e, "track log"), PT_ERR_OOM;
+        c->log_cap_track = cap;
+    }
     c->log_cap = cap;
-    if ((e = cudaMemsetAsync(c->log_n, 0, 2 * sizeof(unsigned long long), c->stream))) return ck(c, e, "log counts"), PT_ERR_CUDA;
+    if ((e = cudaMemsetAsync(c->log_n, 0, 3 * sizeof(unsigned long long), c->stream))) return ck(c, e, "log counts"), PT_ERR_CUDA;
     if (c->log_snap_on &&
         (e = cudaMemcpyAsync(c->log_snap_t, p->snapshots, p->n_snapshots * sizeof(double), cudaMemcpyHostToDevice, c->stream)))
         return ck(c, e, "snapshot times"), PT_ERR_CUDA;
     R.log.cap = cap;
     R.log.hit_n = c->log_n;
     R.log.snap_n = c->log_n + 1;
+    R.log.track_n = c->log_n + 2;
     if (c->log_hit_on) R.log.hit = c->log_hit;
+    if (c->log_track_on) {
+        R.log.track = c->log_track;
+        R.log.track_interval = p->trackloginterval;
+    }
     if (c->log_snap_on) {
         R.log.snap = c->log_snap;
         R.log.snap_t = c->log_snap_t;
@@ -1351,21 +1365,21 @@ pt_status pt_integrate(pt_ctx *c, const pt_run_params *p, const pt_particles *in
 }
 
 pt_status pt_log_read(pt_ctx *c, int32_t kind, int64_t cap, double *rec, int64_t *total) {
-    if (!c || !total || cap < 0 || (cap > 0 && !rec) || (kind != PT_LOG_HIT && kind != PT_LOG_SNAPSHOT)) return PT_ERR_INVALID;
+    if (!c || !total || cap < 0 || (cap > 0 && !rec) || kind < PT_LOG_HIT || kind > PT_LOG_TRACK) return PT_ERR_INVALID;
     *total = 0;
-    const bool on = kind == PT_LOG_HIT ? c->log_hit_on : c->log_snap_on;
+    const bool on = kind == PT_LOG_HIT ? c->log_hit_on : kind == PT_LOG_SNAPSHOT ? c->log_snap_on : c->log_track_on;
     if (!on || !c->log_n) return PT_OK;
     cudaSetDevice(c->device);
     unsigned long long cnt = 0;
-    cudaError_t e = cudaMemcpyAsync(&cnt, c->log_n + (kind == PT_LOG_HIT ? 0 : 1), sizeof(cnt), cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e = cudaMemcpyAsync(&cnt, c->log_n + kind, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream);
     if (!e) e = cudaStreamSynchronize(c->stream);
     if (e) return ck(c, e, "log count"), PT_ERR_CUDA;
     *total = (int64_t)cnt;
     const int64_t kept = std::min<int64_t>((int64_t)cnt, std::min<int64_t>(cap, c->log_cap));
-    const int width = kind == PT_LOG_HIT ? PT_HIT_RECORD : PT_SNAPSHOT_RECORD;
+    const int width = kind == PT_LOG_HIT ? PT_HIT_RECORD : kind == PT_LOG_SNAPSHOT ? PT_SNAPSHOT_RECORD : PT_TRACK_RECORD;
+    const double *src = kind == PT_LOG_HIT ? c->log_hit : kind == PT_LOG_SNAPSHOT ? c->log_snap : c->log_track;
     if (kept > 0) {
-        e = cudaMemcpyAsync(rec, kind == PT_LOG_HIT ? c->log_hit : c->log_snap, (size_t)kept * width * sizeof(double), cudaMemcpyDeviceToHost,
-                            c->stream);
+        e = cudaMemcpyAsync(rec, src, (size_t)kept * width * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
         if (!e) e = cudaStreamSynchronize(c->stream);
         if (e) return ck(c, e, "log read"), PT_ERR_CUDA;
     }

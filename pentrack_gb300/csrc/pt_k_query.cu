@@ -18,6 +18,7 @@ __global__ void __launch_bounds__(128) k_init(const __grid_constant__ DScene S, 
     L.stop = PT_ID_UNKNOWN;
     QueryStats qs{0, 0};
     L.init(qs);
+    if (R.log.track && L.stop == PT_ID_UNKNOWN) L.log_track(L.y[8], L.t, L.y); /* the track log's first point */
     L.store_bc_commit(b, i);
     L.store(b, i);
     b.hstart[i] = L.hmax;

@@ -1031,6 +1031,19 @@ template <class Tape> struct LaneT {
      * and counters as they stand before the step's spin integration.  The
      * log functions stay out of line: inlined, they enlarge the fast step
      * completion that runs without them. */
+    /* TLogger::PrintTrack (src/logger.cpp:143-200): at zero path length (a
+     * particle's start) and when the step from path length l1 to y[8] crossed
+     * a multiple of the interval, the state with the current solid */
+    __device__ __noinline__ void log_track(double l1, double x, const double *y) const {
+        const double iv = R.log.track_interval;
+        if (!(iv > 0)) return;
+        if (y[8] > 0 && (int)(l1 / iv) == (int)(y[8] / iv)) return;
+        const unsigned long long k = atomicAdd(R.log.track_n, 1ull);
+        if ((long long)k >= R.log.cap) return;
+        double *r = R.log.track + k * PT_TRACK_RECORD;
+        const double v[PT_TRACK_RECORD] = {(double)id, x, y[0], y[1], y[2], y[3], y[4], y[5], y[7], (double)S.solids[cur_solid()].id};
+        for (int j = 0; j < PT_TRACK_RECORD; ++j) r[j] = v[j];
+    }
     __device__ __noinline__ bool snapshot_due(double x) const {
         for (int k = 0; k < R.log.n_snap; ++k)
             if (to <= R.log.snap_t[k] && R.log.snap_t[k] < x) return true;
@@ -1704,6 +1717,7 @@ template <class Tape> struct LaneT {
         } else if (flipped) {
             for (int k = 0; k < 5; ++k) spin[k] = 0;
         }
+        if (R.log.track) log_track(xo[8], x, yl);
         if (stop == PT_ID_UNKNOWN && yl[6] >= tau) stop = PT_ID_DECAYED;
         else if (stop == PT_ID_UNKNOWN && (x >= R.simtime || yl[8] >= R.lmax)) stop = PT_ID_NOT_FINISH;
         /* After a reset the stepper restarts from the loop's (x, y) with a fresh

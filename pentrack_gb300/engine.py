@@ -238,11 +238,14 @@ def run_params(species=A.NEUTRON, simtime=100.0, tau=0.0, tmax=9e99, lmax=9e99, 
     return p
 
 
-def set_logs(p, hitlog=False, snapshots=None, capacity=0):
-    """Turn on the hit log and (with snapshot times) the snapshot log of a
-    run (the particle options hitlog, snapshotlog and snapshots of
+def set_logs(p, hitlog=False, snapshots=None, track_interval=0.0, capacity=0):
+    """Turn on the hit log, (with snapshot times) the snapshot log and (with
+    a path-length interval [m]) the track log of a run (the particle options
+    hitlog, snapshotlog / snapshots and tracklog / trackloginterval of
     src/logger.cpp:128-235); read them after the run with Engine.read_log."""
     p.hitlog = int(bool(hitlog))
+    p.tracklog = int(track_interval > 0)
+    p.trackloginterval = float(track_interval)
     ts = np.ascontiguousarray(np.array(() if snapshots is None else snapshots, dtype=np.float64).reshape(-1))
     p.snapshotlog = int(len(ts) > 0)
     p.n_snapshots = len(ts)
@@ -408,10 +411,11 @@ class Engine:
 
     def read_log(self, kind):
         """pt_log_read: the records of the last run's hit log (kind LOG_HIT,
-        columns of A.HIT_RECORD) or snapshot log (LOG_SNAPSHOT), sorted by
+        columns of A.HIT_RECORD), snapshot log (LOG_SNAPSHOT) or track log
+        (LOG_TRACK), sorted by
         particle and time, as an (n, width) array; and the number of events
         (more than n when the log's capacity was exceeded)."""
-        width = A.HIT_RECORD if kind == A.LOG_HIT else A.SNAPSHOT_RECORD
+        width = {A.LOG_HIT: A.HIT_RECORD, A.LOG_SNAPSHOT: A.SNAPSHOT_RECORD, A.LOG_TRACK: A.TRACK_RECORD}[kind]
         total = C.c_int64(0)
         self._check(lib().pt_log_read(self.h, kind, 0, None, C.byref(total)))
         rec = np.zeros((max(total.value, 0), width))

@@ -181,6 +181,33 @@ def write_hitlog(directory, kind, records, jobnumber=0):
     return write_log(directory, jobnumber, SPECIES_NAME[kind], "hit", HIT_TITLES, cols)
 
 
+TRACK_TITLES = ("jobnumber", "particle", "polarisation", "t", "x", "y", "z", "vx", "vy", "vz", "H", "E",
+                "Bx", "dBxdx", "dBxdy", "dBxdz", "By", "dBydx", "dBydy", "dBydz", "Bz", "dBzdx", "dBzdy", "dBzdz",
+                "Ex", "Ey", "Ez", "V")
+
+
+def write_tracklog(directory, scene, kind, records, field, jobnumber=0):
+    """The track log (TLogger::PrintTrack, src/logger.cpp:143-200) from the
+    track records of Engine.read_log(LOG_TRACK): per record the state, the
+    field and its Jacobian, E and V there, and the kinetic and total energy
+    (with the potential of the recorded current solid).  Returns the path."""
+    r = np.asarray(records, dtype=np.float64).reshape(-1, 10)
+    n = len(r)
+    y = np.zeros((9, n))
+    y[0:6] = r[:, 2:8].T
+    y[7] = r[:, 8]
+    B, dB, V, E = field(np.column_stack([y[0], y[1], y[2], r[:, 1]]))
+    index = {int(s["id"]): k for k, s in enumerate(scene.solids)}
+    sidx = np.array([index[int(i)] for i in r[:, 9]], dtype=np.int64)
+    Ek = kinetic_energy(kind, y[3:6])
+    H = Ek + potential_energy(scene, kind, y, B, V, sidx)
+    cols = [np.full(n, float(jobnumber)), r[:, 0] + 1, y[7], r[:, 1], y[0], y[1], y[2], y[3], y[4], y[5], H, Ek]
+    for i in range(3):
+        cols += [B[:, i], dB[:, i, 0], dB[:, i, 1], dB[:, i, 2]]
+    cols += [E[:, 0], E[:, 1], E[:, 2], V]
+    return write_log(directory, jobnumber, SPECIES_NAME[kind], "track", TRACK_TITLES, cols)
+
+
 def snapshot_states(start, records):
     """(start subset, ParticleSet at the snapshots) from snapshot records of
     Engine.read_log(LOG_SNAPSHOT): for each record the particle's start state

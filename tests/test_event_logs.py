@@ -17,13 +17,14 @@ import pytest
 from pentrack_gb300 import _abi as A
 
 SNAPSHOTS = (0.75, 2.25, 3.5)
+TRACK_INTERVAL = 0.5  # m
 
 
 @pytest.fixture(scope="module")
 def cube_logs(oracle_mod):
     from pentrack_gb300 import engine, workloads
     sc, params, parts = workloads.cube_storage(n=200, simtime=4.0)
-    engine.set_logs(params, hitlog=True, snapshots=SNAPSHOTS)
+    engine.set_logs(params, hitlog=True, snapshots=SNAPSHOTS, track_interval=TRACK_INTERVAL)
     orc = oracle_mod.Oracle(sc)
     out, st = orc.integrate(params, parts, nthreads=4)
     return sc, params, parts, out, orc.read_log(A.LOG_HIT), orc.read_log(A.LOG_SNAPSHOT), orc
@@ -65,3 +66,26 @@ def test_snapshots_at_listed_times(cube_logs, tmp_path):
     lines = open(p).read().splitlines()
     assert lines[0].split() == list(logger.HIT_TITLES) and len(lines) == 1 + len(hits)
     assert float(lines[1].split()[1]) == hits[0, 0] + 1
+
+
+def test_track_points(cube_logs, tmp_path):
+    """one point at each particle's start and one after every step whose path
+    length crossed a multiple of the interval: as many points per particle as
+    multiples crossed, plus the start (a step crossing two counts once)"""
+    from pentrack_gb300 import logger
+    sc, params, parts, out, hits, snaps, orc = cube_logs
+    tr = orc.read_log(A.LOG_TRACK)
+    assert tr.shape[1] == A.TRACK_RECORD
+    per = np.bincount(tr[:, 0].astype(np.int64), minlength=parts.n)
+    crossed = np.floor(out.y[8] / TRACK_INTERVAL).astype(np.int64)
+    assert np.all(per >= 1) and np.all(per <= crossed + 1) and np.any(per > 1)
+    first = tr[np.r_[True, tr[1:, 0] != tr[:-1, 0]]]
+    np.testing.assert_array_equal(first[:, 1], parts.t)
+    np.testing.assert_array_equal(first[:, 2:5], parts.y[0:3].T)
+    assert np.all(tr[:, 9] == 2)  # inside the vacuum cube throughout
+    p = logger.write_tracklog(str(tmp_path), sc, A.NEUTRON, tr, orc.field, jobnumber=1)
+    lines = open(p).read().splitlines()
+    assert lines[0].split() == list(logger.TRACK_TITLES) and len(lines) == 1 + len(tr)
+    H = np.array([float(l.split()[10]) for l in lines[1:]])
+    H0 = dict(zip(first[:, 0].astype(np.int64), H[np.r_[True, tr[1:, 0] != tr[:-1, 0]]]))
+    np.testing.assert_allclose(H, [H0[int(i)] for i in tr[:, 0]], rtol=1e-5)  # each particle keeps its energy

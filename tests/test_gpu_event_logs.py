@@ -5,7 +5,7 @@ Criteria: in the closed cube (2,000 UCN over 10 s, deterministic) every
 particle has as many hit records as the oracle's and as its own n_hit, the
 records agree with the oracle's within 1e-6 (relative, 1e-9 absolute) and at
 least 99 % of them bit for bit (the end states' criteria); snapshots at the
-listed times the same way; the plain and the batched forms produce the same
+listed times and track points (every 0.5 m of path) the same way; the plain and the batched forms produce the same
 records bit for bit; in the field-storage scene (batched, FP32 field mode)
 each particle's hit records number its n_hit."""
 import numpy as np
@@ -23,26 +23,27 @@ def run_gpu(e, params, parts, mode):
     out, _ = e.integrate(params, parts)
     hits, nh = e.read_log(A.LOG_HIT)
     snaps, ns = e.read_log(A.LOG_SNAPSHOT)
-    assert nh == len(hits) and ns == len(snaps)
-    return out, hits, snaps
+    tracks, nt = e.read_log(A.LOG_TRACK)
+    assert nh == len(hits) and ns == len(snaps) and nt == len(tracks)
+    return out, hits, snaps, tracks
 
 
 def test_cube_logs_match_oracle(built, oracle_mod):
     from pentrack_gb300 import Engine, engine, workloads
     sc, params, parts = workloads.cube_storage(n=2000, simtime=10.0)
-    engine.set_logs(params, hitlog=True, snapshots=SNAPSHOTS)
+    engine.set_logs(params, hitlog=True, snapshots=SNAPSHOTS, track_interval=0.5)
     orc = oracle_mod.Oracle(sc)
     oout, _ = orc.integrate(params, parts)
-    ohits, osnaps = orc.read_log(A.LOG_HIT), orc.read_log(A.LOG_SNAPSHOT)
+    ohits, osnaps, otracks = orc.read_log(A.LOG_HIT), orc.read_log(A.LOG_SNAPSHOT), orc.read_log(A.LOG_TRACK)
     e = Engine(sc)
-    pout, phits, psnaps = run_gpu(e, params, parts, A.MODE_PLAIN)
-    bout, bhits, bsnaps = run_gpu(e, params, parts, A.MODE_BATCHED)
-    assert np.array_equal(phits, bhits) and np.array_equal(psnaps, bsnaps)
+    pout, phits, psnaps, ptracks = run_gpu(e, params, parts, A.MODE_PLAIN)
+    bout, bhits, bsnaps, btracks = run_gpu(e, params, parts, A.MODE_BATCHED)
+    assert np.array_equal(phits, bhits) and np.array_equal(psnaps, bsnaps) and np.array_equal(ptracks, btracks)
     per = np.bincount(phits[:, 0].astype(np.int64), minlength=parts.n)
     np.testing.assert_array_equal(per, pout.n_hit)
     np.testing.assert_array_equal(per, np.bincount(ohits[:, 0].astype(np.int64), minlength=parts.n))
     assert len(phits) > 10000
-    for g, o in ((phits, ohits), (psnaps, osnaps)):
+    for g, o in ((phits, ohits), (psnaps, osnaps), (ptracks, otracks)):
         assert g.shape == o.shape
         np.testing.assert_allclose(g, o, rtol=1e-6, atol=1e-9)
         assert np.mean(np.all(g == o, axis=1)) >= 0.99
@@ -56,8 +57,8 @@ def test_field_storage_hit_records_count_hits(built):
     engine.set_logs(params, hitlog=True)
     e = Engine(sc)
     params.field_precision = A.PREC_FP32
-    out, hits, snaps = run_gpu(e, params, parts, A.MODE_BATCHED)
-    assert len(snaps) == 0
+    out, hits, snaps, tracks = run_gpu(e, params, parts, A.MODE_BATCHED)
+    assert len(snaps) == 0 and len(tracks) == 0
     per = np.bincount(hits[:, 0].astype(np.int64) - int(parts.id[0]), minlength=parts.n)
     np.testing.assert_array_equal(per, out.n_hit)
     assert out.n_hit.sum() > 1000
