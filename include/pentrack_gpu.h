@@ -188,9 +188,14 @@ typedef struct pt_run_params {
      * trackloginterval (TLogger::PrintTrack, src/logger.cpp:143-200) */
     int32_t tracklog, reserved5;
     double trackloginterval;   /* [m] */
+    /* spinlog: a record at the start of each Bloch integration and after every
+     * Bloch step whose time crossed a multiple of spinloginterval
+     * (TLogger::PrintSpin, src/logger.cpp:237-284) */
+    int32_t spinlog, reserved6;
+    double spinloginterval;    /* [s] */
 } pt_run_params;
 
-enum { PT_LOG_HIT = 0, PT_LOG_SNAPSHOT = 1, PT_LOG_TRACK = 2 };
+enum { PT_LOG_HIT = 0, PT_LOG_SNAPSHOT = 1, PT_LOG_TRACK = 2, PT_LOG_SPIN = 3 };
 #define PT_MAX_SNAPSHOTS 1024
 /* hit record: particle, t, x, y, z, v1x, v1y, v1z, pol1, v2x, v2y, v2z, pol2,
  * nx, ny, nz, solid1 (leaving), solid2 (entering) -- the reference's hit-log
@@ -205,6 +210,9 @@ enum { PT_LOG_HIT = 0, PT_LOG_SNAPSHOT = 1, PT_LOG_TRACK = 2 };
  * current solid (the fields, energies and potential of the track log's
  * columns follow from these) */
 #define PT_TRACK_RECORD 10
+/* spin record: particle, t, x, y, z, Sx, Sy, Sz, Wx, Wy, Wz, Bx, By, Bz (the
+ * reference's spin-log columns after jobnumber) */
+#define PT_SPIN_RECORD 14
 
 /* schedulers of the batched form (results are the same bits with each) */
 enum { PT_SCHED_AUTO = 0, PT_SCHED_PHASED = 1, PT_SCHED_PERSISTENT = 2, PT_SCHED_PERSISTENT_WIDE = 3, PT_SCHED_PHASED_WIDE = 4 };
@@ -295,10 +303,10 @@ pt_status pt_batch_advance(pt_ctx *ctx, pt_batch *batch, double t_pause, pt_stat
  * RK steps in this call (one fixed step-batch of the plain form; 0 = no limit). */
 pt_status pt_batch_advance_steps(pt_ctx *ctx, pt_batch *batch, double t_pause, int32_t max_steps, pt_stats *stats);
 pt_status pt_batch_read(pt_ctx *ctx, pt_batch *batch, pt_particles *out);
-/* The records of log `kind` (PT_LOG_HIT, PT_LOG_SNAPSHOT, PT_LOG_TRACK) collected by the
+/* The records of log `kind` (PT_LOG_HIT, PT_LOG_SNAPSHOT, PT_LOG_TRACK, PT_LOG_SPIN) collected by the
  * last pt_integrate call or since the last pt_batch_create: *total receives the
  * number of events, up to `cap` records (of PT_HIT_RECORD / PT_SNAPSHOT_RECORD /
- * PT_TRACK_RECORD doubles, in no particular order) are copied to `rec` (may be NULL with
+ * PT_TRACK_RECORD / PT_SPIN_RECORD doubles, in no particular order) are copied to `rec` (may be NULL with
  * cap = 0 to ask for the count). */
 pt_status pt_log_read(pt_ctx *ctx, int32_t kind, int64_t cap, double *rec, int64_t *total);
 void pt_batch_destroy(pt_batch *batch);

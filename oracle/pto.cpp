@@ -533,7 +533,7 @@ struct Scene {
  * PrintSnapshot records, the library's record layout) */
 struct pto_ctx {
     Scene sc;
-    std::vector<double> hits, snaps, tracks;
+    std::vector<double> hits, snaps, tracks, spins;
 };
 
 /* ------------------------------------------------------------------ */
@@ -722,7 +722,22 @@ struct Tracker {
     pt_stats *stats;
     std::vector<Coll> cbuf;
     int64_t pid = 0;                        /* the particle being tracked */
-    std::vector<double> hitlog, snaplog, tracklog; /* records of this thread's particles */
+    std::vector<double> hitlog, snaplog, tracklog, spinlog; /* records of this thread's particles */
+
+    /* TLogger::PrintSpin (src/logger.cpp:237-284) */
+    void log_spin(double x1, double x, const double *S) {
+        const double iv = P.spinloginterval;
+        if (!P.spinlog || !(iv > 0)) return;
+        if (x > x1 && (int)(x1 / iv) == (int)(x / iv)) return;
+        double y[9], dydt[9], B[3], dB[3][3], V, E[3], W[3];
+        st.calc_state(x, y);
+        bfield(y[0], y[1], y[2], x, B, dB);
+        efield(y[0], y[1], y[2], x, V, E);
+        eom(y, dydt, B, dB, E);
+        spin_axis(B, E, dydt, W);
+        const double r[PT_SPIN_RECORD] = {(double)pid, x, y[0], y[1], y[2], S[0], S[1], S[2], W[0], W[1], W[2], B[0], B[1], B[2]};
+        spinlog.insert(spinlog.end(), r, r + PT_SPIN_RECORD);
+    }
 
     /* TLogger::PrintTrack (src/logger.cpp:143-200): at zero path length and
      * when a step from path length l1 to y[8] crossed a multiple of the
@@ -1180,6 +1195,7 @@ struct Tracker {
                     for (int k = 0; k < 3; ++k) spin[k] = B1[k] * y1[7] / Babs1;
                 Dense5<5> ss(1e-12, 1e-12);
                 ss.initialize(spin, x1, std::fabs(PT_PI / sp.gamma / Babs1));
+                log_spin(x1, x1, spin);
                 auto sys = [this](const double *S, double *dS, double t) { spin_derivs(S, dS, t); };
                 int64_t rej = 0;
                 for (int64_t steps = 0;; ++steps) {
@@ -1193,6 +1209,7 @@ struct Tracker {
                         std::copy(ss.x, ss.x + 5, spin);
                     }
                     if (stats) stats->spin_steps++;
+                    log_spin(ss.to, t, spin);
                     if (t >= x2) break;
                 }
             } else if (spin[0] != 0 || spin[1] != 0 || spin[2] != 0) {
@@ -1440,8 +1457,9 @@ void pto_destroy(pto_ctx *ctx) { delete ctx; }
 /* the records of the last pto_track call's log `kind` (PT_LOG_HIT,
  * PT_LOG_SNAPSHOT): their number, and up to cap of them into rec */
 int64_t pto_log_read(pto_ctx *ctx, int32_t kind, int64_t cap, double *rec) {
-    const std::vector<double> &v = kind == PT_LOG_HIT ? ctx->hits : kind == PT_LOG_SNAPSHOT ? ctx->snaps : ctx->tracks;
-    const int w = kind == PT_LOG_HIT ? PT_HIT_RECORD : kind == PT_LOG_SNAPSHOT ? PT_SNAPSHOT_RECORD : PT_TRACK_RECORD;
+    const std::vector<double> &v =
+        kind == PT_LOG_HIT ? ctx->hits : kind == PT_LOG_SNAPSHOT ? ctx->snaps : kind == PT_LOG_TRACK ? ctx->tracks : ctx->spins;
+    const int w = kind == PT_LOG_HIT ? PT_HIT_RECORD : kind == PT_LOG_SNAPSHOT ? PT_SNAPSHOT_RECORD : kind == PT_LOG_TRACK ? PT_TRACK_RECORD : PT_SPIN_RECORD;
     const int64_t n = (int64_t)v.size() / w;
     if (rec) std::copy(v.begin(), v.begin() + std::min(n, cap) * w, rec);
     return n;
@@ -1456,7 +1474,7 @@ int pto_track(pto_ctx *ctx, const pt_run_params *params, const pt_particles *in,
     std::vector<pt_stats> st(nthreads);
     std::memset(st.data(), 0, sizeof(pt_stats) * nthreads);
     std::atomic<int64_t> next{0};
-    std::vector<std::vector<double>> hits(nthreads), snaps(nthreads), tracks(nthreads);
+    std::vector<std::vector<double>> hits(nthreads), snaps(nthreads), tracks(nthreads), spins(nthreads);
     auto work = [&](int w) {
         Tracker tr(ctx->sc, *params, &st[w]);
         double ys[9], ss[5];
@@ -1470,6 +1488,7 @@ int pto_track(pto_ctx *ctx, const pt_run_params *params, const pt_particles *in,
         hits[w].swap(tr.hitlog);
         snaps[w].swap(tr.snaplog);
         tracks[w].swap(tr.tracklog);
+        spins[w].swap(tr.spinlog);
     };
     std::vector<std::thread> th;
     for (int w = 1; w < nthreads; ++w) th.emplace_back(work, w);
@@ -1478,10 +1497,12 @@ int pto_track(pto_ctx *ctx, const pt_run_params *params, const pt_particles *in,
     ctx->hits.clear();
     ctx->snaps.clear();
     ctx->tracks.clear();
+    ctx->spins.clear();
     for (int w = 0; w < nthreads; ++w) {
         ctx->hits.insert(ctx->hits.end(), hits[w].begin(), hits[w].end());
         ctx->snaps.insert(ctx->snaps.end(), snaps[w].begin(), snaps[w].end());
         ctx->tracks.insert(ctx->tracks.end(), tracks[w].begin(), tracks[w].end());
+        ctx->spins.insert(ctx->spins.end(), spins[w].begin(), spins[w].end());
     }
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));

@@ -93,7 +93,8 @@ class Oracle:
     def read_log(self, kind):
         """records of the last integrate call's hit log (A.LOG_HIT) or snapshot
         log (A.LOG_SNAPSHOT), sorted by particle and time"""
-        width = {A.LOG_HIT: A.HIT_RECORD, A.LOG_SNAPSHOT: A.SNAPSHOT_RECORD, A.LOG_TRACK: A.TRACK_RECORD}[kind]
+        width = {A.LOG_HIT: A.HIT_RECORD, A.LOG_SNAPSHOT: A.SNAPSHOT_RECORD, A.LOG_TRACK: A.TRACK_RECORD,
+                 A.LOG_SPIN: A.SPIN_RECORD}[kind]
         n = lib().pto_log_read(self.h, kind, 0, None)
         rec = np.zeros((n, width))
         if n:

@@ -72,6 +72,7 @@ class RunParams(C.Structure):
         ("hitlog", C.c_int32), ("snapshotlog", C.c_int32), ("snapshots", c_double_p), ("n_snapshots", C.c_int32),
         ("reserved4", C.c_int32), ("log_capacity", C.c_int64),
         ("tracklog", C.c_int32), ("reserved5", C.c_int32), ("trackloginterval", C.c_double),
+        ("spinlog", C.c_int32), ("reserved6", C.c_int32), ("spinloginterval", C.c_double),
     ]
 
 
@@ -86,8 +87,8 @@ class Particles(C.Structure):
 
 
 SOURCE_BOX, SOURCE_CYLINDER, SOURCE_SOLID = 0, 1, 2
-LOG_HIT, LOG_SNAPSHOT, LOG_TRACK = 0, 1, 2
-HIT_RECORD, SNAPSHOT_RECORD, TRACK_RECORD = 18, 22, 10
+LOG_HIT, LOG_SNAPSHOT, LOG_TRACK, LOG_SPIN = 0, 1, 2, 3
+HIT_RECORD, SNAPSHOT_RECORD, TRACK_RECORD, SPIN_RECORD = 18, 22, 10, 14
 
 
 class SourceParams(C.Structure):

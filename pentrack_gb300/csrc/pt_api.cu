@@ -62,10 +62,10 @@ struct pt_ctx {
     void *arena = nullptr;
     size_t arena_bytes = 0;
     /* event logs of the last run that asked for them (pt_log_read) */
-    double *log_hit = nullptr, *log_snap = nullptr, *log_track = nullptr, *log_snap_t = nullptr;
-    unsigned long long *log_n = nullptr; /* [0] hits, [1] snapshots, [2] track points */
-    long long log_cap_hit = 0, log_cap_snap = 0, log_cap_track = 0, log_cap = 0;
-    bool log_hit_on = false, log_snap_on = false, log_track_on = false;
+    double *log_hit = nullptr, *log_snap = nullptr, *log_track = nullptr, *log_spin = nullptr, *log_snap_t = nullptr;
+    unsigned long long *log_n = nullptr; /* [0] hits, [1] snapshots, [2] track points, [3] spin points */
+    long long log_cap_hit = 0, log_cap_snap = 0, log_cap_track = 0, log_cap_spin = 0, log_cap = 0;
+    bool log_hit_on = false, log_snap_on = false, log_track_on = false, log_spin_on = false;
 };
 
 /* Scratch of pt_segment_collisions_noalloc: a fixed device array in the
@@ -1054,6 +1054,7 @@ void pt_destroy(pt_ctx *c) {
     if (c->log_hit) cudaFree(c->log_hit);
     if (c->log_snap) cudaFree(c->log_snap);
     if (c->log_track) cudaFree(c->log_track);
+    if (c->log_spin) cudaFree(c->log_spin);
     if (c->log_snap_t) cudaFree(c->log_snap_t);
     if (c->log_n) cudaFree(c->log_n);
     if (c->counters) cudaFree(c->counters);
@@ -1119,14 +1120,15 @@ pt_status setup_logs(pt_ctx *c, const pt_run_params *p, DRun &R) {
     c->log_hit_on = p->hitlog != 0;
     c->log_snap_on = p->snapshotlog != 0 && p->n_snapshots > 0;
     c->log_track_on = p->tracklog != 0 && p->trackloginterval > 0;
-    if (!c->log_hit_on && !c->log_snap_on && !c->log_track_on) return PT_OK;
+    c->log_spin_on = p->spinlog != 0 && p->spinloginterval > 0;
+    if (!c->log_hit_on && !c->log_snap_on && !c->log_track_on && !c->log_spin_on) return PT_OK;
     if (c->log_snap_on && (p->n_snapshots > PT_MAX_SNAPSHOTS || !p->snapshots)) {
         c->err = "snapshotlog: 1 to 1024 snapshot times";
         return PT_ERR_INVALID;
     }
     const long long cap = p->log_capacity > 0 ? p->log_capacity : 1000000;
     cudaError_t e = cudaSuccess;
-    if (!c->log_n && (e = cudaMalloc((void **)&c->log_n, 3 * sizeof(unsigned long long)))) return ck(c, e, "log counts"), PT_ERR_OOM;
+    if (!c->log_n && (e = cudaMalloc((void **)&c->log_n, 4 * sizeof(unsigned long long)))) return ck(c, e, "log counts"), PT_ERR_OOM;
     if (!c->log_snap_t && (e = cudaMalloc((void **)&c->log_snap_t, PT_MAX_SNAPSHOTS * sizeof(double)))) return ck(c, e, "log times"), PT_ERR_OOM;
     if (c->log_hit_on && c->log_cap_hit < cap) {
         if (c->log_hit) cudaFree(c->log_hit);
@@ -1149,8 +1151,15 @@ pt_status setup_logs(pt_ctx *c, const pt_run_params *p, DRun &R) {
         if ((e = cudaMalloc((void **)&c->log_track, (size_t)cap * PT_TRACK_RECORD * sizeof(double)))) return ck(c, e, "track log"), PT_ERR_OOM;
         c->log_cap_track = cap;
     }
+    if (c->log_spin_on && c->log_cap_spin < cap) {
+        if (c->log_spin) cudaFree(c->log_spin);
+        c->log_spin = nullptr;
+        c->log_cap_spin = 0;
+        if ((e = cudaMalloc((void **)&c->log_spin, (size_t)cap * PT_SPIN_RECORD * sizeof(double)))) return ck(c, e, "spin log"), PT_ERR_OOM;
+        c->log_cap_spin = cap;
+    }
     c->log_cap = cap;
-    if ((e = cudaMemsetAsync(c->log_n, 0, 3 * sizeof(unsigned long long), c->stream))) return ck(c, e, "log counts"), PT_ERR_CUDA;
+    if ((e = cudaMemsetAsync(c->log_n, 0, 4 * sizeof(unsigned long long), c->stream))) return ck(c, e, "log counts"), PT_ERR_CUDA;
     if (c->log_snap_on &&
         (e = cudaMemcpyAsync(c->log_snap_t, p->snapshots, p->n_snapshots * sizeof(double), cudaMemcpyHostToDevice, c->stream)))
         return ck(c, e, "snapshot times"), PT_ERR_CUDA;
@@ -1158,6 +1167,11 @@ pt_status setup_logs(pt_ctx *c, const pt_run_params *p, DRun &R) {
     R.log.hit_n = c->log_n;
     R.log.snap_n = c->log_n + 1;
     R.log.track_n = c->log_n + 2;
+    R.log.spin_n = c->log_n + 3;
+    if (c->log_spin_on) {
+        R.log.spin = c->log_spin;
+        R.log.spin_interval = p->spinloginterval;
+    }
     if (c->log_hit_on) R.log.hit = c->log_hit;
     if (c->log_track_on) {
         R.log.track = c->log_track;
@@ -1365,9 +1379,9 @@ pt_status pt_integrate(pt_ctx *c, const pt_run_params *p, const pt_particles *in
 }
 
 pt_status pt_log_read(pt_ctx *c, int32_t kind, int64_t cap, double *rec, int64_t *total) {
-    if (!c || !total || cap < 0 || (cap > 0 && !rec) || kind < PT_LOG_HIT || kind > PT_LOG_TRACK) return PT_ERR_INVALID;
+    if (!c || !total || cap < 0 || (cap > 0 && !rec) || kind < PT_LOG_HIT || kind > PT_LOG_SPIN) return PT_ERR_INVALID;
     *total = 0;
-    const bool on = kind == PT_LOG_HIT ? c->log_hit_on : kind == PT_LOG_SNAPSHOT ? c->log_snap_on : c->log_track_on;
+    const bool on = kind == PT_LOG_HIT ? c->log_hit_on : kind == PT_LOG_SNAPSHOT ? c->log_snap_on : kind == PT_LOG_TRACK ? c->log_track_on : c->log_spin_on;
     if (!on || !c->log_n) return PT_OK;
     cudaSetDevice(c->device);
     unsigned long long cnt = 0;
@@ -1376,8 +1390,8 @@ pt_status pt_log_read(pt_ctx *c, int32_t kind, int64_t cap, double *rec, int64_t
     if (e) return ck(c, e, "log count"), PT_ERR_CUDA;
     *total = (int64_t)cnt;
     const int64_t kept = std::min<int64_t>((int64_t)cnt, std::min<int64_t>(cap, c->log_cap));
-    const int width = kind == PT_LOG_HIT ? PT_HIT_RECORD : kind == PT_LOG_SNAPSHOT ? PT_SNAPSHOT_RECORD : PT_TRACK_RECORD;
-    const double *src = kind == PT_LOG_HIT ? c->log_hit : kind == PT_LOG_SNAPSHOT ? c->log_snap : c->log_track;
+    const int width = kind == PT_LOG_HIT ? PT_HIT_RECORD : kind == PT_LOG_SNAPSHOT ? PT_SNAPSHOT_RECORD : kind == PT_LOG_TRACK ? PT_TRACK_RECORD : PT_SPIN_RECORD;
+    const double *src = kind == PT_LOG_HIT ? c->log_hit : kind == PT_LOG_SNAPSHOT ? c->log_snap : kind == PT_LOG_TRACK ? c->log_track : c->log_spin;
     if (kept > 0) {
         e = cudaMemcpyAsync(rec, src, (size_t)kept * width * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
         if (!e) e = cudaStreamSynchronize(c->stream);

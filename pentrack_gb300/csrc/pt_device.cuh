@@ -153,12 +153,12 @@ struct DSpecies {
 /* event-log buffers (null when the log is off): records appended at an
  * atomic count; counts past the capacity are kept, records dropped */
 struct DLog {
-    double *hit, *snap, *track;
-    unsigned long long *hit_n, *snap_n, *track_n;
+    double *hit, *snap, *track, *spin;
+    unsigned long long *hit_n, *snap_n, *track_n, *spin_n;
     long long cap;
     const double *snap_t;
     int n_snap, pad;
-    double track_interval;
+    double track_interval, spin_interval;
 };
 
 struct DRun {

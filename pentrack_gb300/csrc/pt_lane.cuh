@@ -518,6 +518,7 @@ template <class Tape> struct LaneT {
         bs.dt = dt0;
         bs.steps = 0;
         bs.tries = 0;
+        if (R.log.spin) log_spin(x1, x1, spin);
         spin_derivs(bs.x, bs.dxdt, bs.ts, Tape::kSpinStages ? bs.w : nullptr);
     }
     /* Runs the stepper from `bs` towards x2 for at most max_steps accepted
@@ -627,9 +628,11 @@ template <class Tape> struct LaneT {
             }
             for (int i = 0; i < 5; ++i)
                 spin[i] = fma(hb[5], dxdt[i], fma(hb[4], k6_[i], fma(hb[3], k5_[i], fma(hb[2], k4_[i], fma(hb[1], k3_[i], fma(hb[0], dxo5[i], xo5[i]))))));
+            if (R.log.spin) log_spin(tso, x2, spin);
             return 1;
         }
         for (int i = 0; i < 5; ++i) spin[i] = x[i];
+        if (R.log.spin) log_spin(tso, ts, spin);
         return ts >= x2 ? 1 : 0;
     }
 
@@ -1043,6 +1046,23 @@ template <class Tape> struct LaneT {
         double *r = R.log.track + k * PT_TRACK_RECORD;
         const double v[PT_TRACK_RECORD] = {(double)id, x, y[0], y[1], y[2], y[3], y[4], y[5], y[7], (double)S.solids[cur_solid()].id};
         for (int j = 0; j < PT_TRACK_RECORD; ++j) r[j] = v[j];
+    }
+    /* TLogger::PrintSpin (src/logger.cpp:237-284): at the start of a Bloch
+     * integration (x == x1) and when a Bloch step from x1 to x crossed a
+     * multiple of the interval: position, spin, precession axis and B at x */
+    __device__ __noinline__ void log_spin(double x1, double x, const double *Sv) {
+        const double iv = R.log.spin_interval;
+        if (!(iv > 0)) return;
+        if (x > x1 && (int)(x1 / iv) == (int)(x / iv)) return;
+        double yy[9], dS[5], W[3], B[3], dB[3][3];
+        calc_spin_state(x, yy);
+        spin_derivs(Sv, dS, x, W);
+        bfield<true>(S, R.prec, yy[0], yy[1], yy[2], B, dB);
+        const unsigned long long k = atomicAdd(R.log.spin_n, 1ull);
+        if ((long long)k >= R.log.cap) return;
+        double *r = R.log.spin + k * PT_SPIN_RECORD;
+        const double v[PT_SPIN_RECORD] = {(double)id, x, yy[0], yy[1], yy[2], Sv[0], Sv[1], Sv[2], W[0], W[1], W[2], B[0], B[1], B[2]};
+        for (int j = 0; j < PT_SPIN_RECORD; ++j) r[j] = v[j];
     }
     __device__ __noinline__ bool snapshot_due(double x) const {
         for (int k = 0; k < R.log.n_snap; ++k)

@@ -238,12 +238,15 @@ def run_params(species=A.NEUTRON, simtime=100.0, tau=0.0, tmax=9e99, lmax=9e99, 
     return p
 
 
-def set_logs(p, hitlog=False, snapshots=None, track_interval=0.0, capacity=0):
-    """Turn on the hit log, (with snapshot times) the snapshot log and (with
-    a path-length interval [m]) the track log of a run (the particle options
-    hitlog, snapshotlog / snapshots and tracklog / trackloginterval of
-    src/logger.cpp:128-235); read them after the run with Engine.read_log."""
+def set_logs(p, hitlog=False, snapshots=None, track_interval=0.0, spin_interval=0.0, capacity=0):
+    """Turn on the hit log, (with snapshot times) the snapshot log, (with a
+    path-length interval [m]) the track log and (with a time interval [s])
+    the spin log of a run (the particle options hitlog, snapshotlog /
+    snapshots, tracklog / trackloginterval and spinlog / spinloginterval of
+    src/logger.cpp:128-284); read them after the run with Engine.read_log."""
     p.hitlog = int(bool(hitlog))
+    p.spinlog = int(spin_interval > 0)
+    p.spinloginterval = float(spin_interval)
     p.tracklog = int(track_interval > 0)
     p.trackloginterval = float(track_interval)
     ts = np.ascontiguousarray(np.array(() if snapshots is None else snapshots, dtype=np.float64).reshape(-1))
@@ -415,7 +418,8 @@ class Engine:
         (LOG_TRACK), sorted by
         particle and time, as an (n, width) array; and the number of events
         (more than n when the log's capacity was exceeded)."""
-        width = {A.LOG_HIT: A.HIT_RECORD, A.LOG_SNAPSHOT: A.SNAPSHOT_RECORD, A.LOG_TRACK: A.TRACK_RECORD}[kind]
+        width = {A.LOG_HIT: A.HIT_RECORD, A.LOG_SNAPSHOT: A.SNAPSHOT_RECORD, A.LOG_TRACK: A.TRACK_RECORD,
+                 A.LOG_SPIN: A.SPIN_RECORD}[kind]
         total = C.c_int64(0)
         self._check(lib().pt_log_read(self.h, kind, 0, None, C.byref(total)))
         rec = np.zeros((max(total.value, 0), width))

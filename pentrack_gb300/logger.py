@@ -208,6 +208,17 @@ def write_tracklog(directory, scene, kind, records, field, jobnumber=0):
     return write_log(directory, jobnumber, SPECIES_NAME[kind], "track", TRACK_TITLES, cols)
 
 
+SPIN_TITLES = ("jobnumber", "particle", "t", "x", "y", "z", "Sx", "Sy", "Sz", "Wx", "Wy", "Wz", "Bx", "By", "Bz")
+
+
+def write_spinlog(directory, kind, records, jobnumber=0):
+    """The spin log (TLogger::PrintSpin, src/logger.cpp:237-284) from the
+    spin records of Engine.read_log(LOG_SPIN).  Returns the path."""
+    r = np.asarray(records, dtype=np.float64).reshape(-1, 14)
+    cols = [np.full(len(r), float(jobnumber)), r[:, 0] + 1] + [r[:, k] for k in range(1, 14)]
+    return write_log(directory, jobnumber, SPECIES_NAME[kind], "spin", SPIN_TITLES, cols)
+
+
 def snapshot_states(start, records):
     """(start subset, ParticleSet at the snapshots) from snapshot records of
     Engine.read_log(LOG_SNAPSHOT): for each record the particle's start state

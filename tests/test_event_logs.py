@@ -89,3 +89,41 @@ def test_track_points(cube_logs, tmp_path):
     H = np.array([float(l.split()[10]) for l in lines[1:]])
     H0 = dict(zip(first[:, 0].astype(np.int64), H[np.r_[True, tr[1:, 0] != tr[:-1, 0]]]))
     np.testing.assert_allclose(H, [H0[int(i)] for i in tr[:, 0]], rtol=1e-5)  # each particle keeps its energy
+
+
+def test_spin_log(oracle_mod, tmp_path):
+    """spin records at each Bloch integration's start and at every crossing of
+    a multiple of the interval: unit spins, the precession axis |gamma_n| |B|
+    (1 uT along z; the v x E and Thomas terms are below 1e-4 of it), times
+    increasing per particle, at least one record per interval of tracked time"""
+    from pentrack_gb300 import Scene, engine, logger, scenes, workloads
+    sc = Scene()
+    sc.add_material("wall", 335.0)
+    sc.add_material("vacuum", 0.0)
+    sc.add_solid(1, "wall")
+    sc.add_solid(2, "vacuum", scenes.cylinder_mesh(0.2, -0.06, 0.06, 64))
+    ax = (np.linspace(-0.25, 0.25, 6), np.linspace(-0.25, 0.25, 6), np.linspace(-0.1, 0.1, 5))
+    sc.add_table3d(*ax, np.zeros((6, 6, 5)), np.zeros((6, 6, 5)), np.full((6, 6, 5), 1e-6))
+    sc.add_uniform_e(0.0, 0.0, 1e6)
+    ids = np.arange(8, dtype=np.int64)
+    pos, (E, ph, th, pol) = scenes.source_cylinder(1004, ids, 0.0, 0.19, -0.05, 0.05, 0.0, 200e-9, polarization=1.0)
+    parts = scenes.make_particles(1004, ids, pos, E, ph, th, pol)
+    parts.spin[:] = 0.0
+    parts.spin[0] = 1.0
+    params = workloads.run_params(A.NEUTRON, simtime=0.05, tau=0.0, tmax=9e99, lmax=9e99, bmax=1.0, spintimes=(0.0, 100.0),
+                                  seed=1004)
+    engine.set_logs(params, spin_interval=0.002)
+    orc = oracle_mod.Oracle(sc)
+    out, st = orc.integrate(params, parts, nthreads=2)
+    sp = orc.read_log(A.LOG_SPIN)
+    assert sp.shape[1] == A.SPIN_RECORD and len(sp) >= 8 * 25
+    np.testing.assert_allclose(np.sqrt((sp[:, 5:8] ** 2).sum(1)), 1.0, atol=1e-8)
+    W = np.sqrt((sp[:, 8:11] ** 2).sum(1))
+    B = np.sqrt((sp[:, 11:14] ** 2).sum(1))
+    np.testing.assert_allclose(W, abs(scenes.GAMMA_N) * B, rtol=1e-3)
+    for i in ids:
+        t = sp[sp[:, 0] == i, 1]
+        assert np.all(np.diff(t) >= 0) and len(t) >= 25
+    p = logger.write_spinlog(str(tmp_path), A.NEUTRON, sp)
+    lines = open(p).read().splitlines()
+    assert lines[0].split() == list(logger.SPIN_TITLES) and len(lines) == 1 + len(sp)

@@ -62,3 +62,45 @@ def test_field_storage_hit_records_count_hits(built):
     per = np.bincount(hits[:, 0].astype(np.int64) - int(parts.id[0]), minlength=parts.n)
     np.testing.assert_array_equal(per, out.n_hit)
     assert out.n_hit.sum() > 1000
+
+
+def test_spin_log_matches_oracle(built, oracle_mod):
+    """spin records of the plain form against the oracle's in the uniform
+    1 uT field with E = 1e6 V/m (the spin tests' setting): the same numbers
+    of records within 1 %, unit spins, axis |gamma_n| |B|, and where a record
+    falls at the same time on both sides (the Bloch step sequences agree but
+    for rounding) the spins within 1e-8"""
+    from pentrack_gb300 import Engine, Scene, engine, scenes, workloads
+    sc = Scene()
+    sc.add_material("wall", 335.0)
+    sc.add_material("vacuum", 0.0)
+    sc.add_solid(1, "wall")
+    sc.add_solid(2, "vacuum", scenes.cylinder_mesh(0.2, -0.06, 0.06, 128))
+    ax = (np.linspace(-0.25, 0.25, 6), np.linspace(-0.25, 0.25, 6), np.linspace(-0.1, 0.1, 5))
+    sc.add_table3d(*ax, np.zeros((6, 6, 5)), np.zeros((6, 6, 5)), np.full((6, 6, 5), 1e-6))
+    sc.add_uniform_e(0.0, 0.0, 1e6)
+    ids = np.arange(64, dtype=np.int64)
+    pos, (E, ph, th, pol) = scenes.source_cylinder(1004, ids, 0.0, 0.19, -0.05, 0.05, 0.0, 200e-9, polarization=1.0)
+    parts = scenes.make_particles(1004, ids, pos, E, ph, th, pol)
+    parts.spin[:] = 0.0
+    parts.spin[0] = 1.0
+    params = workloads.run_params(A.NEUTRON, simtime=0.1, tau=0.0, tmax=9e99, lmax=9e99, bmax=1.0, spintimes=(0.0, 100.0),
+                                  seed=1004)
+    engine.set_logs(params, spin_interval=0.005)
+    orc = oracle_mod.Oracle(sc)
+    orc.integrate(params, parts)
+    osp = orc.read_log(A.LOG_SPIN)
+    e = Engine(sc)
+    params.mode = A.MODE_PLAIN
+    e.integrate(params, parts)
+    gsp, n = e.read_log(A.LOG_SPIN)
+    assert n == len(gsp) and abs(len(gsp) - len(osp)) <= 0.01 * len(osp) and len(osp) > 64 * 20
+    np.testing.assert_allclose(np.sqrt((gsp[:, 5:8] ** 2).sum(1)), 1.0, atol=1e-8)
+    np.testing.assert_allclose(np.sqrt((gsp[:, 8:11] ** 2).sum(1)), abs(scenes.GAMMA_N) * np.sqrt((gsp[:, 11:14] ** 2).sum(1)),
+                               rtol=1e-3)
+    okeys = {(int(r[0]), r[1]): r for r in osp}
+    same = [(g, okeys[(int(g[0]), g[1])]) for g in gsp if (int(g[0]), g[1]) in okeys]
+    assert len(same) >= 0.5 * len(gsp)
+    g = np.array([a for a, _ in same])
+    o = np.array([b for _, b in same])
+    np.testing.assert_allclose(g[:, 2:8], o[:, 2:8], rtol=0, atol=1e-8)
