@@ -377,7 +377,7 @@ pt_status pt_point_solids(pt_ctx *ctx, int64_t n, const double *p, uint64_t *mas
  * TSTLVolumeSource: include/source.h:186-331), with or without
  * PhaseSpaceWeighting, with a flat energy spectrum, the azimuth uniform and
  * the polar angle sine-distributed, the start time uniform. */
-enum { PT_SOURCE_BOX = 0, PT_SOURCE_CYLINDER = 1, PT_SOURCE_SOLID = 2 };
+enum { PT_SOURCE_BOX = 0, PT_SOURCE_CYLINDER = 1, PT_SOURCE_SOLID = 2, PT_SOURCE_SURFACE_CYLINDER = 3 };
 typedef struct pt_source_params {
     int32_t species;
     int32_t shape;             /* PT_SOURCE_* */
@@ -394,6 +394,14 @@ typedef struct pt_source_params {
     int64_t n_min_samples;     /* phase_space: points for the minimum potential Vmin (0: 100,000) */
     int32_t max_rounds;        /* proposal rounds per particle (0: 100,000); STL points: 10,000 box proposals each */
     int32_t reserved;
+    /* the cylindrical surface source (TSurfaceSource::CreateParticle,
+     * src/source.cpp:102-131; TCylindricalSurfaceSource, include/source.h:
+     * 255-283): a point on the scene's surfaces inside the cylinder's r, phi, z
+     * ranges, moved 1e-8 m off the surface along the face normal, a
+     * cos(theta) sin(theta) direction about the normal, the normal energy
+     * raised by enormal [eV].  (TSTLSurfaceSource's region is an STL that is
+     * not part of the geometry: it stays host-side, pentrack_gb300/sources.py.) */
+    double enormal;
 } pt_source_params;
 
 /* n particles with ids `ids` from the source: out->id, t, y (9n) and spin

@@ -45,6 +45,10 @@ struct pt_ctx {
     int device = 0;
     std::string err;
     DScene scene;
+    /* the scene's triangles in the caller's order (the surface sources pick
+     * them by area in that order; the device copy is in BVH order) */
+    std::vector<double> host_tris;
+    std::vector<int32_t> host_tri_solid;
     std::vector<void *> allocs;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs0 = nullptr, evs1 = nullptr;
@@ -195,6 +199,8 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
     if (d->n_solids > PT_MAX_SOLIDS) { err = "at most 64 solids are supported"; return PT_ERR_UNSUPPORTED; }
     if (d->n_fields > PT_MAX_FIELDS) { err = "at most 8 fields are supported"; return PT_ERR_UNSUPPORTED; }
     if (d->n_triangles > 0 && (!d->triangles || !d->triangle_solid)) { err = "triangles missing"; return PT_ERR_INVALID; }
+    c->host_tris.assign(d->triangles, d->triangles + 9 * d->n_triangles);
+    c->host_tri_solid.assign(d->triangle_solid, d->triangle_solid + d->n_triangles);
     /* materials */
     std::vector<DMat> mats(d->n_materials);
     for (int i = 0; i < d->n_materials; ++i) {
@@ -1654,7 +1660,9 @@ pt_status pt_probe_fp64(pt_ctx *c, double *tflops) {
 pt_status pt_source_volume(pt_ctx *c, const pt_source_params *sp, int64_t n, const int64_t *ids, pt_particles *out, double *vmin_out) {
     if (!c || !sp || n < 0 || (n && (!ids || !out || !out->id || !out->t || !out->y || !out->spin))) return PT_ERR_INVALID;
     if (sp->species < PT_NEUTRON || sp->species > PT_ELECTRON) { c->err = "pt_source_volume: unknown species"; return PT_ERR_INVALID; }
-    if (sp->shape < PT_SOURCE_BOX || sp->shape > PT_SOURCE_SOLID) { c->err = "pt_source_volume: unknown shape"; return PT_ERR_INVALID; }
+    if (sp->shape < PT_SOURCE_BOX || sp->shape > PT_SOURCE_SURFACE_CYLINDER) { c->err = "pt_source_volume: unknown shape"; return PT_ERR_INVALID; }
+    const bool surface = sp->shape == PT_SOURCE_SURFACE_CYLINDER;
+    if (surface && sp->phase_space) { c->err = "pt_source_volume: phase-space weighting applies to volume sources"; return PT_ERR_INVALID; }
     if (sp->shape == PT_SOURCE_SOLID && (sp->solid < 1 || sp->solid >= c->scene.n_solids)) {
         c->err = "pt_source_volume: solid must index a scene solid other than the default one";
         return PT_ERR_INVALID;
@@ -1667,10 +1675,45 @@ pt_status pt_source_volume(pt_ctx *c, const pt_source_params *sp, int64_t n, con
     Q.rmin = sp->rmin; Q.rmax = sp->rmax; Q.phimin = sp->phimin; Q.phimax = sp->phimax; Q.zmin = sp->zmin; Q.zmax = sp->zmax;
     Q.emin = sp->emin; Q.emax = sp->emax; Q.polarization = sp->polarization; Q.tmin = sp->tmin; Q.tmax = sp->tmax;
     Q.thetamin = sp->thetamin; Q.thetamax = sp->thetamax; Q.phimin_v = sp->phimin_v; Q.phimax_v = sp->phimax_v;
+    Q.enormal = sp->enormal;
     const DSpecies spc = make_species(sp->species);
     cudaSetDevice(c->device);
     std::vector<void *> tmp;
     cudaError_t e = cudaSuccess;
+    if (surface) { /* RandomPointOnSurface's candidates: the meshes whose box meets the source box */
+        const double blo[3] = {-sp->rmax, -sp->rmax, sp->zmin}, bhi[3] = {sp->rmax, sp->rmax, sp->zmax};
+        std::vector<double> tri, cum;
+        const int64_t nt = (int64_t)c->host_tri_solid.size();
+        double run = 0;
+        for (int64_t a0 = 0; a0 < nt;) { /* one mesh: a run of triangles of one solid */
+            int64_t a1 = a0;
+            while (a1 < nt && c->host_tri_solid[a1] == c->host_tri_solid[a0]) ++a1;
+            double mlo[3] = {INFINITY, INFINITY, INFINITY}, mhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+            for (int64_t k = a0; k < a1; ++k)
+                for (int v = 0; v < 3; ++v)
+                    for (int a = 0; a < 3; ++a) {
+                        mlo[a] = std::min(mlo[a], c->host_tris[9 * k + 3 * v + a]);
+                        mhi[a] = std::max(mhi[a], c->host_tris[9 * k + 3 * v + a]);
+                    }
+            bool meets = true;
+            for (int a = 0; a < 3; ++a) meets = meets && !(mhi[a] < blo[a]) && !(mlo[a] > bhi[a]);
+            if (meets)
+                for (int64_t k = a0; k < a1; ++k) {
+                    const double *t = &c->host_tris[9 * k];
+                    const double e1[3] = {t[3] - t[0], t[4] - t[1], t[5] - t[2]}, e2[3] = {t[6] - t[0], t[7] - t[1], t[8] - t[2]};
+                    const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2], cz = e1[0] * e2[1] - e1[1] * e2[0];
+                    run = run + 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+                    cum.push_back(run);
+                    tri.insert(tri.end(), t, t + 9);
+                }
+            a0 = a1;
+        }
+        if (cum.empty()) { c->err = "pt_source_volume: no surface of the scene meets the source region"; return PT_ERR_INVALID; }
+        Q.surf_tri = dupload(tmp, tri.data(), tri.size(), e);
+        if (!e) Q.surf_cum = dupload(tmp, cum.data(), cum.size(), e);
+        if (e) { free_list(tmp); return ck(c, e, "surface source upload"), PT_ERR_OOM; }
+        Q.n_surf = (int)cum.size();
+    }
     double vmin = -INFINITY;
     if (Q.phase_space) { /* FindPotentialMinimum over a fixed sample (src/source.cpp:136-156) */
         const int64_t m = sp->n_min_samples > 0 ? sp->n_min_samples : 100000;
@@ -1699,7 +1742,8 @@ pt_status pt_source_volume(pt_ctx *c, const pt_source_params *sp, int64_t n, con
     double *dt = dalloc<double>(tmp, n, e), *dy = dalloc<double>(tmp, 9 * n, e), *ds = dalloc<double>(tmp, 5 * n, e);
     int *dst = dalloc<int>(tmp, n, e);
     if (e) { free_list(tmp); return ck(c, e, "source alloc"), PT_ERR_OOM; }
-    k_source<<<grid_for(n, 128), 128, 0, c->stream>>>(c->scene, Q, spc, n, dids, vmin, dt, dy, ds, dst);
+    if (surface) k_source_surface<<<grid_for(n, 128), 128, 0, c->stream>>>(c->scene, Q, spc, n, dids, dt, dy, ds, dst);
+    else k_source<<<grid_for(n, 128), 128, 0, c->stream>>>(c->scene, Q, spc, n, dids, vmin, dt, dy, ds, dst);
     std::vector<int> hs(n);
     e = cudaGetLastError();
     if (!e) e = cudaMemcpyAsync(out->t, dt, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);

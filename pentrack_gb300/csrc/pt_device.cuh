@@ -238,6 +238,11 @@ struct DSourceSpec {
     double rmin, rmax, phimin, phimax, zmin, zmax;
     double emin, emax, polarization, tmin, tmax;
     double thetamin, thetamax, phimin_v, phimax_v;
+    double enormal;
+    /* surface sources: the candidate triangles (9 doubles each, the scene's
+     * order) and their cumulative areas */
+    const double *surf_tri, *surf_cum;
+    int n_surf, pad;
 };
 
 /* device event counters (one set per launch, summed with atomics per block) */

@@ -24,6 +24,8 @@ constexpr uint64_t SRC_ROUND = 16;       /* counters per proposal round */
 constexpr uint64_t SRC_H = 1ull << 20;   /* total-energy rounds */
 constexpr uint64_t SRC_PS = 1ull << 22;  /* phase-space rounds: time, polarisation, acceptance */
 constexpr int SRC_STL_ROUNDS = 10000;    /* bounding-box proposals per STL point */
+constexpr uint64_t SRC_SURF = 3000;      /* surface points: triangle, two barycentric draws per round */
+constexpr double REFLECT_TOLERANCE = 1e-8; /* include/trianglemesh.h:39 */
 
 __device__ __forceinline__ double sdraw(uint64_t seed, int64_t id, uint64_t k) { return uniform(seed, id, SRC_STREAM + k); }
 
@@ -101,7 +103,94 @@ __device__ double speed_of(double E, double m) {
     return PT_C0 * sqrt(beta2);
 }
 
+/* InSourceVolume of TCylindricalSurfaceSource: its r, phi, z ranges
+ * (include/source.h:279-283, open bounds) */
+__device__ bool in_surface_region(const DSourceSpec &Q, const double p[3]) {
+    const double r = sqrt(p[0] * p[0] + p[1] * p[1]);
+    const double ph = atan2(p[1], p[0]);
+    return r > Q.rmin && r < Q.rmax && ph > Q.phimin && ph < Q.phimax && p[2] > Q.zmin && p[2] < Q.zmax;
+}
+
 } // namespace
+
+/* TSurfaceSource::CreateParticle (src/source.cpp:102-131) with
+ * TTriangleMesh::RandomPointOnSurface (include/trianglemesh.h:210-232): a
+ * candidate triangle by area (the first whose cumulative area exceeds u times
+ * the total), a uniform point on it (barycentric draws folded back into the
+ * triangle), redrawn until inside the region; then 1e-8 m off the surface
+ * along the unit face normal, a cos(theta) sin(theta) direction about the
+ * normal (its normal energy raised by enormal), the polarisation, kinetic
+ * energy and start time from the particle's draws 3, 4 and 7 */
+__global__ void k_source_surface(const __grid_constant__ DScene S, const __grid_constant__ DSourceSpec Q, DSpecies sp, int64_t n,
+                                 const int64_t *ids, double *t_out, double *y, double *spin, int *status) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t id = ids[i];
+    const uint64_t seed = Q.seed;
+    const double total = Q.surf_cum[Q.n_surf - 1];
+    double p[3] = {0, 0, 0}, nrm[3] = {0, 0, 1};
+    int bad = 1;
+    for (int r = 0; r < Q.max_rounds; ++r) {
+        const uint64_t k = SRC_SURF + (uint64_t)r * SRC_ROUND;
+        const double u = sdraw(seed, id, k) * total;
+        int lo = 0, hi = Q.n_surf; /* upper bound: the first cumulative area > u */
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (Q.surf_cum[mid] > u) hi = mid;
+            else lo = mid + 1;
+        }
+        const int j = lo < Q.n_surf ? lo : Q.n_surf - 1;
+        double a = sdraw(seed, id, k + 1), b = sdraw(seed, id, k + 2);
+        if (a + b > 1) {
+            a = 1 - a;
+            b = 1 - b;
+        }
+        const double *t = Q.surf_tri + 9 * (int64_t)j;
+        double e1[3], e2[3], q[3];
+        for (int c = 0; c < 3; ++c) {
+            e1[c] = t[3 + c] - t[c];
+            e2[c] = t[6 + c] - t[c];
+            q[c] = t[c] + a * e1[c] + b * e2[c];
+        }
+        if (!in_surface_region(Q, q)) continue;
+        double nv[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        const double len = sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+        for (int c = 0; c < 3; ++c) {
+            nrm[c] = nv[c] / len;
+            p[c] = q[c];
+        }
+        bad = 0;
+        break;
+    }
+    for (int c = 0; c < 3; ++c) p[c] = p[c] + nrm[c] * REFLECT_TOLERANCE;
+    double E = Q.emin + sdraw(seed, id, 4) * (Q.emax - Q.emin);
+    double ph = 2.0 * PT_PI * sdraw(seed, id, 5);
+    double th = acos(sqrt(1.0 - sdraw(seed, id, 6)));
+    if (Q.enormal > 0) {
+        const double vn = sqrt(E * cos(th) * cos(th) + Q.enormal);
+        const double vt = sqrt(E) * sin(th);
+        th = atan2(vt, vn);
+        E = vn * vn + vt * vt;
+    }
+    double v[3] = {cos(ph) * sin(th), sin(ph) * sin(th), cos(th)};
+    ptd::Lane::rotate_vector(v, nrm, nullptr);
+    ph = atan2(v[1], v[0]);
+    th = acos(fmin(fmax(v[2], -1.0), 1.0));
+    const double pol = sdraw(seed, id, 3) < 0.5 * (Q.polarization + 1) ? 1.0 : -1.0;
+    const double speed = speed_of(E, sp.m);
+    t_out[i] = Q.tmin + sdraw(seed, id, 7) * (Q.tmax - Q.tmin);
+    y[0 * n + i] = p[0];
+    y[1 * n + i] = p[1];
+    y[2 * n + i] = p[2];
+    y[3 * n + i] = speed * cos(ph) * sin(th);
+    y[4 * n + i] = speed * sin(ph) * sin(th);
+    y[5 * n + i] = speed * cos(th);
+    y[6 * n + i] = 0;
+    y[7 * n + i] = pol;
+    y[8 * n + i] = 0;
+    for (int c = 0; c < 5; ++c) spin[c * n + i] = 0;
+    status[i] = bad;
+}
 
 /* FindPotentialMinimum (src/source.cpp:136-156): the rest potential at the
  * fixed sample points (ids 2^62 + k, k < n, start time and polarisation from

@@ -64,5 +64,7 @@ __global__ void k_point_solids(const __grid_constant__ DScene S, int64_t n, cons
 __global__ void k_source_vmin(const __grid_constant__ DScene S, const __grid_constant__ DSourceSpec Q, DSpecies sp, int64_t n, double *v);
 __global__ void k_source(const __grid_constant__ DScene S, const __grid_constant__ DSourceSpec Q, DSpecies sp, int64_t n, const int64_t *ids,
                          double vmin, double *t_out, double *y, double *spin, int *status);
+__global__ void k_source_surface(const __grid_constant__ DScene S, const __grid_constant__ DSourceSpec Q, DSpecies sp, int64_t n,
+                                 const int64_t *ids, double *t_out, double *y, double *spin, int *status);
 
 } // namespace ptk
