@@ -67,8 +67,9 @@ enum {
     PT_FIELD_TAB3D = 1,     /* OPERA3D / 3Dtable / COMSOL: TabField3, tricubic  (src/field_3d.cpp:417-529) */
     PT_FIELD_HARMONIC = 2,  /* HarmonicExpansionBField, l <= 5        (src/harmonicfields.cpp:50-829) */
     PT_FIELD_UNIFORM_E = 3, /* EDMStaticEField                        (src/edmfields.cpp:181-187) */
-    PT_FIELD_SOLENOID = 4   /* finite ideal solenoid along z, closed form (no reference counterpart:
+    PT_FIELD_SOLENOID = 4,  /* finite ideal solenoid along z, closed form (no reference counterpart:
                                the reference approximates it with Conductor segments, src/conductor.cpp) */
+    PT_FIELD_TAB2D = 5      /* OPERA2D / 2Dtable: TabField, bicubic in (r, z)  (src/field_2d.cpp:232-399) */
 };
 
 /* scheduling form of the tracking kernels */
@@ -133,6 +134,12 @@ typedef struct pt_field {
     /* PT_FIELD_SOLENOID: centre = offset, radius [m], half length [m] and the
      * field at the centre [T] of a sheet current on the cylinder */
     double sol_radius, sol_half_length, sol_bcenter;
+    /* PT_FIELD_TAB2D (rotationally symmetric about z): nx radii r >= 0 in x,
+     * nz heights in z (ny, y unused), samples [ir][iz] (iz fastest) in bx
+     * (B_r), by (B_phi), bz (B_z), v (V) and in er, ephi, ez (E_r, E_phi,
+     * E_z, which take precedence over v as in src/field_2d.cpp:262-283);
+     * NULL = column absent */
+    const double *er, *ephi, *ez;
 } pt_field;
 
 typedef struct pt_scene_desc {
@@ -312,7 +319,9 @@ pt_status pt_log_read(pt_ctx *ctx, int32_t kind, int64_t cap, double *rec, int64
 void pt_batch_destroy(pt_batch *batch);
 
 /* Field of the whole scene at n points (x,y,z,t interleaved, 4n doubles):
- * TFieldManager::BField with gradient and EField.  Any output may be NULL. */
+ * TFieldManager::BField and EField.  Any output may be NULL; B is evaluated
+ * with its gradient when dB is given and without (the value-only path, e.g.
+ * spline2dcalc for 2D tables) when dB is NULL. */
 pt_status pt_field_eval(pt_ctx *ctx, int64_t n, const double *xyzt, int32_t precision,
                         double *B, double *dBidxj, double *V, double *E);
 

@@ -265,11 +265,211 @@ struct Tab3 {
     }
 };
 
+/* ------------------------------------------------------------------ */
+/* TabField (src/field_2d.cpp:232-399): ALGLIB bicubic spline2d in (r, z),
+ * restated from alglib-3.15.0/cpp/src/interpolation.cpp:
+ *   spline2dbuildbicubicv / spline2d_bicubiccalcderivatives (44925-45080,
+ *   46791-46880): d/dr along every z row, d/dz along every r column, d2/drdz
+ *   along the rows of d/dz, each from spline1dbuildcubic with parabolically
+ *   terminated ends (the derivatives of spline_derivs) read back with
+ *   spline1ddiff at the nodes (spline1dbuildhermite 23642-23710, spline1ddiff
+ *   23914-23975: every node but the first takes the left piece's derivative
+ *   at its right end);
+ *   spline2dcalc (43381-43537) and spline2ddiff (43538-43700): the cell
+ *   l with x[l] < v <= x[l+1] by bisection, the Hermite basis scaled by the
+ *   cell widths, the 16 products summed in the library's order.            */
+/* ------------------------------------------------------------------ */
+struct Tab2 {
+    std::vector<double> r, z;            /* axes (ALGLIB's x and y) */
+    std::vector<double> t[7];            /* Br, Bphi, Bz, V, Er, Ephi, Ez: 4 tables f, fx, fy, fxy of nr*nz each, [iz][ir] */
+    double r_lo = 0, r_hi = 0, z_lo = 0, z_hi = 0;
+
+    /* spline1ddiff of spline1dbuildcubic(x, y) at every node */
+    static void node_slopes(int n, const double *x, const double *y, double *ds) {
+        std::vector<double> d(n);
+        spline_derivs(n, x, y, d.data());
+        ds[0] = d[0];
+        for (int j = 1; j < n; ++j) {
+            const double delta = x[j] - x[j - 1], delta2 = delta * delta, delta3 = delta * delta2;
+            const double c1 = d[j - 1];
+            const double c2 = (3 * (y[j] - y[j - 1]) - 2 * d[j - 1] * delta - d[j] * delta) / delta2;
+            const double c3 = (2 * (y[j - 1] - y[j]) + d[j - 1] * delta + d[j] * delta) / delta3;
+            const double u = x[j] - x[j - 1];
+            ds[j] = c1 + 2 * u * c2 + 3 * (u * u) * c3;
+        }
+    }
+
+    void build_one(const double *src /* [ir][iz] */, std::vector<double> &out) const {
+        const int m = (int)r.size(), n = (int)z.size();
+        out.assign((size_t)4 * m * n, 0.0);
+        double *F = out.data(), *DX = F + (size_t)m * n, *DY = DX + (size_t)m * n, *DXY = DY + (size_t)m * n;
+        for (int ir = 0; ir < m; ++ir)
+            for (int iz = 0; iz < n; ++iz) F[(size_t)iz * m + ir] = src[(size_t)ir * n + iz];
+        std::vector<double> row(std::max(m, n)), ds(std::max(m, n));
+        for (int iz = 0; iz < n; ++iz) { /* dF/dr */
+            for (int ir = 0; ir < m; ++ir) row[ir] = F[(size_t)iz * m + ir];
+            node_slopes(m, r.data(), row.data(), ds.data());
+            for (int ir = 0; ir < m; ++ir) DX[(size_t)iz * m + ir] = ds[ir];
+        }
+        for (int ir = 0; ir < m; ++ir) { /* dF/dz */
+            for (int iz = 0; iz < n; ++iz) row[iz] = F[(size_t)iz * m + ir];
+            node_slopes(n, z.data(), row.data(), ds.data());
+            for (int iz = 0; iz < n; ++iz) DY[(size_t)iz * m + ir] = ds[iz];
+        }
+        for (int iz = 0; iz < n; ++iz) { /* d2F/drdz */
+            for (int ir = 0; ir < m; ++ir) row[ir] = DY[(size_t)iz * m + ir];
+            node_slopes(m, r.data(), row.data(), ds.data());
+            for (int ir = 0; ir < m; ++ir) DXY[(size_t)iz * m + ir] = ds[ir];
+        }
+    }
+
+    void build(const pt_field &f) {
+        r.assign(f.x, f.x + f.nx);
+        z.assign(f.z, f.z + f.nz);
+        const double *src[7] = {f.bx, f.by, f.bz, f.v, f.er, f.ephi, f.ez};
+        const bool etab = f.er || f.ephi || f.ez; /* an E map replaces the potential (src/field_2d.cpp:262-283) */
+        for (int c = 0; c < 7; ++c)
+            if (src[c] && !(c == 3 && etab)) build_one(src[c], t[c]);
+        /* TabField::CheckTab (src/field_2d.cpp:193-200) and the range of BField/EField */
+        const double rdist = r[1] - r[0], zdist = z[1] - z[0];
+        r_lo = r[0];
+        z_lo = z[0];
+        r_hi = r_lo + rdist * (double)(f.nx - 1);
+        z_hi = z_lo + zdist * (double)(f.nz - 1);
+    }
+    bool in_range(double rr, double zz) const { return rr >= r_lo && rr < r_hi && zz >= z_lo && zz < z_hi; }
+    bool has(int c) const { return !t[c].empty(); }
+
+    static int cell(const std::vector<double> &ax, double v) {
+        int l = 0, h = (int)ax.size() - 1;
+        while (l != h - 1) {
+            const int k = (l + h) / 2;
+            if (ax[k] >= v) h = k;
+            else l = k;
+        }
+        return l;
+    }
+
+    /* spline2dcalc */
+    double calc(int c, double x, double y) const {
+        const int m = (int)r.size(), n = (int)z.size();
+        const int ix = cell(r, x), iy = cell(z, y);
+        const double dt = 1.0 / (r[ix + 1] - r[ix]), t_ = (x - r[ix]) * dt;
+        const double du = 1.0 / (z[iy + 1] - z[iy]), u = (y - z[iy]) * du;
+        const double *F = t[c].data();
+        const size_t sfx = (size_t)m * n, sfy = 2 * sfx, sfxy = 3 * sfx;
+        const size_t s1 = (size_t)m * iy + ix, s2 = s1 + 1, s3 = (size_t)m * (iy + 1) + ix, s4 = s3 + 1;
+        const double t2 = t_ * t_, t3 = t_ * t2, u2 = u * u, u3 = u * u2;
+        double ht00 = 2 * t3 - 3 * t2 + 1, ht10 = t3 - 2 * t2 + t_, ht01 = -2 * t3 + 3 * t2, ht11 = t3 - t2;
+        double hu00 = 2 * u3 - 3 * u2 + 1, hu10 = u3 - 2 * u2 + u, hu01 = -2 * u3 + 3 * u2, hu11 = u3 - u2;
+        ht10 = ht10 / dt; ht11 = ht11 / dt; hu10 = hu10 / du; hu11 = hu11 / du;
+        double v = 0;
+        v = v + F[s1] * ht00 * hu00 + F[s2] * ht01 * hu00 + F[s3] * ht00 * hu01 + F[s4] * ht01 * hu01;
+        v = v + F[sfx + s1] * ht10 * hu00 + F[sfx + s2] * ht11 * hu00 + F[sfx + s3] * ht10 * hu01 + F[sfx + s4] * ht11 * hu01;
+        v = v + F[sfy + s1] * ht00 * hu10 + F[sfy + s2] * ht01 * hu10 + F[sfy + s3] * ht00 * hu11 + F[sfy + s4] * ht01 * hu11;
+        v = v + F[sfxy + s1] * ht10 * hu10 + F[sfxy + s2] * ht11 * hu10 + F[sfxy + s3] * ht10 * hu11 + F[sfxy + s4] * ht11 * hu11;
+        return v;
+    }
+
+    /* spline2ddiff: value, d/dr, d/dz (d2/drdz is not used by TabField) */
+    void diff(int c, double x, double y, double &f, double &fx, double &fy) const {
+        const int m = (int)r.size(), n = (int)z.size();
+        const int ix = cell(r, x), iy = cell(z, y);
+        const double t_ = (x - r[ix]) / (r[ix + 1] - r[ix]), dt = 1.0 / (r[ix + 1] - r[ix]);
+        const double u = (y - z[iy]) / (z[iy + 1] - z[iy]), du = 1.0 / (z[iy + 1] - z[iy]);
+        const double *F = t[c].data();
+        const size_t sfx = (size_t)m * n, sfy = 2 * sfx, sfxy = 3 * sfx;
+        const size_t s1 = (size_t)m * iy + ix, s2 = s1 + 1, s3 = (size_t)m * (iy + 1) + ix, s4 = s3 + 1;
+        const double t2 = t_ * t_, t3 = t_ * t2, u2 = u * u, u3 = u * u2;
+        double ht00 = 2 * t3 - 3 * t2 + 1, ht10 = t3 - 2 * t2 + t_, ht01 = -2 * t3 + 3 * t2, ht11 = t3 - t2;
+        double hu00 = 2 * u3 - 3 * u2 + 1, hu10 = u3 - 2 * u2 + u, hu01 = -2 * u3 + 3 * u2, hu11 = u3 - u2;
+        ht10 = ht10 / dt; ht11 = ht11 / dt; hu10 = hu10 / du; hu11 = hu11 / du;
+        double dht00 = 6 * t2 - 6 * t_, dht10 = 3 * t2 - 4 * t_ + 1, dht01 = -6 * t2 + 6 * t_, dht11 = 3 * t2 - 2 * t_;
+        double dhu00 = 6 * u2 - 6 * u, dhu10 = 3 * u2 - 4 * u + 1, dhu01 = -6 * u2 + 6 * u, dhu11 = 3 * u2 - 2 * u;
+        dht00 = dht00 * dt; dht01 = dht01 * dt; dhu00 = dhu00 * du; dhu01 = dhu01 * du;
+        f = fx = fy = 0;
+        const size_t blk[4] = {0, sfx, sfy, sfxy};
+        for (int b = 0; b < 4; ++b) {
+            const double v0 = F[blk[b] + s1], v1 = F[blk[b] + s2], v2 = F[blk[b] + s3], v3 = F[blk[b] + s4];
+            const double p0 = (b & 1) ? ht10 : ht00, p1 = (b & 1) ? ht11 : ht01;    /* x data: value or slope */
+            const double q0 = (b & 2) ? hu10 : hu00, q1 = (b & 2) ? hu11 : hu01;
+            const double dp0 = (b & 1) ? dht10 : dht00, dp1 = (b & 1) ? dht11 : dht01;
+            const double dq0 = (b & 2) ? dhu10 : dhu00, dq1 = (b & 2) ? dhu11 : dhu01;
+            f = f + v0 * p0 * q0 + v1 * p1 * q0 + v2 * p0 * q1 + v3 * p1 * q1;
+            fx = fx + v0 * dp0 * q0 + v1 * dp1 * q0 + v2 * dp0 * q1 + v3 * dp1 * q1;
+            fy = fy + v0 * p0 * dq0 + v1 * p1 * dq0 + v2 * p0 * dq1 + v3 * p1 * dq1;
+        }
+    }
+
+    /* cos(phi), sin(phi) of phi = atan2(y, x), formed as x/r and y/r (equal up to
+     * rounding, (1, 0) on the axis where atan2(0, 0) = 0) */
+    static void axis_angle(double x, double y, double rr, double &cp, double &sp) {
+        if (rr > 0) { cp = x / rr; sp = y / rr; }
+        else { cp = 1.0; sp = 0.0; }
+    }
+
+    /* TabField::BField (src/field_2d.cpp:289-335) */
+    void bfield(double x, double y, double zz, double B[3], double dB[3][3]) const {
+        const double rr = sqrt(x * x + y * y);
+        if (!in_range(rr, zz)) return;
+        double cp, sp;
+        axis_angle(x, y, rr, cp, sp);
+        double Br = 0, Bphi = 0, Bz = 0;
+        if (dB) {
+            double dBrdr = 0, dBrdz = 0, dBphidr = 0, dBphidz = 0, dBzdr = 0, dBzdz = 0;
+            if (has(0)) diff(0, rr, zz, Br, dBrdr, dBrdz);
+            if (has(1)) diff(1, rr, zz, Bphi, dBphidr, dBphidz);
+            if (rr > 0) {
+                dB[0][0] = dBrdr * cp * cp - dBphidr * cp * sp + (Br * sp * sp + Bphi * cp * sp) / rr;
+                dB[0][1] = dBrdr * cp * sp - dBphidr * sp * sp - (Br * cp * sp + Bphi * cp * cp) / rr;
+                dB[1][0] = dBrdr * cp * sp + dBphidr * cp * cp - (Br * cp * sp - Bphi * sp * sp) / rr;
+                dB[1][1] = dBrdr * sp * sp + dBphidr * cp * sp + (Br * cp * cp - Bphi * cp * sp) / rr;
+            }
+            dB[0][2] = dBrdz * cp - dBphidz * sp;
+            dB[1][2] = dBrdz * sp + dBphidz * cp;
+            if (has(2)) {
+                diff(2, rr, zz, Bz, dBzdr, dBzdz);
+                dB[2][0] = dBzdr * cp;
+                dB[2][1] = dBzdr * sp;
+                dB[2][2] = dBzdz;
+            }
+        } else {
+            if (has(0)) Br = calc(0, rr, zz);
+            if (has(1)) Bphi = calc(1, rr, zz);
+            if (has(2)) Bz = calc(2, rr, zz);
+        }
+        B[0] = Br * cp - Bphi * sp;
+        B[1] = Br * sp + Bphi * cp;
+        B[2] = Bz;
+    }
+
+    /* TabField::EField (src/field_2d.cpp:337-399) */
+    void efield(double x, double y, double zz, double &V, double E[3]) const {
+        const double rr = sqrt(x * x + y * y);
+        if (!in_range(rr, zz)) return;
+        double cp, sp;
+        axis_angle(x, y, rr, cp, sp);
+        if (has(4) || has(5) || has(6)) {
+            const double Er = has(4) ? calc(4, rr, zz) : 0.0, Ephi = has(5) ? calc(5, rr, zz) : 0.0;
+            E[0] = Er * cp - Ephi * sp;
+            E[1] = Er * sp + Ephi * cp;
+            E[2] = has(6) ? calc(6, rr, zz) : 0.0;
+        } else if (has(3)) {
+            double dVdr, dVdz;
+            diff(3, rr, zz, V, dVdr, dVdz);
+            E[0] = -dVdr * cp;
+            E[1] = -dVdr * sp;
+            E[2] = -dVdz;
+        }
+    }
+};
+
 struct Field {
     int type = 0;
     double bscale = 1, escale = 1;
     double xmax = 0, xmin = 0, ymax = 0, ymin = 0, zmax = 0, zmin = 0, bw = 0;
     Tab3 tab;
+    Tab2 tab2;
     double e[3] = {0, 0, 0};
     /* HarmonicExpandedBField (src/harmonicfields.cpp:50-829): (l, m, G) terms and offset */
     std::vector<int> hl, hm;
@@ -321,6 +521,8 @@ struct Field {
         if (!in_bounds(x, y, z) || bscale == 0.) return;
         if (type == PT_FIELD_TAB3D) {
             for (int i = 0; i < 3; ++i) tab.interpolate(x, y, z, tab.coeff[i], B[i], dB ? dB[i] : nullptr);
+        } else if (type == PT_FIELD_TAB2D) {
+            tab2.bfield(x, y, z, B, dB);
         } else if (type == PT_FIELD_SOLENOID) {
             pts_solenoid_field(sol_a, sol_b, sol_B0, x - offset[0], y - offset[1], z - offset[2], B, dB);
         } else if (type == PT_FIELD_HARMONIC) {
@@ -350,6 +552,8 @@ struct Field {
             double dV[3] = {0, 0, 0};
             tab.interpolate(x, y, z, tab.coeff[3], V, dV);
             for (int i = 0; i < 3; ++i) E[i] = -dV[i];
+        } else if (type == PT_FIELD_TAB2D) {
+            tab2.efield(x, y, z, V, E);
         } else {
             return;
         }
@@ -1425,6 +1629,10 @@ int pto_create(const pt_scene_desc *d, pto_ctx **out) {
             F.xmax = f.xmax; F.xmin = f.xmin; F.ymax = f.ymax; F.ymin = f.ymin; F.zmax = f.zmax; F.zmin = f.zmin;
             F.bw = f.boundary_width;
             if (f.type == PT_FIELD_TAB3D) F.tab.build(f);
+            else if (f.type == PT_FIELD_TAB2D) {
+                if (f.nx < 2 || f.nz < 2 || !f.x || !f.z) throw std::runtime_error("2D table needs at least 2 points per axis");
+                F.tab2.build(f);
+            }
             else if (f.type == PT_FIELD_UNIFORM_E) { F.e[0] = f.e[0]; F.e[1] = f.e[1]; F.e[2] = f.e[2]; }
             else if (f.type == PT_FIELD_HARMONIC) {
                 for (int k = 0; k < f.n_coeff; ++k) {
@@ -1523,7 +1731,7 @@ int pto_field(pto_ctx *ctx, int64_t n, const double *xyzt, double *B, double *dB
     for (int64_t i = 0; i < n; ++i) {
         const double *q = xyzt + 4 * i;
         double b[3], db[3][3], v, e[3];
-        tr.bfield(q[0], q[1], q[2], q[3], b, db);
+        tr.bfield(q[0], q[1], q[2], q[3], b, dB ? db : nullptr);
         tr.efield(q[0], q[1], q[2], q[3], v, e);
         if (B) for (int k = 0; k < 3; ++k) B[3 * i + k] = b[k];
         if (dB) for (int k = 0; k < 9; ++k) dB[9 * i + k] = db[k / 3][k % 3];

@@ -60,6 +60,8 @@ def ref_lib():
         R.ref_tricubic_coeff.argtypes = [A.c_double_p, A.c_double_p]
         R.ref_tricubic_eval.argtypes = [A.c_double_p, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int]
         R.ref_tricubic_eval.restype = C.c_double
+        R.ref_spline2d.argtypes = [C.c_int, A.c_double_p, C.c_int, A.c_double_p, A.c_double_p, C.c_int, A.c_double_p,
+                                   A.c_double_p, A.c_double_p]
         _REF = R
     return _REF
 
@@ -102,11 +104,12 @@ class Oracle:
         order = np.lexsort((rec[:, 1], rec[:, 0])) if n else np.arange(0)
         return rec[order]
 
-    def field(self, xyzt):
+    def field(self, xyzt, grad=True):
         q = np.ascontiguousarray(xyzt, dtype=np.float64).reshape(-1, 4)
         n = len(q)
-        B, dB, V, E = np.zeros((n, 3)), np.zeros((n, 3, 3)), np.zeros(n), np.zeros((n, 3))
-        lib().pto_field(self.h, n, _dp(q), _dp(B), _dp(dB), _dp(V), _dp(E))
+        B, V, E = np.zeros((n, 3)), np.zeros(n), np.zeros((n, 3))
+        dB = np.zeros((n, 3, 3)) if grad else None
+        lib().pto_field(self.h, n, _dp(q), _dp(B), _dp(dB) if grad else None, _dp(V), _dp(E))
         return B, dB, V, E
 
     def collisions(self, segs, max_hits=8):

@@ -5,8 +5,9 @@
  * Built by `make -C oracle ref` into oracle/_ref/libptref.so, compiling the
  * sources where they lie in the reference tree.  Used only to pin the
  * oracle's restatements (spline derivatives of TabField3::CalcDerivs,
- * src/field_3d.cpp:336-364, and tricubic_get_coeff of TabField3::PreInterpol,
- * src/field_3d.cpp:367-414) and to generate tests/golden fixtures.
+ * src/field_3d.cpp:336-364, tricubic_get_coeff of TabField3::PreInterpol,
+ * src/field_3d.cpp:367-414, and the bicubic spline2d of TabField,
+ * src/field_2d.cpp:232-399) and to generate tests/golden fixtures.
  */
 #include "interpolation.h"
 #include "tricubic.h"
@@ -39,5 +40,32 @@ void ref_tricubic_coeff(const double *x64, double *a64) {
 /* libtricubic's own evaluator (value and partial derivatives) */
 double ref_tricubic_eval(double *a64, double x, double y, double z, int derx, int dery, int derz) {
     return tricubic_eval(a64, x, y, z, derx, dery, derz);
+}
+
+/* TabField's spline: spline2dbuildbicubicv(x, m, y, n, f, 1) on f[iy*m + ix]
+ * (src/field_2d.cpp:247), then at each of np points spline2ddiff (out[5k..5k+3]
+ * = f, df/dx, df/dy, d2f/dxdy) and spline2dcalc (out[5k+4]) */
+int ref_spline2d(int m, const double *x, int n, const double *y, const double *f, int np, const double *px,
+                 const double *py, double *out) {
+    try {
+        alglib::real_1d_array xa, ya, fa;
+        xa.setcontent(m, x);
+        ya.setcontent(n, y);
+        fa.setcontent((alglib::ae_int_t)m * n, f);
+        alglib::spline2dinterpolant c;
+        alglib::spline2dbuildbicubicv(xa, m, ya, n, fa, 1, c);
+        for (int k = 0; k < np; ++k) {
+            double v, dx, dy, dxy;
+            alglib::spline2ddiff(c, px[k], py[k], v, dx, dy, dxy);
+            out[5 * k + 0] = v;
+            out[5 * k + 1] = dx;
+            out[5 * k + 2] = dy;
+            out[5 * k + 3] = dxy;
+            out[5 * k + 4] = alglib::spline2dcalc(c, px[k], py[k]);
+        }
+        return 0;
+    } catch (...) {
+        return -1;
+    }
 }
 }

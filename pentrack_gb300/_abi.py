@@ -20,7 +20,7 @@ ID_INITIAL_NOT_FOUND, ID_CGAL_ERROR, ID_GEOMETRY_ERROR = -5, -6, -7
 ID_ABSORBED_IN_MATERIAL, ID_ABSORBED_ON_SURFACE = 1, 2
 
 NEUTRON, PROTON, ELECTRON = 0, 1, 2
-FIELD_TAB3D, FIELD_HARMONIC, FIELD_UNIFORM_E, FIELD_SOLENOID = 1, 2, 3, 4
+FIELD_TAB3D, FIELD_HARMONIC, FIELD_UNIFORM_E, FIELD_SOLENOID, FIELD_TAB2D = 1, 2, 3, 4, 5
 MODE_PLAIN, MODE_BATCHED, MODE_PHASED = 0, 1, 2
 PREC_FP64, PREC_FP32 = 0, 1
 SCHED_AUTO, SCHED_PHASED, SCHED_PERSISTENT, SCHED_PERSISTENT_WIDE, SCHED_PHASED_WIDE = 0, 1, 2, 3, 4
@@ -50,6 +50,7 @@ class Field(C.Structure):
         ("l", c_int32_p), ("m", c_int32_p), ("g", c_double_p),
         ("e", C.c_double * 3),
         ("sol_radius", C.c_double), ("sol_half_length", C.c_double), ("sol_bcenter", C.c_double),
+        ("er", c_double_p), ("ephi", c_double_p), ("ez", c_double_p),
     ]
 
 

@@ -381,6 +381,45 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
                 o.a0f[a] = (float)o.a0[a];
                 o.inv_hf[a] = (float)o.inv_h[a];
             }
+        } else if (f.type == PT_FIELD_TAB2D) {
+            if (f.nx < 2 || f.nz < 2 || !f.x || !f.z) { err = "2D table needs at least 2 points per axis"; return PT_ERR_INVALID; }
+            std::vector<double> ax[2] = {std::vector<double>(f.x, f.x + f.nx), std::vector<double>(f.z, f.z + f.nz)};
+            for (int a = 0; a < 2; ++a)
+                for (size_t k = 1; k < ax[a].size(); ++k)
+                    if (!(ax[a][k] > ax[a][k - 1])) { err = "2D table axes must be strictly increasing"; return PT_ERR_INVALID; }
+            /* an E map makes TabField ignore the potential (src/field_2d.cpp:262-283) */
+            const bool etab = f.er || f.ephi || f.ez;
+            const double *comp[PT_T2_NCOMP] = {f.bx, f.by, f.bz, etab ? nullptr : f.v, f.er, f.ephi, f.ez};
+            const size_t tot = (size_t)f.nx * f.nz;
+            std::vector<double> nd(tot * PT_T2_NCOMP * 4, 0.0);
+            o.t2_mask = 0;
+            for (int k = 0; k < PT_T2_NCOMP; ++k)
+                if (comp[k]) {
+                    pth::bicubic_nodes(ax[0], ax[1], comp[k], k, PT_T2_NCOMP * 4, nd);
+                    o.t2_mask |= 1 << k;
+                }
+            o.has_b = (o.t2_mask & 7) ? 1 : 0;
+            o.has_v = (o.t2_mask & 0x78) ? 1 : 0;
+            o.node64 = dupload(c->allocs, nd.data(), nd.size(), e);
+            if (e) return ck(c, e, "upload 2D table"), PT_ERR_CUDA;
+            /* TabField::CheckTab's grid origin and first spacing give the
+             * range r_lo <= r < r_lo + dr (nr - 1), likewise in z (src/field_2d.cpp:193-200, 291) */
+            const double rdist = ax[0][1] - ax[0][0], zdist = ax[1][1] - ax[1][0];
+            const double rspan = rdist * (double)(f.nx - 1), zspan = zdist * (double)(f.nz - 1);
+            o.t2_lim[0] = ax[0][0];
+            o.t2_lim[1] = ax[0][0] + rspan;
+            o.t2_lim[2] = ax[1][0];
+            o.t2_lim[3] = ax[1][0] + zspan;
+            const int axis[2] = {0, 2};
+            for (int a = 0; a < 2; ++a) {
+                const int k = axis[a];
+                o.n[k] = (int)ax[a].size();
+                o.ax[k] = dupload(c->allocs, ax[a].data(), ax[a].size(), e);
+                if (e) return ck(c, e, "upload 2D axis"), PT_ERR_CUDA;
+                o.a0[k] = ax[a][0];
+                o.inv_h[k] = (double)(ax[a].size() - 1) / (ax[a].back() - ax[a][0]);
+            }
+            o.n[1] = 1;
         } else if (f.type == PT_FIELD_HARMONIC) {
             std::vector<double> coef;
             std::vector<int> expo;
@@ -1416,7 +1455,7 @@ pt_status pt_field_eval(pt_ctx *c, int64_t n, const double *xyzt, int32_t prec, 
     double *dB_ = dalloc<double>(tmp, 3 * n, e), *ddB = dalloc<double>(tmp, 9 * n, e), *dV = dalloc<double>(tmp, n, e),
            *dE = dalloc<double>(tmp, 3 * n, e);
     if (e) { free_list(tmp); return ck(c, e, "field eval alloc"), PT_ERR_OOM; }
-    k_field<<<grid_for(n, 128), 128, 0, c->stream>>>(c->scene, prec, n, dq, dB_, ddB, dV, dE);
+    k_field<<<grid_for(n, 128), 128, 0, c->stream>>>(c->scene, prec, n, dq, dB_, dB ? ddB : nullptr, dV, dE);
     e = cudaGetLastError();
     if (!e && B) e = cudaMemcpyAsync(B, dB_, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     if (!e && dB) e = cudaMemcpyAsync(dB, ddB, 9 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);

@@ -20,6 +20,7 @@
 #define PT_MAX_STACK 8        /* entries of the current-solids list (the reference's vector is unbounded) */
 #define PT_MAX_COLLS 8        /* collisions of one segment kept for DoHit */
 #define PT_MAX_FIELDS 8
+#define PT_T2_NCOMP 7       /* components of a 2D table node: B_r, B_phi, B_z, V, E_r, E_phi, E_z */
 #define PT_MAX_SPINTIMES 16
 #define PT_MAX_IGNORE 4       /* ignore intervals per solid */
 #define PT_MAX_SOLIDS 64
@@ -127,6 +128,13 @@ struct DField {
      * n_terms x 3 rows of hp_n coefficients (b_k,x, b_k,y, b_k,z) */
     const double *basis_hp;
     double sol_a, sol_b, sol_B0; /* solenoid radius, half length, mu0 n I / pi */
+    /* 2D table (TabField): r axis in ax[0] / n[0], z axis in ax[2] / n[2];
+     * node64 holds [ir][iz][component][4] = f, df/dr, df/dz, d2f/drdz of
+     * the components B_r, B_phi, B_z, V, E_r, E_phi, E_z (t2_mask bit c set
+     * when component c is tabulated); t2_lim = r_lo, r_hi, z_lo, z_hi of the
+     * half-open range test */
+    int t2_mask, pad5;
+    double t2_lim[4];
 };
 
 struct DScene {

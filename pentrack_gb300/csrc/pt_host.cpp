@@ -209,6 +209,82 @@ bool read_opera3d(const std::string &path, double lengthconv, Table3 &t, std::st
     return true;
 }
 
+bool read_opera2d(const std::string &path, double lengthconv, Table3 &t, std::string &err) {
+    const std::string ext = fs::path(path).extension().string();
+    if (ext == ".gz" || ext == ".bz2") {
+        err = path + ": compressed tables are not supported; decompress the file first";
+        return false;
+    }
+    std::ifstream in(path);
+    if (!in) {
+        err = "Could not open " + path;
+        return false;
+    }
+    long m = 0, one = 0, n = 0;
+    std::string line;
+    if (!std::getline(in, line) || !(std::istringstream(line) >> m >> one >> n) || m < 2 || n < 2) {
+        err = path + ": bad table header";
+        return false;
+    }
+    /* the r line, then " 2 Y [LENGU]" and z or z alone; then the optional
+     * columns in the reference's fixed order, each recognised by substring */
+    std::getline(in, line);
+    std::getline(in, line);
+    const bool skipy = line.compare(0, 12, " 2 Y [LENGU]") != 0;
+    std::getline(in, line);
+    if (!skipy) std::getline(in, line);
+    static const char *tags[7] = {"RBX", "RBY", "RBZ", "EX", "EY", "EZ", "RV"};
+    std::vector<double> *dst[7] = {&t.bx, &t.by, &t.bz, &t.er, &t.ephi, &t.ez, &t.v};
+    std::vector<int> cols;
+    for (int k = 0; k < 7; ++k)
+        if (line.find(tags[k]) != std::string::npos) {
+            cols.push_back(k);
+            dst[k]->assign((size_t)m * n, 0.0);
+            std::getline(in, line);
+        }
+    if (!in || line.compare(0, 2, " 0") != 0) {
+        err = path + " not found or corrupt";
+        return false;
+    }
+    std::vector<double> r((size_t)m), z((size_t)n);
+    std::vector<double> rowv(cols.size());
+    long ri = 0, zi = -1;
+    double rv, yv, zv;
+    while (in >> rv) {
+        if (!skipy && !(in >> yv)) break;
+        if (!(in >> zv)) break;
+        for (size_t c = 0; c < cols.size(); ++c)
+            if (!(in >> rowv[c])) {
+                err = path + ": truncated row";
+                return false;
+            }
+        rv *= lengthconv;
+        zv *= lengthconv;
+        if (zi >= 0 && zv < z[(size_t)zi]) {
+            ++ri;
+            zi = 0;
+        } else {
+            ++zi;
+        }
+        if (ri >= m || zi >= n) {
+            err = path + ": more rows than the header's " + std::to_string(m) + " by " + std::to_string(n);
+            return false;
+        }
+        r[(size_t)ri] = rv;
+        z[(size_t)zi] = zv;
+        for (size_t c = 0; c < cols.size(); ++c) (*dst[cols[c]])[(size_t)ri * n + zi] = rowv[c];
+    }
+    if (ri + 1 != m || zi + 1 != n) {
+        err = "The header says the size is " + std::to_string(m) + " by " + std::to_string(n) + ", actually it is " +
+              std::to_string(ri + 1) + " by " + std::to_string(zi + 1) + "!";
+        return false;
+    }
+    t.ax[0] = r;
+    t.ax[1].clear();
+    t.ax[2] = z;
+    return true;
+}
+
 pt_status load_scene(const std::string &config_path, SceneStore &S, std::string &err) {
     Config cfg;
     if (!read_config(config_path, cfg, err)) return PT_ERR_IO;
@@ -359,6 +435,32 @@ pt_status load_scene(const std::string &config_path, SceneStore &S, std::string 
             f.xmax = t->ax[0].back(); f.xmin = t->ax[0].front();
             f.ymax = t->ax[1].back(); f.ymin = t->ax[1].front();
             f.zmax = t->ax[2].back(); f.zmin = t->ax[2].front();
+            S.tables.push_back(std::move(t));
+        } else if (type == "OPERA2D" || type == "2Dtable") {
+            /* ReadOperaField2 (src/field_2d.cpp:37-66): no box, no smoothing band */
+            std::string file, bs, es;
+            double lconv = 1;
+            if (!(ss >> file >> bs >> es) || (type == "OPERA2D" && !(ss >> lconv))) {
+                err = "Could not read all required parameters for field " + type + "!";
+                return PT_ERR_INVALID;
+            }
+            double b = 0, e = 0;
+            if (!constant_scale(bs, cfg, b, err) || !constant_scale(es, cfg, e, err)) return PT_ERR_UNSUPPORTED;
+            if (type == "2Dtable") { /* centimetres, gauss and volt per centimetre */
+                b *= 0.0001;
+                e *= 100;
+                lconv = 0.01;
+            }
+            auto t = std::make_unique<Table3>();
+            if (!read_opera2d(relative_to(config_path, file).string(), lconv, *t, err)) return PT_ERR_IO;
+            f.type = PT_FIELD_TAB2D;
+            f.b_scale = b;
+            f.e_scale = e;
+            f.nx = (int32_t)t->ax[0].size(); f.ny = 1; f.nz = (int32_t)t->ax[2].size();
+            f.x = t->ax[0].data(); f.z = t->ax[2].data();
+            auto ptr = [](const std::vector<double> &v) { return v.empty() ? nullptr : v.data(); };
+            f.bx = ptr(t->bx); f.by = ptr(t->by); f.bz = ptr(t->bz); f.v = ptr(t->v);
+            f.er = ptr(t->er); f.ephi = ptr(t->ephi); f.ez = ptr(t->ez);
             S.tables.push_back(std::move(t));
         } else if (type == "HarmonicExpansionBField") {
             std::string bs;

@@ -40,8 +40,12 @@ bool read_stl(const std::string &path, std::vector<double> &tris, std::string &e
 struct Table3 {
     std::vector<double> ax[3];
     std::vector<double> bx, by, bz, v;
+    std::vector<double> er, ephi, ez; /* 2D tables only */
 };
 bool read_opera3d(const std::string &path, double lengthconv, Table3 &t, std::string &err);
+/* OPERA2D table (TabField::ReadTabFile, src/field_2d.cpp:68-190) into ax[0] = r,
+ * ax[2] = z and [ir][iz] columns bx = B_r, by = B_phi, bz = B_z, v, er, ephi, ez */
+bool read_opera2d(const std::string &path, double lengthconv, Table3 &t, std::string &err);
 
 /* Owns every array a pt_scene_desc points to. */
 struct SceneStore {

@@ -41,7 +41,8 @@ __global__ void k_field(const __grid_constant__ DScene S, int prec, int64_t n, c
     if (i >= n) return;
     const double *q = xyzt + 4 * i;
     double b[3], db[3][3], v, e[3];
-    bfield<true>(S, prec, q[0], q[1], q[2], b, db);
+    if (dB) bfield<true>(S, prec, q[0], q[1], q[2], b, db);
+    else bfield<false>(S, prec, q[0], q[1], q[2], b, nullptr);
     efield(S, prec, q[0], q[1], q[2], v, e);
     if (B) for (int k = 0; k < 3; ++k) B[3 * i + k] = b[k];
     if (dB) for (int k = 0; k < 9; ++k) dB[9 * i + k] = db[k / 3][k % 3];

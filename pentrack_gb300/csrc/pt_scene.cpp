@@ -189,6 +189,46 @@ void hermite_nodes(const std::vector<double> ax[3], const double *tabp, int comp
         for (int k = 0; k < 8; ++k) out[i * stride + comp * 8 + k] = (*src[k])[i];
 }
 
+/* spline1ddiff of spline1dbuildcubic(x, y) (parabolically terminated) at
+ * every node: the first node's slope is the spline derivative itself, every
+ * other node's is the derivative of the piece on its left at its right end,
+ * from the Hermite coefficients as spline1dbuildhermite forms them */
+static void node_slopes(int n, const double *x, const double *y, double *ds) {
+    std::vector<double> d(n);
+    spline_derivs(n, x, y, d.data());
+    ds[0] = d[0];
+    for (int j = 1; j < n; ++j) {
+        const double w = x[j] - x[j - 1], w2 = w * w, w3 = w * w2;
+        const double c2 = (3 * (y[j] - y[j - 1]) - 2 * d[j - 1] * w - d[j] * w) / w2;
+        const double c3 = (2 * (y[j - 1] - y[j]) + d[j - 1] * w + d[j] * w) / w3;
+        const double u = x[j] - x[j - 1];
+        ds[j] = d[j - 1] + 2 * u * c2 + 3 * (u * u) * c3;
+    }
+}
+
+void bicubic_nodes(const std::vector<double> &r, const std::vector<double> &z, const double *tab, int comp, int stride,
+                   std::vector<double> &out) {
+    const int m = (int)r.size(), n = (int)z.size();
+    std::vector<double> dz((size_t)m * n), line(std::max(m, n)), ds(std::max(m, n));
+    auto at = [&](int ir, int iz) -> double * { return &out[((size_t)ir * n + iz) * stride + comp * 4]; };
+    for (int ir = 0; ir < m; ++ir)
+        for (int iz = 0; iz < n; ++iz) at(ir, iz)[0] = tab[(size_t)ir * n + iz];
+    for (int iz = 0; iz < n; ++iz) { /* d/dr along each z row */
+        for (int ir = 0; ir < m; ++ir) line[ir] = tab[(size_t)ir * n + iz];
+        node_slopes(m, r.data(), line.data(), ds.data());
+        for (int ir = 0; ir < m; ++ir) at(ir, iz)[1] = ds[ir];
+    }
+    for (int ir = 0; ir < m; ++ir) { /* d/dz along each r column */
+        node_slopes(n, z.data(), tab + (size_t)ir * n, ds.data());
+        for (int iz = 0; iz < n; ++iz) { at(ir, iz)[2] = ds[iz]; dz[(size_t)ir * n + iz] = ds[iz]; }
+    }
+    for (int iz = 0; iz < n; ++iz) { /* d2/drdz: d/dr of d/dz along each z row */
+        for (int ir = 0; ir < m; ++ir) line[ir] = dz[(size_t)ir * n + iz];
+        node_slopes(m, r.data(), line.data(), ds.data());
+        for (int ir = 0; ir < m; ++ir) at(ir, iz)[3] = ds[ir];
+    }
+}
+
 int node_table32(const std::vector<double> &nodes, int ncomp, std::vector<float> &out) {
     const int stride = (ncomp * 9 + 3) / 4 * 4;
     const size_t nn = nodes.size() / (size_t)(ncomp * 8);

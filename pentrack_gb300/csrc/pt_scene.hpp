@@ -31,6 +31,15 @@ void spline_derivs(int n, const double *x, const double *y, double *d);
  * (src/field_3d.cpp:374-381).  out[node*stride + comp*8 + k]. */
 void hermite_nodes(const std::vector<double> ax[3], const double *tab, int comp, int stride, std::vector<double> &out);
 
+/* TabField's bicubic spline data (ALGLIB spline2dbuildbicubicv,
+ * alglib-3.15.0/cpp/src/interpolation.cpp:44925-45080 and 46791-46880) of
+ * one [ir][iz] table: per node f, df/dr, df/dz, d2f/drdz, each slope as
+ * spline1ddiff returns it from the parabolically terminated cubic spline
+ * along that axis (d2f/drdz: along r of the d/dz table).
+ * out[(ir*nz + iz)*stride + comp*4 + k]. */
+void bicubic_nodes(const std::vector<double> &r, const std::vector<double> &z, const double *tab, int comp, int stride,
+                   std::vector<double> &out);
+
 /* FP32 node table from per-node Hermite data (stride ncomp*8): per node and
  * component 9 floats -- the value as FP32 high part and FP32 rounding of the
  * rest, then fx, fy, fz, fxy, fxz, fyz, fxyz rounded to FP32 -- with the

@@ -503,6 +503,169 @@ __device__ void tab3_v(const DField &f, int prec, double x, double y, double z, 
     E[2] = -dF[0][2];
 }
 
+/* ---- TabField: ALGLIB's bicubic spline2d in (r, z) (src/field_2d.cpp:232-399) ---- */
+
+/* the cell of spline2dcalc / spline2ddiff's bisection: l in [0, n-2] with
+ * ax[l] < v <= ax[l+1] (l = 0 at the first node), found from the
+ * uniform-grid guess and walked to the same answer */
+__device__ __forceinline__ int cell2(const DField &f, int a, double v) {
+    const double *ax = f.ax[a];
+    const int n = f.n[a];
+    const double g = (v - f.a0[a]) * f.inv_h[a];
+    int l = 0;
+    if (g > 0.0) l = g < (double)(n - 2) ? (int)g : n - 2;
+    while (l > 0 && ax[l] >= v) --l;
+    while (l < n - 2 && ax[l + 1] < v) ++l;
+    return l;
+}
+
+/* Hermite basis of one cell in the library's form and operation order:
+ * ht/hu weigh the value and (scaled by the cell width) slope data, dht/dhu
+ * are their derivatives.  DIFF: spline2ddiff (t = (v - x_l) / w), else
+ * spline2dcalc (t = (v - x_l) * (1 / w)). */
+struct Bic2 {
+    double ht[4], hu[4];   /* h00, h01, h10, h11 */
+    double dht[4], dhu[4];
+    int64_t s1, s2, s3, s4; /* nodes (l_r, l_z), (l_r + 1, l_z), (l_r, l_z + 1), (l_r + 1, l_z + 1) */
+};
+
+template <bool DIFF>
+__device__ __forceinline__ void bic2_basis(double t, double dt, double *h, double *dh) {
+    const double t2 = t * t, t3 = t * t2;
+    h[0] = 2 * t3 - 3 * t2 + 1;
+    h[1] = -2 * t3 + 3 * t2;
+    h[2] = (t3 - 2 * t2 + t) / dt;
+    h[3] = (t3 - t2) / dt;
+    if (DIFF) {
+        dh[0] = (6 * t2 - 6 * t) * dt;
+        dh[1] = (-6 * t2 + 6 * t) * dt;
+        dh[2] = 3 * t2 - 4 * t + 1;
+        dh[3] = 3 * t2 - 2 * t;
+    }
+}
+
+template <bool DIFF>
+__device__ __forceinline__ void bic2_setup(const DField &f, double r, double z, Bic2 &b) {
+    const int lr = cell2(f, 0, r), lz = cell2(f, 2, z);
+    const double *ar = f.ax[0], *az = f.ax[2];
+    double t, dt, u, du;
+    if (DIFF) {
+        t = (r - ar[lr]) / (ar[lr + 1] - ar[lr]);
+        dt = 1.0 / (ar[lr + 1] - ar[lr]);
+        u = (z - az[lz]) / (az[lz + 1] - az[lz]);
+        du = 1.0 / (az[lz + 1] - az[lz]);
+    } else {
+        dt = 1.0 / (ar[lr + 1] - ar[lr]);
+        t = (r - ar[lr]) * dt;
+        du = 1.0 / (az[lz + 1] - az[lz]);
+        u = (z - az[lz]) * du;
+    }
+    bic2_basis<DIFF>(t, dt, b.ht, b.dht);
+    bic2_basis<DIFF>(u, du, b.hu, b.dhu);
+    const int64_t nz = f.n[2];
+    b.s1 = (int64_t)lr * nz + lz;
+    b.s2 = b.s1 + nz;
+    b.s3 = b.s1 + 1;
+    b.s4 = b.s2 + 1;
+}
+
+/* one component: the 16 products in spline2ddiff's order (value, d/dr
+ * data, d/dz data, d2/drdz data); DIFF adds the r and z derivatives */
+template <bool DIFF>
+__device__ __forceinline__ void bic2_eval(const DField &f, const Bic2 &b, int c, double &F, double &Fr, double &Fz) {
+    const double *n1 = f.node64 + b.s1 * (PT_T2_NCOMP * 4) + c * 4, *n2 = f.node64 + b.s2 * (PT_T2_NCOMP * 4) + c * 4,
+                 *n3 = f.node64 + b.s3 * (PT_T2_NCOMP * 4) + c * 4, *n4 = f.node64 + b.s4 * (PT_T2_NCOMP * 4) + c * 4;
+    double v = 0, vr = 0, vz = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        /* data k: 0 value, 1 d/dr, 2 d/dz, 3 d2/drdz; it pairs with the r
+         * basis of slope (k & 1) and the z basis of slope (k >> 1) */
+        const double v0 = n1[k], v1 = n2[k], v2 = n3[k], v3 = n4[k];
+        const int pr = (k & 1) ? 2 : 0, pz = (k & 2) ? 2 : 0;
+        const double p0 = b.ht[pr], p1 = b.ht[pr + 1], q0 = b.hu[pz], q1 = b.hu[pz + 1];
+        v = v + v0 * p0 * q0 + v1 * p1 * q0 + v2 * p0 * q1 + v3 * p1 * q1;
+        if (DIFF) {
+            const double dp0 = b.dht[pr], dp1 = b.dht[pr + 1], dq0 = b.dhu[pz], dq1 = b.dhu[pz + 1];
+            vr = vr + v0 * dp0 * q0 + v1 * dp1 * q0 + v2 * dp0 * q1 + v3 * dp1 * q1;
+            vz = vz + v0 * p0 * dq0 + v1 * p1 * dq0 + v2 * p0 * dq1 + v3 * p1 * dq1;
+        }
+    }
+    F = v;
+    if (DIFF) { Fr = vr; Fz = vz; }
+}
+
+__device__ __forceinline__ bool tab2_in(const DField &f, double r, double z) {
+    return r >= f.t2_lim[0] && r < f.t2_lim[1] && z >= f.t2_lim[2] && z < f.t2_lim[3];
+}
+
+/* cos(phi), sin(phi) of phi = atan2(y, x) as x / r, y / r ((1, 0) on the axis) */
+__device__ __forceinline__ void tab2_angle(double x, double y, double r, double &cp, double &sp) {
+    if (r > 0) { cp = x / r; sp = y / r; }
+    else { cp = 1.0; sp = 0.0; }
+}
+
+/* TabField::BField (src/field_2d.cpp:289-335); outputs untouched outside the range */
+template <bool GRAD>
+__device__ __noinline__ void tab2_b(const DField &f, double x, double y, double z, double B[3], double (*dB)[3]) {
+    const double r = sqrt(x * x + y * y);
+    if (!tab2_in(f, r, z)) return;
+    double cp, sp;
+    tab2_angle(x, y, r, cp, sp);
+    Bic2 b;
+    bic2_setup<GRAD>(f, r, z, b);
+    double Br = 0, Bphi = 0, Bz = 0, dBrdr = 0, dBrdz = 0, dBphidr = 0, dBphidz = 0, dBzdr = 0, dBzdz = 0;
+    if (f.t2_mask & 1) bic2_eval<GRAD>(f, b, 0, Br, dBrdr, dBrdz);
+    if (f.t2_mask & 2) bic2_eval<GRAD>(f, b, 1, Bphi, dBphidr, dBphidz);
+    if (f.t2_mask & 4) bic2_eval<GRAD>(f, b, 2, Bz, dBzdr, dBzdz);
+    if (GRAD) {
+        if (r > 0) {
+            dB[0][0] = dBrdr * cp * cp - dBphidr * cp * sp + (Br * sp * sp + Bphi * cp * sp) / r;
+            dB[0][1] = dBrdr * cp * sp - dBphidr * sp * sp - (Br * cp * sp + Bphi * cp * cp) / r;
+            dB[1][0] = dBrdr * cp * sp + dBphidr * cp * cp - (Br * cp * sp - Bphi * sp * sp) / r;
+            dB[1][1] = dBrdr * sp * sp + dBphidr * cp * sp + (Br * cp * cp - Bphi * cp * sp) / r;
+        }
+        dB[0][2] = dBrdz * cp - dBphidz * sp;
+        dB[1][2] = dBrdz * sp + dBphidz * cp;
+        if (f.t2_mask & 4) {
+            dB[2][0] = dBzdr * cp;
+            dB[2][1] = dBzdr * sp;
+            dB[2][2] = dBzdz;
+        }
+    }
+    B[0] = Br * cp - Bphi * sp;
+    B[1] = Br * sp + Bphi * cp;
+    B[2] = Bz;
+}
+
+/* TabField::EField (src/field_2d.cpp:337-399): an E map (values) takes
+ * precedence over the potential (value and gradient) */
+__device__ __noinline__ void tab2_e(const DField &f, double x, double y, double z, double &V, double E[3]) {
+    const double r = sqrt(x * x + y * y);
+    if (!tab2_in(f, r, z)) return;
+    double cp, sp;
+    tab2_angle(x, y, r, cp, sp);
+    double d0, d1;
+    if (f.t2_mask & 0x70) {
+        Bic2 b;
+        bic2_setup<false>(f, r, z, b);
+        double Er = 0, Ephi = 0, Ez = 0;
+        if (f.t2_mask & 16) bic2_eval<false>(f, b, 4, Er, d0, d1);
+        if (f.t2_mask & 32) bic2_eval<false>(f, b, 5, Ephi, d0, d1);
+        if (f.t2_mask & 64) bic2_eval<false>(f, b, 6, Ez, d0, d1);
+        E[0] = Er * cp - Ephi * sp;
+        E[1] = Er * sp + Ephi * cp;
+        E[2] = Ez;
+    } else if (f.t2_mask & 8) {
+        Bic2 b;
+        bic2_setup<true>(f, r, z, b);
+        double dVdr, dVdz;
+        bic2_eval<true>(f, b, 3, V, dVdr, dVdz);
+        E[0] = -dVdr * cp;
+        E[1] = -dVdr * sp;
+        E[2] = -dVdz;
+    }
+}
+
 /* finite solenoid (include/pt_solenoid.h); one out-of-line copy: its
  * elliptic-integral loops would otherwise be inlined at every field call */
 __device__ __noinline__ void solenoid_b(const DField &f, double x, double y, double z, double B[3], double (*dB)[3]) {
@@ -564,6 +727,7 @@ __device__ void bfield64(const DScene &S, double x, double y, double z, double B
         if (f.type == PT_FIELD_TAB3D) tab3_b<GRAD>(f, x, y, z, Bt, dBt);
         else if (f.type == PT_FIELD_HARMONIC) harmonic_b<GRAD>(f, x, y, z, Bt, dBt);
         else if (f.type == PT_FIELD_SOLENOID) solenoid_b(f, x, y, z, Bt, GRAD ? dBt : nullptr);
+        else if (f.type == PT_FIELD_TAB2D) tab2_b<GRAD>(f, x, y, z, Bt, dBt);
         for (int i = 0; i < 3; ++i) {
             Bt[i] *= f.bscale;
             if (GRAD) for (int j = 0; j < 3; ++j) dBt[i][j] *= f.bscale;
@@ -583,6 +747,7 @@ __device__ __forceinline__ void bfield_other32(const DField &f, double x, double
     if (f.type == PT_FIELD_TAB3D) tab3_b<GRAD>(f, x, y, z, Bd, dBd);
     else if (f.type == PT_FIELD_HARMONIC) harmonic_b<GRAD>(f, x, y, z, Bd, dBd);
     else if (f.type == PT_FIELD_SOLENOID) solenoid_b(f, x, y, z, Bd, GRAD ? dBd : nullptr);
+    else if (f.type == PT_FIELD_TAB2D) tab2_b<GRAD>(f, x, y, z, Bd, dBd);
     for (int i = 0; i < 3; ++i) {
         Bd[i] *= f.bscale;
         if (GRAD) for (int j = 0; j < 3; ++j) dBd[i][j] *= f.bscale;
@@ -658,6 +823,8 @@ __device__ void efield(const DScene &S, int prec, double x, double y, double z, 
             Vt = Et[2] * z;
         } else if (f.type == PT_FIELD_TAB3D) {
             tab3_v(f, prec, x, y, z, Vt, Et);
+        } else if (f.type == PT_FIELD_TAB2D) {
+            tab2_e(f, x, y, z, Vt, Et);
         }
         Vt *= f.escale;
         for (int i = 0; i < 3; ++i) Et[i] *= f.escale;

@@ -101,6 +101,19 @@ class Scene:
         f["box"] = box if box is not None else (x.max(), x.min(), y.max(), y.min(), z.max(), z.min())
         self.fields.append(f)
 
+    def add_table2d(self, r, z, br=None, bphi=None, bz=None, v=None, er=None, ephi=None, ez=None, b_scale=1.0,
+                    e_scale=1.0):
+        """TabField (OPERA2D / 2Dtable): a field rotationally symmetric about
+        the z axis on an (r, z) grid; arrays shaped (nr, nz).  E_r, E_phi,
+        E_z columns take precedence over the potential.  The reference wraps
+        it in a container without a box (src/field_2d.cpp:65)."""
+        r, z = (np.ascontiguousarray(a, dtype=np.float64) for a in (r, z))
+        f = {"type": A.FIELD_TAB2D, "x": r, "z": z, "b_scale": b_scale, "e_scale": e_scale, "boundary_width": 0.0,
+             "box": (0, 0, 0, 0, 0, 0)}
+        for k, arr in (("bx", br), ("by", bphi), ("bz", bz), ("v", v), ("er", er), ("ephi", ephi), ("ez", ez)):
+            f[k] = None if arr is None else np.ascontiguousarray(arr, dtype=np.float64).reshape(-1)
+        self.fields.append(f)
+
     def add_harmonic(self, coeffs, offset=(0.0, 0.0, 0.0), b_scale=1.0, boundary_width=0.0, box=(0, 0, 0, 0, 0, 0)):
         """HarmonicExpansionBField: coeffs = [(l, m, G), ...]."""
         l = np.array([c[0] for c in coeffs], dtype=np.int32)
@@ -152,6 +165,11 @@ class Scene:
                 F.x, F.y, F.z = _dp(f["x"]), _dp(f["y"]), _dp(f["z"])
                 F.bx, F.by, F.bz, F.v = (_dp(f[k]) for k in ("bx", "by", "bz", "v"))
                 keep += [f[k] for k in ("x", "y", "z", "bx", "by", "bz", "v")]
+            elif f["type"] == A.FIELD_TAB2D:
+                F.nx, F.ny, F.nz = len(f["x"]), 1, len(f["z"])
+                F.x, F.z = _dp(f["x"]), _dp(f["z"])
+                F.bx, F.by, F.bz, F.v, F.er, F.ephi, F.ez = (_dp(f[k]) for k in ("bx", "by", "bz", "v", "er", "ephi", "ez"))
+                keep += [f[k] for k in ("x", "z", "bx", "by", "bz", "v", "er", "ephi", "ez")]
             elif f["type"] == A.FIELD_HARMONIC:
                 F.n_coeff = len(f["l"])
                 F.l, F.m, F.g = _ip(f["l"]), _ip(f["m"]), _dp(f["g"])
@@ -358,11 +376,14 @@ class Engine:
             raise ValueError("pt_adjoint differentiates a harmonic-expansion field")
         return [f.g[k] for k in range(f.n_coeff)]
 
-    def field(self, xyzt, precision=A.PREC_FP64):
+    def field(self, xyzt, precision=A.PREC_FP64, grad=True):
+        """B, dB/dx, V, E at (x, y, z, t) rows; grad=False evaluates B on the
+        value-only path and returns dB None."""
         q = np.ascontiguousarray(xyzt, dtype=np.float64).reshape(-1, 4)
         n = len(q)
-        B, dB, V, E = np.zeros((n, 3)), np.zeros((n, 3, 3)), np.zeros(n), np.zeros((n, 3))
-        self._check(lib().pt_field_eval(self.h, n, _dp(q), precision, _dp(B), _dp(dB), _dp(V), _dp(E)))
+        B, V, E = np.zeros((n, 3)), np.zeros(n), np.zeros((n, 3))
+        dB = np.zeros((n, 3, 3)) if grad else None
+        self._check(lib().pt_field_eval(self.h, n, _dp(q), precision, _dp(B), _dp(dB) if grad else None, _dp(V), _dp(E)))
         return B, dB, V, E
 
     def collisions(self, segs, max_hits=8):

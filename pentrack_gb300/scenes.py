@@ -1,4 +1,4 @@
-"""Synthetic scenes, STL/OPERA3D readers and particle sources.
+"""Synthetic scenes, STL/OPERA3D/OPERA2D readers and particle sources.
 
 The workloads named by the benchmark (closed unit cube, field-storage
 cylinder with a 64^3 tricubic quadrupole table, ...) are generated here from
@@ -217,6 +217,77 @@ def write_opera3d(path, axes, comps):
         f.write(" 0\n")
         cols = [X.ravel(), Y.ravel(), Z.ravel()] + [np.asarray(comps[k]).ravel() for k in names]
         np.savetxt(f, np.column_stack(cols), fmt="%.17g")
+
+
+# OPERA2D tables
+OPERA2D_COLUMNS = (("RBX", "BR"), ("RBY", "BPHI"), ("RBZ", "BZ"), ("EX", "ER"), ("EY", "EPHI"), ("EZ", "EZ"),
+                   ("RV", "V"))
+
+
+def read_opera2d(path, lengthconv=1.0):
+    """OPERA2D table (TabField::ReadTabFile, src/field_2d.cpp:68-190): header
+    "m 1 n ...", the coordinate lines (r, an optional " 2 Y [LENGU]", z),
+    then the optional column lines RBX, RBY, RBZ, EX, EY, EZ, RV in that
+    order, recognised by substring as the reference does, up to " 0".  Rows
+    run over z inside r; a z below the previous one starts the next r.
+    Returns (r, z) and (nr, nz) arrays named BR, BPHI, BZ, ER, EPHI, EZ, V."""
+    with open(path) as f:
+        head = f.readline().split()
+        m, n = int(head[0]), int(head[2])
+        f.readline()
+        line = f.readline()
+        skipy = not line.startswith(" 2 Y [LENGU]")
+        line = f.readline()
+        if not skipy:
+            line = f.readline()
+        cols = []
+        for tag, name in OPERA2D_COLUMNS:
+            if tag in line:
+                cols.append(name)
+                line = f.readline()
+        if not line.startswith(" 0"):
+            raise ValueError(f"{path} not found or corrupt")
+        data = np.array(f.read().split(), dtype=np.float64)
+    width = (2 if skipy else 3) + len(cols)
+    rows = data[: len(data) // width * width].reshape(-1, width)
+    r_all, z_all = rows[:, 0] * lengthconv, rows[:, 1 if skipy else 2] * lengthconv
+    ri = np.zeros(len(rows), dtype=np.int64)
+    zi = np.zeros(len(rows), dtype=np.int64)
+    cur_r, cur_z = 0, -1
+    zs = {}
+    for k in range(len(rows)):
+        if cur_z >= 0 and z_all[k] < zs[cur_z]:
+            cur_r, cur_z = cur_r + 1, 0
+        else:
+            cur_z += 1
+        zs[cur_z] = z_all[k]
+        ri[k], zi[k] = cur_r, cur_z
+    if cur_r + 1 != m or cur_z + 1 != n:
+        raise ValueError(f"The header says the size is {m} by {n}, actually it is {cur_r + 1} by {cur_z + 1}!")
+    r = np.zeros(m)
+    z = np.zeros(n)
+    r[ri] = r_all
+    z[zi] = z_all
+    out = {}
+    for c, name in enumerate(cols):
+        arr = np.zeros((m, n))
+        arr[ri, zi] = rows[:, (2 if skipy else 3) + c]
+        out[name] = arr
+    return (r, z), out
+
+
+def write_opera2d(path, r, z, comps, lengthunit=1.0):
+    """Write an OPERA2D table (columns r, z and the named ones of
+    OPERA2D_COLUMNS in their file order); coordinates divided by lengthunit."""
+    tags = [(tag, name) for tag, name in OPERA2D_COLUMNS if name in comps]
+    R, Z = np.meshgrid(r, z, indexing="ij")
+    with open(path, "w") as f:
+        f.write(f"{len(r)} 1 {len(z)} 1\n 1 X [LENGU]\n 2 Z [LENGU]\n")
+        for i, (tag, name) in enumerate(tags):
+            f.write(f" {3 + i} {tag} [{'ENERU' if name == 'V' else 'FLUXU'}]\n")
+        f.write(" 0\n")
+        cols = [R.ravel() / lengthunit, Z.ravel() / lengthunit] + [np.asarray(comps[name]).ravel() for _, name in tags]
+        np.savetxt(f, np.column_stack(cols), fmt="%.17g", delimiter="\t")
 
 
 # ----------------------------------------------------------------------------

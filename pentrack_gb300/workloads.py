@@ -8,8 +8,9 @@ field_storage       closed cylinder R = 0.2 m, z in [-0.05, 0.05] m, 256 segment
                     5 % Lambert and 1e-4 loss per bounce (surface columns on the
                     cylinder's vacuum material, where the reference's OnHit reads
                     them), tau = 880 s, 0-250 neV, 50/50 spin states, 200 s
-integration_test    the reference's test/IntegrationTest with the 3D table only:
-                    linear gradient dBz/dz = 0.5 T/m in a hollow unit cube
+integration_test    the reference's test/IntegrationTest: OPERA3D and (full=True)
+                    OPERA2D linear-gradient tables of dBz/dz = 0.5 T/m each in a
+                    hollow unit cube
 adjoint_spin        closed cylinder R = 0.2 m, z in [-0.06, 0.06] m, 512 segments
                     (2,048 triangles), B0 = 1 uT along z plus 8 harmonic terms
                     (l <= 2, G ~ N(0, (1e-10 T/m^l)^2)), E = 1e6 V/m along z,
@@ -115,16 +116,23 @@ def hollow_cube_mesh():
     return np.vstack([outer, inner])
 
 
-def integration_test(n=1000, seed=7, mesh=None, table=None):
-    """test/IntegrationTest/config.in with only the OPERA3D gradient table
-    (dBz/dz = 0.5 T/m after the 5e-5 scale and cm->m conversion).  Particles
-    start at (0.1, 0.5, 0.01) with theta_v = 5 deg, E in [10, 150] neV, pol +1,
-    inside the hollow of a UCNdet-walled cube."""
+def integration_test(n=1000, seed=7, mesh=None, table=None, full=False):
+    """test/IntegrationTest/config.in: the OPERA3D gradient table (dBz/dz =
+    0.5 T/m after the 5e-5 scale and cm->m conversion) and, with full=True,
+    the OPERA2D one of the same gradient listed before it (1 T/m in total).
+    Particles start at (0.1, 0.5, 0.01) with theta_v = 5 deg, E in [10, 150]
+    neV, pol +1, inside the hollow of a UCNdet-walled cube."""
     sc = Scene()
     sc.add_material("default", 0.0)
     sc.add_material("UCNdet", 0.1, 1.0)
     sc.add_solid(1, "default")
     sc.add_solid(2, "UCNdet", hollow_cube_mesh() if mesh is None else mesh)
+    if full:
+        # VerticalLinearGradientField2D.tab: 11 x 11 (r, z) grid 0..100 cm, RBX = 0, RBZ = RV = 100*z[cm]
+        r2 = np.linspace(0.0, 1.0, 11)
+        R2, Z2 = np.meshgrid(r2, r2, indexing="ij")
+        sc.add_table2d(r2, r2.copy(), br=np.zeros_like(Z2), bz=10000.0 * Z2, v=10000.0 * Z2, b_scale=0.00005,
+                       e_scale=0.0)
     if table is None:
         # VerticalLinearGradientField3D.tab: 6x6x6 grid 0..100 cm, BZ = 100*z[cm] Gauss units before the 5e-5 scale
         ax = np.linspace(0.0, 1.0, 6)

@@ -11,6 +11,10 @@ records:
                       libtricubic's tricubic_eval value/derivatives at points
   reference_fixtures.npz  the IntegrationTest geometry/table and the unit-cube
                       STL read from the reference's test/ directory
+  alglib_spline2d.npz spline2dbuildbicubicv + spline2ddiff / spline2dcalc on
+                      uniform and random (r, z) grids (TabField, src/field_2d.cpp:247-335)
+  opera2d_tables.npz  test/VerticalLinearGradientField2D.tab and
+                      test/CosineGradientField.tab read in centimetres
 """
 import os
 import subprocess
@@ -72,6 +76,34 @@ def main():
     np.savez_compressed(os.path.join(HERE, "reference_fixtures.npz"), hollow=hollow, cube=cube,
                         tab_x=axes[0], tab_y=axes[1], tab_z=axes[2], tab_bz=comps["BZ"], tab_bx=comps["BX"],
                         tab_by=comps["BY"], tab_v=comps["V"])
+    cases = {}
+    for case, (m, n) in enumerate(((2, 2), (3, 2), (2, 5), (4, 4), (7, 5), (11, 11), (6, 9))):
+        if case % 2 == 0:
+            x = np.linspace(0.0, 0.5, m)
+            y = np.linspace(-0.2, 0.3, n)
+        else:
+            x = np.sort(rng.uniform(0.0, 1.0, m)) + 0.01 * np.arange(m)
+            y = np.sort(rng.uniform(-1.0, 1.0, n)) + 0.01 * np.arange(n)
+        F = rng.normal(size=(m, n)) * (10.0 ** rng.integers(-4, 3))  # [ix][iy]
+        # TabField's range: x0 <= x < x0 + (x1 - x0)(m - 1), likewise in y (src/field_2d.cpp:291)
+        xhi = min(x[-1], x[0] + (x[1] - x[0]) * (m - 1))
+        yhi = min(y[-1], y[0] + (y[1] - y[0]) * (n - 1))
+        px = np.concatenate([rng.uniform(x[0], xhi, 64), x[:-1], np.full(n - 1, x[0])])
+        py = np.concatenate([rng.uniform(y[0], yhi, 64), np.full(m - 1, y[0]), y[:-1]])
+        px, py = np.ascontiguousarray(px), np.ascontiguousarray(py)
+        out = np.zeros((len(px), 5))
+        fa = np.ascontiguousarray(F.T)  # ALGLIB's f[iy*m + ix]
+        assert R.ref_spline2d(m, dp(x), n, dp(y), dp(fa), len(px), dp(px), dp(py), dp(out)) == 0
+        cases.update({f"x{case}": x, f"y{case}": y, f"f{case}": F, f"px{case}": px, f"py{case}": py, f"out{case}": out})
+    np.savez_compressed(os.path.join(HERE, "alglib_spline2d.npz"), n_cases=np.array(case + 1), **cases)
+
+    tabs = {}
+    for key, name in (("linear", "VerticalLinearGradientField2D.tab"), ("cosine", "CosineGradientField.tab")):
+        (r, z), cols = scenes.read_opera2d(os.path.join(ref, name), 0.01)
+        tabs[f"{key}_r"], tabs[f"{key}_z"] = r, z
+        for c, arr in cols.items():
+            tabs[f"{key}_{c}"] = arr
+    np.savez_compressed(os.path.join(HERE, "opera2d_tables.npz"), **tabs)
     print("golden vectors written to", HERE)
 
 

@@ -41,7 +41,7 @@ def test_struct_sizes_match_header(built):
     assert ctypes.sizeof(A.Material) == 9 * 8
     assert ctypes.sizeof(A.Solid) == 24
     assert ctypes.sizeof(A.Particles) == 17 * 8
-    assert A.Field.sol_bcenter.offset + 8 == ctypes.sizeof(A.Field)
+    assert A.Field.ez.offset + 8 == ctypes.sizeof(A.Field)
 
 
 def test_create_without_device_fails_cleanly(built):

@@ -4,8 +4,11 @@ The reference's test/IntegrationTest is its only analytic known-answer test of
 integrator + field + collision path: UCN fly on parabolas with
 a = -g - |mu_n| dBz/dz / m_n and the landing x must equal
 x0 + vx0 * t(z_end) (test/IntegrationTest/showintegrationresult.cxx:1-7).
-Here it runs with the OPERA3D half only (dBz/dz = 0.5 T/m).
+It runs with the OPERA3D half only (dBz/dz = 0.5 T/m) and in full, the
+OPERA2D and OPERA3D tables together (1 T/m, a = -15.5754762729 m/s^2 as
+showintegrationresult.cxx states).
 """
+import pytest
 import numpy as np
 
 from pentrack_gb300 import _abi as A
@@ -18,13 +21,14 @@ def landing_residual(parts, out, a):
     return out.y[0] - x0 - vx0 * t_hit
 
 
-def test_integration_test_known_answer_oracle(oracle_mod):
+@pytest.mark.parametrize("full", [False, True])
+def test_integration_test_known_answer_oracle(oracle_mod, full):
     from pentrack_gb300 import workloads
-    sc, params, parts = workloads.integration_test(n=200)
+    sc, params, parts = workloads.integration_test(n=200, full=full)
     orc = oracle_mod.Oracle(sc)
     out, st = orc.integrate(params, parts, nthreads=4)
-    a = workloads.integration_test_acceleration(0.5)
-    assert abs(a - (-12.691)) < 1e-3
+    a = workloads.integration_test_acceleration(1.0 if full else 0.5)
+    assert abs(a - (-15.5754762729 if full else -12.691)) < 1e-3
     # absorbed in the floor on the first wall contact (fast ones reach the ceiling instead)
     first = (out.n_hit == 1) & (out.stop_id == A.ID_ABSORBED_IN_MATERIAL) & (out.y[2] < 0.5)
     assert first.sum() > 100

@@ -115,6 +115,12 @@ def test_synthetic_fixtures_replicate_reference_files(oracle_mod):
     f = sc.fields[0]
     assert np.allclose(f["x"], g["tab_x"]) and np.allclose(f["z"], g["tab_z"])
     assert np.allclose(f["bz"].reshape(6, 6, 6), g["tab_bz"])
+    g2 = np.load(os.path.join(GOLD, "opera2d_tables.npz"))
+    sc, _, _ = workloads.integration_test(n=1, full=True)
+    f = sc.fields[0]
+    assert f["type"] == 5 and np.allclose(f["x"], g2["linear_r"]) and np.allclose(f["z"], g2["linear_z"])
+    for k, c in (("bx", "BR"), ("bz", "BZ"), ("v", "V")):
+        assert np.allclose(f[k].reshape(11, 11), g2[f"linear_{c}"])
 
 
 def test_oracle_harmonic_terms_match_reference_closed_forms(oracle_mod):
