@@ -94,8 +94,8 @@ typedef struct pt_material {
     double fermi_imag;
     double diff_prob;
     double spinflip_prob;
-    double rms_roughness;     /* MicroRoughness: must be 0 on the device path */
-    double correl_length;     /* MicroRoughness: must be 0 on the device path */
+    double rms_roughness;     /* MicroRoughness (src/microroughness.cpp): RMS roughness; with correl_length > 0 */
+    double correl_length;     /* the model applies where MRValid holds (src/neutron.cpp:203) */
     double internal_bfield;
     double modified_lambert_prob;
     double loss_per_bounce;

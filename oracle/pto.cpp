@@ -16,6 +16,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <complex>
 #include <cstring>
 #include <limits>
 #include <memory>
@@ -912,6 +913,150 @@ void rotate_vector(double v[3], const double n[3], const double *x) {
 
 struct SolidRef { int idx; bool ignored; };
 
+/* ------------------------------------------------------------------ */
+/* MicroRoughness (src/microroughness.cpp:15-134), restated with the
+ * reference's complex amplitudes and the library Bessel function.
+ * MRProb integrates like Boost.odeint's integrate() (Dormand-Prince 5(4)
+ * dense output, tolerances 1e-6, first step 0.01, last step shortened to
+ * the end); MRDistMax takes the maximum from a grid and golden-section
+ * refinement where the reference runs ALGLIB's conjugate-gradient
+ * minimiser from pi/4 (a local search that can stop below the maximum).  */
+/* ------------------------------------------------------------------ */
+namespace mr {
+
+/* MR::MRValid (src/microroughness.cpp:15-33) */
+bool valid(const double v[3], double Estep, double b, double w) {
+    if (b == 0 || w == 0) return false;
+    double v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    double E = 0.5 * PT_M_N * v2;
+    double ki = std::sqrt(2 * PT_M_N * E) * PT_ELE_E / PT_HBAR;
+    if (Estep >= 0) {
+        double kc = std::sqrt(2 * PT_M_N * Estep) * PT_ELE_E / PT_HBAR;
+        return 2 * b * ki < 2 && 2 * b * kc < 2;
+    }
+    double kt = std::sqrt(2 * PT_M_N * (E - Estep)) * PT_ELE_E / PT_HBAR;
+    return 2 * b * ki < 2 && 2 * b * kt < 2;
+}
+
+/* MR::MRDist (src/microroughness.cpp:35-85) */
+double dist(bool transmit, bool integral, const double v[3], const double normal[3], double Estep, double b, double w,
+            double theta, double phi) {
+    if (theta < 0 || theta > PT_PI / 2) return 0;
+    double v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    double vnormal = v[0] * normal[0] + v[1] * normal[1] + v[2] * normal[2];
+    double E = 0.5 * PT_M_N * v2;
+    if (transmit && E <= Estep) return 0;
+    double ki = std::sqrt(2 * PT_M_N * E) * PT_ELE_E / PT_HBAR;
+    std::complex<double> kc = std::sqrt(2 * PT_M_N * std::complex<double>(Estep, 0.)) * PT_ELE_E / PT_HBAR;
+    double kt = 0;
+    double costheta_i = std::fabs(vnormal / std::sqrt(v2));
+    std::complex<double> Si = 2 * costheta_i / (costheta_i + std::sqrt(costheta_i * costheta_i - kc * kc / ki / ki));
+    std::complex<double> So;
+    double ct = std::cos(theta), st = std::sin(theta);
+    if (transmit) {
+        kt = std::sqrt(2 * PT_M_N * (E - Estep)) * PT_ELE_E / PT_HBAR;
+        if (-std::real(kc * kc) / kt / kt > ct * ct) return 0;
+        So = 2 * ct / (ct + std::sqrt(ct * ct + kc * kc / kt / kt));
+    } else {
+        So = 2 * ct / (ct + std::sqrt(ct * ct - kc * kc / ki / ki));
+    }
+    double theta_i = std::acos(costheta_i), sti = std::sin(theta_i);
+    double Fmu;
+    if (!integral && !transmit)
+        Fmu = std::exp(-w * w / 2 * ki * ki * (sti * sti + st * st - 2 * sti * st * std::cos(phi)));
+    else if (!integral && transmit)
+        Fmu = std::exp(-w * w / 2 * (ki * ki * sti * sti + kt * kt * st * st - 2 * ki * kt * sti * st * std::cos(phi)));
+    else if (!transmit)
+        Fmu = std::exp(-w * w / 2 * ki * ki * (sti * sti + st * st)) * 2 * PT_PI * std::cyl_bessel_i(0.0, w * w * ki * ki * sti * st);
+    else
+        Fmu = std::exp(-w * w / 2 * (ki * ki * sti * sti + kt * kt * st * st)) * 2 * PT_PI *
+              std::cyl_bessel_i(0.0, w * w * ki * kt * sti * st);
+    double factor = std::real(kc * kc * kc * kc) * b * b * w * w / 8 / PT_PI / costheta_i;
+    if (transmit) factor *= kt / ki;
+    if (integral) factor *= st;
+    return factor * std::norm(Si) * std::norm(So) * Fmu;
+}
+
+/* MR::MRProb (src/microroughness.cpp:101-107); ok = false when a step
+ * fails 500 times (odeint throws) */
+double prob(bool transmit, const double v[3], const double normal[3], double Estep, double b, double w, bool &ok) {
+    auto f = [&](double th) { return dist(transmit, true, v, normal, Estep, b, w, th, 0); };
+    const double T = PT_PI / 2, eps = std::numeric_limits<double>::epsilon();
+    static const double c3 = 3.0 / 10, c4 = 4.0 / 5, c5 = 8.0 / 9;
+    static const double b1 = 35.0 / 384, b3 = 500.0 / 1113, b4 = 125.0 / 192, b5 = -2187.0 / 6784, b6 = 11.0 / 84;
+    static const double e1 = 35.0 / 384 - 5179.0 / 57600, e3 = 500.0 / 1113 - 7571.0 / 16695, e4 = 125.0 / 192 - 393.0 / 640,
+                        e5 = -2187.0 / 6784 + 92097.0 / 339200, e6 = 11.0 / 84 - 187.0 / 2100, e7 = -1.0 / 40;
+    double t = 0, x = 0, dt = 0.01, d0 = f(0.0);
+    long steps = 0;
+    while (T - t > eps) {
+        while (t + dt - T <= eps) {
+            for (int tries = 0;; ++tries) {
+                if (tries >= 500) { ok = false; return x; }
+                double k3 = f(t + dt * c3), k4 = f(t + dt * c4), k5 = f(t + dt * c5), k6 = f(t + dt);
+                double xn = x + dt * (b1 * d0 + b3 * k3 + b4 * k4 + b5 * k5 + b6 * k6);
+                double xe = dt * (e1 * d0 + e3 * k3 + e4 * k4 + e5 * k5 + e6 * k6 + e7 * k6);
+                double err = std::fabs(xe) / (1e-6 + 1e-6 * (std::fabs(x) + std::fabs(dt) * std::fabs(d0)));
+                if (!(err <= 1.0)) {
+                    if (err != err) err = 1e300;
+                    dt *= std::max(0.9 * std::pow(err, -1.0 / 3.0), 0.2);
+                    continue;
+                }
+                t += dt;
+                x = xn;
+                d0 = k6;
+                if (err < 0.5) dt *= 0.9 * std::pow(std::max(3.2e-4, err), -1.0 / 5.0);
+                break;
+            }
+            if (++steps > 100000) { ok = false; return x; }
+        }
+        if (T - t > eps) {
+            dt = T - t;
+            d0 = f(t);
+        }
+    }
+    return x;
+}
+
+/* MR::MRDistMax (src/microroughness.cpp:123-132): the largest of 65 grid
+ * values over [0, pi/2], refined by 60 golden-section steps between the
+ * best point's neighbours, and of the values beside the amplitude's cusp */
+double distmax(bool transmit, const double v[3], const double normal[3], double Estep, double b, double w) {
+    auto f = [&](double th) { return dist(transmit, false, v, normal, Estep, b, w, th, 0); };
+    const double h = PT_PI / 2 / 64;
+    int best = 0;
+    double fbest = f(0.0);
+    for (int k = 1; k <= 64; ++k) {
+        double fk = f(k * h);
+        if (fk > fbest) { fbest = fk; best = k; }
+    }
+    const double g = 0.6180339887498949;
+    double lo = std::max(best - 1, 0) * h, hi = std::min(best + 1, 64) * h;
+    double c = hi - g * (hi - lo), d = lo + g * (hi - lo), fc = f(c), fd = f(d);
+    for (int i = 0; i < 60; ++i) {
+        if (fc >= fd) { hi = d; d = c; fd = fc; c = hi - g * (hi - lo); fc = f(c); }
+        else { lo = c; c = d; fc = fd; d = lo + g * (hi - lo); fd = f(d); }
+    }
+    double m = std::max(fbest, f(0.5 * (lo + hi)));
+    /* the cusp where the outgoing amplitude's square root turns complex
+     * (reflection: cos theta = kc / ki above the step; transmission below a
+     * negative step: the cut-off cos^2 theta = -kc^2 / kt^2, approached from
+     * inside) is a local maximum narrower than the grid */
+    double v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2], E = 0.5 * PT_M_N * v2;
+    double kc2 = 2 * PT_M_N * Estep * (PT_ELE_E / PT_HBAR) * (PT_ELE_E / PT_HBAR);
+    double ki2 = 2 * PT_M_N * E * (PT_ELE_E / PT_HBAR) * (PT_ELE_E / PT_HBAR);
+    double kt2 = 2 * PT_M_N * (E - Estep) * (PT_ELE_E / PT_HBAR) * (PT_ELE_E / PT_HBAR);
+    double c2 = -1;
+    if (!transmit && kc2 > 0 && kc2 < ki2) c2 = kc2 / ki2;
+    if (transmit && E > Estep && kc2 < 0 && -kc2 < kt2) c2 = -kc2 / kt2;
+    if (c2 > 0) {
+        double th = std::acos(std::sqrt(c2));
+        for (double fac : {1 - 1e-12, 1 - 1e-9, 1 + 1e-12, 1 + 1e-9}) m = std::max(m, f(th * fac));
+    }
+    return m;
+}
+
+} // namespace mr
+
 struct Tracker {
     const Scene &sc;
     const pt_run_params &P;
@@ -1183,8 +1328,47 @@ struct Tracker {
             if (it > 10000) { stopID = PT_ID_GEOMETRY_ERROR; break; }
         }
     }
-    /* TNeutron::OnHit (src/neutron.cpp:187-264), MicroRoughness branches absent
-     * (rejected at setup) */
+    /* the MicroRoughness direction (TNeutron::ReflectMR / TransmitMR,
+     * src/neutron.cpp:38-62, 118-148): rejection under 1.5 times the
+     * transmission distribution's maximum, phi uniform, theta
+     * sin-distributed on [0, pi/2] */
+    void mr_direction(bool transmit, const double *v, const double *normal, double Estep, const pt_material &mat,
+                      double &theta, double &phi) {
+        double env = 1.5 * mr::distmax(true, v, normal, Estep, mat.rms_roughness, mat.correl_length);
+        for (int it = 0;; ++it) {
+            phi = 2. * PT_PI * rng.u();
+            theta = std::acos(std::cos(0.0) - rng.u() * (std::cos(0.0) - std::cos(PT_PI / 2.)));
+            if (!(rng.u() * env > mr::dist(transmit, false, v, normal, Estep, mat.rms_roughness, mat.correl_length, theta, phi)))
+                break;
+            if (it > 10000) { stopID = PT_ID_GEOMETRY_ERROR; break; }
+        }
+    }
+    void reflect_mr(double x1, const double *y1, double &x2, double *y2, const double *normal, double Estep, const pt_material &mat) {
+        double th, ph;
+        mr_direction(false, &y1[3], normal, Estep, mat, th, ph);
+        double vn = y1[3] * normal[0] + y1[4] * normal[1] + y1[5] * normal[2];
+        if (vn > 0) th = PT_PI - th;
+        x2 = x1;
+        y2[0] = y1[0]; y2[1] = y1[1]; y2[2] = y1[2];
+        double vabs = std::sqrt(y1[3] * y1[3] + y1[4] * y1[4] + y1[5] * y1[5]);
+        y2[3] = vabs * std::cos(ph) * std::sin(th);
+        y2[4] = vabs * std::sin(ph) * std::sin(th);
+        y2[5] = vabs * std::cos(th);
+        rotate_vector(&y2[3], normal, &y1[3]);
+        y2[6] = y1[6]; y2[8] = y1[8];
+    }
+    void transmit_mr(const double *y1, double *y2, const double *normal, double Estep, const pt_material &mat) {
+        double th, ph;
+        mr_direction(true, &y1[3], normal, Estep, mat, th, ph);
+        double vabs = std::sqrt(y1[3] * y1[3] + y1[4] * y1[4] + y1[5] * y1[5] - 2 * Estep / PT_M_N);
+        double vn = y1[3] * normal[0] + y1[4] * normal[1] + y1[5] * normal[2];
+        if (vn < 0) th = PT_PI - th;
+        y2[3] = vabs * std::cos(ph) * std::sin(th);
+        y2[4] = vabs * std::sin(ph) * std::sin(th);
+        y2[5] = vabs * std::cos(th);
+        rotate_vector(&y2[3], normal, &y1[3]);
+    }
+    /* TNeutron::OnHit (src/neutron.cpp:187-264) */
     void on_hit(double x1, const double *y1, double &x2, double *y2, const double *normal, int leaving, int entering) {
         if (sp.kind != PT_NEUTRON) return; /* TProton/TElectron::OnHit are empty */
         const pt_material &ml = sc.mats[sc.solids[leaving].mat], &me = sc.mats[sc.solids[entering].mat];
@@ -1193,7 +1377,17 @@ struct Tracker {
         const pt_material &mat = vn < 0 ? me : ml;
         if (rng.u() < mat.spinflip_prob) y2[7] *= -1;
         double Estep = mat_pot(me, y2[7]) - mat_pot(ml, y2[7]);
+        bool use_mr = mr::valid(&y1[3], Estep, mat.rms_roughness, mat.correl_length);
+        double mrr = 0, mrt = 0;
+        if (use_mr) {
+            bool ok = true;
+            mrr = mr::prob(false, &y1[3], normal, Estep, mat.rms_roughness, mat.correl_length, ok);
+            if (ekin(&y1[3]) > Estep) mrt = mr::prob(true, &y1[3], normal, Estep, mat.rms_roughness, mat.correl_length, ok);
+            if (!ok) { stopID = PT_ID_ODEINT_ERROR; return; }
+        }
         double prob = rng.u();
+        if (use_mr && prob < mrr) { reflect_mr(x1, y1, x2, y2, normal, Estep, mat); return; }
+        if (use_mr && prob < mrr + mrt) { transmit_mr(y1, y2, normal, Estep, mat); return; }
         double k1r, k1i, k2r, k2i;
         csqrt(En, -ml.fermi_imag * 1e-9, k1r, k1i);
         csqrt(En - Estep, -me.fermi_imag * 1e-9, k2r, k2i);
@@ -1201,18 +1395,24 @@ struct Tracker {
         double nr = k1r - k2r, ni = k1i - k2i, dr = k1r + k2r, di = k1i + k2i;
         double reflprob = (nr * nr + ni * ni) / (dr * dr + di * di);
         if (En > Estep) {
-            if (prob < reflprob) {
-                if (rng.u() < mat.diff_prob + mat.modified_lambert_prob) reflect_lambert(x1, y1, x2, y2, normal, mat);
+            if (prob < mrr + mrt + reflprob * (1 - mrr - mrt)) {
+                if (!use_mr && rng.u() < mat.diff_prob + mat.modified_lambert_prob) reflect_lambert(x1, y1, x2, y2, normal, mat);
                 else reflect(x1, y1, x2, y2, normal);
             } else {
-                if (rng.u() < mat.diff_prob + mat.modified_lambert_prob) transmit_lambert(y1, y2, normal, Estep, mat);
+                if (!use_mr && rng.u() < mat.diff_prob + mat.modified_lambert_prob) transmit_lambert(y1, y2, normal, Estep, mat);
                 else transmit(y1, y2, normal, Estep);
             }
         } else {
             double absprob = 1 - reflprob + mat.loss_per_bounce;
-            if (prob < absprob) stopID = PT_ID_ABSORBED_ON_SURFACE;
+            if (use_mr) {
+                double kc = std::sqrt(2 * PT_M_N * Estep) * PT_ELE_E / PT_HBAR;
+                double addtrans = 2 * std::pow(me.rms_roughness, 2) * kc * kc /
+                                  (1 + 0.85 * kc * me.correl_length + 2 * kc * kc * std::pow(me.correl_length, 2));
+                absprob *= std::sqrt(1 + addtrans); /* second-order correction for rough surfaces */
+            }
+            if (prob < mrr + mrt + absprob * (1 - mrr - mrt)) stopID = PT_ID_ABSORBED_ON_SURFACE;
             else {
-                if (rng.u() < mat.diff_prob + mat.modified_lambert_prob) reflect_lambert(x1, y1, x2, y2, normal, mat);
+                if (!use_mr && rng.u() < mat.diff_prob + mat.modified_lambert_prob) reflect_lambert(x1, y1, x2, y2, normal, mat);
                 else reflect(x1, y1, x2, y2, normal);
             }
         }
@@ -1583,7 +1783,7 @@ int pto_create(const pt_scene_desc *d, pto_ctx **out) {
         if (d->n_solids > 64) throw std::runtime_error("at most 64 solids");
         for (int i = 0; i < d->n_materials; ++i) {
             const pt_material &m = d->materials[i];
-            if (m.rms_roughness != 0 || m.correl_length != 0) throw std::runtime_error("MicroRoughness materials are not supported");
+            if (m.rms_roughness < 0 || m.correl_length < 0) throw std::runtime_error("negative roughness or correlation length");
             sc.mats.push_back(m);
         }
         for (int i = 0; i < d->n_solids; ++i) {
@@ -1763,6 +1963,19 @@ int pto_segment_collisions(pto_ctx *ctx, int64_t n, const double *seg, int32_t m
 int pto_point_solids(pto_ctx *ctx, int64_t n, const double *p, uint64_t *mask) {
     for (int64_t i = 0; i < n; ++i) mask[i] = ctx->sc.point_solids(p + 3 * i);
     return 0;
+}
+
+/* MicroRoughness building blocks; what: 0 MRDist, 1 MRProb (NaN when the
+ * integration fails), 2 MRDistMax */
+double pto_mr(int32_t what, int32_t transmit, int32_t integral, const double *v, const double *normal, double Estep, double b,
+              double w, double theta, double phi) {
+    if (what == 0) return mr::dist(transmit != 0, integral != 0, v, normal, Estep, b, w, theta, phi);
+    if (what == 1) {
+        bool ok = true;
+        double p = mr::prob(transmit != 0, v, normal, Estep, b, w, ok);
+        return ok ? p : std::numeric_limits<double>::quiet_NaN();
+    }
+    return mr::distmax(transmit != 0, v, normal, Estep, b, w);
 }
 
 int pto_spline_derivs(int32_t n, const double *x, const double *y, double *d) {

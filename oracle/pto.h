@@ -52,6 +52,8 @@ int pto_point_solids(pto_ctx *ctx, int64_t n, const double *p, uint64_t *mask);
 
 /* building blocks exposed for the golden-vector tests */
 int pto_spline_derivs(int32_t n, const double *x, const double *y, double *d);
+double pto_mr(int32_t what, int32_t transmit, int32_t integral, const double *v, const double *normal, double Estep, double b,
+              double w, double theta, double phi);
 void pto_tricubic_coeff(const double *stacked64, double *a64);
 void pto_tricubic_eval(const double *a64, double x, double y, double z, int derx, int dery, int derz, double *out);
 void pto_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

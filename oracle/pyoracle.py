@@ -34,6 +34,9 @@ def lib():
         L.pto_segment_collisions.argtypes = [vp, C.c_int64, dp, C.c_int32, A.c_int32_p, dp, dp, A.c_int32_p, dp]
         L.pto_point_solids.argtypes = [vp, C.c_int64, dp, A.c_uint64_p]
         L.pto_spline_derivs.argtypes = [C.c_int32, dp, dp, dp]
+        L.pto_mr.argtypes = [C.c_int32, C.c_int32, C.c_int32, dp, dp, C.c_double, C.c_double, C.c_double, C.c_double,
+                             C.c_double]
+        L.pto_mr.restype = C.c_double
         L.pto_tricubic_coeff.argtypes = [dp, dp]
         L.pto_tricubic_eval.argtypes = [dp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, dp]
         L.pto_philox4x32_10.argtypes = [P(C.c_uint32), P(C.c_uint32), P(C.c_uint32)]
@@ -126,6 +129,15 @@ class Oracle:
         m = np.zeros(len(p), np.uint64)
         lib().pto_point_solids(self.h, len(p), _dp(p), m.ctypes.data_as(A.c_uint64_p))
         return m
+
+
+def mr(what, v, normal, Estep, b, w, transmit=False, integral=False, theta=0.0, phi=0.0):
+    """MicroRoughness of one wall contact: what = "dist" (MRDist), "prob"
+    (MRProb) or "max" (MRDistMax)"""
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    n = np.ascontiguousarray(normal, dtype=np.float64)
+    k = {"dist": 0, "prob": 1, "max": 2}[what]
+    return lib().pto_mr(k, int(transmit), int(integral), _dp(v), _dp(n), Estep, b, w, theta, phi)
 
 
 def spline_derivs(x, y):

@@ -184,9 +184,9 @@ pt_status validate_materials(const pt_scene_desc *d, std::string &err) {
                   "! Now I don't know which to use.";
             return PT_ERR_INVALID;
         }
-        if (m.rms_roughness != 0 || m.correl_length != 0) {
-            err = "material " + std::to_string(i) + ": MicroRoughness materials are not implemented on the device path";
-            return PT_ERR_UNSUPPORTED;
+        if (m.rms_roughness < 0 || m.correl_length < 0) {
+            err = "material " + std::to_string(i) + ": negative roughness or correlation length";
+            return PT_ERR_INVALID;
         }
     }
     return PT_OK;
@@ -205,7 +205,8 @@ pt_status build_scene(pt_ctx *c, const pt_scene_desc *d) {
     std::vector<DMat> mats(d->n_materials);
     for (int i = 0; i < d->n_materials; ++i) {
         const pt_material &m = d->materials[i];
-        mats[i] = DMat{m.fermi_real, m.fermi_imag, m.diff_prob, m.spinflip_prob, m.internal_bfield, m.modified_lambert_prob, m.loss_per_bounce};
+        mats[i] = DMat{m.fermi_real, m.fermi_imag, m.diff_prob,     m.spinflip_prob, m.internal_bfield, m.modified_lambert_prob,
+                       m.loss_per_bounce, m.rms_roughness, m.correl_length};
     }
     /* solids */
     std::vector<DSolid> solids(d->n_solids);

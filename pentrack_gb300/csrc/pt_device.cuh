@@ -79,6 +79,7 @@ struct DSolid {
 
 struct DMat {
     double fermi_real, fermi_imag, diff, spinflip, ibf, modlambert, loss;
+    double rms, corr; /* MicroRoughness: RMS roughness and correlation length [m] */
 };
 
 struct DField {

@@ -8,6 +8,7 @@
  */
 #pragma once
 #include "pt_track.cuh"
+#include "pt_mr.cuh"
 #include "../../include/pt_detmath.h"
 
 namespace ptd {
@@ -1188,6 +1189,49 @@ template <class Tape> struct LaneT {
             if (it > PT_MAX_LAMBERT) { stop = PT_ID_GEOMETRY_ERROR; break; }
         }
     }
+    /* direction drawn from MRDist by rejection under 1.5 times the
+     * transmission distribution's maximum, as TNeutron::ReflectMR and
+     * TransmitMR both take it (src/neutron.cpp:46, 125): phi uniform, theta
+     * sin-distributed on [0, pi/2], a uniform test draw; the polar angle is
+     * turned to the far side of the surface as the motion requires */
+    __device__ __noinline__ void mr_direction(const MRHit &h, bool transmit, double &theta, double &phi) {
+        const double env = 1.5 * mr_distmax(h, true);
+        for (int it = 0;; ++it) {
+            phi = 2. * PT_PI * u01();
+            theta = acos(cos(0.0) - u01() * (cos(0.0) - cos(PT_PI / 2.)));
+            if (!(u01() * env > mr_dist(h, transmit, false, theta, phi))) break;
+            if (it > PT_MAX_LAMBERT) { stop = PT_ID_GEOMETRY_ERROR; break; }
+        }
+    }
+    /* TNeutron::ReflectMR (src/neutron.cpp:118-148) */
+    __device__ void reflect_mr(double x1, const double *y1, double &x2, double *y2, const double *normal, const MRHit &h) {
+        tp.on_other(*this);
+        double th, ph;
+        mr_direction(h, false, th, ph);
+        double vn = y1[3] * normal[0] + y1[4] * normal[1] + y1[5] * normal[2];
+        if (vn > 0) th = PT_PI - th;
+        x2 = x1;
+        y2[0] = y1[0]; y2[1] = y1[1]; y2[2] = y1[2];
+        double vabs = sqrt(y1[3] * y1[3] + y1[4] * y1[4] + y1[5] * y1[5]);
+        y2[3] = vabs * cos(ph) * sin(th);
+        y2[4] = vabs * sin(ph) * sin(th);
+        y2[5] = vabs * cos(th);
+        rotate_vector(&y2[3], normal, &y1[3]);
+        y2[6] = y1[6]; y2[8] = y1[8];
+    }
+    /* TNeutron::TransmitMR (src/neutron.cpp:38-62) */
+    __device__ void transmit_mr(const double *y1, double *y2, const double *normal, double Estep, const MRHit &h) {
+        tp.on_other(*this);
+        double th, ph;
+        mr_direction(h, true, th, ph);
+        double vabs = sqrt(y1[3] * y1[3] + y1[4] * y1[4] + y1[5] * y1[5] - 2 * Estep / PT_M_N);
+        double vn = y1[3] * normal[0] + y1[4] * normal[1] + y1[5] * normal[2];
+        if (vn < 0) th = PT_PI - th;
+        y2[3] = vabs * cos(ph) * sin(th);
+        y2[4] = vabs * sin(ph) * sin(th);
+        y2[5] = vabs * cos(th);
+        rotate_vector(&y2[3], normal, &y1[3]);
+    }
     /* TNeutron::OnHit (src/neutron.cpp:187-264); charged species: empty */
     __device__ void on_hit(double x1, const double *y1, double &x2, double *y2, const double *normal, int leaving, int entering) {
         if (R.sp.kind != PT_NEUTRON) return;
@@ -1197,25 +1241,43 @@ template <class Tape> struct LaneT {
         const DMat &mat = vn < 0 ? me : ml;
         if (u01() < mat.spinflip) y2[7] *= -1;
         double Estep = mat_pot(me, y2[7]) - mat_pot(ml, y2[7]);
+        /* MicroRoughness reflection and transmission probabilities */
+        const bool use_mr = mat.rms != 0 && mat.corr != 0 && mr_valid(&y1[3], Estep, mat.rms, mat.corr);
+        double mrr = 0, mrt = 0;
+        MRHit h;
+        if (use_mr) {
+            bool ok = true;
+            mr_setup(h, &y1[3], normal, Estep, mat.rms, mat.corr);
+            mrr = mr_prob(h, false, ok);
+            if (ekin(&y1[3]) > Estep) mrt = mr_prob(h, true, ok);
+            if (!ok) { stop = PT_ID_ODEINT_ERROR; return; }
+        }
         double prob = u01();
+        if (use_mr && prob < mrr) { reflect_mr(x1, y1, x2, y2, normal, h); return; }
+        if (use_mr && prob < mrr + mrt) { transmit_mr(y1, y2, normal, Estep, h); return; }
         double k1r, k1i, k2r, k2i;
         csqrt(En, -ml.fermi_imag * 1e-9, k1r, k1i);
         csqrt(En - Estep, -me.fermi_imag * 1e-9, k2r, k2i);
         double nr = k1r - k2r, ni = k1i - k2i, dr = k1r + k2r, di = k1i + k2i;
         double reflprob = (nr * nr + ni * ni) / (dr * dr + di * di);
         if (En > Estep) {
-            if (prob < reflprob) {
-                if (u01() < mat.diff + mat.modlambert) reflect_lambert(x1, y1, x2, y2, normal, mat);
+            if (prob < mrr + mrt + reflprob * (1 - mrr - mrt)) {
+                if (!use_mr && u01() < mat.diff + mat.modlambert) reflect_lambert(x1, y1, x2, y2, normal, mat);
                 else reflect(x1, y1, x2, y2, normal);
             } else {
-                if (u01() < mat.diff + mat.modlambert) transmit_lambert(y1, y2, normal, Estep, mat);
+                if (!use_mr && u01() < mat.diff + mat.modlambert) transmit_lambert(y1, y2, normal, Estep, mat);
                 else transmit(y1, y2, normal, Estep);
             }
         } else {
             double absprob = 1 - reflprob + mat.loss;
-            if (prob < absprob) stop = PT_ID_ABSORBED_ON_SURFACE;
+            if (use_mr) { /* second-order correction for reflection on rough surfaces, with the entered solid's roughness */
+                double kc = sqrt(2 * PT_M_N * Estep) * PT_ELE_E / PT_HBAR;
+                double addtrans = 2 * (me.rms * me.rms) * kc * kc / (1 + 0.85 * kc * me.corr + 2 * kc * kc * (me.corr * me.corr));
+                absprob *= sqrt(1 + addtrans);
+            }
+            if (prob < mrr + mrt + absprob * (1 - mrr - mrt)) stop = PT_ID_ABSORBED_ON_SURFACE;
             else {
-                if (u01() < mat.diff + mat.modlambert) reflect_lambert(x1, y1, x2, y2, normal, mat);
+                if (!use_mr && u01() < mat.diff + mat.modlambert) reflect_lambert(x1, y1, x2, y2, normal, mat);
                 else reflect(x1, y1, x2, y2, normal);
             }
         }

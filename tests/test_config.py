@@ -151,7 +151,7 @@ def test_config_errors(built, tmp_path):
     ({"diff_prob": 0.1, "rms_roughness": 1e-9}, A.PT_ERR_INVALID, "more than one diffuse-reflection model"),
     ({"modified_lambert_prob": 1.5}, A.PT_ERR_INVALID, "outside 0..1"),
     ({"modified_lambert_prob": -0.1}, A.PT_ERR_INVALID, "outside 0..1"),
-    ({"rms_roughness": 1e-9, "correl_length": 2e-8}, A.PT_ERR_UNSUPPORTED, "MicroRoughness"),
+    ({"rms_roughness": -1e-9, "correl_length": 2e-8}, A.PT_ERR_INVALID, "negative roughness"),
 ])
 def test_pt_create_rejects_invalid_materials(built, change, status, match):
     """pt_create checks the materials on the host before it looks for a
