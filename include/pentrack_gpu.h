@@ -420,6 +420,30 @@ typedef struct pt_source_params {
 pt_status pt_source_volume(pt_ctx *ctx, const pt_source_params *sp, int64_t n, const int64_t *ids, pt_particles *out,
                            double *vmin);
 
+/* TNeutron::Decay (src/neutron.cpp:285-375) on the device: for n decayed
+ * neutrons (ids, decay times t, end states y: 9n SoA, host buffers) the
+ * proton and the electron each makes, written to protons / electrons (n
+ * entries each, SoA stride n: id, t, y, spin = 0).  Ids: the parent's +
+ * 2^40 (proton) and + 2^41 (electron); the draws come from the parent's
+ * source stream with `seed`.  PT_ERR_INVALID when a proton's recoil-spectrum
+ * sampling did not converge. */
+pt_status pt_neutron_decay(pt_ctx *ctx, uint64_t seed, int64_t n, const int64_t *ids, const double *t, const double *y,
+                           pt_particles *protons, pt_particles *electrons);
+
+/* The reference's secondaries chain (`secondaries 1`, src/main.cpp:163-172)
+ * in one call: the neutrons of `in` tracked with `neutron` into `out`, the
+ * proton and electron of every neutron that decayed (pt_neutron_decay with
+ * neutron->seed), then the protons tracked with `proton` and the electrons
+ * with `electron` (species are per run on the device, so the secondaries
+ * run as two batches after the neutrons).  out_p and out_e hold up to their
+ * n entries (SoA stride their n; in->n always suffices) and receive the
+ * secondaries' end states in the order of their parents; *n_decayed their
+ * number; stats (may be NULL) sums the three runs.  PT_ERR_INVALID when
+ * out_p or out_e is too small. */
+pt_status pt_integrate_secondaries(pt_ctx *ctx, const pt_run_params *neutron, const pt_run_params *proton,
+                                   const pt_run_params *electron, const pt_particles *in, pt_particles *out,
+                                   pt_particles *out_p, pt_particles *out_e, int64_t *n_decayed, pt_stats *stats);
+
 /* Calibration: FP64 fused-multiply-add throughput of this device measured by
  * a dependent-chain DFMA kernel over all SMs (TFLOP/s, 2 flops per FMA). */
 pt_status pt_probe_fp64(pt_ctx *ctx, double *tflops);

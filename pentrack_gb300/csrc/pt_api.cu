@@ -1803,6 +1803,147 @@ pt_status pt_source_volume(pt_ctx *c, const pt_source_params *sp, int64_t n, con
     return PT_OK;
 }
 
+pt_status pt_neutron_decay(pt_ctx *c, uint64_t seed, int64_t n, const int64_t *ids, const double *t, const double *y,
+                           pt_particles *pp, pt_particles *pe) {
+    if (!c || n < 0 || !pp || !pe) return PT_ERR_INVALID;
+    if (n == 0) return PT_OK;
+    if (!ids || !t || !y || pp->n != n || pe->n != n || !pp->id || !pp->t || !pp->y || !pp->spin || !pe->id || !pe->t ||
+        !pe->y || !pe->spin)
+        return PT_ERR_INVALID;
+    cudaSetDevice(c->device);
+    std::vector<void *> tmp;
+    cudaError_t e = cudaSuccess;
+    const int64_t *did = dupload(tmp, ids, n, e);
+    const double *dt = dupload(tmp, t, n, e), *dy = dupload(tmp, y, 9 * n, e);
+    int64_t *dpid = dalloc<int64_t>(tmp, n, e), *deid = dalloc<int64_t>(tmp, n, e);
+    double *dpt = dalloc<double>(tmp, n, e), *det = dalloc<double>(tmp, n, e);
+    double *dpy = dalloc<double>(tmp, 9 * n, e), *dey = dalloc<double>(tmp, 9 * n, e);
+    int *dst = dalloc<int>(tmp, n, e);
+    if (e) { free_list(tmp); return ck(c, e, "decay alloc"), PT_ERR_OOM; }
+    k_decay<<<grid_for(n, 128), 128, 0, c->stream>>>(seed, n, did, dt, dy, dpid, dpt, dpy, deid, det, dey, dst);
+    e = cudaGetLastError();
+    std::vector<int> hs(n);
+    if (!e) e = cudaMemcpyAsync(pp->id, dpid, n * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaMemcpyAsync(pe->id, deid, n * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaMemcpyAsync(pp->t, dpt, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaMemcpyAsync(pe->t, det, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaMemcpyAsync(pp->y, dpy, 9 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaMemcpyAsync(pe->y, dey, 9 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaMemcpyAsync(hs.data(), dst, n * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaStreamSynchronize(c->stream);
+    free_list(tmp);
+    if (e) return ck(c, e, "decay"), PT_ERR_CUDA;
+    std::memset(pp->spin, 0, 5 * n * sizeof(double));
+    std::memset(pe->spin, 0, 5 * n * sizeof(double));
+    for (int64_t i = 0; i < n; ++i)
+        if (hs[i]) {
+            c->err = "pt_neutron_decay: proton spectrum sampling did not converge for particle " + std::to_string(ids[i]);
+            return PT_ERR_INVALID;
+        }
+    return PT_OK;
+}
+
+namespace {
+/* host SoA of m particles with every output array */
+struct HostSet {
+    std::vector<int64_t> id, na, nr;
+    std::vector<double> t, y, spin, hmax, nf, tau, hs;
+    std::vector<int32_t> stop, solid, nhit, nstep, nflip, res;
+    pt_particles p{};
+    explicit HostSet(int64_t m)
+        : id(m), na(m), nr(m), t(m), y(9 * m), spin(5 * m), hmax(m), nf(m), tau(m), hs(m), stop(m), solid(m), nhit(m), nstep(m),
+          nflip(m), res(m) {
+        p.n = m;
+        p.id = id.data(); p.t = t.data(); p.y = y.data(); p.spin = spin.data();
+        p.stop_id = stop.data(); p.solid = solid.data(); p.n_hit = nhit.data(); p.n_step = nstep.data();
+        p.n_spinflip = nflip.data(); p.reserved = res.data(); p.h_max = hmax.data(); p.noflip_prob = nf.data();
+        p.tau = tau.data(); p.h_start = hs.data(); p.n_accepted = na.data(); p.n_rejected = nr.data();
+    }
+};
+
+/* copies the m entries of a size-m set into `o` (stride o->n); absent output arrays are skipped */
+void copy_out(const HostSet &s, pt_particles *o) {
+    const int64_t m = s.p.n, n = o->n;
+    for (int64_t i = 0; i < m; ++i) {
+        if (o->id) o->id[i] = s.id[i];
+        if (o->t) o->t[i] = s.t[i];
+        if (o->y) for (int k = 0; k < 9; ++k) o->y[k * n + i] = s.y[k * m + i];
+        if (o->spin) for (int k = 0; k < 5; ++k) o->spin[k * n + i] = s.spin[k * m + i];
+        if (o->stop_id) o->stop_id[i] = s.stop[i];
+        if (o->solid) o->solid[i] = s.solid[i];
+        if (o->n_hit) o->n_hit[i] = s.nhit[i];
+        if (o->n_step) o->n_step[i] = s.nstep[i];
+        if (o->n_spinflip) o->n_spinflip[i] = s.nflip[i];
+        if (o->h_max) o->h_max[i] = s.hmax[i];
+        if (o->noflip_prob) o->noflip_prob[i] = s.nf[i];
+        if (o->tau) o->tau[i] = s.tau[i];
+        if (o->h_start) o->h_start[i] = s.hs[i];
+        if (o->n_accepted) o->n_accepted[i] = s.na[i];
+        if (o->n_rejected) o->n_rejected[i] = s.nr[i];
+    }
+}
+
+void add_stats(pt_stats &a, const pt_stats &b) {
+    a.kernel_ms += b.kernel_ms; a.span_ms += b.span_ms; a.particle_seconds += b.particle_seconds;
+    a.launches += b.launches; a.active += b.active; a.rk_accepted += b.rk_accepted; a.rk_rejected += b.rk_rejected;
+    a.rhs_evals += b.rhs_evals; a.field_evals += b.field_evals; a.hits += b.hits; a.bisection_levels += b.bisection_levels;
+    a.bvh_nodes += b.bvh_nodes; a.tri_tests += b.tri_tests; a.subsegments += b.subsegments; a.dense_evals += b.dense_evals;
+    a.spin_steps += b.spin_steps; a.aux_launches += b.aux_launches; a.graph_launches += b.graph_launches;
+}
+} // namespace
+
+pt_status pt_integrate_secondaries(pt_ctx *c, const pt_run_params *pn, const pt_run_params *pp, const pt_run_params *pe,
+                                   const pt_particles *in, pt_particles *out, pt_particles *out_p, pt_particles *out_e,
+                                   int64_t *n_decayed, pt_stats *stats) {
+    if (!c || !pn || !pp || !pe || !in || !out || !out_p || !out_e || !n_decayed) return PT_ERR_INVALID;
+    if (pn->species != PT_NEUTRON || pp->species != PT_PROTON || pe->species != PT_ELECTRON) {
+        c->err = "pt_integrate_secondaries: the runs must be neutron, proton and electron";
+        return PT_ERR_INVALID;
+    }
+    if (!out->stop_id || !out->id || !out->t || !out->y) return PT_ERR_INVALID;
+    auto w0 = std::chrono::steady_clock::now();
+    *n_decayed = 0;
+    pt_stats total, s;
+    std::memset(&total, 0, sizeof(total));
+    std::memset(&s, 0, sizeof(s));
+    pt_status st = pt_integrate(c, pn, in, out, &s);
+    total = s;
+    if (st != PT_OK) { if (stats) *stats = total; return st; }
+    std::vector<int64_t> idx;
+    for (int64_t i = 0; i < out->n; ++i)
+        if (out->stop_id[i] == PT_ID_DECAYED) idx.push_back(i);
+    const int64_t m = (int64_t)idx.size();
+    *n_decayed = m;
+    if (m > out_p->n || m > out_e->n) {
+        c->err = "pt_integrate_secondaries: " + std::to_string(m) + " decays exceed the secondaries' output size";
+        return PT_ERR_INVALID;
+    }
+    if (m > 0) {
+        std::vector<int64_t> ids(m);
+        std::vector<double> t(m), y(9 * m);
+        for (int64_t j = 0; j < m; ++j) {
+            const int64_t i = idx[j];
+            ids[j] = out->id[i];
+            t[j] = out->t[i];
+            for (int k = 0; k < 9; ++k) y[k * m + j] = out->y[k * out->n + i];
+        }
+        HostSet p0(m), e0(m), p1(m), e1(m);
+        st = pt_neutron_decay(c, pn->seed, m, ids.data(), t.data(), y.data(), &p0.p, &e0.p);
+        if (st != PT_OK) return st;
+        st = pt_integrate(c, pp, &p0.p, &p1.p, &s);
+        add_stats(total, s);
+        if (st != PT_OK) { if (stats) *stats = total; return st; }
+        st = pt_integrate(c, pe, &e0.p, &e1.p, &s);
+        add_stats(total, s);
+        if (st != PT_OK) { if (stats) *stats = total; return st; }
+        copy_out(p1, out_p);
+        copy_out(e1, out_e);
+    }
+    total.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+    if (stats) *stats = total;
+    return PT_OK;
+}
+
 pt_status pt_point_solids(pt_ctx *c, int64_t n, const double *p, uint64_t *mask) {
     if (!c || n < 0 || !mask) return PT_ERR_INVALID;
     if (n == 0) return PT_OK;

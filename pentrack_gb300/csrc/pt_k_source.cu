@@ -4,7 +4,8 @@
  * cuboid, cylindrical and STL volumes (TCuboidVolumeSource,
  * TCylindricalVolumeSource, TSTLVolumeSource: include/source.h:186-331),
  * with or without PhaseSpaceWeighting, written straight into the particle
- * arrays.
+ * arrays; and the proton and electron of each decayed neutron
+ * (TNeutron::Decay, src/neutron.cpp:285-375).
  *
  * Every particle draws from its own Philox stream (the source stream: bit
  * 63 of the counter set, keyed by the seed and the particle id), one counter
@@ -271,6 +272,107 @@ __global__ void k_source(const __grid_constant__ DScene S, const __grid_constant
     y[8 * n + i] = 0;
     for (int c = 0; c < 5; ++c) spin[c * n + i] = 0;
     status[i] = bad;
+}
+
+/* ---- secondaries of neutron decay (TNeutron::Decay, src/neutron.cpp:285-375) ---- */
+
+namespace {
+constexpr uint64_t DECAY = 5000; /* counter offset of the decay draws in a parent's source stream */
+
+/* ProtonBetaSpectrum (src/globals.cpp:84-92); the reference's 4/3 is integer division (= 1) */
+__device__ double proton_beta_spectrum(double E) {
+    const double dm = PT_M_N - PT_M_P, xi = PT_M_E / dm;
+    const double sigma = 1 - 2 * E * PT_M_N / (dm * dm) / (PT_C0 * PT_C0);
+    const double q = (sigma - xi * xi) / sigma;
+    const double a = q * q * sqrt(1 - sigma);
+    const double g1 = a * (4 * (1 + xi * xi / sigma) - 1 * (q * (1 - sigma)));
+    const double g2 = a * (4 * (1 + xi * xi / sigma - 2 * sigma) - 1 * (q * (1 - sigma)));
+    return 0.5 * (g1 + -0.1017 * g2);
+}
+
+/* BOOST (src/globals.cpp:67-78) of the four-vector p by the velocity beta (units of c) */
+__device__ void boost4(const double beta[3], double p[4]) {
+    const double b2 = beta[0] * beta[0] + beta[1] * beta[1] + beta[2] * beta[2];
+    const double gamma = 1.0 / sqrt(1.0 - b2);
+    const double bp = beta[0] * p[1] + beta[1] * p[2] + beta[2] * p[3];
+    const double gamma2 = b2 > 0 ? (gamma - 1.0) / b2 : 0.0;
+    const double q0 = gamma * (p[0] + bp);
+    const double q1 = p[1] + gamma2 * bp * beta[0] + gamma * beta[0] * p[0];
+    const double q2 = p[2] + gamma2 * bp * beta[1] + gamma * beta[1] * p[0];
+    const double q3 = p[3] + gamma2 * bp * beta[2] + gamma * beta[2] * p[0];
+    p[0] = q0; p[1] = q1; p[2] = q2; p[3] = q3;
+}
+
+/* a secondary's initial state from its four-momentum p [eV/c] and kinetic energy e [eV] */
+__device__ void decay_product(const double p[4], double e, double m, double pol, const double *pos, int64_t n, int64_t i,
+                              double *y) {
+    const double ph = atan2(p[2], p[1]);
+    const double th = acos(p[3] / sqrt(p[1] * p[1] + p[2] * p[2] + p[3] * p[3]));
+    const double v = speed_of(e, m);
+    y[0 * n + i] = pos[0];
+    y[1 * n + i] = pos[1];
+    y[2 * n + i] = pos[2];
+    y[3 * n + i] = v * cos(ph) * sin(th);
+    y[4 * n + i] = v * sin(ph) * sin(th);
+    y[5 * n + i] = v * cos(th);
+    y[6 * n + i] = 0;
+    y[7 * n + i] = pol;
+    y[8 * n + i] = 0;
+}
+} // namespace
+
+/* One thread per decayed neutron: the proton's kinetic energy from the
+ * recoil spectrum on [0, 750] eV by rejection (pairs of draws from counter
+ * 5100 on, at most 256 pairs; the reference interpolates the spectrum), its
+ * direction in the neutron's rest frame (azimuth uniform, polar angle from
+ * the sine distribution on [0, pi/2], as the reference draws it), the
+ * electron from the two-body decay of the remaining virtual state
+ * (neutrino mass 1 eV/c^2) isotropic in that state's rest frame and
+ * boosted, both boosted with the neutron's velocity; polarisations +-1 with
+ * equal probability; start at the neutron's decay time and point.  Ids:
+ * the parent's + 2^40 (proton) and + 2^41 (electron).  status 1: the
+ * spectrum sampling did not converge. */
+__global__ void k_decay(uint64_t seed, int64_t n, const int64_t *id, const double *t, const double *y, int64_t *pid, double *pt,
+                        double *py, int64_t *eid, double *et, double *ey, int *status) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t pa = id[i];
+    const double c0 = PT_C0;
+    double ekin = -1;
+    for (int k = 0; k < 256; ++k) {
+        const double e = 0.0 + sdraw(seed, pa, DECAY + 100 + 2 * k) * (750.0 - 0.0);
+        const double u = sdraw(seed, pa, DECAY + 101 + 2 * k);
+        if (u < proton_beta_spectrum(e)) { ekin = e; break; }
+    }
+    status[i] = ekin < 0 ? 1 : 0;
+    if (ekin < 0) ekin = 0;
+    const double m_nue = 1 / (c0 * c0);
+    const double pp0 = ekin / c0 + PT_M_P * c0;
+    double pabs = sqrt(pp0 * pp0 - PT_M_P * PT_M_P * c0 * c0);
+    const double b1 = 2 * PT_PI * sdraw(seed, pa, DECAY + 0), d1 = acos(1.0 - sdraw(seed, pa, DECAY + 1));
+    double pp[4] = {pp0, pabs * sin(d1) * cos(b1), pabs * sin(d1) * sin(b1), pabs * cos(d1)};
+    const double virt[4] = {PT_M_N * c0 - pp[0], -pp[1], -pp[2], -pp[3]};
+    const double m2v = virt[0] * virt[0] - virt[1] * virt[1] - virt[2] * virt[2] - virt[3] * virt[3];
+    const double pe0 = (m2v + PT_M_E * PT_M_E * c0 * c0 - m_nue * m_nue * c0 * c0) / 2 / sqrt(m2v);
+    pabs = sqrt(pe0 * pe0 - PT_M_E * PT_M_E * c0 * c0);
+    const double b2 = 2 * PT_PI * sdraw(seed, pa, DECAY + 2), d2 = acos(1.0 - sdraw(seed, pa, DECAY + 3));
+    double pe[4] = {pe0, pabs * sin(d2) * cos(b2), pabs * sin(d2) * sin(b2), pabs * cos(d2)};
+    const double bv[3] = {virt[1] / virt[0], virt[2] / virt[0], virt[3] / virt[0]};
+    boost4(bv, pe);
+    const double bn[3] = {y[3 * n + i] / c0, y[4 * n + i] / c0, y[5 * n + i] / c0};
+    boost4(bn, pp);
+    boost4(bn, pe);
+    const double bp2 = (pp[1] * pp[1] + pp[2] * pp[2] + pp[3] * pp[3]) / pp[0] / pp[0];
+    const double e_p = PT_M_P * c0 * c0 * bp2 * (0.5 + bp2 * (3. / 8. + bp2 * (5. / 16.)));
+    const double e_e = pe[0] * c0 - PT_M_E * c0 * c0;
+    const double pos[3] = {y[0 * n + i], y[1 * n + i], y[2 * n + i]};
+    const double pol_p = sdraw(seed, pa, DECAY + 4) < 0.5 ? 1.0 : -1.0, pol_e = sdraw(seed, pa, DECAY + 5) < 0.5 ? 1.0 : -1.0;
+    decay_product(pp, e_p, PT_M_P, pol_p, pos, n, i, py);
+    decay_product(pe, e_e, PT_M_E, pol_e, pos, n, i, ey);
+    pid[i] = pa + (1ll << 40);
+    eid[i] = pa + (1ll << 41);
+    pt[i] = t[i];
+    et[i] = t[i];
 }
 
 } // namespace ptk

@@ -61,6 +61,8 @@ __global__ void k_field(const __grid_constant__ DScene S, int prec, int64_t n, c
 __global__ void k_collisions(const __grid_constant__ DScene S, int64_t n, const double *seg, int maxh, int *count, double *s, double *nrm, int *sid,
                              double *dn);
 __global__ void k_point_solids(const __grid_constant__ DScene S, int64_t n, const double *p, unsigned long long *mask);
+__global__ void k_decay(uint64_t seed, int64_t n, const int64_t *id, const double *t, const double *y, int64_t *pid, double *pt,
+                        double *py, int64_t *eid, double *et, double *ey, int *status);
 __global__ void k_source_vmin(const __grid_constant__ DScene S, const __grid_constant__ DSourceSpec Q, DSpecies sp, int64_t n, double *v);
 __global__ void k_source(const __grid_constant__ DScene S, const __grid_constant__ DSourceSpec Q, DSpecies sp, int64_t n, const int64_t *ids,
                          double vmin, double *t_out, double *y, double *spin, int *status);

@@ -227,6 +227,13 @@ class ParticleSet:
         p = ParticleSet(len(idx), self.id[idx], self.t[idx], self.y[:, idx], self.spin[:, idx])
         return p
 
+    def head(self, m):
+        """the first m particles, outputs included (copies)"""
+        p = ParticleSet(m, self.id[:m].copy(), self.t[:m].copy(), self.y[:, :m].copy(), self.spin[:, :m].copy())
+        for name, _ in self.OUT_FIELDS:
+            setattr(p, name, getattr(self, name)[:m].copy())
+        return p
+
     def abi(self, outputs=True):
         P = A.Particles()
         P.n = self.n
@@ -375,6 +382,34 @@ class Engine:
         if f.type != A.FIELD_HARMONIC:
             raise ValueError("pt_adjoint differentiates a harmonic-expansion field")
         return [f.g[k] for k in range(f.n_coeff)]
+
+    def neutron_decay(self, seed, neutrons, which=None):
+        """pt_neutron_decay: the protons and electrons of the decayed neutrons of
+        a tracked set (stop ID ID_DECAYED, or the indices `which`), made on the
+        device; the same draws and formulas as secondaries.neutron_decay."""
+        idx = np.nonzero(neutrons.stop_id == A.ID_DECAYED)[0] if which is None else np.asarray(which)
+        m = len(idx)
+        ids = np.ascontiguousarray(neutrons.id[idx])
+        t = np.ascontiguousarray(neutrons.t[idx])
+        y = np.ascontiguousarray(neutrons.y[:, idx])
+        pp, pe = ParticleSet(m), ParticleSet(m)
+        a, b = pp.abi(outputs=False), pe.abi(outputs=False)
+        self._check(lib().pt_neutron_decay(self.h, seed, m, _lp(ids), _dp(t), _dp(y), C.byref(a), C.byref(b)))
+        return pp, pe
+
+    def integrate_secondaries(self, neutron, proton, electron, particles):
+        """pt_integrate_secondaries: neutrons, then the protons and electrons of
+        those that decayed, in one call; returns the three end-state sets and
+        the summed stats."""
+        n = particles.n
+        out, op, oe = ParticleSet.empty(n), ParticleSet.empty(n), ParticleSet.empty(n)
+        st, nd = A.Stats(), C.c_int64(0)
+        pin = particles.abi(outputs=False)
+        a, b, c = out.abi(), op.abi(), oe.abi()
+        self._check(lib().pt_integrate_secondaries(self.h, C.byref(neutron), C.byref(proton), C.byref(electron), C.byref(pin),
+                                                   C.byref(a), C.byref(b), C.byref(c), C.byref(nd), C.byref(st)))
+        m = nd.value
+        return out, op.head(m), oe.head(m), st.as_dict()
 
     def field(self, xyzt, precision=A.PREC_FP64, grad=True):
         """B, dB/dx, V, E at (x, y, z, t) rows; grad=False evaluates B on the
