@@ -420,6 +420,16 @@ typedef struct pt_source_params {
 pt_status pt_source_volume(pt_ctx *ctx, const pt_source_params *sp, int64_t n, const int64_t *ids, pt_particles *out,
                            double *vmin);
 
+/* MicroRoughness of n wall contacts with the kernels' own code (MR::MRDist,
+ * MRProb, MRDistMax, src/microroughness.cpp:35-132; no entry point of the
+ * reference): what 0 = MRDist at (theta[i], phi[i]) (with `integral`: its
+ * phi integral times sin theta), 1 = MRProb, 2 = MRDistMax; v and normal
+ * 3n, Estep [eV], b and w [m] per contact; out[i] NaN where MRProb's
+ * integration failed.  theta and phi may be NULL unless what == 0. */
+pt_status pt_mr_eval(pt_ctx *ctx, int32_t what, int32_t transmit, int32_t integral, int64_t n, const double *v,
+                     const double *normal, const double *Estep, const double *b, const double *w, const double *theta,
+                     const double *phi, double *out);
+
 /* TNeutron::Decay (src/neutron.cpp:285-375) on the device: for n decayed
  * neutrons (ids, decay times t, end states y: 9n SoA, host buffers) the
  * proton and the electron each makes, written to protons / electrons (n

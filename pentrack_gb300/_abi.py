@@ -159,6 +159,8 @@ def declare(lib):
                                                       c_double_p, c_int32_p, c_double_p]),
         "pt_point_solids": (C.c_int32, [vp, C.c_int64, c_double_p, c_uint64_p]),
         "pt_source_volume": (C.c_int32, [vp, P(SourceParams), C.c_int64, c_int64_p, P(Particles), c_double_p]),
+        "pt_mr_eval": (C.c_int32, [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int64, c_double_p, c_double_p, c_double_p,
+                                   c_double_p, c_double_p, c_double_p, c_double_p, c_double_p]),
         "pt_neutron_decay": (C.c_int32, [vp, C.c_uint64, C.c_int64, c_int64_p, c_double_p, c_double_p, P(Particles),
                                          P(Particles)]),
         "pt_integrate_secondaries": (C.c_int32, [vp, P(RunParams), P(RunParams), P(RunParams), P(Particles), P(Particles),

@@ -1944,6 +1944,28 @@ pt_status pt_integrate_secondaries(pt_ctx *c, const pt_run_params *pn, const pt_
     return PT_OK;
 }
 
+pt_status pt_mr_eval(pt_ctx *c, int32_t what, int32_t transmit, int32_t integral, int64_t n, const double *v, const double *normal,
+                     const double *Estep, const double *b, const double *w, const double *theta, const double *phi, double *out) {
+    if (!c || n < 0 || what < 0 || what > 2) return PT_ERR_INVALID;
+    if (n == 0) return PT_OK;
+    if (!v || !normal || !Estep || !b || !w || !out || (what == 0 && (!theta || !phi))) return PT_ERR_INVALID;
+    cudaSetDevice(c->device);
+    std::vector<void *> tmp;
+    cudaError_t e = cudaSuccess;
+    const double *dv = dupload(tmp, v, 3 * n, e), *dn = dupload(tmp, normal, 3 * n, e), *dE = dupload(tmp, Estep, n, e);
+    const double *db = dupload(tmp, b, n, e), *dw = dupload(tmp, w, n, e);
+    const double *dth = what == 0 ? dupload(tmp, theta, n, e) : nullptr, *dph = what == 0 ? dupload(tmp, phi, n, e) : nullptr;
+    double *dout = dalloc<double>(tmp, n, e);
+    if (e) { free_list(tmp); return ck(c, e, "mr alloc"), PT_ERR_OOM; }
+    k_mr<<<grid_for(n, 64), 64, 0, c->stream>>>(what, transmit, integral, n, dv, dn, dE, db, dw, dth, dph, dout);
+    e = cudaGetLastError();
+    if (!e) e = cudaMemcpyAsync(out, dout, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaStreamSynchronize(c->stream);
+    free_list(tmp);
+    if (e) return ck(c, e, "mr eval"), PT_ERR_CUDA;
+    return PT_OK;
+}
+
 pt_status pt_point_solids(pt_ctx *c, int64_t n, const double *p, uint64_t *mask) {
     if (!c || n < 0 || !mask) return PT_ERR_INVALID;
     if (n == 0) return PT_OK;

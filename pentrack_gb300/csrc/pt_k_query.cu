@@ -50,6 +50,24 @@ __global__ void k_field(const __grid_constant__ DScene S, int prec, int64_t n, c
     if (E) for (int k = 0; k < 3; ++k) E[3 * i + k] = e[k];
 }
 
+/* MicroRoughness of wall contacts: what 0 MRDist at (theta, phi), 1 MRProb
+ * (NaN when the integration fails), 2 MRDistMax */
+__global__ void k_mr(int what, int transmit, int integral, int64_t n, const double *v, const double *nrm, const double *Estep,
+                     const double *b, const double *w, const double *theta, const double *phi, double *out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    MRHit h;
+    mr_setup(h, v + 3 * i, nrm + 3 * i, Estep[i], b[i], w[i]);
+    double r;
+    if (what == 0) r = mr_dist(h, transmit != 0, integral != 0, theta[i], phi[i]);
+    else if (what == 1) {
+        bool ok = true;
+        r = mr_prob(h, transmit != 0, ok);
+        if (!ok) r = __longlong_as_double(0x7ff8000000000000ll);
+    } else r = mr_distmax(h, transmit != 0);
+    out[i] = r;
+}
+
 __global__ void k_collisions(const __grid_constant__ DScene S, int64_t n, const double *seg, int maxh, int *count, double *s, double *nrm, int *sid,
                              double *dn) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -57,6 +57,8 @@ __global__ void k_plain(const __grid_constant__ DScene S, const __grid_constant_
 __global__ void k_plain_spin(const __grid_constant__ DScene S, const __grid_constant__ DRun R, const __grid_constant__ DBatch b, DCounters *C, int steps,
                              int budget_from_nacc0);
 __global__ void k_fp64_probe(double *out, int iters, double a, double b);
+__global__ void k_mr(int what, int transmit, int integral, int64_t n, const double *v, const double *nrm, const double *Estep,
+                     const double *b, const double *w, const double *theta, const double *phi, double *out);
 __global__ void k_field(const __grid_constant__ DScene S, int prec, int64_t n, const double *xyzt, double *B, double *dB, double *V, double *E);
 __global__ void k_collisions(const __grid_constant__ DScene S, int64_t n, const double *seg, int maxh, int *count, double *s, double *nrm, int *sid,
                              double *dn);

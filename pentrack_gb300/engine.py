@@ -383,6 +383,22 @@ class Engine:
             raise ValueError("pt_adjoint differentiates a harmonic-expansion field")
         return [f.g[k] for k in range(f.n_coeff)]
 
+    def mr(self, what, v, normal, Estep, b, w, transmit=False, integral=False, theta=None, phi=None):
+        """pt_mr_eval over contacts: v, normal (n, 3); Estep, b, w (n,) or
+        scalars; what = "dist" (with theta, phi), "prob" or "max"."""
+        v = np.ascontiguousarray(np.atleast_2d(v), dtype=np.float64)
+        n = len(v)
+        arr = lambda a: np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64), (n,)))  # noqa: E731
+        nr = np.ascontiguousarray(np.broadcast_to(np.asarray(normal, dtype=np.float64), (n, 3)))
+        E, bb, ww = arr(Estep), arr(b), arr(w)
+        th = arr(0.0 if theta is None else theta)
+        ph = arr(0.0 if phi is None else phi)
+        out = np.zeros(n)
+        k = {"dist": 0, "prob": 1, "max": 2}[what]
+        self._check(lib().pt_mr_eval(self.h, k, int(transmit), int(integral), n, _dp(v), _dp(nr), _dp(E), _dp(bb), _dp(ww),
+                                     _dp(th), _dp(ph), _dp(out)))
+        return out
+
     def neutron_decay(self, seed, neutrons, which=None):
         """pt_neutron_decay: the protons and electrons of the decayed neutrons of
         a tracked set (stop ID ID_DECAYED, or the indices `which`), made on the

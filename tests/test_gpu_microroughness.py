@@ -1,5 +1,9 @@
 """MicroRoughness walls on the device (needs a GB300) against the oracle.
 
+* The kernels' MRDist, MRProb and MRDistMax (pt_mr_eval) equal the oracle's
+  (1e-12; integrals and maxima 1e-9) and reproduce the reference's Steyerl
+  copper known answers with its tolerances.
+
 * A rough floor below the UCN's energies (tests/test_microroughness.py's
   box, 1,500 UCN x 3 s): the plain and batched forms are identical; the
   diffuse fraction of the GPU's floor contacts equals their mean MRProb
@@ -19,7 +23,32 @@ from pentrack_gb300 import _abi as A
 
 pytestmark = pytest.mark.gpu
 
-from test_microroughness import floor_contacts, rough_box_run  # noqa: E402
+from test_microroughness import check_steyerl, contacts, floor_contacts, rough_box_run  # noqa: E402
+
+
+def test_device_mr_functions_equal_oracle_and_steyerl(built, oracle_mod):
+    """pt_mr_eval (the kernels' own MRDist / MRProb / MRDistMax) against the
+    oracle's restatement (std::complex, the library I0) at random contacts,
+    and against the reference's Steyerl copper known answers"""
+    from pentrack_gb300 import Engine
+    from test_opera2d import table_scene
+    e = Engine(table_scene(np.linspace(0, 1, 3), np.linspace(0, 1, 3), bz=np.zeros((3, 3))))
+    rng = np.random.default_rng(2)
+    cs = contacts(seed=6, n=64)
+    for transmit in (False, True):
+        for integral in (False, True):
+            th, ph = rng.uniform(0, np.pi / 2, len(cs)), rng.uniform(0, 2 * np.pi, len(cs))
+            g = e.mr("dist", [c[0] for c in cs], [c[1] for c in cs], [c[2] for c in cs], [c[3] for c in cs],
+                     [c[4] for c in cs], transmit, integral, th, ph)
+            o = np.array([oracle_mod.mr("dist", *c, transmit, integral, th[i], ph[i]) for i, c in enumerate(cs)])
+            np.testing.assert_allclose(g, o, rtol=1e-12, atol=1e-300)
+        for what in ("prob", "max"):
+            g = e.mr(what, [c[0] for c in cs], [c[1] for c in cs], [c[2] for c in cs], [c[3] for c in cs],
+                     [c[4] for c in cs], transmit)
+            o = np.array([oracle_mod.mr(what, *c, transmit) for c in cs])
+            np.testing.assert_allclose(g, o, rtol=1e-9, atol=1e-300)
+    check_steyerl(lambda tr, v, n, E, b, w, th, ph: e.mr("dist", v, n, E, b, w, tr, False, th, ph)[0],
+                  lambda tr, v, n, E, b, w: e.mr("prob", v, n, E, b, w, tr)[0])
 
 
 def run_both(sc, params, parts, oracle_mod):

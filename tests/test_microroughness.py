@@ -1,6 +1,8 @@
 """MicroRoughness (src/microroughness.cpp, TNeutron::OnHit's MR branches) in
 the oracle, on the CPU.
 
+* Steyerl's copper data, the reference's own MicroRoughness known answers
+  (test/microroughnessTests.cpp, with its tolerances).
 * MRDist against the reference's formula written out here with numpy complex
   numbers and scipy's I0, for reflection and transmission, with and
   without the phi integration.
@@ -71,6 +73,49 @@ def contacts(seed=3, n=40):
         out.append((v, np.array([0.0, 0.0, 1.0]), rng.choice([250e-9, 90e-9, -40e-9]), rng.uniform(0.5e-9, 3e-9),
                     rng.uniform(5e-9, 40e-9)))
     return out
+
+
+def steyerl_cases():
+    """the reference's MicroRoughness known answers (test/microroughnessTests.cpp,
+    Steyerl's copper data; tests/golden/steyerl_mr.npz by gen_mr_fixture.py)"""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "steyerl_mr.npz"))
+    kCu, b, w = float(g["kCu"]), float(g["bCu"]), float(g["wCu"])
+    fermi = HBAR * HBAR * kCu * kCu / 2.0 / M_N / ELE_E / ELE_E
+    vabs = 2.0 * np.pi * HBAR / M_N / ELE_E / float(g["wavelength"])
+    th = float(g["theta_i"])
+    v = np.array([vabs * np.sin(th), 0.0, vabs * np.cos(th)])
+    normal = np.array([0.0, 0.0, -1.0])
+    totals = []
+    for lam, p in g["total"]:
+        k = 2.0 * np.pi / lam / 1e-10
+        ti = np.arccos(2.0 / 3.0 * kCu / k) if k > kCu else 48.0 / 180.0 * np.pi
+        va = HBAR * k / M_N / ELE_E
+        totals.append((np.array([va * np.sin(ti), 0.0, va * np.cos(ti)]), p))
+    return dict(v=v, normal=normal, fermi=fermi, b=b, w=w, reflection=g["reflection"], transmission=g["transmission"],
+                totals=totals)
+
+
+def check_steyerl(dist, prob):
+    """the reference's tolerances: a distribution value above 0.01 within 20 %
+    of the iso-line's level, below it within 0.005; the total diffuse
+    probability (reflection + transmission) within 2 %"""
+    c = steyerl_cases()
+    for transmit, table in ((False, c["reflection"]), (True, c["transmission"])):
+        for level, th, ph in table:
+            d = dist(transmit, c["v"], c["normal"], c["fermi"], c["b"], c["w"], th / 180 * np.pi, ph / 180 * np.pi)
+            if d > 0.01:
+                assert abs(d - level) <= 0.2 * level, (transmit, level, th, ph, d)
+            else:
+                assert abs(d - level) <= 0.005, (transmit, level, th, ph, d)
+    for v, p in c["totals"]:
+        r = prob(False, v, c["normal"], c["fermi"], c["b"], c["w"]) + prob(True, v, c["normal"], c["fermi"], c["b"], c["w"])
+        assert abs(r - p) <= 0.02 * p, (p, r)
+
+
+def test_oracle_reproduces_steyerl_copper_data(oracle_mod):
+    check_steyerl(lambda tr, v, n, E, b, w, th, ph: oracle_mod.mr("dist", v, n, E, b, w, tr, False, th, ph),
+                  lambda tr, v, n, E, b, w: oracle_mod.mr("prob", v, n, E, b, w, tr))
 
 
 def test_mr_dist_matches_the_reference_formula(oracle_mod):
