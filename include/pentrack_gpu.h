@@ -386,7 +386,7 @@ pt_status pt_point_solids(pt_ctx *ctx, int64_t n, const double *p, uint64_t *mas
  * TSTLVolumeSource: include/source.h:186-331), with or without
  * PhaseSpaceWeighting, with a flat energy spectrum, the azimuth uniform and
  * the polar angle sine-distributed, the start time uniform. */
-enum { PT_SOURCE_BOX = 0, PT_SOURCE_CYLINDER = 1, PT_SOURCE_SOLID = 2, PT_SOURCE_SURFACE_CYLINDER = 3 };
+enum { PT_SOURCE_BOX = 0, PT_SOURCE_CYLINDER = 1, PT_SOURCE_SOLID = 2, PT_SOURCE_SURFACE_CYLINDER = 3, PT_SOURCE_SURFACE_STL = 4 };
 typedef struct pt_source_params {
     int32_t species;
     int32_t shape;             /* PT_SOURCE_* */
@@ -408,9 +408,13 @@ typedef struct pt_source_params {
      * 255-283): a point on the scene's surfaces inside the cylinder's r, phi, z
      * ranges, moved 1e-8 m off the surface along the face normal, a
      * cos(theta) sin(theta) direction about the normal, the normal energy
-     * raised by enormal [eV].  (TSTLSurfaceSource's region is an STL that is
-     * not part of the geometry: it stays host-side, pentrack_gb300/sources.py.) */
+     * raised by enormal [eV]. */
     double enormal;
+    /* PT_SOURCE_SURFACE_STL (TSTLSurfaceSource, include/source.h:287-298):
+     * the same on the scene's surfaces inside an STL that is not part of the
+     * geometry, given as a context on the same device whose scene holds that
+     * STL as solid index 1 (its triangles' box is the source box) */
+    const struct pt_ctx *region;
 } pt_source_params;
 
 /* n particles with ids `ids` from the source: out->id, t, y (9n) and spin

@@ -87,7 +87,7 @@ class Particles(C.Structure):
     ]
 
 
-SOURCE_BOX, SOURCE_CYLINDER, SOURCE_SOLID, SOURCE_SURFACE_CYLINDER = 0, 1, 2, 3
+SOURCE_BOX, SOURCE_CYLINDER, SOURCE_SOLID, SOURCE_SURFACE_CYLINDER, SOURCE_SURFACE_STL = 0, 1, 2, 3, 4
 LOG_HIT, LOG_SNAPSHOT, LOG_TRACK, LOG_SPIN = 0, 1, 2, 3
 HIT_RECORD, SNAPSHOT_RECORD, TRACK_RECORD, SPIN_RECORD = 18, 22, 10, 14
 
@@ -102,7 +102,7 @@ class SourceParams(C.Structure):
         ("emin", C.c_double), ("emax", C.c_double), ("polarization", C.c_double), ("tmin", C.c_double),
         ("tmax", C.c_double), ("thetamin", C.c_double), ("thetamax", C.c_double), ("phimin_v", C.c_double),
         ("phimax_v", C.c_double), ("n_min_samples", C.c_int64), ("max_rounds", C.c_int32), ("reserved", C.c_int32),
-        ("enormal", C.c_double),
+        ("enormal", C.c_double), ("region", C.c_void_p),
     ]
 
 

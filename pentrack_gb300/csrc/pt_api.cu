@@ -1700,8 +1700,13 @@ pt_status pt_probe_fp64(pt_ctx *c, double *tflops) {
 pt_status pt_source_volume(pt_ctx *c, const pt_source_params *sp, int64_t n, const int64_t *ids, pt_particles *out, double *vmin_out) {
     if (!c || !sp || n < 0 || (n && (!ids || !out || !out->id || !out->t || !out->y || !out->spin))) return PT_ERR_INVALID;
     if (sp->species < PT_NEUTRON || sp->species > PT_ELECTRON) { c->err = "pt_source_volume: unknown species"; return PT_ERR_INVALID; }
-    if (sp->shape < PT_SOURCE_BOX || sp->shape > PT_SOURCE_SURFACE_CYLINDER) { c->err = "pt_source_volume: unknown shape"; return PT_ERR_INVALID; }
-    const bool surface = sp->shape == PT_SOURCE_SURFACE_CYLINDER;
+    if (sp->shape < PT_SOURCE_BOX || sp->shape > PT_SOURCE_SURFACE_STL) { c->err = "pt_source_volume: unknown shape"; return PT_ERR_INVALID; }
+    const bool surface = sp->shape == PT_SOURCE_SURFACE_CYLINDER || sp->shape == PT_SOURCE_SURFACE_STL;
+    const pt_ctx *reg = sp->shape == PT_SOURCE_SURFACE_STL ? sp->region : nullptr;
+    if (sp->shape == PT_SOURCE_SURFACE_STL && (!reg || reg->device != c->device || reg->scene.n_solids < 2 || reg->host_tris.empty())) {
+        c->err = "pt_source_volume: the STL surface source needs a region context on the same device with the STL as solid 1";
+        return PT_ERR_INVALID;
+    }
     if (surface && sp->phase_space) { c->err = "pt_source_volume: phase-space weighting applies to volume sources"; return PT_ERR_INVALID; }
     if (sp->shape == PT_SOURCE_SOLID && (sp->solid < 1 || sp->solid >= c->scene.n_solids)) {
         c->err = "pt_source_volume: solid must index a scene solid other than the default one";
@@ -1721,7 +1726,16 @@ pt_status pt_source_volume(pt_ctx *c, const pt_source_params *sp, int64_t n, con
     std::vector<void *> tmp;
     cudaError_t e = cudaSuccess;
     if (surface) { /* RandomPointOnSurface's candidates: the meshes whose box meets the source box */
-        const double blo[3] = {-sp->rmax, -sp->rmax, sp->zmin}, bhi[3] = {sp->rmax, sp->rmax, sp->zmax};
+        double blo[3] = {-sp->rmax, -sp->rmax, sp->zmin}, bhi[3] = {sp->rmax, sp->rmax, sp->zmax};
+        if (reg) { /* the region STL's box (TSTLSurfaceSource, include/source.h:292-296) */
+            for (int a = 0; a < 3; ++a) { blo[a] = INFINITY; bhi[a] = -INFINITY; }
+            for (size_t k = 0; k < reg->host_tris.size(); ++k) {
+                blo[k % 3] = std::min(blo[k % 3], reg->host_tris[k]);
+                bhi[k % 3] = std::max(bhi[k % 3], reg->host_tris[k]);
+            }
+            Q.region = dupload(tmp, &reg->scene, 1, e);
+            if (e) { free_list(tmp); return ck(c, e, "region upload"), PT_ERR_OOM; }
+        }
         std::vector<double> tri, cum;
         const int64_t nt = (int64_t)c->host_tri_solid.size();
         double run = 0;

@@ -252,6 +252,7 @@ struct DSourceSpec {
      * order) and their cumulative areas */
     const double *surf_tri, *surf_cum;
     int n_surf, pad;
+    const DScene *region; /* STL surface source: the region's scene (solid index 1), device copy */
 };
 
 /* device event counters (one set per launch, summed with atomics per block) */

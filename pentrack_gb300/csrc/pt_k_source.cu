@@ -107,6 +107,10 @@ __device__ double speed_of(double E, double m) {
 /* InSourceVolume of TCylindricalSurfaceSource: its r, phi, z ranges
  * (include/source.h:279-283, open bounds) */
 __device__ bool in_surface_region(const DSourceSpec &Q, const double p[3]) {
+    if (Q.shape == PT_SOURCE_SURFACE_STL) { /* TSTLSurfaceSource::InSourceVolume: inside the region STL */
+        QueryStats qs{0, 0};
+        return (point_solids(*Q.region, p, qs) >> 1) & 1ull;
+    }
     const double r = sqrt(p[0] * p[0] + p[1] * p[1]);
     const double ph = atan2(p[1], p[0]);
     return r > Q.rmin && r < Q.rmax && ph > Q.phimin && ph < Q.phimax && p[2] > Q.zmin && p[2] < Q.zmax;

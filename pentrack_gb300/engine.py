@@ -459,14 +459,16 @@ class Engine:
     def source_volume(self, ids, seed, species=A.NEUTRON, shape=A.SOURCE_BOX, lo=(0, 0, 0), hi=(0, 0, 0),
                       cylinder=(0, 0, 0, 0, 0, 0), solid=0, phase_space=False, emin=0.0, emax=0.0, polarization=0.0,
                       t_range=(0.0, 0.0), theta=(0.0, np.pi), phi=(0.0, 2 * np.pi), n_min_samples=100_000,
-                      max_rounds=100_000, enormal=0.0):
+                      max_rounds=100_000, enormal=0.0, region=None):
         """pt_source_volume: initial states of the particles `ids` from a
         cuboid (lo, hi), cylindrical (cylinder = rmin, rmax, phimin, phimax,
         zmin, zmax) or STL volume (scene solid index `solid`, points proposed
         in the box lo..hi), optionally phase-space weighted, or from the
         scene's surfaces inside a cylindrical region (SOURCE_SURFACE_CYLINDER,
-        `cylinder` as above), with the normal energy raised by `enormal`,
-        generated on the device.
+        `cylinder` as above) or inside an STL (SOURCE_SURFACE_STL: `region`
+        an Engine on the same device whose scene holds the STL as solid
+        index 1), with the normal energy raised by `enormal`, generated on the
+        device.
         Returns (ParticleSet, minimum potential or -inf)."""
         ids = np.ascontiguousarray(ids, dtype=np.int64)
         n = len(ids)
@@ -482,6 +484,7 @@ class Engine:
         sp.phimin_v, sp.phimax_v = phi
         sp.n_min_samples, sp.max_rounds = n_min_samples, max_rounds
         sp.enormal = enormal
+        sp.region = region.h if region is not None else None
         out = ParticleSet(n, ids.copy())
         vmin = C.c_double(0)
         P = out.abi(outputs=False)

@@ -119,3 +119,33 @@ def test_cylindrical_surface_source_equals_host(storage):
     same = np.all(dev.y[0:3] == host.y[0:3], axis=0)
     assert same.mean() >= 0.999
     np.testing.assert_allclose(dev.y[3:6, same], host.y[3:6, same], rtol=1e-13, atol=1e-14)
+
+
+def test_stl_surface_source_equals_host(storage):
+    """TSTLSurfaceSource on the device against sources.surface_source: the
+    region is a box STL that is not part of the geometry (an Engine of its
+    own), cutting a band of the storage cylinder's wall and floor; the same
+    criteria as the cylindrical surface source"""
+    from pentrack_gb300 import Engine, Scene, scenes as S, sources
+    sc, e = storage
+    rs = Scene()
+    rs.add_material("m", 0.0)
+    rs.add_solid(1, "m")
+    box = S.box_mesh((-0.25, -0.07, -0.06), (0.05, 0.23, 0.02))
+    rs.add_solid(2, "m", box)
+    region = Engine(rs)
+    tri = box.reshape(-1, 3, 3)
+    bbox = (tri.min(axis=(0, 1)), tri.max(axis=(0, 1)))
+    ids = np.arange(5 * N, 6 * N, dtype=np.int64)
+    dev, _ = e.source_volume(ids, SEED, shape=A.SOURCE_SURFACE_STL, region=region, emin=0.0, emax=100e-9,
+                             polarization=-0.3, t_range=(0.0, 2.0), enormal=10e-9)
+    host = sources.surface_source(SEED, ids, sc, sources.solid_inside(region.point_solids, 1), bbox, 0.0, 100e-9,
+                                  enormal=10e-9, polarization=-0.3, t_range=(0.0, 2.0))
+    np.testing.assert_array_equal(dev.t, host.t)
+    np.testing.assert_array_equal(dev.y[7], host.y[7])
+    same = np.all(dev.y[0:3] == host.y[0:3], axis=0)
+    assert same.mean() >= 0.999
+    np.testing.assert_allclose(dev.y[3:6, same], host.y[3:6, same], rtol=1e-13, atol=1e-14)
+    inside = sources.solid_inside(region.point_solids, 1)(dev.y[0:3].T)
+    assert inside.mean() > 0.999
+
