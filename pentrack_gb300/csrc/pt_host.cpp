@@ -209,6 +209,67 @@ bool read_opera3d(const std::string &path, double lengthconv, Table3 &t, std::st
     return true;
 }
 
+bool read_comsol(const std::string &path, double lengthconv, Table3 &t, std::string &err) {
+    const std::string ext = fs::path(path).extension().string();
+    if (ext == ".gz" || ext == ".bz2") {
+        err = path + ": compressed tables are not supported; decompress the file first";
+        return false;
+    }
+    std::ifstream in(path);
+    if (!in) {
+        err = "Could not open " + path;
+        return false;
+    }
+    std::vector<double> pts; /* x y z bx by bz per point */
+    std::string line;
+    long num = 0;
+    while (std::getline(in, line)) {
+        ++num;
+        if (!line.empty() && (line[0] == '%' || line[0] == '#')) continue;
+        for (char &ch : line)
+            if (ch == ',' || ch == '\t' || ch == '\r') ch = ' ';
+        std::istringstream ss(line);
+        std::vector<double> v;
+        double x;
+        while (ss >> x) v.push_back(x);
+        if (v.empty()) continue;
+        if (v.size() != 6) {
+            err = "Error reading line " + std::to_string(num) + " of file " + path;
+            return false;
+        }
+        for (int k = 0; k < 3; ++k) v[k] *= lengthconv;
+        pts.insert(pts.end(), v.begin(), v.end());
+    }
+    const size_t np = pts.size() / 6;
+    if (np == 0) {
+        err = "No data read from " + path;
+        return false;
+    }
+    for (int a = 0; a < 3; ++a) {
+        std::vector<double> &ax = t.ax[a];
+        ax.resize(np);
+        for (size_t i = 0; i < np; ++i) ax[i] = pts[6 * i + a];
+        std::sort(ax.begin(), ax.end());
+        ax.erase(std::unique(ax.begin(), ax.end()), ax.end());
+    }
+    const size_t nx = t.ax[0].size(), ny = t.ax[1].size(), nz = t.ax[2].size();
+    if (nx * ny * nz != np || nx < 2 || ny < 2 || nz < 2) {
+        err = path + ": the points do not fill a rectilinear grid";
+        return false;
+    }
+    auto index = [](const std::vector<double> &ax, double x) { return (size_t)(std::lower_bound(ax.begin(), ax.end(), x) - ax.begin()); };
+    t.bx.assign(np, 0.0);
+    t.by.assign(np, 0.0);
+    t.bz.assign(np, 0.0);
+    for (size_t i = 0; i < np; ++i) {
+        const size_t o = (index(t.ax[0], pts[6 * i]) * ny + index(t.ax[1], pts[6 * i + 1])) * nz + index(t.ax[2], pts[6 * i + 2]);
+        t.bx[o] = pts[6 * i + 3];
+        t.by[o] = pts[6 * i + 4];
+        t.bz[o] = pts[6 * i + 5];
+    }
+    return true;
+}
+
 bool read_opera2d(const std::string &path, double lengthconv, Table3 &t, std::string &err) {
     const std::string ext = fs::path(path).extension().string();
     if (ext == ".gz" || ext == ".bz2") {
@@ -432,6 +493,29 @@ pt_status load_scene(const std::string &config_path, SceneStore &S, std::string 
             f.bz = t->bz.empty() ? nullptr : t->bz.data();
             f.v = t->v.empty() ? nullptr : t->v.data();
             /* the container box is the table's extent (src/field_3d.cpp:308) */
+            f.xmax = t->ax[0].back(); f.xmin = t->ax[0].front();
+            f.ymax = t->ax[1].back(); f.ymin = t->ax[1].front();
+            f.zmax = t->ax[2].back(); f.zmin = t->ax[2].front();
+            S.tables.push_back(std::move(t));
+        } else if (type == "COMSOL") {
+            /* ReadComsolField (src/field_3d.cpp:124-183): B only, box = the data's extent */
+            std::string file, bs;
+            double bw = 0, lconv = 1;
+            if (!(ss >> file >> bs >> bw >> lconv)) {
+                err = "Could not read all required parameters for field " + type + "!";
+                return PT_ERR_INVALID;
+            }
+            double b = 0;
+            if (!constant_scale(bs, cfg, b, err)) return PT_ERR_UNSUPPORTED;
+            auto t = std::make_unique<Table3>();
+            if (!read_comsol(relative_to(config_path, file).string(), lconv, *t, err)) return PT_ERR_IO;
+            f.type = PT_FIELD_TAB3D;
+            f.b_scale = b;
+            f.e_scale = 0;
+            f.boundary_width = bw;
+            f.nx = (int32_t)t->ax[0].size(); f.ny = (int32_t)t->ax[1].size(); f.nz = (int32_t)t->ax[2].size();
+            f.x = t->ax[0].data(); f.y = t->ax[1].data(); f.z = t->ax[2].data();
+            f.bx = t->bx.data(); f.by = t->by.data(); f.bz = t->bz.data(); f.v = nullptr;
             f.xmax = t->ax[0].back(); f.xmin = t->ax[0].front();
             f.ymax = t->ax[1].back(); f.ymin = t->ax[1].front();
             f.zmax = t->ax[2].back(); f.zmin = t->ax[2].front();

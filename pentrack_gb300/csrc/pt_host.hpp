@@ -43,6 +43,10 @@ struct Table3 {
     std::vector<double> er, ephi, ez; /* 2D tables only */
 };
 bool read_opera3d(const std::string &path, double lengthconv, Table3 &t, std::string &err);
+/* COMSOL text export (ReadComsolField, src/field_3d.cpp:124-183): lines of x y z Bx By Bz
+ * separated by spaces, tabs or commas, '%' and '#' lines skipped; the points
+ * must fill a rectilinear grid */
+bool read_comsol(const std::string &path, double lengthconv, Table3 &t, std::string &err);
 /* OPERA2D table (TabField::ReadTabFile, src/field_2d.cpp:68-190) into ax[0] = r,
  * ax[2] = z and [ir][iz] columns bx = B_r, by = B_phi, bz = B_z, v, er, ephi, ez */
 bool read_opera2d(const std::string &path, double lengthconv, Table3 &t, std::string &err);

@@ -205,6 +205,35 @@ def read_opera3d(path, lengthconv=1.0):
     return axes, out
 
 
+def read_comsol(path, lengthconv=1.0):
+    """COMSOL text export (ReadComsolField, src/field_3d.cpp:124-183): lines of
+    x y z Bx By Bz separated by spaces, tabs or commas, lines starting with %
+    or # skipped; returns the axes and (nx, ny, nz) arrays BX, BY, BZ."""
+    rows = []
+    with open(path) as f:
+        for num, line in enumerate(f, 1):
+            if line.startswith("%") or line.startswith("#"):
+                continue
+            parts = line.replace(",", " ").replace("\t", " ").split()
+            if not parts:
+                continue
+            if len(parts) != 6:
+                raise ValueError(f"Error reading line {num} of file {path}")
+            rows.append([float(p) for p in parts])
+    data = np.array(rows)
+    xyz = data[:, :3] * lengthconv
+    axes = [np.unique(xyz[:, k]) for k in range(3)]
+    if np.prod([len(a) for a in axes]) != len(data):
+        raise ValueError(f"{path}: the points do not fill a rectilinear grid")
+    idx = [np.searchsorted(axes[k], xyz[:, k]) for k in range(3)]
+    out = {}
+    for c, name in enumerate(("BX", "BY", "BZ")):
+        arr = np.zeros([len(a) for a in axes])
+        arr[idx[0], idx[1], idx[2]] = data[:, 3 + c]
+        out[name] = arr
+    return axes, out
+
+
 def write_opera3d(path, axes, comps):
     """Write an OPERA3D table in metres (lengthconv 1) with the given columns."""
     X, Y, Z = np.meshgrid(*axes, indexing="ij")

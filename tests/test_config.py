@@ -186,6 +186,41 @@ def test_3dtable_units(built, tmp_path):
     np.testing.assert_allclose(_arr(f.x, f.nx), ax[0] * 0.01, rtol=1e-15)
 
 
+def test_comsol_table(built, tmp_path, oracle_mod):
+    """COMSOL (ReadComsolField, src/field_3d.cpp:124-183): a text export of
+    x y z Bx By Bz with '%' headers and space, tab or comma separators, in
+    any point order, read by the config front end and by scenes.read_comsol
+    into the same TabField3 (B scale, boundary width, coordinate scale; box =
+    the data's extent) -- the same field at random points."""
+    from pentrack_gb300 import ConfigScene, Scene, scenes, workloads
+    ax, comps = workloads.quadrupole_table(8)
+    X, Y, Z = np.meshgrid(*ax, indexing="ij")
+    rows = np.column_stack([X.ravel() * 100, Y.ravel() * 100, Z.ravel() * 100] + [c.ravel() for c in comps[:3]])
+    rows = rows[np.random.default_rng(3).permutation(len(rows))]
+    seps = [" ", "\t", ", "]
+    lines = ["% Model: synthetic", "% x y z VectorX VectorY VectorZ"]
+    lines += [seps[i % 3].join(f"{v:.17g}" for v in r) for i, r in enumerate(rows)]
+    (tmp_path / "comsol.txt").write_text("\n".join(lines) + "\n")
+    (tmp_path / "config.in").write_text("[GLOBAL]\nsimtime 1\n\n[MATERIALS]\ndefault 0 0 0 0 0 0 0 0 0\n\n"
+                                        "[GEOMETRY]\n1 ignored default\n\n[FIELDS]\n1 COMSOL comsol.txt 2 0.01 0.01\n")
+    cs = ConfigScene(tmp_path / "config.in")
+    axes, c = scenes.read_comsol(tmp_path / "comsol.txt", 0.01)
+    for a, b in zip(axes, ax):
+        np.testing.assert_allclose(a, b, rtol=1e-15, atol=1e-17)
+    sc = Scene()
+    sc.add_material("default", 0.0)
+    sc.add_solid(1, "default")
+    sc.add_table3d(*axes, c["BX"], c["BY"], c["BZ"], b_scale=2.0, e_scale=0.0, boundary_width=0.01)
+    rng = np.random.default_rng(4)
+    lo, hi = [a[0] for a in axes], [a[-1] for a in axes]
+    q = np.column_stack([rng.uniform(lo[k] - 0.01, hi[k] + 0.01, 400) for k in range(3)] + [np.zeros(400)])
+    a = oracle_mod.Oracle(cs).field(q)
+    b = oracle_mod.Oracle(sc).field(q)
+    for u, v in zip(a, b):
+        np.testing.assert_array_equal(u, v)
+    assert np.abs(a[0]).max() > 0
+
+
 @pytest.mark.gpu
 def test_config_scene_tracks_like_direct_scene(built, tmp_path):
     from pentrack_gb300 import ConfigScene, Engine, Scene, config_run_params, scenes
