@@ -200,6 +200,11 @@ typedef struct pt_run_params {
      * (TLogger::PrintSpin, src/logger.cpp:237-284) */
     int32_t spinlog, reserved6;
     double spinloginterval;    /* [s] */
+    /* interpolatefields 1 (TTracker::IntegrateSpin, src/tracking.cpp:404-421):
+     * the Bloch integration of a trajectory step takes the precession axis
+     * from cubic splines through its values at 11 equally spaced times of the
+     * step instead of evaluating it at every stage */
+    int32_t interpolatefields, reserved7;
 } pt_run_params;
 
 enum { PT_LOG_HIT = 0, PT_LOG_SNAPSHOT = 1, PT_LOG_TRACK = 2, PT_LOG_SPIN = 3 };

@@ -54,7 +54,7 @@ inline pt_run_params run_params(std::map<std::string, std::string> &conf, double
     std::istringstream(conf["Bmax"]) >> p.bmax;
     int interpolate = 0;
     std::istringstream(conf["interpolatefields"]) >> interpolate;
-    if (interpolate) throw std::runtime_error("TTrackerGPU: interpolatefields 1 is not supported on the device path");
+    p.interpolatefields = interpolate ? 1 : 0;
     spintimes.clear();
     std::istringstream st(conf["spintimes"]);
     double a, b;

@@ -267,6 +267,41 @@ struct Tab3 {
 };
 
 /* ------------------------------------------------------------------ */
+/* ALGLIB spline1dbuildcubic (parabolically terminated ends) and spline1dcalc
+ * (alglib-3.15.0/cpp/src/interpolation.cpp: spline1dbuildhermite
+ * 23642-23710, spline1dcalc 23850-23912), as IntegrateSpin interpolates the
+ * precession axis (src/tracking.cpp:404-421) and SpinDerivs reads it
+ * (src/particle.cpp:180-184).                                             */
+/* ------------------------------------------------------------------ */
+struct Spline1 {
+    std::vector<double> x, c; /* nodes; per interval c0, c1, c2, c3 */
+    void build(int n, const double *xs, const double *ys) {
+        x.assign(xs, xs + n);
+        std::vector<double> d(n);
+        spline_derivs(n, xs, ys, d.data());
+        c.assign((size_t)4 * (n - 1), 0.0);
+        for (int i = 0; i + 1 < n; ++i) {
+            const double delta = xs[i + 1] - xs[i], delta2 = delta * delta, delta3 = delta * delta2;
+            c[4 * i + 0] = ys[i];
+            c[4 * i + 1] = d[i];
+            c[4 * i + 2] = (3 * (ys[i + 1] - ys[i]) - 2 * d[i] * delta - d[i + 1] * delta) / delta2;
+            c[4 * i + 3] = (2 * (ys[i] - ys[i + 1]) + d[i] * delta + d[i + 1] * delta) / delta3;
+        }
+    }
+    double calc(double t) const {
+        int l = 0, r = (int)x.size() - 1;
+        while (l != r - 1) {
+            const int m = (l + r) / 2;
+            if (x[m] >= t) r = m;
+            else l = m;
+        }
+        const double u = t - x[l];
+        const double *k = &c[4 * l];
+        return k[0] + u * (k[1] + u * (k[2] + u * k[3]));
+    }
+};
+
+/* ------------------------------------------------------------------ */
 /* TabField (src/field_2d.cpp:232-399): ALGLIB bicubic spline2d in (r, z),
  * restated from alglib-3.15.0/cpp/src/interpolation.cpp:
  *   spline2dbuildbicubicv / spline2d_bicubiccalcderivatives (44925-45080,
@@ -1147,13 +1182,21 @@ struct Tracker {
     }
     /* TParticle::SpinDerivs (src/particle.cpp:178-193) along the trajectory's
      * dense output: dS/dt = Omega x S, integrated time, integrated phase */
-    void spin_derivs(const double *S, double *dS, double t) {
-        double y[9], dydt[9], B[3], dB[3][3], V, E[3], W[3];
+    void spin_axis_at(double t, double W[3]) {
+        double y[9], dydt[9], B[3], dB[3][3], V, E[3];
         st.calc_state(t, y);
         bfield(y[0], y[1], y[2], t, B, dB);
         efield(y[0], y[1], y[2], t, V, E);
         eom(y, dydt, B, dB, E);
         spin_axis(B, E, dydt, W);
+    }
+    const Spline1 *omega = nullptr; /* interpolatefields: the axis splines of the current step */
+    void spin_derivs(const double *S, double *dS, double t) {
+        double W[3];
+        if (omega)
+            for (int k = 0; k < 3; ++k) W[k] = omega[k].calc(t);
+        else
+            spin_axis_at(t, W);
         dS[0] = W[1] * S[2] - W[2] * S[1];
         dS[1] = W[2] * S[0] - W[0] * S[2];
         dS[2] = W[0] * S[1] - W[1] * S[0];
@@ -1595,6 +1638,24 @@ struct Tracker {
             if (i1 || i2) {
                 /* LOOP D: a fresh dopri5 dense-output stepper (abs = rel = 1e-12)
                  * started with half a Larmor turn as its step */
+                Spline1 om[3];
+                if (P.interpolatefields) { /* the axis at 11 times of the step, one cubic spline per component */
+                    const int int_points = 10;
+                    double ts[int_points + 1], w[3][int_points + 1];
+                    for (int i = 0; i <= int_points; ++i) {
+                        const double t = x1 + i * (x2 - x1) / int_points;
+                        ts[i] = t;
+                        double W[3];
+                        spin_axis_at(t, W);
+                        for (int k = 0; k < 3; ++k) w[k][i] = W[k];
+                    }
+                    for (int k = 0; k < 3; ++k) om[k].build(int_points + 1, ts, w[k]);
+                }
+                struct OmegaScope {
+                    const Spline1 *&slot;
+                    OmegaScope(const Spline1 *&s_, const Spline1 *v) : slot(s_) { slot = v; }
+                    ~OmegaScope() { slot = nullptr; }
+                } scope(omega, P.interpolatefields ? om : nullptr);
                 if (spin[0] == 0 && spin[1] == 0 && spin[2] == 0)
                     for (int k = 0; k < 3; ++k) spin[k] = B1[k] * y1[7] / Babs1;
                 Dense5<5> ss(1e-12, 1e-12);
@@ -1962,6 +2023,15 @@ int pto_segment_collisions(pto_ctx *ctx, int64_t n, const double *seg, int32_t m
 
 int pto_point_solids(pto_ctx *ctx, int64_t n, const double *p, uint64_t *mask) {
     for (int64_t i = 0; i < n; ++i) mask[i] = ctx->sc.point_solids(p + 3 * i);
+    return 0;
+}
+
+/* Spline1 (the interpolatefields axis spline) at np points */
+int pto_spline1d_calc(int32_t n, const double *x, const double *y, int32_t np, const double *pts, double *out) {
+    if (n < 2) return PT_ERR_INVALID;
+    Spline1 s;
+    s.build(n, x, y);
+    for (int32_t k = 0; k < np; ++k) out[k] = s.calc(pts[k]);
     return 0;
 }
 

@@ -52,6 +52,7 @@ int pto_point_solids(pto_ctx *ctx, int64_t n, const double *p, uint64_t *mask);
 
 /* building blocks exposed for the golden-vector tests */
 int pto_spline_derivs(int32_t n, const double *x, const double *y, double *d);
+int pto_spline1d_calc(int32_t n, const double *x, const double *y, int32_t np, const double *pts, double *out);
 double pto_mr(int32_t what, int32_t transmit, int32_t integral, const double *v, const double *normal, double Estep, double b,
               double w, double theta, double phi);
 void pto_tricubic_coeff(const double *stacked64, double *a64);

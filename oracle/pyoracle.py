@@ -34,6 +34,7 @@ def lib():
         L.pto_segment_collisions.argtypes = [vp, C.c_int64, dp, C.c_int32, A.c_int32_p, dp, dp, A.c_int32_p, dp]
         L.pto_point_solids.argtypes = [vp, C.c_int64, dp, A.c_uint64_p]
         L.pto_spline_derivs.argtypes = [C.c_int32, dp, dp, dp]
+        L.pto_spline1d_calc.argtypes = [C.c_int32, dp, dp, C.c_int32, dp, dp]
         L.pto_mr.argtypes = [C.c_int32, C.c_int32, C.c_int32, dp, dp, C.c_double, C.c_double, C.c_double, C.c_double,
                              C.c_double]
         L.pto_mr.restype = C.c_double
@@ -63,6 +64,7 @@ def ref_lib():
         R.ref_tricubic_coeff.argtypes = [A.c_double_p, A.c_double_p]
         R.ref_tricubic_eval.argtypes = [A.c_double_p, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int]
         R.ref_tricubic_eval.restype = C.c_double
+        R.ref_spline1d_calc.argtypes = [C.c_int, A.c_double_p, A.c_double_p, C.c_int, A.c_double_p, A.c_double_p]
         R.ref_spline2d.argtypes = [C.c_int, A.c_double_p, C.c_int, A.c_double_p, A.c_double_p, C.c_int, A.c_double_p,
                                    A.c_double_p, A.c_double_p]
         _REF = R
@@ -138,6 +140,14 @@ def mr(what, v, normal, Estep, b, w, transmit=False, integral=False, theta=0.0, 
     n = np.ascontiguousarray(normal, dtype=np.float64)
     k = {"dist": 0, "prob": 1, "max": 2}[what]
     return lib().pto_mr(k, int(transmit), int(integral), _dp(v), _dp(n), Estep, b, w, theta, phi)
+
+
+def spline1d_calc(x, y, pts):
+    """the oracle's cubic spline through (x, y) (spline1dbuildcubic) at pts (spline1dcalc)"""
+    x, y, p = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, pts))
+    out = np.zeros_like(p)
+    lib().pto_spline1d_calc(len(x), _dp(x), _dp(y), len(p), _dp(p), _dp(out))
+    return out
 
 
 def spline_derivs(x, y):

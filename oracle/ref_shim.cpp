@@ -68,4 +68,20 @@ int ref_spline2d(int m, const double *x, int n, const double *y, const double *f
         return -1;
     }
 }
+
+/* IntegrateSpin's axis spline: spline1dbuildcubic(x, y) (the short form,
+ * src/tracking.cpp:419) and spline1dcalc at np points */
+int ref_spline1d_calc(int n, const double *x, const double *y, int np, const double *pts, double *out) {
+    try {
+        alglib::real_1d_array xa, ya;
+        xa.setcontent(n, x);
+        ya.setcontent(n, y);
+        alglib::spline1dinterpolant c;
+        alglib::spline1dbuildcubic(xa, ya, c);
+        for (int k = 0; k < np; ++k) out[k] = alglib::spline1dcalc(c, pts[k]);
+        return 0;
+    } catch (...) {
+        return -1;
+    }
+}
 }

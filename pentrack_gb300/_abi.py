@@ -74,6 +74,7 @@ class RunParams(C.Structure):
         ("reserved4", C.c_int32), ("log_capacity", C.c_int64),
         ("tracklog", C.c_int32), ("reserved5", C.c_int32), ("trackloginterval", C.c_double),
         ("spinlog", C.c_int32), ("reserved6", C.c_int32), ("spinloginterval", C.c_double),
+        ("interpolatefields", C.c_int32), ("reserved7", C.c_int32),
     ]
 
 

@@ -1254,6 +1254,7 @@ pt_status batch_create(pt_ctx *c, const pt_run_params *p, const pt_particles *in
     R.n_spintimes = p->n_spintimes;
     for (int k = 0; k < p->n_spintimes; ++k) R.spintimes[k] = p->spintimes[k];
     R.flipspin = p->flipspin;
+    R.interp = p->interpolatefields != 0;
     R.mode = p->mode;
     R.prec = p->field_precision;
     R.steps_per_launch = p->steps_per_launch > 0 ? p->steps_per_launch : 64;
@@ -1546,6 +1547,10 @@ pt_status pt_adjoint(pt_ctx *c, const pt_run_params *p, const pt_particles *in, 
     if (nc < 1 || nc > PT_ADJ_MAX_COEF) { c->err = "pt_adjoint: 1 to 16 coefficients"; return PT_ERR_UNSUPPORTED; }
     if (p->species != PT_NEUTRON || p->field_precision != PT_PREC_FP64) {
         c->err = "pt_adjoint: neutrons in the FP64 field mode only";
+        return PT_ERR_UNSUPPORTED;
+    }
+    if (p->interpolatefields) {
+        c->err = "pt_adjoint: the exact precession axis only (interpolatefields 0)";
         return PT_ERR_UNSUPPORTED;
     }
     for (int fi = 0; fi < S.n_fields; ++fi) {

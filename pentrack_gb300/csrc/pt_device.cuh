@@ -177,6 +177,7 @@ struct DRun {
     double spintimes[PT_MAX_SPINTIMES];
     int n_spintimes, flipspin, prec, steps_per_launch;
     int mode, max_steps;      /* max_steps: accepted RK steps per particle in one advance call (0 = no limit) */
+    int interp, pad_i;        /* interpolatefields: spline of the precession axis per trajectory step */
     uint64_t seed;
     double t_pause;
     volatile int *cancel;   /* host-mapped cancel word (the reference's quit flag) */

@@ -644,10 +644,7 @@ pt_status load_run_params(const std::string &config_path, const std::string &spe
     p.lmax = num(opt("lmax"), 0);
     p.bmax = num(opt("Bmax"), 0);
     p.flipspin = (int32_t)num(opt("flipspin"), 0);
-    if (num(opt("interpolatefields"), 0) != 0) {
-        err = "interpolatefields 1 is not implemented on the device path";
-        return PT_ERR_UNSUPPORTED;
-    }
+    p.interpolatefields = num(opt("interpolatefields"), 0) != 0 ? 1 : 0;
     spintimes.clear();
     {
         std::istringstream ss(opt("spintimes"));

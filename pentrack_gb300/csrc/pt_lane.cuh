@@ -116,6 +116,8 @@ static __device__ __forceinline__ bool rhs_general(const DScene &S, const DRun &
 /* State of a Bloch (LOOP D) integration between its steps: time, step
  * size, spin state, its FSAL derivative and the precession axis at it, and
  * the accepted steps so far. */
+#define PT_OM_POINTS 10 /* intervals of the precession-axis spline (src/tracking.cpp:409) */
+
 struct BlochState {
     double ts, dt, x[5], dxdt[5], w[3];
     long steps;
@@ -175,11 +177,18 @@ template <class Tape> struct LaneT {
     /* a pending Bloch integration (spin_begin / finish_begin): its stepper,
      * end time, B at the step's end point and the finish_step arguments */
     BlochState bst;
+    /* interpolatefields: the precession axis of the pending Bloch
+     * integration as cubic splines over its trajectory step (times om_t,
+     * per component and interval the coefficients of
+     * c0 + u (c1 + u (c2 + u c3)), u = t - om_t[interval]) */
+    bool om_on;
+    double om_t[PT_OM_POINTS + 1], om_c[3][PT_OM_POINTS][4];
     double bx2, sBabs2, sB2[3], fx;
     double *fyl;
     bool freset;
 
     __device__ LaneT(const DScene &s, const DRun &r) : S(s), R(r) {
+        om_on = false;
         bc_ok[0] = bc_ok[1] = false;
         bc_next = 0;
         ntry = 0;
@@ -485,15 +494,93 @@ template <class Tape> struct LaneT {
         const double cb = -R.sp.gamma * sq, ct = gr * gr / (gr + 1) * PT_INV_C0_SQ;
         for (int j = 0; j < 3; ++j) W[j] = cb * ((1 - gr) * Bpar[j] + gr * B[j] - gr * vxE[j] * PT_INV_C0_SQ) + ct * axv[j];
     }
-    /* TParticle::SpinDerivs (src/particle.cpp:178-193) along the trajectory's dense output */
-    __device__ __noinline__ void spin_derivs(const double *Sv, double *dS, double tt, double *Wout = nullptr) {
-        double yy[9], dydt[9], B[3], dB[3][3], V, E[3], W[3];
+    /* the precession axis at tt from the trajectory's dense output */
+    __device__ void spin_axis_at(double tt, double W[3]) {
+        double yy[9], dydt[9], B[3], dB[3][3], V, E[3];
         calc_spin_state(tt, yy);
         bfield<true>(S, R.prec, yy[0], yy[1], yy[2], B, dB);
         efield(S, R.prec, yy[0], yy[1], yy[2], V, E);
         ++lc.fields;
         eom_fields(yy, B, dB, E, dydt);
         spin_axis(B, E, dydt, W);
+    }
+    /* interpolatefields (src/tracking.cpp:404-421): the axis at x1 + i (x2 -
+     * x1) / 10, i = 0..10, and per component ALGLIB's spline1dbuildcubic with
+     * parabolically terminated ends (the slopes of spline_slopes, the
+     * coefficients as spline1dbuildhermite forms them) */
+    __device__ __noinline__ void omega_spline(double x1, double x2) {
+        const int n = PT_OM_POINTS + 1;
+        double w[3][PT_OM_POINTS + 1];
+        for (int i = 0; i < n; ++i) {
+            const double t = x1 + i * (x2 - x1) / PT_OM_POINTS;
+            om_t[i] = t;
+            double W[3];
+            spin_axis_at(t, W);
+            for (int c = 0; c < 3; ++c) w[c][i] = W[c];
+        }
+        for (int c = 0; c < 3; ++c) {
+            double d[PT_OM_POINTS + 1];
+            spline_slopes(n, om_t, w[c], d);
+            for (int i = 0; i + 1 < n; ++i) {
+                const double delta = om_t[i + 1] - om_t[i], delta2 = delta * delta, delta3 = delta * delta2;
+                om_c[c][i][0] = w[c][i];
+                om_c[c][i][1] = d[i];
+                om_c[c][i][2] = (3 * (w[c][i + 1] - w[c][i]) - 2 * d[i] * delta - d[i + 1] * delta) / delta2;
+                om_c[c][i][3] = (2 * (w[c][i] - w[c][i + 1]) + d[i] * delta + d[i + 1] * delta) / delta3;
+            }
+        }
+        om_on = true;
+    }
+    /* ALGLIB spline1dgriddiffcubic's slopes with parabolically terminated
+     * ends (tridiagonal system, Thomas algorithm in the library's order) */
+    __device__ static void spline_slopes(int n, const double *x, const double *y, double *d) {
+        if (n == 2) {
+            d[0] = (y[1] - y[0]) / (x[1] - x[0]);
+            d[1] = d[0];
+            return;
+        }
+        double a1[PT_OM_POINTS + 1], a2[PT_OM_POINTS + 1], a3[PT_OM_POINTS + 1], b[PT_OM_POINTS + 1];
+        a1[0] = 0; a2[0] = 1; a3[0] = 1;
+        b[0] = 2 * (y[1] - y[0]) / (x[1] - x[0]);
+        for (int i = 1; i <= n - 2; ++i) {
+            a1[i] = x[i + 1] - x[i];
+            a2[i] = 2 * (x[i + 1] - x[i - 1]);
+            a3[i] = x[i] - x[i - 1];
+            b[i] = 3 * (y[i] - y[i - 1]) / (x[i] - x[i - 1]) * (x[i + 1] - x[i]) +
+                   3 * (y[i + 1] - y[i]) / (x[i + 1] - x[i]) * (x[i] - x[i - 1]);
+        }
+        a1[n - 1] = 1; a2[n - 1] = 1; a3[n - 1] = 0;
+        b[n - 1] = 2 * (y[n - 1] - y[n - 2]) / (x[n - 1] - x[n - 2]);
+        for (int k = 1; k <= n - 1; ++k) {
+            const double t = a1[k] / a2[k - 1];
+            a2[k] = a2[k] - t * a3[k - 1];
+            b[k] = b[k] - t * b[k - 1];
+        }
+        d[n - 1] = b[n - 1] / a2[n - 1];
+        for (int k = n - 2; k >= 0; --k) d[k] = (b[k] - a3[k] * d[k + 1]) / a2[k];
+    }
+    /* spline1dcalc of the three axis splines: the interval by the library's
+     * bisection (the last one whose start is below tt, the first at or
+     * below om_t[0]), then Horner in u = tt - its start */
+    __device__ void omega_eval(double tt, double W[3]) const {
+        int l = 0, r = PT_OM_POINTS + 1 - 1;
+        while (l != r - 1) {
+            const int m = (l + r) / 2;
+            if (om_t[m] >= tt) r = m;
+            else l = m;
+        }
+        const double u = tt - om_t[l];
+        for (int c = 0; c < 3; ++c) {
+            const double *k = om_c[c][l];
+            W[c] = k[0] + u * (k[1] + u * (k[2] + u * k[3]));
+        }
+    }
+    /* TParticle::SpinDerivs (src/particle.cpp:178-193) along the trajectory's
+     * dense output, or from the axis splines (interpolatefields) */
+    __device__ __noinline__ void spin_derivs(const double *Sv, double *dS, double tt, double *Wout = nullptr) {
+        double W[3];
+        if (om_on) omega_eval(tt, W);
+        else spin_axis_at(tt, W);
         dS[0] = W[1] * Sv[2] - W[2] * Sv[1];
         dS[1] = W[2] * Sv[0] - W[0] * Sv[2];
         dS[2] = W[0] * Sv[1] - W[1] * Sv[0];
@@ -1055,9 +1142,9 @@ template <class Tape> struct LaneT {
         const double iv = R.log.spin_interval;
         if (!(iv > 0)) return;
         if (x > x1 && (int)(x1 / iv) == (int)(x / iv)) return;
-        double yy[9], dS[5], W[3], B[3], dB[3][3];
+        double yy[9], W[3], B[3], dB[3][3];
         calc_spin_state(x, yy);
-        spin_derivs(Sv, dS, x, W);
+        spin_axis_at(x, W); /* TLogger::PrintSpin evaluates SpinPrecessionAxis itself */
         bfield<true>(S, R.prec, yy[0], yy[1], yy[2], B, dB);
         const unsigned long long k = atomicAdd(R.log.spin_n, 1ull);
         if ((long long)k >= R.log.cap) return;
@@ -1545,6 +1632,8 @@ template <class Tape> struct LaneT {
                 sBabs2 = Babs2;
                 for (int k = 0; k < 3; ++k) sB2[k] = B2[k];
                 bx2 = x2;
+                om_on = false;
+                if (R.interp) omega_spline(to, x2);
                 bloch_begin(bst, to, x2, fabs(PT_PI / R.sp.gamma / Babs1));
                 return 1;
             } else if (spin[0] != 0 || spin[1] != 0 || spin[2] != 0) {

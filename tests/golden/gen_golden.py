@@ -13,6 +13,8 @@ records:
                       STL read from the reference's test/ directory
   alglib_spline2d.npz spline2dbuildbicubicv + spline2ddiff / spline2dcalc on
                       uniform and random (r, z) grids (TabField, src/field_2d.cpp:247-335)
+  alglib_spline1d.npz spline1dbuildcubic + spline1dcalc at random points and
+                      the nodes (IntegrateSpin's axis spline, src/tracking.cpp:404-421)
   opera2d_tables.npz  test/VerticalLinearGradientField2D.tab and
                       test/CosineGradientField.tab read in centimetres
 """
@@ -96,6 +98,18 @@ def main():
         assert R.ref_spline2d(m, dp(x), n, dp(y), dp(fa), len(px), dp(px), dp(py), dp(out)) == 0
         cases.update({f"x{case}": x, f"y{case}": y, f"f{case}": F, f"px{case}": px, f"py{case}": py, f"out{case}": out})
     np.savez_compressed(os.path.join(HERE, "alglib_spline2d.npz"), n_cases=np.array(case + 1), **cases)
+
+    sp1 = {}
+    for case in range(8):
+        n = (2, 3, 5, 11, 11, 11, 7, 11)[case]
+        t0, t1 = rng.uniform(-1, 1), rng.uniform(1e-6, 2.0)
+        x = np.array([t0 + i * (t1 - t0 + 1) / (n - 1) for i in range(n)])  # x1 + i (x2 - x1) / (n - 1), as IntegrateSpin
+        y = rng.normal(size=n) * (10.0 ** rng.integers(-8, 3))
+        pts = np.concatenate([rng.uniform(x[0] - 0.1 * (x[-1] - x[0]), x[-1] + 0.1 * (x[-1] - x[0]), 40), x])
+        out = np.zeros(len(pts))
+        assert R.ref_spline1d_calc(n, dp(x), dp(np.ascontiguousarray(y)), len(pts), dp(pts), dp(out)) == 0
+        sp1.update({f"x{case}": x, f"y{case}": y, f"p{case}": pts, f"v{case}": out})
+    np.savez_compressed(os.path.join(HERE, "alglib_spline1d.npz"), n_cases=np.array(8), **sp1)
 
     tabs = {}
     for key, name in (("linear", "VerticalLinearGradientField2D.tab"), ("cosine", "CosineGradientField.tab")):

@@ -59,3 +59,21 @@ def test_spin_precession_matches_oracle(built, oracle_mod, mode):
     np.testing.assert_allclose(gout.spin[3], t, rtol=1e-12)
     np.testing.assert_allclose(np.sqrt((gout.spin[:3] ** 2).sum(0)), 1.0, atol=1e-8)
     np.testing.assert_allclose(gout.spin[2], 0.0, atol=1e-3)  # tilt of the axis by v x E / c^2 ~ 1e-4
+
+
+def test_interpolated_axis_matches_oracle(built, oracle_mod):
+    """interpolatefields 1 (src/tracking.cpp:404-421): the precession axis
+    from cubic splines through 11 values per trajectory step; GPU against the
+    oracle with the same criteria, and against the exact axis within the
+    interpolation error"""
+    from pentrack_gb300 import Engine
+    sc, params, parts = spin_setup(n=32)
+    exact, _ = Engine(sc).integrate(params, parts)
+    params.interpolatefields = 1
+    oout, ost = oracle_mod.Oracle(sc).integrate(params, parts)
+    gout, gst = Engine(sc).integrate(params, parts)
+    assert ost["spin_steps"] > 500 and abs(gst["spin_steps"] - ost["spin_steps"]) <= 1e-3 * ost["spin_steps"]
+    assert np.array_equal(gout.y, oout.y) and np.array_equal(gout.t, oout.t)
+    assert np.max(np.abs(gout.spin - oout.spin)) < 1e-9
+    assert np.max(np.abs(gout.spin[:3] - exact.spin[:3])) < 1e-6
+    assert np.max(np.abs(gout.spin[4] - exact.spin[4])) < 1e-6 * np.max(exact.spin[4])

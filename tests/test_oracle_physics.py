@@ -236,3 +236,24 @@ def test_exb_drift_is_a_straight_line(oracle_mod):
     np.testing.assert_allclose(out.y[1], parts.y[1] - 1e4 * dt, rtol=0, atol=1e-9)
     np.testing.assert_allclose(out.y[0], parts.y[0], rtol=0, atol=1e-9)
     np.testing.assert_allclose(out.y[3:6], parts.y[3:6], rtol=0, atol=1e-3)
+
+
+def test_interpolated_precession_axis_oracle(oracle_mod):
+    """interpolatefields 1 in the oracle: the spin end states of the spline
+    axis agree with the exact axis within the interpolation error, and the
+    accumulated phase with |gamma_n| B0 t"""
+    import sys
+    import os
+    sys.path.insert(0, os.path.dirname(__file__))
+    from test_gpu_spin import spin_setup
+    from pentrack_gb300 import scenes
+    sc, params, parts = spin_setup(n=6, simtime=0.05)
+    o = oracle_mod.Oracle(sc)
+    exact, _ = o.integrate(params, parts)
+    params.interpolatefields = 1
+    interp, st = o.integrate(params, parts)
+    assert st["spin_steps"] > 100
+    assert np.array_equal(interp.y, exact.y)
+    assert np.max(np.abs(interp.spin[:3] - exact.spin[:3])) < 1e-6
+    w = abs(scenes.GAMMA_N) * 1e-6
+    np.testing.assert_allclose(interp.spin[4], w * (interp.t - parts.t), rtol=1e-6)

@@ -155,3 +155,14 @@ def test_oracle_harmonic_terms_match_reference_closed_forms(oracle_mod):
     assert np.max(np.abs(B - ref)) < 1e-13 * np.abs(ref).max()
     assert np.max(np.abs(np.trace(dB, axis1=1, axis2=2))) < 1e-12
     assert np.max(np.abs(dB - np.transpose(dB, (0, 2, 1)))) < 1e-12
+
+
+def test_axis_spline_matches_alglib_bitwise(oracle_mod):
+    """IntegrateSpin's precession-axis spline (interpolatefields 1):
+    spline1dbuildcubic + spline1dcalc of the reference's ALGLIB
+    (tests/golden/alglib_spline1d.npz) at random points, the nodes and beyond
+    both ends, equal to the oracle's Spline1 bit for bit"""
+    g = np.load(os.path.join(GOLD, "alglib_spline1d.npz"))
+    for k in range(int(g["n_cases"])):
+        v = oracle_mod.spline1d_calc(g[f"x{k}"], g[f"y{k}"], g[f"p{k}"])
+        assert np.array_equal(v, g[f"v{k}"]), k
