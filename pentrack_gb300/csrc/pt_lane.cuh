@@ -177,12 +177,6 @@ template <class Tape> struct LaneT {
     /* a pending Bloch integration (spin_begin / finish_begin): its stepper,
      * end time, B at the step's end point and the finish_step arguments */
     BlochState bst;
-    /* interpolatefields: the precession axis of the pending Bloch
-     * integration as cubic splines over its trajectory step (times om_t,
-     * per component and interval the coefficients of
-     * c0 + u (c1 + u (c2 + u c3)), u = t - om_t[interval]) */
-    bool om_on;
-    double om_t[PT_OM_POINTS + 1], om_c[3][PT_OM_POINTS][4];
     double bx2, sBabs2, sB2[3], fx;
     double *fyl;
     bool freset;
@@ -1943,6 +1937,13 @@ template <class Tape> struct LaneT {
         if (r < 0) { stop = PT_ID_ODEINT_ERROR; return; }
         post_step();
     }
+
+    /* interpolatefields: the precession axis of the pending Bloch
+     * integration as cubic splines over its trajectory step (times om_t,
+     * per component and interval the coefficients of
+     * c0 + u (c1 + u (c2 + u c3)), u = t - om_t[interval]) */
+    bool om_on;
+    double om_t[PT_OM_POINTS + 1], om_c[3][PT_OM_POINTS][4];
 };
 
 using Lane = LaneT<NoTape>;
