@@ -168,3 +168,41 @@ def test_cylindrical_conversion_of_a_rotating_field(oracle_mod):
         d[j] = h
         fd = (o.field(q + d)[0] - o.field(q - d)[0]) / (2 * h)
         np.testing.assert_allclose(dB[:, :, j], fd, atol=1e-6)
+
+
+def test_opera2d_all_columns_and_y_column(tmp_path, oracle_mod):
+    """A table with the optional " 2 Y [LENGU]" coordinate and every field
+    column (RBX, RBY, RBZ, EX, EY, EZ, RV), read by the Python reader and by
+    the config front end into the same field; the E map takes precedence
+    over the potential (src/field_2d.cpp:262-283), so V is zero"""
+    from pentrack_gb300 import scenes as S
+    from pentrack_gb300.engine import ConfigScene
+    r = np.linspace(0.0, 30.0, 7)
+    z = np.linspace(-20.0, 40.0, 9)
+    R, Z = np.meshgrid(r, z, indexing="ij")
+    cols = {"BR": R * Z * 1e-2, "BPHI": R * R * 1e-3, "BZ": np.cos(R / 10) + Z * 1e-2, "ER": R * 3.0, "EPHI": -R,
+            "EZ": Z * 2.0, "V": R + Z}
+    tags = [("RBX", "BR"), ("RBY", "BPHI"), ("RBZ", "BZ"), ("EX", "ER"), ("EY", "EPHI"), ("EZ", "EZ"), ("RV", "V")]
+    lines = [f"{len(r)} 1 {len(z)} 2", " 1 X [LENGU]", " 2 Y [LENGU]", " 3 Z [LENGU]"]
+    lines += [f" {4 + i} {t} [UNIT]" for i, (t, _) in enumerate(tags)]
+    lines.append(" 0")
+    for i in range(len(r)):
+        for j in range(len(z)):
+            lines.append(" ".join(f"{v:.17g}" for v in [r[i], 0.0, z[j]] + [cols[c][i, j] for _, c in tags]))
+    (tmp_path / "t.tab").write_text("\n".join(lines) + "\n")
+    (r2, z2), c2 = S.read_opera2d(str(tmp_path / "t.tab"), 0.01)
+    np.testing.assert_allclose(r2, r * 0.01, rtol=1e-15)
+    np.testing.assert_allclose(z2, z * 0.01, rtol=1e-15, atol=1e-18)
+    for _, c in tags:
+        np.testing.assert_array_equal(c2[c], cols[c])
+    (tmp_path / "config.in").write_text("[GLOBAL]\nsimtime 1\n\n[MATERIALS]\ndefault 0 0 0 0 0 0 0 0 0\n\n"
+                                        "[GEOMETRY]\n1 ignored default\n\n[FIELDS]\n1 OPERA2D t.tab 0.5 2 0.01\n")
+    cs = ConfigScene(tmp_path / "config.in")
+    sc = table_scene(r2, z2, br=c2["BR"], bphi=c2["BPHI"], bz=c2["BZ"], v=c2["V"], er=c2["ER"], ephi=c2["EPHI"],
+                     ez=c2["EZ"], b_scale=0.5, e_scale=2.0)
+    rng = np.random.default_rng(8)
+    q = np.column_stack([rng.uniform(-0.35, 0.35, (300, 2)), rng.uniform(-0.25, 0.45, 300), np.zeros(300)])
+    a, b = oracle_mod.Oracle(cs).field(q), oracle_mod.Oracle(sc).field(q)
+    for u, v in zip(a, b):
+        np.testing.assert_array_equal(u, v)
+    assert np.all(a[2] == 0) and np.abs(a[3]).max() > 0
