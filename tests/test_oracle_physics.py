@@ -257,3 +257,44 @@ def test_interpolated_precession_axis_oracle(oracle_mod):
     assert np.max(np.abs(interp.spin[:3] - exact.spin[:3])) < 1e-6
     w = abs(scenes.GAMMA_N) * 1e-6
     np.testing.assert_allclose(interp.spin[4], w * (interp.t - parts.t), rtol=1e-6)
+
+
+def test_geometry_test_ignored_solids_oracle(oracle_mod):
+    """test/GeometryTest/config.in: UCN stored in the steel hollow unit cube,
+    which two unit cubes (centred on (0,0,0) and (1,0,0)) overlap, each listed
+    twice -- as the default material ignored from 5 s to 10 s and as detector
+    material ignored from 0 s to 5 s -- so the same surfaces change role at
+    5 s, while UCN are inside them.  The reference's criterion: no geometry
+    or integration errors; here also: absorption inside the box happens only
+    in the cubes and only after 5 s."""
+    from pentrack_gb300 import Scene, scenes as S, workloads
+    from pentrack_gb300.engine import run_params
+    sc = Scene()
+    sc.add_material("default", 0.0)
+    sc.add_material("Steel", 183.0, 0.1, 0.03)
+    sc.add_material("UCNdet", 0.0, 0.1)
+    c0 = S.box_mesh((-0.5, -0.5, -0.5), (0.5, 0.5, 0.5))
+    c1 = S.box_mesh((0.5, -0.5, -0.5), (1.5, 0.5, 0.5))
+    sc.add_solid(1, "default")
+    sc.add_solid(2, "default", c0, ignore=[(5.0, 10.0)])
+    sc.add_solid(3, "default", c1, ignore=[(5.0, 10.0)])
+    sc.add_solid(4, "Steel", workloads.hollow_cube_mesh())
+    sc.add_solid(5, "UCNdet", c0, ignore=[(0.0, 5.0)])
+    sc.add_solid(6, "UCNdet", c1, ignore=[(0.0, 5.0)])
+    n = 2000
+    ids = np.arange(n, dtype=np.int64)
+    pos, (E, ph, th, pol) = S.source_box(5, ids, (0, 0, 0), (1, 1, 1), 0.0, 300e-9, polarization=0.0)
+    parts = S.make_particles(5, ids, pos, E, ph, th, pol)
+    params = run_params(A.NEUTRON, simtime=10.0, tau=0.0, tmax=9e99, lmax=9e99, bmax=0.1, spintimes=(0, 0), seed=5)
+    out, st = oracle_mod.Oracle(sc).integrate(params, parts, nthreads=8)
+    bad = (A.ID_GEOMETRY_ERROR, A.ID_CGAL_ERROR, A.ID_ODEINT_ERROR, A.ID_INITIAL_NOT_FOUND)
+    assert not np.isin(out.stop_id, bad).any(), np.unique(out.stop_id, return_counts=True)
+    # absorption in material inside the box: in the detector cubes, which are
+    # ignored until 5 s (the default-material copies of the same cubes, which
+    # do not absorb, are the active ones until then), so only after 5 s
+    absorbed = out.stop_id == A.ID_ABSORBED_IN_MATERIAL
+    p = out.y[0:3]
+    interior = np.all((p > 0) & (p < 1), axis=0)
+    in_cubes = ((np.abs(p[0]) < 0.5) | (np.abs(p[0] - 1) < 0.5)) & (np.abs(p[1]) < 0.5) & (np.abs(p[2]) < 0.5)
+    det = absorbed & interior
+    assert det.sum() > 100 and np.all(in_cubes[det]) and np.all(out.t[det] >= 5.0)
